@@ -1,0 +1,747 @@
+// FP64 oracle: entropic-regularised OT (EROT) problem pieces and the
+// sinkhorn_bcd / sinkhorn_newton / sinkhorn_ssns solvers.
+// Test infrastructure only (see oracle.h). Each function cites the reference
+// file:line whose math and control flow it restates.
+#include "oracle_util.h"
+
+namespace oracle {
+namespace erot {
+
+struct Problem {
+    int n, m;
+    const double* M;  // column-major n x m
+    const double* a;
+    const double* b;
+    double reg;
+    Vec loga, logb;
+    // sinkhorn_problem.h:36-44
+    Problem(const double* M_, int n_, int m_, const double* a_, const double* b_, double reg_)
+        : n(n_), m(m_), M(M_), a(a_), b(b_), reg(reg_), loga(n_), logb(m_) {
+        for (int i = 0; i < n; i++) loga[i] = std::log(a[i]);
+        for (int j = 0; j < m; j++) logb[j] = std::log(b[j]);
+    }
+    double Mij(int i, int j) const { return M[(size_t)j * n + i]; }
+};
+
+// optimal_beta: sinkhorn_problem_bcd.cpp:149-174 with log_sum_exp_colwise
+// (111-146): D = (alpha - M)/reg, beta_j = reg (log b_j - LSE_i D_ij),
+// LSE with the column max as shift.
+static void optimal_beta(const Problem& p, const double* alpha, double* beta) {
+    const int n = p.n;
+    Vec D(n);
+    for (int j = 0; j < p.m; j++) {
+        const double* Mj = p.M + (size_t)j * n;
+        double c = -std::numeric_limits<double>::infinity();
+        for (int i = 0; i < n; i++) {
+            D[i] = (alpha[i] - Mj[i]) / p.reg;
+            c = std::max(c, D[i]);
+        }
+        double s = 0.0;
+        for (int i = 0; i < n; i++) s += std::exp(D[i] - c);
+        const double lse = c + std::log(s);
+        beta[j] = p.reg * (p.logb[j] - lse);
+    }
+}
+
+// optimal_alpha: sinkhorn_problem_bcd.cpp:177-201 with log_sum_exp_rowwise
+// (82-108): row max first, then exp sums accumulated column by column.
+static void optimal_alpha(const Problem& p, const double* beta, double* alpha) {
+    const int n = p.n, m = p.m;
+    Vec c(n, -std::numeric_limits<double>::infinity()), res(n, 0.0);
+    for (int j = 0; j < m; j++) {
+        const double* Mj = p.M + (size_t)j * n;
+        for (int i = 0; i < n; i++) c[i] = std::max(c[i], (beta[j] - Mj[i]) / p.reg);
+    }
+    for (int j = 0; j < m; j++) {
+        const double* Mj = p.M + (size_t)j * n;
+        for (int i = 0; i < n; i++) res[i] += std::exp((beta[j] - Mj[i]) / p.reg - c[i]);
+    }
+    for (int i = 0; i < n; i++) alpha[i] = p.reg * (p.loga[i] - (c[i] + std::log(res[i])));
+}
+
+// compute_T: sinkhorn_problem_obj.cpp:139-188 (with compute_column_helper
+// 16-136): T_ij = exp((alpha_i + beta_j - M_ij)/reg), last column with
+// beta_m = 0 ("NoBeta"); returns sum(T).
+static double compute_T(const Problem& p, const double* gamma, double* T) {
+    const int n = p.n, m = p.m;
+    const double* alpha = gamma;
+    const double* beta = gamma + n;
+    double Tsum = 0.0;
+    for (int j = 0; j < m; j++) {
+        const double* Mj = p.M + (size_t)j * n;
+        double* Tj = T + (size_t)j * n;
+        double colsum = 0.0;
+        if (j < m - 1) {
+            const double bj = beta[j];
+            for (int i = 0; i < n; i++) {
+                const double t = std::exp((alpha[i] + bj - Mj[i]) / p.reg);
+                colsum += t;
+                Tj[i] = t;
+            }
+        } else {
+            for (int i = 0; i < n; i++) {
+                const double t = std::exp((alpha[i] - Mj[i]) / p.reg);
+                colsum += t;
+                Tj[i] = t;
+            }
+        }
+        Tsum += colsum;
+    }
+    return Tsum;
+}
+
+// compute_sums: sinkhorn_problem_obj.cpp:192-297. Row sums in sums[0:n],
+// column sums of the first m-1 columns in sums[n:n+m-1].
+static void compute_sums(const Problem& p, const double* T, double* sums) {
+    const int n = p.n, m = p.m;
+    double* rs = sums;
+    double* cs = sums + n;
+    std::fill(rs, rs + n, 0.0);
+    for (int j = 0; j < m; j++) {
+        const double* Tj = T + (size_t)j * n;
+        double c = 0.0;
+        for (int i = 0; i < n; i++) {
+            c += Tj[i];
+            rs[i] += Tj[i];
+        }
+        if (j < m - 1) cs[j] = c;
+    }
+}
+
+// dual_obj: sinkhorn_problem_obj.cpp:324-342.
+static double dual_obj(const Problem& p, const double* gamma, double* T) {
+    const double Tsum = compute_T(p, gamma, T);
+    return p.reg * Tsum - dot(gamma, p.a, p.n) - dot(gamma + p.n, p.b, p.m - 1);
+}
+
+// dual_obj_grad: sinkhorn_problem_obj.cpp:371-393 (computeT selects whether
+// T is recomputed or reused).
+static double dual_obj_grad(const Problem& p, const double* gamma, double* grad, double* T,
+                            bool computeT) {
+    const int n = p.n, m = p.m;
+    if (computeT) compute_T(p, gamma, T);
+    compute_sums(p, T, grad);
+    const double Tsum = sum(grad, n);
+    for (int i = 0; i < n; i++) grad[i] -= p.a[i];
+    for (int j = 0; j < m - 1; j++) grad[n + j] -= p.b[j];
+    return p.reg * Tsum - dot(gamma, p.a, n) - dot(gamma + n, p.b, m - 1);
+}
+
+// Gauge fix of sinkhorn_bcd.cpp:50-51: gamma = (alpha + beta_m, beta~ - beta_m).
+static void gauge(int n, int m, const double* alpha, const double* beta, double* gamma) {
+    for (int i = 0; i < n; i++) gamma[i] = alpha[i] + beta[m - 1];
+    for (int j = 0; j < m - 1; j++) gamma[n + j] = beta[j] - beta[m - 1];
+}
+
+// Recovered plan, sinkhorn_result.h:32-50, written row-major.
+static void get_plan(const Problem& p, const double* gamma, double* plan) {
+    const int n = p.n, m = p.m;
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < m; j++) {
+            const double bj = (j < m - 1) ? gamma[n + j] : 0.0;
+            plan[(size_t)i * m + j] = std::exp((gamma[i] + bj - p.Mij(i, j)) / p.reg);
+        }
+}
+
+// ---------------- sparsify_mat3 (sinkhorn_sparsify3.cpp) ----------------
+// The non-AVX2 build of the reference (what runs on Arm hosts) selects with
+// std::nth_element and sorts with std::sort; the same calls are used here.
+
+// select_and_find: sinkhorn_sparsify3.cpp:35-64.
+static int select_and_find(double* x, int n, int k, double target, double& block_sum) {
+    std::nth_element(x, x + k, x + n);
+    block_sum = 0.0;
+    for (int i = 0; i < k; i++) block_sum += x[i];
+    if (block_sum <= target) return k;
+    std::sort(x, x + k);
+    double s = 0.0;
+    for (int i = 0; i < k; i++) {
+        s += x[i];
+        if (s > target) return i;
+    }
+    return k - 1;
+}
+
+// select_and_find_reverse: sinkhorn_sparsify3.cpp:73-102.
+static int select_and_find_reverse(double* x, int n, int k, double target, double& block_sum) {
+    std::nth_element(x, x + k, x + n);
+    block_sum = 0.0;
+    for (int i = k; i < n; i++) block_sum += x[i];
+    if (block_sum < target) return k - 1;
+    std::sort(x + k, x + n);
+    double s = 0.0;
+    for (int i = n - 1; i >= k; i--) {
+        s += x[i];
+        if (s >= target) return i;
+    }
+    return k;
+}
+
+static int block_size(int n) {
+    int b = n / 32;
+    b = std::max(b, 32);
+    return std::min(b, n);
+}
+
+// find_small: sinkhorn_sparsify3.cpp:112-148 (blocks of max(n/32, 32)
+// smallest elements, scanned from the left).
+static int find_small(double* x, int n, double delta) {
+    const int blk = block_size(n);
+    int found = n;
+    double target = delta;
+    for (int w = 0; w < n; w += blk) {
+        const int len = n - w;
+        const int bs = std::min(len, blk);
+        double block_sum;
+        const int L = select_and_find(x + w, len, bs, target, block_sum);
+        if (L < bs) {
+            found = w + L;
+            break;
+        }
+        target -= block_sum;
+    }
+    return found;
+}
+
+// find_large: sinkhorn_sparsify3.cpp:160-196 (blocks of the largest
+// elements, scanned from the right; target = sum - delta).
+static int find_large(double* x, int n, double target) {
+    const int blk = block_size(n);
+    int found = 0;
+    for (int w = n; w >= 0; w -= (blk > 0 ? blk : 1)) {
+        const int len = w;
+        const int bs = std::min(len, blk);
+        const int k = len - bs;
+        double block_sum;
+        const int L = select_and_find_reverse(x, len, k, target, block_sum);
+        if (L >= k) {
+            found = L;
+            break;
+        }
+        target -= block_sum;
+        if (blk == 0) break;
+    }
+    return found;
+}
+
+struct CSC {
+    int n = 0, ncol = 0;
+    std::vector<int> outer;   // ncol + 1
+    std::vector<int> inner;
+    std::vector<double> val;
+    long nnz() const { return (long)val.size(); }
+};
+
+// sparsify_mat3: sinkhorn_sparsify3.cpp:276-405.
+static CSC sparsify_mat3(const double* T, int n, int m, double delta, double density_hint) {
+    const double Inf = std::numeric_limits<double>::infinity();
+    std::vector<double> Delta(T, T + (size_t)n * m);
+    std::fill(Delta.begin() + (size_t)(m - 1) * n, Delta.end(), 0.0);
+    // Column stage (lines 295-319).
+    for (int j = 0; j < m - 1; j++) {
+        const double* Tj = T + (size_t)j * n;
+        double* data = Delta.data() + (size_t)j * n;
+        int L;
+        if (density_hint > 0.2) {
+            L = find_small(data, n, delta);
+        } else {
+            const double s = sum(Tj, n);
+            L = find_large(data, n, s - delta);
+        }
+        const double thresh = (L >= n) ? Inf : data[L];
+        for (int i = 0; i < n; i++) data[i] = (Tj[i] >= thresh) ? 0.0 : Tj[i];
+    }
+    // Row stage (lines 333-353).
+    std::vector<double> row(m);
+    for (int i = 0; i < n; i++) {
+        for (int j = 0; j < m; j++) row[j] = Delta[(size_t)j * n + i];
+        const double rowsum = sum(row.data(), m);
+        if (rowsum > 2.0 * delta) {
+            const double target = rowsum - 2.0 * delta;
+            const int L = find_large(row.data(), m - 1, target);
+            const double thresh = (L >= m - 1) ? Inf : row[L];
+            for (int j = 0; j < m - 1; j++) {
+                double& d = Delta[(size_t)j * n + i];
+                d = (d >= thresh) ? 0.0 : d;
+            }
+        }
+    }
+    // Kept entries are those with Delta == 0 (line 378), exact zeros of T
+    // included.
+    CSC sp;
+    sp.n = n;
+    sp.ncol = m - 1;
+    sp.outer.assign(m, 0);
+    for (int j = 0; j < m - 1; j++) {
+        const double* Tj = T + (size_t)j * n;
+        const double* Dj = Delta.data() + (size_t)j * n;
+        for (int i = 0; i < n; i++) {
+            if (Dj[i] == 0.0) {
+                sp.val.push_back(Tj[i]);
+                sp.inner.push_back(i);
+            }
+        }
+        sp.outer[j + 1] = (int)sp.val.size();
+    }
+    return sp;
+}
+
+// Sparsified Hessian: sinkhorn_hess.h:46-158, sinkhorn_hess.cpp:15-164.
+struct Hessian {
+    int n = 0, m = 0;
+    Vec h1, h2;
+    CSC sigmad;  // values already divided by reg
+    double density() const {
+        const long nnz = 2 * sigmad.nnz() + n + m - 1;
+        const double d = (double)(n + m - 1);
+        return (double)nnz / d / d;
+    }
+    // res = sigmad * x, x [m-1], res [n]
+    void apply_sigmadx(const double* x, double* res) const {
+        std::fill(res, res + n, 0.0);
+        for (int j = 0; j < m - 1; j++)
+            for (int k = sigmad.outer[j]; k < sigmad.outer[j + 1]; k++)
+                res[sigmad.inner[k]] += sigmad.val[k] * x[j];
+    }
+    // res = sigmad' * x, x [n], res [m-1]
+    void apply_sigmadtx(const double* x, double* res) const {
+        for (int j = 0; j < m - 1; j++) {
+            double s = 0.0;
+            for (int k = sigmad.outer[j]; k < sigmad.outer[j + 1]; k++)
+                s += sigmad.val[k] * x[sigmad.inner[k]];
+            res[j] = s;
+        }
+    }
+    // apply_Deltax: sinkhorn_hess.cpp:136-148.
+    void apply_Deltax(const Vec& x, double shift, Vec& res) const {
+        Vec sx(n), t(n), stx(m - 1);
+        apply_sigmadx(x.data(), sx.data());
+        for (int i = 0; i < n; i++) t[i] = sx[i] / (h1[i] + shift);
+        apply_sigmadtx(t.data(), stx.data());
+        res.resize(m - 1);
+        for (int j = 0; j < m - 1; j++) res[j] = h2[j] * x[j] + shift * x[j] - stx[j];
+    }
+    // apply_Hsx: sinkhorn_hess.cpp:151-164.
+    void apply_Hsx(const Vec& x, Vec& res) const {
+        res.resize(n + m - 1);
+        apply_sigmadx(x.data() + n, res.data());
+        apply_sigmadtx(x.data(), res.data() + n);
+        for (int i = 0; i < n; i++) res[i] += h1[i] * x[i];
+        for (int j = 0; j < m - 1; j++) res[n + j] += h2[j] * x[n + j];
+    }
+};
+
+// dual_sparsified_hess: sinkhorn_problem_obj.cpp:432-443 + compute_hess
+// sinkhorn_hess.cpp:15-33.
+static void sparsified_hess(const Problem& p, const double* T, const Vec& grad, double delta,
+                            double density_hint, Hessian& H) {
+    const int n = p.n, m = p.m;
+    H.n = n;
+    H.m = m;
+    H.h1.resize(n);
+    H.h2.resize(m - 1);
+    for (int i = 0; i < n; i++) H.h1[i] = (grad[i] + p.a[i]) / p.reg;
+    for (int j = 0; j < m - 1; j++) H.h2[j] = (grad[n + j] + p.b[j]) / p.reg;
+    H.sigmad = sparsify_mat3(T, n, m, delta, density_hint);
+    for (auto& v : H.sigmad.val) v /= p.reg;
+}
+
+// hess_cg: sinkhorn_cg.cpp:9-50 (Schur complement on the beta block).
+static int hess_cg(const Hessian& H, const Vec& rhs, double shift, const Vec* guess, double tol,
+                   Vec& res) {
+    const int n = H.n, m = H.m;
+    res.assign(n + m - 1, 0.0);
+    Vec v(n), y(m - 1), zy(m - 1);
+    for (int i = 0; i < n; i++) v[i] = rhs[i] / (H.h1[i] + shift);
+    H.apply_sigmadtx(v.data(), y.data());
+    for (int j = 0; j < m - 1; j++) zy[j] = rhs[n + j] - y[j];
+    Vec r2;
+    const int it = cg_solve([&](const Vec& x, Vec& out) { H.apply_Deltax(x, shift, out); }, zy, r2,
+                            tol, guess);
+    std::copy(r2.begin(), r2.end(), res.begin() + n);
+    Vec bx(n);
+    H.apply_sigmadx(r2.data(), bx.data());
+    for (int i = 0; i < n; i++) res[i] = (rhs[i] - bx[i]) / (H.h1[i] + shift);
+    return it;
+}
+
+// Direct solve of (Hs + shift I) x = rhs. The reference factors the sparse
+// matrix with SimplicialLDLT/LLT/SparseLU (sinkhorn_linsolve.cpp:58-106);
+// the oracle solves the same SPD system exactly through a dense Cholesky of
+// its Schur complement on the beta block.
+static bool hess_direct(const Hessian& H, const Vec& rhs, double shift, Vec& res) {
+    const int n = H.n, m1 = H.m - 1;
+    // CSR view of sigmad.
+    std::vector<std::vector<std::pair<int, double>>> rows(n);
+    for (int j = 0; j < m1; j++)
+        for (int k = H.sigmad.outer[j]; k < H.sigmad.outer[j + 1]; k++)
+            rows[H.sigmad.inner[k]].push_back({j, H.sigmad.val[k]});
+    std::vector<double> S((size_t)m1 * m1, 0.0);
+    for (int j = 0; j < m1; j++) S[(size_t)j * m1 + j] = H.h2[j] + shift;
+    for (int i = 0; i < n; i++) {
+        const double w = 1.0 / (H.h1[i] + shift);
+        const auto& r = rows[i];
+        for (size_t p = 0; p < r.size(); p++)
+            for (size_t q = 0; q <= p; q++) {
+                const int j = r[p].first, k = r[q].first;
+                const double v = r[p].second * r[q].second * w;
+                S[(size_t)std::max(j, k) * m1 + std::min(j, k)] -= v;
+            }
+    }
+    if (!cholesky(S, m1)) return false;
+    Vec t(n), y(m1);
+    for (int i = 0; i < n; i++) t[i] = rhs[i] / (H.h1[i] + shift);
+    H.apply_sigmadtx(t.data(), y.data());
+    Vec r2(m1);
+    for (int j = 0; j < m1; j++) r2[j] = rhs[n + j] - y[j];
+    cholesky_solve(S, m1, r2);
+    res.assign(n + m1, 0.0);
+    Vec bx(n);
+    H.apply_sigmadx(r2.data(), bx.data());
+    for (int i = 0; i < n; i++) res[i] = (rhs[i] - bx[i]) / (H.h1[i] + shift);
+    for (int j = 0; j < m1; j++) res[n + j] = r2[j];
+    return true;
+}
+
+// Newton direction -H^{-1} g for the dense dual Hessian
+// H = [diag(r) T~; T~' diag(c~)]/reg (sinkhorn_problem_obj.cpp:396-418),
+// solved exactly (the reference uses Eigen::LLT on H, sinkhorn_newton.cpp:91)
+// via a dense Cholesky of the Schur complement
+// diag(c~) - T~' diag(1/r) T~ (all divided by reg).
+static bool newton_direction(const Problem& p, const double* T, const Vec& g, Vec& direc) {
+    const int n = p.n, m1 = p.m - 1;
+    Vec r(n), c(m1);
+    for (int i = 0; i < n; i++) r[i] = g[i] + p.a[i];
+    for (int j = 0; j < m1; j++) c[j] = g[n + j] + p.b[j];
+    const double reg = p.reg;
+    // Columns of T~/reg scaled by sqrt(reg/r_i), so S = diag(c~)/reg - U'U.
+    std::vector<double> U((size_t)m1 * n);
+    for (int j = 0; j < m1; j++)
+        for (int i = 0; i < n; i++)
+            U[(size_t)j * n + i] = (T[(size_t)j * n + i] / reg) * std::sqrt(reg / r[i]);
+    std::vector<double> S((size_t)m1 * m1, 0.0);
+    for (int j = 0; j < m1; j++) {
+        const double* Uj = U.data() + (size_t)j * n;
+        for (int k = 0; k <= j; k++) {
+            const double* Uk = U.data() + (size_t)k * n;
+            double s = 0.0;
+            for (int i = 0; i < n; i++) s += Uj[i] * Uk[i];
+            S[(size_t)j * m1 + k] = (j == k ? c[j] / reg : 0.0) - s;
+        }
+    }
+    if (!cholesky(S, m1)) return false;
+    // rhs = -g; x_b = S^{-1}(-g_b + B' A^{-1} g_a); x_a = A^{-1}(-g_a - B x_b)
+    Vec xb(m1);
+    for (int j = 0; j < m1; j++) {
+        const double* Tj = T + (size_t)j * n;
+        double s = 0.0;
+        for (int i = 0; i < n; i++) s += (Tj[i] / reg) * (g[i] / (r[i] / reg));
+        xb[j] = -g[n + j] + s;
+    }
+    cholesky_solve(S, m1, xb);
+    direc.assign(n + m1, 0.0);
+    for (int i = 0; i < n; i++) {
+        double s = 0.0;
+        for (int j = 0; j < m1; j++) s += (T[(size_t)j * n + i] / reg) * xb[j];
+        direc[i] = (-g[i] - s) / (r[i] / reg);
+    }
+    for (int j = 0; j < m1; j++) direc[n + j] = xb[j];
+    return true;
+}
+
+// line_selection: sinkhorn_problem_ls.cpp:13-41. T is left holding the last
+// candidate evaluated.
+static double line_selection(const Problem& p, const std::vector<double>& candid, const Vec& gamma,
+                             const Vec& direc, double curobj, double* T, double& objval) {
+    double best = 1.0;
+    objval = std::numeric_limits<double>::infinity();
+    Vec ng(gamma.size());
+    for (double alpha : candid) {
+        for (size_t k = 0; k < gamma.size(); k++) ng[k] = gamma[k] + alpha * direc[k];
+        const double f = dual_obj(p, ng.data(), T);
+        if (f < objval) {
+            best = alpha;
+            objval = f;
+        }
+        if (objval < curobj) return best;
+    }
+    return best;
+}
+
+static void init_gamma(const Problem& p, const oracle_opts* opts, Vec& gamma) {
+    const int n = p.n, m = p.m;
+    gamma.assign(n + m - 1, 0.0);
+    if (opts && opts->x0 && opts->x0_len == n + m - 1) {
+        std::copy(opts->x0, opts->x0 + n + m - 1, gamma.begin());
+        return;
+    }
+    Vec alpha(n, 0.0), beta(m);
+    optimal_beta(p, alpha.data(), beta.data());
+    gauge(n, m, alpha.data(), beta.data(), gamma.data());
+}
+
+static void finish(const Problem& p, int niter, const Vec& gamma, History& h, oracle_result* r) {
+    r->niter = niter;
+    r->hist_len = h.len;
+    std::copy(gamma.begin(), gamma.end(), r->dual);
+    if (r->plan) get_plan(p, gamma.data(), r->plan);
+}
+
+}  // namespace erot
+}  // namespace oracle
+
+using namespace oracle;
+using namespace oracle::erot;
+
+extern "C" {
+
+void oracle_erot_optimal_beta(const double* M, int n, int m, const double* b, double reg,
+                              const double* alpha, double* beta) {
+    std::vector<double> ones(n, 1.0);
+    Problem p(M, n, m, ones.data(), b, reg);
+    optimal_beta(p, alpha, beta);
+}
+
+void oracle_erot_optimal_alpha(const double* M, int n, int m, const double* a, double reg,
+                               const double* beta, double* alpha) {
+    std::vector<double> ones(m, 1.0);
+    Problem p(M, n, m, a, ones.data(), reg);
+    optimal_alpha(p, beta, alpha);
+}
+
+double oracle_erot_dual_obj(const double* M, int n, int m, const double* a, const double* b,
+                            double reg, const double* gamma) {
+    Problem p(M, n, m, a, b, reg);
+    std::vector<double> T((size_t)n * m);
+    return dual_obj(p, gamma, T.data());
+}
+
+double oracle_erot_dual_obj_grad(const double* M, int n, int m, const double* a, const double* b,
+                                 double reg, const double* gamma, double* grad) {
+    Problem p(M, n, m, a, b, reg);
+    std::vector<double> T((size_t)n * m);
+    return dual_obj_grad(p, gamma, grad, T.data(), true);
+}
+
+void oracle_erot_hvp(const double* M, int n, int m, const double* a, const double* b, double reg,
+                     const double* gamma, const double* x, double* y) {
+    Problem p(M, n, m, a, b, reg);
+    std::vector<double> T((size_t)n * m);
+    Vec g(n + m - 1);
+    dual_obj_grad(p, gamma, g.data(), T.data(), true);
+    for (int i = 0; i < n; i++) y[i] = (g[i] + a[i]) * x[i];
+    for (int j = 0; j < m - 1; j++) y[n + j] = (g[n + j] + b[j]) * x[n + j];
+    for (int j = 0; j < m - 1; j++) {
+        const double* Tj = T.data() + (size_t)j * n;
+        double s = 0.0;
+        for (int i = 0; i < n; i++) {
+            y[i] += Tj[i] * x[n + j];
+            s += Tj[i] * x[i];
+        }
+        y[n + j] += s;
+    }
+    for (int k = 0; k < n + m - 1; k++) y[k] /= reg;
+}
+
+int oracle_erot_newton_direction(const double* M, int n, int m, const double* a, const double* b,
+                                 double reg, const double* gamma, double* direc) {
+    Problem p(M, n, m, a, b, reg);
+    std::vector<double> T((size_t)n * m);
+    Vec g(n + m - 1), d;
+    dual_obj_grad(p, gamma, g.data(), T.data(), true);
+    if (!newton_direction(p, T.data(), g, d)) return 1;
+    std::copy(d.begin(), d.end(), direc);
+    return 0;
+}
+
+double oracle_erot_compute_T(const double* M, int n, int m, double reg, const double* gamma,
+                             double* T) {
+    std::vector<double> ones(std::max(n, m), 1.0);
+    Problem p(M, n, m, ones.data(), ones.data(), reg);
+    return compute_T(p, gamma, T);
+}
+
+long oracle_sparsify_mat3(const double* T, int n, int m, double delta, double density_hint,
+                          int* outer, int* inner, double* values, long cap) {
+    CSC sp = sparsify_mat3(T, n, m, delta, density_hint);
+    if (sp.nnz() > cap) return -1;
+    std::copy(sp.outer.begin(), sp.outer.end(), outer);
+    std::copy(sp.inner.begin(), sp.inner.end(), inner);
+    std::copy(sp.val.begin(), sp.val.end(), values);
+    return sp.nnz();
+}
+
+void oracle_erot_plan(const double* M, int n, int m, double reg, const double* gamma,
+                      double* plan) {
+    std::vector<double> ones(std::max(n, m), 1.0);
+    Problem p(M, n, m, ones.data(), ones.data(), reg);
+    get_plan(p, gamma, plan);
+}
+
+// sinkhorn_bcd_internal: sinkhorn_bcd.cpp:14-124.
+int oracle_sinkhorn_bcd(const double* M, int n, int m, const double* a, const double* b,
+                        double reg, double tol, int max_iter, int verbose,
+                        const oracle_opts* opts, oracle_result* res) {
+    try {
+        Problem p(M, n, m, a, b, reg);
+        Vec alpha(n), beta(m), gamma(n + m - 1), grad(n + m - 1);
+        std::vector<double> T((size_t)n * m);
+        History h(res);
+        if (opts && opts->x0 && opts->x0_len == n + m - 1) {
+            std::copy(opts->x0, opts->x0 + n, alpha.begin());
+            std::copy(opts->x0 + n, opts->x0 + n + m - 1, beta.begin());
+            beta[m - 1] = 0.0;
+        } else {
+            std::fill(alpha.begin(), alpha.end(), 0.0);
+            optimal_beta(p, alpha.data(), beta.data());
+        }
+        Timer timer;
+        timer.tic();
+        gauge(n, m, alpha.data(), beta.data(), gamma.data());
+        double f = dual_obj_grad(p, gamma.data(), grad.data(), T.data(), true);
+        double gnorm = norm(grad);
+        h.push(f, gnorm, timer.toc());
+        int i;
+        for (i = 0; i < max_iter; i++) {
+            if (verbose >= 1)
+                std::printf("iter = %d, objval = %g, ||grad|| = %g\n", i, f, gnorm);
+            timer.tic();
+            if (gnorm < tol) break;
+            optimal_alpha(p, beta.data(), alpha.data());
+            optimal_beta(p, alpha.data(), beta.data());
+            gauge(n, m, alpha.data(), beta.data(), gamma.data());
+            f = dual_obj_grad(p, gamma.data(), grad.data(), T.data(), true);
+            gnorm = norm(grad);
+            const double d = timer.toc();
+            h.push(f, gnorm, h.last_time() + d);
+        }
+        finish(p, i, gamma, h, res);
+        return 0;
+    } catch (const std::exception& e) {
+        set_err(res, e.what());
+        return 1;
+    }
+}
+
+// sinkhorn_newton_internal: sinkhorn_newton.cpp:17-129.
+int oracle_sinkhorn_newton(const double* M, int n, int m, const double* a, const double* b,
+                           double reg, double tol, int max_iter, int verbose,
+                           const oracle_opts* opts, oracle_result* res) {
+    try {
+        constexpr double theta = 0.5, kappa = 0.5;
+        constexpr int nlinesearch = 20;
+        Problem p(M, n, m, a, b, reg);
+        Vec gamma, newgamma(n + m - 1), direc, g(n + m - 1);
+        std::vector<double> T((size_t)n * m), Tls((size_t)n * m);
+        History h(res);
+        init_gamma(p, opts, gamma);
+        Timer timer;
+        timer.tic();
+        double f = dual_obj_grad(p, gamma.data(), g.data(), T.data(), true);
+        double gnorm = norm(g);
+        h.push(f, gnorm, timer.toc());
+        int i;
+        for (i = 0; i < max_iter; i++) {
+            if (verbose >= 1)
+                std::printf("iter = %d, objval = %g, ||grad|| = %g\n", i, f, gnorm);
+            timer.tic();
+            if ((gnorm < tol) || (!std::isfinite(f))) break;
+            if (!newton_direction(p, T.data(), g, direc))
+                throw std::runtime_error("Newton Hessian is not positive definite");
+            double step = 1.0;
+            const double thresh = theta * dot(g, direc);
+            for (int k = 0; k < nlinesearch; k++) {
+                for (int q = 0; q < n + m - 1; q++) newgamma[q] = gamma[q] + step * direc[q];
+                const double newf = dual_obj(p, newgamma.data(), Tls.data());
+                if (newf <= f + step * thresh) break;
+                step *= kappa;
+            }
+            gamma.swap(newgamma);
+            f = dual_obj_grad(p, gamma.data(), g.data(), T.data(), true);
+            gnorm = norm(g);
+            const double d = timer.toc();
+            h.push(f, gnorm, h.last_time() + d);
+        }
+        finish(p, i, gamma, h, res);
+        return 0;
+    } catch (const std::exception& e) {
+        set_err(res, e.what());
+        return 1;
+    }
+}
+
+// sinkhorn_ssns_internal: sinkhorn_ssns.cpp:16-234.
+int oracle_sinkhorn_ssns(const double* M, int n, int m, const double* a, const double* b,
+                         double reg, double tol, int max_iter, int verbose,
+                         const oracle_opts* opts, oracle_result* res) {
+    try {
+        const int method = opts ? opts->method : 1;
+        const double mu0 = opts ? opts->mu0 : 1.0;
+        constexpr double rho_t1 = 0.25, rho_t2 = 0.75, mu_s1 = 4.0, mu_s2 = 0.5, kappa = 0.001,
+                         cg_tol = 1e-8, nu0 = 0.01;
+        double mu = mu0, rho = 1.0;
+        Problem p(M, n, m, a, b, reg);
+        Vec gamma, step(n + m - 1), Hstep, direc(n + m - 1, 0.0), g(n + m - 1);
+        std::vector<double> T((size_t)n * m);
+        History h(res);
+        init_gamma(p, opts, gamma);
+        Timer timer;
+        timer.tic();
+        double f = dual_obj_grad(p, gamma.data(), g.data(), T.data(), true);
+        double gnorm = norm(g);
+        double delta = nu0 * gnorm;
+        Hessian H;
+        sparsified_hess(p, T.data(), g, delta, 0.001, H);
+        h.push(f, gnorm, timer.toc(), H.density());
+        const std::vector<double> alphas{1.0, 0.5, 0.25, 0.1};
+        int i;
+        for (i = 0; i < max_iter; i++) {
+            if (verbose >= 1)
+                std::printf("iter = %d, objval = %g, ||grad|| = %g\n", i, f, gnorm);
+            timer.tic();
+            if (gnorm < tol) break;
+            const double shift = mu * gnorm;
+            // The warm start the reference sets here has length m while the
+            // CG solves a system of size m-1, so it is never used
+            // (sinkhorn_ssns.cpp:124 vs sinkhorn_cg.cpp:35).
+            Vec rhs(n + m - 1);
+            for (int q = 0; q < n + m - 1; q++) rhs[q] = -g[q];
+            if (method == 0) {
+                hess_cg(H, rhs, shift, nullptr, cg_tol, direc);
+            } else {
+                if (!hess_direct(H, rhs, shift, direc))
+                    throw std::runtime_error("sparse factorization failed");
+            }
+            double newf;
+            const double alpha = line_selection(p, alphas, gamma, direc, f, T.data(), newf);
+            for (int q = 0; q < n + m - 1; q++) step[q] = alpha * direc[q];
+            H.apply_Hsx(step, Hstep);
+            const double numer = f - newf;
+            const double denom = -dot(g, step) - 0.5 * dot(step, Hstep);
+            rho = numer / denom;
+            if (rho > 0.0)
+                for (int q = 0; q < n + m - 1; q++) gamma[q] += step[q];
+            if (rho < rho_t1) {
+                mu = mu_s1 * mu;
+            } else if (rho > rho_t2) {
+                mu = std::max(mu_s2 * mu, kappa);
+            }
+            if (rho > 0.0) {
+                f = dual_obj_grad(p, gamma.data(), g.data(), T.data(), false);
+                gnorm = norm(g);
+                delta = nu0 * gnorm;
+                const double dens = H.density();
+                sparsified_hess(p, T.data(), g, delta, dens, H);
+            }
+            const double d = timer.toc();
+            h.push(f, gnorm, h.last_time() + d, H.density());
+        }
+        finish(p, i, gamma, h, res);
+        return 0;
+    } catch (const std::exception& e) {
+        set_err(res, e.what());
+        return 1;
+    }
+}
+
+}  // extern "C"

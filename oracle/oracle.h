@@ -1,0 +1,143 @@
+/*
+ * FP64 CPU oracle for the RegOT dense dual-evaluation hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY. This library is the checker that the CUDA path
+ * is compared against (and the timed CPU baseline). Product code never
+ * links, loads or calls it.
+ *
+ * It restates, in plain C++17 without Eigen, the math and control flow of
+ * the reference solvers of yixuan/regot-python:
+ *   src/sinkhorn_problem_bcd.cpp, src/sinkhorn_problem_obj.cpp,
+ *   src/sinkhorn_result.h, src/sinkhorn_bcd.cpp, src/sinkhorn_newton.cpp,
+ *   src/sinkhorn_ssns.cpp, src/sinkhorn_problem_ls.cpp, src/sinkhorn_hess.cpp,
+ *   src/sinkhorn_sparsify3.cpp, src/sinkhorn_linsolve.cpp, src/sinkhorn_cg.cpp,
+ *   src/qrot_problem.cpp, src/approx_proj.h, src/qrot_result.h,
+ *   src/qrot_lbfgs_dual.cpp, src/qrot_assn.cpp, src/qrot_hess.cpp,
+ *   src/qrot_linsolve.cpp, src/qrot_cg.cpp, src/LBFGSpp/LBFGS.h,
+ *   src/LBFGSpp/LBFGSpp/BFGSMat.h, src/LBFGSpp/LBFGSpp/LineSearchNocedalWright.h,
+ *   src/LBFGSpp/LBFGSpp/Param.h, src/solvers.cpp (kwargs defaults).
+ *
+ * Parity status: UNPINNED. The reference ships no tests, fixtures or golden
+ * vectors, and it cannot be compiled here (its numerics need Eigen 5.0.1,
+ * which setup.py downloads at build time). The oracle is therefore checked
+ * against known-answer problems (separable costs with closed-form plans),
+ * KKT conditions, and independent numpy/scipy restatements in tests/.
+ *
+ * Storage: M is column-major n x m (column j contiguous), like the Eigen
+ * MatrixXd the reference computes on; loops run j-outer, i-inner as there.
+ * Plans are written row-major n x m (REGOT_USE_ROW_MAJOR_MATRIX, config.h:5).
+ */
+#ifndef REGOT_ORACLE_H
+#define REGOT_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Options; defaults of SinkhornSolverOpts (sinkhorn_solvers.h:35-37) and
+ * QROTSolverOpts (qrot_solvers.h:28-30). x0 == NULL means "not given". */
+typedef struct {
+    const double* x0;
+    int x0_len;
+    int method;
+    double mu0;
+    double shift;
+    double density;
+    double tau;
+} oracle_opts;
+
+/* Caller-owned result buffers. History arrays have capacity hist_cap.
+ * plan may be NULL (skipped). densities / prim_vals may be NULL. */
+typedef struct {
+    int niter;
+    int hist_len;
+    int hist_cap;
+    double* dual;
+    double* plan;
+    double* obj_vals;
+    double* mar_errs;
+    double* run_times;
+    double* densities;
+    double* prim_vals;
+    char err[256];
+} oracle_result;
+
+/* ---- EROT problem pieces (M column-major) ---- */
+void oracle_erot_optimal_beta(const double* M, int n, int m, const double* b,
+                              double reg, const double* alpha, double* beta);
+void oracle_erot_optimal_alpha(const double* M, int n, int m, const double* a,
+                               double reg, const double* beta, double* alpha);
+double oracle_erot_dual_obj(const double* M, int n, int m, const double* a,
+                            const double* b, double reg, const double* gamma);
+double oracle_erot_dual_obj_grad(const double* M, int n, int m, const double* a,
+                                 const double* b, double reg,
+                                 const double* gamma, double* grad);
+/* y = H x with H the exact dual Hessian (sinkhorn_problem_obj.cpp:396-418). */
+void oracle_erot_hvp(const double* M, int n, int m, const double* a,
+                     const double* b, double reg, const double* gamma,
+                     const double* x, double* y);
+/* Newton direction -H^{-1} g by a dense Cholesky of the Schur complement. */
+int oracle_erot_newton_direction(const double* M, int n, int m, const double* a,
+                                 const double* b, double reg,
+                                 const double* gamma, double* direc);
+/* T = exp((alpha (+) [beta~, 0] - M)/reg), written column-major. */
+double oracle_erot_compute_T(const double* M, int n, int m, double reg,
+                             const double* gamma, double* T);
+/* sparsify_mat3 (sinkhorn_sparsify3.cpp:276-405). T column-major n x m.
+ * Output CSC of the kept entries of the first m-1 columns:
+ * outer[m] (m entries: 0..m-1), inner[cap], values[cap]. Returns nnz,
+ * or -1 if cap is too small. */
+long oracle_sparsify_mat3(const double* T, int n, int m, double delta,
+                          double density_hint, int* outer, int* inner,
+                          double* values, long cap);
+void oracle_erot_plan(const double* M, int n, int m, double reg,
+                      const double* gamma, double* plan_rowmajor);
+
+/* ---- EROT solvers ---- */
+int oracle_sinkhorn_bcd(const double* M, int n, int m, const double* a,
+                        const double* b, double reg, double tol, int max_iter,
+                        int verbose, const oracle_opts* opts,
+                        oracle_result* res);
+int oracle_sinkhorn_newton(const double* M, int n, int m, const double* a,
+                           const double* b, double reg, double tol,
+                           int max_iter, int verbose, const oracle_opts* opts,
+                           oracle_result* res);
+int oracle_sinkhorn_ssns(const double* M, int n, int m, const double* a,
+                         const double* b, double reg, double tol, int max_iter,
+                         int verbose, const oracle_opts* opts,
+                         oracle_result* res);
+
+/* ---- QROT problem pieces ---- */
+double oracle_qrot_dual_obj(const double* M, int n, int m, const double* a,
+                            const double* b, double reg, double tau,
+                            const double* gamma);
+double oracle_qrot_dual_obj_grad(const double* M, int n, int m,
+                                 const double* a, const double* b, double reg,
+                                 double tau, const double* gamma, double* grad);
+void oracle_qrot_optimal_beta(const double* M, int n, int m, const double* b,
+                              double reg, const double* alpha, double* beta);
+double oracle_qrot_primal_val(const double* M, int n, int m, const double* a,
+                              const double* b, double reg,
+                              const double* gamma);
+/* Generalized-Jacobian solve (H + shift I)^{-1} rhs by Schur CG
+ * (qrot_cg.cpp:9-50); sigma = 1[alpha_i + beta_j - M_ij > 0]. */
+int oracle_qrot_hess_cg(const double* M, int n, int m, const double* gamma,
+                        const double* rhs, double shift, double tau,
+                        double cg_tol, double* res);
+void oracle_qrot_plan(const double* M, int n, int m, double reg,
+                      const double* gamma, double* plan_rowmajor);
+
+/* ---- QROT solvers ---- */
+int oracle_qrot_lbfgs_dual(const double* M, int n, int m, const double* a,
+                           const double* b, double reg, double tol,
+                           int max_iter, int verbose, const oracle_opts* opts,
+                           oracle_result* res);
+int oracle_qrot_assn(const double* M, int n, int m, const double* a,
+                     const double* b, double reg, double tol, int max_iter,
+                     int verbose, const oracle_opts* opts, oracle_result* res);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* REGOT_ORACLE_H */

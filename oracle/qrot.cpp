@@ -1,0 +1,717 @@
+// FP64 oracle: quadratically regularised OT (QROT) problem pieces and the
+// qrot_lbfgs_dual / qrot_assn solvers, including a restatement of the
+// L-BFGS driver, two-loop recursion and Nocedal-Wright line search of the
+// vendored LBFGS++ (MIT). Test infrastructure only (see oracle.h).
+#include "oracle_util.h"
+
+namespace oracle {
+namespace qrot {
+
+struct Problem {
+    int n, m;
+    const double* M;  // column-major
+    const double* a;
+    const double* b;
+    double reg, tau;
+    double Mij(int i, int j) const { return M[(size_t)j * n + i]; }
+};
+
+// compute_D_stats: qrot_problem.cpp:36-94. C = alpha_i + beta_j - M_ij,
+// D = C+ ; returns ||D||^2 and fills row/column sums of D when requested.
+static double D_stats(const Problem& p, const double* gamma, double* rs, double* cs) {
+    const int n = p.n, m = p.m;
+    const double* alpha = gamma;
+    const double* beta = gamma + n;
+    double sq = 0.0;
+    if (rs) std::fill(rs, rs + n, 0.0);
+    for (int j = 0; j < m; j++) {
+        const double* Mj = p.M + (size_t)j * n;
+        const double bj = beta[j];
+        double c = 0.0;
+        for (int i = 0; i < n; i++) {
+            const double C = alpha[i] + bj - Mj[i];
+            if (C > 0.0) {
+                sq += C * C;
+                if (rs) rs[i] += C;
+                c += C;
+            }
+        }
+        if (cs) cs[j] = c;
+    }
+    return sq;
+}
+
+static double tau_diff(const Problem& p, const double* gamma) {
+    return sum(gamma, p.n) - sum(gamma + p.n, p.m);
+}
+
+// dual_obj: qrot_problem.cpp:118-198.
+static double dual_obj(const Problem& p, const double* gamma) {
+    const double sq = D_stats(p, gamma, nullptr, nullptr);
+    double obj = 0.5 * sq - p.reg * (dot(gamma, p.a, p.n) + dot(gamma + p.n, p.b, p.m));
+    if (p.tau > 0.0) {
+        const double d = tau_diff(p, gamma);
+        obj += 0.5 * p.tau * d * d;
+    }
+    return obj;
+}
+
+// dual_obj_grad: qrot_problem.cpp:226-253; dual_grad 201-223.
+static double dual_obj_grad(const Problem& p, const double* gamma, double* grad) {
+    const int n = p.n, m = p.m;
+    const double sq = D_stats(p, gamma, grad, grad + n);
+    for (int i = 0; i < n; i++) grad[i] -= p.reg * p.a[i];
+    for (int j = 0; j < m; j++) grad[n + j] -= p.reg * p.b[j];
+    double obj = 0.5 * sq - p.reg * (dot(gamma, p.a, n) + dot(gamma + n, p.b, m));
+    if (p.tau > 0.0) {
+        const double d = tau_diff(p, gamma);
+        obj += 0.5 * p.tau * d * d;
+        for (int i = 0; i < n; i++) grad[i] += p.tau * d;
+        for (int j = 0; j < m; j++) grad[n + j] -= p.tau * d;
+    }
+    return obj;
+}
+
+// piecewise_linear_equation: qrot_problem.cpp:368-392. Solves
+// sum_i (x - y_i)+ = b for x from the sorted y.
+static double piecewise_linear_equation(std::vector<double>& y, double b) {
+    const int n = (int)y.size();
+    std::sort(y.begin(), y.end());
+    double cs = 0.0, f = 0.0;
+    for (int i = 0; i < n - 1; i++) {
+        cs += y[i];
+        const double fnext = (i + 1) * y[i + 1] - cs;
+        if (b >= f && b < fnext) return (b + cs) / (i + 1);
+        f = fnext;
+    }
+    cs += y[n - 1];
+    return (b + cs) / n;
+}
+
+// optimal_beta: qrot_problem.cpp:397-404.
+static void optimal_beta(const Problem& p, const double* alpha, double* beta) {
+    std::vector<double> y(p.n);
+    for (int j = 0; j < p.m; j++) {
+        const double* Mj = p.M + (size_t)j * p.n;
+        for (int i = 0; i < p.n; i++) y[i] = Mj[i] - alpha[i];
+        beta[j] = piecewise_linear_equation(y, p.reg * p.b[j]);
+    }
+}
+
+// primal_val: qrot_problem.cpp:10-24 with approx_proj (approx_proj.h:6-26).
+static double primal_val(const Problem& p, const double* gamma) {
+    const int n = p.n, m = p.m;
+    std::vector<double> P((size_t)n * m);  // column-major
+    for (int j = 0; j < m; j++)
+        for (int i = 0; i < n; i++) {
+            const double C = gamma[i] + gamma[n + j] - p.Mij(i, j);
+            P[(size_t)j * n + i] = std::max(C, 0.0) / p.reg;
+        }
+    Vec rs(n, 0.0), x(n), cs(m), y(m);
+    for (int j = 0; j < m; j++)
+        for (int i = 0; i < n; i++) rs[i] += P[(size_t)j * n + i];
+    for (int i = 0; i < n; i++) x[i] = std::min(p.a[i] / rs[i], 1.0);
+    for (int j = 0; j < m; j++)
+        for (int i = 0; i < n; i++) P[(size_t)j * n + i] *= x[i];
+    for (int j = 0; j < m; j++) {
+        double c = 0.0;
+        for (int i = 0; i < n; i++) c += P[(size_t)j * n + i];
+        cs[j] = c;
+    }
+    for (int j = 0; j < m; j++) y[j] = std::min(p.b[j] / cs[j], 1.0);
+    for (int j = 0; j < m; j++)
+        for (int i = 0; i < n; i++) P[(size_t)j * n + i] *= y[j];
+    Vec ea(n), eb(m);
+    std::fill(rs.begin(), rs.end(), 0.0);
+    for (int j = 0; j < m; j++) {
+        double c = 0.0;
+        for (int i = 0; i < n; i++) {
+            rs[i] += P[(size_t)j * n + i];
+            c += P[(size_t)j * n + i];
+        }
+        eb[j] = p.b[j] - c;
+    }
+    double l1 = 0.0;
+    for (int i = 0; i < n; i++) {
+        ea[i] = p.a[i] - rs[i];
+        l1 += std::abs(ea[i]);
+    }
+    double val = 0.0, sq = 0.0;
+    for (int j = 0; j < m; j++)
+        for (int i = 0; i < n; i++) {
+            const double v = P[(size_t)j * n + i] + ea[i] * eb[j] / l1;
+            val += v * p.Mij(i, j);
+            sq += v * v;
+        }
+    return val + 0.5 * p.reg * sq;
+}
+
+// Generalized Hessian: qrot_hess.h:37-176, qrot_hess.cpp:41-216.
+// sigma = 1[C > 0] kept as per-row and per-column index lists.
+struct Hessian {
+    int n = 0, m = 0;
+    Vec h1, h2;
+    std::vector<std::vector<int>> sigma, sigmat;
+    void apply_sigmax(const double* x, double* res) const {
+        for (int i = 0; i < n; i++) {
+            double s = 0.0;
+            for (int j : sigma[i]) s += x[j];
+            res[i] = s;
+        }
+    }
+    void apply_sigmatx(const double* x, double* res) const {
+        for (int j = 0; j < m; j++) {
+            double s = 0.0;
+            for (int i : sigmat[j]) s += x[i];
+            res[j] = s;
+        }
+    }
+    // solve_Ax: qrot_hess.cpp:127-142.
+    void solve_Ax(const double* x, double shift, double tau, double* res) const {
+        if (tau > 0.0) {
+            double c1 = 1.0 / tau, c2 = 0.0;
+            Vec xh(n);
+            for (int i = 0; i < n; i++) {
+                xh[i] = x[i] / (h1[i] + shift);
+                c1 += 1.0 / (h1[i] + shift);
+                c2 += xh[i];
+            }
+            for (int i = 0; i < n; i++) res[i] = xh[i] - (c2 / c1) / (h1[i] + shift);
+        } else {
+            for (int i = 0; i < n; i++) res[i] = x[i] / (h1[i] + shift);
+        }
+    }
+    void apply_Bx(const double* x, double tau, double* res) const {
+        apply_sigmax(x, res);
+        if (tau > 0.0) {
+            const double s = sum(x, m);
+            for (int i = 0; i < n; i++) res[i] -= tau * s;
+        }
+    }
+    void apply_Cx(const double* x, double tau, double* res) const {
+        apply_sigmatx(x, res);
+        if (tau > 0.0) {
+            const double s = sum(x, n);
+            for (int j = 0; j < m; j++) res[j] -= tau * s;
+        }
+    }
+    // apply_Deltax: qrot_hess.cpp:173-189.
+    void apply_Deltax(const Vec& x, double shift, double tau, Vec& res) const {
+        Vec bx(n), t(n), ct(m);
+        apply_Bx(x.data(), tau, bx.data());
+        solve_Ax(bx.data(), shift, tau, t.data());
+        apply_Cx(t.data(), tau, ct.data());
+        res.resize(m);
+        for (int j = 0; j < m; j++) res[j] = h2[j] * x[j] + shift * x[j] - ct[j];
+        if (tau > 0.0) {
+            const double s = sum(x.data(), m);
+            for (int j = 0; j < m; j++) res[j] += tau * s;
+        }
+    }
+};
+
+// compute_D_hess: qrot_hess.cpp:41-96 (also gives ||D||^2 and D sums).
+static double D_hess(const Problem& p, const double* gamma, double* rs, double* cs, Hessian& H) {
+    const int n = p.n, m = p.m;
+    H.n = n;
+    H.m = m;
+    H.h1.assign(n, 0.0);
+    H.h2.assign(m, 0.0);
+    H.sigma.assign(n, {});
+    H.sigmat.assign(m, {});
+    std::fill(rs, rs + n, 0.0);
+    double sq = 0.0;
+    for (int j = 0; j < m; j++) {
+        const double* Mj = p.M + (size_t)j * n;
+        const double bj = gamma[n + j];
+        double c = 0.0;
+        int h2j = 0;
+        for (int i = 0; i < n; i++) {
+            const double C = gamma[i] + bj - Mj[i];
+            if (C > 0.0) {
+                H.sigma[i].push_back(j);
+                H.sigmat[j].push_back(i);
+                sq += C * C;
+                rs[i] += C;
+                c += C;
+                H.h1[i] += 1;
+                h2j++;
+            }
+        }
+        cs[j] = c;
+        H.h2[j] = h2j;
+    }
+    return sq;
+}
+
+// dual_obj_grad_hess: qrot_problem.cpp:262-290.
+static double dual_obj_grad_hess(const Problem& p, const double* gamma, double* grad, Hessian& H) {
+    const int n = p.n, m = p.m;
+    const double sq = D_hess(p, gamma, grad, grad + n, H);
+    double obj = 0.5 * sq - p.reg * (dot(gamma, p.a, n) + dot(gamma + n, p.b, m));
+    for (int i = 0; i < n; i++) grad[i] -= p.reg * p.a[i];
+    for (int j = 0; j < m; j++) grad[n + j] -= p.reg * p.b[j];
+    if (p.tau > 0.0) {
+        const double d = tau_diff(p, gamma);
+        obj += 0.5 * p.tau * d * d;
+        for (int i = 0; i < n; i++) grad[i] += p.tau * d;
+        for (int j = 0; j < m; j++) grad[n + j] -= p.tau * d;
+    }
+    return obj;
+}
+
+// hess_cg: qrot_cg.cpp:9-50 (Schur complement on the beta block).
+static int hess_cg(const Hessian& H, const Vec& rhs, double shift, double tau, double tol,
+                   Vec& res) {
+    const int n = H.n, m = H.m;
+    res.assign(n + m, 0.0);
+    Vec v(n), y(m), zy(m);
+    H.solve_Ax(rhs.data(), shift, tau, v.data());
+    H.apply_Cx(v.data(), tau, y.data());
+    for (int j = 0; j < m; j++) zy[j] = rhs[n + j] - y[j];
+    Vec r2;
+    const int it = cg_solve([&](const Vec& x, Vec& out) { H.apply_Deltax(x, shift, tau, out); },
+                            zy, r2, tol, nullptr);
+    std::copy(r2.begin(), r2.end(), res.begin() + n);
+    Vec bx(n), t(n);
+    H.apply_Bx(r2.data(), tau, bx.data());
+    for (int i = 0; i < n; i++) t[i] = rhs[i] - bx[i];
+    H.solve_Ax(t.data(), shift, tau, res.data());
+    return it;
+}
+
+// Direct solve used for method != 0 (the reference factors the sparse
+// matrix, qrot_linsolve.cpp:72-105): dense Cholesky of the Schur
+// complement, exact for the same SPD system (tau = 0 only).
+static bool hess_direct(const Hessian& H, const Vec& rhs, double shift, Vec& res) {
+    const int n = H.n, m = H.m;
+    std::vector<double> S((size_t)m * m, 0.0);
+    for (int j = 0; j < m; j++) S[(size_t)j * m + j] = H.h2[j] + shift;
+    for (int i = 0; i < n; i++) {
+        const double w = 1.0 / (H.h1[i] + shift);
+        const auto& r = H.sigma[i];
+        for (size_t p = 0; p < r.size(); p++)
+            for (size_t q = 0; q <= p; q++) {
+                const int j = r[p], k = r[q];
+                S[(size_t)std::max(j, k) * m + std::min(j, k)] -= w;
+            }
+    }
+    if (!cholesky(S, m)) return false;
+    Vec v(n), y(m), r2(m);
+    for (int i = 0; i < n; i++) v[i] = rhs[i] / (H.h1[i] + shift);
+    H.apply_sigmatx(v.data(), y.data());
+    for (int j = 0; j < m; j++) r2[j] = rhs[n + j] - y[j];
+    cholesky_solve(S, m, r2);
+    res.assign(n + m, 0.0);
+    Vec bx(n);
+    H.apply_sigmax(r2.data(), bx.data());
+    for (int i = 0; i < n; i++) res[i] = (rhs[i] - bx[i]) / (H.h1[i] + shift);
+    for (int j = 0; j < m; j++) res[n + j] = r2[j];
+    return true;
+}
+
+// ---------------- L-BFGS (LBFGS++ restated) ----------------
+
+struct LineSearchError : std::runtime_error {
+    using std::runtime_error::runtime_error;
+};
+
+// L-BFGS parameters: LBFGSParam() defaults (Param.h:168-182) with the
+// overrides of qrot_lbfgs_dual.cpp:100-103.
+struct LbfgsParam {
+    int m = 6;
+    double epsilon = 1e-5, epsilon_rel = 1e-5;
+    int max_iterations = 0;
+    int max_linesearch = 20;
+    double ftol = 1e-4, wolfe = 0.9;
+};
+
+// Compact two-loop storage: BFGSMat.h:61-100 (reset/add_correction) and
+// apply_Hv 276-302.
+struct BfgsMat {
+    int mm = 0, ncorr = 0, ptr = 0;
+    double theta = 1.0;
+    std::vector<Vec> s, y;
+    Vec ys, alpha;
+    void reset(int n, int m_) {
+        mm = m_;
+        theta = 1.0;
+        s.assign(mm, Vec(n));
+        y.assign(mm, Vec(n));
+        ys.assign(mm, 0.0);
+        alpha.assign(mm, 0.0);
+        ncorr = 0;
+        ptr = mm;
+    }
+    void add_correction(const Vec& sv, const Vec& yv) {
+        const int loc = ptr % mm;
+        s[loc] = sv;
+        y[loc] = yv;
+        const double yts = dot(s[loc], y[loc]);
+        ys[loc] = yts;
+        theta = sqnorm(y[loc]) / yts;
+        if (ncorr < mm) ncorr++;
+        ptr = loc + 1;
+    }
+    void apply_Hv(const Vec& v, double a, Vec& res) {
+        const size_t n = v.size();
+        res.resize(n);
+        for (size_t k = 0; k < n; k++) res[k] = a * v[k];
+        int j = ptr % mm;
+        for (int i = 0; i < ncorr; i++) {
+            j = (j + mm - 1) % mm;
+            alpha[j] = dot(s[j], res) / ys[j];
+            for (size_t k = 0; k < n; k++) res[k] -= alpha[j] * y[j][k];
+        }
+        for (size_t k = 0; k < n; k++) res[k] /= theta;
+        for (int i = 0; i < ncorr; i++) {
+            const double beta = dot(y[j], res) / ys[j];
+            for (size_t k = 0; k < n; k++) res[k] += (alpha[j] - beta) * s[j][k];
+            j = (j + 1) % mm;
+        }
+    }
+};
+
+using FunGrad = std::function<double(const Vec&, Vec&)>;
+
+// quad_interp: LineSearchNocedalWright.h:30-60.
+static double quad_interp(double step_lo, double step_hi, double fx_lo, double fx_hi,
+                          double dg_lo) {
+    const double fdiff = fx_hi - fx_lo;
+    const double sdiff = step_hi - step_lo;
+    const double smid = (step_hi + step_lo) / 2.0;
+    double cand = fdiff * step_lo - smid * sdiff * dg_lo;
+    cand = cand / (fdiff - sdiff * dg_lo);
+    const bool cand_nan = !std::isfinite(cand);
+    const double end_dist = std::min(std::abs(cand - step_lo), std::abs(cand - step_hi));
+    const bool near_end = end_dist < 0.01 * std::abs(sdiff);
+    const bool bisect = cand_nan || (cand <= std::min(step_lo, step_hi)) ||
+                        (cand >= std::max(step_lo, step_hi)) || near_end;
+    return bisect ? smid : cand;
+}
+
+// LineSearchNocedalWright::LineSearch: LineSearchNocedalWright.h:85-280
+// (bracketing, then zoom with quadratic interpolation).
+static void line_search_nw(const FunGrad& f, const LbfgsParam& param, const Vec& xp,
+                           const Vec& drt, double& step, double& fx, Vec& grad, double& dg,
+                           Vec& x) {
+    const size_t n = xp.size();
+    if (step <= 0.0) throw std::invalid_argument("'step' must be positive");
+    const double expansion = 2.0;
+    const double fx_init = fx;
+    const double dg_init = dg;
+    if (dg_init > 0.0)
+        throw std::logic_error("the moving direction increases the objective function value");
+    const double test_decr = param.ftol * dg_init, test_curv = -param.wolfe * dg_init;
+    double step_hi = 0.0, fx_hi = 0.0;
+    double step_lo = 0.0, fx_lo = fx_init, dg_lo = dg_init;
+    Vec x_lo = xp, grad_lo = grad;
+    int iter = 0;
+    for (;;) {
+        for (size_t k = 0; k < n; k++) x[k] = xp[k] + step * drt[k];
+        fx = f(x, grad);
+        dg = dot(grad, drt);
+        if (fx - fx_init > step * test_decr || (0.0 < step_lo && fx >= fx_lo)) {
+            step_hi = step;
+            fx_hi = fx;
+            break;
+        }
+        if (std::abs(dg) <= test_curv) return;
+        step_hi = step_lo;
+        fx_hi = fx_lo;
+        step_lo = step;
+        fx_lo = fx;
+        dg_lo = dg;
+        x_lo.swap(x);
+        grad_lo.swap(grad);
+        if (dg >= 0.0) break;
+        iter++;
+        if (iter >= param.max_linesearch) {
+            x.swap(x_lo);
+            grad.swap(grad_lo);
+            return;
+        }
+        step *= expansion;
+    }
+    for (;;) {
+        step = quad_interp(step_lo, step_hi, fx_lo, fx_hi, dg_lo);
+        for (size_t k = 0; k < n; k++) x[k] = xp[k] + step * drt[k];
+        fx = f(x, grad);
+        dg = dot(grad, drt);
+        if (fx - fx_init > step * test_decr || fx >= fx_lo) {
+            if (step == step_hi)
+                throw LineSearchError(
+                    "the line search routine failed, possibly due to insufficient numeric precision");
+            step_hi = step;
+            fx_hi = fx;
+        } else {
+            if (std::abs(dg) <= test_curv) return;
+            if (dg * (step_hi - step_lo) >= 0.0) {
+                step_hi = step_lo;
+                fx_hi = fx_lo;
+            }
+            if (step == step_lo)
+                throw LineSearchError(
+                    "the line search routine failed, possibly due to insufficient numeric precision");
+            step_lo = step;
+            fx_lo = fx;
+            dg_lo = dg;
+            x_lo.swap(x);
+            grad_lo.swap(grad);
+        }
+        iter++;
+        if (iter >= param.max_linesearch) {
+            if (step_lo <= 0.0)
+                throw LineSearchError(
+                    "the line search routine failed, unable to sufficiently decrease the function value");
+            step = step_lo;
+            fx = fx_lo;
+            dg = dg_lo;
+            x.swap(x_lo);
+            grad.swap(grad_lo);
+            return;
+        }
+    }
+}
+
+// LBFGSSolver::minimize: LBFGS.h:79-175. `iterate` is called after the
+// initial evaluation and after every line search (QROTDual::iterate).
+static int lbfgs_minimize(const FunGrad& f, const std::function<void(const Vec&, double)>& iterate,
+                          const LbfgsParam& param, Vec& x, double& fx) {
+    const size_t n = x.size();
+    BfgsMat bfgs;
+    bfgs.reset((int)n, param.m);
+    Vec xp(n), grad(n), gradp(n), drt(n);
+    fx = f(x, grad);
+    double gnorm = norm(grad);
+    iterate(x, gnorm);
+    if (gnorm <= param.epsilon || gnorm <= param.epsilon_rel * norm(x)) return 1;
+    for (size_t k = 0; k < n; k++) drt[k] = -grad[k];
+    double step = 1.0 / norm(drt);
+    const double eps = std::numeric_limits<double>::epsilon();
+    Vec vs(n), vy(n);
+    int k = 1;
+    for (;;) {
+        xp = x;
+        gradp = grad;
+        double dg = dot(grad, drt);
+        line_search_nw(f, param, xp, drt, step, fx, grad, dg, x);
+        gnorm = norm(grad);
+        iterate(x, gnorm);
+        if (gnorm <= param.epsilon || gnorm <= param.epsilon_rel * norm(x)) return k;
+        if (param.max_iterations != 0 && k >= param.max_iterations) return k;
+        for (size_t q = 0; q < n; q++) {
+            vs[q] = x[q] - xp[q];
+            vy[q] = grad[q] - gradp[q];
+        }
+        if (dot(vs, vy) > eps * sqnorm(vy)) bfgs.add_correction(vs, vy);
+        bfgs.apply_Hv(grad, -1.0, drt);
+        step = 1.0;
+        k++;
+    }
+}
+
+static void get_plan(const Problem& p, const double* gamma, double* plan) {
+    // qrot_result.h:31-43, written row-major.
+    for (int i = 0; i < p.n; i++)
+        for (int j = 0; j < p.m; j++) {
+            const double C = gamma[i] + gamma[p.n + j] - p.Mij(i, j);
+            plan[(size_t)i * p.m + j] = std::max(C, 0.0) / p.reg;
+        }
+}
+
+static void init_gamma(const Problem& p, const oracle_opts* opts, Vec& gamma) {
+    gamma.assign(p.n + p.m, 0.0);
+    if (opts && opts->x0 && opts->x0_len == p.n + p.m) {
+        std::copy(opts->x0, opts->x0 + p.n + p.m, gamma.begin());
+        return;
+    }
+    optimal_beta(p, gamma.data(), gamma.data() + p.n);
+}
+
+}  // namespace qrot
+}  // namespace oracle
+
+using namespace oracle;
+using namespace oracle::qrot;
+
+static Problem make_problem(const double* M, int n, int m, const double* a, const double* b,
+                            double reg, double tau) {
+    Problem p;
+    p.n = n;
+    p.m = m;
+    p.M = M;
+    p.a = a;
+    p.b = b;
+    p.reg = reg;
+    p.tau = tau;
+    return p;
+}
+
+extern "C" {
+
+double oracle_qrot_dual_obj(const double* M, int n, int m, const double* a, const double* b,
+                            double reg, double tau, const double* gamma) {
+    return dual_obj(make_problem(M, n, m, a, b, reg, tau), gamma);
+}
+
+double oracle_qrot_dual_obj_grad(const double* M, int n, int m, const double* a, const double* b,
+                                 double reg, double tau, const double* gamma, double* grad) {
+    return dual_obj_grad(make_problem(M, n, m, a, b, reg, tau), gamma, grad);
+}
+
+void oracle_qrot_optimal_beta(const double* M, int n, int m, const double* b, double reg,
+                              const double* alpha, double* beta) {
+    Problem p = make_problem(M, n, m, nullptr, b, reg, 0.0);
+    optimal_beta(p, alpha, beta);
+}
+
+double oracle_qrot_primal_val(const double* M, int n, int m, const double* a, const double* b,
+                              double reg, const double* gamma) {
+    return primal_val(make_problem(M, n, m, a, b, reg, 0.0), gamma);
+}
+
+int oracle_qrot_hess_cg(const double* M, int n, int m, const double* gamma, const double* rhs,
+                        double shift, double tau, double cg_tol, double* res) {
+    std::vector<double> ones(std::max(n, m), 1.0);
+    Problem p = make_problem(M, n, m, ones.data(), ones.data(), 1.0, tau);
+    Hessian H;
+    Vec g(n + m), r(rhs, rhs + n + m), out;
+    D_hess(p, gamma, g.data(), g.data() + n, H);
+    const int it = hess_cg(H, r, shift, tau, cg_tol, out);
+    std::copy(out.begin(), out.end(), res);
+    return it;
+}
+
+void oracle_qrot_plan(const double* M, int n, int m, double reg, const double* gamma,
+                      double* plan) {
+    get_plan(make_problem(M, n, m, nullptr, nullptr, reg, 0.0), gamma, plan);
+}
+
+// qrot_lbfgs_dual_internal: qrot_lbfgs_dual.cpp:81-126 (QROTDual 18-79).
+int oracle_qrot_lbfgs_dual(const double* M, int n, int m, const double* a, const double* b,
+                           double reg, double tol, int max_iter, int verbose,
+                           const oracle_opts* opts, oracle_result* res) {
+    try {
+        const double tau = opts ? opts->tau : 0.0;
+        Problem p = make_problem(M, n, m, a, b, reg, tau);
+        LbfgsParam param;
+        param.epsilon = tol;
+        param.epsilon_rel = tol;
+        param.max_iterations = max_iter;
+        Vec gamma;
+        init_gamma(p, opts, gamma);
+        History h(res);
+        Timer timer;
+        double last_obj = std::numeric_limits<double>::infinity();
+        int it = 0;
+        FunGrad fg = [&](const Vec& x, Vec& g) {
+            last_obj = dual_obj_grad(p, x.data(), g.data());
+            return last_obj;
+        };
+        auto iterate = [&](const Vec& x, double gnorm) {
+            const double d = timer.toc();
+            const double prim = primal_val(p, x.data());
+            h.push(last_obj, gnorm / reg, h.last_time() + d, 0.0, prim);
+            if (verbose >= 1)
+                std::printf("iter = %d, objval = %g, ||grad|| = %g\n", it, last_obj, gnorm);
+            it++;
+            timer.tic();
+        };
+        timer.tic();
+        double fx;
+        const int niter = lbfgs_minimize(fg, iterate, param, gamma, fx);
+        res->niter = niter;
+        res->hist_len = h.len;
+        std::copy(gamma.begin(), gamma.end(), res->dual);
+        if (res->plan) get_plan(p, gamma.data(), res->plan);
+        return 0;
+    } catch (const std::invalid_argument& e) {
+        set_err(res, e.what());
+        return 2;
+    } catch (const std::exception& e) {
+        set_err(res, e.what());
+        return 1;
+    }
+}
+
+// qrot_assn_internal: qrot_assn.cpp:16-170.
+int oracle_qrot_assn(const double* M, int n, int m, const double* a, const double* b, double reg,
+                     double tol, int max_iter, int verbose, const oracle_opts* opts,
+                     oracle_result* res) {
+    try {
+        const double tau = opts ? opts->tau : 0.0;
+        const int method = opts ? opts->method : 0;
+        constexpr double nu = 0.99, eta1 = 0.25, eta2 = 0.75, gamma1 = 2.0, gamma2 = 4.0,
+                         lam_min = 0.01, beta = 0.5, cg_tol = 1e-8;
+        double xi = 0.0, lam = 1.0;
+        Problem p = make_problem(M, n, m, a, b, reg, tau);
+        const int N = n + m;
+        Vec gamma, u(N), gu(N), v(N), gv(N), direc, g(N);
+        init_gamma(p, opts, gamma);
+        History h(res);
+        Timer timer;
+        timer.tic();
+        Hessian H;
+        double f = dual_obj_grad_hess(p, gamma.data(), g.data(), H);
+        double gnorm = norm(g);
+        double d = timer.toc();
+        h.push(f, gnorm / reg, d, 0.0, primal_val(p, gamma.data()));
+        int i;
+        for (i = 0; i < max_iter; i++) {
+            if (verbose >= 1)
+                std::printf("iter = %d, objval = %g, ||grad|| = %g\n", i, f, gnorm);
+            timer.tic();
+            if (gnorm < tol) break;
+            if (i == 0) xi = gnorm;
+            const double mu = lam * gnorm;
+            Vec rhs(N);
+            for (int q = 0; q < N; q++) rhs[q] = -g[q];
+            if (method == 0 || tau > 0.0) {
+                hess_cg(H, rhs, mu, tau, cg_tol, direc);
+            } else if (!hess_direct(H, rhs, mu, direc)) {
+                throw std::runtime_error("sparse factorization failed");
+            }
+            for (int q = 0; q < N; q++) u[q] = gamma[q] + direc[q];
+            dual_obj_grad(p, u.data(), gu.data());
+            const double gunorm = norm(gu);
+            if (gunorm <= nu * xi) {
+                gamma.swap(u);
+                xi = gunorm;
+            } else {
+                const double numer = -dot(gu, direc);
+                const double denom = sqnorm(direc);
+                const double rho = numer / denom;
+                for (int q = 0; q < N; q++) v[q] = gamma[q] + (-numer) / (gunorm * gunorm) * gu[q];
+                dual_obj_grad(p, v.data(), gv.data());
+                const double gvnorm = norm(gv);
+                if (rho >= eta1 && gvnorm <= gnorm) {
+                    gamma.swap(v);
+                } else {
+                    for (int q = 0; q < N; q++) gamma[q] -= beta * g[q];
+                }
+                if (rho >= eta2) {
+                    lam = 0.5 * (lam_min + lam);
+                } else if (rho >= eta1) {
+                    lam *= gamma1;
+                } else {
+                    lam *= gamma2;
+                }
+            }
+            f = dual_obj_grad_hess(p, gamma.data(), g.data(), H);
+            gnorm = norm(g);
+            d = timer.toc();
+            h.push(f, gnorm / reg, h.last_time() + d, 0.0, primal_val(p, gamma.data()));
+        }
+        res->niter = i;
+        res->hist_len = h.len;
+        std::copy(gamma.begin(), gamma.end(), res->dual);
+        if (res->plan) get_plan(p, gamma.data(), res->plan);
+        return 0;
+    } catch (const std::exception& e) {
+        set_err(res, e.what());
+        return 1;
+    }
+}
+
+}  // extern "C"
