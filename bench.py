@@ -1,0 +1,354 @@
+#!/usr/bin/env python3
+"""Benchmark: EROT time-to-tolerance (mar_err <= 1e-6) at n = m = 8192 on one GB300.
+
+Workload (large dense EROT): x_i ~ N(0, I_3), y_j ~ N(0.5, I_3) (seed 0),
+M = squared Euclidean distance / max, stored FP32; a, b ~ U(0.5, 1.5)
+normalised; reg = 0.01; tol = 1e-6; solver sinkhorn_bcd (mixed precision:
+FP32 M, FP64 duals). Synthetic data of the benchmark's shape.
+
+One step = one solve to tolerance.
+  value : ms per solve with M already resident in HBM (duals only; no plan).
+  e2e   : the same solve through the public API regot.sinkhorn_bcd with M in
+          pinned host memory: upload of M, solve, plan recovery and the
+          device->host copy of dual, histories and the FP64 plan, per step.
+M (256 MiB) is larger than L2 (129 MB), so no flush between steps is needed.
+
+Also reported: the roofline of the dominant kernel (the row/column
+log-sum-exp pass over M) timed with CUDA events on torch's current stream,
+the CPU baseline (the FP64 oracle restatement of the reference, timed on the
+host), clocks sampled during the timed region, and the number of kernels
+launched in the timed region.
+
+--impl reference times the reference algorithm on the host CPU (the oracle
+port: the reference itself cannot be built here) on the same workload and
+prints the same JSON line with "impl": "reference".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+for sub in ("regot-python_gb300", "oracle", "tests"):
+    p = os.path.join(REPO, sub)
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "EROT ms-to-mar_err<=1e-6 (n=m=8192)"
+UNIT = "ms"
+N = 8192
+REG = 0.01
+TOL = 1e-6
+MAX_ITER = 1000
+
+
+def workload_config(n):
+    return {"workload": f"large dense EROT n=m={n}, sqeuclid/max of 3-D Gaussian clouds "
+                        f"(seed 0), FP32 M, FP64 duals, reg={REG}, tol={TOL}",
+            "solver": "sinkhorn_bcd", "n": n, "m": n, "reg": REG, "tol": TOL,
+            "precision": "mixed", "l2": "M (4*n*m bytes) larger than L2; no flush needed",
+            "value": "device-resident solve, duals only",
+            "e2e": "regot.sinkhorn_bcd on pinned host M incl. upload, plan and D2H"}
+
+
+def rank_env():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.thread.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per launch of the row pass from the committed ncu summary."""
+    path = os.path.join(REPO, "profiles", "dense_pass_erot_row_8192.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return int(line.split(":")[1].strip())
+    except OSError:
+        pass
+    return None
+
+
+def cpu_solve_sample(M64, a, b, iters):
+    """Oracle (FP64 CPU restatement) init + `iters` BCD iterations; returns
+    (init_ms, per_iter_ms)."""
+    import regot_oracle as O
+
+    t = time.perf_counter()
+    O.sinkhorn_bcd(M64, a, b, REG, tol=TOL, max_iter=0, plan=False)
+    t_init = (time.perf_counter() - t) * 1e3
+    t = time.perf_counter()
+    O.sinkhorn_bcd(M64, a, b, REG, tol=TOL, max_iter=iters, plan=False)
+    t_all = (time.perf_counter() - t) * 1e3
+    return t_init, max(t_all - t_init, 0.0) / max(iters, 1)
+
+
+def run_reference(args, n):
+    rank, world, _ = rank_env()
+    if rank != 0:
+        return
+    from problems import erot_points
+
+    import regot_oracle as O
+
+    M, a, b = erot_points(n, n, seed=0, dtype=np.float32)
+    M64 = np.asfortranarray(M.astype(np.float64))
+    t = time.perf_counter()
+    full = O.sinkhorn_bcd(M64, a, b, REG, tol=TOL, max_iter=MAX_ITER, plan=False)
+    full_ms = (time.perf_counter() - t) * 1e3
+    niter = full.niter
+    samples = []
+    for step in range(args.warmup + args.steps):
+        t_init, t_iter = cpu_solve_sample(M64, a, b, 1)
+        if step >= args.warmup:
+            samples.append(t_init + niter * t_iter)
+    value = statistics.median(samples)
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "impl": "reference",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(value, 3), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_config(n),
+        "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": 1, "kind": "port",
+                         "sample": f"FP64 oracle restatement of sinkhorn_bcd (single-threaded "
+                                   f"like the reference): init + 1 iteration per step, "
+                                   f"extrapolated to the {niter} iterations of one full oracle "
+                                   f"solve ({full_ms:.0f} ms wall)"},
+        "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ncu-case", action="store_true",
+                    help="one short solve for an ncu capture (no timing, no JSON)")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    n = args.n
+
+    if args.impl == "reference":
+        run_reference(args, n)
+        return
+    if args.ncu_case:
+        import regot
+        from problems import erot_points
+
+        M, a, b = erot_points(n, n, seed=0, dtype=np.float32)
+        prob = regot.Problem(M, a, b, precision="mixed")
+        r = prob.sinkhorn_bcd(REG, tol=TOL, max_iter=3, plan=False)
+        print("ncu case: niter", r.niter, "mar_err", r.mar_errs[-1])
+        return
+
+    import torch
+
+    rank, world, local = rank_env()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    import regot
+    from problems import erot_points
+    from regot import _lib
+
+    M, a, b = erot_points(n, n, seed=rank, dtype=np.float32)
+    ctx = _lib.context(local)
+    # The library launches on this (non-default) torch stream, so that
+    # torch.cuda.Event records on the stream the kernels run on.
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+
+    # ---- device-resident value ----
+    prob = regot.Problem(M, a, b, precision="mixed", device=local)
+    for _ in range(args.warmup):
+        r = prob.sinkhorn_bcd(REG, tol=TOL, max_iter=MAX_ITER, plan=False)
+    launches0 = ctx.kernel_launches()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize(dev)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            r = prob.sinkhorn_bcd(REG, tol=TOL, max_iter=MAX_ITER, plan=False)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+    if dist:
+        dist.barrier()
+    launches = ctx.kernel_launches() - launches0
+    elapsed = e0.elapsed_time(e1)
+    if dist:
+        t = torch.tensor([elapsed], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    ms_per_step = elapsed / args.steps
+    value = elapsed / (args.steps * world)
+    niter, mar = r.niter, r.mar_errs[-1]
+
+    # ---- roofline of the dominant kernel (row / column LSE pass) ----
+    reps = 20
+    torch.cuda.synchronize(dev)
+    k0 = torch.cuda.Event(enable_timing=True)
+    k1 = torch.cuda.Event(enable_timing=True)
+    _lib.load().regot_time_pass(ctx.handle, prob.handle, 0, REG, 1)  # warm
+    torch.cuda.synchronize(dev)
+    k0.record(stream)
+    ctx.check(_lib.load().regot_time_pass(ctx.handle, prob.handle, 0, REG, reps))
+    k1.record(stream)
+    torch.cuda.synchronize(dev)
+    row_ms = k0.elapsed_time(k1) / reps
+    k0.record(stream)
+    ctx.check(_lib.load().regot_time_pass(ctx.handle, prob.handle, 1, REG, reps))
+    k1.record(stream)
+    torch.cuda.synchronize(dev)
+    col_ms = k0.elapsed_time(k1) / reps
+    alg_bytes = 4 * n * n
+    achieved = alg_bytes / (row_ms * 1e-3) / 1e9
+    peak, peak_src = measured_peaks()
+    traffic = profiled_traffic()
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                "frac": round(achieved / peak, 4), "traffic": traffic,
+                "kernel": "dense_pass<float, OP_E_ROW> (row log-sum-exp pass)",
+                "algorithmic_bytes_per_launch": alg_bytes, "launch_ms": round(row_ms, 5),
+                "col_pass_launch_ms": round(col_ms, 5),
+                "col_pass_frac": round(alg_bytes / (col_ms * 1e-3) / 1e9 / peak, 4),
+                "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)"}
+    prob.close()
+
+    # ---- end to end through the public API (pinned host M) ----
+    Mp = torch.empty((n, n), dtype=torch.float32, pin_memory=True)
+    Mp.numpy()[:] = M
+    Mh = Mp.numpy()
+    for _ in range(1):
+        regot.sinkhorn_bcd(Mh, a, b, REG, tol=TOL, max_iter=MAX_ITER, device=local)
+    torch.cuda.synchronize(dev)
+    t = time.perf_counter()
+    e2e_steps = max(1, min(args.steps, 5))
+    for _ in range(e2e_steps):
+        re = regot.sinkhorn_bcd(Mh, a, b, REG, tol=TOL, max_iter=MAX_ITER, device=local)
+    torch.cuda.synchronize(dev)
+    e2e_ms = (time.perf_counter() - t) * 1e3 / e2e_steps
+    h2d = M.nbytes + a.nbytes + b.nbytes
+    d2h = re.plan.nbytes + re.dual.nbytes + 3 * 8 * len(re.mar_errs)
+
+    # ---- CPU baseline (rank 0, N = 1) ----
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        prob64 = regot.Problem(M, a, b, precision="fp64", device=local)
+        n64 = prob64.sinkhorn_bcd(REG, tol=TOL, max_iter=MAX_ITER, plan=False).niter
+        prob64.close()
+        M64 = np.asfortranarray(M.astype(np.float64))
+        iters = 3
+        t_init, t_iter = cpu_solve_sample(M64, a, b, iters)
+        cpu = {"value": round(t_init + n64 * t_iter, 1), "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"FP64 oracle sinkhorn_bcd on the same problem: init + {iters} "
+                         f"iterations timed ({t_init:.0f} ms + {t_iter:.0f} ms/iter), "
+                         f"extrapolated to the {n64} iterations the FP64 algorithm needs"}
+
+    line = {
+        "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+        "data": "synthetic", "config": dict(workload_config(n), parallelism=f"replicas x{world}",
+                                            niter=niter, final_mar_err=mar),
+        "e2e": {"value": round(e2e_ms, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
+        "gpu_launches": int(launches),
+    }
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,195 @@
+/*
+ * regot_gb300 -- C ABI of the GB300 (sm_103a) implementation of RegOT's dense
+ * dual-evaluation hot path.
+ *
+ * The reference exposes its solvers through one pybind11 module,
+ * regot._internal (src/solvers.cpp:463-569); each solver takes
+ * (M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs) and returns a
+ * result object with niter / dual / plan / obj_vals / mar_errs / run_times
+ * (+ densities for EROT, prim_vals for QROT). The entry points below are what
+ * a binding of that module needs: one call per solver with plain pointers and
+ * sizes, caller-owned output buffers, an int status and a per-context error
+ * string. No torch or CUDA types appear in the signatures; device pointers
+ * are accepted where a descriptor says so.
+ *
+ * Threading: one regot_ctx per host thread; calls on one context are not
+ * thread-safe. Every call is synchronous with respect to the host.
+ */
+#ifndef REGOT_GB300_H
+#define REGOT_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. Python maps INVALID_ARG to ValueError and the others to
+ * RuntimeError, like pybind11 maps the reference's std::invalid_argument and
+ * std::runtime_error / std::logic_error (src/solvers.cpp:280,290;
+ * src/LBFGSpp/LBFGSpp/LineSearchNocedalWright.h:93-117,227,247,267). */
+enum {
+    REGOT_OK = 0,
+    REGOT_ERR_INVALID_ARG = 1,
+    REGOT_ERR_NONFINITE = 2,
+    REGOT_ERR_LINESEARCH = 3,
+    REGOT_ERR_CUDA = 4,
+    REGOT_ERR_TIMEOUT = 5,
+    REGOT_ERR_NUMERIC = 6,
+    REGOT_ERR_NO_DEVICE = 7
+};
+
+enum { REGOT_F64 = 0, REGOT_F32 = 1 };              /* element type of M */
+enum { REGOT_MEM_HOST = 0, REGOT_MEM_DEVICE = 1 };  /* where a buffer lives */
+/* Arithmetic of the dense passes. FP64: M stored in FP64 and every
+ * element-wise operation in FP64 (the plain comparator). MIXED: M stored in
+ * FP32, exponent/relu arguments formed with an exact hi/lo split of the FP64
+ * duals, FP32 exp2 and accumulation in short FP32 chunks merged in FP64;
+ * duals, objective differences and marginal errors stay FP64. */
+enum { REGOT_PREC_FP64 = 0, REGOT_PREC_MIXED = 1 };
+
+typedef struct regot_ctx regot_ctx;
+typedef struct regot_dproblem regot_dproblem;
+
+/* Dense problem description. M is n x m row-major with row stride ldm
+ * elements (ldm >= m); a has n entries, b has m entries (FP64). */
+typedef struct {
+    const void* M;
+    int M_dtype;     /* REGOT_F64 or REGOT_F32 */
+    int M_mem;       /* REGOT_MEM_HOST or REGOT_MEM_DEVICE */
+    long long ldm;
+    int n, m;
+    const double* a;
+    const double* b;
+    int ab_mem;      /* REGOT_MEM_HOST or REGOT_MEM_DEVICE */
+} regot_problem_desc;
+
+/* Solver options. Defaults (regot_opts_init) follow SinkhornSolverOpts
+ * (src/sinkhorn_solvers.h:35-37) and QROTSolverOpts (src/qrot_solvers.h:28-30),
+ * with the per-solver overrides of src/solvers.cpp:124,415,433,451. */
+typedef struct {
+    int precision;        /* REGOT_PREC_* (default MIXED) */
+    int method;           /* linear solver selector; -1 = solver default */
+    double mu0;           /* SSNS initial shift factor (1.0) */
+    double shift;         /* (1e-3) */
+    double density;       /* (0.01) */
+    double tau;           /* QROT extra regularisation (0.0) */
+    const double* x0;     /* optional initial duals on the host, or NULL */
+    int x0_len;
+    double cg_tol;        /* Newton-CG relative residual target (1e-10) */
+    int cg_max_iter;      /* per Newton step (0 = 2*(n+m)) */
+    int verbose;
+    int plan;             /* 1 = fill result->plan, 0 = skip */
+    int plan_mem;         /* REGOT_MEM_HOST or REGOT_MEM_DEVICE */
+    int prim_vals;        /* QROT: 1 = evaluate prim_vals every iteration */
+} regot_opts;
+
+/* Caller-owned result buffers (host unless plan_mem says otherwise).
+ * History arrays need hist_cap >= max_iter + 2 entries; any may be NULL. */
+typedef struct {
+    int niter;
+    int hist_len;
+    int hist_cap;
+    double* dual;      /* n+m-1 (EROT, beta_m = 0 gauge) or n+m (QROT) */
+    double* plan;      /* n*m row-major FP64, or NULL */
+    double* obj_vals;
+    double* mar_errs;
+    double* run_times; /* cumulative milliseconds, device clock */
+    double* densities; /* EROT SSNS */
+    double* prim_vals; /* QROT */
+    /* statistics of the call */
+    long long passes;  /* streamed passes over M */
+    double solve_ms;   /* device time of the solve, upload excluded */
+} regot_result;
+
+void regot_opts_init(regot_opts* opts);
+
+/* Context: one CUDA device, one stream, a workspace grown on demand. */
+int regot_ctx_create(int device, regot_ctx** out);
+void regot_ctx_destroy(regot_ctx* ctx);
+const char* regot_ctx_last_error(const regot_ctx* ctx);
+/* Launch on an external cudaStream_t (as void*). NULL is the CUDA legacy
+ * default stream, as in the CUDA runtime; regot_ctx_set_stream(ctx,
+ * regot_ctx_own_stream(ctx)) restores the context's own stream. */
+int regot_ctx_set_stream(regot_ctx* ctx, void* stream);
+void* regot_ctx_own_stream(const regot_ctx* ctx);
+/* Number of kernels this context has launched so far. */
+long long regot_ctx_kernel_launches(const regot_ctx* ctx);
+
+/* Device-resident problem: M is converted to the storage of `precision`
+ * (FP64 or FP32, rows padded to 16 bytes) once; solves reuse it. */
+int regot_problem_create(regot_ctx* ctx, const regot_problem_desc* desc, int precision,
+                         regot_dproblem** out);
+void regot_problem_destroy(regot_dproblem* prob);
+
+/* ---- Solvers (reference: src/solvers.cpp:359-441 and 69-148) ---- */
+
+/* sinkhorn_bcd (src/sinkhorn_bcd.cpp:14-124). */
+int regot_sinkhorn_bcd(regot_ctx* ctx, regot_dproblem* prob, double reg, double tol,
+                       int max_iter, const regot_opts* opts, regot_result* res);
+/* sinkhorn_newton (src/sinkhorn_newton.cpp:17-129); the Newton system is
+ * solved matrix-free by CG on the exact Hessian instead of a dense LLT. */
+int regot_sinkhorn_newton(regot_ctx* ctx, regot_dproblem* prob, double reg, double tol,
+                          int max_iter, const regot_opts* opts, regot_result* res);
+/* sinkhorn_ssns (src/sinkhorn_ssns.cpp:16-234). */
+int regot_sinkhorn_ssns(regot_ctx* ctx, regot_dproblem* prob, double reg, double tol,
+                        int max_iter, const regot_opts* opts, regot_result* res);
+/* qrot_lbfgs_dual (src/qrot_lbfgs_dual.cpp:81-126). */
+int regot_qrot_lbfgs_dual(regot_ctx* ctx, regot_dproblem* prob, double reg, double tol,
+                          int max_iter, const regot_opts* opts, regot_result* res);
+/* qrot_assn (src/qrot_assn.cpp:16-170). */
+int regot_qrot_assn(regot_ctx* ctx, regot_dproblem* prob, double reg, double tol,
+                    int max_iter, const regot_opts* opts, regot_result* res);
+
+/* ---- Pass-level entry points (host vectors in and out) ---- */
+
+/* Problem::optimal_beta / optimal_alpha (src/sinkhorn_problem_bcd.cpp:149-201). */
+int regot_erot_optimal_beta(regot_ctx* ctx, regot_dproblem* prob, double reg,
+                            const double* alpha, double* beta);
+int regot_erot_optimal_alpha(regot_ctx* ctx, regot_dproblem* prob, double reg,
+                             const double* beta, double* alpha);
+/* Problem::dual_obj_grad (src/sinkhorn_problem_obj.cpp:363-393);
+ * gamma has n+m-1 entries (beta_m = 0). */
+int regot_erot_dual_obj_grad(regot_ctx* ctx, regot_dproblem* prob, double reg,
+                             const double* gamma, double* obj, double* grad);
+/* y = H x with H the dual Hessian of dual_obj_grad_densehess
+ * (src/sinkhorn_problem_obj.cpp:396-418), without forming H. */
+int regot_erot_hvp(regot_ctx* ctx, regot_dproblem* prob, double reg, const double* gamma,
+                   const double* x, double* y);
+/* SinkhornResult::get_plan (src/sinkhorn_result.h:32-50); plan row-major. */
+int regot_erot_plan(regot_ctx* ctx, regot_dproblem* prob, double reg, const double* gamma,
+                    double* plan, int plan_mem);
+/* QROT Problem::dual_obj_grad (src/qrot_problem.cpp:226-253). */
+int regot_qrot_dual_obj_grad(regot_ctx* ctx, regot_dproblem* prob, double reg,
+                             const double* gamma, double* obj, double* grad);
+/* QROT Problem::optimal_beta (src/qrot_problem.cpp:397-404). */
+int regot_qrot_optimal_beta(regot_ctx* ctx, regot_dproblem* prob, double reg,
+                            const double* alpha, double* beta);
+/* QROT Problem::primal_val (src/qrot_problem.cpp:10-24, src/approx_proj.h:6-26). */
+int regot_qrot_primal_val(regot_ctx* ctx, regot_dproblem* prob, double reg,
+                          const double* gamma, double* value);
+/* QROTResult::get_plan (src/qrot_result.h:31-43). */
+int regot_qrot_plan(regot_ctx* ctx, regot_dproblem* prob, double reg, const double* gamma,
+                    double* plan, int plan_mem);
+
+/* ---- Measurement ---- */
+
+/* Kinds of dense pass for regot_time_pass. */
+enum {
+    REGOT_PASS_EROT_ROW = 0,   /* row log-sum-exp pass of sinkhorn_bcd */
+    REGOT_PASS_EROT_COL = 1,   /* column log-sum-exp pass of sinkhorn_bcd */
+    REGOT_PASS_EROT_GRAD = 2,  /* fused row+column sums (objective / gradient) */
+    REGOT_PASS_EROT_HVP = 3,   /* Hessian-vector product */
+    REGOT_PASS_QROT_GRAD = 4   /* QROT relu objective / gradient */
+};
+/* Enqueue `reps` launches of one dense pass over M on the context's stream
+ * (duals zero, beta = 0) and return without synchronising, so that the
+ * caller can bracket them with its own events. No counterpart in the
+ * reference: it measures the kernels behind the solvers above. */
+int regot_time_pass(regot_ctx* ctx, regot_dproblem* prob, int kind, double reg, int reps);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* REGOT_GB300_H */

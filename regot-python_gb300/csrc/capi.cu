@@ -1,0 +1,487 @@
+// C ABI of regot_gb300 (declarations and reference citations in
+// include/regot_gb300.h): contexts, device-resident problems, the solver
+// entry points and the pass-level entry points. Every entry point converts
+// exceptions into a status code and a per-context message.
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "device_util.cuh"
+#include "erot_ops.cuh"
+#include "internal.h"
+#include "solvers.h"
+
+using namespace regot;
+
+namespace {
+
+template <typename F>
+int guarded(regot_ctx* ctx, F&& f) {
+    if (!ctx) return REGOT_ERR_INVALID_ARG;
+    long long* saved = g_launch_counter;
+    g_launch_counter = &ctx->launches;
+    int rc = REGOT_OK;
+    try {
+        REGOT_CUDA(cudaSetDevice(ctx->device));
+        f();
+        ctx->last_error.clear();
+    } catch (const Error& e) {
+        ctx->last_error = e.what();
+        rc = e.code;
+    } catch (const std::exception& e) {
+        ctx->last_error = e.what();
+        rc = REGOT_ERR_NUMERIC;
+    }
+    g_launch_counter = saved;
+    return rc;
+}
+
+template <typename TS, typename TD>
+__global__ void k_convert(const TS* src, long long lds, TD* dst, long long ldd, int n, int m) {
+    const long long total = (long long)n * ldd;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const long long i = t / ldd, j = t - i * ldd;
+        dst[t] = j < m ? (TD)src[i * lds + j] : (TD)0;
+    }
+}
+
+__global__ void k_check_finite(const double* x, int len, int* bad) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < len; i += gridDim.x * blockDim.x)
+        if (!isfinite(x[i])) atomicOr(bad, 1);
+}
+
+void check_solver_args(regot_dproblem* P, double reg, double tol, int max_iter, regot_result* res,
+                       int dual_len) {
+    require(P != nullptr, "problem is NULL");
+    require(res != nullptr, "result is NULL");
+    require(std::isfinite(reg) && reg > 0.0, "reg must be a positive finite number");
+    require(!std::isnan(tol), "tol must not be NaN");
+    require(max_iter >= 0, "max_iter must be non-negative");
+    require(res->dual != nullptr, "result dual buffer is NULL");
+    require(res->hist_cap >= max_iter + 2 ||
+                (!res->obj_vals && !res->mar_errs && !res->run_times && !res->densities &&
+                 !res->prim_vals),
+            "history capacity must be at least max_iter + 2");
+    (void)dual_len;
+}
+
+regot_opts effective_opts(const regot_opts* o) {
+    regot_opts e;
+    regot_opts_init(&e);
+    if (o) e = *o;
+    return e;
+}
+
+}  // namespace
+
+namespace regot {
+
+void finish_erot_result(ErotOps& ops, const double* d_gamma, const double* hobj,
+                        const double* hmar, const double* htime, const double* hdens,
+                        int hist_len, int hist_cap, int niter, long long passes,
+                        const regot_opts& o, regot_result* res) {
+    cudaStream_t st = ops.stream();
+    const int n = ops.n(), m = ops.m();
+    (void)hist_cap;
+    res->niter = niter;
+    res->hist_len = hist_len;
+    res->passes = passes;
+    d2h(res->dual, d_gamma, (size_t)(n + m - 1) * sizeof(double), st);
+    if (res->obj_vals) d2h(res->obj_vals, hobj, hist_len * sizeof(double), st);
+    if (res->mar_errs) d2h(res->mar_errs, hmar, hist_len * sizeof(double), st);
+    if (res->run_times) d2h(res->run_times, htime, hist_len * sizeof(double), st);
+    if (res->densities && hdens) d2h(res->densities, hdens, hist_len * sizeof(double), st);
+    if (o.plan && res->plan) {
+        DBuf<double> mx(1, st);
+        if (o.plan_mem == REGOT_MEM_DEVICE) {
+            ops.plan(d_gamma, d_gamma + n, res->plan, mx.get());
+        } else {
+            DBuf<double> P((size_t)n * m, st);
+            ops.plan(d_gamma, d_gamma + n, P.get(), mx.get());
+            d2h(res->plan, P.get(), (size_t)n * m * sizeof(double), st);
+            sync(st);
+        }
+    }
+    sync(st);
+}
+
+}  // namespace regot
+
+extern "C" {
+
+void regot_opts_init(regot_opts* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->precision = REGOT_PREC_MIXED;
+    o->method = -1;
+    o->mu0 = 1.0;
+    o->shift = 1e-3;
+    o->density = 0.01;
+    o->tau = 0.0;
+    o->x0 = nullptr;
+    o->x0_len = 0;
+    o->cg_tol = 1e-10;
+    o->cg_max_iter = 0;
+    o->verbose = 0;
+    o->plan = 1;
+    o->plan_mem = REGOT_MEM_HOST;
+    o->prim_vals = 1;
+}
+
+int regot_ctx_create(int device, regot_ctx** out) {
+    if (!out) return REGOT_ERR_INVALID_ARG;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) return REGOT_ERR_NO_DEVICE;
+    if (device < 0 || device >= count) return REGOT_ERR_INVALID_ARG;
+    regot_ctx* ctx = new regot_ctx();
+    ctx->device = device;
+    const int rc = guarded(ctx, [&] {
+        REGOT_CUDA(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking));
+        ctx->stream = ctx->own_stream;
+    });
+    if (rc != REGOT_OK) {
+        delete ctx;
+        return rc;
+    }
+    *out = ctx;
+    return REGOT_OK;
+}
+
+void regot_ctx_destroy(regot_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->own_stream) {
+        cudaStreamSynchronize(ctx->own_stream);
+        cudaStreamDestroy(ctx->own_stream);
+    }
+    delete ctx;
+}
+
+const char* regot_ctx_last_error(const regot_ctx* ctx) {
+    return ctx ? ctx->last_error.c_str() : "NULL context";
+}
+
+int regot_ctx_set_stream(regot_ctx* ctx, void* stream) {
+    if (!ctx) return REGOT_ERR_INVALID_ARG;
+    ctx->stream = reinterpret_cast<cudaStream_t>(stream);
+    return REGOT_OK;
+}
+
+void* regot_ctx_own_stream(const regot_ctx* ctx) {
+    return ctx ? reinterpret_cast<void*>(ctx->own_stream) : nullptr;
+}
+
+long long regot_ctx_kernel_launches(const regot_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+int regot_problem_create(regot_ctx* ctx, const regot_problem_desc* d, int precision,
+                         regot_dproblem** out) {
+    return guarded(ctx, [&] {
+        require(d != nullptr && out != nullptr, "NULL argument");
+        *out = nullptr;
+        require(d->n > 0 && d->m > 0, "M must have at least one row and one column");
+        require(d->ldm >= d->m, "ldm must be >= m");
+        require(d->M && d->a && d->b, "M, a and b must not be NULL");
+        require(d->M_dtype == REGOT_F64 || d->M_dtype == REGOT_F32, "unsupported dtype of M");
+        require(precision == REGOT_PREC_FP64 || precision == REGOT_PREC_MIXED,
+                "unsupported precision");
+        cudaStream_t st = ctx->stream;
+        const int n = d->n, m = d->m;
+        auto* P = new regot_dproblem();
+        try {
+            P->ctx = ctx;
+            P->n = n;
+            P->m = m;
+            P->prec = precision;
+            const size_t es = precision == REGOT_PREC_FP64 ? 8 : 4;
+            const long long vw = 16 / (long long)es;
+            P->ldm = (m + vw - 1) / vw * vw;
+            REGOT_CUDA(cudaMallocAsync(&P->M, (size_t)n * P->ldm * es, st));
+            REGOT_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&P->a), n * sizeof(double), st));
+            REGOT_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&P->b), m * sizeof(double), st));
+            P->ha.resize(n);
+            P->hb.resize(m);
+            if (d->ab_mem == REGOT_MEM_DEVICE) {
+                d2h(P->ha.data(), d->a, n * sizeof(double), st);
+                d2h(P->hb.data(), d->b, m * sizeof(double), st);
+                sync(st);
+            } else {
+                std::memcpy(P->ha.data(), d->a, n * sizeof(double));
+                std::memcpy(P->hb.data(), d->b, m * sizeof(double));
+            }
+            for (int i = 0; i < n; ++i)
+                require(std::isfinite(P->ha[i]) && P->ha[i] > 0.0,
+                        "a must be finite and positive");
+            for (int j = 0; j < m; ++j)
+                require(std::isfinite(P->hb[j]) && P->hb[j] > 0.0,
+                        "b must be finite and positive");
+            h2d(P->a, P->ha.data(), n * sizeof(double), st);
+            h2d(P->b, P->hb.data(), m * sizeof(double), st);
+
+            const size_t src_es = d->M_dtype == REGOT_F64 ? 8 : 4;
+            const bool same = src_es == es;
+            const cudaMemcpyKind kind =
+                d->M_mem == REGOT_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+            if (same) {
+                if (P->ldm != m)
+                    REGOT_CUDA(cudaMemsetAsync(P->M, 0, (size_t)n * P->ldm * es, st));
+                REGOT_CUDA(cudaMemcpy2DAsync(P->M, P->ldm * es, d->M, d->ldm * src_es, m * es, n,
+                                             kind, st));
+            } else {
+                // Stage the source on the device, then convert row by row.
+                void* stage = nullptr;
+                const void* src = d->M;
+                if (d->M_mem != REGOT_MEM_DEVICE) {
+                    REGOT_CUDA(cudaMallocAsync(&stage, (size_t)n * m * src_es, st));
+                    REGOT_CUDA(cudaMemcpy2DAsync(stage, m * src_es, d->M, d->ldm * src_es,
+                                                 m * src_es, n, kind, st));
+                    src = stage;
+                }
+                const long long lds = d->M_mem == REGOT_MEM_DEVICE ? d->ldm : m;
+                if (src_es == 8)
+                    k_convert<double, float><<<1024, 256, 0, st>>>(
+                        (const double*)src, lds, (float*)P->M, P->ldm, n, m);
+                else
+                    k_convert<float, double><<<1024, 256, 0, st>>>(
+                        (const float*)src, lds, (double*)P->M, P->ldm, n, m);
+                count_launch();
+                REGOT_CHECK_LAUNCH();
+                if (stage) REGOT_CUDA(cudaFreeAsync(stage, st));
+            }
+            sync(st);
+        } catch (...) {
+            if (P->M) cudaFreeAsync(P->M, st);
+            if (P->a) cudaFreeAsync(P->a, st);
+            if (P->b) cudaFreeAsync(P->b, st);
+            delete P;
+            throw;
+        }
+        *out = P;
+    });
+}
+
+static void drop_time_pass_state(regot_dproblem* P);
+
+void regot_problem_destroy(regot_dproblem* P) {
+    if (!P) return;
+    drop_time_pass_state(P);
+    cudaStream_t st = P->ctx ? P->ctx->stream : nullptr;
+    if (P->M) cudaFreeAsync(P->M, st);
+    if (P->a) cudaFreeAsync(P->a, st);
+    if (P->b) cudaFreeAsync(P->b, st);
+    cudaStreamSynchronize(st);
+    delete P;
+}
+
+#define REGOT_SOLVER_ENTRY(NAME, IMPL, DUAL)                                                 \
+    int NAME(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,        \
+             const regot_opts* opts, regot_result* res) {                                    \
+        return guarded(ctx, [&] {                                                            \
+            require(P != nullptr, "problem is NULL");                                        \
+            check_solver_args(P, reg, tol, max_iter, res, DUAL);                             \
+            const regot_opts o = effective_opts(opts);                                       \
+            cudaEvent_t e0, e1;                                                              \
+            REGOT_CUDA(cudaEventCreate(&e0));                                                \
+            REGOT_CUDA(cudaEventCreate(&e1));                                                \
+            REGOT_CUDA(cudaEventRecord(e0, ctx->stream));                                    \
+            IMPL(ctx, P, reg, tol, max_iter, o, res);                                        \
+            REGOT_CUDA(cudaEventRecord(e1, ctx->stream));                                    \
+            REGOT_CUDA(cudaEventSynchronize(e1));                                            \
+            float ms = 0.f;                                                                  \
+            cudaEventElapsedTime(&ms, e0, e1);                                               \
+            res->solve_ms = ms;                                                              \
+            cudaEventDestroy(e0);                                                            \
+            cudaEventDestroy(e1);                                                            \
+        });                                                                                  \
+    }
+
+REGOT_SOLVER_ENTRY(regot_sinkhorn_bcd, sinkhorn_bcd_gpu, P->n + P->m - 1)
+REGOT_SOLVER_ENTRY(regot_sinkhorn_newton, sinkhorn_newton_gpu, P->n + P->m - 1)
+REGOT_SOLVER_ENTRY(regot_sinkhorn_ssns, sinkhorn_ssns_gpu, P->n + P->m - 1)
+REGOT_SOLVER_ENTRY(regot_qrot_lbfgs_dual, qrot_lbfgs_dual_gpu, P->n + P->m)
+REGOT_SOLVER_ENTRY(regot_qrot_assn, qrot_assn_gpu, P->n + P->m)
+
+// ---------------------------------------------------------------- passes --
+
+int regot_erot_optimal_beta(regot_ctx* ctx, regot_dproblem* P, double reg, const double* alpha,
+                            double* beta) {
+    return guarded(ctx, [&] {
+        require(P && alpha && beta, "NULL argument");
+        require(reg > 0.0, "reg must be positive");
+        cudaStream_t st = ctx->stream;
+        ErotOps ops(P, reg, st);
+        DBuf<double> da(P->n, st), db(P->m, st), mx(1, st);
+        h2d(da.get(), alpha, P->n * sizeof(double), st);
+        ops.optimal_beta(da.get(), db.get(), mx.get());
+        d2h(beta, db.get(), P->m * sizeof(double), st);
+        sync(st);
+    });
+}
+
+int regot_erot_optimal_alpha(regot_ctx* ctx, regot_dproblem* P, double reg, const double* beta,
+                             double* alpha) {
+    return guarded(ctx, [&] {
+        require(P && alpha && beta, "NULL argument");
+        require(reg > 0.0, "reg must be positive");
+        cudaStream_t st = ctx->stream;
+        ErotOps ops(P, reg, st);
+        DBuf<double> da(P->n, st), db(P->m, st), mx(1, st);
+        h2d(db.get(), beta, P->m * sizeof(double), st);
+        ops.optimal_alpha(db.get(), da.get(), mx.get());
+        d2h(alpha, da.get(), P->n * sizeof(double), st);
+        sync(st);
+    });
+}
+
+// Upload gamma = (alpha, beta~) into device alpha[n], beta[m] with beta_m = 0.
+static void upload_gamma(const double* gamma, int n, int m, double* d_ab, cudaStream_t st) {
+    std::vector<double> h((size_t)n + m, 0.0);
+    std::memcpy(h.data(), gamma, (size_t)(n + m - 1) * sizeof(double));
+    h2d(d_ab, h.data(), h.size() * sizeof(double), st);
+    sync(st);
+}
+
+int regot_erot_dual_obj_grad(regot_ctx* ctx, regot_dproblem* P, double reg, const double* gamma,
+                             double* obj, double* grad) {
+    return guarded(ctx, [&] {
+        require(P && gamma && obj && grad, "NULL argument");
+        require(reg > 0.0, "reg must be positive");
+        cudaStream_t st = ctx->stream;
+        const int n = P->n, m = P->m;
+        ErotOps ops(P, reg, st);
+        DBuf<double> g(n + m, st), rc(n + m, st), mx(1, st);
+        upload_gamma(gamma, n, m, g.get(), st);
+        ops.row_col_sums(g.get(), g.get() + n, rc.get(), rc.get() + n, mx.get());
+        std::vector<double> h(n + m);
+        d2h(h.data(), rc.get(), (n + m) * sizeof(double), st);
+        sync(st);
+        // sinkhorn_problem_obj.cpp:371-393
+        double tsum = 0.0, ga = 0.0, gb = 0.0;
+        for (int i = 0; i < n; ++i) {
+            tsum += h[i];
+            grad[i] = h[i] - P->ha[i];
+            ga += gamma[i] * P->ha[i];
+        }
+        for (int j = 0; j < m - 1; ++j) {
+            grad[n + j] = h[n + j] - P->hb[j];
+            gb += gamma[n + j] * P->hb[j];
+        }
+        *obj = reg * tsum - ga - gb;
+    });
+}
+
+int regot_erot_hvp(regot_ctx* ctx, regot_dproblem* P, double reg, const double* gamma,
+                   const double* x, double* y) {
+    return guarded(ctx, [&] {
+        require(P && gamma && x && y, "NULL argument");
+        require(reg > 0.0, "reg must be positive");
+        cudaStream_t st = ctx->stream;
+        const int n = P->n, m = P->m;
+        ErotOps ops(P, reg, st);
+        DBuf<double> g(n + m, st), xv(n + m, st), rc(n + m, st), yy(n + m, st), mx(1, st);
+        upload_gamma(gamma, n, m, g.get(), st);
+        upload_gamma(x, n, m, xv.get(), st);
+        ops.row_col_sums(g.get(), g.get() + n, rc.get(), rc.get() + n, mx.get());
+        ops.tmatvec(g.get(), g.get() + n, xv.get(), xv.get() + n, yy.get(), yy.get() + n,
+                    mx.get());
+        std::vector<double> hrc(n + m), hy(n + m);
+        d2h(hrc.data(), rc.get(), (n + m) * sizeof(double), st);
+        d2h(hy.data(), yy.get(), (n + m) * sizeof(double), st);
+        sync(st);
+        for (int i = 0; i < n; ++i) y[i] = (hrc[i] * x[i] + hy[i]) / reg;
+        for (int j = 0; j < m - 1; ++j) y[n + j] = (hrc[n + j] * x[n + j] + hy[n + j]) / reg;
+    });
+}
+
+int regot_erot_plan(regot_ctx* ctx, regot_dproblem* P, double reg, const double* gamma,
+                    double* plan, int plan_mem) {
+    return guarded(ctx, [&] {
+        require(P && gamma && plan, "NULL argument");
+        cudaStream_t st = ctx->stream;
+        const int n = P->n, m = P->m;
+        ErotOps ops(P, reg, st);
+        DBuf<double> g(n + m, st), mx(1, st);
+        upload_gamma(gamma, n, m, g.get(), st);
+        if (plan_mem == REGOT_MEM_DEVICE) {
+            ops.plan(g.get(), g.get() + n, plan, mx.get());
+        } else {
+            DBuf<double> out((size_t)n * m, st);
+            ops.plan(g.get(), g.get() + n, out.get(), mx.get());
+            d2h(plan, out.get(), (size_t)n * m * sizeof(double), st);
+        }
+        sync(st);
+    });
+}
+
+}  // extern "C"
+
+// ------------------------------------------------------------ measurement --
+namespace {
+struct TimePassState {
+    regot_dproblem* P = nullptr;
+    double reg = 0.0;
+    cudaStream_t stream = nullptr;
+    ErotOps* ops = nullptr;
+    DBuf<double> vec, mx;
+};
+TimePassState* g_tp = nullptr;
+}  // namespace
+
+static void drop_time_pass_state(regot_dproblem* P) {
+    if (g_tp && g_tp->P == P) {
+        delete g_tp->ops;
+        delete g_tp;
+        g_tp = nullptr;
+    }
+}
+
+extern "C" int regot_time_pass(regot_ctx* ctx, regot_dproblem* P, int kind, double reg,
+                               int reps) {
+    return guarded(ctx, [&] {
+        require(P != nullptr && reps >= 0, "invalid argument");
+        require(kind >= REGOT_PASS_EROT_ROW && kind <= REGOT_PASS_QROT_GRAD, "unknown pass kind");
+        cudaStream_t st = ctx->stream;
+        // Workspace kept between calls for the same problem (the timed region
+        // should contain the passes only).
+        if (!g_tp || g_tp->P != P || g_tp->reg != reg || g_tp->stream != st) {
+            if (g_tp) {
+                delete g_tp->ops;
+                delete g_tp;
+            }
+            g_tp = new TimePassState();
+            g_tp->P = P;
+            g_tp->reg = reg;
+            g_tp->stream = st;
+            g_tp->ops = new ErotOps(P, reg, st);
+            g_tp->vec.alloc(2 * ((size_t)P->n + P->m), st);
+            g_tp->vec.zero();
+            g_tp->mx.alloc(1, st);
+            g_tp->mx.zero();
+            sync(st);
+        }
+        ErotOps& ops = *g_tp->ops;
+        const int n = P->n;
+        PassParams p = ops.base_params();
+        double* v = g_tp->vec.get();
+        p.ra = v;
+        p.cb = v + n;
+        p.rx = v + n + P->m;
+        p.cx = v + 2 * n + P->m;
+        p.grid = g_tp->mx.get();
+        int op = OP_E_ROW;
+        if (kind == REGOT_PASS_EROT_COL) op = OP_E_COL;
+        if (kind == REGOT_PASS_EROT_GRAD) op = OP_E_ROWCOL;
+        if (kind == REGOT_PASS_EROT_HVP) op = OP_E_HVP;
+        if (kind == REGOT_PASS_QROT_GRAD) op = OP_Q_GRAD;
+        if (P->prec == REGOT_PREC_MIXED) {
+            // split once, then time the dense kernel alone
+            ops.pass(op, p);
+            sync(st);
+            for (int r = 0; r < reps; ++r) ops.pass_presplit(op, p);
+        } else {
+            for (int r = 0; r < reps; ++r) ops.pass(op, p);
+        }
+    });
+}

@@ -1,0 +1,142 @@
+// Device-side helpers shared by the solver translation units: grid-wide
+// deterministic reductions (per-block partials summed in block order by the
+// last block to finish), the device clock, and stream-ordered buffers.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <utility>
+
+#include "internal.h"
+
+namespace regot {
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Running maximum of |v| for the hi/lo split grid (positive doubles order
+// like their bit patterns, so an integer atomicMax is exact).
+__device__ __forceinline__ void atomic_max_abs(double* target, double v) {
+    const double a = fabs(v);
+    if (!(a == a)) return;
+    atomicMax(reinterpret_cast<unsigned long long*>(target),
+              (unsigned long long)__double_as_longlong(a));
+}
+
+// Warp-aggregated version: one atomic per warp (all lanes must call it).
+__device__ __forceinline__ void warp_atomic_max_abs(double* target, double v) {
+    double a = fabs(v);
+    if (!(a == a) || isinf(a)) a = 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a = fmax(a, __shfl_xor_sync(0xffffffffu, a, o));
+    if ((threadIdx.x & 31) == 0 && a > 0.0)
+        atomicMax(reinterpret_cast<unsigned long long*>(target),
+                  (unsigned long long)__double_as_longlong(a));
+}
+
+// Grid-wide sum of K values per thread. Returns true in thread 0 of the last
+// block to finish, with the totals in out[] (summed in block order).
+template <int K>
+__device__ bool grid_reduce(const double (&vals)[K], double* block_parts, unsigned* counter,
+                            double (&out)[K]) {
+    __shared__ double s_red[K][32];
+    __shared__ bool s_last;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const double v = warp_sum_d(vals[k]);
+        if (lane == 0) s_red[k][warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+            double s = 0.0;
+            for (int w = 0; w < nw; ++w) s += s_red[k][w];
+            block_parts[(size_t)blockIdx.x * K + k] = s;
+        }
+        __threadfence();
+        const unsigned ticket = atomicAdd(counter, 1u);
+        s_last = (ticket == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (!s_last || threadIdx.x != 0) return false;
+    __threadfence();
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        double s = 0.0;
+        for (unsigned b = 0; b < gridDim.x; ++b) s += __ldcg(&block_parts[(size_t)b * K + k]);
+        out[k] = s;
+    }
+    *counter = 0u;
+    return true;
+}
+
+// Stream-ordered device buffer (cudaMallocAsync / cudaFreeAsync).
+template <typename T>
+class DBuf {
+public:
+    DBuf() = default;
+    DBuf(size_t count, cudaStream_t st) { alloc(count, st); }
+    ~DBuf() { release(); }
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    DBuf(DBuf&& o) noexcept { swap(o); }
+    DBuf& operator=(DBuf&& o) noexcept {
+        if (this != &o) {
+            release();
+            swap(o);
+        }
+        return *this;
+    }
+    void alloc(size_t count, cudaStream_t st) {
+        release();
+        st_ = st;
+        count_ = count;
+        if (count) REGOT_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&p_), count * sizeof(T), st));
+    }
+    void zero() {
+        if (count_) REGOT_CUDA(cudaMemsetAsync(p_, 0, count_ * sizeof(T), st_));
+    }
+    T* get() const { return p_; }
+    size_t size() const { return count_; }
+    void release() {
+        if (p_) cudaFreeAsync(p_, st_);
+        p_ = nullptr;
+        count_ = 0;
+    }
+
+private:
+    void swap(DBuf& o) {
+        std::swap(p_, o.p_);
+        std::swap(count_, o.count_);
+        std::swap(st_, o.st_);
+    }
+    T* p_ = nullptr;
+    size_t count_ = 0;
+    cudaStream_t st_ = nullptr;
+};
+
+inline void h2d(void* dst, const void* src, size_t bytes, cudaStream_t st) {
+    if (bytes) REGOT_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st));
+}
+inline void d2h(void* dst, const void* src, size_t bytes, cudaStream_t st) {
+    if (bytes) REGOT_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, st));
+}
+inline void d2d(void* dst, const void* src, size_t bytes, cudaStream_t st) {
+    if (bytes) REGOT_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, st));
+}
+inline void sync(cudaStream_t st) { REGOT_CUDA(cudaStreamSynchronize(st)); }
+
+}  // namespace regot

@@ -1,0 +1,383 @@
+// sinkhorn_bcd on the GPU (reference: src/sinkhorn_bcd.cpp:14-124).
+//
+// One BCD iteration is two streamed passes over M:
+//   K1 (row pass, anchor alpha_k):  S_i = sum_j exp((alpha_k,i + beta_k,j - M_ij)/reg)
+//        S_i is the row marginal of iterate k, so the gradient, objective and
+//        marginal error of iterate k come out of this pass, and
+//        alpha_{k+1,i} = alpha_k,i + reg (log a_i - log S_i).
+//   K2 (column pass, anchor beta_k): S_j = sum_i exp((alpha_{k+1,i} + beta_k,j - M_ij)/reg)
+//        beta_{k+1,j} = beta_k,j + reg (log b_j - log S_j).
+// After K2 the column marginals are exact, so the beta part of the gradient
+// of the next iterate is zero up to rounding, as in the reference
+// (optimal_beta runs last in each sweep). The anchors keep every exponent of
+// the passes <= 0 (T <= a_i or b_j <= 1), which makes the FP32 exp safe; a
+// row or column sum that still leaves the safe range is redone with an
+// explicit max anchor (robust path) without changing the result.
+//
+// The iteration is captured once in a CUDA graph and replayed in batches;
+// every kernel returns immediately once the device-side `done` flag is set,
+// so the host only synchronises once per batch.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "device_util.cuh"
+#include "erot_ops.cuh"
+#include "solvers.h"
+
+namespace regot {
+
+namespace {
+
+// Finalize kernels merge FP64 partials: small blocks spread them over all SMs
+// (FP64 throughput per SM is low on this part).
+constexpr int kFinThreads = 64;
+
+struct BcdState {
+    int done;
+    int bad;       // 1: row sums out of range, 2: column sums out of range
+    int iter;      // index of the iterate whose gradient the next K1 evaluates
+    int niter;
+    int hist_len;
+    int max_iter;
+    unsigned counter;
+    int pad;
+    double tol;
+    double sum_bb;     // sum_{j<m-1} b_j beta_j of the current beta
+    double beta_last;  // beta_{m-1}
+    double gb2_once;   // squared beta-part of the gradient of iterate 0 (x0 given)
+    double maxabs;     // running max |alpha|, |beta| (hi/lo split grid)
+    double last_gnorm; // marginal error of the last recorded iterate
+    unsigned long long t0;
+};
+
+template <bool MIXED>
+__device__ __forceinline__ bool sum_ok(double s) {
+    return isfinite(s) && s > (MIXED ? 1e-30 : 1e-290);
+}
+
+// Row finalize of K1: gradient/objective of iterate k, history, stopping
+// test, alpha_{k+1}. `anchor` is the row vector the pass used (alpha itself
+// on the fast path, -max_j(beta_j - M_ij) on the robust path).
+template <typename Acc, bool MIXED>
+__global__ void k_bcd_row(const Acc* rp, int nslabs, int n, const double* anchor,
+                          const double* alpha, const double* a, const double* loga, double reg,
+                          double sum_a, double sum_bt, double* alpha_next, double* hobj,
+                          double* hmar, double* htime, double* parts, BcdState* st,
+                          int robust) {
+    if (st->done) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[3] = {0.0, 0.0, 0.0};
+    double vmax = 0.0;
+    if (i < n) {
+        double S = 0.0;
+        for (int k = 0; k < nslabs; ++k) S += (double)rp[(size_t)k * n + i];
+        const double al = alpha[i];
+        const double an = anchor[i];
+        if (!robust && !sum_ok<MIXED>(S)) atomicOr(&st->bad, 1);
+        const double r = robust ? exp(log(S) + (al - an) / reg) : S;
+        const double g = r - a[i];
+        v[0] = g * g;
+        v[1] = r;
+        v[2] = a[i] * al;
+        const double an_next = an + reg * (loga[i] - log(S));
+        alpha_next[i] = an_next;
+        vmax = an_next;
+    }
+    warp_atomic_max_abs(&st->maxabs, vmax);
+    __threadfence();
+    double out[3];
+    if (grid_reduce<3>(v, parts, &st->counter, out)) {
+        if (atomicAdd(&st->bad, 0)) {
+            st->done = 1;
+            return;
+        }
+        const int k = st->iter;
+        const double gnorm = sqrt(out[0] + st->gb2_once);
+        st->gb2_once = 0.0;
+        const double bl = st->beta_last;
+        const double obj = reg * out[1] - out[2] - bl * sum_a - st->sum_bb + bl * sum_bt;
+        hobj[k] = obj;
+        hmar[k] = gnorm;
+        st->last_gnorm = gnorm;
+        htime[k] = (double)(globaltimer_ns() - st->t0) * 1e-6;
+        st->hist_len = k + 1;
+        if (gnorm < st->tol || k >= st->max_iter) {
+            st->done = 1;
+            st->niter = k;
+        }
+    }
+}
+
+// Column finalize of K2: beta_{k+1} into beta_next.
+template <typename Acc, bool MIXED>
+__global__ void k_bcd_col(const Acc* cp, int nrb, int m, const double* anchor,
+                          const double* logb, const double* b, double reg, double* beta_next,
+                          double* parts, BcdState* st, int robust) {
+    if (st->done) return;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[1] = {0.0};
+    double vmax = 0.0;
+    if (j < m) {
+        double S = 0.0;
+        for (int k = 0; k < nrb; ++k) S += (double)cp[(size_t)k * m + j];
+        if (!robust && !sum_ok<MIXED>(S)) atomicOr(&st->bad, 2);
+        const double bn = anchor[j] + reg * (logb[j] - log(S));
+        beta_next[j] = bn;
+        if (j < m - 1) v[0] = b[j] * bn;
+        vmax = bn;
+    }
+    warp_atomic_max_abs(&st->maxabs, vmax);
+    __threadfence();
+    double out[1];
+    if (grid_reduce<1>(v, parts, &st->counter, out)) {
+        if (atomicAdd(&st->bad, 0)) {
+            st->done = 1;
+            return;
+        }
+        st->sum_bb = out[0];
+        st->beta_last = beta_next[m - 1];
+    }
+}
+
+// Commit the sweep: alpha <- alpha_next, beta <- beta_next, iter++.
+__global__ void k_bcd_commit(int n, int m, double* alpha, const double* alpha_next, double* beta,
+                             const double* beta_next, BcdState* st) {
+    if (st->done) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) alpha[t] = alpha_next[t];
+    if (t < m) beta[t] = beta_next[t];
+    if (t == 0) st->iter += 1;
+}
+
+__global__ void k_bcd_start(BcdState* st) { st->t0 = globaltimer_ns(); }
+
+__global__ void k_gauge(int n, int m, const double* alpha, const double* beta, double* ga,
+                        double* gb) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const double bl = beta[m - 1];
+    if (t < n) ga[t] = alpha[t] + bl;
+    if (t < m) gb[t] = (t < m - 1) ? beta[t] - bl : 0.0;
+}
+
+__global__ void k_colgrad_sq(const double* c, const double* b, int m, double* out) {
+    double v = 0.0;
+    for (int j = threadIdx.x; j < m - 1; j += blockDim.x) {
+        const double g = c[j] - b[j];
+        v += g * g;
+    }
+    __shared__ double s[32];
+    v = warp_sum_d(v);
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s[w];
+        *out = t;
+    }
+}
+
+__global__ void k_dot_bt(const double* b, const double* beta, int m, BcdState* st) {
+    double v = 0.0;
+    for (int j = threadIdx.x; j < m - 1; j += blockDim.x) v += b[j] * beta[j];
+    __shared__ double s[32];
+    v = warp_sum_d(v);
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s[w];
+        st->sum_bb = t;
+        st->beta_last = beta[m - 1];
+    }
+}
+
+}  // namespace
+
+void sinkhorn_bcd_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
+                      const regot_opts& o, regot_result* res) {
+    cudaStream_t st = ctx->stream;
+    const int n = P->n, m = P->m;
+    const bool mixed = P->prec == REGOT_PREC_MIXED;
+    ErotOps ops(P, reg, st);
+    const PassShape sh = ops.buf().shape;
+    const int hist_cap = max_iter + 2;
+
+    DBuf<double> alpha(n, st), alpha_next(n, st), beta(m, st), beta_next(m, st), anchor(
+        std::max(n, m), st);
+    DBuf<double> hist(3 * (size_t)hist_cap, st), parts(3 * (size_t)cdiv(std::max(n, m), kFinThreads), st);
+    DBuf<double> scratch(std::max(n, m) + 8, st), rsum(n, st), csum(m, st);
+    DBuf<BcdState> dst(1, st);
+    double* hobj = hist.get();
+    double* hmar = hobj + hist_cap;
+    double* htime = hmar + hist_cap;
+
+    BcdState h0{};
+    h0.max_iter = max_iter;
+    h0.tol = tol;
+    h2d(dst.get(), &h0, sizeof(h0), st);
+    BcdState* S = dst.get();
+    double* mx = scratch.get();
+
+    // Initial value (sinkhorn_bcd.cpp:38-47).
+    const bool has_x0 = o.x0 && o.x0_len == n + m - 1;
+    if (has_x0) {
+        std::vector<double> hb(m, 0.0);
+        std::copy(o.x0 + n, o.x0 + n + m - 1, hb.begin());
+        h2d(alpha.get(), o.x0, n * sizeof(double), st);
+        h2d(beta.get(), hb.data(), m * sizeof(double), st);
+    } else {
+        alpha.zero();
+        ops.optimal_beta(alpha.get(), beta.get(), mx);
+    }
+    // Timer starts after the initial value (sinkhorn_bcd.cpp:49-51).
+    k_bcd_start<<<1, 1, 0, st>>>(S);
+    k_dot_bt<<<1, 256, 0, st>>>(P->b, beta.get(), m, S);
+    count_launch(2);
+    if (has_x0) {
+        // With a user x0 the beta part of the first gradient is not zero.
+        ops.row_col_sums(alpha.get(), beta.get(), rsum.get(), csum.get(), mx);
+        k_colgrad_sq<<<1, 256, 0, st>>>(csum.get(), P->b, m, &S->gb2_once);
+        count_launch();
+    }
+    ops.maxabs(alpha.get(), n, beta.get(), m, &S->maxabs);
+    REGOT_CHECK_LAUNCH();
+
+    PassParams p1 = ops.base_params();
+    p1.grid = &S->maxabs;
+    p1.done = &S->done;
+    PassParams p2 = p1;
+    // K1: anchor alpha_k, column dual beta_k
+    p1.ra = alpha.get();
+    p1.cb = beta.get();
+    // K2: row dual alpha_{k+1}, anchor beta_k
+    p2.ra = alpha_next.get();
+    p2.cb = beta.get();
+    const int gn = cdiv(n, kFinThreads), gm = cdiv(m, kFinThreads), gnm = cdiv(std::max(n, m), 256);
+
+    auto launch_row = [&](const double* anc, int robust) {
+        if (mixed)
+            k_bcd_row<float, true><<<gn, kFinThreads, 0, st>>>(
+                (const float*)ops.buf().rowpart.get(), sh.nslabs, n, anc, alpha.get(), P->a,
+                ops.loga(), reg, ops.sum_a(), ops.sum_bt(), alpha_next.get(), hobj, hmar, htime,
+                parts.get(), S, robust);
+        else
+            k_bcd_row<double, false><<<gn, kFinThreads, 0, st>>>(
+                (const double*)ops.buf().rowpart.get(), sh.nslabs, n, anc, alpha.get(), P->a,
+                ops.loga(), reg, ops.sum_a(), ops.sum_bt(), alpha_next.get(), hobj, hmar, htime,
+                parts.get(), S, robust);
+        count_launch();
+    };
+    auto launch_col = [&](const double* anc, int robust) {
+        if (mixed)
+            k_bcd_col<float, true><<<gm, kFinThreads, 0, st>>>(
+                (const float*)ops.buf().colpart.get(), sh.nrb, m, anc, ops.logb(), P->b, reg,
+                beta_next.get(), parts.get(), S, robust);
+        else
+            k_bcd_col<double, false><<<gm, kFinThreads, 0, st>>>(
+                (const double*)ops.buf().colpart.get(), sh.nrb, m, anc, ops.logb(), P->b, reg,
+                beta_next.get(), parts.get(), S, robust);
+        count_launch();
+    };
+    auto launch_commit = [&]() {
+        k_bcd_commit<<<gnm, 256, 0, st>>>(n, m, alpha.get(), alpha_next.get(), beta.get(),
+                                          beta_next.get(), S);
+        count_launch();
+    };
+    auto sweep = [&]() {
+        ops.pass(OP_E_ROW, p1);
+        launch_row(alpha.get(), 0);
+        ops.pass(OP_E_COL, p2);
+        launch_col(beta.get(), 0);
+        launch_commit();
+    };
+
+    // Capture one sweep as a graph; replay it in batches.
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    long long* saved_counter = g_launch_counter;
+    long long graph_kernels = 0;
+    g_launch_counter = &graph_kernels;
+    REGOT_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    sweep();
+    REGOT_CUDA(cudaStreamEndCapture(st, &graph));
+    g_launch_counter = saved_counter;
+    REGOT_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+
+    BcdState hs{};
+    int batch = 4;
+    long long passes = 0;
+    long long launched = 0;
+    int prev_iter = -1;
+    double prev_g = 0.0;
+    for (;;) {
+        for (int q = 0; q < batch; ++q) REGOT_CUDA(cudaGraphLaunch(exec, st));
+        launched += batch;
+        count_launch(graph_kernels * batch);
+        d2h(&hs, S, sizeof(hs), st);
+        sync(st);
+        if (hs.bad) {
+            // Robust redo of the half-sweep that left the safe range.
+            const int which = hs.bad;
+            const int zero = 0;
+            h2d(&S->bad, &zero, sizeof(int), st);
+            h2d(&S->done, &zero, sizeof(int), st);
+            PassParams pr = ops.base_params();
+            pr.grid = &S->maxabs;
+            if (which & 1) {
+                // alpha_{k+1} with an explicit max anchor, then the row sums of
+                // iterate k measured against it.
+                ops.optimal_alpha(beta.get(), anchor.get(), mx);
+                ops.maxabs(anchor.get(), n, beta.get(), m, &S->maxabs);
+                pr.ra = anchor.get();
+                pr.cb = beta.get();
+                ops.pass(OP_E_ROW, pr);
+                launch_row(anchor.get(), 1);
+                ops.maxabs(alpha_next.get(), n, beta.get(), m, &S->maxabs);
+                ops.pass(OP_E_COL, p2);
+                launch_col(beta.get(), 0);
+                launch_commit();
+            } else {
+                // beta_{k+1} with an explicit max anchor.
+                ops.optimal_beta(alpha_next.get(), anchor.get(), mx);
+                ops.maxabs(alpha_next.get(), n, anchor.get(), m, &S->maxabs);
+                pr.ra = alpha_next.get();
+                pr.cb = anchor.get();
+                ops.pass(OP_E_COL, pr);
+                launch_col(anchor.get(), 1);
+                launch_commit();
+            }
+            REGOT_CHECK_LAUNCH();
+            d2h(&hs, S, sizeof(hs), st);
+            sync(st);
+            if (hs.bad) throw Error(REGOT_ERR_NONFINITE, "non-finite row or column sums in BCD");
+        }
+        if (hs.done) break;
+        if (launched > 2LL * max_iter + 64)
+            throw Error(REGOT_ERR_NUMERIC, "BCD did not terminate");
+        // Size the next batch from the observed linear convergence rate, so
+        // that few sweeps are launched past convergence.
+        const int k = hs.hist_len - 1;
+        int next = std::min(batch * 2, 64);
+        if (prev_iter >= 0 && k > prev_iter && hs.last_gnorm > 0.0 && prev_g > hs.last_gnorm) {
+            const double rate = std::log(prev_g / hs.last_gnorm) / (k - prev_iter);
+            const double need = std::log(hs.last_gnorm / std::max(tol, 1e-300)) / rate;
+            if (std::isfinite(need)) next = (int)std::ceil(need) + 1;
+        }
+        prev_iter = k;
+        prev_g = hs.last_gnorm;
+        batch = std::max(1, std::min(next, std::min(64, max_iter + 1 - k)));
+    }
+    cudaGraphExecDestroy(exec);
+    cudaGraphDestroy(graph);
+    passes = 2LL * hs.hist_len;
+
+    // Results: gauge-fixed dual, plan, histories.
+    DBuf<double> gamma(n + m, st);
+    k_gauge<<<gnm, 256, 0, st>>>(n, m, alpha.get(), beta.get(), gamma.get(), gamma.get() + n);
+    count_launch();
+    finish_erot_result(ops, gamma.get(), hobj, hmar, htime, nullptr, hs.hist_len, hist_cap,
+                       hs.niter, passes, o, res);
+}
+
+}  // namespace regot

@@ -1,0 +1,87 @@
+// EROT building blocks on top of the dense passes: robust log-sum-exp
+// updates (optimal_alpha / optimal_beta), the fused objective/gradient,
+// the Hessian-vector product and the plan, plus the small vector kernels
+// that merge pass partials in FP64.
+#pragma once
+
+#include "device_util.cuh"
+#include "internal.h"
+
+namespace regot {
+
+// Partial-sum buffers of one problem shape (sized for the widest pass).
+struct PassBuffers {
+    PassShape shape{};
+    bool mixed = true;
+    DBuf<char> rowpart, colpart;
+    DBuf<double> totpart;
+    void init(int n, int m, bool mixed_, int max_nr, int max_nc, int max_nt, cudaStream_t st) {
+        mixed = mixed_;
+        shape = mixed ? pass_shape<float>(n, m) : pass_shape<double>(n, m);
+        // column partials of the FP64 root-finding pass are FP64 in both modes
+        const size_t acc = 8;
+        rowpart.alloc((size_t)max_nr * shape.nslabs * n * acc, st);
+        colpart.alloc((size_t)max_nc * shape.nrb * m * acc, st);
+        totpart.alloc((size_t)max_nt * shape.nblocks, st);
+    }
+};
+
+// Engine bound to one device problem and one regularisation value.
+class ErotOps {
+public:
+    ErotOps(regot_dproblem* P, double reg, cudaStream_t st);
+
+    int n() const { return n_; }
+    int m() const { return m_; }
+    bool mixed() const { return mixed_; }
+    cudaStream_t stream() const { return st_; }
+    const double* a() const { return P_->a; }
+    const double* b() const { return P_->b; }
+    const double* loga() const { return loga_.get(); }
+    const double* logb() const { return logb_.get(); }
+    double sum_a() const { return sum_a_; }
+    double sum_bt() const { return sum_bt_; }
+    double reg() const { return reg_; }
+    PassBuffers& buf() { return buf_; }
+
+    // Dense pass with this problem's M, reg and partial buffers.
+    void pass(int op, PassParams p);
+    // Dense pass reusing the FP32 split of the previous pass (mixed mode).
+    void pass_presplit(int op, PassParams p);
+    PassParams base_params() const;
+
+    // Maximum of |x| over up to two device vectors, into *out (device).
+    void maxabs(const double* x, int nx, const double* y, int ny, double* out);
+
+    // beta = optimal_beta(alpha) (robust: column max anchor, then sums).
+    void optimal_beta(const double* alpha, double* beta, double* maxabs_scratch);
+    // alpha = optimal_alpha(beta).
+    void optimal_alpha(const double* beta, double* alpha, double* maxabs_scratch);
+    // Row sums r[n] and column sums c[m] of T(alpha, beta) (beta full length).
+    void row_col_sums(const double* alpha, const double* beta, double* r, double* c,
+                      double* maxabs_scratch);
+    // y_r = T x_c (rows), y_c = T' x_r (cols), for T(alpha, beta).
+    void tmatvec(const double* alpha, const double* beta, const double* xr, const double* xc,
+                 double* yr, double* yc, double* maxabs_scratch);
+    // plan = T(alpha, beta) (device output, row-major, stride m).
+    void plan(const double* alpha, const double* beta, double* out, double* maxabs_scratch);
+
+    // Merge helpers (FP64 outputs).
+    void merge_rows(int nr, double* out);  // out[r*n + i]
+    void merge_cols(int nc, double* out);  // out[c*m + j]
+
+private:
+    regot_dproblem* P_;
+    cudaStream_t st_;
+    int n_, m_;
+    bool mixed_;
+    double reg_;
+    DBuf<double> loga_, logb_;
+    double sum_a_ = 0, sum_bt_ = 0;
+    PassBuffers buf_;
+    DBuf<double> anchor_;
+    DBuf<float4> rsplit_, csplit_;
+    DBuf<float> cdsplit_;
+};
+
+}  // namespace regot

@@ -1,0 +1,158 @@
+// Internal declarations shared by the CUDA translation units of regot_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "regot_gb300.h"
+
+namespace regot {
+
+// ---------------------------------------------------------------- errors --
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& msg) : std::runtime_error(msg), code(c) {}
+};
+
+#define REGOT_CUDA(call)                                                                 \
+    do {                                                                                 \
+        cudaError_t e_ = (call);                                                         \
+        if (e_ != cudaSuccess)                                                           \
+            throw ::regot::Error(REGOT_ERR_CUDA, std::string(#call) + ": " +             \
+                                                     cudaGetErrorString(e_));            \
+    } while (0)
+
+#define REGOT_CHECK_LAUNCH() REGOT_CUDA(cudaGetLastError())
+
+inline void require(bool ok, const std::string& msg, int code = REGOT_ERR_INVALID_ARG) {
+    if (!ok) throw Error(code, msg);
+}
+
+// ------------------------------------------------------------- geometry --
+// Dense passes tile M (row-major, row stride ldm) into CTAs of RB rows x
+// CW columns. A CTA has 8 warps; each warp streams RB/8 consecutive rows and
+// each lane owns two 16-byte vectors per row (8 FP32 or 4 FP64 columns).
+constexpr int kThreads = 256;
+constexpr int kWarps = kThreads / 32;
+constexpr int kRB = 64;  // rows per CTA
+
+template <typename TM> struct Geo;
+template <> struct Geo<float> {
+    static constexpr int VW = 4;
+    static constexpr int LC = 8;
+    static constexpr int CW = 256;
+};
+template <> struct Geo<double> {
+    static constexpr int VW = 2;
+    static constexpr int LC = 4;
+    static constexpr int CW = 128;
+};
+
+inline int cdiv(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+// Dense pass operations (see passes.cu for the element formulas).
+enum PassOp : int {
+    OP_E_ROW = 0,     // row sums of T
+    OP_E_COL,         // column sums of T
+    OP_E_ROWCOL,      // row and column sums of T
+    OP_E_HVP,         // rows: sum_j T cx_j ; cols: sum_i T rx_i
+    OP_E_LS,          // totals_k: sum T expm1(s_k (rd_i + cd_j)/reg)
+    OP_E_PLAN,        // write T
+    OP_E_ROWMAX,      // rows: max_j (cb_j - M_ij)
+    OP_E_COLMAX,      // cols: max_i (ra_i - M_ij)
+    OP_Q_GRAD,        // rows/cols: sum D ; total: sum D^2
+    OP_Q_GRADMASK,    // + bitmask of C > 0, row/col counts
+    OP_Q_OBJ,         // total: sum D^2
+    OP_Q_P1,          // rows: sum D
+    OP_Q_P2,          // cols: sum D rx_i
+    OP_Q_P3,          // rows: sum D cx, sum D cx cx2, sum M cx2 ; totals
+    OP_Q_PLAN,        // write D / reg
+    OP_Q_COLROOT,     // cols: count and sum of y = M - ra below cb (FP64)
+    OP_COUNT
+};
+
+// Parameters of one dense pass. Row vectors have n entries, column vectors
+// m entries; all FP64 on the device.
+struct PassParams {
+    const void* M = nullptr;
+    long long ldm = 0;
+    int n = 0, m = 0;
+    const double* ra = nullptr;  // row dual (alpha or anchor)
+    const double* cb = nullptr;  // column dual (beta, full length m)
+    const double* rx = nullptr;  // extra row weights
+    const double* cx = nullptr;  // extra column weights
+    const double* cx2 = nullptr;
+    const double* rd = nullptr;  // line-search direction (rows)
+    const double* cd = nullptr;  // line-search direction (cols)
+    double steps[4] = {0, 0, 0, 0};
+    int nsteps = 0;
+    double reg = 1.0;
+    const double* grid = nullptr;  // device scalar: bound on |ra|, |cb| (mixed hi/lo grid)
+    // Mixed mode: FP32 copies prepared once per pass by the split kernel.
+    const float4* rsplit = nullptr;  // per row: (hi, lo, rx, rd)
+    const float4* csplit = nullptr;  // per column: (hi, lo, cx, cx2)
+    const float* cdsplit = nullptr;  // per column: cd
+    // Filled by launch_pass from reg.
+    float kexp_f = 0.f, inv_reg_f = 0.f;
+    double kexp_d = 0.0, inv_reg_d = 0.0;
+    void* rowpart = nullptr;       // [NR][nslabs][n] (Acc)
+    void* colpart = nullptr;       // [NC][nrb][m]   (Acc)
+    double* totpart = nullptr;     // [NT][nblocks]
+    uint32_t* bitmask = nullptr;   // [n][nslabs][LC]
+    double* out = nullptr;         // plan output, row-major, stride m
+    const int* done = nullptr;     // early-exit flag (device)
+};
+
+struct PassShape {
+    int nslabs, nrb, nblocks;
+};
+
+template <typename TM>
+inline PassShape pass_shape(int n, int m) {
+    PassShape s;
+    s.nslabs = cdiv(m, Geo<TM>::CW);
+    s.nrb = cdiv(n, kRB);
+    s.nblocks = s.nslabs * s.nrb;
+    return s;
+}
+
+// Launch a dense pass (passes.cu).
+template <typename TM>
+void launch_pass(int op, const PassParams& p, cudaStream_t st);
+
+// Mixed mode: fill p.rsplit / p.csplit / p.cdsplit (buffers of n, m, m
+// entries) from the FP64 vectors of p, on the hi/lo grid of *p.grid.
+void launch_split(const PassParams& p, float4* rs, float4* cs, float* cds, cudaStream_t st);
+
+// Count of kernels launched (for gpu_launches accounting).
+extern thread_local long long* g_launch_counter;
+inline void count_launch(int k = 1) {
+    if (g_launch_counter) *g_launch_counter += k;
+}
+
+}  // namespace regot
+
+// ---------------------------------------------------------- C-ABI objects --
+struct regot_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;
+    std::string last_error;
+    long long launches = 0;
+};
+
+struct regot_dproblem {
+    regot_ctx* ctx = nullptr;
+    int n = 0, m = 0;
+    long long ldm = 0;
+    int prec = REGOT_PREC_MIXED;  // storage: FP64 or FP32
+    void* M = nullptr;            // device, n x ldm
+    double* a = nullptr;          // device
+    double* b = nullptr;          // device
+    std::vector<double> ha, hb;   // host copies
+};

@@ -1,0 +1,29 @@
+// Solver entry points behind the C ABI (capi.cu).
+#pragma once
+
+#include "internal.h"
+
+namespace regot {
+
+class ErotOps;
+
+void sinkhorn_bcd_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
+                      const regot_opts& o, regot_result* res);
+void sinkhorn_newton_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
+                         const regot_opts& o, regot_result* res);
+void sinkhorn_ssns_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
+                       const regot_opts& o, regot_result* res);
+void qrot_lbfgs_dual_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
+                         const regot_opts& o, regot_result* res);
+void qrot_assn_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
+                   const regot_opts& o, regot_result* res);
+
+// Copy an EROT solve out: gamma = (alpha, beta~) with beta_m = 0 held on the
+// device as n + m doubles (last one 0); device histories of length hist_len
+// (each array hist_cap apart is not assumed: separate pointers).
+void finish_erot_result(ErotOps& ops, const double* d_gamma, const double* hobj,
+                        const double* hmar, const double* htime, const double* hdens,
+                        int hist_len, int hist_cap, int niter, long long passes,
+                        const regot_opts& o, regot_result* res);
+
+}  // namespace regot

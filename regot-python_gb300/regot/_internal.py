@@ -1,0 +1,352 @@
+"""GPU mirror of the reference's ``regot._internal`` module.
+
+Same names, positional/keyword arguments and defaults as the pybind11
+bindings of src/solvers.cpp:463-528:
+
+    sinkhorn_bcd / sinkhorn_newton / sinkhorn_ssns
+    qrot_lbfgs_dual / qrot_assn
+        (M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs)
+
+and the same result classes (``sinkhorn_result`` with niter, dual, plan,
+obj_vals, mar_errs, run_times, densities; ``qrot_result`` with niter, dual,
+plan, obj_vals, prim_vals, mar_errs, run_times; solvers.cpp:531-564).
+
+Reference kwargs: ``method``, ``mu0``, ``shift``, ``density`` (EROT) and
+``method``, ``shift`` (QROT), with the reference defaults; unknown kwargs are
+ignored as in the reference. Additional kwargs of this implementation:
+
+    precision  "fp64" (M stored and processed in FP64) or "mixed" (M in FP32,
+               FP64 duals); default "fp64" for float64 M, "mixed" for float32 M
+    x0         initial dual vector (n+m-1 for EROT, n+m for QROT)
+    device     CUDA device index (default 0)
+    plan       False to skip computing the plan (default True)
+    prim_vals  QROT: False to skip the per-iteration primal value
+    cg_tol     Newton-CG relative residual target
+
+M may be a NumPy array (C or Fortran order, float64 or float32) or a CUDA
+torch tensor (used in place, no host round trip). The solve runs on the GPU;
+there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+
+__all__ = [
+    "sinkhorn_bcd", "sinkhorn_newton", "sinkhorn_ssns", "qrot_lbfgs_dual", "qrot_assn",
+    "sinkhorn_result", "qrot_result", "Problem",
+]
+
+
+class sinkhorn_result:
+    """Result of an EROT solver (src/sinkhorn_result.h:13-30)."""
+
+    def __init__(self):
+        self.niter = 0
+        self.dual = np.zeros(0)
+        self.plan = np.zeros((0, 0))
+        self.obj_vals = []
+        self.mar_errs = []
+        self.run_times = []
+        self.densities = []
+
+    def __repr__(self):
+        return f"<sinkhorn_result niter={self.niter}>"
+
+
+class qrot_result:
+    """Result of a QROT solver (src/qrot_result.h:13-30)."""
+
+    def __init__(self):
+        self.niter = 0
+        self.dual = np.zeros(0)
+        self.plan = np.zeros((0, 0))
+        self.obj_vals = []
+        self.prim_vals = []
+        self.mar_errs = []
+        self.run_times = []
+
+    def __repr__(self):
+        return f"<qrot_result niter={self.niter}>"
+
+
+def _is_torch_cuda(x) -> bool:
+    t = type(x)
+    return t.__module__.startswith("torch") and getattr(x, "is_cuda", False)
+
+
+def _precision_code(precision, dtype) -> int:
+    if precision is None:
+        return L.REGOT_PREC_FP64 if dtype == np.float64 else L.REGOT_PREC_MIXED
+    p = str(precision).lower()
+    if p in ("fp64", "float64", "double", "plain"):
+        return L.REGOT_PREC_FP64
+    if p in ("mixed", "fp32", "float32"):
+        return L.REGOT_PREC_MIXED
+    raise ValueError(f"unknown precision {precision!r}; use 'fp64' or 'mixed'")
+
+
+class Problem:
+    """A cost matrix and marginals resident on one GPU (regot_dproblem).
+
+    Reusing a Problem for several solves uploads M once.
+    """
+
+    def __init__(self, M, a, b, precision=None, device: int = 0):
+        self.ctx = L.context(device)
+        lib = L.load()
+        self._keep = []
+        a = np.ascontiguousarray(np.asarray(a, dtype=np.float64).ravel())
+        b = np.ascontiguousarray(np.asarray(b, dtype=np.float64).ravel())
+        d = L.ProblemDesc()
+        if _is_torch_cuda(M):
+            import torch  # only when a torch tensor is passed
+
+            if M.dim() != 2:
+                raise ValueError("M must be a 2-D matrix")
+            if M.dtype not in (torch.float32, torch.float64):
+                M = M.to(torch.float64)
+            if M.stride(1) != 1:
+                M = M.contiguous()
+            n, m = M.shape
+            d.M = C.c_void_p(M.data_ptr())
+            d.M_dtype = L.REGOT_F64 if M.dtype == torch.float64 else L.REGOT_F32
+            d.M_mem = L.REGOT_MEM_DEVICE
+            d.ldm = M.stride(0)
+            dtype = np.float64 if M.dtype == torch.float64 else np.float32
+            self._keep.append(M)
+        else:
+            M = np.asarray(M)
+            if M.ndim != 2:
+                raise ValueError("M must be a 2-D matrix")
+            if M.dtype not in (np.float64, np.float32):
+                M = M.astype(np.float64)
+            M = np.ascontiguousarray(M)
+            n, m = M.shape
+            d.M = C.c_void_p(M.ctypes.data)
+            d.M_dtype = L.REGOT_F64 if M.dtype == np.float64 else L.REGOT_F32
+            d.M_mem = L.REGOT_MEM_HOST
+            d.ldm = m
+            dtype = M.dtype
+            self._keep.append(M)
+        if a.size != n or b.size != m:
+            raise ValueError(f"a must have {n} entries and b {m} entries (M is {n}x{m})")
+        d.n, d.m = n, m
+        d.a = C.c_void_p(a.ctypes.data)
+        d.b = C.c_void_p(b.ctypes.data)
+        d.ab_mem = L.REGOT_MEM_HOST
+        self.n, self.m = n, m
+        self.precision = _precision_code(precision, dtype)
+        h = C.c_void_p()
+        self.ctx.check(lib.regot_problem_create(self.ctx.handle, C.byref(d), self.precision,
+                                                C.byref(h)))
+        self.handle = h
+        self._keep = []
+        self._lib = lib
+
+    def close(self):
+        if getattr(self, "handle", None):
+            self._lib.regot_problem_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- solver calls -------------------------------------------------
+    def _solve(self, fname, reg, tol, max_iter, verbose, kwargs, qrot):
+        n, m = self.n, self.m
+        o = L.Opts()
+        self._lib.regot_opts_init(C.byref(o))
+        o.precision = self.precision
+        if "method" in kwargs:
+            o.method = int(kwargs["method"])
+        if "mu0" in kwargs:
+            o.mu0 = float(kwargs["mu0"])
+        if "shift" in kwargs:
+            o.shift = float(kwargs["shift"])
+        if "density" in kwargs:
+            o.density = float(kwargs["density"])
+        if "cg_tol" in kwargs:
+            o.cg_tol = float(kwargs["cg_tol"])
+        if "cg_max_iter" in kwargs:
+            o.cg_max_iter = int(kwargs["cg_max_iter"])
+        o.verbose = int(verbose)
+        want_plan = bool(kwargs.get("plan", True))
+        o.plan = 1 if want_plan else 0
+        o.prim_vals = 1 if kwargs.get("prim_vals", True) else 0
+        x0 = kwargs.get("x0")
+        keep = []
+        if x0 is not None:
+            x0 = np.ascontiguousarray(np.asarray(x0, dtype=np.float64).ravel())
+            keep.append(x0)
+            o.x0 = x0.ctypes.data_as(C.POINTER(C.c_double))
+            o.x0_len = x0.size
+        max_iter = int(max_iter)
+        if max_iter < 0:
+            raise ValueError("max_iter must be non-negative")
+        cap = max_iter + 2
+        dual = np.zeros(n + m if qrot else n + m - 1)
+        plan = np.zeros((n, m)) if want_plan else None
+        hist = np.zeros((5, cap))
+        r = L.Result()
+        r.hist_cap = cap
+        r.dual = dual.ctypes.data
+        r.plan = plan.ctypes.data if want_plan else None
+        r.obj_vals = hist[0].ctypes.data
+        r.mar_errs = hist[1].ctypes.data
+        r.run_times = hist[2].ctypes.data
+        r.densities = hist[3].ctypes.data
+        r.prim_vals = hist[4].ctypes.data
+        fn = getattr(self._lib, fname)
+        self.ctx.check(fn(self.ctx.handle, self.handle, float(reg), float(tol), max_iter,
+                          C.byref(o), C.byref(r)))
+        k = r.hist_len
+        res = qrot_result() if qrot else sinkhorn_result()
+        res.niter = int(r.niter)
+        res.dual = dual
+        res.plan = plan
+        res.obj_vals = hist[0, :k].tolist()
+        res.mar_errs = hist[1, :k].tolist()
+        res.run_times = hist[2, :k].tolist()
+        if qrot:
+            res.prim_vals = hist[4, :k].tolist()
+        elif fname == "regot_sinkhorn_ssns":
+            res.densities = hist[3, :k].tolist()
+        res.passes = int(r.passes)
+        res.solve_ms = float(r.solve_ms)
+        if verbose:
+            for i in range(k):
+                print(f"iter = {i}, objval = {res.obj_vals[i]}, ||grad|| = {res.mar_errs[i]}")
+        return res
+
+    def sinkhorn_bcd(self, reg, tol=1e-6, max_iter=1000, verbose=0, **kw):
+        return self._solve("regot_sinkhorn_bcd", reg, tol, max_iter, verbose, kw, False)
+
+    def sinkhorn_newton(self, reg, tol=1e-6, max_iter=1000, verbose=0, **kw):
+        return self._solve("regot_sinkhorn_newton", reg, tol, max_iter, verbose, kw, False)
+
+    def sinkhorn_ssns(self, reg, tol=1e-6, max_iter=1000, verbose=0, **kw):
+        return self._solve("regot_sinkhorn_ssns", reg, tol, max_iter, verbose, kw, False)
+
+    def qrot_lbfgs_dual(self, reg, tol=1e-6, max_iter=1000, verbose=0, **kw):
+        return self._solve("regot_qrot_lbfgs_dual", reg, tol, max_iter, verbose, kw, True)
+
+    def qrot_assn(self, reg, tol=1e-6, max_iter=1000, verbose=0, **kw):
+        return self._solve("regot_qrot_assn", reg, tol, max_iter, verbose, kw, True)
+
+    # ---- pass-level calls --------------------------------------------
+    def _vec(self, x, size):
+        x = np.ascontiguousarray(np.asarray(x, dtype=np.float64).ravel())
+        if x.size != size:
+            raise ValueError(f"expected a vector of length {size}")
+        return x
+
+    def erot_optimal_beta(self, reg, alpha):
+        alpha = self._vec(alpha, self.n)
+        out = np.zeros(self.m)
+        self.ctx.check(self._lib.regot_erot_optimal_beta(
+            self.ctx.handle, self.handle, float(reg), alpha.ctypes.data, out.ctypes.data))
+        return out
+
+    def erot_optimal_alpha(self, reg, beta):
+        beta = self._vec(beta, self.m)
+        out = np.zeros(self.n)
+        self.ctx.check(self._lib.regot_erot_optimal_alpha(
+            self.ctx.handle, self.handle, float(reg), beta.ctypes.data, out.ctypes.data))
+        return out
+
+    def erot_dual_obj_grad(self, reg, gamma):
+        gamma = self._vec(gamma, self.n + self.m - 1)
+        obj = np.zeros(1)
+        grad = np.zeros(self.n + self.m - 1)
+        self.ctx.check(self._lib.regot_erot_dual_obj_grad(
+            self.ctx.handle, self.handle, float(reg), gamma.ctypes.data, obj.ctypes.data,
+            grad.ctypes.data))
+        return float(obj[0]), grad
+
+    def erot_hvp(self, reg, gamma, x):
+        gamma = self._vec(gamma, self.n + self.m - 1)
+        x = self._vec(x, self.n + self.m - 1)
+        y = np.zeros(self.n + self.m - 1)
+        self.ctx.check(self._lib.regot_erot_hvp(
+            self.ctx.handle, self.handle, float(reg), gamma.ctypes.data, x.ctypes.data,
+            y.ctypes.data))
+        return y
+
+    def erot_plan(self, reg, gamma):
+        gamma = self._vec(gamma, self.n + self.m - 1)
+        P = np.zeros((self.n, self.m))
+        self.ctx.check(self._lib.regot_erot_plan(
+            self.ctx.handle, self.handle, float(reg), gamma.ctypes.data, P.ctypes.data,
+            L.REGOT_MEM_HOST))
+        return P
+
+    def qrot_dual_obj_grad(self, reg, gamma):
+        gamma = self._vec(gamma, self.n + self.m)
+        obj = np.zeros(1)
+        grad = np.zeros(self.n + self.m)
+        self.ctx.check(self._lib.regot_qrot_dual_obj_grad(
+            self.ctx.handle, self.handle, float(reg), gamma.ctypes.data, obj.ctypes.data,
+            grad.ctypes.data))
+        return float(obj[0]), grad
+
+    def qrot_optimal_beta(self, reg, alpha):
+        alpha = self._vec(alpha, self.n)
+        out = np.zeros(self.m)
+        self.ctx.check(self._lib.regot_qrot_optimal_beta(
+            self.ctx.handle, self.handle, float(reg), alpha.ctypes.data, out.ctypes.data))
+        return out
+
+    def qrot_primal_val(self, reg, gamma):
+        gamma = self._vec(gamma, self.n + self.m)
+        out = np.zeros(1)
+        self.ctx.check(self._lib.regot_qrot_primal_val(
+            self.ctx.handle, self.handle, float(reg), gamma.ctypes.data, out.ctypes.data))
+        return float(out[0])
+
+    def qrot_plan(self, reg, gamma):
+        gamma = self._vec(gamma, self.n + self.m)
+        P = np.zeros((self.n, self.m))
+        self.ctx.check(self._lib.regot_qrot_plan(
+            self.ctx.handle, self.handle, float(reg), gamma.ctypes.data, P.ctypes.data,
+            L.REGOT_MEM_HOST))
+        return P
+
+
+def _solve(name, M, a, b, reg, tol, max_iter, verbose, kwargs):
+    prob = Problem(M, a, b, precision=kwargs.get("precision"), device=int(kwargs.get("device", 0)))
+    try:
+        return getattr(prob, name)(reg, tol, max_iter, verbose, **kwargs)
+    finally:
+        prob.close()
+
+
+def sinkhorn_bcd(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
+    """BCD (Sinkhorn) for EROT; reference src/sinkhorn_bcd.cpp:14-124."""
+    return _solve("sinkhorn_bcd", M, a, b, reg, tol, max_iter, verbose, kwargs)
+
+
+def sinkhorn_newton(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
+    """Newton's method for EROT; reference src/sinkhorn_newton.cpp:17-129."""
+    return _solve("sinkhorn_newton", M, a, b, reg, tol, max_iter, verbose, kwargs)
+
+
+def sinkhorn_ssns(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
+    """Safe and sparse Newton for EROT; reference src/sinkhorn_ssns.cpp:16-234."""
+    return _solve("sinkhorn_ssns", M, a, b, reg, tol, max_iter, verbose, kwargs)
+
+
+def qrot_lbfgs_dual(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
+    """L-BFGS on the QROT dual; reference src/qrot_lbfgs_dual.cpp:81-126."""
+    return _solve("qrot_lbfgs_dual", M, a, b, reg, tol, max_iter, verbose, kwargs)
+
+
+def qrot_assn(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
+    """Adaptive semi-smooth Newton for QROT; reference src/qrot_assn.cpp:16-170."""
+    return _solve("qrot_assn", M, a, b, reg, tol, max_iter, verbose, kwargs)

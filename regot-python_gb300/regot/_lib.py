@@ -1,0 +1,190 @@
+"""Loader and ctypes declarations of libregot_gb300.so (include/regot_gb300.h).
+
+The library is built in-tree by ``regot-python_gb300/build.py`` (called from
+``__graft_entry__.build()``). There is no CPU fallback: importing a solver
+without the compiled library raises ImportError, and calling one without a
+CUDA device raises RuntimeError.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(os.path.dirname(_HERE), "_build", "libregot_gb300.so")
+
+REGOT_OK = 0
+REGOT_ERR_INVALID_ARG = 1
+REGOT_ERR_NO_DEVICE = 7
+REGOT_F64, REGOT_F32 = 0, 1
+REGOT_MEM_HOST, REGOT_MEM_DEVICE = 0, 1
+REGOT_PREC_FP64, REGOT_PREC_MIXED = 0, 1
+
+_dp = C.POINTER(C.c_double)
+
+
+class ProblemDesc(C.Structure):
+    _fields_ = [
+        ("M", C.c_void_p),
+        ("M_dtype", C.c_int),
+        ("M_mem", C.c_int),
+        ("ldm", C.c_longlong),
+        ("n", C.c_int),
+        ("m", C.c_int),
+        ("a", C.c_void_p),
+        ("b", C.c_void_p),
+        ("ab_mem", C.c_int),
+    ]
+
+
+class Opts(C.Structure):
+    _fields_ = [
+        ("precision", C.c_int),
+        ("method", C.c_int),
+        ("mu0", C.c_double),
+        ("shift", C.c_double),
+        ("density", C.c_double),
+        ("tau", C.c_double),
+        ("x0", _dp),
+        ("x0_len", C.c_int),
+        ("cg_tol", C.c_double),
+        ("cg_max_iter", C.c_int),
+        ("verbose", C.c_int),
+        ("plan", C.c_int),
+        ("plan_mem", C.c_int),
+        ("prim_vals", C.c_int),
+    ]
+
+
+class Result(C.Structure):
+    _fields_ = [
+        ("niter", C.c_int),
+        ("hist_len", C.c_int),
+        ("hist_cap", C.c_int),
+        ("dual", C.c_void_p),
+        ("plan", C.c_void_p),
+        ("obj_vals", C.c_void_p),
+        ("mar_errs", C.c_void_p),
+        ("run_times", C.c_void_p),
+        ("densities", C.c_void_p),
+        ("prim_vals", C.c_void_p),
+        ("passes", C.c_longlong),
+        ("solve_ms", C.c_double),
+    ]
+
+
+# Every symbol include/regot_gb300.h declares.
+EXPORTS = [
+    "regot_opts_init", "regot_ctx_create", "regot_ctx_destroy", "regot_ctx_last_error",
+    "regot_ctx_set_stream", "regot_ctx_own_stream", "regot_ctx_kernel_launches", "regot_problem_create",
+    "regot_problem_destroy", "regot_sinkhorn_bcd", "regot_sinkhorn_newton",
+    "regot_sinkhorn_ssns", "regot_qrot_lbfgs_dual", "regot_qrot_assn",
+    "regot_erot_optimal_beta", "regot_erot_optimal_alpha", "regot_erot_dual_obj_grad",
+    "regot_erot_hvp", "regot_erot_plan", "regot_qrot_dual_obj_grad", "regot_qrot_optimal_beta",
+    "regot_qrot_primal_val", "regot_qrot_plan", "regot_time_pass",
+]
+
+_lib = None
+_lock = threading.Lock()
+
+
+def load() -> C.CDLL:
+    """Load the shared library (once) and declare the signatures."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(
+                f"{LIB_PATH} is missing; build it with "
+                "`python regot-python_gb300/build.py` (needs nvcc)")
+        lib = C.CDLL(LIB_PATH)
+        vp = C.c_void_p
+        lib.regot_opts_init.argtypes = [C.POINTER(Opts)]
+        lib.regot_opts_init.restype = None
+        lib.regot_ctx_create.argtypes = [C.c_int, C.POINTER(vp)]
+        lib.regot_ctx_destroy.argtypes = [vp]
+        lib.regot_ctx_destroy.restype = None
+        lib.regot_ctx_last_error.argtypes = [vp]
+        lib.regot_ctx_last_error.restype = C.c_char_p
+        lib.regot_ctx_set_stream.argtypes = [vp, vp]
+        lib.regot_ctx_own_stream.argtypes = [vp]
+        lib.regot_ctx_own_stream.restype = vp
+        lib.regot_ctx_kernel_launches.argtypes = [vp]
+        lib.regot_ctx_kernel_launches.restype = C.c_longlong
+        lib.regot_problem_create.argtypes = [vp, C.POINTER(ProblemDesc), C.c_int, C.POINTER(vp)]
+        lib.regot_problem_destroy.argtypes = [vp]
+        lib.regot_problem_destroy.restype = None
+        for name in ("regot_sinkhorn_bcd", "regot_sinkhorn_newton", "regot_sinkhorn_ssns",
+                     "regot_qrot_lbfgs_dual", "regot_qrot_assn"):
+            f = getattr(lib, name)
+            f.argtypes = [vp, vp, C.c_double, C.c_double, C.c_int, C.POINTER(Opts),
+                          C.POINTER(Result)]
+        lib.regot_erot_optimal_beta.argtypes = [vp, vp, C.c_double, vp, vp]
+        lib.regot_erot_optimal_alpha.argtypes = [vp, vp, C.c_double, vp, vp]
+        lib.regot_erot_dual_obj_grad.argtypes = [vp, vp, C.c_double, vp, vp, vp]
+        lib.regot_erot_hvp.argtypes = [vp, vp, C.c_double, vp, vp, vp]
+        lib.regot_erot_plan.argtypes = [vp, vp, C.c_double, vp, vp, C.c_int]
+        lib.regot_qrot_dual_obj_grad.argtypes = [vp, vp, C.c_double, vp, vp, vp]
+        lib.regot_qrot_optimal_beta.argtypes = [vp, vp, C.c_double, vp, vp]
+        lib.regot_qrot_primal_val.argtypes = [vp, vp, C.c_double, vp, vp]
+        lib.regot_qrot_plan.argtypes = [vp, vp, C.c_double, vp, vp, C.c_int]
+        lib.regot_time_pass.argtypes = [vp, vp, C.c_int, C.c_double, C.c_int]
+        _lib = lib
+        return lib
+
+
+class Context:
+    """One CUDA device and stream (regot_ctx)."""
+
+    def __init__(self, device: int = 0):
+        lib = load()
+        h = C.c_void_p()
+        rc = lib.regot_ctx_create(int(device), C.byref(h))
+        if rc == REGOT_ERR_NO_DEVICE:
+            raise RuntimeError("regot_gb300 needs a CUDA device; none is visible")
+        if rc != REGOT_OK:
+            raise RuntimeError(f"regot_ctx_create failed with status {rc}")
+        self.handle = h
+        self.device = device
+        self._lib = lib
+
+    def check(self, rc: int):
+        if rc == REGOT_OK:
+            return
+        msg = self._lib.regot_ctx_last_error(self.handle).decode(errors="replace")
+        if rc == REGOT_ERR_INVALID_ARG:
+            raise ValueError(msg)
+        raise RuntimeError(msg)
+
+    def kernel_launches(self) -> int:
+        return int(self._lib.regot_ctx_kernel_launches(self.handle))
+
+    def set_stream(self, stream_ptr: int | None):
+        """Launch on this cudaStream_t (0 = legacy default stream); None
+        restores the context's own stream."""
+        if stream_ptr is None:
+            stream_ptr = self._lib.regot_ctx_own_stream(self.handle)
+        self.check(self._lib.regot_ctx_set_stream(self.handle, C.c_void_p(stream_ptr or 0)))
+
+    def __del__(self):
+        try:
+            if getattr(self, "handle", None):
+                self._lib.regot_ctx_destroy(self.handle)
+                self.handle = None
+        except Exception:
+            pass
+
+
+_contexts: dict[int, Context] = {}
+
+
+def context(device: int = 0) -> Context:
+    with _lock:
+        ctx = _contexts.get(device)
+    if ctx is None:
+        ctx = Context(device)
+        with _lock:
+            _contexts[device] = ctx
+    return ctx
