@@ -36,7 +36,8 @@ enum {
     REGOT_ERR_CUDA = 4,
     REGOT_ERR_TIMEOUT = 5,
     REGOT_ERR_NUMERIC = 6,
-    REGOT_ERR_NO_DEVICE = 7
+    REGOT_ERR_NO_DEVICE = 7,
+    REGOT_ERR_TOO_LARGE = 8   /* problem exceeds a fixed scratch maximum */
 };
 
 enum { REGOT_F64 = 0, REGOT_F32 = 1 };              /* element type of M */
@@ -187,6 +188,28 @@ enum {
  * caller can bracket them with its own events. No counterpart in the
  * reference: it measures the kernels behind the solvers above. */
 int regot_time_pass(regot_ctx* ctx, regot_dproblem* prob, int kind, double reg, int reps);
+
+/* ---- Allocation-free variant ----
+ * No counterpart in the reference. regot_erot_dual_obj_grad for callers that
+ * cannot allocate device memory: code running while another framework
+ * captures a CUDA graph (cudaMalloc is not allowed inside such a capture),
+ * custom-call hooks of frameworks that own all device memory, and loops that
+ * cannot afford cudaMalloc's implicit device synchronisation. It allocates
+ * nothing: its scratch is one static device array of
+ * REGOT_NOALLOC_SCRATCH_BYTES (16 MiB) that every GPU loading the library
+ * holds until exit; a problem that needs more (beyond about n = m = 14000)
+ * returns REGOT_ERR_TOO_LARGE. All pointers are device pointers: M is n x m
+ * FP32 row-major with row stride ldm (a multiple of 4, 16-byte aligned
+ * base), gamma = (alpha, beta~) has n+m-1 entries (beta_m = 0), grad has
+ * n+m-1 entries, obj one. The work is enqueued on `stream` (a cudaStream_t,
+ * NULL = legacy default) and not synchronised. The first call on a device
+ * looks up the scratch address (cudaGetSymbolAddress) and should come before
+ * any stream capture. All calls share the scratch: calls that overlap on the
+ * GPU race and must be serialised by the caller. */
+#define REGOT_NOALLOC_SCRATCH_BYTES (16u << 20)
+int regot_erot_dual_obj_grad_noalloc(const float* M, long long ldm, int n, int m,
+                                     const double* gamma, const double* a, const double* b,
+                                     double reg, double* grad, double* obj, void* stream);
 
 #ifdef __cplusplus
 }

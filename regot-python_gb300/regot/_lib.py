@@ -17,6 +17,7 @@ LIB_PATH = os.path.join(os.path.dirname(_HERE), "_build", "libregot_gb300.so")
 REGOT_OK = 0
 REGOT_ERR_INVALID_ARG = 1
 REGOT_ERR_NO_DEVICE = 7
+REGOT_ERR_TOO_LARGE = 8
 REGOT_F64, REGOT_F32 = 0, 1
 REGOT_MEM_HOST, REGOT_MEM_DEVICE = 0, 1
 REGOT_PREC_FP64, REGOT_PREC_MIXED = 0, 1
@@ -83,6 +84,7 @@ EXPORTS = [
     "regot_erot_optimal_beta", "regot_erot_optimal_alpha", "regot_erot_dual_obj_grad",
     "regot_erot_hvp", "regot_erot_plan", "regot_qrot_dual_obj_grad", "regot_qrot_optimal_beta",
     "regot_qrot_primal_val", "regot_qrot_plan", "regot_time_pass",
+    "regot_erot_dual_obj_grad_noalloc",
 ]
 
 _lib = None
@@ -131,6 +133,8 @@ def load() -> C.CDLL:
         lib.regot_qrot_primal_val.argtypes = [vp, vp, C.c_double, vp, vp]
         lib.regot_qrot_plan.argtypes = [vp, vp, C.c_double, vp, vp, C.c_int]
         lib.regot_time_pass.argtypes = [vp, vp, C.c_int, C.c_double, C.c_int]
+        lib.regot_erot_dual_obj_grad_noalloc.argtypes = [
+            vp, C.c_longlong, C.c_int, C.c_int, vp, vp, vp, C.c_double, vp, vp, vp]
         _lib = lib
         return lib
 
