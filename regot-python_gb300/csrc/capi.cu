@@ -93,6 +93,7 @@ void finish_erot_result(ErotOps& ops, const double* d_gamma, const double* hobj,
     if (res->mar_errs) d2h(res->mar_errs, hmar, hist_len * sizeof(double), st);
     if (res->run_times) d2h(res->run_times, htime, hist_len * sizeof(double), st);
     if (res->densities && hdens) d2h(res->densities, hdens, hist_len * sizeof(double), st);
+    ops.check_err();
     if (o.plan && res->plan) {
         DBuf<double> mx(1, st);
         if (o.plan_mem == REGOT_MEM_DEVICE) {
@@ -316,7 +317,7 @@ int regot_erot_optimal_beta(regot_ctx* ctx, regot_dproblem* P, double reg, const
         h2d(da.get(), alpha, P->n * sizeof(double), st);
         ops.optimal_beta(da.get(), db.get(), mx.get());
         d2h(beta, db.get(), P->m * sizeof(double), st);
-        sync(st);
+        ops.check_err();
     });
 }
 
@@ -331,7 +332,7 @@ int regot_erot_optimal_alpha(regot_ctx* ctx, regot_dproblem* P, double reg, cons
         h2d(db.get(), beta, P->m * sizeof(double), st);
         ops.optimal_alpha(db.get(), da.get(), mx.get());
         d2h(alpha, da.get(), P->n * sizeof(double), st);
-        sync(st);
+        ops.check_err();
     });
 }
 
@@ -356,7 +357,7 @@ int regot_erot_dual_obj_grad(regot_ctx* ctx, regot_dproblem* P, double reg, cons
         ops.row_col_sums(g.get(), g.get() + n, rc.get(), rc.get() + n, mx.get());
         std::vector<double> h(n + m);
         d2h(h.data(), rc.get(), (n + m) * sizeof(double), st);
-        sync(st);
+        ops.check_err();
         // sinkhorn_problem_obj.cpp:371-393
         double tsum = 0.0, ga = 0.0, gb = 0.0;
         for (int i = 0; i < n; ++i) {
@@ -389,7 +390,7 @@ int regot_erot_hvp(regot_ctx* ctx, regot_dproblem* P, double reg, const double* 
         std::vector<double> hrc(n + m), hy(n + m);
         d2h(hrc.data(), rc.get(), (n + m) * sizeof(double), st);
         d2h(hy.data(), yy.get(), (n + m) * sizeof(double), st);
-        sync(st);
+        ops.check_err();
         for (int i = 0; i < n; ++i) y[i] = (hrc[i] * x[i] + hy[i]) / reg;
         for (int j = 0; j < m - 1; ++j) y[n + j] = (hrc[n + j] * x[n + j] + hy[n + j]) / reg;
     });

@@ -44,6 +44,42 @@ __device__ __forceinline__ void warp_atomic_max_abs(double* target, double v) {
                   (unsigned long long)__double_as_longlong(a));
 }
 
+// Sum of count values p[k * stride], k = 0..count-1, in FP64. Loads are
+// issued eight at a time into four independent accumulators, so that the
+// merge is bound by memory throughput instead of one load latency per term;
+// the order is fixed, so results are reproducible.
+template <typename Acc>
+__device__ __forceinline__ double merge_strided(const Acc* p, int count, size_t stride) {
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    int k = 0;
+    for (; k + 8 <= count; k += 8) {
+        Acc v[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) v[q] = p[(size_t)(k + q) * stride];
+        s0 += (double)v[0] + (double)v[4];
+        s1 += (double)v[1] + (double)v[5];
+        s2 += (double)v[2] + (double)v[6];
+        s3 += (double)v[3] + (double)v[7];
+    }
+    for (; k < count; ++k) s0 += (double)p[(size_t)k * stride];
+    return (s0 + s1) + (s2 + s3);
+}
+
+template <typename Acc>
+__device__ __forceinline__ double max_strided(const Acc* p, int count, size_t stride) {
+    double s0 = -INFINITY, s1 = -INFINITY;
+    int k = 0;
+    for (; k + 8 <= count; k += 8) {
+        Acc v[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) v[q] = p[(size_t)(k + q) * stride];
+        s0 = fmax(s0, fmax(fmax((double)v[0], (double)v[1]), fmax((double)v[2], (double)v[3])));
+        s1 = fmax(s1, fmax(fmax((double)v[4], (double)v[5]), fmax((double)v[6], (double)v[7])));
+    }
+    for (; k < count; ++k) s0 = fmax(s0, (double)p[(size_t)k * stride]);
+    return fmax(s0, s1);
+}
+
 // Grid-wide sum of K values per thread. Returns true in thread 0 of the last
 // block to finish, with the totals in out[] (summed in block order).
 template <int K>

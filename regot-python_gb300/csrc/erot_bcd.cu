@@ -70,8 +70,7 @@ __global__ void k_bcd_row(const Acc* rp, int nslabs, int n, const double* anchor
     double v[3] = {0.0, 0.0, 0.0};
     double vmax = 0.0;
     if (i < n) {
-        double S = 0.0;
-        for (int k = 0; k < nslabs; ++k) S += (double)rp[(size_t)k * n + i];
+        const double S = merge_strided(rp + i, nslabs, (size_t)n);
         const double al = alpha[i];
         const double an = anchor[i];
         if (!robust && !sum_ok<MIXED>(S)) atomicOr(&st->bad, 1);
@@ -119,8 +118,7 @@ __global__ void k_bcd_col(const Acc* cp, int nrb, int m, const double* anchor,
     double v[1] = {0.0};
     double vmax = 0.0;
     if (j < m) {
-        double S = 0.0;
-        for (int k = 0; k < nrb; ++k) S += (double)cp[(size_t)k * m + j];
+        const double S = merge_strided(cp + j, nrb, (size_t)m);
         if (!robust && !sum_ok<MIXED>(S)) atomicOr(&st->bad, 2);
         const double bn = anchor[j] + reg * (logb[j] - log(S));
         beta_next[j] = bn;

@@ -9,32 +9,22 @@ namespace {
 
 template <typename Acc>
 __device__ __forceinline__ double merge_row(const Acc* rp, int nslabs, int n, int i, int r = 0) {
-    const Acc* q = rp + (size_t)r * nslabs * n + i;
-    double s = 0.0;
-    for (int k = 0; k < nslabs; ++k) s += (double)q[(size_t)k * n];
-    return s;
+    return merge_strided(rp + (size_t)r * nslabs * n + i, nslabs, (size_t)n);
 }
 
 template <typename Acc>
 __device__ __forceinline__ double merge_col(const Acc* cp, int nrb, int m, int j, int c = 0) {
-    const Acc* q = cp + (size_t)c * nrb * m + j;
-    double s = 0.0;
-    for (int k = 0; k < nrb; ++k) s += (double)q[(size_t)k * m];
-    return s;
+    return merge_strided(cp + (size_t)c * nrb * m + j, nrb, (size_t)m);
 }
 
 template <typename Acc>
 __device__ __forceinline__ double max_row(const Acc* rp, int nslabs, int n, int i) {
-    double s = -INFINITY;
-    for (int k = 0; k < nslabs; ++k) s = fmax(s, (double)rp[(size_t)k * n + i]);
-    return s;
+    return max_strided(rp + i, nslabs, (size_t)n);
 }
 
 template <typename Acc>
 __device__ __forceinline__ double max_col(const Acc* cp, int nrb, int m, int j) {
-    double s = -INFINITY;
-    for (int k = 0; k < nrb; ++k) s = fmax(s, (double)cp[(size_t)k * m + j]);
-    return s;
+    return max_strided(cp + j, nrb, (size_t)m);
 }
 
 __global__ void k_log(const double* x, int len, double* y) {
@@ -109,6 +99,8 @@ ErotOps::ErotOps(regot_dproblem* P, double reg, cudaStream_t st)
     for (int j = 0; j < m_ - 1; ++j) sum_bt_ += P->hb[j];
     buf_.init(n_, m_, mixed_, 3, 2, 4, st_);
     anchor_.alloc((size_t)(n_ > m_ ? n_ : m_), st_);
+    err_.alloc(1, st_);
+    err_.zero();
     if (mixed_) {
         rsplit_.alloc(n_, st_);
         csplit_.alloc(m_, st_);
@@ -118,6 +110,7 @@ ErotOps::ErotOps(regot_dproblem* P, double reg, cudaStream_t st)
 
 PassParams ErotOps::base_params() const {
     PassParams p;
+    p.err = err_.get();
     p.M = P_->M;
     p.ldm = P_->ldm;
     p.n = n_;
@@ -129,7 +122,15 @@ PassParams ErotOps::base_params() const {
     return p;
 }
 
+void ErotOps::check_err() {
+    int e = 0;
+    d2h(&e, err_.get(), sizeof(int), st_);
+    sync(st_);
+    if (e) throw Error(REGOT_ERR_TIMEOUT, "a dense pass gave up waiting for its tile copies");
+}
+
 void ErotOps::pass(int op, PassParams p) {
+    if (!p.err) p.err = err_.get();
     if (mixed_) {
         launch_split(p, rsplit_.get(), csplit_.get(), cdsplit_.get(), st_);
         p.rsplit = rsplit_.get();
@@ -142,6 +143,7 @@ void ErotOps::pass(int op, PassParams p) {
 }
 
 void ErotOps::pass_presplit(int op, PassParams p) {
+    if (!p.err) p.err = err_.get();
     if (mixed_) {
         p.rsplit = rsplit_.get();
         p.csplit = csplit_.get();
@@ -163,10 +165,10 @@ void ErotOps::maxabs(const double* x, int nx, const double* y, int ny, double* o
 #define REGOT_LAUNCH_ACC(KERNEL, LEN, PART, ...)                                   \
     do {                                                                           \
         if (mixed_)                                                                \
-            KERNEL<float><<<cdiv(LEN, 256), 256, 0, st_>>>(                        \
+            KERNEL<float><<<cdiv(LEN, 64), 64, 0, st_>>>(                          \
                 reinterpret_cast<const float*>(PART), __VA_ARGS__);                \
         else                                                                       \
-            KERNEL<double><<<cdiv(LEN, 256), 256, 0, st_>>>(                       \
+            KERNEL<double><<<cdiv(LEN, 64), 64, 0, st_>>>(                         \
                 reinterpret_cast<const double*>(PART), __VA_ARGS__);               \
         count_launch();                                                            \
         REGOT_CHECK_LAUNCH();                                                      \

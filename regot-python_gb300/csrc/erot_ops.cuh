@@ -46,6 +46,9 @@ public:
 
     // Dense pass with this problem's M, reg and partial buffers.
     void pass(int op, PassParams p);
+    // Throw REGOT_ERR_TIMEOUT if a pass gave up a bounded wait (synchronises).
+    void check_err();
+    int* err_flag() const { return err_.get(); }
     // Dense pass reusing the FP32 split of the previous pass (mixed mode).
     void pass_presplit(int op, PassParams p);
     PassParams base_params() const;
@@ -82,6 +85,7 @@ private:
     DBuf<double> anchor_;
     DBuf<float4> rsplit_, csplit_;
     DBuf<float> cdsplit_;
+    DBuf<int> err_;
 };
 
 }  // namespace regot

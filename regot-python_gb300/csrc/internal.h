@@ -34,23 +34,24 @@ inline void require(bool ok, const std::string& msg, int code = REGOT_ERR_INVALI
 }
 
 // ------------------------------------------------------------- geometry --
-// Dense passes tile M (row-major, row stride ldm) into CTAs of RB rows x
-// CW columns. A CTA has 8 warps; each warp streams RB/8 consecutive rows and
-// each lane owns two 16-byte vectors per row (8 FP32 or 4 FP64 columns).
-constexpr int kThreads = 256;
+// Dense passes tile M (row-major, row stride ldm) into tiles of RB rows x
+// CW columns. A CTA has 8 warps; each warp streams RB/8 consecutive rows of
+// a tile and each lane owns LC / VW 16-byte vectors per row (16 FP32 or 8 FP64
+// columns).
+constexpr int kThreads = 256;            // 8 warps per CTA
 constexpr int kWarps = kThreads / 32;
-constexpr int kRB = 64;  // rows per CTA
+constexpr int kRB = 64;                  // rows per tile (8 per warp)
 
 template <typename TM> struct Geo;
 template <> struct Geo<float> {
-    static constexpr int VW = 4;
-    static constexpr int LC = 8;
-    static constexpr int CW = 256;
+    static constexpr int VW = 4;    // elements per 16-byte vector
+    static constexpr int LC = 16;   // columns per lane
+    static constexpr int CW = 512;  // columns per slab (one 2 KB row segment)
 };
 template <> struct Geo<double> {
     static constexpr int VW = 2;
-    static constexpr int LC = 4;
-    static constexpr int CW = 128;
+    static constexpr int LC = 8;
+    static constexpr int CW = 256;
 };
 
 inline int cdiv(long long a, long long b) { return (int)((a + b - 1) / b); }
@@ -98,7 +99,7 @@ struct PassParams {
     const float4* csplit = nullptr;  // per column: (hi, lo, cx, cx2)
     const float* cdsplit = nullptr;  // per column: cd
     // Filled by launch_pass from reg.
-    float kexp_f = 0.f, inv_reg_f = 0.f;
+    float kexp_f = 0.f, inv_kexp_f = 0.f, inv_reg_f = 0.f;
     double kexp_d = 0.0, inv_reg_d = 0.0;
     void* rowpart = nullptr;       // [NR][nslabs][n] (Acc)
     void* colpart = nullptr;       // [NC][nrb][m]   (Acc)
@@ -106,18 +107,28 @@ struct PassParams {
     uint32_t* bitmask = nullptr;   // [n][nslabs][LC]
     double* out = nullptr;         // plan output, row-major, stride m
     const int* done = nullptr;     // early-exit flag (device)
+    int* err = nullptr;            // set to 1 if a bounded wait gave up (device)
 };
 
 struct PassShape {
-    int nslabs, nrb, nblocks;
+    int nslabs, nrb, ntiles;
+    int nblocks;  // capacity for per-CTA totals (>= the grid of any dense pass)
 };
+
+constexpr int kMaxPassCtasPerSm = 4;
+int device_sm_count();
+// Grid of the persistent dense pass `op` (SMs x resident CTAs, at most the
+// number of tiles); per-CTA totals of that pass have this many entries.
+int pass_blocks(int op, bool mixed, int n, int m);
 
 template <typename TM>
 inline PassShape pass_shape(int n, int m) {
     PassShape s;
     s.nslabs = cdiv(m, Geo<TM>::CW);
     s.nrb = cdiv(n, kRB);
-    s.nblocks = s.nslabs * s.nrb;
+    s.ntiles = s.nslabs * s.nrb;
+    const int cap = device_sm_count() * kMaxPassCtasPerSm;
+    s.nblocks = s.ntiles < cap ? s.ntiles : cap;
     return s;
 }
 

@@ -103,15 +103,13 @@ __global__ void k_noalloc_grad(const float* rowpart, int nslabs, const float* co
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     double v[3] = {0.0, 0.0, 0.0};
     if (t < n) {
-        double r = 0.0;
-        for (int k = 0; k < nslabs; ++k) r += (double)rowpart[(size_t)k * n + t];
+        const double r = merge_strided(rowpart + t, nslabs, (size_t)n);
         grad[t] = r - a[t];
         v[0] = r;
         v[1] = gamma[t] * a[t];
     } else if (t < n + m - 1) {
         const int j = t - n;
-        double c = 0.0;
-        for (int k = 0; k < nrb; ++k) c += (double)colpart[(size_t)k * m + j];
+        const double c = merge_strided(colpart + j, nrb, (size_t)m);
         grad[t] = c - b[j];
         v[2] = gamma[t] * b[j];
     }

@@ -26,12 +26,71 @@ namespace regot {
 
 thread_local long long* g_launch_counter = nullptr;
 
+int device_sm_count() {
+    int dev = 0, count = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+    static int cache[64] = {0};
+    if (dev < 64 && cache[dev]) return cache[dev];
+    if (cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        count <= 0)
+        count = 1;
+    if (dev < 64) cache[dev] = count;
+    return count;
+}
+
 namespace {
 
 __device__ __forceinline__ float ex2_approx(float x) {
     float y;
     asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
     return y;
+}
+
+// ---- bulk asynchronous copies (TMA engine) completing on an mbarrier ----
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+                 : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+// try_wait with a suspend-time hint: a waiting warp sleeps until the phase
+// completes (or the hint elapses) instead of spinning on issue slots that the
+// computing warps need.
+constexpr uint32_t kSuspendHintNs = 200000;
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity), "r"(kSuspendHintNs)
+        : "memory");
+    return ok != 0;
+}
+// Global -> shared bulk copy; dst, src 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes,
+                                         uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+        ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+// Bounded wait: gives up after kMaxSpins suspended polls (a few seconds at
+// most) and reports it through *err.
+constexpr long long kMaxSpins = 1LL << 14;
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* err) {
+    for (long long s = 0; s < kMaxSpins; ++s)
+        if (mbar_try_wait(bar, parity)) return true;
+    if (err) atomicOr(err, 1);
+    return false;
 }
 
 template <typename T>
@@ -106,11 +165,67 @@ __device__ __forceinline__ void split(double v, double g, double inv_g, float& h
     lo = (float)(v - h);
 }
 
+// Row stages of the per-warp copy ring (one row segment of CW elements each).
+// Four 2 KB row buffers per warp: with two CTAs of 8 warps per SM, 128 KB of
+// copies are in flight per SM, where bulk-copy streaming reaches the measured
+// HBM bandwidth on this part (it loses bandwidth well beyond that).
+template <int OP, typename Acc, int CW>
+__host__ __device__ constexpr int ring_stages() {
+    return 4;
+}
+
+__host__ __device__ constexpr bool op_uses_cx(int op) {
+    return op == OP_E_HVP || op == OP_Q_P3;
+}
+__host__ __device__ constexpr bool op_uses_cx2(int op) { return op == OP_Q_P3; }
+__host__ __device__ constexpr bool op_uses_cd(int op) { return op == OP_E_LS; }
+__host__ __device__ constexpr bool op_uses_rx(int op) {
+    return op == OP_E_HVP || op == OP_Q_P2 || op == OP_Q_P3;
+}
+__host__ __device__ constexpr bool op_uses_rd(int op) { return op == OP_E_LS; }
+
+// Sum (or max) of the per-lane partials of a warp's N rows (N a power of
+// two <= 32): a transposed butterfly whose first log2(N) exchange levels
+// halve the number of values per lane, then plain levels; N - 1 + 5 - log2(N)
+// shuffles instead of 5 N. Afterwards lane L holds the total of row
+// L >> (5 - log2 N).
+template <bool ISMAX, int N, typename T>
+__device__ __forceinline__ T warp_reduce_rows(T (&v)[N], int lane) {
+    constexpr int L = N >= 32 ? 5 : N >= 16 ? 4 : N >= 8 ? 3 : N >= 4 ? 2 : N >= 2 ? 1 : 0;
+#pragma unroll
+    for (int lvl = 0; lvl < L; ++lvl) {
+        const int o = 16 >> lvl;
+        const int K = N >> lvl;
+        const bool upper = (lane & o) != 0;
+#pragma unroll
+        for (int k = 0; k < K / 2; ++k) {
+            const T send = upper ? v[k] : v[k + K / 2];
+            const T keep = upper ? v[k + K / 2] : v[k];
+            const T got = __shfl_xor_sync(0xffffffffu, send, o);
+            v[k] = ISMAX ? fmax(keep, got) : keep + got;
+        }
+    }
+    T r = v[0];
+#pragma unroll
+    for (int o = 16 >> L; o > 0; o >>= 1) {
+        const T got = __shfl_xor_sync(0xffffffffu, r, o);
+        r = ISMAX ? fmax(r, got) : r + got;
+    }
+    return r;
+}
+
+// Persistent dense pass. The grid holds as many CTAs as fit on the SMs; CTA
+// b processes tiles b, b + G, b + 2G, ... (tile t = row block t / nslabs,
+// column slab t % nslabs; RB rows x CW columns). Each warp streams RB/8 rows
+// of every tile through its own ring of NS shared-memory row buffers: lane 0
+// keeps NS row copies (cp.async.bulk, one mbarrier per buffer) in flight
+// ahead of the row the warp is reducing, across tile boundaries, so HBM
+// never idles between waves of CTAs.
 template <typename TM, int OP>
-__global__ void __launch_bounds__(kThreads) dense_pass(const PassParams p) {
+__global__ void __launch_bounds__(kThreads, 2) dense_pass(const PassParams p) {
     if (p.done && *p.done) return;
     using G = Geo<TM>;
-    constexpr int VW = G::VW, LC = G::LC, CW = G::CW;
+    constexpr int VW = G::VW, LC = G::LC, CW = G::CW, NV = LC / VW;
     constexpr bool MIXED = std::is_same<TM, float>::value;
     constexpr bool COLROOT = (OP == OP_Q_COLROOT);
     using Acc = typename std::conditional<COLROOT, double, TM>::type;
@@ -119,240 +234,440 @@ __global__ void __launch_bounds__(kThreads) dense_pass(const PassParams p) {
     constexpr int NRa = NR > 0 ? NR : 1, NCa = NC > 0 ? NC : 1, NTa = NT > 0 ? NT : 1;
     constexpr bool ISMAX = op_is_max(OP);
     constexpr bool EROT = (OP <= OP_E_COLMAX);
-    constexpr int RPW = kRB / kWarps;  // rows per warp
+    constexpr int RPW = kRB / kWarps;  // rows per warp per tile (4)
+    constexpr int LOGR = RPW >= 8 ? 3 : RPW >= 4 ? 2 : RPW >= 2 ? 1 : 0;
+    constexpr int NS = ring_stages<OP, Acc, CW>();
 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int slab = blockIdx.x, rb = blockIdx.y;
-    const int nslabs = gridDim.x, nrb = gridDim.y;
-    const int c0 = slab * CW, r0 = rb * kRB;
     const int n = p.n, m = p.m;
     const long long ldm = p.ldm;
+    const int nslabs = (m + CW - 1) / CW;
+    const int nrb = (n + kRB - 1) / kRB;
+    const int ntiles = nslabs * nrb;
+    const int my_tiles =
+        (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    const int rw0 = warp * RPW;
+    const TM* Mb = reinterpret_cast<const TM*>(p.M);
+
+    extern __shared__ __align__(128) unsigned char dyn_smem[];
+    TM* ring = reinterpret_cast<TM*>(dyn_smem) + (size_t)warp * NS * CW;
+    Acc* s_cred = reinterpret_cast<Acc*>(dyn_smem + (size_t)kWarps * NS * CW * sizeof(TM));
+    // Mixed mode: per-tile column and row parameters (FP32 splits), double
+    // buffered and prefetched one tile ahead with bulk copies.
+    constexpr size_t kCredBytes = (size_t)NCa * (kWarps / 2) * CW * sizeof(Acc);
+    float4* s_colp = reinterpret_cast<float4*>(dyn_smem + (size_t)kWarps * NS * CW * sizeof(TM) +
+                                               (NC > 0 ? kCredBytes : 0));  // [2][CW]
+    float4* s_rowp = s_colp + 2 * CW;                                      // [2][kRB]
+    float* s_cdp = reinterpret_cast<float*>(s_rowp + 2 * kRB);             // [2][CW] (LS only)
+    __shared__ __align__(8) uint64_t s_bar[kWarps][NS];
+    __shared__ __align__(8) uint64_t s_pbar[2];
+    constexpr bool STAGE_PARAMS = MIXED && !COLROOT;
+
+    if (lane == 0)
+        for (int s = 0; s < NS; ++s) mbar_init(&s_bar[warp][s], 1);
+    if (STAGE_PARAMS && threadIdx.x == 0) {
+        mbar_init(&s_pbar[0], 1);
+        mbar_init(&s_pbar[1], 1);
+    }
+    __syncthreads();
+    // Issue the parameter copies of tile number kk (of this CTA) into buffer kk % 2.
+    auto issue_params = [&](int kk) {
+        const int t = (int)blockIdx.x + kk * (int)gridDim.x;
+        const int slab = t % nslabs, rb = t / nslabs;
+        const int c0 = slab * CW, r0 = rb * kRB;
+        const int ncol = (m - c0) < CW ? (m - c0) : CW;
+        const int nrow = (n - r0) < kRB ? (n - r0) : kRB;
+        uint64_t* bar = &s_pbar[kk & 1];
+        const bool want_cd = op_uses_cd(OP) && p.cdsplit != nullptr;
+        // 16-byte multiples: float4 entries always; cd floats in groups of 4
+        const int ncd = want_cd ? (ncol / 4) * 4 : 0;
+        const uint32_t bytes = (p.csplit ? (uint32_t)ncol * 16u : 0u) +
+                               (p.rsplit ? (uint32_t)nrow * 16u : 0u) + (uint32_t)ncd * 4u;
+        mbar_arrive_expect_tx(bar, bytes);
+        if (p.csplit) bulk_g2s(s_colp + (kk & 1) * CW, p.csplit + c0, (uint32_t)ncol * 16u, bar);
+        if (p.rsplit) bulk_g2s(s_rowp + (kk & 1) * kRB, p.rsplit + r0, (uint32_t)nrow * 16u, bar);
+        if (ncd) bulk_g2s(s_cdp + (kk & 1) * CW, p.cdsplit + c0, (uint32_t)ncd * 4u, bar);
+    };
+    if (STAGE_PARAMS && threadIdx.x == 0) {
+        if (my_tiles > 0) issue_params(0);
+        if (my_tiles > 1) issue_params(1);
+    }
+
+    // Producer cursor (lane 0): the next row to issue, advanced in order.
+    const int total = my_tiles * RPW;  // rows this warp streams
+    int pk = 0, pu = 0;                // tile counter, row within the tile
+    long long prow = 0;                // first row of this warp in the current tile
+    const TM* psrc = nullptr;          // &M[prow, c0]
+    uint32_t pseg = 0;                 // row segment bytes of the tile's slab
+    auto cursor_tile = [&]() {
+        const int t = (int)blockIdx.x + pk * (int)gridDim.x;
+        const int slab = t % nslabs, rb = t / nslabs;
+        const long long c0 = (long long)slab * CW;
+        prow = (long long)rb * kRB + rw0;
+        psrc = Mb + prow * ldm + c0;
+        pseg = (uint32_t)((ldm - c0) < CW ? (ldm - c0) : CW) * (uint32_t)sizeof(TM);
+    };
+    auto issue = [&](int q) {  // row q of this warp == (pk, pu)
+        uint64_t* bar = &s_bar[warp][q % NS];
+        const bool valid = prow + pu < n;
+        mbar_arrive_expect_tx(bar, valid ? pseg : 0u);
+        if (valid) bulk_g2s(ring + (size_t)(q % NS) * CW, psrc + (long long)pu * ldm, pseg, bar);
+        if (++pu == RPW) {
+            pu = 0;
+            if (++pk < my_tiles) cursor_tile();
+        }
+    };
+    if (lane == 0 && total > 0) {
+        cursor_tile();
+        for (int q = 0; q < NS && q < total; ++q) issue(q);
+    }
 
     // Constants prepared on the host (no FP64 arithmetic in this kernel:
     // FP64 throughput on this part is a small fraction of FP32).
-    const double reg = p.reg;
     const TM kexp = MIXED ? (TM)p.kexp_f : (TM)p.kexp_d;
     const TM inv_reg = MIXED ? (TM)p.inv_reg_f : (TM)p.inv_reg_d;
-
-    // ---- per-row parameters, staged once per CTA in shared memory ----
-    __shared__ TM s_rh[kRB], s_rl[kRB], s_rx[kRB], s_rd[kRB];
-    __shared__ double s_rad[COLROOT ? kRB : 1];
-    if (threadIdx.x < kRB) {
-        const int i = r0 + threadIdx.x;
-        const bool ok = i < n;
-        if constexpr (MIXED) {
-            const float4 v = (ok && p.rsplit) ? p.rsplit[i] : make_float4(0.f, 0.f, 0.f, 0.f);
-            s_rh[threadIdx.x] = v.x;
-            s_rl[threadIdx.x] = v.y;
-            s_rx[threadIdx.x] = v.z;
-            s_rd[threadIdx.x] = v.w;
-        } else {
-            s_rh[threadIdx.x] = (ok && p.ra && op_needs_ra(OP)) ? (TM)p.ra[i] : (TM)0;
-            s_rl[threadIdx.x] = 0;
-            s_rx[threadIdx.x] = (ok && p.rx) ? (TM)p.rx[i] : (TM)0;
-            s_rd[threadIdx.x] = (ok && p.rd) ? (TM)p.rd[i] : (TM)0;
-        }
-        if constexpr (COLROOT) s_rad[threadIdx.x] = (ok && p.ra) ? p.ra[i] : 0.0;
-    }
-
-    // ---- per-column parameters in registers ----
-    TM ch[LC], cl[LC], cxv[LC], cx2v[LC], cdv[LC];
-    double cbd[COLROOT ? LC : 1];
-    bool cvalid[LC];
-#pragma unroll
-    for (int k = 0; k < LC; ++k) {
-        const int v = k / VW, e = k % VW;
-        const int j = c0 + (v * 32 + lane) * VW + e;
-        const bool ok = j < m;
-        cvalid[k] = ok;
-        if constexpr (COLROOT) cbd[k] = ok ? p.cb[j] : -INFINITY;
-        if constexpr (MIXED) {
-            const float4 c = (ok && p.csplit) ? p.csplit[j] : make_float4(0.f, 0.f, 0.f, 0.f);
-            ch[k] = ok ? c.x : -INFINITY;
-            cl[k] = ok ? c.y : 0.f;
-            cxv[k] = c.z;
-            cx2v[k] = c.w;
-            cdv[k] = (ok && p.cdsplit) ? p.cdsplit[j] : 0.f;
-        } else {
-            ch[k] = ok ? ((p.cb && op_needs_cb(OP)) ? (TM)p.cb[j] : (TM)0) : (TM)(-INFINITY);
-            cl[k] = 0;
-            cxv[k] = (ok && p.cx) ? (TM)p.cx[j] : (TM)0;
-            cx2v[k] = (ok && p.cx2) ? (TM)p.cx2[j] : (TM)0;
-            cdv[k] = (ok && p.cd) ? (TM)p.cd[j] : (TM)0;
-        }
-    }
-    __syncthreads();
-
     const TM init = ISMAX ? (TM)(-INFINITY) : (TM)0;
-    Acc cacc[NCa][LC];
-#pragma unroll
-    for (int c = 0; c < NCa; ++c)
-#pragma unroll
-        for (int k = 0; k < LC; ++k) cacc[c][k] = (Acc)init;
-    Acc tot[NTa];
-#pragma unroll
-    for (int t = 0; t < NTa; ++t) tot[t] = 0;
-
     TM steps[4];
 #pragma unroll
     for (int t = 0; t < 4; ++t) steps[t] = (TM)p.steps[t];
     const int nsteps = p.nsteps;
 
-    const TM* Mbase = reinterpret_cast<const TM*>(p.M);
-    const int rw0 = warp * RPW;
+    Acc tot[NTa];
+#pragma unroll
+    for (int t = 0; t < NTa; ++t) tot[t] = 0;
+    bool ok_wait = true;
 
 #pragma unroll 1
-    for (int u0 = 0; u0 < RPW; u0 += 4) {
-        VT mv[4][2];
+    for (int k = 0; k < my_tiles; ++k) {
+        const int t = (int)blockIdx.x + k * (int)gridDim.x;
+        const int slab = t % nslabs, rb = t / nslabs;
+        const int c0 = slab * CW, r0 = rb * kRB;
+        const int seg = (int)((ldm - c0) < CW ? (ldm - c0) : CW);
+
+        if constexpr (STAGE_PARAMS) {
+            const bool got = mbar_wait_bounded(&s_pbar[k & 1], (uint32_t)((k >> 1) & 1), p.err);
+            ok_wait = ok_wait && got;
+        }
+        // ---- per-column parameters of this slab (only what OP uses) ----
+        TM ch[LC], clk[LC], cxv[op_uses_cx(OP) ? LC : 1], cx2v[op_uses_cx2(OP) ? LC : 1],
+            cdv[op_uses_cd(OP) ? LC : 1];
+        double cbd[COLROOT ? LC : 1];
+        bool cvalid[LC];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const int i = r0 + rw0 + u0 + u;
-#pragma unroll
-            for (int v = 0; v < 2; ++v) {
-                const long long col = c0 + (long long)(v * 32 + lane) * VW;
-                if (i < n && col < ldm)
-                    mv[u][v] = *reinterpret_cast<const VT*>(Mbase + (long long)i * ldm + col);
-                else
-                    mv[u][v] = Vec<TM>::zero();
+        for (int q = 0; q < LC; ++q) {
+            const int v = q / VW, e = q % VW;
+            const int j = c0 + (v * 32 + lane) * VW + e;
+            const bool ok = j < m;
+            cvalid[q] = ok;
+            if constexpr (COLROOT) {
+                cbd[q] = ok ? p.cb[j] : -INFINITY;
+                ch[q] = 0;
+                clk[q] = 0;
+            } else if constexpr (MIXED) {
+                const float4 c = (ok && p.csplit) ? s_colp[(k & 1) * CW + (j - c0)]
+                                                  : make_float4(0.f, 0.f, 0.f, 0.f);
+                ch[q] = ok ? c.x : -INFINITY;
+                // EROT folds the exp2 scale into the low part: lo * kexp.
+                clk[q] = ok ? (EROT ? c.y * kexp : c.y) : 0.f;
+                if constexpr (op_uses_cx(OP)) cxv[q] = c.z;
+                if constexpr (op_uses_cx2(OP)) cx2v[q] = c.w;
+                if constexpr (op_uses_cd(OP)) {
+                    // entries past the last group of four were not staged
+                    const int jj = j - c0;
+                    const int ncol = (m - c0) < CW ? (m - c0) : CW;
+                    cdv[q] = (ok && p.cdsplit)
+                                 ? (jj < (ncol / 4) * 4 ? s_cdp[(k & 1) * CW + jj] : p.cdsplit[j])
+                                 : 0.f;
+                }
+            } else {
+                ch[q] = ok ? ((p.cb && op_needs_cb(OP)) ? (TM)p.cb[j] : (TM)0) : (TM)(-INFINITY);
+                clk[q] = 0;
+                if constexpr (op_uses_cx(OP)) cxv[q] = (ok && p.cx) ? (TM)p.cx[j] : (TM)0;
+                if constexpr (op_uses_cx2(OP)) cx2v[q] = (ok && p.cx2) ? (TM)p.cx2[j] : (TM)0;
+                if constexpr (op_uses_cd(OP)) cdv[q] = (ok && p.cd) ? (TM)p.cd[j] : (TM)0;
             }
         }
+        Acc cacc[NCa][LC];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const int li = rw0 + u0 + u;
-            const int i = r0 + li;
-            if (i >= n) break;
-            const TM rh = s_rh[li], rl = s_rl[li], rxv = s_rx[li], rdv = s_rd[li];
-            const double rad = COLROOT ? s_rad[COLROOT ? li : 0] : 0.0;
-            Acc racc[NRa];
+        for (int c = 0; c < NCa; ++c)
 #pragma unroll
-            for (int r = 0; r < NRa; ++r) racc[r] = (Acc)init;
-            uint32_t bits = 0;  // for OP_Q_GRADMASK: one word per column slot
-            (void)bits;
+            for (int q = 0; q < LC; ++q) cacc[c][q] = (Acc)init;
+        // Per-lane partials of the warp's RPW rows of this tile.
+        Acc rowv[NRa][RPW];
+#pragma unroll
+        for (int rr = 0; rr < NRa; ++rr)
+#pragma unroll
+            for (int u = 0; u < RPW; ++u) rowv[rr][u] = (Acc)init;
 
+        // Rows are processed in pairs: both waits and both shared-memory
+        // loads come first, so the two rows' element chains interleave.
 #pragma unroll
-            for (int k = 0; k < LC; ++k) {
-                const TM mval = Vec<TM>::get(mv[u][k / VW], k % VW);
-                if constexpr (OP == OP_E_ROWMAX) {
-                    TM a;
-                    if constexpr (MIXED) a = (ch[k] - mval) + cl[k];
-                    else a = ch[k] - mval;
-                    racc[0] = fmax(racc[0], a);
-                } else if constexpr (OP == OP_E_COLMAX) {
-                    TM a;
-                    if constexpr (MIXED) a = (rh - mval) + rl;
-                    else a = rh - mval;
-                    if (cvalid[k]) cacc[0][k] = fmax(cacc[0][k], (Acc)a);
-                } else if constexpr (COLROOT) {
-                    const double y = (double)mval - rad;
-                    if (cvalid[k] && y < cbd[k]) {
-                        cacc[0][k] += 1.0;
-                        cacc[1][k] += y;
-                    }
-                } else {
-                    TM arg;
-                    if constexpr (MIXED) arg = ((rh + ch[k]) - mval) + (rl + cl[k]);
-                    else arg = (rh + ch[k]) - mval;
-                    if constexpr (EROT) {
-                        TM T;
-                        if constexpr (MIXED) T = ex2_approx(arg * kexp);
-                        else T = exp(arg * kexp);
-                        if constexpr (OP == OP_E_ROW) {
-                            racc[0] += T;
-                        } else if constexpr (OP == OP_E_COL) {
-                            cacc[0][k] += T;
-                        } else if constexpr (OP == OP_E_ROWCOL) {
-                            racc[0] += T;
-                            cacc[0][k] += T;
-                        } else if constexpr (OP == OP_E_HVP) {
-                            racc[0] += T * cxv[k];
-                            cacc[0][k] += T * rxv;
-                        } else if constexpr (OP == OP_E_LS) {
-                            const TM w = (rdv + cdv[k]) * inv_reg;
+        for (int u2 = 0; u2 < RPW; u2 += 2) {
+            VT mvp[2][NV];
+            TM prh[2], prlk[2], prx[2], prd[2];
+            double prad[2];
 #pragma unroll
-                            for (int t = 0; t < 4; ++t)
-                                if (t < nsteps) tot[t] += T * expm1(steps[t] * w);
-                        } else if constexpr (OP == OP_E_PLAN) {
-                            if (cvalid[k]) {
-                                const int j = c0 + ((k / VW) * 32 + lane) * VW + (k % VW);
-                                p.out[(long long)i * m + j] = (double)T;
-                            }
-                        }
+            for (int r2 = 0; r2 < 2; ++r2) {
+                const int u = u2 + r2;
+                const int qs = k * RPW + u;
+                const int i = r0 + rw0 + u;
+                prh[r2] = 0;
+                prlk[r2] = 0;
+                prx[r2] = 0;
+                prd[r2] = 0;
+                prad[r2] = 0.0;
+#pragma unroll
+                for (int v = 0; v < NV; ++v) mvp[r2][v] = Vec<TM>::zero();
+                if (i < n) {
+                    if constexpr (COLROOT) {
+                        prad[r2] = p.ra ? p.ra[i] : 0.0;
+                    } else if constexpr (MIXED) {
+                        const float4 r = p.rsplit ? s_rowp[(k & 1) * kRB + (i - r0)]
+                                                  : make_float4(0.f, 0.f, 0.f, 0.f);
+                        prh[r2] = r.x;
+                        prlk[r2] = EROT ? r.y * kexp : r.y;
+                        prx[r2] = r.z;
+                        prd[r2] = r.w;
                     } else {
-                        const TM D = arg > (TM)0 ? arg : (TM)0;
-                        if constexpr (OP == OP_Q_GRAD) {
-                            racc[0] += D;
-                            cacc[0][k] += D;
-                            tot[0] += D * D;
-                        } else if constexpr (OP == OP_Q_GRADMASK) {
-                            const bool pos = arg > (TM)0;
-                            racc[0] += D;
-                            cacc[0][k] += D;
-                            tot[0] += D * D;
-                            racc[1] += pos ? (TM)1 : (TM)0;
-                            cacc[1][k] += pos ? (TM)1 : (TM)0;
-                            const uint32_t word = __ballot_sync(0xffffffffu, pos);
-                            if (lane == k) bits = word;
-                        } else if constexpr (OP == OP_Q_OBJ) {
-                            tot[0] += D * D;
-                        } else if constexpr (OP == OP_Q_P1) {
-                            racc[0] += D;
-                        } else if constexpr (OP == OP_Q_P2) {
-                            cacc[0][k] += D * rxv;
-                        } else if constexpr (OP == OP_Q_P3) {
-                            const TM Dy = D * cxv[k];
-                            racc[0] += Dy;
-                            racc[1] += Dy * cx2v[k];
-                            racc[2] += mval * cx2v[k];
-                            const TM R = rxv * Dy;
-                            tot[0] += R * mval;
-                            tot[1] += R * R;
-                        } else if constexpr (OP == OP_Q_PLAN) {
-                            if (cvalid[k]) {
-                                const int j = c0 + ((k / VW) * 32 + lane) * VW + (k % VW);
-                                p.out[(long long)i * m + j] = (double)D * p.inv_reg_d;
-                            }
-                        }
+                        prh[r2] = (p.ra && op_needs_ra(OP)) ? (TM)p.ra[i] : (TM)0;
+                        if constexpr (op_uses_rx(OP)) prx[r2] = p.rx ? (TM)p.rx[i] : (TM)0;
+                        if constexpr (op_uses_rd(OP)) prd[r2] = p.rd ? (TM)p.rd[i] : (TM)0;
+                    }
+                    // Every row with data is waited for (bounded), even after
+                    // a timeout, so no copy is left in flight when the CTA exits.
+                    const bool arrived = mbar_wait_bounded(&s_bar[warp][qs % NS],
+                                                           (uint32_t)((qs / NS) & 1), p.err);
+                    ok_wait = ok_wait && arrived;
+                    const TM* buf = ring + (size_t)(qs % NS) * CW;
+#pragma unroll
+                    for (int v = 0; v < NV; ++v) {
+                        const int off = (v * 32 + lane) * VW;
+                        if (ok_wait && off < seg)
+                            mvp[r2][v] = *reinterpret_cast<const VT*>(buf + off);
                     }
                 }
             }
-            if constexpr (OP == OP_Q_GRADMASK) {
-                if (lane < LC) p.bitmask[((long long)i * nslabs + slab) * LC + lane] = bits;
+#pragma unroll
+            for (int r2 = 0; r2 < 2; ++r2) {
+                const int u = u2 + r2;
+                const int i = r0 + rw0 + u;
+                if (i >= n) continue;
+                const TM rh = prh[r2], rlk = prlk[r2], rxv = prx[r2], rdv = prd[r2];
+                const double rad = prad[r2];
+                (void)rxv;
+                (void)rdv;
+                (void)rad;
+                const VT(&mv)[NV] = mvp[r2];
+                    Acc racc[NRa];
+    #pragma unroll
+                    for (int rr = 0; rr < NRa; ++rr) racc[rr] = (Acc)init;
+                    uint32_t bits = 0;
+                    (void)bits;
+                    constexpr bool PAIRED = MIXED && (OP == OP_E_ROW || OP == OP_E_COL ||
+                                                      OP == OP_E_ROWCOL || OP == OP_E_HVP);
+                    if constexpr (PAIRED) {
+                        // Two columns per instruction with the packed FP32x2
+                        // arithmetic of sm_100+: same roundings as the scalar path.
+                        const float2 rh2 = make_float2(rh, rh), rl2 = make_float2(rlk, rlk);
+                        const float2 k2 = make_float2(kexp, kexp), neg1 = make_float2(-1.f, -1.f);
+                        float2 racc2 = make_float2(0.f, 0.f);
+    #pragma unroll
+                        for (int q = 0; q < LC; q += 2) {
+                            const float2 mv2 = make_float2(Vec<TM>::get(mv[q / VW], q % VW),
+                                                           Vec<TM>::get(mv[q / VW], (q + 1) % VW));
+                            float2 sv = __fadd2_rn(rh2, make_float2(ch[q], ch[q + 1]));
+                            sv = __ffma2_rn(mv2, neg1, sv);  // (hi_i + hi_j) - M_ij, one rounding
+                            const float2 lo = __fadd2_rn(rl2, make_float2(clk[q], clk[q + 1]));
+                            const float2 z = __ffma2_rn(sv, k2, lo);
+                            const float2 T = make_float2(ex2_approx(z.x), ex2_approx(z.y));
+                            if constexpr (OP == OP_E_ROW || OP == OP_E_ROWCOL) {
+                                racc2 = __fadd2_rn(racc2, T);
+                            }
+                            if constexpr (OP == OP_E_COL || OP == OP_E_ROWCOL) {
+                                const float2 c = __fadd2_rn(make_float2(cacc[0][q], cacc[0][q + 1]), T);
+                                cacc[0][q] = c.x;
+                                cacc[0][q + 1] = c.y;
+                            }
+                            if constexpr (OP == OP_E_HVP) {
+                                racc2 = __ffma2_rn(T, make_float2(cxv[q], cxv[q + 1]), racc2);
+                                const float2 c = __ffma2_rn(T, make_float2(rxv, rxv),
+                                                            make_float2(cacc[0][q], cacc[0][q + 1]));
+                                cacc[0][q] = c.x;
+                                cacc[0][q + 1] = c.y;
+                            }
+                        }
+                        racc[0] = racc2.x + racc2.y;
+                    }
+    #pragma unroll
+                    for (int q = 0; q < (PAIRED ? 0 : LC); ++q) {
+                        const TM mval = Vec<TM>::get(mv[q / VW], q % VW);
+                        if constexpr (OP == OP_E_ROWMAX) {
+                            TM a;
+                            if constexpr (MIXED) a = (ch[q] - mval) + clk[q] * (TM)p.inv_kexp_f;
+                            else a = ch[q] - mval;
+                            racc[0] = fmax(racc[0], a);
+                        } else if constexpr (OP == OP_E_COLMAX) {
+                            TM a;
+                            if constexpr (MIXED) a = (rh - mval) + rlk * (TM)p.inv_kexp_f;
+                            else a = rh - mval;
+                            if (cvalid[q]) cacc[0][q] = fmax(cacc[0][q], (Acc)a);
+                        } else if constexpr (COLROOT) {
+                            const double y = (double)mval - rad;
+                            if (cvalid[q] && y < cbd[q]) {
+                                cacc[0][q] += 1.0;
+                                cacc[1][q] += y;
+                            }
+                        } else if constexpr (EROT) {
+                            // T = 2^((ra_i + cb_j - M_ij) log2(e) / reg): exact hi sum,
+                            // then (hi - M) * k + (lo_i + lo_j) * k in one FMA.
+                            TM T;
+                            if constexpr (MIXED) {
+                                const TM s = (rh + ch[q]) - mval;
+                                T = ex2_approx(fmaf(s, kexp, rlk + clk[q]));
+                            } else {
+                                T = exp(((rh + ch[q]) - mval) * kexp);
+                            }
+                            if constexpr (OP == OP_E_ROW) {
+                                racc[0] += T;
+                            } else if constexpr (OP == OP_E_COL) {
+                                cacc[0][q] += T;
+                            } else if constexpr (OP == OP_E_ROWCOL) {
+                                racc[0] += T;
+                                cacc[0][q] += T;
+                            } else if constexpr (OP == OP_E_HVP) {
+                                racc[0] += T * cxv[q];
+                                cacc[0][q] += T * rxv;
+                            } else if constexpr (OP == OP_E_LS) {
+                                const TM w = (rdv + cdv[q]) * inv_reg;
+    #pragma unroll
+                                for (int s2 = 0; s2 < 4; ++s2)
+                                    if (s2 < nsteps) tot[s2] += T * expm1(steps[s2] * w);
+                            } else if constexpr (OP == OP_E_PLAN) {
+                                if (cvalid[q]) {
+                                    const int j = c0 + ((q / VW) * 32 + lane) * VW + (q % VW);
+                                    p.out[(long long)i * m + j] = (double)T;
+                                }
+                            }
+                        } else {
+                            TM arg;
+                            if constexpr (MIXED) arg = ((rh + ch[q]) - mval) + (rlk + clk[q]);
+                            else arg = (rh + ch[q]) - mval;
+                            const TM D = arg > (TM)0 ? arg : (TM)0;
+                            if constexpr (OP == OP_Q_GRAD) {
+                                racc[0] += D;
+                                cacc[0][q] += D;
+                                tot[0] += D * D;
+                            } else if constexpr (OP == OP_Q_GRADMASK) {
+                                const bool pos = arg > (TM)0;
+                                racc[0] += D;
+                                cacc[0][q] += D;
+                                tot[0] += D * D;
+                                racc[1] += pos ? (TM)1 : (TM)0;
+                                cacc[1][q] += pos ? (TM)1 : (TM)0;
+                                const uint32_t word = __ballot_sync(0xffffffffu, pos);
+                                if (lane == q) bits = word;
+                            } else if constexpr (OP == OP_Q_OBJ) {
+                                tot[0] += D * D;
+                            } else if constexpr (OP == OP_Q_P1) {
+                                racc[0] += D;
+                            } else if constexpr (OP == OP_Q_P2) {
+                                cacc[0][q] += D * rxv;
+                            } else if constexpr (OP == OP_Q_P3) {
+                                const TM Dy = D * cxv[q];
+                                racc[0] += Dy;
+                                racc[1] += Dy * cx2v[q];
+                                racc[2] += mval * cx2v[q];
+                                const TM R = rxv * Dy;
+                                tot[0] += R * mval;
+                                tot[1] += R * R;
+                            } else if constexpr (OP == OP_Q_PLAN) {
+                                if (cvalid[q]) {
+                                    const int j = c0 + ((q / VW) * 32 + lane) * VW + (q % VW);
+                                    p.out[(long long)i * m + j] = (double)D * p.inv_reg_d;
+                                }
+                            }
+                        }
+                    }
+                    if constexpr (OP == OP_Q_GRADMASK) {
+                        if (lane < LC) p.bitmask[((long long)i * nslabs + slab) * LC + lane] = bits;
+                    }
+
+#pragma unroll
+                for (int rr = 0; rr < NR; ++rr) rowv[rr][u] = racc[rr];
             }
-            if constexpr (NR > 0) {
+            // Both buffers are free once every lane has read them: order those
+            // generic-proxy reads before the async-proxy refills.
+            __syncwarp();
+            if (lane == 0) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 #pragma unroll
-                for (int r = 0; r < NR; ++r) {
-                    racc[r] = ISMAX ? warp_max(racc[r]) : warp_sum(racc[r]);
-                }
-                if (lane == 0) {
-                    Acc* rp = reinterpret_cast<Acc*>(p.rowpart);
-#pragma unroll
-                    for (int r = 0; r < NR; ++r) rp[((long long)r * nslabs + slab) * n + i] = racc[r];
+                for (int r2 = 0; r2 < 2; ++r2) {
+                    const int qs = k * RPW + u2 + r2;
+                    if (qs + NS < total) issue(qs + NS);
                 }
             }
         }
-    }
 
-    // ---- column partials: reduce the 8 warps through shared memory ----
-    if constexpr (NC > 0) {
-        __shared__ Acc s_c[NC][kWarps][CW];
+        // ---- row partials of this tile ----
+        if constexpr (NR > 0) {
+            Acc* rp = reinterpret_cast<Acc*>(p.rowpart);
+            const int i = r0 + rw0 + (lane >> (5 - LOGR));
 #pragma unroll
-        for (int c = 0; c < NC; ++c)
-#pragma unroll
-            for (int k = 0; k < LC; ++k) {
-                const int off = (k / VW) * 32 * VW + lane * VW + (k % VW);
-                s_c[c][warp][off] = cacc[c][k];
+            for (int rr = 0; rr < NR; ++rr) {
+                const Acc tot_r = warp_reduce_rows<ISMAX, RPW>(rowv[rr], lane);
+                if ((lane & ((1 << (5 - LOGR)) - 1)) == 0 && i < n)
+                    rp[((long long)rr * nslabs + slab) * n + i] = tot_r;
             }
-        __syncthreads();
-        Acc* cp = reinterpret_cast<Acc*>(p.colpart);
-        for (int t = threadIdx.x; t < CW; t += kThreads) {
-            const int j = c0 + t;
-            if (j >= m) continue;
+        }
+
+        // ---- column partials of this tile: reduce the warps through a
+        // buffer of half of them (upper half stores, lower half adds) ----
+        if constexpr (NC > 0) {
+            constexpr int HW = kWarps / 2;
+            if (warp >= HW) {
 #pragma unroll
-            for (int c = 0; c < NC; ++c) {
-                Acc s = s_c[c][0][t];
+                for (int c = 0; c < NC; ++c)
 #pragma unroll
-                for (int w = 1; w < kWarps; ++w) s = ISMAX ? fmax(s, s_c[c][w][t]) : s + s_c[c][w][t];
-                cp[((long long)c * nrb + rb) * m + j] = s;
+                    for (int q = 0; q < LC; ++q) {
+                        const int off = (q / VW) * 32 * VW + lane * VW + (q % VW);
+                        s_cred[((size_t)c * HW + (warp - HW)) * CW + off] = cacc[c][q];
+                    }
+            }
+            __syncthreads();
+            if (warp < HW) {
+#pragma unroll
+                for (int c = 0; c < NC; ++c)
+#pragma unroll
+                    for (int q = 0; q < LC; ++q) {
+                        const int off = (q / VW) * 32 * VW + lane * VW + (q % VW);
+                        Acc& slot = s_cred[((size_t)c * HW + warp) * CW + off];
+                        slot = ISMAX ? fmax(slot, cacc[c][q]) : slot + cacc[c][q];
+                    }
+            }
+            __syncthreads();
+            Acc* cp = reinterpret_cast<Acc*>(p.colpart);
+            for (int tt = threadIdx.x; tt < CW; tt += kThreads) {
+                const int j = c0 + tt;
+                if (j >= m) continue;
+#pragma unroll
+                for (int c = 0; c < NC; ++c) {
+                    Acc s = s_cred[((size_t)c * HW + 0) * CW + tt];
+#pragma unroll
+                    for (int w = 1; w < HW; ++w) {
+                        const Acc x = s_cred[((size_t)c * HW + w) * CW + tt];
+                        s = ISMAX ? fmax(s, x) : s + x;
+                    }
+                    cp[((long long)c * nrb + rb) * m + j] = s;
+                }
+            }
+            __syncthreads();
+        }
+        if constexpr (STAGE_PARAMS) {
+            // Every warp is done with this tile's parameter buffer: refill it.
+            if constexpr (NC == 0) __syncthreads();
+            if (threadIdx.x == 0 && k + 2 < my_tiles) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                issue_params(k + 2);
             }
         }
     }
@@ -370,7 +685,7 @@ __global__ void __launch_bounds__(kThreads) dense_pass(const PassParams p) {
             double s = 0.0;
 #pragma unroll
             for (int w = 0; w < kWarps; ++w) s += s_t[threadIdx.x][w];
-            p.totpart[(long long)threadIdx.x * (nslabs * nrb) + rb * nslabs + slab] = s;
+            p.totpart[(long long)threadIdx.x * gridDim.x + blockIdx.x] = s;
         }
     }
 }
@@ -403,12 +718,54 @@ __global__ void k_split(const PassParams p, float4* rs, float4* cs, float* cds) 
 
 template <typename TM, int OP>
 void launch_one(const PassParams& p, cudaStream_t st) {
+    using Acc = typename std::conditional<OP == OP_Q_COLROOT, double, TM>::type;
+    constexpr int CW = Geo<TM>::CW;
+    constexpr int NS = ring_stages<OP, Acc, CW>();
+    constexpr size_t smem = (size_t)kWarps * NS * CW * sizeof(TM) +
+                            (size_t)(op_nc(OP) > 0 ? op_nc(OP) : 0) * (kWarps / 2) * CW * sizeof(Acc) +
+                            2 * ((size_t)CW * 16 + (size_t)kRB * 16 +
+                                 (op_uses_cd(OP) ? (size_t)CW * 4 : 0));
+    static unsigned long long configured = 0;  // per instantiation, one bit per device
+    int dev = 0;
+    REGOT_CUDA(cudaGetDevice(&dev));
+    if (dev >= 64 || !(configured & (1ULL << dev))) {
+        REGOT_CUDA(cudaFuncSetAttribute(dense_pass<TM, OP>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        if (dev < 64) configured |= (1ULL << dev);
+    }
     const PassShape s = pass_shape<TM>(p.n, p.m);
-    dim3 grid(s.nslabs, s.nrb);
-    dense_pass<TM, OP><<<grid, kThreads, 0, st>>>(p);
+    const int blocks = pass_blocks(OP, std::is_same<TM, float>::value, p.n, p.m);
+    (void)s;
+    dense_pass<TM, OP><<<blocks, kThreads, smem, st>>>(p);
     REGOT_CHECK_LAUNCH();
     count_launch();
 }
+
+template <typename TM, int OP>
+int occupancy_of() {
+    using Acc = typename std::conditional<OP == OP_Q_COLROOT, double, TM>::type;
+    constexpr int CW = Geo<TM>::CW;
+    constexpr int NS = ring_stages<OP, Acc, CW>();
+    constexpr size_t smem = (size_t)kWarps * NS * CW * sizeof(TM) +
+                            (size_t)(op_nc(OP) > 0 ? op_nc(OP) : 0) * (kWarps / 2) * CW * sizeof(Acc) +
+                            2 * ((size_t)CW * 16 + (size_t)kRB * 16 +
+                                 (op_uses_cd(OP) ? (size_t)CW * 4 : 0));
+    REGOT_CUDA(cudaFuncSetAttribute(dense_pass<TM, OP>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int occ = 0;
+    REGOT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, dense_pass<TM, OP>, kThreads,
+                                                             smem));
+    return occ > 0 ? (occ < 2 ? occ : 2) : 1;
+}
+
+template <typename TM>
+struct OccTable {
+    template <int OP>
+    static int get(int op) {
+        if constexpr (OP < OP_COUNT) return op == OP ? occupancy_of<TM, OP>() : get<OP + 1>(op);
+        else return 1;
+    }
+};
 
 template <typename TM>
 struct Dispatch {
@@ -430,10 +787,25 @@ void launch_pass(int op, const PassParams& p, cudaStream_t st) {
     if (p.n <= 0 || p.m <= 0) return;
     PassParams q = p;
     q.kexp_f = (float)(1.4426950408889634 / p.reg);
+    q.inv_kexp_f = 1.0f / q.kexp_f;
     q.inv_reg_f = (float)(1.0 / p.reg);
     q.kexp_d = 1.0 / p.reg;
     q.inv_reg_d = 1.0 / p.reg;
     Dispatch<TM>::template go<0>(op, q, st);
+}
+
+int pass_blocks(int op, bool mixed, int n, int m) {
+    int dev = 0;
+    REGOT_CUDA(cudaGetDevice(&dev));
+    static int cache[64][2][OP_COUNT] = {};
+    int occ = (dev < 64 && op >= 0 && op < OP_COUNT) ? cache[dev][mixed][op] : 0;
+    if (!occ) {
+        occ = mixed ? OccTable<float>::get<0>(op) : OccTable<double>::get<0>(op);
+        if (dev < 64 && op >= 0 && op < OP_COUNT) cache[dev][mixed][op] = occ;
+    }
+    const PassShape s = mixed ? pass_shape<float>(n, m) : pass_shape<double>(n, m);
+    const int cap = device_sm_count() * occ;
+    return s.ntiles < cap ? s.ntiles : cap;
 }
 
 void launch_split(const PassParams& p, float4* rs, float4* cs, float* cds, cudaStream_t st) {

@@ -11,8 +11,11 @@ regot = pytest.importorskip("regot")
 
 # FP64 storage: every element-wise operation in FP64 -> agreement to ~1e-12.
 # Mixed: M rounded to FP32 (the oracle sees the same FP32 values), FP32
-# exp2/accumulation -> relative agreement ~1e-5 on plans and sums.
+# exp2/accumulation -> relative agreement ~1e-5 on plans and sums, and
+# marginal errors within FP32 rounding of the row sums (absolute ~1e-9,
+# bounded here by MAR_ATOL).
 TOL = {"fp64": 1e-10, "mixed": 2e-4}
+MAR_ATOL = {"fp64": 1e-12, "mixed": 2e-8}
 
 
 def _problem(kind):
@@ -85,7 +88,8 @@ def test_sinkhorn_bcd_readme(precision, reg):
     else:
         assert abs(r.niter - o.niter) <= max(3, o.niter // 20)
         k = min(len(r.mar_errs), len(o.mar_errs), 20)
-        np.testing.assert_allclose(r.mar_errs[:k], o.mar_errs[:k], rtol=1e-3, atol=1e-9)
+        np.testing.assert_allclose(r.mar_errs[:k], o.mar_errs[:k], rtol=1e-3,
+                                   atol=MAR_ATOL["mixed"])
         np.testing.assert_allclose(r.obj_vals[-1], o.obj_vals[-1], rtol=1e-6)
         np.testing.assert_allclose(r.plan, o.plan, rtol=0, atol=2e-4 * o.plan.max())
     # the returned dual meets the tolerance when checked in FP64 by the oracle
@@ -105,6 +109,6 @@ def test_sinkhorn_bcd_x0_and_max_iter(precision):
     o = O.sinkhorn_bcd(Mq, a, b, reg, tol=1e-12, max_iter=7, x0=x0)
     assert r.niter == o.niter == 7
     rt = 1e-8 if precision == "fp64" else 1e-3
-    np.testing.assert_allclose(r.mar_errs, o.mar_errs, rtol=rt, atol=1e-12)
+    np.testing.assert_allclose(r.mar_errs, o.mar_errs, rtol=rt, atol=MAR_ATOL[precision])
     r0 = regot.sinkhorn_bcd(M, a, b, reg, tol=1e-12, max_iter=0, precision=precision)
     assert r0.niter == 0 and len(r0.mar_errs) == 1
