@@ -62,7 +62,7 @@ enum PassOp : int {
     OP_E_COL,         // column sums of T
     OP_E_ROWCOL,      // row and column sums of T
     OP_E_HVP,         // rows: sum_j T cx_j ; cols: sum_i T rx_i
-    OP_E_LS,          // totals_k: sum T expm1(s_k (rd_i + cd_j)/reg)
+    OP_E_LS,          // totals_k: sum T (e^w - 1 - w), w = s_k (rd_i + cd_j)/reg
     OP_E_PLAN,        // write T
     OP_E_ROWMAX,      // rows: max_j (cb_j - M_ij)
     OP_E_COLMAX,      // cols: max_i (ra_i - M_ij)
@@ -74,6 +74,8 @@ enum PassOp : int {
     OP_Q_P3,          // rows: sum D cx, sum D cx cx2, sum M cx2 ; totals
     OP_Q_PLAN,        // write D / reg
     OP_Q_COLROOT,     // cols: count and sum of y = M - ra below cb (FP64)
+    OP_Q_GRADLS,      // at C + s w (w = rd_i + cd_j): rows/cols sum Dn; totals sum Dn^2,
+                      // sum of 0.5 (Dn^2 - D^2) - s w D (second-order part of the change)
     OP_COUNT
 };
 

@@ -93,6 +93,24 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
     return false;
 }
 
+// e^x - 1 - x without cancellation: the Taylor series x^2/2! + ... + x^9/9!
+// (Horner form) for |x| < 1/2, where its truncation error is below 2^-24
+// relative; expm1(x) - x beyond, where no cancellation occurs.
+template <typename T>
+__device__ __forceinline__ T expm1_minus_x(T x) {
+    if (fabs(x) < (T)0.5) {
+        T p = (T)1 + x / (T)9;
+        p = (T)1 + x / (T)8 * p;
+        p = (T)1 + x / (T)7 * p;
+        p = (T)1 + x / (T)6 * p;
+        p = (T)1 + x / (T)5 * p;
+        p = (T)1 + x / (T)4 * p;
+        p = (T)1 + x / (T)3 * p;
+        return (T)0.5 * x * x * p;
+    }
+    return expm1(x) - x;
+}
+
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll
@@ -125,16 +143,16 @@ template <> struct Vec<double> {
 __host__ __device__ constexpr int op_nr(int op) {
     return op == OP_E_ROW ? 1 : op == OP_E_ROWCOL ? 1 : op == OP_E_HVP ? 1 : op == OP_E_ROWMAX ? 1
          : op == OP_Q_GRAD ? 1 : op == OP_Q_GRADMASK ? 2 : op == OP_Q_P1 ? 1 : op == OP_Q_P3 ? 3
-         : 0;
+         : op == OP_Q_GRADLS ? 1 : 0;
 }
 __host__ __device__ constexpr int op_nc(int op) {
     return op == OP_E_COL ? 1 : op == OP_E_ROWCOL ? 1 : op == OP_E_HVP ? 1 : op == OP_E_COLMAX ? 1
          : op == OP_Q_GRAD ? 1 : op == OP_Q_GRADMASK ? 2 : op == OP_Q_P2 ? 1 : op == OP_Q_COLROOT ? 2
-         : 0;
+         : op == OP_Q_GRADLS ? 1 : 0;
 }
 __host__ __device__ constexpr int op_nt(int op) {
     return op == OP_E_LS ? 4 : op == OP_Q_GRAD ? 1 : op == OP_Q_GRADMASK ? 1 : op == OP_Q_OBJ ? 1
-         : op == OP_Q_P3 ? 2 : 0;
+         : op == OP_Q_P3 ? 2 : op == OP_Q_GRADLS ? 2 : 0;
 }
 __host__ __device__ constexpr bool op_is_max(int op) {
     return op == OP_E_ROWMAX || op == OP_E_COLMAX;
@@ -178,11 +196,15 @@ __host__ __device__ constexpr bool op_uses_cx(int op) {
     return op == OP_E_HVP || op == OP_Q_P3;
 }
 __host__ __device__ constexpr bool op_uses_cx2(int op) { return op == OP_Q_P3; }
-__host__ __device__ constexpr bool op_uses_cd(int op) { return op == OP_E_LS; }
+__host__ __device__ constexpr bool op_uses_cd(int op) {
+    return op == OP_E_LS || op == OP_Q_GRADLS;
+}
 __host__ __device__ constexpr bool op_uses_rx(int op) {
     return op == OP_E_HVP || op == OP_Q_P2 || op == OP_Q_P3;
 }
-__host__ __device__ constexpr bool op_uses_rd(int op) { return op == OP_E_LS; }
+__host__ __device__ constexpr bool op_uses_rd(int op) {
+    return op == OP_E_LS || op == OP_Q_GRADLS;
+}
 
 // Sum (or max) of the per-lane partials of a warp's N rows (N a power of
 // two <= 32): a transposed butterfly whose first log2(N) exchange levels
@@ -541,7 +563,7 @@ __global__ void __launch_bounds__(kThreads, 2) dense_pass(const PassParams p) {
                                 const TM w = (rdv + cdv[q]) * inv_reg;
     #pragma unroll
                                 for (int s2 = 0; s2 < 4; ++s2)
-                                    if (s2 < nsteps) tot[s2] += T * expm1(steps[s2] * w);
+                                    if (s2 < nsteps) tot[s2] += T * expm1_minus_x(steps[s2] * w);
                             } else if constexpr (OP == OP_E_PLAN) {
                                 if (cvalid[q]) {
                                     const int j = c0 + ((q / VW) * 32 + lane) * VW + (q % VW);
@@ -566,7 +588,21 @@ __global__ void __launch_bounds__(kThreads, 2) dense_pass(const PassParams p) {
                                 cacc[1][q] += pos ? (TM)1 : (TM)0;
                                 const uint32_t word = __ballot_sync(0xffffffffu, pos);
                                 if (lane == q) bits = word;
-                            } else if constexpr (OP == OP_Q_OBJ) {
+                            } else if constexpr (OP == OP_Q_GRADLS) {
+                            // objective change along s w without cancellation:
+                            // 0.5 (Dn^2 - D^2) - s w D >= 0 in every case
+                            const TM sw = steps[0] * (rdv + cdv[q]);
+                            const TM Cn = arg + sw;
+                            const TM Dn = Cn > (TM)0 ? Cn : (TM)0;
+                            TM rem;
+                            if (arg > (TM)0) rem = Cn > (TM)0 ? (TM)0.5 * sw * sw
+                                                              : -arg * ((TM)0.5 * arg + sw);
+                            else rem = Cn > (TM)0 ? (TM)0.5 * Cn * Cn : (TM)0;
+                            racc[0] += Dn;
+                            cacc[0][q] += Dn;
+                            tot[0] += Dn * Dn;
+                            tot[1] += rem;
+                        } else if constexpr (OP == OP_Q_OBJ) {
                                 tot[0] += D * D;
                             } else if constexpr (OP == OP_Q_P1) {
                                 racc[0] += D;

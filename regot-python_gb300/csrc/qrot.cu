@@ -1,0 +1,997 @@
+// QROT on the GPU: qrot_lbfgs_dual (reference src/qrot_lbfgs_dual.cpp:81-126)
+// and qrot_assn (src/qrot_assn.cpp:16-170), with the dense passes of
+// src/qrot_problem.cpp and src/qrot_hess.cpp.
+//
+//   grad / obj   one pass: D = (alpha_i + beta_j - M_ij)+, row and column sums
+//                of D and sum D^2 (compute_D_stats, qrot_problem.cpp:36-94).
+//   Jacobian     the same pass also writes sigma = 1[C > 0] as a bitmask
+//                (one bit per entry, 32x smaller than FP32 M and L2-resident
+//                for the benchmark sizes) plus the row/column counts
+//                h1 = sigma 1, h2 = sigma' 1 (compute_D_hess, qrot_hess.cpp:41-96).
+//                sigma x and sigma' y then read the bitmask only.
+//   primal_val   three passes (row sums of P; column sums of P x; per-row
+//                sums of P y, P y f, M f and the totals <R, M>, ||R||^2),
+//                the rank-one correction of approx_proj (approx_proj.h:6-26)
+//                expanded analytically, so no n x m plan is materialised.
+//   optimal_beta per column, Newton's method from above on the convex
+//                piecewise-linear sum_i (x - y_i)+ = reg b_j (y = M_:j - alpha):
+//                x <- (reg b_j + sum_{y_i < x} y_i) / #{y_i < x}, one pass per
+//                step until no active set changes; the fixed point is the root
+//                that piecewise_linear_equation (qrot_problem.cpp:368-392) finds
+//                by sorting.
+// The L-BFGS driver and the ASSN outer loop run on the host in FP64; the
+// ASSN Schur-complement CG (qrot_cg.cpp:9-50: identity preconditioner,
+// relative tolerance 1e-8, at most 2m steps) runs on the device, captured in
+// a CUDA graph.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "device_util.cuh"
+#include "erot_ops.cuh"
+#include "lbfgs.h"
+#include "solvers.h"
+
+namespace regot {
+
+namespace {
+
+constexpr int kVT = 64;           // vector-kernel block size
+constexpr int kColChunks = 32;    // row chunks of the sigma' y kernel
+
+struct QState {
+    unsigned counter;
+    int cg_done;
+    int cg_it;
+    int cg_max;
+    int changed;
+    int pad;
+    double dot_ab;   // alpha' a + beta' b
+    double sum_a;    // 1' alpha
+    double sum_b;    // 1' beta
+    double sq;       // sum D^2
+    double rr;       // CG r'r
+    double alpha;
+    double beta;
+    double thresh2;
+    double prim[6];  // primal-value scalars
+    double maxabs;
+};
+
+// ---- gradient / objective merge ----
+template <typename Acc>
+__global__ void k_q_grad(const Acc* rp, int nslabs, const Acc* cp, int nrb, int n, int m,
+                         int with_counts, const double* gamma, const double* a, const double* b,
+                         double reg, double* grad, double* h1, double* h2, double* parts,
+                         QState* st) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[3] = {0.0, 0.0, 0.0};
+    if (t < n) {
+        const double rs = merge_strided(rp + t, nslabs, (size_t)n);
+        grad[t] = rs - reg * a[t];
+        if (with_counts) h1[t] = merge_strided(rp + (size_t)nslabs * n + t, nslabs, (size_t)n);
+        v[0] = gamma[t] * a[t];
+        v[1] = gamma[t];
+    } else if (t < n + m) {
+        const int j = t - n;
+        const double cs = merge_strided(cp + j, nrb, (size_t)m);
+        grad[t] = cs - reg * b[j];
+        if (with_counts) h2[j] = merge_strided(cp + (size_t)nrb * m + j, nrb, (size_t)m);
+        v[0] = gamma[t] * b[j];
+        v[2] = gamma[t];
+    }
+    double out[3];
+    __threadfence();
+    if (grid_reduce<3>(v, parts, &st->counter, out)) {
+        st->dot_ab = out[0];
+        st->sum_a = out[1];
+        st->sum_b = out[2];
+    }
+}
+
+// Sum of one row of per-CTA totals into *out (single block).
+__global__ void k_sum_totals(const double* totpart, int nblocks, double* out) {
+    double v = 0.0;
+    for (int k = threadIdx.x; k < nblocks; k += blockDim.x) v += totpart[k];
+    __shared__ double s[32];
+    v = warp_sum_d(v);
+    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double r = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) r += s[w];
+        *out = r;
+    }
+}
+
+// ---- optimal_beta by Newton's method from above (per column) ----
+__global__ void k_root_init(int m, double* x, double* prev_cnt) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < m) {
+        x[j] = INFINITY;
+        prev_cnt[j] = -1.0;
+    }
+}
+
+__global__ void k_root_update(const double* cp, int nrb, int m, const double* b, double reg,
+                              double* x, double* prev_cnt, QState* st) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= m) return;
+    const double cnt = merge_strided(cp + j, nrb, (size_t)m);
+    const double sum = merge_strided(cp + (size_t)nrb * m + j, nrb, (size_t)m);
+    if (cnt != prev_cnt[j]) {
+        prev_cnt[j] = cnt;
+        x[j] = (reg * b[j] + sum) / cnt;
+        atomicOr(&st->changed, 1);
+    }
+}
+
+// ---- primal value (approx_proj) ----
+// P1 merge: x_i = min(a_i / (rowsum(D)_i / reg), 1)
+template <typename Acc>
+__global__ void k_prim1(const Acc* rp, int nslabs, int n, const double* a, double reg,
+                        double* xr) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) xr[i] = fmin(a[i] / (merge_strided(rp + i, nslabs, (size_t)n) / reg), 1.0);
+}
+// P2 merge: c_j = colsum(D x)/reg; y_j = min(b_j / c_j, 1); f_j = b_j - y_j c_j
+template <typename Acc>
+__global__ void k_prim2(const Acc* cp, int nrb, int m, const double* b, double reg, double* yc,
+                        double* fc, double* parts, QState* st) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[1] = {0.0};
+    if (j < m) {
+        const double c = merge_strided(cp + j, nrb, (size_t)m) / reg;
+        const double y = fmin(b[j] / c, 1.0);
+        const double f = b[j] - y * c;
+        yc[j] = y;
+        fc[j] = f;
+        v[0] = f * f;
+    }
+    double out[1];
+    __threadfence();
+    if (grid_reduce<1>(v, parts, &st->counter, out)) st->prim[0] = out[0];  // ||f||^2
+}
+// P3 merge: e_i = a_i - x_i A_i; sums |e|, e . Cc, x e B, e^2
+template <typename Acc>
+__global__ void k_prim3(const Acc* rp, int nslabs, int n, const double* a, const double* xr,
+                        double reg, double* parts, QState* st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[4] = {0.0, 0.0, 0.0, 0.0};
+    if (i < n) {
+        const double A = merge_strided(rp + i, nslabs, (size_t)n) / reg;
+        const double B = merge_strided(rp + (size_t)nslabs * n + i, nslabs, (size_t)n) / reg;
+        const double Cc = merge_strided(rp + 2 * (size_t)nslabs * n + i, nslabs, (size_t)n);
+        const double e = a[i] - xr[i] * A;
+        v[0] = fabs(e);
+        v[1] = e * Cc;
+        v[2] = xr[i] * e * B;
+        v[3] = e * e;
+    }
+    double out[4];
+    __threadfence();
+    if (grid_reduce<4>(v, parts, &st->counter, out)) {
+        st->prim[1] = out[0];
+        st->prim[2] = out[1];
+        st->prim[3] = out[2];
+        st->prim[4] = out[3];
+    }
+}
+
+// ---- sigma x and sigma' y from the bitmask ----
+// The bitmask follows the dense-pass tiling: for row i and column slab s,
+// LC words; bit L of word q covers column s*CW + ((q/VW)*32 + L)*VW + q%VW.
+template <int CW, int VW, int LC>
+__device__ __forceinline__ int bit_col(int s, int q, int L) {
+    return s * CW + ((q / VW) * 32 + L) * VW + (q % VW);
+}
+
+// out_i = scale_i * sum_j sigma_ij x_j, scale_i = 1 / (h1_i + mu) (or 1).
+template <int CW, int VW, int LC>
+__global__ void k_sigma_rows(const uint32_t* bm, int n, int m, int nslabs, const double* x,
+                             const double* h1, double mu, int divide, double* out, const int* done) {
+    if (done && *done) return;
+    const int lane = threadIdx.x & 31;
+    const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (i >= n) return;
+    double acc = 0.0;
+    const uint32_t* row = bm + (size_t)i * nslabs * LC;
+    for (int s = 0; s < nslabs; ++s) {
+#pragma unroll
+        for (int q = 0; q < LC; ++q) {
+            const uint32_t w = row[s * LC + q];
+            if ((w >> lane) & 1u) {
+                const int j = bit_col<CW, VW, LC>(s, q, lane);
+                acc += x[j];
+            }
+        }
+    }
+    acc = warp_sum_d(acc);
+    if (lane == 0) out[i] = divide ? acc / (h1[i] + mu) : acc;
+}
+
+// partial[c][j] = sum_{i in chunk c} sigma_ij y_i
+template <int CW, int VW, int LC>
+__global__ void k_sigma_cols(const uint32_t* bm, int n, int m, int nslabs, const double* y,
+                             double* partial, const int* done) {
+    if (done && *done) return;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = blockIdx.y;
+    if (j >= m) return;
+    const int s = j / CW, o = j - s * CW;
+    const int L = (o % (32 * VW)) / VW;
+    const int q = (o / (32 * VW)) * VW + (o % VW);
+    const int rows_per = (n + gridDim.y - 1) / gridDim.y;
+    const int i0 = c * rows_per, i1 = min(n, i0 + rows_per);
+    double acc = 0.0;
+    for (int i = i0; i < i1; ++i) {
+        const uint32_t w = bm[((size_t)i * nslabs + s) * LC + q];
+        if ((w >> L) & 1u) acc += y[i];
+    }
+    partial[(size_t)c * m + j] = acc;
+}
+
+// ---- ASSN Schur-complement CG: Delta x = h2 o x + mu x - sigma' ((sigma x) / (h1 + mu)) ----
+__global__ void k_acg_init(int m, const double* zy, double tol, double* x, double* r, double* p,
+                           double* parts, QState* st) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[1] = {0.0};
+    if (j < m) {
+        x[j] = 0.0;
+        r[j] = zy[j];
+        p[j] = zy[j];
+        v[0] = zy[j] * zy[j];
+    }
+    double out[1];
+    __threadfence();
+    if (grid_reduce<1>(v, parts, &st->counter, out)) {
+        st->rr = out[0];
+        st->thresh2 = fmax(tol * tol * out[0], 2.2250738585072014e-308);
+        st->cg_it = 0;
+        st->cg_done = (out[0] == 0.0 || out[0] < st->thresh2) ? 1 : 0;
+    }
+}
+
+__global__ void k_acg_a(int m, const double* partial, int chunks, const double* h2, double mu,
+                        const double* p, double* y, double* parts, QState* st) {
+    if (st->cg_done) return;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[1] = {0.0};
+    if (j < m) {
+        double u = 0.0;
+        for (int c = 0; c < chunks; ++c) u += partial[(size_t)c * m + j];
+        const double yj = h2[j] * p[j] + mu * p[j] - u;
+        y[j] = yj;
+        v[0] = p[j] * yj;
+    }
+    double out[1];
+    __threadfence();
+    if (grid_reduce<1>(v, parts, &st->counter, out)) st->alpha = st->rr / out[0];
+}
+
+__global__ void k_acg_b(int m, const double* p, const double* y, double* x, double* r,
+                        double* parts, QState* st) {
+    if (st->cg_done) return;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const double al = st->alpha;
+    double v[1] = {0.0};
+    if (j < m) {
+        x[j] += al * p[j];
+        const double rj = r[j] - al * y[j];
+        r[j] = rj;
+        v[0] = rj * rj;
+    }
+    double out[1];
+    __threadfence();
+    if (grid_reduce<1>(v, parts, &st->counter, out)) {
+        st->cg_it += 1;
+        if (out[0] < st->thresh2 || st->cg_it >= st->cg_max || !(out[0] == out[0])) {
+            st->cg_done = 1;
+        } else {
+            st->beta = out[0] / st->rr;
+            st->rr = out[0];
+        }
+    }
+}
+
+__global__ void k_acg_c(int m, const double* r, double* p, QState* st) {
+    if (st->cg_done) return;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < m) p[j] = r[j] + st->beta * p[j];
+}
+
+// w / (h1 + mu) for the Schur right-hand side
+__global__ void k_div_h1(int n, const double* w, const double* h1, double mu, double* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = w[i] / (h1[i] + mu);
+}
+// zy_j = rhs_j - sum_c partial[c][j]
+__global__ void k_sub_partial(int m, const double* rhs, const double* partial, int chunks,
+                              double* out) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= m) return;
+    double u = 0.0;
+    for (int c = 0; c < chunks; ++c) u += partial[(size_t)c * m + j];
+    out[j] = rhs[j] - u;
+}
+// r1_i = (w_i - (sigma r2)_i) / (h1_i + mu)
+__global__ void k_backsub(int n, const double* w, const double* sr2, const double* h1, double mu,
+                          double* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = (w[i] - sr2[i]) / (h1[i] + mu);
+}
+
+__global__ void k_time(unsigned long long t0, unsigned long long* out) {
+    *out = globaltimer_ns() - t0;
+}
+
+}  // namespace
+
+// --------------------------------------------------------------- engine --
+class QrotEngine {
+public:
+    QrotEngine(regot_dproblem* P, double reg, double tau, cudaStream_t st)
+        : P_(P), st_(st), ops_(P, reg, st), n_(P->n), m_(P->m), reg_(reg), tau_(tau),
+          mixed_(P->prec == REGOT_PREC_MIXED) {
+        const int N = n_ + m_;
+        gamma_.alloc(N, st);
+        grad_.alloc(N, st);
+        h_.alloc(N, st);
+        vec_.alloc(6 * (size_t)std::max(n_, m_), st);
+        parts_.alloc(6 * (size_t)cdiv(N, kVT), st);
+        state_.alloc(1, st);
+        QState z{};
+        h2d(state_.get(), &z, sizeof(z), st);
+        scal_.alloc(8, st);
+        const PassShape sh = ops_.buf().shape;
+        bm_words_ = (size_t)n_ * sh.nslabs * (mixed_ ? Geo<float>::LC : Geo<double>::LC);
+        for (int i = 0; i < n_; ++i) sum_a_ += P->ha[i];
+    }
+
+    int n() const { return n_; }
+    int m() const { return m_; }
+    ErotOps& ops() { return ops_; }
+    cudaStream_t stream() const { return st_; }
+    double* gamma() { return gamma_.get(); }
+    double* grad() { return grad_.get(); }
+    QState* state() { return state_.get(); }
+
+    // obj and grad at the device vector gamma (n + m). With `mask`, also the
+    // sigma bitmask and h = (h1, h2) of compute_D_hess.
+    double eval(const double* gamma, double* grad, bool mask) {
+        const PassShape sh = ops_.buf().shape;
+        if (mask && !bm_.get()) bm_.alloc(bm_words_, st_);
+        ops_.maxabs(gamma, n_ + m_, nullptr, 0, &state_.get()->maxabs);
+        PassParams p = ops_.base_params();
+        p.ra = gamma;
+        p.cb = gamma + n_;
+        p.grid = &state_.get()->maxabs;
+        p.bitmask = mask ? bm_.get() : nullptr;
+        ops_.pass(mask ? OP_Q_GRADMASK : OP_Q_GRAD, p);
+        const int blocks = pass_blocks(mask ? OP_Q_GRADMASK : OP_Q_GRAD, mixed_, n_, m_);
+        k_sum_totals<<<1, 256, 0, st_>>>(ops_.buf().totpart.get(), blocks, scal_.get());
+        const int g = cdiv(n_ + m_, kVT);
+        if (mixed_)
+            k_q_grad<float><<<g, kVT, 0, st_>>>(
+                (const float*)ops_.buf().rowpart.get(), sh.nslabs,
+                (const float*)ops_.buf().colpart.get(), sh.nrb, n_, m_, mask ? 1 : 0, gamma,
+                P_->a, P_->b, reg_, grad, h_.get(), h_.get() + n_, parts_.get(), state_.get());
+        else
+            k_q_grad<double><<<g, kVT, 0, st_>>>(
+                (const double*)ops_.buf().rowpart.get(), sh.nslabs,
+                (const double*)ops_.buf().colpart.get(), sh.nrb, n_, m_, mask ? 1 : 0, gamma,
+                P_->a, P_->b, reg_, grad, h_.get(), h_.get() + n_, parts_.get(), state_.get());
+        count_launch(2);
+        REGOT_CHECK_LAUNCH();
+        double sq = 0.0;
+        QState hs;
+        d2h(&sq, scal_.get(), sizeof(double), st_);
+        d2h(&hs, state_.get(), sizeof(hs), st_);
+        sync(st_);
+        ++passes_;
+        // qrot_problem.cpp:226-253 (tau terms: 342-351)
+        double obj = 0.5 * sq - reg_ * hs.dot_ab;
+        if (tau_ > 0.0) {
+            const double d = hs.sum_a - hs.sum_b;
+            obj += 0.5 * tau_ * d * d;
+            tau_grad_ = tau_ * d;
+        }
+        return obj;
+    }
+    double tau_grad() const { return tau_grad_; }
+
+    // Line-search trial at x = xp + step d: writes grad f(x) (without the tau
+    // term) to grad() and returns f(x) - f(xp) without the tau and linear
+    // terms' cancellation: with w_ij = d_i + d_j (row and column parts of d),
+    // 0.5 sum (D(x)^2 - D(xp)^2) = step sum w D(xp) + sum rem, where
+    // rem = 0.5 (Dn^2 - D^2) - step w D >= 0 is accumulated per entry by
+    // the pass. sum w D(xp) is the quadratic part of grad f(xp)' d, so the
+    // change is step * (grad f(xp)' d) + sum rem (+ the exact tau term, added
+    // by the caller). Also returns sum D(x)^2 in *sq.
+    double eval_step(const double* xp, const double* d, double step, double* sq) {
+        const PassShape sh = ops_.buf().shape;
+        ops_.maxabs(xp, n_ + m_, nullptr, 0, &state_.get()->maxabs);
+        PassParams p = ops_.base_params();
+        p.ra = xp;
+        p.cb = xp + n_;
+        p.rd = d;
+        p.cd = d + n_;
+        p.steps[0] = step;
+        p.nsteps = 1;
+        p.grid = &state_.get()->maxabs;
+        ops_.pass(OP_Q_GRADLS, p);
+        const int blocks = pass_blocks(OP_Q_GRADLS, mixed_, n_, m_);
+        k_sum_totals<<<1, 256, 0, st_>>>(ops_.buf().totpart.get(), blocks, scal_.get());
+        k_sum_totals<<<1, 256, 0, st_>>>(ops_.buf().totpart.get() + blocks, blocks,
+                                          scal_.get() + 1);
+        const int g = cdiv(n_ + m_, kVT);
+        if (mixed_)
+            k_q_grad<float><<<g, kVT, 0, st_>>>(
+                (const float*)ops_.buf().rowpart.get(), sh.nslabs,
+                (const float*)ops_.buf().colpart.get(), sh.nrb, n_, m_, 0, gamma_.get(), P_->a,
+                P_->b, reg_, grad_.get(), h_.get(), h_.get() + n_, parts_.get(), state_.get());
+        else
+            k_q_grad<double><<<g, kVT, 0, st_>>>(
+                (const double*)ops_.buf().rowpart.get(), sh.nslabs,
+                (const double*)ops_.buf().colpart.get(), sh.nrb, n_, m_, 0, gamma_.get(), P_->a,
+                P_->b, reg_, grad_.get(), h_.get(), h_.get() + n_, parts_.get(), state_.get());
+        count_launch(3);
+        REGOT_CHECK_LAUNCH();
+        double tot[2];
+        d2h(tot, scal_.get(), 2 * sizeof(double), st_);
+        sync(st_);
+        ++passes_;
+        *sq = tot[0];
+        return tot[1];
+    }
+
+    // primal_val (qrot_problem.cpp:10-24)
+    double primal(const double* gamma) {
+        const PassShape sh = ops_.buf().shape;
+        double* xr = vec_.get();
+        double* yc = xr + std::max(n_, m_);
+        double* fc = yc + std::max(n_, m_);
+        ops_.maxabs(gamma, n_ + m_, nullptr, 0, &state_.get()->maxabs);
+        PassParams p = ops_.base_params();
+        p.ra = gamma;
+        p.cb = gamma + n_;
+        p.grid = &state_.get()->maxabs;
+        const int gn = cdiv(n_, kVT), gm = cdiv(m_, kVT);
+        ops_.pass(OP_Q_P1, p);
+        if (mixed_)
+            k_prim1<float><<<gn, kVT, 0, st_>>>((const float*)ops_.buf().rowpart.get(), sh.nslabs,
+                                                 n_, P_->a, reg_, xr);
+        else
+            k_prim1<double><<<gn, kVT, 0, st_>>>((const double*)ops_.buf().rowpart.get(),
+                                                  sh.nslabs, n_, P_->a, reg_, xr);
+        p.rx = xr;
+        ops_.pass(OP_Q_P2, p);
+        if (mixed_)
+            k_prim2<float><<<gm, kVT, 0, st_>>>((const float*)ops_.buf().colpart.get(), sh.nrb,
+                                                 m_, P_->b, reg_, yc, fc, parts_.get(),
+                                                 state_.get());
+        else
+            k_prim2<double><<<gm, kVT, 0, st_>>>((const double*)ops_.buf().colpart.get(), sh.nrb,
+                                                  m_, P_->b, reg_, yc, fc, parts_.get(),
+                                                  state_.get());
+        p.cx = yc;
+        p.cx2 = fc;
+        ops_.pass(OP_Q_P3, p);
+        const int blocks = pass_blocks(OP_Q_P3, mixed_, n_, m_);
+        k_sum_totals<<<1, 256, 0, st_>>>(ops_.buf().totpart.get(), blocks, scal_.get());
+        k_sum_totals<<<1, 256, 0, st_>>>(ops_.buf().totpart.get() + blocks, blocks,
+                                          scal_.get() + 1);
+        if (mixed_)
+            k_prim3<float><<<gn, kVT, 0, st_>>>((const float*)ops_.buf().rowpart.get(), sh.nslabs,
+                                                 n_, P_->a, xr, reg_, parts_.get(), state_.get());
+        else
+            k_prim3<double><<<gn, kVT, 0, st_>>>((const double*)ops_.buf().rowpart.get(),
+                                                  sh.nslabs, n_, P_->a, xr, reg_, parts_.get(),
+                                                  state_.get());
+        count_launch(5);
+        REGOT_CHECK_LAUNCH();
+        double tot[2];
+        QState hs;
+        d2h(tot, scal_.get(), 2 * sizeof(double), st_);
+        d2h(&hs, state_.get(), sizeof(hs), st_);
+        sync(st_);
+        passes_ += 3;
+        const double RM = tot[0] / reg_;            // <R, M>, R_ij = P_ij x_i y_j
+        const double RR = tot[1] / (reg_ * reg_);  // ||R||^2
+        const double f2 = hs.prim[0], S = hs.prim[1], eCc = hs.prim[2], xeB = hs.prim[3],
+                     e2 = hs.prim[4];
+        // res = R + e f' / S (approx_proj.h:22-24)
+        const double val_M = RM + eCc / S;
+        const double sqn = RR + 2.0 * xeB / S + e2 * f2 / (S * S);
+        return val_M + 0.5 * reg_ * sqn;
+    }
+
+    // beta = optimal_beta(alpha) (qrot_problem.cpp:397-404), into beta (device).
+    void optimal_beta(const double* alpha, double* beta) {
+        double* prev = vec_.get();
+        const int gm = cdiv(m_, kVT);
+        k_root_init<<<gm, kVT, 0, st_>>>(m_, beta, prev);
+        count_launch();
+        PassParams p = ops_.base_params();
+        p.ra = alpha;
+        p.cb = beta;
+        const PassShape sh = ops_.buf().shape;
+        for (int it = 0; it <= n_ + 1; ++it) {
+            const int zero = 0;
+            h2d(&state_.get()->changed, &zero, sizeof(int), st_);
+            ops_.pass(OP_Q_COLROOT, p);
+            k_root_update<<<gm, kVT, 0, st_>>>((const double*)ops_.buf().colpart.get(), sh.nrb,
+                                               m_, P_->b, reg_, beta, prev, state_.get());
+            count_launch();
+            REGOT_CHECK_LAUNCH();
+            int changed = 0;
+            d2h(&changed, &state_.get()->changed, sizeof(int), st_);
+            sync(st_);
+            ++passes_;
+            if (!changed) return;
+        }
+        throw Error(REGOT_ERR_NUMERIC, "optimal_beta did not converge");
+    }
+
+    // sigma x (n) with optional division by (h1 + mu)
+    void sigma_rows(const double* x, double mu, bool divide, double* out, const int* done) {
+        const int warps = 8;
+        if (mixed_)
+            k_sigma_rows<Geo<float>::CW, Geo<float>::VW, Geo<float>::LC>
+                <<<cdiv(n_, warps), warps * 32, 0, st_>>>(bm_.get(), n_, m_, nslabs(), x, h_.get(),
+                                                          mu, divide ? 1 : 0, out, done);
+        else
+            k_sigma_rows<Geo<double>::CW, Geo<double>::VW, Geo<double>::LC>
+                <<<cdiv(n_, warps), warps * 32, 0, st_>>>(bm_.get(), n_, m_, nslabs(), x, h_.get(),
+                                                          mu, divide ? 1 : 0, out, done);
+        count_launch();
+    }
+    // partial sums of sigma' y over kColChunks row chunks
+    void sigma_cols(const double* y, double* partial, const int* done) {
+        dim3 grid(cdiv(m_, 128), kColChunks);
+        if (mixed_)
+            k_sigma_cols<Geo<float>::CW, Geo<float>::VW, Geo<float>::LC>
+                <<<grid, 128, 0, st_>>>(bm_.get(), n_, m_, nslabs(), y, partial, done);
+        else
+            k_sigma_cols<Geo<double>::CW, Geo<double>::VW, Geo<double>::LC>
+                <<<grid, 128, 0, st_>>>(bm_.get(), n_, m_, nslabs(), y, partial, done);
+        count_launch();
+    }
+    const double* h1() const { return h_.get(); }
+    const double* h2() const { return h_.get() + n_; }
+    double* parts() { return parts_.get(); }
+    long long passes() const { return passes_; }
+    void add_passes(long long k) { passes_ += k; }
+
+    void plan(const double* gamma, double* out) {
+        ops_.maxabs(gamma, n_ + m_, nullptr, 0, &state_.get()->maxabs);
+        PassParams p = ops_.base_params();
+        p.ra = gamma;
+        p.cb = gamma + n_;
+        p.grid = &state_.get()->maxabs;
+        p.out = out;
+        ops_.pass(OP_Q_PLAN, p);
+    }
+
+private:
+    int nslabs() { return ops_.buf().shape.nslabs; }
+    regot_dproblem* P_;
+    cudaStream_t st_;
+    ErotOps ops_;
+    int n_, m_;
+    double reg_, tau_;
+    bool mixed_;
+    DBuf<double> gamma_, grad_, h_, vec_, parts_, scal_;
+    DBuf<QState> state_;
+    DBuf<uint32_t> bm_;
+    size_t bm_words_ = 0;
+    double sum_a_ = 0.0;
+    double tau_grad_ = 0.0;
+    long long passes_ = 0;
+};
+
+namespace {
+
+void finish_qrot(QrotEngine& E, const double* d_gamma, const std::vector<double>& hobj,
+                 const std::vector<double>& hmar, const std::vector<double>& htime,
+                 const std::vector<double>& hprim, int niter, const regot_opts& o,
+                 regot_result* res) {
+    cudaStream_t st = E.stream();
+    const int n = E.n(), m = E.m();
+    const int L = (int)hobj.size();
+    res->niter = niter;
+    res->hist_len = L;
+    res->passes = E.passes();
+    d2h(res->dual, d_gamma, (size_t)(n + m) * sizeof(double), st);
+    sync(st);
+    if (res->obj_vals) std::memcpy(res->obj_vals, hobj.data(), L * sizeof(double));
+    if (res->mar_errs) std::memcpy(res->mar_errs, hmar.data(), L * sizeof(double));
+    if (res->run_times) std::memcpy(res->run_times, htime.data(), L * sizeof(double));
+    if (res->prim_vals) std::memcpy(res->prim_vals, hprim.data(), L * sizeof(double));
+    if (o.plan && res->plan) {
+        if (o.plan_mem == REGOT_MEM_DEVICE) {
+            E.plan(d_gamma, res->plan);
+        } else {
+            DBuf<double> Pl((size_t)n * m, st);
+            E.plan(d_gamma, Pl.get());
+            d2h(res->plan, Pl.get(), (size_t)n * m * sizeof(double), st);
+        }
+    }
+    E.ops().check_err();
+}
+
+// Wall clock in milliseconds on the device (globaltimer), like the
+// reference's std::chrono Timer (timer.h:9-54).
+class DevClock {
+public:
+    explicit DevClock(cudaStream_t st) : st_(st), buf_(1, st) {}
+    double now_ms() {
+        unsigned long long t = 0;
+        k_time<<<1, 1, 0, st_>>>(0ULL, buf_.get());
+        count_launch();
+        d2h(&t, buf_.get(), sizeof(t), st_);
+        sync(st_);
+        return (double)t * 1e-6;
+    }
+
+private:
+    cudaStream_t st_;
+    DBuf<unsigned long long> buf_;
+};
+
+void init_gamma(QrotEngine& E, const regot_opts& o, std::vector<double>& gamma) {
+    const int n = E.n(), m = E.m();
+    gamma.assign(n + m, 0.0);
+    if (o.x0 && o.x0_len == n + m) {
+        std::copy(o.x0, o.x0 + n + m, gamma.begin());
+        h2d(E.gamma(), gamma.data(), (n + m) * sizeof(double), E.stream());
+        return;
+    }
+    // alpha = 0, beta = optimal_beta(0) (qrot_lbfgs_dual.cpp:111-117)
+    DBuf<double> zero(n, E.stream());
+    zero.zero();
+    E.optimal_beta(zero.get(), E.gamma() + n);
+    REGOT_CUDA(cudaMemsetAsync(E.gamma(), 0, n * sizeof(double), E.stream()));
+    d2h(gamma.data(), E.gamma(), (n + m) * sizeof(double), E.stream());
+    sync(E.stream());
+}
+
+}  // namespace
+
+// qrot_lbfgs_dual_internal (qrot_lbfgs_dual.cpp:81-126, QROTDual 18-79).
+void qrot_lbfgs_dual_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
+                         const regot_opts& o, regot_result* res) {
+    cudaStream_t st = ctx->stream;
+    const int n = P->n, m = P->m, N = n + m;
+    QrotEngine E(P, reg, o.tau, st);
+    const bool mixed = P->prec == REGOT_PREC_MIXED;
+    DevClock clock(st);
+    lbfgs::Param param;
+    param.epsilon = tol;
+    param.epsilon_rel = tol;
+    param.max_iterations = max_iter;
+    std::vector<double> gamma;
+    init_gamma(E, o, gamma);
+
+    std::vector<double> hobj, hmar, htime, hprim;
+    double last_obj = std::numeric_limits<double>::infinity();
+    int it = 0;
+    lbfgs::FunGrad fg = [&](const lbfgs::Vec& x, lbfgs::Vec& g) {
+        h2d(E.gamma(), x.data(), N * sizeof(double), st);
+        last_obj = E.eval(E.gamma(), E.grad(), false);
+        d2h(g.data(), E.grad(), N * sizeof(double), st);
+        sync(st);
+        if (E.tau_grad() != 0.0) {
+            for (int i = 0; i < n; ++i) g[i] += E.tau_grad();
+            for (int j = 0; j < m; ++j) g[n + j] -= E.tau_grad();
+        }
+        return last_obj;
+    };
+    double t_prev = clock.now_ms();
+    auto iterate = [&](const lbfgs::Vec& x, double gnorm) {
+        const double t = clock.now_ms();
+        const double d = t - t_prev;
+        // prim_vals are outside the timed region, as in QROTDual::iterate.
+        double prim = 0.0;
+        if (o.prim_vals) {
+            h2d(E.gamma(), x.data(), N * sizeof(double), st);
+            prim = E.primal(E.gamma());
+        }
+        hobj.push_back(last_obj);
+        hmar.push_back(gnorm / reg);
+        htime.push_back((htime.empty() ? 0.0 : htime.back()) + d);
+        hprim.push_back(prim);
+        if (o.verbose >= 1)
+            std::printf("iter = %d, objval = %g, ||grad|| = %g\n", it, last_obj, gnorm);
+        it++;
+        t_prev = clock.now_ms();
+    };
+    // In mixed precision, f(x) - f(xp) is far below the FP32 rounding of f
+    // itself near convergence, and the line search compares such values: the
+    // trial evaluates the change directly (eval_step) and returns
+    // f(xp) + change. FP64 evaluates f(x) as the reference does.
+    DBuf<double> xp_d(N, st), d_d(N, st);
+    const std::vector<double>& ha = P->ha;
+    const std::vector<double>& hb = P->hb;
+    lbfgs::TrialFn trial = [&](const lbfgs::Vec& xp, const lbfgs::Vec& drt, double step,
+                               double fx_init, double dg_init, lbfgs::Vec& x, lbfgs::Vec& g) {
+        for (int k = 0; k < N; ++k) x[k] = xp[k] + step * drt[k];
+        if (!mixed) return fg(x, g);
+        h2d(E.gamma(), x.data(), N * sizeof(double), st);
+        h2d(xp_d.get(), xp.data(), N * sizeof(double), st);
+        h2d(d_d.get(), drt.data(), N * sizeof(double), st);
+        double sq = 0.0;
+        const double rem = E.eval_step(xp_d.get(), d_d.get(), step, &sq);
+        d2h(g.data(), E.grad(), N * sizeof(double), st);
+        sync(st);
+        double change = step * dg_init + rem;
+        double dab = 0.0;
+        for (int i = 0; i < n; ++i) dab += x[i] * ha[i];
+        for (int j = 0; j < m; ++j) dab += x[n + j] * hb[j];
+        // History records f(x) evaluated directly; the line search gets the
+        // accumulated value.
+        last_obj = 0.5 * sq - reg * dab;
+        if (o.tau > 0.0) {
+            double sa = 0.0, sb = 0.0, ea = 0.0, eb = 0.0;
+            for (int i = 0; i < n; ++i) {
+                sa += x[i];
+                ea += drt[i];
+            }
+            for (int j = 0; j < m; ++j) {
+                sb += x[n + j];
+                eb += drt[n + j];
+            }
+            const double dn = sa - sb, e = ea - eb;
+            last_obj += 0.5 * o.tau * dn * dn;
+            change += 0.5 * o.tau * step * step * e * e;
+            for (int i = 0; i < n; ++i) g[i] += o.tau * dn;
+            for (int j = 0; j < m; ++j) g[n + j] -= o.tau * dn;
+        }
+        return fx_init + change;
+    };
+    double fx;
+    const int niter = lbfgs::minimize(fg, trial, iterate, param, gamma, fx);
+    h2d(E.gamma(), gamma.data(), N * sizeof(double), st);
+    finish_qrot(E, E.gamma(), hobj, hmar, htime, hprim, niter, o, res);
+}
+
+// qrot_assn_internal (qrot_assn.cpp:16-170) with the CG solve of
+// QROTLinearSolver (method 0, qrot_linsolve.cpp:72-105; qrot_cg.cpp:9-50).
+void qrot_assn_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
+                   const regot_opts& o, regot_result* res) {
+    require(o.tau == 0.0, "qrot_assn: tau > 0 is not supported");
+    cudaStream_t st = ctx->stream;
+    const int n = P->n, m = P->m, N = n + m;
+    QrotEngine E(P, reg, 0.0, st);
+    DevClock clock(st);
+    constexpr double nu = 0.99, eta1 = 0.25, eta2 = 0.75, gamma1 = 2.0, gamma2 = 4.0,
+                     lam_min = 0.01, beta_ = 0.5, cg_tol = 1e-8;
+    double xi = 0.0, lam = 1.0;
+
+    std::vector<double> gamma, g(N), u(N), gu(N), v(N), gv(N), direc(N);
+    init_gamma(E, o, gamma);
+    DBuf<double> dvec(8 * (size_t)std::max(n, m), st), partial((size_t)kColChunks * m, st);
+    double* w_d = dvec.get();                  // rhs alpha part (n)
+    double* t_d = w_d + std::max(n, m);        // temp (n)
+    double* zy = t_d + std::max(n, m);         // Schur rhs (m)
+    double* xs = zy + std::max(n, m);          // CG solution r2 (m)
+    double* rs = xs + std::max(n, m);          // CG residual (m)
+    double* ps = rs + std::max(n, m);          // CG direction (m)
+    double* ys = ps + std::max(n, m);          // Delta p (m)
+    double* r1 = ys + std::max(n, m);          // back-substitution (n)
+    DBuf<double> rhs_d(N, st);
+    QState* S = E.state();
+    const int gn = cdiv(n, kVT), gm = cdiv(m, kVT);
+    const int cg_max = 2 * m;
+    {
+        QState hs;
+        d2h(&hs, S, sizeof(hs), st);
+        sync(st);
+        hs.cg_max = cg_max;
+        h2d(S, &hs, sizeof(hs), st);
+    }
+
+    double mu_cur = 0.0;
+    // One CG step on Delta (captured once per distinct mu is not possible:
+    // mu changes every iteration, so it is read from device memory).
+    DBuf<double> mu_d(1, st);
+    auto cg_step_launch = [&](double mu) {
+        E.sigma_rows(ps, mu, true, t_d, &S->cg_done);
+        E.sigma_cols(t_d, partial.get(), &S->cg_done);
+        k_acg_a<<<gm, kVT, 0, st>>>(m, partial.get(), kColChunks, E.h2(), mu, ps, ys, E.parts(), S);
+        k_acg_b<<<gm, kVT, 0, st>>>(m, ps, ys, xs, rs, E.parts(), S);
+        k_acg_c<<<gm, kVT, 0, st>>>(m, rs, ps, S);
+        count_launch(3);
+    };
+
+    // (H + mu I)^{-1} rhs with H the generalized Hessian (hess_cg, qrot_cg.cpp:9-50).
+    auto solve = [&](const std::vector<double>& rhs, double mu, std::vector<double>& out) {
+        h2d(rhs_d.get(), rhs.data(), N * sizeof(double), st);
+        // v = w / (h1 + mu); zy = z - sigma' v
+        k_div_h1<<<gn, kVT, 0, st>>>(n, rhs_d.get(), E.h1(), mu, t_d);
+        count_launch();
+        E.sigma_cols(t_d, partial.get(), nullptr);
+        k_sub_partial<<<gm, kVT, 0, st>>>(m, rhs_d.get() + n, partial.get(), kColChunks, zy);
+        k_acg_init<<<gm, kVT, 0, st>>>(m, zy, cg_tol, xs, rs, ps, E.parts(), S);
+        count_launch(2);
+        int batch = 16;
+        for (;;) {
+            for (int q = 0; q < batch; ++q) cg_step_launch(mu);
+            int done = 0;
+            d2h(&done, &S->cg_done, sizeof(int), st);
+            sync(st);
+            if (done) break;
+            batch = std::min(batch * 2, 256);
+        }
+        // r1 = (w - sigma r2) / (h1 + mu)
+        E.sigma_rows(xs, mu, false, t_d, nullptr);
+        k_backsub<<<gn, kVT, 0, st>>>(n, rhs_d.get(), t_d, E.h1(), mu, r1);
+        count_launch();
+        out.resize(N);
+        d2h(out.data(), r1, n * sizeof(double), st);
+        d2h(out.data() + n, xs, m * sizeof(double), st);
+        sync(st);
+    };
+    auto grad_at = [&](const std::vector<double>& x, std::vector<double>& gr, bool mask) {
+        h2d(E.gamma(), x.data(), N * sizeof(double), st);
+        const double f = E.eval(E.gamma(), E.grad(), mask);
+        d2h(gr.data(), E.grad(), N * sizeof(double), st);
+        sync(st);
+        return f;
+    };
+    auto primal = [&](const std::vector<double>& x) {
+        if (!o.prim_vals) return 0.0;
+        h2d(E.gamma(), x.data(), N * sizeof(double), st);
+        return E.primal(E.gamma());
+    };
+    (void)mu_cur;
+    (void)w_d;
+
+    std::vector<double> hobj, hmar, htime, hprim;
+    double t0 = clock.now_ms();
+    double f = grad_at(gamma, g, true);
+    double gnorm = lbfgs::norm(g);
+    double dur = clock.now_ms() - t0;
+    hobj.push_back(f);
+    hmar.push_back(gnorm / reg);
+    htime.push_back(dur);
+    hprim.push_back(primal(gamma));
+    int i;
+    for (i = 0; i < max_iter; i++) {
+        if (o.verbose >= 1)
+            std::printf("iter = %d, objval = %g, ||grad|| = %g\n", i, f, gnorm);
+        t0 = clock.now_ms();
+        if (gnorm < tol) break;
+        if (i == 0) xi = gnorm;
+        const double mu = lam * gnorm;
+        std::vector<double> rhs(N);
+        for (int q = 0; q < N; ++q) rhs[q] = -g[q];
+        solve(rhs, mu, direc);
+        for (int q = 0; q < N; ++q) u[q] = gamma[q] + direc[q];
+        grad_at(u, gu, false);
+        const double gunorm = lbfgs::norm(gu);
+        if (gunorm <= nu * xi) {
+            gamma.swap(u);
+            xi = gunorm;
+        } else {
+            const double numer = -lbfgs::dot(gu, direc);
+            const double denom = lbfgs::dot(direc, direc);
+            const double rho = numer / denom;
+            for (int q = 0; q < N; ++q) v[q] = gamma[q] + (-numer) / (gunorm * gunorm) * gu[q];
+            grad_at(v, gv, false);
+            const double gvnorm = lbfgs::norm(gv);
+            if (rho >= eta1 && gvnorm <= gnorm) {
+                gamma.swap(v);
+            } else {
+                for (int q = 0; q < N; ++q) gamma[q] -= beta_ * g[q];
+            }
+            if (rho >= eta2) {
+                lam = 0.5 * (lam_min + lam);
+            } else if (rho >= eta1) {
+                lam *= gamma1;
+            } else {
+                lam *= gamma2;
+            }
+        }
+        f = grad_at(gamma, g, true);
+        gnorm = lbfgs::norm(g);
+        dur = clock.now_ms() - t0;
+        hobj.push_back(f);
+        hmar.push_back(gnorm / reg);
+        htime.push_back(htime.back() + dur);
+        hprim.push_back(primal(gamma));
+    }
+    h2d(E.gamma(), gamma.data(), N * sizeof(double), st);
+    finish_qrot(E, E.gamma(), hobj, hmar, htime, hprim, i, o, res);
+}
+
+}  // namespace regot
+
+// ------------------------------------------------------- pass-level C ABI --
+using namespace regot;
+
+namespace {
+template <typename F>
+int qguard(regot_ctx* ctx, F&& f) {
+    if (!ctx) return REGOT_ERR_INVALID_ARG;
+    long long* saved = g_launch_counter;
+    g_launch_counter = &ctx->launches;
+    int rc = REGOT_OK;
+    try {
+        REGOT_CUDA(cudaSetDevice(ctx->device));
+        f();
+        ctx->last_error.clear();
+    } catch (const Error& e) {
+        ctx->last_error = e.what();
+        rc = e.code;
+    } catch (const std::exception& e) {
+        ctx->last_error = e.what();
+        rc = REGOT_ERR_NUMERIC;
+    }
+    g_launch_counter = saved;
+    return rc;
+}
+}  // namespace
+
+extern "C" {
+
+int regot_qrot_dual_obj_grad(regot_ctx* ctx, regot_dproblem* P, double reg, const double* gamma,
+                             double* obj, double* grad) {
+    return qguard(ctx, [&] {
+        require(P && gamma && obj && grad, "NULL argument");
+        require(reg > 0.0, "reg must be positive");
+        QrotEngine E(P, reg, 0.0, ctx->stream);
+        const int N = P->n + P->m;
+        h2d(E.gamma(), gamma, N * sizeof(double), ctx->stream);
+        *obj = E.eval(E.gamma(), E.grad(), false);
+        d2h(grad, E.grad(), N * sizeof(double), ctx->stream);
+        E.ops().check_err();
+    });
+}
+
+int regot_qrot_optimal_beta(regot_ctx* ctx, regot_dproblem* P, double reg, const double* alpha,
+                            double* beta) {
+    return qguard(ctx, [&] {
+        require(P && alpha && beta, "NULL argument");
+        require(reg > 0.0, "reg must be positive");
+        QrotEngine E(P, reg, 0.0, ctx->stream);
+        h2d(E.gamma(), alpha, P->n * sizeof(double), ctx->stream);
+        E.optimal_beta(E.gamma(), E.gamma() + P->n);
+        d2h(beta, E.gamma() + P->n, P->m * sizeof(double), ctx->stream);
+        E.ops().check_err();
+    });
+}
+
+int regot_qrot_primal_val(regot_ctx* ctx, regot_dproblem* P, double reg, const double* gamma,
+                          double* value) {
+    return qguard(ctx, [&] {
+        require(P && gamma && value, "NULL argument");
+        require(reg > 0.0, "reg must be positive");
+        QrotEngine E(P, reg, 0.0, ctx->stream);
+        h2d(E.gamma(), gamma, (P->n + P->m) * sizeof(double), ctx->stream);
+        *value = E.primal(E.gamma());
+        E.ops().check_err();
+    });
+}
+
+int regot_qrot_plan(regot_ctx* ctx, regot_dproblem* P, double reg, const double* gamma,
+                    double* plan, int plan_mem) {
+    return qguard(ctx, [&] {
+        require(P && gamma && plan, "NULL argument");
+        require(reg > 0.0, "reg must be positive");
+        QrotEngine E(P, reg, 0.0, ctx->stream);
+        const int n = P->n, m = P->m;
+        h2d(E.gamma(), gamma, (n + m) * sizeof(double), ctx->stream);
+        if (plan_mem == REGOT_MEM_DEVICE) {
+            E.plan(E.gamma(), plan);
+        } else {
+            DBuf<double> out((size_t)n * m, ctx->stream);
+            E.plan(E.gamma(), out.get());
+            d2h(plan, out.get(), (size_t)n * m * sizeof(double), ctx->stream);
+        }
+        E.ops().check_err();
+    });
+}
+
+}  // extern "C"
