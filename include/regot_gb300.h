@@ -160,6 +160,14 @@ int regot_erot_hvp(regot_ctx* ctx, regot_dproblem* prob, double reg, const doubl
 /* SinkhornResult::get_plan (src/sinkhorn_result.h:32-50); plan row-major. */
 int regot_erot_plan(regot_ctx* ctx, regot_dproblem* prob, double reg, const double* gamma,
                     double* plan, int plan_mem);
+/* sparsify_mat3 (src/sinkhorn_sparsify3.cpp:276-405) of T(gamma) with the
+ * threshold delta and the density hint that selects find_small (> 0.2) or
+ * find_large, as dual_sparsified_hess calls it (src/sinkhorn_problem_obj.cpp:432-443).
+ * *nnz = number of kept entries of the first m-1 columns, exact zeros of T
+ * included (the reference's SparseMatrix::nonZeros()). If mask is not NULL it
+ * receives the kept nonzero entries as a row-major n x (m-1) array of 0/1. */
+int regot_erot_sparsify(regot_ctx* ctx, regot_dproblem* prob, double reg, const double* gamma,
+                        double delta, double density_hint, long long* nnz, int* mask);
 /* QROT Problem::dual_obj_grad (src/qrot_problem.cpp:226-253). */
 int regot_qrot_dual_obj_grad(regot_ctx* ctx, regot_dproblem* prob, double reg,
                              const double* gamma, double* obj, double* grad);

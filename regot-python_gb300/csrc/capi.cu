@@ -416,6 +416,16 @@ int regot_erot_plan(regot_ctx* ctx, regot_dproblem* P, double reg, const double*
     });
 }
 
+int regot_erot_sparsify(regot_ctx* ctx, regot_dproblem* P, double reg, const double* gamma,
+                        double delta, double density_hint, long long* nnz, int* mask) {
+    return guarded(ctx, [&] {
+        require(P && gamma && nnz, "NULL argument");
+        require(reg > 0.0, "reg must be positive");
+        require(delta >= 0.0, "delta must be non-negative");
+        erot_sparsify_gpu(ctx, P, reg, gamma, delta, density_hint, nnz, mask);
+    });
+}
+
 }  // extern "C"
 
 // ------------------------------------------------------------ measurement --

@@ -81,7 +81,10 @@ __device__ __forceinline__ double max_strided(const Acc* p, int count, size_t st
 }
 
 // Grid-wide sum of K values per thread. Returns true in thread 0 of the last
-// block to finish, with the totals in out[] (summed in block order).
+// block to finish, with the totals in out[]. The last block sums the
+// per-block partials with all its threads (thread t takes blocks t, t + bs,
+// ... in order, then a fixed butterfly and warp order), so the result does
+// not depend on which block finishes last.
 template <int K>
 __device__ bool grid_reduce(const double (&vals)[K], double* block_parts, unsigned* counter,
                             double (&out)[K]) {
@@ -107,12 +110,27 @@ __device__ bool grid_reduce(const double (&vals)[K], double* block_parts, unsign
         s_last = (ticket == gridDim.x - 1);
     }
     __syncthreads();
-    if (!s_last || threadIdx.x != 0) return false;
+    if (!s_last) return false;
     __threadfence();
+    double part[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) part[k] = 0.0;
+    for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) part[k] += __ldcg(&block_parts[(size_t)b * K + k]);
+    }
+    __syncthreads();  // s_red is reused
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const double v = warp_sum_d(part[k]);
+        if (lane == 0) s_red[k][warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x != 0) return false;
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         double s = 0.0;
-        for (unsigned b = 0; b < gridDim.x; ++b) s += __ldcg(&block_parts[(size_t)b * K + k]);
+        for (int w = 0; w < nw; ++w) s += s_red[k][w];
         out[k] = s;
     }
     *counter = 0u;

@@ -43,6 +43,10 @@ public:
     double sum_bt() const { return sum_bt_; }
     double reg() const { return reg_; }
     PassBuffers& buf() { return buf_; }
+    // FP32 split of the row / column vectors of the last mixed pass
+    // (x = hi, y = lo, z = rx, w = rd), valid until the next pass.
+    const float4* rsplit() const { return rsplit_.get(); }
+    const float4* csplit() const { return csplit_.get(); }
 
     // Dense pass with this problem's M, reg and partial buffers.
     void pass(int op, PassParams p);

@@ -1,0 +1,1295 @@
+// sinkhorn_ssns on the GPU (reference: src/sinkhorn_ssns.cpp:16-234).
+//
+// One iteration:
+//  * the direction solves (H_s + shift I) d = -g for the sparsified Hessian
+//    H_s = [diag(h1) S; S' diag(h2)], S = sparsify(T) / reg
+//    (sinkhorn_hess.h:46-158, sinkhorn_hess.cpp:15-164), by conjugate
+//    gradients on the Schur complement of the beta block
+//    Delta = diag(h2 + shift) - S' diag(1 / (h1 + shift)) S (sinkhorn_cg.cpp:9-50);
+//  * line_selection over {1, .5, .25, .1} (sinkhorn_problem_ls.cpp:13-41)
+//    evaluates all four candidates in one dense pass, on exact objective
+//    differences f(gamma + s d) - f(gamma) = s g'd + reg sum T phi(s w)
+//    (phi(x) = e^x - 1 - x, w_ij = (d_i + d_j) / reg);
+//  * rho = (f - f_new) / (-g's - s'H_s s / 2) decides whether gamma moves and
+//    how the shift factor mu changes (sinkhorn_ssns.cpp:146-176);
+//  * after a move: gradient pass, then the sparsification.
+//
+// Linear solver. Method 0 is the reference's CG exactly: identity
+// preconditioner, relative residual 1e-8, at most 2 (m - 1) iterations.
+// Method 1 (the default) factors H_s with SimplicialLDLT in the reference
+// (sinkhorn_linsolve.cpp:58-106); here it is the same Schur-complement CG with
+// a Jacobi preconditioner run to the relative residual cg_tol (1e-10), so the
+// direction equals the factorisation's to that accuracy.
+//
+// Sparsification (sparsify_mat3, sinkhorn_sparsify3.cpp:276-405):
+//  1. k_tt writes T' (column j of T as a contiguous row, j < m - 1);
+//  2. k_col_select finds per column the threshold
+//       x_j = min{x in column j : sum of the column's values <= x exceeds delta}
+//     by a weighted radix select over the bit patterns of T (non-negative
+//     floating-point numbers order like their bit patterns). The entries
+//     below x_j are the dropped ones: the smallest entries whose sum stays
+//     <= delta. find_small (from the small side) and find_large (from the
+//     large side, target colsum - delta) both select exactly this set in
+//     exact arithmetic. They differ when the column sum is <= delta:
+//     find_small then drops every entry (x_j = inf), find_large keeps the
+//     largest (x_j = column maximum). density_hint > 0.2 selects find_small
+//     (sinkhorn_sparsify3.cpp:303);
+//  3. k_row_stage forms per row the dropped values d_ij, their sum R_i and,
+//     where R_i > 2 delta, the threshold y_i = min{y : sum of d_ij <= y
+//     exceeds 2 delta}; dropped entries >= y_i are kept again
+//     (sinkhorn_sparsify3.cpp:333-353). It writes the row's kept entries in
+//     column order (CSR rows, fixed stride m - 1);
+//  4. k_csc_fill writes the same kept entries per column in row order from T'
+//     (CSC columns, fixed stride n).
+// The kept entries are those with Delta == 0 (sinkhorn_sparsify3.cpp:378):
+// every exact zero of the FP64 T is one. Zeros count towards nnz and the
+// density but add nothing to a product, so k_tt counts them and they are not
+// stored. In mixed mode T is FP32 with flush-to-zero; the FP64 T is zero when
+// its base-2 exponent argument is below -1075.
+//
+// Threshold sums are exact integer sums of the values in a fixed-point scale
+// of about 2^-61 times the column (row) sum, so the selection does not depend
+// on the summation order and uses no FP64 arithmetic (slow on this GPU). It
+// can differ from the reference's sequential FP64 sums only where a partial
+// sum lies within about 1e-15 (relative) of delta.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <limits>
+#include <vector>
+
+#include "device_util.cuh"
+#include "erot_ops.cuh"
+#include "solvers.h"
+
+namespace regot {
+
+namespace {
+
+constexpr int kVT = 64;            // vector kernels
+constexpr int kSelThreads = 256;   // selection / fill kernels
+constexpr int kSelWarps = kSelThreads / 32;
+constexpr int kSpWarps = 8;        // warp-per-row sparse kernels: 8 warps per block
+constexpr unsigned kFull = 0xffffffffu;
+constexpr size_t kMaxCacheBytes = 160 * 1024;
+
+struct SsnState {
+    unsigned counter;
+    int done;
+    int it;
+    int max_it;
+    double shift;
+    double absnew;   // r'z of the CG residual
+    double alpha;
+    double beta;
+    double thresh2;
+    double rr;
+    double f;
+    double gnorm;
+    double gtd;      // g'd
+    double dhd;      // d'H_s d
+    double maxabs;
+    double nnz;      // stored kept entries
+};
+
+__device__ __forceinline__ float ex2_approx_f(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// T_ij exactly as the mixed dense passes form it (hi parts summed exactly,
+// lo parts scaled, one FMA, ex2.approx), and whether the FP64 T is zero.
+__device__ __forceinline__ float t_mixed(float mv, float4 r, float4 c, float kexp, bool& zero64) {
+    const float s = (r.x + c.x) - mv;
+    const float z = fmaf(s, kexp, __fadd_rn(__fmul_rn(r.y, kexp), __fmul_rn(c.y, kexp)));
+    zero64 = z < -1075.0f;
+    return ex2_approx_f(z);
+}
+
+__device__ __forceinline__ double t_plain(double mv, double ra, double cb, double kexp,
+                                          bool& zero64) {
+    const double t = exp(((ra + cb) - mv) * kexp);
+    zero64 = (t == 0.0);
+    return t;
+}
+
+template <typename TM>
+struct KeyOf;
+template <>
+struct KeyOf<float> {
+    using U = unsigned;
+    static constexpr int kBits = 32;
+    __device__ static U key(float v) { return __float_as_uint(v); }
+    __device__ static float val(U k) { return __uint_as_float(k); }
+};
+template <>
+struct KeyOf<double> {
+    using U = unsigned long long;
+    static constexpr int kBits = 64;
+    __device__ static U key(double v) { return (U)__double_as_longlong(v); }
+    __device__ static double val(U k) { return __longlong_as_double((long long)k); }
+};
+
+constexpr int kBins = 2048;  // widest radix digit: 11 bits
+
+struct SelSmem {
+    unsigned long long hsum[kBins];
+    unsigned hcnt[kBins];
+    unsigned long long wscan[kSelWarps];
+    double red[kSelWarps];
+    double red2[kSelWarps];
+    int wcount[kSelWarps];
+    unsigned long long base;
+    double result;
+    int bin;
+    unsigned count;
+};
+
+// v * 2^k truncated to an integer, from the bit pattern (v >= 0 finite,
+// v * 2^k < 2^63): the threshold sums are exact integer sums, so they do not
+// depend on the summation order and need no FP64 arithmetic.
+__device__ __forceinline__ unsigned long long fix_of(float v, int k) {
+    const unsigned bits = __float_as_uint(v);
+    const int e = (int)(bits >> 23);
+    unsigned long long mant = bits & 0x7fffffu;
+    int sh;
+    if (e == 0) {
+        sh = k - 149;
+    } else {
+        mant |= 0x800000u;
+        sh = e - 150 + k;
+    }
+    if (sh >= 0) return mant << sh;
+    return sh > -64 ? (mant >> -sh) : 0ull;
+}
+__device__ __forceinline__ unsigned long long fix_of(double v, int k) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+    const int e = (int)(bits >> 52);
+    unsigned long long mant = bits & 0xfffffffffffffull;
+    int sh;
+    if (e == 0) {
+        sh = k - 1074;
+    } else {
+        mant |= 0x10000000000000ull;
+        sh = e - 1075 + k;
+    }
+    if (sh >= 0) return mant << sh;
+    return sh > -64 ? (mant >> -sh) : 0ull;
+}
+
+// Scale 2^k with est * 2^k < 2^61 (est >= the sum to be formed, up to the
+// rounding of its estimate) and target * 2^k as an integer (saturated).
+__device__ __forceinline__ int fix_scale(double est) {
+    return est > 0.0 ? 60 - ilogb(est) : 0;
+}
+__device__ __forceinline__ unsigned long long fix_target(double target, int k) {
+    const double t = ldexp(target, k);
+    return t >= 1.8e19 ? ~0ull : (unsigned long long)floor(t);
+}
+
+// Block-wide sum (in TM: an estimate that only sets the fixed-point scale)
+// and maximum of v[0, len).
+template <typename TM>
+__device__ void block_est_max(const TM* v, int len, SelSmem& sh, double& est, double& mx) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    TM s = 0, m = 0;
+    for (int k = threadIdx.x; k < len; k += kSelThreads) {
+        const TM x = v[k];
+        s += x;
+        m = x > m ? x : m;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        s += __shfl_xor_sync(kFull, s, o);
+        const TM mo = __shfl_xor_sync(kFull, m, o);
+        m = mo > m ? mo : m;
+    }
+    if (lane == 0) {
+        sh.red[w] = (double)s;
+        sh.red2[w] = (double)m;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0, mm = 0.0;
+        for (int q = 0; q < kSelWarps; ++q) {
+            t += sh.red[q];
+            mm = fmax(mm, sh.red2[q]);
+        }
+        sh.result = mm;
+        // headroom for the rounding of the estimate
+        sh.red[0] = t * (1.0 + 1e-3) + mm;
+    }
+    __syncthreads();
+    est = sh.red[0];
+    mx = sh.result;
+    __syncthreads();
+}
+
+template <typename TM>
+struct Digits;
+template <>
+struct Digits<float> {
+    static constexpr int kTop = 30;  // key bits 30..0 (the sign bit is 0)
+};
+template <>
+struct Digits<double> {
+    static constexpr int kTop = 62;
+};
+
+// Smallest x among v[0, len) (values >= 0) with sum_{v_k <= x} v_k > target,
+// in the fixed-point scale 2^k (target already scaled; x > 0), by a radix select
+// over the bit patterns: 11-bit then 10/11-bit digits, most significant
+// first. Each round histograms the candidates (entries sharing the digits
+// chosen so far) into integer bin sums and counts with shared-memory atomics,
+// scans the bins and keeps the bin where the running sum first exceeds
+// target. Returns false when the total does not exceed target.
+template <typename TM>
+__device__ bool block_select(const TM* v, int len, unsigned long long target, int k,
+                             SelSmem& sh, TM& out) {
+    using K = KeyOf<TM>;
+    using U = typename K::U;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    U prefix = 0, mask = 0;
+    unsigned long long base = 0;
+    int hi = Digits<TM>::kTop;
+    bool first = true;
+    while (hi >= 0) {
+        const int width = first ? 11 : ((hi + 1) % 11 == 0 ? 11 : 10);
+        const int lo = hi - width + 1 > 0 ? hi - width + 1 : 0;
+        const int nb = 1 << (hi - lo + 1);
+        for (int b = threadIdx.x; b < nb; b += kSelThreads) {
+            sh.hsum[b] = 0ull;
+            sh.hcnt[b] = 0u;
+        }
+        if (threadIdx.x == 0) sh.bin = -1;
+        __syncthreads();
+        for (int q = threadIdx.x; q < len; q += kSelThreads) {
+            const TM val = v[q];
+            const U key = K::key(val);
+            // zeros add nothing and cannot complete a crossing
+            if (key != 0 && (key & mask) == prefix) {
+                const int b = (int)((key >> lo) & (U)(nb - 1));
+                atomicAdd(&sh.hsum[b], fix_of(val, k));
+                atomicAdd(&sh.hcnt[b], 1u);
+            }
+        }
+        __syncthreads();
+        // Exclusive scan over the bins: each thread owns nb / 256 consecutive bins.
+        const int per = nb / kSelThreads;
+        const int b0 = threadIdx.x * per;
+        unsigned long long ls = 0;
+        for (int q = 0; q < per; ++q) ls += sh.hsum[b0 + q];
+        unsigned long long inc = ls;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const unsigned long long o = __shfl_up_sync(kFull, inc, d);
+            if (lane >= d) inc += o;
+        }
+        if (lane == 31) sh.wscan[w] = inc;
+        __syncthreads();
+        unsigned long long run = base + (inc - ls);
+        for (int q = 0; q < w; ++q) run += sh.wscan[q];
+        for (int q = 0; q < per; ++q) {
+            const unsigned long long nx = run + sh.hsum[b0 + q];
+            if (run <= target && nx > target && sh.hcnt[b0 + q] > 0) {
+                sh.bin = b0 + q;
+                sh.base = run;
+                sh.count = sh.hcnt[b0 + q];
+            }
+            run = nx;
+        }
+        __syncthreads();
+        const int sb = sh.bin;
+        const unsigned cnt = sh.count;
+        const unsigned long long nbase = sh.base;
+        __syncthreads();
+        if (sb < 0) return false;
+        prefix |= (U)sb << lo;
+        mask |= (U)(nb - 1) << lo;
+        base = nbase;
+        if (cnt == 1 && lo > 0) {
+            // a single candidate left: it is the answer
+            for (int q = threadIdx.x; q < len; q += kSelThreads) {
+                const TM val = v[q];
+                if ((K::key(val) & mask) == prefix) sh.result = (double)val;
+            }
+            __syncthreads();
+            out = (TM)sh.result;
+            __syncthreads();
+            return true;
+        }
+        hi = lo - 1;
+        first = false;
+    }
+    out = K::val(prefix);
+    return true;
+}
+
+// Ordered compaction of the indices k in [0, len) with keep(k): emit(k, slot)
+// with consecutive slots in index order. Each warp owns a contiguous segment:
+// it counts its kept entries, the warps' offsets come from one block-wide
+// exchange, and a second sweep writes. Returns the total.
+template <typename Keep, typename Emit>
+__device__ int block_compact(int len, SelSmem& sh, Keep keep, Emit emit) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int seg = (len + kSelThreads - 1) / kSelThreads * 32;
+    const int lo = w * seg;
+    const int hi = lo + seg < len ? lo + seg : len;
+    int cnt = 0;
+    for (int k0 = lo; k0 < hi; k0 += 32) {
+        const int k = k0 + lane;
+        cnt += __popc(__ballot_sync(kFull, k < hi && keep(k)));
+    }
+    if (lane == 0) sh.wcount[w] = cnt;
+    __syncthreads();
+    int off = 0, tot = 0;
+#pragma unroll
+    for (int q = 0; q < kSelWarps; ++q) {
+        const int c = sh.wcount[q];
+        off += q < w ? c : 0;
+        tot += c;
+    }
+    for (int k0 = lo; k0 < hi; k0 += 32) {
+        const int k = k0 + lane;
+        const bool kp = k < hi && keep(k);
+        const unsigned bal = __ballot_sync(kFull, kp);
+        if (kp) emit(k, off + __popc(bal & ((1u << lane) - 1u)));
+        off += __popc(bal);
+    }
+    __syncthreads();
+    return tot;
+}
+
+struct DenseArgs {
+    const void* M;
+    long long ldm;
+    int n, m1;
+    const float4* rs;  // mixed: row split
+    const float4* cs;  // mixed: column split
+    float kexp_f;
+    const double* gamma;  // plain: duals (beta at gamma + n)
+    double kexp_d;
+};
+
+template <typename TM>
+__device__ __forceinline__ TM t_at(const DenseArgs& a, int i, int j, TM mv, bool& z64);
+template <>
+__device__ __forceinline__ float t_at<float>(const DenseArgs& a, int i, int j, float mv,
+                                             bool& z64) {
+    return t_mixed(mv, a.rs[i], a.cs[j], a.kexp_f, z64);
+}
+template <>
+__device__ __forceinline__ double t_at<double>(const DenseArgs& a, int i, int j, double mv,
+                                               bool& z64) {
+    return t_plain(mv, a.gamma[i], a.gamma[a.n + j], a.kexp_d, z64);
+}
+
+// T' (rows j < m - 1 of length n, stride ldt) and the count of FP64 zeros.
+template <typename TM>
+__global__ void __launch_bounds__(256) k_tt(DenseArgs a, TM* TT, long long ldt,
+                                            unsigned long long* zeros) {
+    __shared__ TM tile[32][33];
+    const TM* M = static_cast<const TM*>(a.M);
+    const int j0 = blockIdx.x * 32, i0 = blockIdx.y * 32;
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    unsigned zc = 0;
+    const int j = j0 + tx;
+#pragma unroll
+    for (int k = ty; k < 32; k += 8) {
+        const int i = i0 + k;
+        TM t = 0;
+        if (i < a.n && j < a.m1) {
+            bool z64;
+            t = t_at<TM>(a, i, j, M[(size_t)i * a.ldm + j], z64);
+            zc += z64 ? 1u : 0u;
+        }
+        tile[tx][k] = t;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = ty; k < 32; k += 8) {
+        const int jj = j0 + k, ii = i0 + tx;
+        if (jj < a.m1 && ii < a.n) TT[(size_t)jj * ldt + ii] = tile[k][tx];
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) zc += __shfl_xor_sync(kFull, zc, o);
+    if (tx == 0 && zc) atomicAdd(zeros, (unsigned long long)zc);
+}
+
+// Column thresholds x_j (see the file comment).
+template <typename TM>
+__global__ void __launch_bounds__(kSelThreads) k_col_select(const TM* TT, long long ldt, int n,
+                                                            int m1, double delta, int from_large,
+                                                            int cache, TM* xout) {
+    extern __shared__ __align__(16) unsigned char s_dyn[];
+    __shared__ SelSmem sh;
+    TM* s_col = reinterpret_cast<TM*>(s_dyn);
+    for (int j = blockIdx.x; j < m1; j += gridDim.x) {
+        const TM* col = TT + (size_t)j * ldt;
+        const TM* v = col;
+        if (cache) {
+            const int nvec = (int)(((size_t)n * sizeof(TM) + 15) / 16);
+            const float4* src = reinterpret_cast<const float4*>(col);
+            float4* dst = reinterpret_cast<float4*>(s_col);
+            for (int k = threadIdx.x; k < nvec; k += kSelThreads) dst[k] = src[k];
+            __syncthreads();
+            v = s_col;
+        }
+        double est, mx;
+        block_est_max(v, n, sh, est, mx);
+        const int k = fix_scale(est);
+        TM x;
+        if (!block_select(v, n, fix_target(delta, k), k, sh, x))
+            x = from_large ? (TM)mx : (TM)INFINITY;  // column sum <= delta
+        if (threadIdx.x == 0) xout[j] = x;
+        __syncthreads();
+    }
+}
+
+struct RowStageArgs {
+    int ldr;          // CSR row stride (m - 1)
+    int cache;        // rows of T and d in shared memory
+    long long lds;    // per-block scratch stride (2 rows) when not cached
+};
+
+// Row stage and CSR rows (see the file comment).
+template <typename TM>
+__global__ void __launch_bounds__(kSelThreads) k_row_stage(DenseArgs a, RowStageArgs r,
+                                                           const TM* xcol, double delta2,
+                                                           TM* scratch, TM* yout, int* rcount,
+                                                           int* rcols, TM* rvals) {
+    extern __shared__ __align__(16) unsigned char s_dyn[];
+    __shared__ SelSmem sh;
+    const TM* M = static_cast<const TM*>(a.M);
+    const int m1 = a.m1;
+    TM* tbuf = r.cache ? reinterpret_cast<TM*>(s_dyn) : scratch + (size_t)blockIdx.x * r.lds;
+    TM* dbuf = tbuf + (r.cache ? (size_t)((m1 + 3) & ~3) : (size_t)(r.lds / 2));
+    for (int i = blockIdx.x; i < a.n; i += gridDim.x) {
+        const TM* Mi = M + (size_t)i * a.ldm;
+        for (int j = threadIdx.x; j < m1; j += kSelThreads) {
+            bool z64;
+            const TM t = t_at<TM>(a, i, j, Mi[j], z64);
+            tbuf[j] = t;
+            dbuf[j] = t < xcol[j] ? t : (TM)0;
+        }
+        __syncthreads();
+        double est, mx;
+        block_est_max(dbuf, m1, sh, est, mx);
+        TM y = (TM)INFINITY;
+        if (est > delta2) {  // est bounds the dropped mass from above
+            const int k = fix_scale(est);
+            TM yy;
+            // the dropped mass exceeds 2 delta: re-keep down to y
+            if (block_select(dbuf, m1, fix_target(delta2, k), k, sh, yy)) y = yy;
+        }
+        int* cols = rcols + (size_t)i * r.ldr;
+        TM* vals = rvals + (size_t)i * r.ldr;
+        const int total = block_compact(
+            m1, sh,
+            [&](int j) {
+                const TM t = tbuf[j];
+                return t != (TM)0 && (t >= xcol[j] || t >= y);
+            },
+            [&](int j, int slot) {
+                cols[slot] = j;
+                vals[slot] = tbuf[j];
+            });
+        if (threadIdx.x == 0) {
+            rcount[i] = total;
+            yout[i] = y;
+        }
+        __syncthreads();
+    }
+}
+
+// CSC columns from T' with the column and row thresholds.
+template <typename TM>
+__global__ void __launch_bounds__(kSelThreads) k_csc_fill(const TM* TT, long long ldt, int n,
+                                                          int m1, const TM* xcol, const TM* yrow,
+                                                          int ldc, int cache, int* ccount,
+                                                          int* crows, TM* cvals) {
+    extern __shared__ __align__(16) unsigned char s_dyn[];
+    __shared__ SelSmem sh;
+    TM* s_col = reinterpret_cast<TM*>(s_dyn);
+    for (int j = blockIdx.x; j < m1; j += gridDim.x) {
+        const TM* col = TT + (size_t)j * ldt;
+        if (cache) {
+            const int nvec = (int)(((size_t)n * sizeof(TM) + 15) / 16);
+            const float4* src = reinterpret_cast<const float4*>(col);
+            float4* dst = reinterpret_cast<float4*>(s_col);
+            for (int k = threadIdx.x; k < nvec; k += kSelThreads) dst[k] = src[k];
+            __syncthreads();
+            col = s_col;
+        }
+        const TM xj = xcol[j];
+        int* rows = crows + (size_t)j * ldc;
+        TM* vals = cvals + (size_t)j * ldc;
+        const int total = block_compact(
+            n, sh,
+            [&](int i) {
+                const TM t = col[i];
+                return t != (TM)0 && (t >= xj || t >= __ldg(yrow + i));
+            },
+            [&](int i, int slot) {
+                rows[slot] = i;
+                vals[slot] = col[i];
+            });
+        if (threadIdx.x == 0) ccount[j] = total;
+    }
+}
+
+// Number of stored entries (sum of the row counts).
+__global__ void k_nnz(const int* rcount, int n, double* parts, SsnState* st) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[1] = {t < n ? (double)rcount[t] : 0.0};
+    double out[1];
+    __threadfence();
+    if (grid_reduce<1>(v, parts, &st->counter, out)) st->nnz = out[0];
+}
+
+// ---- sparse products (one warp per row or column; FP64 accumulation) ----
+struct Sparse {
+    const int* rcount;
+    const int* rcols;
+    const void* rvals;
+    int ldr;
+    const int* ccount;
+    const int* crows;
+    const void* cvals;
+    int ldc;
+    int n, m1;
+    double inv_reg;
+};
+
+template <typename TM>
+__device__ __forceinline__ double row_dot(const Sparse& S, int i, const double* x) {
+    const int lane = threadIdx.x & 31;
+    const int cnt = S.rcount[i];
+    const int* c = S.rcols + (size_t)i * S.ldr;
+    const TM* v = static_cast<const TM*>(S.rvals) + (size_t)i * S.ldr;
+    double s = 0.0;
+    for (int k = lane; k < cnt; k += 32) s += (double)v[k] * x[c[k]];
+    return warp_sum_d(s) * S.inv_reg;
+}
+
+template <typename TM>
+__device__ __forceinline__ double col_dot(const Sparse& S, int j, const double* x) {
+    const int lane = threadIdx.x & 31;
+    const int cnt = S.ccount[j];
+    const int* r = S.crows + (size_t)j * S.ldc;
+    const TM* v = static_cast<const TM*>(S.cvals) + (size_t)j * S.ldc;
+    double s = 0.0;
+    for (int k = lane; k < cnt; k += 32) s += (double)v[k] * x[r[k]];
+    return warp_sum_d(s) * S.inv_reg;
+}
+
+// Vectors: h = (h1 [n], h2 [m - 1]) from the gradient pass, g, direction
+// dir = (d_alpha [n], d_beta~ [m - 1], 0). The Schur CG works on x = d_beta~.
+
+// Jacobi diagonal of the Schur complement (method 1).
+template <typename TM>
+__global__ void k_schur_diag(Sparse S, const double* h, SsnState* st, double* diag) {
+    const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (j >= S.m1) return;
+    const double shift = st->shift;
+    const int cnt = S.ccount[j];
+    const int* r = S.crows + (size_t)j * S.ldc;
+    const TM* v = static_cast<const TM*>(S.cvals) + (size_t)j * S.ldc;
+    double s = 0.0;
+    for (int k = lane; k < cnt; k += 32) {
+        const double sv = (double)v[k] * S.inv_reg;
+        s += sv * sv / (h[r[k]] + shift);
+    }
+    s = warp_sum_d(s);
+    if (lane == 0) {
+        const double dj = h[S.n + j] + shift;
+        const double dd = dj - s;
+        diag[j] = dd > 1e-3 * dj ? dd : dj;
+    }
+}
+
+// u_i = rhs_alpha_i / (h1_i + shift) with rhs = -g.
+__global__ void k_schur_rhs_rows(int n, const double* g, const double* h, SsnState* st,
+                                 double* u) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) u[i] = -g[i] / (h[i] + st->shift);
+}
+
+// CG set-up on Delta x = rhs_beta - S' u: x = 0, r = that, z = r / diag, p = z.
+template <typename TM>
+__global__ void k_schur_init(Sparse S, const double* g, const double* u, const double* diag,
+                             double tol, double* x, double* rv, double* z, double* p,
+                             double* parts, SsnState* st) {
+    const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    double v[2] = {0.0, 0.0};
+    if (j < S.m1) {
+        const double w = col_dot<TM>(S, j, u);
+        if (lane == 0) {
+            const double rj = -g[S.n + j] - w;
+            const double zj = diag ? rj / diag[j] : rj;
+            x[j] = 0.0;
+            rv[j] = rj;
+            z[j] = zj;
+            p[j] = zj;
+            v[0] = rj * rj;
+            v[1] = rj * zj;
+        }
+    }
+    double out[2];
+    __threadfence();
+    if (grid_reduce<2>(v, parts, &st->counter, out)) {
+        st->thresh2 = fmax(tol * tol * out[0], 2.2250738585072014e-308);
+        st->rr = out[0];
+        st->absnew = out[1];
+        st->it = 0;
+        st->done = (out[0] == 0.0 || out[0] < st->thresh2) ? 1 : 0;
+    }
+}
+
+// u_i = (S p)_i / (h1_i + shift).
+template <typename TM>
+__global__ void k_schur_rows(Sparse S, const double* p, const double* h, double* u,
+                             SsnState* st) {
+    if (st->done) return;
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (i >= S.n) return;
+    const double s = row_dot<TM>(S, i, p);
+    if ((threadIdx.x & 31) == 0) u[i] = s / (h[i] + st->shift);
+}
+
+// q_j = (h2_j + shift) p_j - (S' u)_j; alpha = r'z / p'q.
+template <typename TM>
+__global__ void k_schur_cols(Sparse S, const double* p, const double* u, const double* h,
+                             double* q, double* parts, SsnState* st) {
+    if (st->done) return;
+    const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    double v[1] = {0.0};
+    if (j < S.m1) {
+        const double w = col_dot<TM>(S, j, u);
+        if ((threadIdx.x & 31) == 0) {
+            const double qj = (h[S.n + j] + st->shift) * p[j] - w;
+            q[j] = qj;
+            v[0] = p[j] * qj;
+        }
+    }
+    double out[1];
+    __threadfence();
+    if (grid_reduce<1>(v, parts, &st->counter, out)) st->alpha = st->absnew / out[0];
+}
+
+// x += alpha p, r -= alpha q, z = r / diag; stop on ||r||^2 < thresh2 or
+// at the iteration limit (Eigen's ConjugateGradient loop).
+__global__ void k_schur_b(int m1, const double* p, const double* q, const double* diag,
+                          double* x, double* rv, double* z, double* parts, SsnState* st) {
+    if (st->done) return;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const double al = st->alpha;
+    double v[2] = {0.0, 0.0};
+    if (j < m1) {
+        x[j] += al * p[j];
+        const double rj = rv[j] - al * q[j];
+        rv[j] = rj;
+        const double zj = diag ? rj / diag[j] : rj;
+        z[j] = zj;
+        v[0] = rj * rj;
+        v[1] = rj * zj;
+    }
+    double out[2];
+    __threadfence();
+    if (grid_reduce<2>(v, parts, &st->counter, out)) {
+        st->rr = out[0];
+        st->it += 1;
+        if (out[0] < st->thresh2 || st->it >= st->max_it || !(out[0] == out[0])) {
+            st->done = 1;
+        } else {
+            st->beta = out[1] / st->absnew;
+            st->absnew = out[1];
+        }
+    }
+}
+
+__global__ void k_schur_c(int m1, const double* z, double* p, SsnState* st) {
+    if (st->done) return;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < m1) p[j] = z[j] + st->beta * p[j];
+}
+
+// d_alpha_i = (rhs_alpha_i - (S d_beta)_i) / (h1_i + shift).
+template <typename TM>
+__global__ void k_schur_back(Sparse S, const double* g, const double* h, double* dir,
+                             SsnState* st) {
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (i >= S.n) return;
+    const double s = row_dot<TM>(S, i, dir + S.n);
+    if ((threadIdx.x & 31) == 0) dir[i] = (-g[i] - s) / (h[i] + st->shift);
+}
+
+// d'H_s d and g'd: rows give d_a (h1 d_a + S d_b), cols d_b (h2 d_b + S' d_a).
+template <typename TM>
+__global__ void k_dhd_rows(Sparse S, const double* dir, const double* g, const double* h,
+                           double* parts, SsnState* st) {
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    double v[2] = {0.0, 0.0};
+    if (i < S.n) {
+        const double s = row_dot<TM>(S, i, dir + S.n);
+        if ((threadIdx.x & 31) == 0) {
+            const double di = dir[i];
+            v[0] = di * (h[i] * di + s);
+            v[1] = g[i] * di;
+        }
+    }
+    double out[2];
+    __threadfence();
+    if (grid_reduce<2>(v, parts, &st->counter, out)) {
+        st->dhd = out[0];
+        st->gtd = out[1];
+    }
+}
+
+template <typename TM>
+__global__ void k_dhd_cols(Sparse S, const double* dir, const double* g, const double* h,
+                           double* parts, SsnState* st) {
+    const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    double v[2] = {0.0, 0.0};
+    if (j < S.m1) {
+        const double s = col_dot<TM>(S, j, dir);
+        if ((threadIdx.x & 31) == 0) {
+            const double dj = dir[S.n + j];
+            v[0] = dj * (h[S.n + j] * dj + s);
+            v[1] = g[S.n + j] * dj;
+        }
+    }
+    double out[2];
+    __threadfence();
+    if (grid_reduce<2>(v, parts, &st->counter, out)) {
+        st->dhd += out[0];
+        st->gtd += out[1];
+    }
+}
+
+// f, g and h = (r / reg, c~ / reg) from the row/column sums of T.
+template <typename Acc>
+__global__ void k_ssns_grad(const Acc* rp, int nslabs, const Acc* cp, int nrb, int n, int m,
+                            const double* gamma, const double* a, const double* b, double reg,
+                            double* g, double* h, double* parts, SsnState* st) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[4] = {0.0, 0.0, 0.0, 0.0};
+    if (t < n) {
+        const double r = merge_strided(rp + t, nslabs, (size_t)n);
+        const double gi = r - a[t];
+        g[t] = gi;
+        h[t] = r / reg;
+        v[0] = gi * gi;
+        v[1] = r;
+        v[2] = gamma[t] * a[t];
+    } else if (t < n + m) {
+        const int j = t - n;
+        if (j < m - 1) {
+            const double c = merge_strided(cp + j, nrb, (size_t)m);
+            const double gj = c - b[j];
+            g[t] = gj;
+            h[t] = c / reg;
+            v[0] = gj * gj;
+            v[3] = gamma[t] * b[j];
+        } else {
+            g[t] = 0.0;
+            h[t] = 1.0;
+        }
+    }
+    double out[4];
+    __threadfence();
+    if (grid_reduce<4>(v, parts, &st->counter, out)) {
+        st->gnorm = sqrt(out[0]);
+        st->f = reg * out[1] - out[2] - out[3];  // sinkhorn_problem_obj.cpp:389-390
+    }
+}
+
+__global__ void k_ssns_move(int N, double s, const double* d, double* gamma) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < N) gamma[t] += s * d[t];
+}
+
+__global__ void k_ls_sum(const double* totpart, int nblocks, int nsteps, double* out) {
+    const int s = threadIdx.x;
+    if (s >= nsteps) return;
+    double acc = 0.0;
+    for (int k = 0; k < nblocks; ++k) acc += totpart[(size_t)s * nblocks + k];
+    out[s] = acc;
+}
+
+template <typename TM>
+class SsnsEngine {
+public:
+    SsnsEngine(regot_ctx* ctx, regot_dproblem* P, double reg, const regot_opts& o)
+        : P_(P), st_(ctx->stream), ops_(P, reg, st_), n_(P->n), m_(P->m), m1_(P->m - 1),
+          reg_(reg), mixed_(P->prec == REGOT_PREC_MIXED) {
+        const int N = n_ + m_;
+        const int method = o.method < 0 ? 1 : o.method;
+        require(method == 0 || method == 1, "sinkhorn_ssns: method must be 0 (CG) or 1 (direct)");
+        jacobi_ = method == 1;
+        cg_tol_ = method == 0 ? 1e-8 : (o.cg_tol > 0.0 ? o.cg_tol : 1e-10);
+        cg_max_ = o.cg_max_iter > 0 ? o.cg_max_iter : 2 * std::max(m1_, 1);
+        if (jacobi_ && o.cg_max_iter <= 0) cg_max_ = 10 * std::max(m1_, 1);
+        gamma_.alloc(N, st_);
+        g_.alloc(N, st_);
+        h_.alloc(N, st_);
+        dir_.alloc(N, st_);
+        u_.alloc(n_, st_);
+        const int mm = std::max(m1_, 1);
+        rv_.alloc(mm, st_);
+        z_.alloc(mm, st_);
+        p_.alloc(mm, st_);
+        q_.alloc(mm, st_);
+        diag_.alloc(mm, st_);
+        parts_.alloc(4 * (size_t)std::max(cdiv(N, kVT), cdiv((long long)std::max(n_, m1_) * 32, 256)),
+                     st_);
+        state_.alloc(1, st_);
+        SsnState z{};
+        z.max_it = cg_max_;
+        h2d(state_.get(), &z, sizeof(z), st_);
+        lsout_.alloc(4, st_);
+        zeros_.alloc(1, st_);
+        // T' rows padded to 16 bytes; CSR / CSC with full-width strides.
+        const int vec = 16 / (int)sizeof(TM);
+        ldt_ = ((long long)n_ + vec - 1) / vec * vec;
+        tt_.alloc((size_t)m1_ * ldt_, st_);
+        xcol_.alloc(mm, st_);
+        yrow_.alloc(n_, st_);
+        rcount_.alloc(n_, st_);
+        rcols_.alloc((size_t)n_ * m1_, st_);
+        rvals_.alloc((size_t)n_ * m1_, st_);
+        ccount_.alloc(mm, st_);
+        crows_.alloc((size_t)m1_ * n_, st_);
+        cvals_.alloc((size_t)m1_ * n_, st_);
+        const int sms = device_sm_count();
+        col_cache_ = (size_t)ldt_ * sizeof(TM) <= kMaxCacheBytes;
+        const size_t col_smem = col_cache_ ? (size_t)ldt_ * sizeof(TM) : 0;
+        REGOT_CUDA(cudaFuncSetAttribute(k_col_select<TM>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)col_smem));
+        REGOT_CUDA(cudaFuncSetAttribute(k_csc_fill<TM>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)col_smem));
+        col_smem_ = col_smem;
+        const long long rowpad = ((long long)m1_ + 3) & ~3LL;
+        row_cache_ = 2 * (size_t)rowpad * sizeof(TM) <= kMaxCacheBytes;
+        row_smem_ = row_cache_ ? 2 * (size_t)rowpad * sizeof(TM) : 0;
+        REGOT_CUDA(cudaFuncSetAttribute(k_row_stage<TM>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)row_smem_));
+        col_grid_ = std::max(1, std::min(m1_, sms * 4));
+        row_grid_ = std::max(1, std::min(n_, sms * 4));
+        if (!row_cache_) row_scratch_.alloc((size_t)row_grid_ * 2 * rowpad, st_);
+        lds_ = 2 * rowpad;
+        S_.rcount = rcount_.get();
+        S_.rcols = rcols_.get();
+        S_.rvals = rvals_.get();
+        S_.ldr = m1_;
+        S_.ccount = ccount_.get();
+        S_.crows = crows_.get();
+        S_.cvals = cvals_.get();
+        S_.ldc = n_;
+        S_.n = n_;
+        S_.m1 = m1_;
+        S_.inv_reg = 1.0 / reg;
+    }
+
+    double* gamma() { return gamma_.get(); }
+    ErotOps& ops() { return ops_; }
+    SsnState* state() { return state_.get(); }
+    long long passes() const { return passes_; }
+
+    SsnState read_state() {
+        SsnState hs;
+        d2h(&hs, state_.get(), sizeof(hs), st_);
+        sync(st_);
+        return hs;
+    }
+
+    // f, g, h at gamma; leaves the FP32 split of gamma in the ops (mixed).
+    void grad() {
+        const PassShape sh = ops_.buf().shape;
+        ops_.maxabs(gamma_.get(), n_ + m_, nullptr, 0, &state_.get()->maxabs);
+        PassParams p = ops_.base_params();
+        p.ra = gamma_.get();
+        p.cb = gamma_.get() + n_;
+        p.grid = &state_.get()->maxabs;
+        ops_.pass(OP_E_ROWCOL, p);
+        const int gv = cdiv(n_ + m_, kVT);
+        if (mixed_)
+            k_ssns_grad<float><<<gv, kVT, 0, st_>>>(
+                (const float*)ops_.buf().rowpart.get(), sh.nslabs,
+                (const float*)ops_.buf().colpart.get(), sh.nrb, n_, m_, gamma_.get(), P_->a,
+                P_->b, reg_, g_.get(), h_.get(), parts_.get(), state_.get());
+        else
+            k_ssns_grad<double><<<gv, kVT, 0, st_>>>(
+                (const double*)ops_.buf().rowpart.get(), sh.nslabs,
+                (const double*)ops_.buf().colpart.get(), sh.nrb, n_, m_, gamma_.get(), P_->a,
+                P_->b, reg_, g_.get(), h_.get(), parts_.get(), state_.get());
+        count_launch();
+        REGOT_CHECK_LAUNCH();
+        ++passes_;
+    }
+
+    DenseArgs dense_args() const {
+        DenseArgs a;
+        a.M = P_->M;
+        a.ldm = P_->ldm;
+        a.n = n_;
+        a.m1 = m1_;
+        a.rs = ops_.rsplit();
+        a.cs = ops_.csplit();
+        a.kexp_f = (float)(1.4426950408889634 / reg_);
+        a.gamma = gamma_.get();
+        a.kexp_d = 1.0 / reg_;
+        return a;
+    }
+
+    // sparsify_mat3 of T(gamma) (right after grad()); returns the density
+    // (2 nnz + n + m - 1) / (n + m - 1)^2 (sinkhorn_hess.h:75-80).
+    double sparsify(double delta, double density_hint) {
+        if (m1_ <= 0) return 1.0;
+        const DenseArgs a = dense_args();
+        zeros_.zero();
+        dim3 tgrid(cdiv(m1_, 32), cdiv(n_, 32));
+        k_tt<TM><<<tgrid, dim3(32, 8), 0, st_>>>(a, tt_.get(), ldt_, zeros_.get());
+        k_col_select<TM><<<col_grid_, kSelThreads, col_smem_, st_>>>(
+            tt_.get(), ldt_, n_, m1_, delta, density_hint > 0.2 ? 0 : 1, col_cache_ ? 1 : 0,
+            xcol_.get());
+        RowStageArgs r;
+        r.ldr = m1_;
+        r.cache = row_cache_ ? 1 : 0;
+        r.lds = lds_;
+        k_row_stage<TM><<<row_grid_, kSelThreads, row_smem_, st_>>>(
+            a, r, xcol_.get(), 2.0 * delta, row_scratch_.get(), yrow_.get(), rcount_.get(),
+            rcols_.get(), rvals_.get());
+        k_csc_fill<TM><<<col_grid_, kSelThreads, col_smem_, st_>>>(
+            tt_.get(), ldt_, n_, m1_, xcol_.get(), yrow_.get(), n_, col_cache_ ? 1 : 0,
+            ccount_.get(), crows_.get(), cvals_.get());
+        k_nnz<<<cdiv(n_, kVT), kVT, 0, st_>>>(rcount_.get(), n_, parts_.get(), state_.get());
+        count_launch(5);
+        REGOT_CHECK_LAUNCH();
+        passes_ += 4;
+        unsigned long long zc = 0;
+        d2h(&zc, zeros_.get(), sizeof(zc), st_);
+        const SsnState hs = read_state();
+        const double nnz = hs.nnz + (double)zc;
+        const double dim = (double)(n_ + m_ - 1);
+        return (2.0 * nnz + dim) / dim / dim;
+    }
+
+    // direction = -(H_s + shift I)^{-1} g into dir (sinkhorn_ssns.cpp:118-140).
+    void direction(double shift) {
+        SsnState* S = state_.get();
+        REGOT_CUDA(cudaMemcpyAsync(&S->shift, &shift, sizeof(double), cudaMemcpyHostToDevice,
+                                   st_));
+        REGOT_CUDA(cudaMemsetAsync(dir_.get(), 0, (size_t)(n_ + m_) * sizeof(double), st_));
+        if (m1_ <= 0) {
+            k_schur_rhs_rows<<<cdiv(n_, kVT), kVT, 0, st_>>>(n_, g_.get(), h_.get(), S,
+                                                             dir_.get());
+            count_launch();
+            return;
+        }
+        const int gr = cdiv((long long)n_ * 32, 32 * kSpWarps);
+        const int gc = cdiv((long long)m1_ * 32, 32 * kSpWarps);
+        const int bt = 32 * kSpWarps;
+        const double* diag = nullptr;
+        if (jacobi_) {
+            k_schur_diag<TM><<<gc, bt, 0, st_>>>(S_, h_.get(), S, diag_.get());
+            count_launch();
+            diag = diag_.get();
+        }
+        k_schur_rhs_rows<<<cdiv(n_, kVT), kVT, 0, st_>>>(n_, g_.get(), h_.get(), S, u_.get());
+        double* x = dir_.get() + n_;
+        k_schur_init<TM><<<gc, bt, 0, st_>>>(S_, g_.get(), u_.get(), diag, cg_tol_, x, rv_.get(),
+                                             z_.get(), p_.get(), parts_.get(), S);
+        count_launch(2);
+        REGOT_CHECK_LAUNCH();
+        if (!exec_ || graph_jacobi_ != jacobi_) build_graph(diag);
+        int batch = 8;
+        for (;;) {
+            for (int q = 0; q < batch; ++q) REGOT_CUDA(cudaGraphLaunch(exec_, st_));
+            count_launch(graph_kernels_ * batch);
+            int done = 0;
+            d2h(&done, &S->done, sizeof(int), st_);
+            sync(st_);
+            if (done) break;
+            batch = std::min(batch * 2, 64);
+        }
+        k_schur_back<TM><<<gr, bt, 0, st_>>>(S_, g_.get(), h_.get(), dir_.get(), S);
+        count_launch();
+        REGOT_CHECK_LAUNCH();
+    }
+
+    // g'd and d'H_s d into the state.
+    void dir_dots() {
+        const int bt = 32 * kSpWarps;
+        const int gr = cdiv((long long)n_ * 32, bt);
+        const int gc = cdiv((long long)std::max(m1_, 1) * 32, bt);
+        k_dhd_rows<TM><<<gr, bt, 0, st_>>>(S_, dir_.get(), g_.get(), h_.get(), parts_.get(),
+                                           state_.get());
+        k_dhd_cols<TM><<<gc, bt, 0, st_>>>(S_, dir_.get(), g_.get(), h_.get(), parts_.get(),
+                                           state_.get());
+        count_launch(2);
+        REGOT_CHECK_LAUNCH();
+    }
+
+    // reg * sum T phi(s w) for up to four steps s (one dense pass).
+    void ls_pass(const double* steps, int ns, double* tots) {
+        ops_.maxabs(gamma_.get(), n_ + m_, dir_.get(), n_ + m_, &state_.get()->maxabs);
+        PassParams p = ops_.base_params();
+        p.ra = gamma_.get();
+        p.cb = gamma_.get() + n_;
+        p.rd = dir_.get();
+        p.cd = dir_.get() + n_;
+        p.grid = &state_.get()->maxabs;
+        for (int s = 0; s < 4; ++s) p.steps[s] = s < ns ? steps[s] : 0.0;
+        p.nsteps = ns;
+        ops_.pass(OP_E_LS, p);
+        ++passes_;
+        const int blocks = pass_blocks(OP_E_LS, mixed_, n_, m_);
+        k_ls_sum<<<1, 32, 0, st_>>>(ops_.buf().totpart.get(), blocks, ns, lsout_.get());
+        count_launch();
+        d2h(tots, lsout_.get(), ns * sizeof(double), st_);
+        sync(st_);
+    }
+
+    void move(double s) {
+        k_ssns_move<<<cdiv(n_ + m_, kVT), kVT, 0, st_>>>(n_ + m_, s, dir_.get(), gamma_.get());
+        count_launch();
+        REGOT_CHECK_LAUNCH();
+    }
+
+    // Kept pattern of the last sparsify(): mask[i * (m - 1) + j] = 1 for the
+    // stored entries (row-major), from the CSR rows.
+    void kept_mask(int* mask) {
+        std::vector<int> cnt(n_);
+        std::vector<int> cols((size_t)n_ * m1_);
+        d2h(cnt.data(), rcount_.get(), n_ * sizeof(int), st_);
+        d2h(cols.data(), rcols_.get(), cols.size() * sizeof(int), st_);
+        sync(st_);
+        std::fill(mask, mask + (size_t)n_ * m1_, 0);
+        for (int i = 0; i < n_; ++i)
+            for (int k = 0; k < cnt[i]; ++k) mask[(size_t)i * m1_ + cols[(size_t)i * m1_ + k]] = 1;
+    }
+    // Stored entries of the CSC copy (equal to the CSR's when both are built
+    // from the same thresholds).
+    long long csc_nnz() {
+        std::vector<int> cnt(std::max(m1_, 1));
+        d2h(cnt.data(), ccount_.get(), m1_ * sizeof(int), st_);
+        sync(st_);
+        long long s = 0;
+        for (int j = 0; j < m1_; ++j) s += cnt[j];
+        return s;
+    }
+    long long zero_count() {
+        unsigned long long zc = 0;
+        d2h(&zc, zeros_.get(), sizeof(zc), st_);
+        sync(st_);
+        return (long long)zc;
+    }
+
+    ~SsnsEngine() {
+        if (exec_) cudaGraphExecDestroy(exec_);
+        if (graph_) cudaGraphDestroy(graph_);
+    }
+
+private:
+    void build_graph(const double* diag) {
+        if (exec_) cudaGraphExecDestroy(exec_);
+        if (graph_) cudaGraphDestroy(graph_);
+        exec_ = nullptr;
+        graph_ = nullptr;
+        SsnState* S = state_.get();
+        const int bt = 32 * kSpWarps;
+        const int gr = cdiv((long long)n_ * 32, bt);
+        const int gc = cdiv((long long)m1_ * 32, bt);
+        const int gv = cdiv(m1_, kVT);
+        double* x = dir_.get() + n_;
+        long long* saved = g_launch_counter;
+        graph_kernels_ = 0;
+        g_launch_counter = &graph_kernels_;
+        REGOT_CUDA(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
+        k_schur_rows<TM><<<gr, bt, 0, st_>>>(S_, p_.get(), h_.get(), u_.get(), S);
+        k_schur_cols<TM><<<gc, bt, 0, st_>>>(S_, p_.get(), u_.get(), h_.get(), q_.get(),
+                                             parts_.get(), S);
+        k_schur_b<<<gv, kVT, 0, st_>>>(m1_, p_.get(), q_.get(), diag, x, rv_.get(), z_.get(),
+                                       parts_.get(), S);
+        k_schur_c<<<gv, kVT, 0, st_>>>(m1_, z_.get(), p_.get(), S);
+        count_launch(4);
+        REGOT_CUDA(cudaStreamEndCapture(st_, &graph_));
+        g_launch_counter = saved;
+        REGOT_CUDA(cudaGraphInstantiate(&exec_, graph_, 0));
+        graph_jacobi_ = jacobi_;
+    }
+
+    regot_dproblem* P_;
+    cudaStream_t st_;
+    ErotOps ops_;
+    int n_, m_, m1_;
+    double reg_;
+    bool mixed_;
+    bool jacobi_ = true;
+    double cg_tol_ = 1e-10;
+    int cg_max_ = 0;
+    DBuf<double> gamma_, g_, h_, dir_, u_, rv_, z_, p_, q_, diag_, parts_, lsout_;
+    DBuf<SsnState> state_;
+    DBuf<unsigned long long> zeros_;
+    long long ldt_ = 0, lds_ = 0;
+    DBuf<TM> tt_, xcol_, yrow_, rvals_, cvals_, row_scratch_;
+    DBuf<int> rcount_, rcols_, ccount_, crows_;
+    bool col_cache_ = false, row_cache_ = false;
+    size_t col_smem_ = 0, row_smem_ = 0;
+    int col_grid_ = 1, row_grid_ = 1;
+    Sparse S_{};
+    cudaGraph_t graph_ = nullptr;
+    cudaGraphExec_t exec_ = nullptr;
+    bool graph_jacobi_ = false;
+    long long graph_kernels_ = 0;
+    long long passes_ = 0;
+};
+
+template <typename TM>
+void run_ssns(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
+              const regot_opts& o, regot_result* res) {
+    using clock = std::chrono::steady_clock;
+    cudaStream_t st = ctx->stream;
+    const int n = P->n, m = P->m, N = n + m;
+    // sinkhorn_ssns.cpp:32-35, 94
+    constexpr double rho_t1 = 0.25, rho_t2 = 0.75, mu_s1 = 4.0, mu_s2 = 0.5, kappa = 0.001,
+                     nu0 = 0.01;
+    double mu = o.mu0 > 0.0 ? o.mu0 : 1.0;
+    SsnsEngine<TM> E(ctx, P, reg, o);
+    ErotOps& ops = E.ops();
+
+    // Initial value (sinkhorn_ssns.cpp:48-62): x0, or (0 + beta_m, beta~ - beta_m)
+    // with beta = optimal_beta(alpha = 0).
+    {
+        std::vector<double> h(N, 0.0);
+        if (o.x0 && o.x0_len == n + m - 1) {
+            std::copy(o.x0, o.x0 + n + m - 1, h.begin());
+        } else {
+            DBuf<double> beta(m, st), zero(n, st), mx(1, st);
+            zero.zero();
+            ops.optimal_beta(zero.get(), beta.get(), mx.get());
+            std::vector<double> hb(m);
+            d2h(hb.data(), beta.get(), m * sizeof(double), st);
+            sync(st);
+            for (int i = 0; i < n; ++i) h[i] = hb[m - 1];
+            for (int j = 0; j < m - 1; ++j) h[n + j] = hb[j] - hb[m - 1];
+        }
+        h2d(E.gamma(), h.data(), N * sizeof(double), st);
+    }
+    std::vector<double> hobj, hmar, htime, hdens;
+    auto t0 = clock::now();
+    E.grad();
+    SsnState hs = E.read_state();
+    double f = hs.f, gnorm = hs.gnorm;
+    double density = E.sparsify(nu0 * gnorm, 0.001);
+    sync(st);
+    auto ms_since = [](clock::time_point t) {
+        return std::chrono::duration<double, std::milli>(clock::now() - t).count();
+    };
+    hobj.push_back(f);
+    hmar.push_back(gnorm);
+    htime.push_back(ms_since(t0));
+    hdens.push_back(density);
+    const double cands[4] = {1.0, 0.5, 0.25, 0.1};
+    int i;
+    for (i = 0; i < max_iter; i++) {
+        if (o.verbose >= 1) std::printf("iter = %d, objval = %g, ||grad|| = %g\n", i, f, gnorm);
+        const auto t_it = clock::now();
+        if (gnorm < tol || !std::isfinite(f)) break;
+        const double shift = mu * gnorm;
+        E.direction(shift);
+        E.dir_dots();
+        hs = E.read_state();
+        const double gtd = hs.gtd, dhd = hs.dhd;
+        // line_selection: first candidate below f, else the best.
+        double tots[4];
+        E.ls_pass(cands, 4, tots);
+        double best = 1.0, best_df = std::numeric_limits<double>::infinity();
+        for (int s = 0; s < 4; ++s) {
+            const double df = cands[s] * gtd + reg * tots[s];
+            if (df < best_df) {
+                best = cands[s];
+                best_df = df;
+            }
+            if (best_df < 0.0) break;
+        }
+        const double numer = -best_df;  // f - newf
+        const double denom = -best * gtd - 0.5 * best * best * dhd;
+        const double rho = numer / denom;
+        if (rho > 0.0) E.move(best);
+        if (rho < rho_t1) {
+            mu = mu_s1 * mu;
+        } else if (rho > rho_t2) {
+            mu = std::max(mu_s2 * mu, kappa);
+        }
+        if (rho > 0.0) {
+            E.grad();
+            hs = E.read_state();
+            f = hs.f;
+            gnorm = hs.gnorm;
+            density = E.sparsify(nu0 * gnorm, density);
+        }
+        sync(st);
+        hobj.push_back(f);
+        hmar.push_back(gnorm);
+        htime.push_back(htime.back() + ms_since(t_it));
+        hdens.push_back(density);
+    }
+    const int L = (int)hobj.size();
+    DBuf<double> hist(4 * (size_t)std::max(L, 1), st);
+    h2d(hist.get(), hobj.data(), L * sizeof(double), st);
+    h2d(hist.get() + L, hmar.data(), L * sizeof(double), st);
+    h2d(hist.get() + 2 * L, htime.data(), L * sizeof(double), st);
+    h2d(hist.get() + 3 * L, hdens.data(), L * sizeof(double), st);
+    finish_erot_result(ops, E.gamma(), hist.get(), hist.get() + L, hist.get() + 2 * L,
+                       hist.get() + 3 * L, L, L, i, E.passes(), o, res);
+}
+
+template <typename TM>
+void sparsify_at(regot_ctx* ctx, regot_dproblem* P, double reg, const double* gamma,
+                 double delta, double density_hint, long long* nnz, int* mask) {
+    const int n = P->n, m = P->m;
+    regot_opts o;
+    regot_opts_init(&o);
+    SsnsEngine<TM> E(ctx, P, reg, o);
+    std::vector<double> h(n + m, 0.0);
+    std::copy(gamma, gamma + n + m - 1, h.begin());
+    h2d(E.gamma(), h.data(), (n + m) * sizeof(double), ctx->stream);
+    E.grad();
+    E.sparsify(delta, density_hint);
+    const SsnState hs = E.read_state();
+    const long long stored = (long long)hs.nnz;
+    require(E.csc_nnz() == stored, "CSR and CSC copies of the sparsified matrix differ",
+            REGOT_ERR_NUMERIC);
+    *nnz = stored + E.zero_count();
+    if (mask) E.kept_mask(mask);
+    E.ops().check_err();
+}
+
+}  // namespace
+
+void erot_sparsify_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, const double* gamma,
+                       double delta, double density_hint, long long* nnz, int* mask) {
+    if (P->prec == REGOT_PREC_MIXED)
+        sparsify_at<float>(ctx, P, reg, gamma, delta, density_hint, nnz, mask);
+    else
+        sparsify_at<double>(ctx, P, reg, gamma, delta, density_hint, nnz, mask);
+}
+
+void sinkhorn_ssns_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
+                       const regot_opts& o, regot_result* res) {
+    if (P->prec == REGOT_PREC_MIXED)
+        run_ssns<float>(ctx, P, reg, tol, max_iter, o, res);
+    else
+        run_ssns<double>(ctx, P, reg, tol, max_iter, o, res);
+}
+
+}  // namespace regot

@@ -93,20 +93,50 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
     return false;
 }
 
-// e^x - 1 - x without cancellation: the Taylor series x^2/2! + ... + x^9/9!
-// (Horner form) for |x| < 1/2, where its truncation error is below 2^-24
-// relative; expm1(x) - x beyond, where no cancellation occurs.
+// e^x - 1 - x without cancellation: for |x| < 1/2 the Taylor series
+// x^2 (1/2! + x/3! + x^2/4! + ...) by Horner's rule with the coefficients
+// 1/k! as constants (no divisions), FP32 up to x^9 (truncation below 2e-9
+// relative), FP64 up to x^17 (below 1e-20); expm1(x) - x beyond, where no
+// cancellation occurs.
 template <typename T>
-__device__ __forceinline__ T expm1_minus_x(T x) {
-    if (fabs(x) < (T)0.5) {
-        T p = (T)1 + x / (T)9;
-        p = (T)1 + x / (T)8 * p;
-        p = (T)1 + x / (T)7 * p;
-        p = (T)1 + x / (T)6 * p;
-        p = (T)1 + x / (T)5 * p;
-        p = (T)1 + x / (T)4 * p;
-        p = (T)1 + x / (T)3 * p;
-        return (T)0.5 * x * x * p;
+__device__ __forceinline__ T expm1_minus_x(T x);
+template <>
+__device__ __forceinline__ float expm1_minus_x<float>(float x) {
+    if (fabsf(x) < 0.5f) {
+        float p = 2.7557319e-06f;           // 1/9!
+        p = fmaf(p, x, 2.4801587e-05f);     // 1/8!
+        p = fmaf(p, x, 1.9841270e-04f);     // 1/7!
+        p = fmaf(p, x, 1.3888889e-03f);     // 1/6!
+        p = fmaf(p, x, 8.3333333e-03f);     // 1/5!
+        p = fmaf(p, x, 4.1666667e-02f);     // 1/4!
+        p = fmaf(p, x, 1.6666667e-01f);     // 1/3!
+        p = fmaf(p, x, 0.5f);               // 1/2!
+        return (x * x) * p;
+    }
+    // no cancellation here: e^x - 1 - x >= 0.106, so the relative error of
+    // ex2.approx (about 2^-22) grows at most elevenfold
+    return (ex2_approx(x * 1.44269504f) - 1.0f) - x;
+}
+template <>
+__device__ __forceinline__ double expm1_minus_x<double>(double x) {
+    if (fabs(x) < 0.5) {
+        double p = 2.8114572543455206e-15;  // 1/17!
+        p = fma(p, x, 4.7794773323873853e-14);  // 1/16!
+        p = fma(p, x, 7.6471637318198164e-13);  // 1/15!
+        p = fma(p, x, 1.1470745597729725e-11);  // 1/14!
+        p = fma(p, x, 1.6059043836821613e-10);  // 1/13!
+        p = fma(p, x, 2.0876756987868099e-09);  // 1/12!
+        p = fma(p, x, 2.5052108385441720e-08);  // 1/11!
+        p = fma(p, x, 2.7557319223985888e-07);  // 1/10!
+        p = fma(p, x, 2.7557319223985893e-06);  // 1/9!
+        p = fma(p, x, 2.4801587301587302e-05);  // 1/8!
+        p = fma(p, x, 1.9841269841269841e-04);  // 1/7!
+        p = fma(p, x, 1.3888888888888889e-03);  // 1/6!
+        p = fma(p, x, 8.3333333333333333e-03);  // 1/5!
+        p = fma(p, x, 4.1666666666666667e-02);  // 1/4!
+        p = fma(p, x, 1.6666666666666667e-01);  // 1/3!
+        p = fma(p, x, 0.5);                     // 1/2!
+        return (x * x) * p;
     }
     return expm1(x) - x;
 }
@@ -390,7 +420,7 @@ __global__ void __launch_bounds__(kThreads, 2) dense_pass(const PassParams p) {
                                                   : make_float4(0.f, 0.f, 0.f, 0.f);
                 ch[q] = ok ? c.x : -INFINITY;
                 // EROT folds the exp2 scale into the low part: lo * kexp.
-                clk[q] = ok ? (EROT ? c.y * kexp : c.y) : 0.f;
+                clk[q] = ok ? (EROT ? __fmul_rn(c.y, kexp) : c.y) : 0.f;
                 if constexpr (op_uses_cx(OP)) cxv[q] = c.z;
                 if constexpr (op_uses_cx2(OP)) cx2v[q] = c.w;
                 if constexpr (op_uses_cd(OP)) {
@@ -447,7 +477,7 @@ __global__ void __launch_bounds__(kThreads, 2) dense_pass(const PassParams p) {
                         const float4 r = p.rsplit ? s_rowp[(k & 1) * kRB + (i - r0)]
                                                   : make_float4(0.f, 0.f, 0.f, 0.f);
                         prh[r2] = r.x;
-                        prlk[r2] = EROT ? r.y * kexp : r.y;
+                        prlk[r2] = EROT ? __fmul_rn(r.y, kexp) : r.y;
                         prx[r2] = r.z;
                         prd[r2] = r.w;
                     } else {

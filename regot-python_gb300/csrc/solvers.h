@@ -13,6 +13,11 @@ void sinkhorn_newton_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double t
                          const regot_opts& o, regot_result* res);
 void sinkhorn_ssns_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
                        const regot_opts& o, regot_result* res);
+// sparsify_mat3 of T(gamma) (sinkhorn_sparsify3.cpp:276-405): nnz as the
+// reference counts it (kept entries including exact zeros of T) and, if mask
+// is not NULL, the stored kept entries as a row-major n x (m - 1) 0/1 mask.
+void erot_sparsify_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, const double* gamma,
+                       double delta, double density_hint, long long* nnz, int* mask);
 void qrot_lbfgs_dual_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
                          const regot_opts& o, regot_result* res);
 void qrot_assn_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,

@@ -287,6 +287,18 @@ class Problem:
             L.REGOT_MEM_HOST))
         return P
 
+    def erot_sparsify(self, reg, gamma, delta, density_hint, mask=True):
+        """sparsify_mat3 of T(gamma) (sinkhorn_sparsify3.cpp:276-405): returns
+        (nnz, kept) with nnz counted as the reference does (exact zeros of T
+        included) and kept the n x (m-1) boolean mask of stored entries."""
+        gamma = self._vec(gamma, self.n + self.m - 1)
+        nnz = np.zeros(1, dtype=np.int64)
+        K = np.zeros((self.n, self.m - 1), dtype=np.int32) if mask else None
+        self.ctx.check(self._lib.regot_erot_sparsify(
+            self.ctx.handle, self.handle, float(reg), gamma.ctypes.data, float(delta),
+            float(density_hint), nnz.ctypes.data, K.ctypes.data if mask else None))
+        return int(nnz[0]), (K.astype(bool) if mask else None)
+
     def qrot_dual_obj_grad(self, reg, gamma):
         gamma = self._vec(gamma, self.n + self.m)
         obj = np.zeros(1)

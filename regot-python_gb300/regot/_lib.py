@@ -82,7 +82,8 @@ EXPORTS = [
     "regot_problem_destroy", "regot_sinkhorn_bcd", "regot_sinkhorn_newton",
     "regot_sinkhorn_ssns", "regot_qrot_lbfgs_dual", "regot_qrot_assn",
     "regot_erot_optimal_beta", "regot_erot_optimal_alpha", "regot_erot_dual_obj_grad",
-    "regot_erot_hvp", "regot_erot_plan", "regot_qrot_dual_obj_grad", "regot_qrot_optimal_beta",
+    "regot_erot_hvp", "regot_erot_plan", "regot_erot_sparsify", "regot_qrot_dual_obj_grad",
+    "regot_qrot_optimal_beta",
     "regot_qrot_primal_val", "regot_qrot_plan", "regot_time_pass",
     "regot_erot_dual_obj_grad_noalloc",
 ]
@@ -128,6 +129,8 @@ def load() -> C.CDLL:
         lib.regot_erot_dual_obj_grad.argtypes = [vp, vp, C.c_double, vp, vp, vp]
         lib.regot_erot_hvp.argtypes = [vp, vp, C.c_double, vp, vp, vp]
         lib.regot_erot_plan.argtypes = [vp, vp, C.c_double, vp, vp, C.c_int]
+        lib.regot_erot_sparsify.argtypes = [vp, vp, C.c_double, vp, C.c_double, C.c_double, vp,
+                                             vp]
         lib.regot_qrot_dual_obj_grad.argtypes = [vp, vp, C.c_double, vp, vp, vp]
         lib.regot_qrot_optimal_beta.argtypes = [vp, vp, C.c_double, vp, vp]
         lib.regot_qrot_primal_val.argtypes = [vp, vp, C.c_double, vp, vp]
