@@ -59,6 +59,17 @@ def workload_config(n):
             "e2e": "regot.sinkhorn_bcd on pinned host M incl. upload, plan and D2H"}
 
 
+def max_over_ranks(x, dist=None, device="cpu"):
+    """Maximum of a per-rank scalar over all ranks (the slowest rank's time)."""
+    if dist is None:
+        return float(x)
+    import torch
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def rank_env():
     return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
             int(os.environ.get("LOCAL_RANK", "0")))
@@ -264,11 +275,7 @@ def main():
     if dist:
         dist.barrier()
     launches = ctx.kernel_launches() - launches0
-    elapsed = e0.elapsed_time(e1)
-    if dist:
-        t = torch.tensor([elapsed], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
+    elapsed = max_over_ranks(e0.elapsed_time(e1), dist, dev)
     ms_per_step = elapsed / args.steps
     value = elapsed / (args.steps * world)
     niter, mar = r.niter, r.mar_errs[-1]

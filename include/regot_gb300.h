@@ -77,8 +77,10 @@ typedef struct {
     double tau;           /* QROT extra regularisation (0.0) */
     const double* x0;     /* optional initial duals on the host, or NULL */
     int x0_len;
-    double cg_tol;        /* Newton-CG relative residual target (1e-10) */
-    int cg_max_iter;      /* per Newton step (0 = 2*(n+m)) */
+    double cg_tol;        /* relative residual target of the Newton-CG solve and of the
+                             SSNS method-1 solve (1e-10) */
+    int cg_max_iter;      /* per linear solve (0 = solver default: Newton 2*(n+m),
+                             SSNS method 0 2*(m-1), method 1 10*(m-1)) */
     int verbose;
     int plan;             /* 1 = fill result->plan, 0 = skip */
     int plan_mem;         /* REGOT_MEM_HOST or REGOT_MEM_DEVICE */

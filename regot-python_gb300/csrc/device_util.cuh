@@ -90,15 +90,17 @@ __device__ bool grid_reduce(const double (&vals)[K], double* block_parts, unsign
                             double (&out)[K]) {
     __shared__ double s_red[K][32];
     __shared__ bool s_last;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int nw = (blockDim.x + 31) >> 5;
+    const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    const int nthreads = blockDim.x * blockDim.y * blockDim.z;
+    const int lane = tid & 31, warp = tid >> 5;
+    const int nw = (nthreads + 31) >> 5;
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         const double v = warp_sum_d(vals[k]);
         if (lane == 0) s_red[k][warp] = v;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (tid == 0) {
 #pragma unroll
         for (int k = 0; k < K; ++k) {
             double s = 0.0;
@@ -115,7 +117,7 @@ __device__ bool grid_reduce(const double (&vals)[K], double* block_parts, unsign
     double part[K];
 #pragma unroll
     for (int k = 0; k < K; ++k) part[k] = 0.0;
-    for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x) {
+    for (unsigned b = tid; b < gridDim.x; b += nthreads) {
 #pragma unroll
         for (int k = 0; k < K; ++k) part[k] += __ldcg(&block_parts[(size_t)b * K + k]);
     }
@@ -126,7 +128,7 @@ __device__ bool grid_reduce(const double (&vals)[K], double* block_parts, unsign
         if (lane == 0) s_red[k][warp] = v;
     }
     __syncthreads();
-    if (threadIdx.x != 0) return false;
+    if (tid != 0) return false;
 #pragma unroll
     for (int k = 0; k < K; ++k) {
         double s = 0.0;
@@ -135,6 +137,33 @@ __device__ bool grid_reduce(const double (&vals)[K], double* block_parts, unsign
     }
     *counter = 0u;
     return true;
+}
+
+// Merge of `count` partials p[k * stride] (k = 0 .. count-1) for the 32
+// items of a (32, 8) block: item threadIdx.x, partials split over
+// threadIdx.y (k = y, y + 8, ...), then summed over y in order. The result
+// is valid in the threads with threadIdx.y == 0. Loads of one k are
+// coalesced across the 32 items.
+template <typename Acc>
+__device__ __forceinline__ double merge_2d(const Acc* p, int count, size_t stride, bool valid) {
+    __shared__ double s_m2[8][33];
+    double a0 = 0.0, a1 = 0.0;
+    if (valid) {
+        int k = threadIdx.y;
+        for (; k + 8 < count; k += 16) {
+            a0 += (double)p[(size_t)k * stride];
+            a1 += (double)p[(size_t)(k + 8) * stride];
+        }
+        if (k < count) a0 += (double)p[(size_t)k * stride];
+    }
+    s_m2[threadIdx.y][threadIdx.x] = a0 + a1;
+    __syncthreads();
+    double S = 0.0;
+    if (threadIdx.y == 0) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) S += s_m2[q][threadIdx.x];
+    }
+    return S;
 }
 
 // Stream-ordered device buffer (cudaMallocAsync / cudaFreeAsync).

@@ -29,9 +29,11 @@ namespace regot {
 
 namespace {
 
-// Finalize kernels merge FP64 partials: small blocks spread them over all SMs
-// (FP64 throughput per SM is low on this part).
-constexpr int kFinThreads = 64;
+// Finalize kernels: (32, 8) blocks, 32 rows (columns) per block with their
+// partials merged by 8 threads each (merge_2d), so the merge is not bound by
+// the latency of one thread's dependent loads.
+constexpr int kFinItems = 32;
+const dim3 kFinBlock(32, 8);
 
 struct BcdState {
     int done;
@@ -66,11 +68,11 @@ __global__ void k_bcd_row(const Acc* rp, int nslabs, int n, const double* anchor
                           double* hmar, double* htime, double* parts, BcdState* st,
                           int robust) {
     if (st->done) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.x * kFinItems + threadIdx.x;
     double v[3] = {0.0, 0.0, 0.0};
     double vmax = 0.0;
-    if (i < n) {
-        const double S = merge_strided(rp + i, nslabs, (size_t)n);
+    const double S = merge_2d(rp + i, nslabs, (size_t)n, i < n);
+    if (i < n && threadIdx.y == 0) {
         const double al = alpha[i];
         const double an = anchor[i];
         if (!robust && !sum_ok<MIXED>(S)) atomicOr(&st->bad, 1);
@@ -114,11 +116,11 @@ __global__ void k_bcd_col(const Acc* cp, int nrb, int m, const double* anchor,
                           const double* logb, const double* b, double reg, double* beta_next,
                           double* parts, BcdState* st, int robust) {
     if (st->done) return;
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.x * kFinItems + threadIdx.x;
     double v[1] = {0.0};
     double vmax = 0.0;
-    if (j < m) {
-        const double S = merge_strided(cp + j, nrb, (size_t)m);
+    const double S = merge_2d(cp + j, nrb, (size_t)m, j < m);
+    if (j < m && threadIdx.y == 0) {
         if (!robust && !sum_ok<MIXED>(S)) atomicOr(&st->bad, 2);
         const double bn = anchor[j] + reg * (logb[j] - log(S));
         beta_next[j] = bn;
@@ -203,7 +205,7 @@ void sinkhorn_bcd_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol,
 
     DBuf<double> alpha(n, st), alpha_next(n, st), beta(m, st), beta_next(m, st), anchor(
         std::max(n, m), st);
-    DBuf<double> hist(3 * (size_t)hist_cap, st), parts(3 * (size_t)cdiv(std::max(n, m), kFinThreads), st);
+    DBuf<double> hist(3 * (size_t)hist_cap, st), parts(3 * (size_t)cdiv(std::max(n, m), kFinItems), st);
     DBuf<double> scratch(std::max(n, m) + 8, st), rsum(n, st), csum(m, st);
     DBuf<BcdState> dst(1, st);
     double* hobj = hist.get();
@@ -251,16 +253,16 @@ void sinkhorn_bcd_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol,
     // K2: row dual alpha_{k+1}, anchor beta_k
     p2.ra = alpha_next.get();
     p2.cb = beta.get();
-    const int gn = cdiv(n, kFinThreads), gm = cdiv(m, kFinThreads), gnm = cdiv(std::max(n, m), 256);
+    const int gn = cdiv(n, kFinItems), gm = cdiv(m, kFinItems), gnm = cdiv(std::max(n, m), 256);
 
     auto launch_row = [&](const double* anc, int robust) {
         if (mixed)
-            k_bcd_row<float, true><<<gn, kFinThreads, 0, st>>>(
+            k_bcd_row<float, true><<<gn, kFinBlock, 0, st>>>(
                 (const float*)ops.buf().rowpart.get(), sh.nslabs, n, anc, alpha.get(), P->a,
                 ops.loga(), reg, ops.sum_a(), ops.sum_bt(), alpha_next.get(), hobj, hmar, htime,
                 parts.get(), S, robust);
         else
-            k_bcd_row<double, false><<<gn, kFinThreads, 0, st>>>(
+            k_bcd_row<double, false><<<gn, kFinBlock, 0, st>>>(
                 (const double*)ops.buf().rowpart.get(), sh.nslabs, n, anc, alpha.get(), P->a,
                 ops.loga(), reg, ops.sum_a(), ops.sum_bt(), alpha_next.get(), hobj, hmar, htime,
                 parts.get(), S, robust);
@@ -268,11 +270,11 @@ void sinkhorn_bcd_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol,
     };
     auto launch_col = [&](const double* anc, int robust) {
         if (mixed)
-            k_bcd_col<float, true><<<gm, kFinThreads, 0, st>>>(
+            k_bcd_col<float, true><<<gm, kFinBlock, 0, st>>>(
                 (const float*)ops.buf().colpart.get(), sh.nrb, m, anc, ops.logb(), P->b, reg,
                 beta_next.get(), parts.get(), S, robust);
         else
-            k_bcd_col<double, false><<<gm, kFinThreads, 0, st>>>(
+            k_bcd_col<double, false><<<gm, kFinBlock, 0, st>>>(
                 (const double*)ops.buf().colpart.get(), sh.nrb, m, anc, ops.logb(), P->b, reg,
                 beta_next.get(), parts.get(), S, robust);
         count_launch();
