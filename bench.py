@@ -314,8 +314,10 @@ def main():
     Mp = torch.empty((n, n), dtype=torch.float32, pin_memory=True)
     Mp.numpy()[:] = M
     Mh = Mp.numpy()
-    for _ in range(1):
-        regot.sinkhorn_bcd(Mh, a, b, REG, tol=TOL, max_iter=MAX_ITER, device=local)
+    # two warm-up calls: a result kept alive across the next call holds one
+    # page-locked plan block, so steady state cycles through two
+    for _ in range(2):
+        re = regot.sinkhorn_bcd(Mh, a, b, REG, tol=TOL, max_iter=MAX_ITER, device=local)
     torch.cuda.synchronize(dev)
     t = time.perf_counter()
     e2e_steps = max(1, min(args.steps, 5))

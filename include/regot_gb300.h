@@ -125,6 +125,14 @@ int regot_problem_create(regot_ctx* ctx, const regot_problem_desc* desc, int pre
                          regot_dproblem** out);
 void regot_problem_destroy(regot_dproblem* prob);
 
+/* Page-locked host memory for result buffers (the n x m plan): a device to
+ * host copy into it runs at the full link bandwidth, where a copy into
+ * pageable memory is staged by the driver. Freed blocks are kept (up to
+ * 4 GiB) and reused. No counterpart in the reference, which returns plans in
+ * ordinary heap memory (src/sinkhorn_result.h:32-50). */
+int regot_host_alloc(size_t bytes, void** out);
+void regot_host_free(void* ptr);
+
 /* ---- Solvers (reference: src/solvers.cpp:359-441 and 69-148) ---- */
 
 /* sinkhorn_bcd (src/sinkhorn_bcd.cpp:14-124). */

@@ -4,7 +4,10 @@
 // exceptions into a status code and a per-context message.
 #include <cmath>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "device_util.cuh"
@@ -110,7 +113,60 @@ void finish_erot_result(ErotOps& ops, const double* d_gamma, const double* hobj,
 
 }  // namespace regot
 
+namespace {
+
+// Page-locked host blocks for results. cudaHostAlloc of a large block costs
+// milliseconds, so freed blocks are kept (up to kPinnedCacheBytes) and handed
+// out again to requests of up to their size.
+constexpr size_t kPinnedCacheBytes = size_t(4) << 30;
+std::mutex g_pinned_mutex;
+std::unordered_map<void*, size_t> g_pinned_live;
+std::multimap<size_t, void*> g_pinned_free;
+size_t g_pinned_free_bytes = 0;
+
+}  // namespace
+
 extern "C" {
+
+int regot_host_alloc(size_t bytes, void** out) {
+    if (!out) return REGOT_ERR_INVALID_ARG;
+    *out = nullptr;
+    if (bytes == 0) bytes = 1;
+    std::lock_guard<std::mutex> lock(g_pinned_mutex);
+    auto it = g_pinned_free.lower_bound(bytes);
+    if (it != g_pinned_free.end() && it->first <= 2 * bytes) {
+        *out = it->second;
+        g_pinned_live[it->second] = it->first;
+        g_pinned_free_bytes -= it->first;
+        g_pinned_free.erase(it);
+        return REGOT_OK;
+    }
+    void* p = nullptr;
+    if (cudaHostAlloc(&p, bytes, cudaHostAllocPortable) != cudaSuccess) {
+        cudaGetLastError();
+        return REGOT_ERR_CUDA;
+    }
+    g_pinned_live[p] = bytes;
+    *out = p;
+    return REGOT_OK;
+}
+
+void regot_host_free(void* ptr) {
+    if (!ptr) return;
+    std::lock_guard<std::mutex> lock(g_pinned_mutex);
+    auto it = g_pinned_live.find(ptr);
+    if (it == g_pinned_live.end()) return;
+    const size_t bytes = it->second;
+    g_pinned_live.erase(it);
+    g_pinned_free.emplace(bytes, ptr);
+    g_pinned_free_bytes += bytes;
+    while (g_pinned_free_bytes > kPinnedCacheBytes && !g_pinned_free.empty()) {
+        auto small = g_pinned_free.begin();  // release the smallest blocks first
+        cudaFreeHost(small->second);
+        g_pinned_free_bytes -= small->first;
+        g_pinned_free.erase(small);
+    }
+}
 
 void regot_opts_init(regot_opts* o) {
     if (!o) return;

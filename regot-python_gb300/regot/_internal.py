@@ -192,7 +192,7 @@ class Problem:
             raise ValueError("max_iter must be non-negative")
         cap = max_iter + 2
         dual = np.zeros(n + m if qrot else n + m - 1)
-        plan = np.zeros((n, m)) if want_plan else None
+        plan = L.host_empty((n, m)) if want_plan else None
         hist = np.zeros((5, cap))
         r = L.Result()
         r.hist_cap = cap

@@ -10,6 +10,9 @@ from __future__ import annotations
 import ctypes as C
 import os
 import threading
+import weakref
+
+import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(os.path.dirname(_HERE), "_build", "libregot_gb300.so")
@@ -85,7 +88,7 @@ EXPORTS = [
     "regot_erot_hvp", "regot_erot_plan", "regot_erot_sparsify", "regot_qrot_dual_obj_grad",
     "regot_qrot_optimal_beta",
     "regot_qrot_primal_val", "regot_qrot_plan", "regot_time_pass",
-    "regot_erot_dual_obj_grad_noalloc",
+    "regot_erot_dual_obj_grad_noalloc", "regot_host_alloc", "regot_host_free",
 ]
 
 _lib = None
@@ -138,6 +141,9 @@ def load() -> C.CDLL:
         lib.regot_time_pass.argtypes = [vp, vp, C.c_int, C.c_double, C.c_int]
         lib.regot_erot_dual_obj_grad_noalloc.argtypes = [
             vp, C.c_longlong, C.c_int, C.c_int, vp, vp, vp, C.c_double, vp, vp, vp]
+        lib.regot_host_alloc.argtypes = [C.c_size_t, C.POINTER(vp)]
+        lib.regot_host_free.argtypes = [vp]
+        lib.regot_host_free.restype = None
         _lib = lib
         return lib
 
@@ -195,3 +201,25 @@ def context(device: int = 0) -> Context:
         with _lock:
             _contexts[device] = ctx
     return ctx
+
+
+# Results at least this large go to page-locked memory.
+PINNED_MIN_BYTES = 1 << 20
+
+
+def host_empty(shape, dtype=np.float64) -> np.ndarray:
+    """numpy array in page-locked host memory (regot_host_alloc) for large
+    device-to-host results; the block returns to the library's cache when the
+    last view of the array is gone. Small arrays are ordinary numpy arrays."""
+    dtype = np.dtype(dtype)
+    count = int(np.prod(shape))
+    nbytes = count * dtype.itemsize
+    if nbytes < PINNED_MIN_BYTES:
+        return np.empty(shape, dtype=dtype)
+    lib = load()
+    ptr = C.c_void_p()
+    if lib.regot_host_alloc(nbytes, C.byref(ptr)) != REGOT_OK:
+        return np.empty(shape, dtype=dtype)
+    buf = (C.c_byte * nbytes).from_address(ptr.value)
+    weakref.finalize(buf, lib.regot_host_free, C.c_void_p(ptr.value))
+    return np.frombuffer(buf, dtype=dtype, count=count).reshape(shape)
