@@ -112,3 +112,24 @@ def test_sinkhorn_bcd_x0_and_max_iter(precision):
     np.testing.assert_allclose(r.mar_errs, o.mar_errs, rtol=rt, atol=MAR_ATOL[precision])
     r0 = regot.sinkhorn_bcd(M, a, b, reg, tol=1e-12, max_iter=0, precision=precision)
     assert r0.niter == 0 and len(r0.mar_errs) == 1
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_sinkhorn_bcd_fallback_paths(precision):
+    # Duals far below their final size (x0 ~ 1e-3, final duals ~ 10) and an
+    # iterate whose row sums all underflow (alpha = -40 at reg 0.05, handled
+    # by the max-anchored updates): the solve must follow the oracle.
+    M, a, b = readme_example(100, 80)
+    Mq = _as_precision(M, precision)
+    n, m = M.shape
+    reg = 0.05
+    for x0 in (np.full(n + m - 1, 1e-3), np.r_[np.full(n, -40.0), np.zeros(m - 1)]):
+        tol = TOL[precision]
+        r = regot.sinkhorn_bcd(M, a, b, reg, tol=tol, max_iter=3000, precision=precision, x0=x0)
+        o = O.sinkhorn_bcd(Mq, a, b, reg, tol=tol, max_iter=3000, x0=x0)
+        assert abs(r.niter - o.niter) <= (1 if precision == "fp64" else 0.05 * o.niter + 3)
+        k = min(len(o.mar_errs), len(r.mar_errs), 50)
+        rt = 1e-8 if precision == "fp64" else 1e-3
+        np.testing.assert_allclose(r.mar_errs[:k], o.mar_errs[:k], rtol=rt, atol=MAR_ATOL[precision])
+        np.testing.assert_allclose(r.plan, o.plan, rtol=0,
+                                   atol=(1e-9 if precision == "fp64" else 1e-5) * o.plan.max())
