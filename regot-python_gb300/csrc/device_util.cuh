@@ -44,6 +44,29 @@ __device__ __forceinline__ void warp_atomic_max_abs(double* target, double v) {
                   (unsigned long long)__double_as_longlong(a));
 }
 
+// Block-wide version (all threads of the block must call it): one atomic
+// per block instead of one per warp, so that the many blocks of a finalize
+// kernel do not serialise on the target's cache line.
+__device__ __forceinline__ void block_atomic_max_abs(double* target, double v) {
+    __shared__ double s_bmax[32];
+    const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    const int nthreads = blockDim.x * blockDim.y * blockDim.z;
+    double a = fabs(v);
+    if (!(a == a) || isinf(a)) a = 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) a = fmax(a, __shfl_xor_sync(0xffffffffu, a, o));
+    if ((tid & 31) == 0) s_bmax[tid >> 5] = a;
+    __syncthreads();
+    if (tid == 0) {
+        double mx = 0.0;
+        for (int w = 0; w < (nthreads + 31) >> 5; ++w) mx = fmax(mx, s_bmax[w]);
+        if (mx > 0.0)
+            atomicMax(reinterpret_cast<unsigned long long*>(target),
+                      (unsigned long long)__double_as_longlong(mx));
+    }
+    __syncthreads();
+}
+
 // Sum of count values p[k * stride], k = 0..count-1, in FP64. Loads are
 // issued eight at a time into four independent accumulators, so that the
 // merge is bound by memory throughput instead of one load latency per term;

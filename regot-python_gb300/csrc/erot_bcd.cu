@@ -61,12 +61,25 @@ __device__ __forceinline__ bool sum_ok(double s) {
 // Row finalize of K1: gradient/objective of iterate k, history, stopping
 // test, alpha_{k+1}. `anchor` is the row vector the pass used (alpha itself
 // on the fast path, -max_j(beta_j - M_ij) on the robust path).
+// Fixed hi/lo grid of the ping-pong sweeps: the finalize kernels write the
+// FP32 split of the duals they produce, for the next pass.
+struct SplitOut {
+    float4* out = nullptr;  // null: no split written
+    double g = 1.0, inv_g = 1.0;
+    double bound = 0.0;     // |dual| < bound keeps hi exact on the grid g
+};
+
+__device__ __forceinline__ float4 split_fixed(double v, const SplitOut& so) {
+    const double h = rint(v * so.inv_g) * so.g;
+    return make_float4((float)h, (float)(v - h), 0.f, 0.f);
+}
+
 template <typename Acc, bool MIXED>
 __global__ void k_bcd_row(const Acc* rp, int nslabs, int n, const double* anchor,
                           const double* alpha, const double* a, const double* loga, double reg,
                           double sum_a, double sum_bt, double* alpha_next, double* hobj,
                           double* hmar, double* htime, double* parts, BcdState* st,
-                          int robust) {
+                          int robust, SplitOut so) {
     if (st->done) return;
     const int i = blockIdx.x * kFinItems + threadIdx.x;
     double v[3] = {0.0, 0.0, 0.0};
@@ -84,8 +97,12 @@ __global__ void k_bcd_row(const Acc* rp, int nslabs, int n, const double* anchor
         const double an_next = an + reg * (loga[i] - log(S));
         alpha_next[i] = an_next;
         vmax = an_next;
+        if (so.out) {
+            if (!(fabs(an_next) < so.bound)) atomicOr(&st->bad, 4);
+            so.out[i] = split_fixed(an_next, so);
+        }
     }
-    warp_atomic_max_abs(&st->maxabs, vmax);
+    block_atomic_max_abs(&st->maxabs, vmax);
     __threadfence();
     double out[3];
     if (grid_reduce<3>(v, parts, &st->counter, out)) {
@@ -114,7 +131,7 @@ __global__ void k_bcd_row(const Acc* rp, int nslabs, int n, const double* anchor
 template <typename Acc, bool MIXED>
 __global__ void k_bcd_col(const Acc* cp, int nrb, int m, const double* anchor,
                           const double* logb, const double* b, double reg, double* beta_next,
-                          double* parts, BcdState* st, int robust) {
+                          double* parts, BcdState* st, int robust, SplitOut so, int advance) {
     if (st->done) return;
     const int j = blockIdx.x * kFinItems + threadIdx.x;
     double v[1] = {0.0};
@@ -126,8 +143,12 @@ __global__ void k_bcd_col(const Acc* cp, int nrb, int m, const double* anchor,
         beta_next[j] = bn;
         if (j < m - 1) v[0] = b[j] * bn;
         vmax = bn;
+        if (so.out) {
+            if (!(fabs(bn) < so.bound)) atomicOr(&st->bad, 8);
+            so.out[j] = split_fixed(bn, so);
+        }
     }
-    warp_atomic_max_abs(&st->maxabs, vmax);
+    block_atomic_max_abs(&st->maxabs, vmax);
     __threadfence();
     double out[1];
     if (grid_reduce<1>(v, parts, &st->counter, out)) {
@@ -137,6 +158,7 @@ __global__ void k_bcd_col(const Acc* cp, int nrb, int m, const double* anchor,
         }
         st->sum_bb = out[0];
         st->beta_last = beta_next[m - 1];
+        if (advance) st->iter += 1;
     }
 }
 
@@ -243,82 +265,200 @@ void sinkhorn_bcd_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol,
     ops.maxabs(alpha.get(), n, beta.get(), m, &S->maxabs);
     REGOT_CHECK_LAUNCH();
 
-    PassParams p1 = ops.base_params();
-    p1.grid = &S->maxabs;
-    p1.done = &S->done;
-    PassParams p2 = p1;
-    // K1: anchor alpha_k, column dual beta_k
-    p1.ra = alpha.get();
-    p1.cb = beta.get();
-    // K2: row dual alpha_{k+1}, anchor beta_k
-    p2.ra = alpha_next.get();
-    p2.cb = beta.get();
-    const int gn = cdiv(n, kFinItems), gm = cdiv(m, kFinItems), gnm = cdiv(std::max(n, m), 256);
-
-    auto launch_row = [&](const double* anc, int robust) {
-        if (mixed)
-            k_bcd_row<float, true><<<gn, kFinBlock, 0, st>>>(
-                (const float*)ops.buf().rowpart.get(), sh.nslabs, n, anc, alpha.get(), P->a,
-                ops.loga(), reg, ops.sum_a(), ops.sum_bt(), alpha_next.get(), hobj, hmar, htime,
-                parts.get(), S, robust);
-        else
-            k_bcd_row<double, false><<<gn, kFinBlock, 0, st>>>(
-                (const double*)ops.buf().rowpart.get(), sh.nslabs, n, anc, alpha.get(), P->a,
-                ops.loga(), reg, ops.sum_a(), ops.sum_bt(), alpha_next.get(), hobj, hmar, htime,
-                parts.get(), S, robust);
-        count_launch();
-    };
-    auto launch_col = [&](const double* anc, int robust) {
-        if (mixed)
-            k_bcd_col<float, true><<<gm, kFinBlock, 0, st>>>(
-                (const float*)ops.buf().colpart.get(), sh.nrb, m, anc, ops.logb(), P->b, reg,
-                beta_next.get(), parts.get(), S, robust);
-        else
-            k_bcd_col<double, false><<<gm, kFinBlock, 0, st>>>(
-                (const double*)ops.buf().colpart.get(), sh.nrb, m, anc, ops.logb(), P->b, reg,
-                beta_next.get(), parts.get(), S, robust);
-        count_launch();
-    };
-    auto launch_commit = [&]() {
-        k_bcd_commit<<<gnm, 256, 0, st>>>(n, m, alpha.get(), alpha_next.get(), beta.get(),
-                                          beta_next.get(), S);
-        count_launch();
-    };
-    auto sweep = [&]() {
-        ops.pass(OP_E_ROW, p1);
-        launch_row(alpha.get(), 0);
-        ops.pass(OP_E_COL, p2);
-        launch_col(beta.get(), 0);
-        launch_commit();
-    };
-
-    // Capture one sweep as a graph; replay it in batches.
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    long long* saved_counter = g_launch_counter;
-    long long graph_kernels = 0;
-    g_launch_counter = &graph_kernels;
-    REGOT_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    sweep();
-    REGOT_CUDA(cudaStreamEndCapture(st, &graph));
-    g_launch_counter = saved_counter;
-    REGOT_CUDA(cudaGraphInstantiate(&exec, graph, 0));
-
     BcdState hs{};
-    int batch = 4;
-    long long passes = 0;
-    long long launched = 0;
-    int prev_iter = -1;
-    double prev_g = 0.0;
-    for (;;) {
-        for (int q = 0; q < batch; ++q) REGOT_CUDA(cudaGraphLaunch(exec, st));
-        launched += batch;
-        count_launch(graph_kernels * batch);
+    auto read_state = [&]() {
         d2h(&hs, S, sizeof(hs), st);
         sync(st);
-        if (hs.bad) {
-            // Robust redo of the half-sweep that left the safe range.
-            const int which = hs.bad;
+    };
+    // Size the next batch of sweeps from the observed linear convergence
+    // rate, so that few sweeps are launched past convergence.
+    int prev_iter = -1;
+    double prev_g = 0.0;
+    auto next_batch = [&](int batch) {
+        const int k = hs.hist_len - 1;
+        int next = std::min(batch * 2, 64);
+        if (prev_iter >= 0 && k > prev_iter && hs.last_gnorm > 0.0 && prev_g > hs.last_gnorm) {
+            const double rate = std::log(prev_g / hs.last_gnorm) / (k - prev_iter);
+            const double need = std::log(hs.last_gnorm / std::max(tol, 1e-300)) / rate;
+            if (std::isfinite(need)) next = (int)std::ceil(need) + 1;
+        }
+        prev_iter = k;
+        prev_g = hs.last_gnorm;
+        return std::max(1, std::min(next, std::min(64, max_iter + 1 - k)));
+    };
+    const int gn = cdiv(n, kFinItems), gm = cdiv(m, kFinItems), gnm = cdiv(std::max(n, m), 256);
+
+    // ---- ping-pong path: 4 kernels per sweep ----
+    // The duals alternate between (alpha, beta) for even iterates and
+    // (alpha_next, beta_next) for odd ones, so no commit kernel is needed, and
+    // the finalize kernels write the FP32 hi/lo split of the duals they
+    // produce on a grid fixed for the solve (8x headroom over the initial
+    // duals), so no split kernel runs before the passes either. A dual that
+    // outgrows the grid, or a sum out of range, hands the solve over to the
+    // general path below, which re-splits before every pass.
+    int pending = 0;  // robust column half-sweep owed to the general path
+    bool finished = false;
+    {
+        read_state();
+        const double m0 = hs.maxabs;
+        const int e = (m0 > 0.0 && std::isfinite(m0)) ? std::ilogb(m0) : 0;
+        float4* rs = const_cast<float4*>(ops.rsplit());
+        float4* cs = const_cast<float4*>(ops.csplit());
+        SplitOut so_r, so_c;
+        if (mixed) {
+            DBuf<double> gval(1, st);
+            const double gv = std::ldexp(1.0, e + 3);
+            h2d(gval.get(), &gv, sizeof(double), st);
+            PassParams q = ops.base_params();
+            q.ra = alpha.get();
+            q.cb = beta.get();
+            q.grid = gval.get();
+            launch_split(q, rs, cs, nullptr, st);
+            so_r.g = so_c.g = std::ldexp(1.0, e + 3 - 21);
+            so_r.inv_g = so_c.inv_g = std::ldexp(1.0, -(e + 3 - 21));
+            so_r.bound = so_c.bound = std::ldexp(1.0, e + 4);
+            so_r.out = rs;
+            so_c.out = cs;
+        }
+        double* A[2] = {alpha.get(), alpha_next.get()};
+        double* B[2] = {beta.get(), beta_next.get()};
+        auto half_sweeps = [&](int q) {
+            PassParams pr = ops.base_params();
+            pr.done = &S->done;
+            pr.ra = A[q];
+            pr.cb = B[q];
+            ops.pass_presplit(OP_E_ROW, pr);
+            if (mixed)
+                k_bcd_row<float, true><<<gn, kFinBlock, 0, st>>>(
+                    (const float*)ops.buf().rowpart.get(), sh.nslabs, n, A[q], A[q], P->a,
+                    ops.loga(), reg, ops.sum_a(), ops.sum_bt(), A[1 - q], hobj, hmar, htime,
+                    parts.get(), S, 0, so_r);
+            else
+                k_bcd_row<double, false><<<gn, kFinBlock, 0, st>>>(
+                    (const double*)ops.buf().rowpart.get(), sh.nslabs, n, A[q], A[q], P->a,
+                    ops.loga(), reg, ops.sum_a(), ops.sum_bt(), A[1 - q], hobj, hmar, htime,
+                    parts.get(), S, 0, so_r);
+            PassParams pc = pr;
+            pc.ra = A[1 - q];
+            pc.cb = B[q];
+            ops.pass_presplit(OP_E_COL, pc);
+            if (mixed)
+                k_bcd_col<float, true><<<gm, kFinBlock, 0, st>>>(
+                    (const float*)ops.buf().colpart.get(), sh.nrb, m, B[q], ops.logb(), P->b,
+                    reg, B[1 - q], parts.get(), S, 0, so_c, 1);
+            else
+                k_bcd_col<double, false><<<gm, kFinBlock, 0, st>>>(
+                    (const double*)ops.buf().colpart.get(), sh.nrb, m, B[q], ops.logb(), P->b,
+                    reg, B[1 - q], parts.get(), S, 0, so_c, 1);
+            count_launch(2);
+        };
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        long long* saved_counter = g_launch_counter;
+        long long graph_kernels = 0;
+        g_launch_counter = &graph_kernels;
+        REGOT_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        half_sweeps(0);
+        half_sweeps(1);
+        REGOT_CUDA(cudaStreamEndCapture(st, &graph));
+        g_launch_counter = saved_counter;
+        REGOT_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+
+        int batch = 4;  // sweeps; the graph runs two per launch
+        long long launched = 0;
+        for (;;) {
+            const int reps = (batch + 1) / 2;
+            for (int q = 0; q < reps; ++q) REGOT_CUDA(cudaGraphLaunch(exec, st));
+            launched += 2LL * reps;
+            count_launch(graph_kernels * reps);
+            read_state();
+            if (hs.bad) break;
+            if (hs.done) {
+                finished = true;
+                break;
+            }
+            if (launched > 2LL * max_iter + 64)
+                throw Error(REGOT_ERR_NUMERIC, "BCD did not terminate");
+            batch = next_batch(batch);
+        }
+        cudaGraphExecDestroy(exec);
+        cudaGraphDestroy(graph);
+        const int k = hs.iter;
+        const size_t an = n * sizeof(double), bm = m * sizeof(double);
+        if (finished || (hs.bad & (1 | 4))) {
+            // iterate k (alpha_k, beta_k) is complete in slot k % 2; when
+            // handing over it is not yet recorded
+            if (k % 2 == 1) {
+                d2d(alpha.get(), alpha_next.get(), an, st);
+                d2d(beta.get(), beta_next.get(), bm, st);
+            }
+        } else {
+            // column side: iterate k is recorded, alpha_{k+1} is complete in
+            // slot (k + 1) % 2 and beta_k intact in slot k % 2; beta_{k+1} is
+            // recomputed from alpha_{k+1} by the robust update
+            if ((k + 1) % 2 == 0) d2d(alpha_next.get(), alpha.get(), an, st);
+            if (k % 2 == 1) d2d(beta.get(), beta_next.get(), bm, st);
+            pending = 2;
+        }
+        if (!finished) {
+            const int zero = 0;
+            h2d(&S->bad, &zero, sizeof(int), st);
+            h2d(&S->done, &zero, sizeof(int), st);
+            sync(st);
+        }
+    }
+
+    // ---- general path: split before each pass, commit after each sweep ----
+    if (!finished) {
+        PassParams p1 = ops.base_params();
+        p1.grid = &S->maxabs;
+        p1.done = &S->done;
+        PassParams p2 = p1;
+        // K1: anchor alpha_k, column dual beta_k
+        p1.ra = alpha.get();
+        p1.cb = beta.get();
+        // K2: row dual alpha_{k+1}, anchor beta_k
+        p2.ra = alpha_next.get();
+        p2.cb = beta.get();
+
+        auto launch_row = [&](const double* anc, int robust) {
+            if (mixed)
+                k_bcd_row<float, true><<<gn, kFinBlock, 0, st>>>(
+                    (const float*)ops.buf().rowpart.get(), sh.nslabs, n, anc, alpha.get(), P->a,
+                    ops.loga(), reg, ops.sum_a(), ops.sum_bt(), alpha_next.get(), hobj, hmar,
+                    htime, parts.get(), S, robust, SplitOut());
+            else
+                k_bcd_row<double, false><<<gn, kFinBlock, 0, st>>>(
+                    (const double*)ops.buf().rowpart.get(), sh.nslabs, n, anc, alpha.get(), P->a,
+                    ops.loga(), reg, ops.sum_a(), ops.sum_bt(), alpha_next.get(), hobj, hmar,
+                    htime, parts.get(), S, robust, SplitOut());
+            count_launch();
+        };
+        auto launch_col = [&](const double* anc, int robust) {
+            if (mixed)
+                k_bcd_col<float, true><<<gm, kFinBlock, 0, st>>>(
+                    (const float*)ops.buf().colpart.get(), sh.nrb, m, anc, ops.logb(), P->b, reg,
+                    beta_next.get(), parts.get(), S, robust, SplitOut(), 0);
+            else
+                k_bcd_col<double, false><<<gm, kFinBlock, 0, st>>>(
+                    (const double*)ops.buf().colpart.get(), sh.nrb, m, anc, ops.logb(), P->b,
+                    reg, beta_next.get(), parts.get(), S, robust, SplitOut(), 0);
+            count_launch();
+        };
+        auto launch_commit = [&]() {
+            k_bcd_commit<<<gnm, 256, 0, st>>>(n, m, alpha.get(), alpha_next.get(), beta.get(),
+                                              beta_next.get(), S);
+            count_launch();
+        };
+        auto sweep = [&]() {
+            ops.pass(OP_E_ROW, p1);
+            launch_row(alpha.get(), 0);
+            ops.pass(OP_E_COL, p2);
+            launch_col(beta.get(), 0);
+            launch_commit();
+        };
+        // Robust redo of the half-sweep that left the safe range.
+        auto robust = [&](int which) {
             const int zero = 0;
             h2d(&S->bad, &zero, sizeof(int), st);
             h2d(&S->done, &zero, sizeof(int), st);
@@ -348,29 +488,40 @@ void sinkhorn_bcd_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol,
                 launch_commit();
             }
             REGOT_CHECK_LAUNCH();
-            d2h(&hs, S, sizeof(hs), st);
-            sync(st);
+            read_state();
             if (hs.bad) throw Error(REGOT_ERR_NONFINITE, "non-finite row or column sums in BCD");
+        };
+        if (pending) robust(pending);
+
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        long long* saved_counter = g_launch_counter;
+        long long graph_kernels = 0;
+        g_launch_counter = &graph_kernels;
+        REGOT_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        sweep();
+        REGOT_CUDA(cudaStreamEndCapture(st, &graph));
+        g_launch_counter = saved_counter;
+        REGOT_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+
+        int batch = 4;
+        long long launched = 0;
+        read_state();
+        while (!hs.done) {
+            for (int q = 0; q < batch; ++q) REGOT_CUDA(cudaGraphLaunch(exec, st));
+            launched += batch;
+            count_launch(graph_kernels * batch);
+            read_state();
+            if (hs.bad) robust(hs.bad);
+            if (hs.done) break;
+            if (launched > 2LL * max_iter + 64)
+                throw Error(REGOT_ERR_NUMERIC, "BCD did not terminate");
+            batch = next_batch(batch);
         }
-        if (hs.done) break;
-        if (launched > 2LL * max_iter + 64)
-            throw Error(REGOT_ERR_NUMERIC, "BCD did not terminate");
-        // Size the next batch from the observed linear convergence rate, so
-        // that few sweeps are launched past convergence.
-        const int k = hs.hist_len - 1;
-        int next = std::min(batch * 2, 64);
-        if (prev_iter >= 0 && k > prev_iter && hs.last_gnorm > 0.0 && prev_g > hs.last_gnorm) {
-            const double rate = std::log(prev_g / hs.last_gnorm) / (k - prev_iter);
-            const double need = std::log(hs.last_gnorm / std::max(tol, 1e-300)) / rate;
-            if (std::isfinite(need)) next = (int)std::ceil(need) + 1;
-        }
-        prev_iter = k;
-        prev_g = hs.last_gnorm;
-        batch = std::max(1, std::min(next, std::min(64, max_iter + 1 - k)));
+        cudaGraphExecDestroy(exec);
+        cudaGraphDestroy(graph);
     }
-    cudaGraphExecDestroy(exec);
-    cudaGraphDestroy(graph);
-    passes = 2LL * hs.hist_len;
+    const long long passes = 2LL * hs.hist_len;
 
     // Results: gauge-fixed dual, plan, histories.
     DBuf<double> gamma(n + m, st);

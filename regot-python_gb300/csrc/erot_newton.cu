@@ -184,7 +184,7 @@ __global__ void k_cg_c(int N, const double* z, double* p, NewtonState* st) {
         pv = z[t] + st->beta * p[t];
         p[t] = pv;
     }
-    warp_atomic_max_abs(&st->maxabs, pv);
+    block_atomic_max_abs(&st->maxabs, pv);
 }
 
 // g'd and a'd_alpha + b~'d_beta~ for the line search.
@@ -202,7 +202,7 @@ __global__ void k_dir_dots(int n, int m, const double* g, const double* d, const
         v[0] = g[t] * dv;
         v[1] = b[t - n] * dv;
     }
-    warp_atomic_max_abs(&st->maxabs, dv);
+    block_atomic_max_abs(&st->maxabs, dv);
     double out[2];
     __threadfence();
     if (grid_reduce<2>(v, parts, &st->counter, out)) {
@@ -218,7 +218,7 @@ __global__ void k_axpy_gamma(int N, double s, const double* d, double* gamma, Ne
         gv = gamma[t] + s * d[t];
         gamma[t] = gv;
     }
-    warp_atomic_max_abs(&st->maxabs, gv);
+    block_atomic_max_abs(&st->maxabs, gv);
 }
 
 __global__ void k_newton_start(NewtonState* st) { st->t0 = globaltimer_ns(); }

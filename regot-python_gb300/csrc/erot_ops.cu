@@ -38,12 +38,7 @@ __global__ void k_maxabs(const double* x, int nx, const double* y, int ny, doubl
         const double t = i < nx ? x[i] : y[i - nx];
         if (isfinite(t)) v = fmax(v, fabs(t));
     }
-    v = fmax(v, __shfl_xor_sync(0xffffffffu, v, 16));
-    v = fmax(v, __shfl_xor_sync(0xffffffffu, v, 8));
-    v = fmax(v, __shfl_xor_sync(0xffffffffu, v, 4));
-    v = fmax(v, __shfl_xor_sync(0xffffffffu, v, 2));
-    v = fmax(v, __shfl_xor_sync(0xffffffffu, v, 1));
-    if ((threadIdx.x & 31) == 0) atomic_max_abs(out, v);
+    block_atomic_max_abs(out, v);
 }
 
 // anchor = -max partials (row or column direction).
