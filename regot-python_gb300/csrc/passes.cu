@@ -213,10 +213,9 @@ __device__ __forceinline__ void split(double v, double g, double inv_g, float& h
     lo = (float)(v - h);
 }
 
-// Row stages of the per-warp copy ring (one row segment of CW elements each).
-// Four 2 KB row buffers per warp: with two CTAs of 8 warps per SM, 128 KB of
-// copies are in flight per SM, where bulk-copy streaming reaches the measured
-// HBM bandwidth on this part (it loses bandwidth well beyond that).
+// Row stages of the per-warp copy ring (one row segment of CW elements each):
+// four 2 KB row buffers per warp, 128 KB per SM with two CTAs of 8 warps.
+// Three stages stream measurably slower; five gain nothing.
 template <int OP, typename Acc, int CW>
 __host__ __device__ constexpr int ring_stages() {
     return 4;
@@ -269,10 +268,15 @@ __device__ __forceinline__ T warp_reduce_rows(T (&v)[N], int lane) {
 // Persistent dense pass. The grid holds as many CTAs as fit on the SMs; CTA
 // b processes tiles b, b + G, b + 2G, ... (tile t = row block t / nslabs,
 // column slab t % nslabs; RB rows x CW columns). Each warp streams RB/8 rows
-// of every tile through its own ring of NS shared-memory row buffers: lane 0
-// keeps NS row copies (cp.async.bulk, one mbarrier per buffer) in flight
-// ahead of the row the warp is reducing, across tile boundaries, so HBM
-// never idles between waves of CTAs.
+// of every tile through its own ring of NS shared-memory row buffers, NS rows
+// ahead of the row it is reducing and across tile boundaries, so HBM never
+// idles between waves of CTAs. Every lane copies the 16-byte vectors of a row
+// that it will itself read (cp.async.cg, one commit group per row), so a
+// row is ready once the lane's own group has landed (cp.async.wait_group):
+// no barrier between lanes and no proxy fence. Issuing each 2 KB row as one
+// bulk copy from lane 0 (cp.async.bulk on an mbarrier) streamed about 10 %
+// slower at n = m = 8192 (0.71 against 0.79 of the measured HBM bandwidth).
+// The per-tile column / row parameters do go through bulk copies.
 template <typename TM, int OP>
 __global__ void __launch_bounds__(kThreads, 2) dense_pass(const PassParams p) {
     if (p.done && *p.done) return;
@@ -311,12 +315,9 @@ __global__ void __launch_bounds__(kThreads, 2) dense_pass(const PassParams p) {
                                                (NC > 0 ? kCredBytes : 0));  // [2][CW]
     float4* s_rowp = s_colp + 2 * CW;                                      // [2][kRB]
     float* s_cdp = reinterpret_cast<float*>(s_rowp + 2 * kRB);             // [2][CW] (LS only)
-    __shared__ __align__(8) uint64_t s_bar[kWarps][NS];
     __shared__ __align__(8) uint64_t s_pbar[2];
     constexpr bool STAGE_PARAMS = MIXED && !COLROOT;
 
-    if (lane == 0)
-        for (int s = 0; s < NS; ++s) mbar_init(&s_bar[warp][s], 1);
     if (STAGE_PARAMS && threadIdx.x == 0) {
         mbar_init(&s_pbar[0], 1);
         mbar_init(&s_pbar[1], 1);
@@ -359,19 +360,28 @@ __global__ void __launch_bounds__(kThreads, 2) dense_pass(const PassParams p) {
         psrc = Mb + prow * ldm + c0;
         pseg = (uint32_t)((ldm - c0) < CW ? (ldm - c0) : CW) * (uint32_t)sizeof(TM);
     };
-    auto issue = [&](int q) {  // row q of this warp == (pk, pu)
-        uint64_t* bar = &s_bar[warp][q % NS];
+    auto issue = [&](int q) {  // row q of this warp == (pk, pu): each lane copies its own vectors
         const bool valid = prow + pu < n;
-        mbar_arrive_expect_tx(bar, valid ? pseg : 0u);
-        if (valid) bulk_g2s(ring + (size_t)(q % NS) * CW, psrc + (long long)pu * ldm, pseg, bar);
+        if (valid) {
+            TM* dst = ring + (size_t)(q % NS) * CW;
+            const TM* src = psrc + (long long)pu * ldm;
+#pragma unroll
+            for (int v = 0; v < NV; ++v) {
+                const int off = (v * 32 + lane) * VW;
+                if ((uint32_t)(off * (int)sizeof(TM)) < pseg)
+                    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst + off)), "l"(src + off) : "memory");
+            }
+        }
+        asm volatile("cp.async.commit_group;" ::: "memory");
         if (++pu == RPW) {
             pu = 0;
             if (++pk < my_tiles) cursor_tile();
         }
     };
-    if (lane == 0 && total > 0) {
-        cursor_tile();
-        for (int q = 0; q < NS && q < total; ++q) issue(q);
+    if (total > 0) cursor_tile();
+    for (int q = 0; q < NS; ++q) {
+        if (q < total) issue(q);
+        else asm volatile("cp.async.commit_group;" ::: "memory");
     }
 
     // Constants prepared on the host (no FP64 arithmetic in this kernel:
@@ -460,6 +470,10 @@ __global__ void __launch_bounds__(kThreads, 2) dense_pass(const PassParams p) {
             double prad[2];
 #pragma unroll
             for (int r2 = 0; r2 < 2; ++r2) {
+                // groups are committed one per row (empty past the end), so
+                // the pair's two rows are complete when at most NS - 2 of the
+                // lane's groups are still pending
+                if (r2 == 0) asm volatile("cp.async.wait_group %0;" ::"n"(NS - 2) : "memory");
                 const int u = u2 + r2;
                 const int qs = k * RPW + u;
                 const int i = r0 + rw0 + u;
@@ -485,11 +499,6 @@ __global__ void __launch_bounds__(kThreads, 2) dense_pass(const PassParams p) {
                         if constexpr (op_uses_rx(OP)) prx[r2] = p.rx ? (TM)p.rx[i] : (TM)0;
                         if constexpr (op_uses_rd(OP)) prd[r2] = p.rd ? (TM)p.rd[i] : (TM)0;
                     }
-                    // Every row with data is waited for (bounded), even after
-                    // a timeout, so no copy is left in flight when the CTA exits.
-                    const bool arrived = mbar_wait_bounded(&s_bar[warp][qs % NS],
-                                                           (uint32_t)((qs / NS) & 1), p.err);
-                    ok_wait = ok_wait && arrived;
                     const TM* buf = ring + (size_t)(qs % NS) * CW;
 #pragma unroll
                     for (int v = 0; v < NV; ++v) {
@@ -498,6 +507,16 @@ __global__ void __launch_bounds__(kThreads, 2) dense_pass(const PassParams p) {
                             mvp[r2][v] = *reinterpret_cast<const VT*>(buf + off);
                     }
                 }
+            }
+            // Both buffers are free once every lane has read them into
+            // registers: refill them before the rows are reduced, so that the
+            // copies overlap this pair's arithmetic. The warp barrier orders
+            // the generic-proxy reads before the async-proxy writes.
+#pragma unroll
+            for (int r2 = 0; r2 < 2; ++r2) {
+                const int qs = k * RPW + u2 + r2;
+                if (qs + NS < total) issue(qs + NS);
+                else asm volatile("cp.async.commit_group;" ::: "memory");
             }
 #pragma unroll
             for (int r2 = 0; r2 < 2; ++r2) {
@@ -661,17 +680,6 @@ __global__ void __launch_bounds__(kThreads, 2) dense_pass(const PassParams p) {
 #pragma unroll
                 for (int rr = 0; rr < NR; ++rr) rowv[rr][u] = racc[rr];
             }
-            // Both buffers are free once every lane has read them: order those
-            // generic-proxy reads before the async-proxy refills.
-            __syncwarp();
-            if (lane == 0) {
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-#pragma unroll
-                for (int r2 = 0; r2 < 2; ++r2) {
-                    const int qs = k * RPW + u2 + r2;
-                    if (qs + NS < total) issue(qs + NS);
-                }
-            }
         }
 
         // ---- row partials of this tile ----
@@ -738,6 +746,7 @@ __global__ void __launch_bounds__(kThreads, 2) dense_pass(const PassParams p) {
         }
     }
 
+    asm volatile("cp.async.wait_all;" ::: "memory");  // nothing in flight at exit
     // ---- per-CTA totals ----
     if constexpr (NT > 0) {
         __shared__ double s_t[NT][kWarps];
