@@ -123,6 +123,8 @@ long long regot_ctx_kernel_launches(const regot_ctx* ctx);
  * (FP64 or FP32, rows padded to 16 bytes) once; solves reuse it. */
 int regot_problem_create(regot_ctx* ctx, const regot_problem_desc* desc, int precision,
                          regot_dproblem** out);
+/* Frees the problem's device memory on its context's stream and waits for
+ * it. Destroy every problem of a context before the context itself. */
 void regot_problem_destroy(regot_dproblem* prob);
 
 /* Page-locked host memory for result buffers (the n x m plan): a device to

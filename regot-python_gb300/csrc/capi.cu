@@ -81,6 +81,35 @@ regot_opts effective_opts(const regot_opts* o) {
 
 namespace regot {
 
+static std::mutex g_pool_mutex;
+static std::unordered_map<int, cudaMemPool_t> g_pools;  // per device, kept for the process
+
+void* dev_alloc(size_t bytes, cudaStream_t st) {
+    int dev = 0;
+    REGOT_CUDA(cudaGetDevice(&dev));
+    cudaMemPool_t pool = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_pool_mutex);
+        auto it = g_pools.find(dev);
+        if (it != g_pools.end()) {
+            pool = it->second;
+        } else {
+            cudaMemPoolProps props;
+            std::memset(&props, 0, sizeof(props));
+            props.allocType = cudaMemAllocationTypePinned;
+            props.location.type = cudaMemLocationTypeDevice;
+            props.location.id = dev;
+            REGOT_CUDA(cudaMemPoolCreate(&pool, &props));
+            unsigned long long keep = kPoolKeepBytes;
+            REGOT_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+            g_pools[dev] = pool;
+        }
+    }
+    void* p = nullptr;
+    REGOT_CUDA(cudaMallocFromPoolAsync(&p, bytes, pool, st));
+    return p;
+}
+
 void finish_erot_result(ErotOps& ops, const double* d_gamma, const double* hobj,
                         const double* hmar, const double* htime, const double* hdens,
                         int hist_len, int hist_cap, int niter, long long passes,
@@ -255,9 +284,9 @@ int regot_problem_create(regot_ctx* ctx, const regot_problem_desc* d, int precis
             const size_t es = precision == REGOT_PREC_FP64 ? 8 : 4;
             const long long vw = 16 / (long long)es;
             P->ldm = (m + vw - 1) / vw * vw;
-            REGOT_CUDA(cudaMallocAsync(&P->M, (size_t)n * P->ldm * es, st));
-            REGOT_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&P->a), n * sizeof(double), st));
-            REGOT_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&P->b), m * sizeof(double), st));
+            P->M = dev_alloc((size_t)n * P->ldm * es, st);
+            P->a = static_cast<double*>(dev_alloc(n * sizeof(double), st));
+            P->b = static_cast<double*>(dev_alloc(m * sizeof(double), st));
             P->ha.resize(n);
             P->hb.resize(m);
             if (d->ab_mem == REGOT_MEM_DEVICE) {
@@ -291,7 +320,7 @@ int regot_problem_create(regot_ctx* ctx, const regot_problem_desc* d, int precis
                 void* stage = nullptr;
                 const void* src = d->M;
                 if (d->M_mem != REGOT_MEM_DEVICE) {
-                    REGOT_CUDA(cudaMallocAsync(&stage, (size_t)n * m * src_es, st));
+                    stage = dev_alloc((size_t)n * m * src_es, st);
                     REGOT_CUDA(cudaMemcpy2DAsync(stage, m * src_es, d->M, d->ldm * src_es,
                                                  m * src_es, n, kind, st));
                     src = stage;
@@ -323,6 +352,7 @@ static void drop_time_pass_state(regot_dproblem* P);
 
 void regot_problem_destroy(regot_dproblem* P) {
     if (!P) return;
+    if (P->ctx) cudaSetDevice(P->ctx->device);
     drop_time_pass_state(P);
     cudaStream_t st = P->ctx ? P->ctx->stream : nullptr;
     if (P->M) cudaFreeAsync(P->M, st);

@@ -33,36 +33,42 @@ __device__ __forceinline__ void atomic_max_abs(double* target, double v) {
               (unsigned long long)__double_as_longlong(a));
 }
 
+// Bit pattern of |v| for the running maximum (NaN and infinities count as 0),
+// and its maximum over a full warp in integer arithmetic (FP64 instructions
+// issue at a small fraction of the integer rate on this part).
+__device__ __forceinline__ unsigned long long abs_bits(double v) {
+    unsigned long long bits = (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffULL;
+    return (bits >> 52) == 0x7ffULL ? 0ULL : bits;
+}
+
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long bits) {
+    const unsigned hi = (unsigned)(bits >> 32), lo = (unsigned)bits;
+    const unsigned mhi = __reduce_max_sync(0xffffffffu, hi);
+    const unsigned mlo = __reduce_max_sync(0xffffffffu, hi == mhi ? lo : 0u);
+    return ((unsigned long long)mhi << 32) | mlo;
+}
+
 // Warp-aggregated version: one atomic per warp (all lanes must call it).
 __device__ __forceinline__ void warp_atomic_max_abs(double* target, double v) {
-    double a = fabs(v);
-    if (!(a == a) || isinf(a)) a = 0.0;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) a = fmax(a, __shfl_xor_sync(0xffffffffu, a, o));
-    if ((threadIdx.x & 31) == 0 && a > 0.0)
-        atomicMax(reinterpret_cast<unsigned long long*>(target),
-                  (unsigned long long)__double_as_longlong(a));
+    const unsigned long long mx = warp_max_u64(abs_bits(v));
+    if ((threadIdx.x & 31) == 0 && mx != 0ULL)
+        atomicMax(reinterpret_cast<unsigned long long*>(target), mx);
 }
 
 // Block-wide version (all threads of the block must call it): one atomic
 // per block instead of one per warp, so that the many blocks of a finalize
 // kernel do not serialise on the target's cache line.
 __device__ __forceinline__ void block_atomic_max_abs(double* target, double v) {
-    __shared__ double s_bmax[32];
+    __shared__ unsigned long long s_bmax[32];
     const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
     const int nthreads = blockDim.x * blockDim.y * blockDim.z;
-    double a = fabs(v);
-    if (!(a == a) || isinf(a)) a = 0.0;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) a = fmax(a, __shfl_xor_sync(0xffffffffu, a, o));
+    const unsigned long long a = warp_max_u64(abs_bits(v));
     if ((tid & 31) == 0) s_bmax[tid >> 5] = a;
     __syncthreads();
     if (tid == 0) {
-        double mx = 0.0;
-        for (int w = 0; w < (nthreads + 31) >> 5; ++w) mx = fmax(mx, s_bmax[w]);
-        if (mx > 0.0)
-            atomicMax(reinterpret_cast<unsigned long long*>(target),
-                      (unsigned long long)__double_as_longlong(mx));
+        unsigned long long mx = 0ULL;
+        for (int w = 0; w < (nthreads + 31) >> 5; ++w) mx = s_bmax[w] > mx ? s_bmax[w] : mx;
+        if (mx != 0ULL) atomicMax(reinterpret_cast<unsigned long long*>(target), mx);
     }
     __syncthreads();
 }
@@ -189,7 +195,101 @@ __device__ __forceinline__ double merge_2d(const Acc* p, int count, size_t strid
     return S;
 }
 
-// Stream-ordered device buffer (cudaMallocAsync / cudaFreeAsync).
+// Knuth's TwoSum in FP32: s + e == a + b exactly (no FMA can be formed, so
+// contraction does not change it).
+__device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float z = s - a;
+    e = (a - (s - z)) + (b - z);
+}
+
+// FP32 partials: the same merge with compensated FP32 sums (TwoSum, the
+// rounding errors accumulated beside the sum), converted to FP64 once per
+// item. FP64 arithmetic issues at a small fraction of the FP32 rate on this
+// part, and converting and adding every partial in FP64 dominated the
+// finalize kernels; the compensated sum keeps the merge error at the level of
+// the FP64 one (about count * 2^-48 relative instead of count * 2^-24).
+template <>
+__device__ __forceinline__ double merge_2d<float>(const float* p, int count, size_t stride,
+                                                  bool valid) {
+    __shared__ float2 s_mf[8][33];
+    float s = 0.f, c = 0.f;
+    if (valid) {
+        int k = threadIdx.y;
+        for (; k + 24 < count; k += 32) {
+            float v[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) v[q] = p[(size_t)(k + 8 * q) * stride];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                float t, e;
+                two_sum_f(s, v[q], t, e);
+                s = t;
+                c += e;
+            }
+        }
+        for (; k < count; k += 8) {
+            float t, e;
+            two_sum_f(s, p[(size_t)k * stride], t, e);
+            s = t;
+            c += e;
+        }
+    }
+    s_mf[threadIdx.y][threadIdx.x] = make_float2(s, c);
+    __syncthreads();
+    double S = 0.0;
+    if (threadIdx.y == 0) {
+        float ss = 0.f, cc = 0.f;
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+            const float2 v = s_mf[q][threadIdx.x];
+            float t, e;
+            two_sum_f(ss, v.x, t, e);
+            ss = t;
+            cc += e + v.y;
+        }
+        S = (double)ss + (double)cc;
+    }
+    return S;
+}
+
+// Grid-wide sum of K values when one full warp of each block holds them (the
+// other warps of the block take no part). Returns true in every lane of that
+// warp of the last block to finish, with the totals in out[]. The last warp
+// sums the per-block partials lane l taking blocks l, l + 32, ... in order,
+// then a fixed butterfly, so the result does not depend on which block
+// finishes last.
+template <int K>
+__device__ bool warp_grid_reduce(const double (&vals)[K], double* block_parts, unsigned* counter,
+                                 double (&out)[K]) {
+    const int lane = threadIdx.x & 31;
+    unsigned last = 0;
+    double s[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) s[k] = warp_sum_d(vals[k]);
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) block_parts[(size_t)blockIdx.x * K + k] = s[k];
+        __threadfence();
+        last = atomicAdd(counter, 1u) == gridDim.x - 1 ? 1u : 0u;
+    }
+    last = __shfl_sync(0xffffffffu, last, 0);
+    if (!last) return false;
+    __threadfence();
+    double part[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) part[k] = 0.0;
+    for (unsigned b = lane; b < gridDim.x; b += 32) {
+#pragma unroll
+        for (int k = 0; k < K; ++k) part[k] += __ldcg(&block_parts[(size_t)b * K + k]);
+    }
+#pragma unroll
+    for (int k = 0; k < K; ++k) out[k] = warp_sum_d(part[k]);
+    if (lane == 0) *counter = 0u;
+    return true;
+}
+
+// Stream-ordered device buffer (dev_alloc / cudaFreeAsync).
 template <typename T>
 class DBuf {
 public:
@@ -210,7 +310,7 @@ public:
         release();
         st_ = st;
         count_ = count;
-        if (count) REGOT_CUDA(cudaMallocAsync(reinterpret_cast<void**>(&p_), count * sizeof(T), st));
+        if (count) p_ = static_cast<T*>(dev_alloc(count * sizeof(T), st));
     }
     void zero() {
         if (count_) REGOT_CUDA(cudaMemsetAsync(p_, 0, count_ * sizeof(T), st_));

@@ -31,7 +31,11 @@ namespace {
 
 // Finalize kernels: (32, 8) blocks, 32 rows (columns) per block with their
 // partials merged by 8 threads each (merge_2d), so the merge is not bound by
-// the latency of one thread's dependent loads.
+// the latency of one thread's dependent loads. After the merge only warp 0
+// continues: the dual update, the split, the max-abs (integer) and the grid
+// sums (warp_grid_reduce) need one thread per row or column, and keeping
+// FP64 instructions to that one warp matters on a part whose FP64 rate is a
+// small fraction of its FP32 rate.
 constexpr int kFinItems = 32;
 const dim3 kFinBlock(32, 8);
 
@@ -82,10 +86,11 @@ __global__ void k_bcd_row(const Acc* rp, int nslabs, int n, const double* anchor
                           int robust, SplitOut so) {
     if (st->done) return;
     const int i = blockIdx.x * kFinItems + threadIdx.x;
+    const double S = merge_2d(rp + i, nslabs, (size_t)n, i < n);
+    if (threadIdx.y != 0) return;  // the rest runs in warp 0 only
     double v[3] = {0.0, 0.0, 0.0};
     double vmax = 0.0;
-    const double S = merge_2d(rp + i, nslabs, (size_t)n, i < n);
-    if (i < n && threadIdx.y == 0) {
+    if (i < n) {
         const double al = alpha[i];
         const double an = anchor[i];
         if (!robust && !sum_ok<MIXED>(S)) atomicOr(&st->bad, 1);
@@ -102,10 +107,10 @@ __global__ void k_bcd_row(const Acc* rp, int nslabs, int n, const double* anchor
             so.out[i] = split_fixed(an_next, so);
         }
     }
-    block_atomic_max_abs(&st->maxabs, vmax);
+    warp_atomic_max_abs(&st->maxabs, vmax);
     __threadfence();
     double out[3];
-    if (grid_reduce<3>(v, parts, &st->counter, out)) {
+    if (warp_grid_reduce<3>(v, parts, &st->counter, out) && threadIdx.x == 0) {
         if (atomicAdd(&st->bad, 0)) {
             st->done = 1;
             return;
@@ -134,10 +139,11 @@ __global__ void k_bcd_col(const Acc* cp, int nrb, int m, const double* anchor,
                           double* parts, BcdState* st, int robust, SplitOut so, int advance) {
     if (st->done) return;
     const int j = blockIdx.x * kFinItems + threadIdx.x;
+    const double S = merge_2d(cp + j, nrb, (size_t)m, j < m);
+    if (threadIdx.y != 0) return;  // the rest runs in warp 0 only
     double v[1] = {0.0};
     double vmax = 0.0;
-    const double S = merge_2d(cp + j, nrb, (size_t)m, j < m);
-    if (j < m && threadIdx.y == 0) {
+    if (j < m) {
         if (!robust && !sum_ok<MIXED>(S)) atomicOr(&st->bad, 2);
         const double bn = anchor[j] + reg * (logb[j] - log(S));
         beta_next[j] = bn;
@@ -148,16 +154,16 @@ __global__ void k_bcd_col(const Acc* cp, int nrb, int m, const double* anchor,
             so.out[j] = split_fixed(bn, so);
         }
     }
-    block_atomic_max_abs(&st->maxabs, vmax);
+    warp_atomic_max_abs(&st->maxabs, vmax);
     __threadfence();
     double out[1];
-    if (grid_reduce<1>(v, parts, &st->counter, out)) {
+    if (warp_grid_reduce<1>(v, parts, &st->counter, out) && threadIdx.x == 0) {
         if (atomicAdd(&st->bad, 0)) {
             st->done = 1;
             return;
         }
         st->sum_bb = out[0];
-        st->beta_last = beta_next[m - 1];
+        st->beta_last = __ldcg(&beta_next[m - 1]);
         if (advance) st->iter += 1;
     }
 }

@@ -33,6 +33,14 @@ inline void require(bool ok, const std::string& msg, int code = REGOT_ERR_INVALI
     if (!ok) throw Error(code, msg);
 }
 
+// Stream-ordered device allocation from the library's own memory pool of the
+// current device. The pool keeps up to kPoolKeepBytes of freed memory mapped
+// across synchronisations, so consecutive problems and solves reuse it
+// instead of mapping fresh pages (the default pool returns everything at each
+// synchronisation). Free with cudaFreeAsync.
+constexpr unsigned long long kPoolKeepBytes = 4ULL << 30;
+void* dev_alloc(size_t bytes, cudaStream_t st);
+
 // ------------------------------------------------------------- geometry --
 // Dense passes tile M (row-major, row stride ldm) into tiles of RB rows x
 // CW columns. A CTA has 8 warps; each warp streams RB/8 consecutive rows of
