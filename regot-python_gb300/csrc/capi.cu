@@ -2,6 +2,7 @@
 // include/regot_gb300.h): contexts, device-resident problems, the solver
 // entry points and the pass-level entry points. Every entry point converts
 // exceptions into a status code and a per-context message.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -110,6 +111,25 @@ void* dev_alloc(size_t bytes, cudaStream_t st) {
     return p;
 }
 
+void* ctx_stage(regot_ctx* ctx, size_t bytes) {
+    if (bytes > ctx->stage_bytes) {
+        if (ctx->stage) REGOT_CUDA(cudaFreeHost(ctx->stage));
+        ctx->stage = nullptr;
+        ctx->stage_bytes = 0;
+        const size_t want = std::max(bytes, (size_t)64 << 10);
+        REGOT_CUDA(cudaHostAlloc(&ctx->stage, want, cudaHostAllocPortable));
+        ctx->stage_bytes = want;
+    }
+    return ctx->stage;
+}
+
+void read_small(regot_ctx* ctx, void* dst, const void* src, size_t bytes, cudaStream_t st) {
+    void* h = ctx_stage(ctx, bytes);
+    d2h(h, src, bytes, st);
+    sync(st);
+    std::memcpy(dst, h, bytes);
+}
+
 void finish_erot_result(ErotOps& ops, const double* d_gamma, const double* hobj,
                         const double* hmar, const double* htime, const double* hdens,
                         int hist_len, int hist_cap, int niter, long long passes,
@@ -120,12 +140,28 @@ void finish_erot_result(ErotOps& ops, const double* d_gamma, const double* hobj,
     res->niter = niter;
     res->hist_len = hist_len;
     res->passes = passes;
-    d2h(res->dual, d_gamma, (size_t)(n + m - 1) * sizeof(double), st);
-    if (res->obj_vals) d2h(res->obj_vals, hobj, hist_len * sizeof(double), st);
-    if (res->mar_errs) d2h(res->mar_errs, hmar, hist_len * sizeof(double), st);
-    if (res->run_times) d2h(res->run_times, htime, hist_len * sizeof(double), st);
-    if (res->densities && hdens) d2h(res->densities, hdens, hist_len * sizeof(double), st);
-    ops.check_err();
+    // Dual, histories and the pass error flag in one staging block, behind
+    // one synchronisation.
+    const size_t nd = (size_t)n + m - 1, L = (size_t)hist_len;
+    double* h = static_cast<double*>(ctx_stage(ops.problem()->ctx, (nd + 4 * L + 1) * sizeof(double)));
+    double* h_obj = h + nd;
+    double* h_mar = h_obj + L;
+    double* h_time = h_mar + L;
+    double* h_dens = h_time + L;
+    int* h_err = reinterpret_cast<int*>(h_dens + L);
+    d2h(h, d_gamma, nd * sizeof(double), st);
+    d2h(h_obj, hobj, L * sizeof(double), st);
+    d2h(h_mar, hmar, L * sizeof(double), st);
+    d2h(h_time, htime, L * sizeof(double), st);
+    if (hdens) d2h(h_dens, hdens, L * sizeof(double), st);
+    d2h(h_err, ops.err_flag(), sizeof(int), st);
+    sync(st);
+    if (*h_err) throw Error(REGOT_ERR_TIMEOUT, "a dense pass gave up waiting for its tile copies");
+    std::memcpy(res->dual, h, nd * sizeof(double));
+    if (res->obj_vals) std::memcpy(res->obj_vals, h_obj, L * sizeof(double));
+    if (res->mar_errs) std::memcpy(res->mar_errs, h_mar, L * sizeof(double));
+    if (res->run_times) std::memcpy(res->run_times, h_time, L * sizeof(double));
+    if (res->densities && hdens) std::memcpy(res->densities, h_dens, L * sizeof(double));
     if (o.plan && res->plan) {
         DBuf<double> mx(1, st);
         if (o.plan_mem == REGOT_MEM_DEVICE) {
@@ -243,6 +279,7 @@ void regot_ctx_destroy(regot_ctx* ctx) {
         cudaStreamSynchronize(ctx->own_stream);
         cudaStreamDestroy(ctx->own_stream);
     }
+    if (ctx->stage) cudaFreeHost(ctx->stage);
     delete ctx;
 }
 
@@ -358,6 +395,8 @@ void regot_problem_destroy(regot_dproblem* P) {
     if (P->M) cudaFreeAsync(P->M, st);
     if (P->a) cudaFreeAsync(P->a, st);
     if (P->b) cudaFreeAsync(P->b, st);
+    if (P->loga) cudaFreeAsync(P->loga, st);
+    if (P->logb) cudaFreeAsync(P->logb, st);
     cudaStreamSynchronize(st);
     delete P;
 }

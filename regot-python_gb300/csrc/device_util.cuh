@@ -58,11 +58,11 @@ __device__ __forceinline__ void warp_atomic_max_abs(double* target, double v) {
 // Block-wide version (all threads of the block must call it): one atomic
 // per block instead of one per warp, so that the many blocks of a finalize
 // kernel do not serialise on the target's cache line.
-__device__ __forceinline__ void block_atomic_max_abs(double* target, double v) {
+__device__ __forceinline__ void block_atomic_max_bits(double* target, unsigned long long bits) {
     __shared__ unsigned long long s_bmax[32];
     const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
     const int nthreads = blockDim.x * blockDim.y * blockDim.z;
-    const unsigned long long a = warp_max_u64(abs_bits(v));
+    const unsigned long long a = warp_max_u64(bits);
     if ((tid & 31) == 0) s_bmax[tid >> 5] = a;
     __syncthreads();
     if (tid == 0) {
@@ -71,6 +71,10 @@ __device__ __forceinline__ void block_atomic_max_abs(double* target, double v) {
         if (mx != 0ULL) atomicMax(reinterpret_cast<unsigned long long*>(target), mx);
     }
     __syncthreads();
+}
+
+__device__ __forceinline__ void block_atomic_max_abs(double* target, double v) {
+    block_atomic_max_bits(target, abs_bits(v));
 }
 
 // Sum of count values p[k * stride], k = 0..count-1, in FP64. Loads are
@@ -251,6 +255,25 @@ __device__ __forceinline__ double merge_2d<float>(const float* p, int count, siz
         S = (double)ss + (double)cc;
     }
     return S;
+}
+
+// Maximum of `count` partials p[k * stride] for the 32 items of a (32, 8)
+// block, laid out as in merge_2d (exact in the partials' own type). Valid in
+// the threads with threadIdx.y == 0.
+template <typename Acc>
+__device__ __forceinline__ double max_2d(const Acc* p, int count, size_t stride, bool valid) {
+    __shared__ Acc s_mx[8][33];
+    Acc v = (Acc)(-INFINITY);
+    if (valid)
+        for (int k = threadIdx.y; k < count; k += 8) v = fmax(v, p[(size_t)k * stride]);
+    s_mx[threadIdx.y][threadIdx.x] = v;
+    __syncthreads();
+    Acc r = (Acc)(-INFINITY);
+    if (threadIdx.y == 0) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) r = fmax(r, s_mx[q][threadIdx.x]);
+    }
+    return (double)r;
 }
 
 // Grid-wide sum of K values when one full warp of each block holds them (the

@@ -54,6 +54,10 @@ struct BcdState {
     double gb2_once;   // squared beta-part of the gradient of iterate 0 (x0 given)
     double maxabs;     // running max |alpha|, |beta| (hi/lo split grid)
     double last_gnorm; // marginal error of the last recorded iterate
+    // Fixed hi/lo grid of the ping-pong sweeps (k_bcd_grid): the split value
+    // handed to k_split, the grid g and 1/g, and the bound on |dual| that
+    // keeps hi exact on g.
+    double gval, sg, sinv, sbound;
     unsigned long long t0;
 };
 
@@ -66,16 +70,26 @@ __device__ __forceinline__ bool sum_ok(double s) {
 // test, alpha_{k+1}. `anchor` is the row vector the pass used (alpha itself
 // on the fast path, -max_j(beta_j - M_ij) on the robust path).
 // Fixed hi/lo grid of the ping-pong sweeps: the finalize kernels write the
-// FP32 split of the duals they produce, for the next pass.
+// FP32 split of the duals they produce, for the next pass, on the grid kept
+// in BcdState.
 struct SplitOut {
     float4* out = nullptr;  // null: no split written
-    double g = 1.0, inv_g = 1.0;
-    double bound = 0.0;     // |dual| < bound keeps hi exact on the grid g
 };
 
-__device__ __forceinline__ float4 split_fixed(double v, const SplitOut& so) {
-    const double h = rint(v * so.inv_g) * so.g;
+__device__ __forceinline__ float4 split_fixed(double v, const BcdState* st) {
+    const double h = rint(v * st->sinv) * st->sg;
     return make_float4((float)h, (float)(v - h), 0.f, 0.f);
+}
+
+// Grid of the ping-pong sweeps from the running max |dual| of the initial
+// value: g = 2^(e + 3 - 21), e = ilogb(max), i.e. 8x headroom.
+__global__ void k_bcd_grid(BcdState* st) {
+    const double m0 = st->maxabs;
+    const int e = (m0 > 0.0 && isfinite(m0)) ? ilogb(m0) : 0;
+    st->gval = ldexp(1.0, e + 3);
+    st->sg = ldexp(1.0, e + 3 - 21);
+    st->sinv = ldexp(1.0, -(e + 3 - 21));
+    st->sbound = ldexp(1.0, e + 4);
 }
 
 template <typename Acc, bool MIXED>
@@ -103,8 +117,8 @@ __global__ void k_bcd_row(const Acc* rp, int nslabs, int n, const double* anchor
         alpha_next[i] = an_next;
         vmax = an_next;
         if (so.out) {
-            if (!(fabs(an_next) < so.bound)) atomicOr(&st->bad, 4);
-            so.out[i] = split_fixed(an_next, so);
+            if (!(fabs(an_next) < st->sbound)) atomicOr(&st->bad, 4);
+            so.out[i] = split_fixed(an_next, st);
         }
     }
     warp_atomic_max_abs(&st->maxabs, vmax);
@@ -150,8 +164,8 @@ __global__ void k_bcd_col(const Acc* cp, int nrb, int m, const double* anchor,
         if (j < m - 1) v[0] = b[j] * bn;
         vmax = bn;
         if (so.out) {
-            if (!(fabs(bn) < so.bound)) atomicOr(&st->bad, 8);
-            so.out[j] = split_fixed(bn, so);
+            if (!(fabs(bn) < st->sbound)) atomicOr(&st->bad, 8);
+            so.out[j] = split_fixed(bn, st);
         }
     }
     warp_atomic_max_abs(&st->maxabs, vmax);
@@ -205,18 +219,16 @@ __global__ void k_colgrad_sq(const double* c, const double* b, int m, double* ou
     }
 }
 
-__global__ void k_dot_bt(const double* b, const double* beta, int m, BcdState* st) {
-    double v = 0.0;
-    for (int j = threadIdx.x; j < m - 1; j += blockDim.x) v += b[j] * beta[j];
-    __shared__ double s[32];
-    v = warp_sum_d(v);
-    if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = v;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double t = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s[w];
-        st->sum_bb = t;
-        st->beta_last = beta[m - 1];
+// sum_{j<m-1} b_j beta_j and beta_{m-1} of the initial beta.
+__global__ void k_dot_bt(const double* b, const double* beta, int m, double* parts,
+                         BcdState* st) {
+    double v[1] = {0.0};
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < m - 1; j += gridDim.x * blockDim.x)
+        v[0] += b[j] * beta[j];
+    double out[1];
+    if (grid_reduce<1>(v, parts, &st->counter, out)) {
+        st->sum_bb = out[0];
+        st->beta_last = __ldcg(&beta[m - 1]);
     }
 }
 
@@ -260,7 +272,8 @@ void sinkhorn_bcd_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol,
     }
     // Timer starts after the initial value (sinkhorn_bcd.cpp:49-51).
     k_bcd_start<<<1, 1, 0, st>>>(S);
-    k_dot_bt<<<1, 256, 0, st>>>(P->b, beta.get(), m, S);
+    k_dot_bt<<<std::min(std::max(cdiv(m - 1, 256), 1), 64), 256, 0, st>>>(P->b, beta.get(), m,
+                                                                         parts.get(), S);
     count_launch(2);
     if (has_x0) {
         // With a user x0 the beta part of the first gradient is not zero.
@@ -273,8 +286,7 @@ void sinkhorn_bcd_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol,
 
     BcdState hs{};
     auto read_state = [&]() {
-        d2h(&hs, S, sizeof(hs), st);
-        sync(st);
+        read_small(ctx, &hs, S, sizeof(hs), st);
     };
     // Size the next batch of sweeps from the observed linear convergence
     // rate, so that few sweeps are launched past convergence.
@@ -305,24 +317,19 @@ void sinkhorn_bcd_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol,
     int pending = 0;  // robust column half-sweep owed to the general path
     bool finished = false;
     {
-        read_state();
-        const double m0 = hs.maxabs;
-        const int e = (m0 > 0.0 && std::isfinite(m0)) ? std::ilogb(m0) : 0;
+        // The grid comes from the initial duals on the device, so the graph
+        // below is captured while the initialisation still runs.
         float4* rs = const_cast<float4*>(ops.rsplit());
         float4* cs = const_cast<float4*>(ops.csplit());
         SplitOut so_r, so_c;
         if (mixed) {
-            DBuf<double> gval(1, st);
-            const double gv = std::ldexp(1.0, e + 3);
-            h2d(gval.get(), &gv, sizeof(double), st);
+            k_bcd_grid<<<1, 1, 0, st>>>(S);
+            count_launch();
             PassParams q = ops.base_params();
             q.ra = alpha.get();
             q.cb = beta.get();
-            q.grid = gval.get();
+            q.grid = &S->gval;
             launch_split(q, rs, cs, nullptr, st);
-            so_r.g = so_c.g = std::ldexp(1.0, e + 3 - 21);
-            so_r.inv_g = so_c.inv_g = std::ldexp(1.0, -(e + 3 - 21));
-            so_r.bound = so_c.bound = std::ldexp(1.0, e + 4);
             so_r.out = rs;
             so_c.out = cs;
         }

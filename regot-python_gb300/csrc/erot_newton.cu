@@ -352,8 +352,7 @@ void sinkhorn_newton_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double t
     auto record = [&]() {
         k_newton_time<<<1, 1, 0, st>>>(S, htime + hist_len);
         count_launch();
-        d2h(&hs, S, sizeof(hs), st);
-        sync(st);
+        read_small(ctx, &hs, S, sizeof(hs), st);
         h2d(hobj + hist_len, &hs.f, sizeof(double), st);
         h2d(hmar + hist_len, &hs.gnorm, sizeof(double), st);
         ++hist_len;
@@ -391,8 +390,7 @@ void sinkhorn_newton_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double t
         // Armijo backtracking on exact objective differences.
         k_dir_dots<<<gv, kVecThreads, 0, st>>>(n, m, g.get(), x.get(), P->a, P->b, parts.get(), S);
         count_launch();
-        d2h(&hs, S, sizeof(hs), st);
-        sync(st);
+        read_small(ctx, &hs, S, sizeof(hs), st);
         const double thresh = theta * hs.gtd;
         double step = 1.0, accepted = -1.0;
         for (int k0 = 0; k0 < nlinesearch && accepted < 0.0; k0 += 4) {

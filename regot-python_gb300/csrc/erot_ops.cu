@@ -7,25 +7,11 @@ namespace regot {
 
 namespace {
 
-template <typename Acc>
-__device__ __forceinline__ double merge_row(const Acc* rp, int nslabs, int n, int i, int r = 0) {
-    return merge_strided(rp + (size_t)r * nslabs * n + i, nslabs, (size_t)n);
-}
-
-template <typename Acc>
-__device__ __forceinline__ double merge_col(const Acc* cp, int nrb, int m, int j, int c = 0) {
-    return merge_strided(cp + (size_t)c * nrb * m + j, nrb, (size_t)m);
-}
-
-template <typename Acc>
-__device__ __forceinline__ double max_row(const Acc* rp, int nslabs, int n, int i) {
-    return max_strided(rp + i, nslabs, (size_t)n);
-}
-
-template <typename Acc>
-__device__ __forceinline__ double max_col(const Acc* cp, int nrb, int m, int j) {
-    return max_strided(cp + j, nrb, (size_t)m);
-}
+// Partial-merging kernels: (32, 8) blocks, 32 rows (columns) per block with
+// their partials split over threadIdx.y (merge_2d / max_2d), so that a merge
+// is not bound by one thread's chain of loads and FP32 partials are summed
+// without FP64 arithmetic.
+constexpr int kMergeItems = 32;
 
 __global__ void k_log(const double* x, int len, double* y) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -33,63 +19,76 @@ __global__ void k_log(const double* x, int len, double* y) {
 }
 
 __global__ void k_maxabs(const double* x, int nx, const double* y, int ny, double* out) {
-    double v = 0.0;
+    unsigned long long v = 0ULL;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nx + ny; i += gridDim.x * blockDim.x) {
-        const double t = i < nx ? x[i] : y[i - nx];
-        if (isfinite(t)) v = fmax(v, fabs(t));
+        const unsigned long long t = abs_bits(i < nx ? x[i] : y[i - nx]);
+        v = t > v ? t : v;
     }
-    block_atomic_max_abs(out, v);
+    block_atomic_max_bits(out, v);
 }
 
 // anchor = -max partials (row or column direction).
 template <typename Acc>
 __global__ void k_row_anchor(const Acc* rp, int nslabs, int n, double* anchor) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) anchor[i] = -max_row(rp, nslabs, n, i);
+    const int i = blockIdx.x * kMergeItems + threadIdx.x;
+    const double v = max_2d(rp + i, nslabs, (size_t)n, i < n);
+    if (threadIdx.y == 0 && i < n) anchor[i] = -v;
 }
 template <typename Acc>
 __global__ void k_col_anchor(const Acc* cp, int nrb, int m, double* anchor) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j < m) anchor[j] = -max_col(cp, nrb, m, j);
+    const int j = blockIdx.x * kMergeItems + threadIdx.x;
+    const double v = max_2d(cp + j, nrb, (size_t)m, j < m);
+    if (threadIdx.y == 0 && j < m) anchor[j] = -v;
 }
 
 // out = anchor + reg (logw - log S'), S' from the partial sums.
 template <typename Acc>
 __global__ void k_row_lse(const Acc* rp, int nslabs, int n, const double* anchor,
                           const double* logw, double reg, double* out) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] = anchor[i] + reg * (logw[i] - log(merge_row(rp, nslabs, n, i)));
+    const int i = blockIdx.x * kMergeItems + threadIdx.x;
+    const double S = merge_2d(rp + i, nslabs, (size_t)n, i < n);
+    if (threadIdx.y == 0 && i < n) out[i] = anchor[i] + reg * (logw[i] - log(S));
 }
 template <typename Acc>
 __global__ void k_col_lse(const Acc* cp, int nrb, int m, const double* anchor,
                           const double* logw, double reg, double* out) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j < m) out[j] = anchor[j] + reg * (logw[j] - log(merge_col(cp, nrb, m, j)));
+    const int j = blockIdx.x * kMergeItems + threadIdx.x;
+    const double S = merge_2d(cp + j, nrb, (size_t)m, j < m);
+    if (threadIdx.y == 0 && j < m) out[j] = anchor[j] + reg * (logw[j] - log(S));
 }
 
+// out[r][i] = merged partial r of row i (r < nr); columns likewise.
 template <typename Acc>
 __global__ void k_merge_rows(const Acc* rp, int nslabs, int n, int nr, double* out) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n)
-        for (int r = 0; r < nr; ++r) out[(size_t)r * n + i] = merge_row(rp, nslabs, n, i, r);
+    const int i = blockIdx.x * kMergeItems + threadIdx.x;
+    for (int r = 0; r < nr; ++r) {
+        const double S = merge_2d(rp + (size_t)r * nslabs * n + i, nslabs, (size_t)n, i < n);
+        if (threadIdx.y == 0 && i < n) out[(size_t)r * n + i] = S;
+        __syncthreads();  // merge_2d's shared buffer is reused
+    }
 }
 template <typename Acc>
 __global__ void k_merge_cols(const Acc* cp, int nrb, int m, int nc, double* out) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j < m)
-        for (int c = 0; c < nc; ++c) out[(size_t)c * m + j] = merge_col(cp, nrb, m, j, c);
+    const int j = blockIdx.x * kMergeItems + threadIdx.x;
+    for (int c = 0; c < nc; ++c) {
+        const double S = merge_2d(cp + (size_t)c * nrb * m + j, nrb, (size_t)m, j < m);
+        if (threadIdx.y == 0 && j < m) out[(size_t)c * m + j] = S;
+        __syncthreads();
+    }
 }
 
 }  // namespace
 
 ErotOps::ErotOps(regot_dproblem* P, double reg, cudaStream_t st)
     : P_(P), st_(st), n_(P->n), m_(P->m), mixed_(P->prec == REGOT_PREC_MIXED), reg_(reg) {
-    loga_.alloc(n_, st_);
-    logb_.alloc(m_, st_);
-    k_log<<<cdiv(n_, 256), 256, 0, st_>>>(P->a, n_, loga_.get());
-    k_log<<<cdiv(m_, 256), 256, 0, st_>>>(P->b, m_, logb_.get());
-    count_launch(2);
-    REGOT_CHECK_LAUNCH();
+    if (!P->loga) {  // once per problem, kept with it
+        P->loga = static_cast<double*>(dev_alloc(n_ * sizeof(double), st_));
+        P->logb = static_cast<double*>(dev_alloc(m_ * sizeof(double), st_));
+        k_log<<<cdiv(n_, 256), 256, 0, st_>>>(P->a, n_, P->loga);
+        k_log<<<cdiv(m_, 256), 256, 0, st_>>>(P->b, m_, P->logb);
+        count_launch(2);
+        REGOT_CHECK_LAUNCH();
+    }
     for (int i = 0; i < n_; ++i) sum_a_ += P->ha[i];
     for (int j = 0; j < m_ - 1; ++j) sum_bt_ += P->hb[j];
     buf_.init(n_, m_, mixed_, 3, 2, 4, st_);
@@ -119,8 +118,7 @@ PassParams ErotOps::base_params() const {
 
 void ErotOps::check_err() {
     int e = 0;
-    d2h(&e, err_.get(), sizeof(int), st_);
-    sync(st_);
+    read_small(P_->ctx, &e, err_.get(), sizeof(int), st_);
     if (e) throw Error(REGOT_ERR_TIMEOUT, "a dense pass gave up waiting for its tile copies");
 }
 
@@ -160,10 +158,10 @@ void ErotOps::maxabs(const double* x, int nx, const double* y, int ny, double* o
 #define REGOT_LAUNCH_ACC(KERNEL, LEN, PART, ...)                                   \
     do {                                                                           \
         if (mixed_)                                                                \
-            KERNEL<float><<<cdiv(LEN, 64), 64, 0, st_>>>(                          \
+            KERNEL<float><<<cdiv(LEN, kMergeItems), dim3(32, 8), 0, st_>>>(        \
                 reinterpret_cast<const float*>(PART), __VA_ARGS__);                \
         else                                                                       \
-            KERNEL<double><<<cdiv(LEN, 64), 64, 0, st_>>>(                         \
+            KERNEL<double><<<cdiv(LEN, kMergeItems), dim3(32, 8), 0, st_>>>(       \
                 reinterpret_cast<const double*>(PART), __VA_ARGS__);               \
         count_launch();                                                            \
         REGOT_CHECK_LAUNCH();                                                      \
@@ -191,7 +189,7 @@ void ErotOps::optimal_beta(const double* alpha, double* beta, double* mx) {
     p.cb = anchor_.get();
     pass(OP_E_COL, p);
     REGOT_LAUNCH_ACC(k_col_lse, m_, buf_.colpart.get(), buf_.shape.nrb, m_, anchor_.get(),
-                     logb_.get(), reg_, beta);
+                     P_->logb, reg_, beta);
 }
 
 // sinkhorn_problem_bcd.cpp:177-201, the row analogue of optimal_beta.
@@ -206,7 +204,7 @@ void ErotOps::optimal_alpha(const double* beta, double* alpha, double* mx) {
     p.ra = anchor_.get();
     pass(OP_E_ROW, p);
     REGOT_LAUNCH_ACC(k_row_lse, n_, buf_.rowpart.get(), buf_.shape.nslabs, n_, anchor_.get(),
-                     loga_.get(), reg_, alpha);
+                     P_->loga, reg_, alpha);
 }
 
 void ErotOps::row_col_sums(const double* alpha, const double* beta, double* r, double* c,

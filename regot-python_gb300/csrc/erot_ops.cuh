@@ -37,8 +37,9 @@ public:
     cudaStream_t stream() const { return st_; }
     const double* a() const { return P_->a; }
     const double* b() const { return P_->b; }
-    const double* loga() const { return loga_.get(); }
-    const double* logb() const { return logb_.get(); }
+    regot_dproblem* problem() const { return P_; }
+    const double* loga() const { return P_->loga; }
+    const double* logb() const { return P_->logb; }
     double sum_a() const { return sum_a_; }
     double sum_bt() const { return sum_bt_; }
     double reg() const { return reg_; }
@@ -83,7 +84,6 @@ private:
     int n_, m_;
     bool mixed_;
     double reg_;
-    DBuf<double> loga_, logb_;
     double sum_a_ = 0, sum_bt_ = 0;
     PassBuffers buf_;
     DBuf<double> anchor_;

@@ -905,8 +905,7 @@ public:
 
     SsnState read_state() {
         SsnState hs;
-        d2h(&hs, state_.get(), sizeof(hs), st_);
-        sync(st_);
+        read_small(P_->ctx, &hs, state_.get(), sizeof(hs), st_);
         return hs;
     }
 

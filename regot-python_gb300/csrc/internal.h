@@ -158,6 +158,18 @@ inline void count_launch(int k = 1) {
 
 }  // namespace regot
 
+struct regot_ctx;
+namespace regot {
+// Page-locked staging block of the context, at least `bytes` long (grown on
+// demand, freed with the context). A copy from the device to pageable memory
+// is a blocking round trip per call; copies into this block are
+// asynchronous, so several results come back behind one synchronisation.
+void* ctx_stage(regot_ctx* ctx, size_t bytes);
+// Blocking read of `bytes` (at most a few KB) from the device through the
+// staging block.
+void read_small(regot_ctx* ctx, void* dst, const void* src, size_t bytes, cudaStream_t st);
+}  // namespace regot
+
 // ---------------------------------------------------------- C-ABI objects --
 struct regot_ctx {
     int device = 0;
@@ -165,6 +177,8 @@ struct regot_ctx {
     cudaStream_t own_stream = nullptr;
     std::string last_error;
     long long launches = 0;
+    void* stage = nullptr;  // page-locked staging for small device-to-host reads
+    size_t stage_bytes = 0;
 };
 
 struct regot_dproblem {
@@ -175,5 +189,7 @@ struct regot_dproblem {
     void* M = nullptr;            // device, n x ldm
     double* a = nullptr;          // device
     double* b = nullptr;          // device
+    double* loga = nullptr;       // device log(a), log(b): made by the first EROT solve
+    double* logb = nullptr;
     std::vector<double> ha, hb;   // host copies
 };
