@@ -164,14 +164,8 @@ void finish_erot_result(ErotOps& ops, const double* d_gamma, const double* hobj,
     if (res->densities && hdens) std::memcpy(res->densities, h_dens, L * sizeof(double));
     if (o.plan && res->plan) {
         DBuf<double> mx(1, st);
-        if (o.plan_mem == REGOT_MEM_DEVICE) {
-            ops.plan(d_gamma, d_gamma + n, res->plan, mx.get());
-        } else {
-            DBuf<double> P((size_t)n * m, st);
-            ops.plan(d_gamma, d_gamma + n, P.get(), mx.get());
-            d2h(res->plan, P.get(), (size_t)n * m * sizeof(double), st);
-            sync(st);
-        }
+        emit_plan(res->plan, o.plan_mem, (size_t)n * m, st,
+                  [&](double* dst) { ops.plan(d_gamma, d_gamma + n, dst, mx.get()); });
     }
     sync(st);
 }
@@ -185,7 +179,7 @@ namespace {
 // out again to requests of up to their size.
 constexpr size_t kPinnedCacheBytes = size_t(4) << 30;
 std::mutex g_pinned_mutex;
-std::unordered_map<void*, size_t> g_pinned_live;
+std::map<void*, size_t> g_pinned_live;  // ordered: host_block_view finds the enclosing block
 std::multimap<size_t, void*> g_pinned_free;
 size_t g_pinned_free_bytes = 0;
 
@@ -207,7 +201,7 @@ int regot_host_alloc(size_t bytes, void** out) {
         return REGOT_OK;
     }
     void* p = nullptr;
-    if (cudaHostAlloc(&p, bytes, cudaHostAllocPortable) != cudaSuccess) {
+    if (cudaHostAlloc(&p, bytes, cudaHostAllocPortable | cudaHostAllocMapped) != cudaSuccess) {
         cudaGetLastError();
         return REGOT_ERR_CUDA;
     }
@@ -232,6 +226,31 @@ void regot_host_free(void* ptr) {
         g_pinned_free.erase(small);
     }
 }
+
+}  // extern "C"
+
+namespace regot {
+
+void* host_block_view(void* p, size_t bytes) {
+    if (!p) return nullptr;
+    std::lock_guard<std::mutex> lock(g_pinned_mutex);
+    const char* q = static_cast<const char*>(p);
+    auto it = g_pinned_live.upper_bound(p);  // first block starting after p
+    if (it == g_pinned_live.begin()) return nullptr;
+    --it;
+    const char* base = static_cast<const char*>(it->first);
+    if (q < base || q + bytes > base + it->second) return nullptr;
+    void* dev = nullptr;
+    if (cudaHostGetDevicePointer(&dev, it->first, 0) != cudaSuccess || !dev) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return static_cast<char*>(dev) + (q - base);
+}
+
+}  // namespace regot
+
+extern "C" {
 
 void regot_opts_init(regot_opts* o) {
     if (!o) return;
@@ -340,6 +359,8 @@ int regot_problem_create(regot_ctx* ctx, const regot_problem_desc* d, int precis
             for (int j = 0; j < m; ++j)
                 require(std::isfinite(P->hb[j]) && P->hb[j] > 0.0,
                         "b must be finite and positive");
+            for (int i = 0; i < n; ++i) P->sum_a += P->ha[i];
+            for (int j = 0; j < m - 1; ++j) P->sum_bt += P->hb[j];
             h2d(P->a, P->ha.data(), n * sizeof(double), st);
             h2d(P->b, P->hb.data(), m * sizeof(double), st);
 
@@ -530,13 +551,8 @@ int regot_erot_plan(regot_ctx* ctx, regot_dproblem* P, double reg, const double*
         ErotOps ops(P, reg, st);
         DBuf<double> g(n + m, st), mx(1, st);
         upload_gamma(gamma, n, m, g.get(), st);
-        if (plan_mem == REGOT_MEM_DEVICE) {
-            ops.plan(g.get(), g.get() + n, plan, mx.get());
-        } else {
-            DBuf<double> out((size_t)n * m, st);
-            ops.plan(g.get(), g.get() + n, out.get(), mx.get());
-            d2h(plan, out.get(), (size_t)n * m * sizeof(double), st);
-        }
+        emit_plan(plan, plan_mem, (size_t)n * m, st,
+                  [&](double* dst) { ops.plan(g.get(), g.get() + n, dst, mx.get()); });
         sync(st);
     });
 }

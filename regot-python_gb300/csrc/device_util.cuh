@@ -368,4 +368,26 @@ inline void d2d(void* dst, const void* src, size_t bytes, cudaStream_t st) {
 }
 inline void sync(cudaStream_t st) { REGOT_CUDA(cudaStreamSynchronize(st)); }
 
+// Plan output of `count` doubles at `plan` (device or host memory per
+// plan_mem); compute(dst) launches the kernel that writes dst. A host
+// destination inside a regot_host_alloc block is written by the kernel
+// directly (the transfer overlaps the computation and no device copy of the
+// plan is made); other host memory goes through a device buffer and one copy.
+// The caller synchronises the stream before reading the host result.
+template <typename F>
+void emit_plan(double* plan, int plan_mem, size_t count, cudaStream_t st, F&& compute) {
+    if (plan_mem == REGOT_MEM_DEVICE) {
+        compute(plan);
+        return;
+    }
+    if (void* view = host_block_view(plan, count * sizeof(double))) {
+        compute(static_cast<double*>(view));
+        return;
+    }
+    DBuf<double> out(count, st);
+    compute(out.get());
+    d2h(plan, out.get(), count * sizeof(double), st);
+    sync(st);
+}
+
 }  // namespace regot

@@ -19,6 +19,7 @@
 // so the host only synchronises once per batch.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 #include "device_util.cuh"
@@ -47,6 +48,8 @@ struct BcdState {
     int hist_len;
     int max_iter;
     unsigned counter;
+    int loops;     // bodies of the device-side sweep loop run so far
+    int loop_cap;  // hard bound on loops (the loop kernel stops there)
     int pad;
     double tol;
     double sum_bb;     // sum_{j<m-1} b_j beta_j of the current beta
@@ -54,7 +57,7 @@ struct BcdState {
     double gb2_once;   // squared beta-part of the gradient of iterate 0 (x0 given)
     double maxabs;     // running max |alpha|, |beta| (hi/lo split grid)
     double last_gnorm; // marginal error of the last recorded iterate
-    // Fixed hi/lo grid of the ping-pong sweeps (k_bcd_grid): the split value
+    // Fixed hi/lo grid of the ping-pong sweeps (k_bcd_init): the split value
     // handed to k_split, the grid g and 1/g, and the bound on |dual| that
     // keeps hi exact on g.
     double gval, sg, sinv, sbound;
@@ -66,9 +69,6 @@ __device__ __forceinline__ bool sum_ok(double s) {
     return isfinite(s) && s > (MIXED ? 1e-30 : 1e-290);
 }
 
-// Row finalize of K1: gradient/objective of iterate k, history, stopping
-// test, alpha_{k+1}. `anchor` is the row vector the pass used (alpha itself
-// on the fast path, -max_j(beta_j - M_ij) on the robust path).
 // Fixed hi/lo grid of the ping-pong sweeps: the finalize kernels write the
 // FP32 split of the duals they produce, for the next pass, on the grid kept
 // in BcdState.
@@ -81,17 +81,60 @@ __device__ __forceinline__ float4 split_fixed(double v, const BcdState* st) {
     return make_float4((float)h, (float)(v - h), 0.f, 0.f);
 }
 
-// Grid of the ping-pong sweeps from the running max |dual| of the initial
-// value: g = 2^(e + 3 - 21), e = ilogb(max), i.e. 8x headroom.
-__global__ void k_bcd_grid(BcdState* st) {
-    const double m0 = st->maxabs;
-    const int e = (m0 > 0.0 && isfinite(m0)) ? ilogb(m0) : 0;
-    st->gval = ldexp(1.0, e + 3);
-    st->sg = ldexp(1.0, e + 3 - 21);
-    st->sinv = ldexp(1.0, -(e + 3 - 21));
-    st->sbound = ldexp(1.0, e + 4);
+// Start of the sweeps, after the initial value (sinkhorn_bcd.cpp:49-51): the
+// timer, sum_{j<m-1} b_j beta_j and beta_{m-1}, max |alpha|, |beta|, and
+// from it the grid of the ping-pong sweeps, g = 2^(e + 3 - 21) with
+// e = ilogb(max), i.e. 8x headroom. st->maxabs is zero on entry.
+__global__ void k_bcd_init(const double* b, const double* alpha, int n, const double* beta,
+                           int m, double* parts, BcdState* st) {
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
+    if (gt == 0) st->t0 = globaltimer_ns();
+    double v[1] = {0.0};
+    unsigned long long mb = 0ULL;
+    for (int j = gt; j < m - 1; j += gs) v[0] += b[j] * beta[j];
+    for (int t = gt; t < n + m; t += gs) {
+        const unsigned long long q = abs_bits(t < n ? alpha[t] : beta[t - n]);
+        mb = q > mb ? q : mb;
+    }
+    block_atomic_max_bits(&st->maxabs, mb);
+    __threadfence();
+    double out[1];
+    if (grid_reduce<1>(v, parts, &st->counter, out)) {
+        st->sum_bb = out[0];
+        st->beta_last = __ldcg(&beta[m - 1]);
+        const double m0 =
+            __longlong_as_double((long long)atomicAdd(reinterpret_cast<unsigned long long*>(&st->maxabs), 0ULL));
+        const int e = (m0 > 0.0 && isfinite(m0)) ? ilogb(m0) : 0;
+        st->gval = ldexp(1.0, e + 3);
+        st->sg = ldexp(1.0, e + 3 - 21);
+        st->sinv = ldexp(1.0, -(e + 3 - 21));
+        st->sbound = ldexp(1.0, e + 4);
+    }
 }
 
+// Condition of the device-side sweep loop (the last node of its body, run
+// on every pass through it): continue while not done and no hand-over is
+// pending, and never beyond loop_cap bodies, so the loop ends even if no
+// other kernel of the body ran.
+__global__ void k_bcd_loop(BcdState* st, cudaGraphConditionalHandle h) {
+    const int loops = ++st->loops;
+    const bool go = !st->done && !st->bad && loops < st->loop_cap;
+    cudaGraphSetConditional(h, go ? 1u : 0u);
+}
+
+// Graph and executable graph of the sweep loop, destroyed on every exit.
+struct LoopGraph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    ~LoopGraph() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+    }
+};
+
+// Row finalize of K1: gradient/objective of iterate k, history, stopping
+// test, alpha_{k+1}. `anchor` is the row vector the pass used (alpha itself
+// on the fast path, -max_j(beta_j - M_ij) on the robust path).
 template <typename Acc, bool MIXED>
 __global__ void k_bcd_row(const Acc* rp, int nslabs, int n, const double* anchor,
                           const double* alpha, const double* a, const double* loga, double reg,
@@ -192,8 +235,6 @@ __global__ void k_bcd_commit(int n, int m, double* alpha, const double* alpha_ne
     if (t == 0) st->iter += 1;
 }
 
-__global__ void k_bcd_start(BcdState* st) { st->t0 = globaltimer_ns(); }
-
 __global__ void k_gauge(int n, int m, const double* alpha, const double* beta, double* ga,
                         double* gb) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -216,19 +257,6 @@ __global__ void k_colgrad_sq(const double* c, const double* b, int m, double* ou
         double t = 0.0;
         for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s[w];
         *out = t;
-    }
-}
-
-// sum_{j<m-1} b_j beta_j and beta_{m-1} of the initial beta.
-__global__ void k_dot_bt(const double* b, const double* beta, int m, double* parts,
-                         BcdState* st) {
-    double v[1] = {0.0};
-    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < m - 1; j += gridDim.x * blockDim.x)
-        v[0] += b[j] * beta[j];
-    double out[1];
-    if (grid_reduce<1>(v, parts, &st->counter, out)) {
-        st->sum_bb = out[0];
-        st->beta_last = __ldcg(&beta[m - 1]);
     }
 }
 
@@ -255,6 +283,9 @@ void sinkhorn_bcd_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol,
     BcdState h0{};
     h0.max_iter = max_iter;
     h0.tol = tol;
+    // two sweeps per body of the device-side loop; iterate max_iter always
+    // stops it, this bound only guards the loop itself
+    h0.loop_cap = max_iter / 2 + 3;
     h2d(dst.get(), &h0, sizeof(h0), st);
     BcdState* S = dst.get();
     double* mx = scratch.get();
@@ -271,17 +302,15 @@ void sinkhorn_bcd_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol,
         ops.optimal_beta(alpha.get(), beta.get(), mx);
     }
     // Timer starts after the initial value (sinkhorn_bcd.cpp:49-51).
-    k_bcd_start<<<1, 1, 0, st>>>(S);
-    k_dot_bt<<<std::min(std::max(cdiv(m - 1, 256), 1), 64), 256, 0, st>>>(P->b, beta.get(), m,
-                                                                         parts.get(), S);
-    count_launch(2);
+    k_bcd_init<<<std::min(cdiv((long long)n + m, 256), 64), 256, 0, st>>>(
+        P->b, alpha.get(), n, beta.get(), m, parts.get(), S);
+    count_launch();
     if (has_x0) {
         // With a user x0 the beta part of the first gradient is not zero.
         ops.row_col_sums(alpha.get(), beta.get(), rsum.get(), csum.get(), mx);
         k_colgrad_sq<<<1, 256, 0, st>>>(csum.get(), P->b, m, &S->gb2_once);
         count_launch();
     }
-    ops.maxabs(alpha.get(), n, beta.get(), m, &S->maxabs);
     REGOT_CHECK_LAUNCH();
 
     BcdState hs{};
@@ -323,8 +352,6 @@ void sinkhorn_bcd_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol,
         float4* cs = const_cast<float4*>(ops.csplit());
         SplitOut so_r, so_c;
         if (mixed) {
-            k_bcd_grid<<<1, 1, 0, st>>>(S);
-            count_launch();
             PassParams q = ops.base_params();
             q.ra = alpha.get();
             q.cb = beta.get();
@@ -365,37 +392,48 @@ void sinkhorn_bcd_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol,
                     reg, B[1 - q], parts.get(), S, 0, so_c, 1);
             count_launch(2);
         };
-        cudaGraph_t graph = nullptr;
-        cudaGraphExec_t exec = nullptr;
+        // The sweeps run as a device-side loop: a graph whose only node is a
+        // conditional WHILE node; its body is two sweeps and k_bcd_loop,
+        // which sets the condition. One launch and one read of the state
+        // per solve: no host round trip between sweeps and none launched
+        // past convergence.
+        LoopGraph lg;
+        REGOT_CUDA(cudaGraphCreate(&lg.graph, 0));
+        cudaGraphConditionalHandle loop_h;
+        REGOT_CUDA(cudaGraphConditionalHandleCreate(&loop_h, lg.graph, 1, cudaGraphCondAssignDefault));
+        cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+        cp.conditional.handle = loop_h;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t loop_node;
+        REGOT_CUDA(cudaGraphAddNode(&loop_node, lg.graph, nullptr, nullptr, 0, &cp));
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
         long long* saved_counter = g_launch_counter;
         long long graph_kernels = 0;
         g_launch_counter = &graph_kernels;
-        REGOT_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-        half_sweeps(0);
-        half_sweeps(1);
-        REGOT_CUDA(cudaStreamEndCapture(st, &graph));
-        g_launch_counter = saved_counter;
-        REGOT_CUDA(cudaGraphInstantiate(&exec, graph, 0));
-
-        int batch = 4;  // sweeps; the graph runs two per launch
-        long long launched = 0;
-        for (;;) {
-            const int reps = (batch + 1) / 2;
-            for (int q = 0; q < reps; ++q) REGOT_CUDA(cudaGraphLaunch(exec, st));
-            launched += 2LL * reps;
-            count_launch(graph_kernels * reps);
-            read_state();
-            if (hs.bad) break;
-            if (hs.done) {
-                finished = true;
-                break;
-            }
-            if (launched > 2LL * max_iter + 64)
-                throw Error(REGOT_ERR_NUMERIC, "BCD did not terminate");
-            batch = next_batch(batch);
+        REGOT_CUDA(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0,
+                                                 cudaStreamCaptureModeThreadLocal));
+        try {
+            half_sweeps(0);
+            half_sweeps(1);
+            k_bcd_loop<<<1, 1, 0, st>>>(S, loop_h);
+            count_launch();
+        } catch (...) {
+            cudaGraph_t g = nullptr;
+            cudaStreamEndCapture(st, &g);
+            g_launch_counter = saved_counter;
+            throw;
         }
-        cudaGraphExecDestroy(exec);
-        cudaGraphDestroy(graph);
+        REGOT_CUDA(cudaStreamEndCapture(st, &body));
+        g_launch_counter = saved_counter;
+        REGOT_CUDA(cudaGraphInstantiate(&lg.exec, lg.graph, 0));
+        REGOT_CUDA(cudaGraphLaunch(lg.exec, st));
+        read_state();
+        count_launch(graph_kernels * hs.loops);
+        if (!hs.bad) {
+            if (!hs.done) throw Error(REGOT_ERR_NUMERIC, "BCD did not terminate");
+            finished = true;
+        }
         const int k = hs.iter;
         const size_t an = n * sizeof(double), bm = m * sizeof(double);
         if (finished || (hs.bad & (1 | 4))) {

@@ -27,18 +27,23 @@ __global__ void k_maxabs(const double* x, int nx, const double* y, int ny, doubl
     block_atomic_max_bits(out, v);
 }
 
-// anchor = -max partials (row or column direction).
+// anchor = -max partials (row or column direction); *mx is raised to
+// max |anchor| as well.
 template <typename Acc>
-__global__ void k_row_anchor(const Acc* rp, int nslabs, int n, double* anchor) {
+__global__ void k_row_anchor(const Acc* rp, int nslabs, int n, double* anchor, double* mx) {
     const int i = blockIdx.x * kMergeItems + threadIdx.x;
     const double v = max_2d(rp + i, nslabs, (size_t)n, i < n);
-    if (threadIdx.y == 0 && i < n) anchor[i] = -v;
+    const bool own = threadIdx.y == 0 && i < n;
+    if (own) anchor[i] = -v;
+    block_atomic_max_bits(mx, own ? abs_bits(v) : 0ULL);
 }
 template <typename Acc>
-__global__ void k_col_anchor(const Acc* cp, int nrb, int m, double* anchor) {
+__global__ void k_col_anchor(const Acc* cp, int nrb, int m, double* anchor, double* mx) {
     const int j = blockIdx.x * kMergeItems + threadIdx.x;
     const double v = max_2d(cp + j, nrb, (size_t)m, j < m);
-    if (threadIdx.y == 0 && j < m) anchor[j] = -v;
+    const bool own = threadIdx.y == 0 && j < m;
+    if (own) anchor[j] = -v;
+    block_atomic_max_bits(mx, own ? abs_bits(v) : 0ULL);
 }
 
 // out = anchor + reg (logw - log S'), S' from the partial sums.
@@ -89,8 +94,8 @@ ErotOps::ErotOps(regot_dproblem* P, double reg, cudaStream_t st)
         count_launch(2);
         REGOT_CHECK_LAUNCH();
     }
-    for (int i = 0; i < n_; ++i) sum_a_ += P->ha[i];
-    for (int j = 0; j < m_ - 1; ++j) sum_bt_ += P->hb[j];
+    sum_a_ = P->sum_a;
+    sum_bt_ = P->sum_bt;
     buf_.init(n_, m_, mixed_, 3, 2, 4, st_);
     anchor_.alloc((size_t)(n_ > m_ ? n_ : m_), st_);
     err_.alloc(1, st_);
@@ -184,8 +189,8 @@ void ErotOps::optimal_beta(const double* alpha, double* beta, double* mx) {
     maxabs(alpha, n_, nullptr, 0, mx);
     p.grid = mx;
     pass(OP_E_COLMAX, p);
-    REGOT_LAUNCH_ACC(k_col_anchor, m_, buf_.colpart.get(), buf_.shape.nrb, m_, anchor_.get());
-    maxabs(alpha, n_, anchor_.get(), m_, mx);
+    // mx = max(|alpha|, |anchor|): the anchor kernel raises max |alpha|
+    REGOT_LAUNCH_ACC(k_col_anchor, m_, buf_.colpart.get(), buf_.shape.nrb, m_, anchor_.get(), mx);
     p.cb = anchor_.get();
     pass(OP_E_COL, p);
     REGOT_LAUNCH_ACC(k_col_lse, m_, buf_.colpart.get(), buf_.shape.nrb, m_, anchor_.get(),
@@ -199,8 +204,7 @@ void ErotOps::optimal_alpha(const double* beta, double* alpha, double* mx) {
     maxabs(beta, m_, nullptr, 0, mx);
     p.grid = mx;
     pass(OP_E_ROWMAX, p);
-    REGOT_LAUNCH_ACC(k_row_anchor, n_, buf_.rowpart.get(), buf_.shape.nslabs, n_, anchor_.get());
-    maxabs(beta, m_, anchor_.get(), n_, mx);
+    REGOT_LAUNCH_ACC(k_row_anchor, n_, buf_.rowpart.get(), buf_.shape.nslabs, n_, anchor_.get(), mx);
     p.ra = anchor_.get();
     pass(OP_E_ROW, p);
     REGOT_LAUNCH_ACC(k_row_lse, n_, buf_.rowpart.get(), buf_.shape.nslabs, n_, anchor_.get(),

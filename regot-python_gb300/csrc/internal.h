@@ -168,6 +168,9 @@ void* ctx_stage(regot_ctx* ctx, size_t bytes);
 // Blocking read of `bytes` (at most a few KB) from the device through the
 // staging block.
 void read_small(regot_ctx* ctx, void* dst, const void* src, size_t bytes, cudaStream_t st);
+// Device address of host memory [p, p + bytes) when it lies inside one live
+// block of regot_host_alloc (page-locked and mapped), else nullptr.
+void* host_block_view(void* p, size_t bytes);
 }  // namespace regot
 
 // ---------------------------------------------------------- C-ABI objects --
@@ -192,4 +195,6 @@ struct regot_dproblem {
     double* loga = nullptr;       // device log(a), log(b): made by the first EROT solve
     double* logb = nullptr;
     std::vector<double> ha, hb;   // host copies
+    double sum_a = 0.0;           // sum_i a_i
+    double sum_bt = 0.0;          // sum_{j < m-1} b_j
 };

@@ -265,6 +265,56 @@ __device__ __forceinline__ T warp_reduce_rows(T (&v)[N], int lane) {
     return r;
 }
 
+// Plan output: the VW values of one lane vector are collected in pv and
+// stored together once the vector is complete. The plan may be host memory
+// written across the host link, where only whole, contiguous lines per warp
+// store run at the link's rate, so with FP32 M (VW = 4: a lane owns 32 bytes
+// of every 1 KB block of the row) the values are first exchanged between
+// lanes so that each store instruction of the warp covers 512 contiguous
+// bytes. Partial blocks and rows that do not start on 16 bytes are stored
+// lane by lane. With FP64 M (VW = 2) a lane's 16 bytes are already
+// contiguous across the warp. The control flow around the call is uniform
+// across the warp (one row per warp), as the shuffles require.
+template <int VW>
+__device__ __forceinline__ void plan_put(double (&pv)[VW], int q, double val, double* out, int i,
+                                         int m, int c0, int lane) {
+    const int e = q % VW;
+    pv[e] = val;
+    if (e != VW - 1) return;
+    double* row = out + (long long)i * m;
+    const int j0 = c0 + ((q / VW) * 32 + lane) * VW;
+    if constexpr (VW == 4) {
+        const int jb = c0 + (q / VW) * 128;  // first column of the warp's 1 KB block
+        if (jb + 128 <= m && (reinterpret_cast<uintptr_t>(row + jb) & 15) == 0) {
+            const int s1 = lane >> 1, s2 = 16 + (lane >> 1);
+            const bool odd = lane & 1;
+            const double a0 = __shfl_sync(0xffffffffu, pv[0], s1);
+            const double a1 = __shfl_sync(0xffffffffu, pv[1], s1);
+            const double a2 = __shfl_sync(0xffffffffu, pv[2], s1);
+            const double a3 = __shfl_sync(0xffffffffu, pv[3], s1);
+            const double b0 = __shfl_sync(0xffffffffu, pv[0], s2);
+            const double b1 = __shfl_sync(0xffffffffu, pv[1], s2);
+            const double b2 = __shfl_sync(0xffffffffu, pv[2], s2);
+            const double b3 = __shfl_sync(0xffffffffu, pv[3], s2);
+            *reinterpret_cast<double2*>(row + jb + 2 * lane) =
+                odd ? make_double2(a2, a3) : make_double2(a0, a1);
+            *reinterpret_cast<double2*>(row + jb + 64 + 2 * lane) =
+                odd ? make_double2(b2, b3) : make_double2(b0, b1);
+            return;
+        }
+    }
+    double* dst = row + j0;
+    if (j0 + VW <= m && (reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
+#pragma unroll
+        for (int h = 0; h < VW; h += 2)
+            *reinterpret_cast<double2*>(dst + h) = make_double2(pv[h], pv[h + 1]);
+    } else {
+#pragma unroll
+        for (int h = 0; h < VW; ++h)
+            if (j0 + h < m) dst[h] = pv[h];
+    }
+}
+
 // Persistent dense pass. The grid holds as many CTAs as fit on the SMs; CTA
 // b processes tiles b, b + G, b + 2G, ... (tile t = row block t / nslabs,
 // column slab t % nslabs; RB rows x CW columns). Each warp streams RB/8 rows
@@ -569,6 +619,8 @@ __global__ void __launch_bounds__(kThreads, 2) dense_pass(const PassParams p) {
                         }
                         racc[0] = racc2.x + racc2.y;
                     }
+                    double pv[VW];  // plan values of one vector (plan passes)
+                    (void)pv;
     #pragma unroll
                     for (int q = 0; q < (PAIRED ? 0 : LC); ++q) {
                         const TM mval = Vec<TM>::get(mv[q / VW], q % VW);
@@ -614,10 +666,7 @@ __global__ void __launch_bounds__(kThreads, 2) dense_pass(const PassParams p) {
                                 for (int s2 = 0; s2 < 4; ++s2)
                                     if (s2 < nsteps) tot[s2] += T * expm1_minus_x(steps[s2] * w);
                             } else if constexpr (OP == OP_E_PLAN) {
-                                if (cvalid[q]) {
-                                    const int j = c0 + ((q / VW) * 32 + lane) * VW + (q % VW);
-                                    p.out[(long long)i * m + j] = (double)T;
-                                }
+                                plan_put<VW>(pv, q, (double)T, p.out, i, m, c0, lane);
                             }
                         } else {
                             TM arg;
@@ -666,10 +715,7 @@ __global__ void __launch_bounds__(kThreads, 2) dense_pass(const PassParams p) {
                                 tot[0] += R * mval;
                                 tot[1] += R * R;
                             } else if constexpr (OP == OP_Q_PLAN) {
-                                if (cvalid[q]) {
-                                    const int j = c0 + ((q / VW) * 32 + lane) * VW + (q % VW);
-                                    p.out[(long long)i * m + j] = (double)D * p.inv_reg_d;
-                                }
+                                plan_put<VW>(pv, q, (double)D * p.inv_reg_d, p.out, i, m, c0, lane);
                             }
                         }
                     }

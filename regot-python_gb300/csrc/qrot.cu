@@ -346,7 +346,7 @@ public:
         scal_.alloc(8, st);
         const PassShape sh = ops_.buf().shape;
         bm_words_ = (size_t)n_ * sh.nslabs * (mixed_ ? Geo<float>::LC : Geo<double>::LC);
-        for (int i = 0; i < n_; ++i) sum_a_ += P->ha[i];
+        sum_a_ = P->sum_a;
     }
 
     int n() const { return n_; }
@@ -609,15 +609,9 @@ void finish_qrot(QrotEngine& E, const double* d_gamma, const std::vector<double>
     if (res->mar_errs) std::memcpy(res->mar_errs, hmar.data(), L * sizeof(double));
     if (res->run_times) std::memcpy(res->run_times, htime.data(), L * sizeof(double));
     if (res->prim_vals) std::memcpy(res->prim_vals, hprim.data(), L * sizeof(double));
-    if (o.plan && res->plan) {
-        if (o.plan_mem == REGOT_MEM_DEVICE) {
-            E.plan(d_gamma, res->plan);
-        } else {
-            DBuf<double> Pl((size_t)n * m, st);
-            E.plan(d_gamma, Pl.get());
-            d2h(res->plan, Pl.get(), (size_t)n * m * sizeof(double), st);
-        }
-    }
+    if (o.plan && res->plan)
+        emit_plan(res->plan, o.plan_mem, (size_t)n * m, st,
+                  [&](double* dst) { E.plan(d_gamma, dst); });
     E.ops().check_err();
 }
 
@@ -983,13 +977,8 @@ int regot_qrot_plan(regot_ctx* ctx, regot_dproblem* P, double reg, const double*
         QrotEngine E(P, reg, 0.0, ctx->stream);
         const int n = P->n, m = P->m;
         h2d(E.gamma(), gamma, (n + m) * sizeof(double), ctx->stream);
-        if (plan_mem == REGOT_MEM_DEVICE) {
-            E.plan(E.gamma(), plan);
-        } else {
-            DBuf<double> out((size_t)n * m, ctx->stream);
-            E.plan(E.gamma(), out.get());
-            d2h(plan, out.get(), (size_t)n * m * sizeof(double), ctx->stream);
-        }
+        emit_plan(plan, plan_mem, (size_t)n * m, ctx->stream,
+                  [&](double* dst) { E.plan(E.gamma(), dst); });
         E.ops().check_err();
     });
 }

@@ -281,7 +281,7 @@ class Problem:
 
     def erot_plan(self, reg, gamma):
         gamma = self._vec(gamma, self.n + self.m - 1)
-        P = np.zeros((self.n, self.m))
+        P = L.host_empty((self.n, self.m))
         self.ctx.check(self._lib.regot_erot_plan(
             self.ctx.handle, self.handle, float(reg), gamma.ctypes.data, P.ctypes.data,
             L.REGOT_MEM_HOST))
@@ -324,7 +324,7 @@ class Problem:
 
     def qrot_plan(self, reg, gamma):
         gamma = self._vec(gamma, self.n + self.m)
-        P = np.zeros((self.n, self.m))
+        P = L.host_empty((self.n, self.m))
         self.ctx.check(self._lib.regot_qrot_plan(
             self.ctx.handle, self.handle, float(reg), gamma.ctypes.data, P.ctypes.data,
             L.REGOT_MEM_HOST))
