@@ -206,6 +206,86 @@ def run_reference(args, n):
     print(json.dumps(line))
 
 
+def run_probe(kind, n):
+    """Ceilings on this GPU, printed as one JSON line.
+
+    hbm-read : one read of a 4 n^2-byte FP32 array by torch's sum reduction
+               (CUDA events, best of 10 after warm-up; the array is larger
+               than L2), next to the row pass over M of the same size.
+    host-link: page-locked host <-> device copies of M's size up and the FP64
+               plan's size down (torch, one copy engine), and the library's
+               plan kernel writing the FP64 plan straight into a page-locked
+               block of regot_host_alloc.
+    """
+    import torch
+
+    import regot
+    from problems import erot_points
+    from regot import _lib
+
+    dev = torch.device("cuda", 0)
+
+    def best_ms(fn, reps=10):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize(dev)
+        out = []
+        for _ in range(reps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            torch.cuda.synchronize(dev)
+            out.append(e0.elapsed_time(e1))
+        return min(out)
+
+    res = {"probe": kind, "n": n}
+    if kind == "hbm-read":
+        x = torch.ones(n * n, dtype=torch.float32, device=dev)
+        ms = best_ms(lambda: x.sum())
+        res["torch_sum_us"] = round(ms * 1e3, 2)
+        res["torch_sum_gbs"] = round(4 * n * n / (ms * 1e-3) / 1e9, 1)
+        del x
+        M, a, b = erot_points(n, n, seed=0, dtype=np.float32)
+        prob = regot.Problem(M, a, b, precision="mixed")
+        ctx = _lib.context(0)
+        stream = torch.cuda.current_stream(dev)
+        ctx.set_stream(stream.cuda_stream)
+        lib = _lib.load()
+        ctx.check(lib.regot_time_pass(ctx.handle, prob.handle, 0, REG, 1))  # prepares
+        ms = best_ms(lambda: ctx.check(lib.regot_time_pass(ctx.handle, prob.handle, 0, REG, 1)))
+        res["row_pass_us"] = round(ms * 1e3, 2)
+        res["row_pass_gbs"] = round(4 * n * n / (ms * 1e-3) / 1e9, 1)
+        prob.close()
+        ctx.set_stream(None)
+    else:
+        h = torch.empty(n * n, dtype=torch.float32, pin_memory=True)
+        d = torch.empty(n * n, dtype=torch.float32, device=dev)
+        ms = best_ms(lambda: d.copy_(h, non_blocking=True))
+        res["h2d_M_ms"] = round(ms, 3)
+        res["h2d_gbs"] = round(4 * n * n / (ms * 1e-3) / 1e9, 1)
+        h64 = torch.empty(n * n, dtype=torch.float64, pin_memory=True)
+        d64 = torch.empty(n * n, dtype=torch.float64, device=dev)
+        ms = best_ms(lambda: h64.copy_(d64, non_blocking=True))
+        res["d2h_plan_ms"] = round(ms, 3)
+        res["d2h_gbs"] = round(8 * n * n / (ms * 1e-3) / 1e9, 1)
+        del h, d, h64, d64
+        M, a, b = erot_points(n, n, seed=0, dtype=np.float32)
+        prob = regot.Problem(M, a, b, precision="mixed")
+        gamma = prob.sinkhorn_bcd(REG, tol=TOL, max_iter=MAX_ITER, plan=False).dual
+        prob.erot_plan(REG, gamma)
+        ts = []
+        for _ in range(5):
+            t = time.perf_counter()
+            prob.erot_plan(REG, gamma)
+            ts.append((time.perf_counter() - t) * 1e3)
+        res["plan_to_host_block_ms"] = round(min(ts), 3)
+        res["plan_to_host_block_gbs"] = round(8 * n * n / (min(ts) * 1e-3) / 1e9, 1)
+        prob.close()
+    print(json.dumps(res))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -215,7 +295,9 @@ def main():
     ap.add_argument("--n", type=int, default=N)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ncu-case", action="store_true",
-                    help="one short solve for an ncu capture (no timing, no JSON)")
+                    help="a few passes for an ncu capture (no timing, no JSON)")
+    ap.add_argument("--probe", choices=["hbm-read", "host-link"],
+                    help="measure the ceilings the numbers are read against (no JSON line)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     n = args.n
@@ -224,13 +306,26 @@ def main():
         run_reference(args, n)
         return
     if args.ncu_case:
+        # The BCD sweeps run inside a conditional graph node, whose kernels
+        # ncu does not list; the passes are launched here on their own.
+        # dense_pass launches: optimal_beta's column-max and column passes,
+        # then row, row, column, column (regot_time_pass runs a pass once
+        # with its split, then `reps` times reusing it), so
+        # `-k regex:dense_pass -s 3 -c 2` captures one row and one column pass.
         import regot
         from problems import erot_points
+        from regot import _lib
 
         M, a, b = erot_points(n, n, seed=0, dtype=np.float32)
         prob = regot.Problem(M, a, b, precision="mixed")
         r = prob.sinkhorn_bcd(REG, tol=TOL, max_iter=3, plan=False)
+        ctx = _lib.context(0)
+        for kind in (0, 1):
+            ctx.check(_lib.load().regot_time_pass(ctx.handle, prob.handle, kind, REG, 1))
         print("ncu case: niter", r.niter, "mar_err", r.mar_errs[-1])
+        return
+    if args.probe:
+        run_probe(args.probe, n)
         return
 
     import torch
@@ -292,6 +387,8 @@ def main():
     k1.record(stream)
     torch.cuda.synchronize(dev)
     row_ms = k0.elapsed_time(k1) / reps
+    _lib.load().regot_time_pass(ctx.handle, prob.handle, 1, REG, 1)  # warm, prepares the split
+    torch.cuda.synchronize(dev)
     k0.record(stream)
     ctx.check(_lib.load().regot_time_pass(ctx.handle, prob.handle, 1, REG, reps))
     k1.record(stream)

@@ -205,8 +205,11 @@ enum {
 };
 /* Enqueue `reps` launches of one dense pass over M on the context's stream
  * (duals zero, beta = 0) and return without synchronising, so that the
- * caller can bracket them with its own events. No counterpart in the
- * reference: it measures the kernels behind the solvers above. */
+ * caller can bracket them with its own events. The first call for a
+ * (problem, kind, reg) also prepares the pass inputs (in mixed precision the
+ * FP32 split and one pass) and synchronises before enqueueing; later calls
+ * enqueue the `reps` passes only. No counterpart in the reference: it
+ * measures the kernels behind the solvers above. */
 int regot_time_pass(regot_ctx* ctx, regot_dproblem* prob, int kind, double reg, int reps);
 
 /* ---- Allocation-free variant ----
