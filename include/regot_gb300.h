@@ -147,6 +147,13 @@ int regot_sinkhorn_newton(regot_ctx* ctx, regot_dproblem* prob, double reg, doub
 /* sinkhorn_ssns (src/sinkhorn_ssns.cpp:16-234). */
 int regot_sinkhorn_ssns(regot_ctx* ctx, regot_dproblem* prob, double reg, double tol,
                         int max_iter, const regot_opts* opts, regot_result* res);
+/* sinkhorn_lbfgs_dual (src/sinkhorn_lbfgs_dual.cpp:81-126). */
+int regot_sinkhorn_lbfgs_dual(regot_ctx* ctx, regot_dproblem* prob, double reg, double tol,
+                              int max_iter, const regot_opts* opts, regot_result* res);
+/* sinkhorn_apdagd (src/sinkhorn_apdagd.cpp:14-183); the returned plan is
+ * the averaged primal plan, the dual the last extrapolated point. */
+int regot_sinkhorn_apdagd(regot_ctx* ctx, regot_dproblem* prob, double reg, double tol,
+                          int max_iter, const regot_opts* opts, regot_result* res);
 /* qrot_lbfgs_dual (src/qrot_lbfgs_dual.cpp:81-126). */
 int regot_qrot_lbfgs_dual(regot_ctx* ctx, regot_dproblem* prob, double reg, double tol,
                           int max_iter, const regot_opts* opts, regot_result* res);

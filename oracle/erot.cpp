@@ -2,6 +2,7 @@
 // sinkhorn_bcd / sinkhorn_newton / sinkhorn_ssns solvers.
 // Test infrastructure only (see oracle.h). Each function cites the reference
 // file:line whose math and control flow it restates.
+#include "oracle_lbfgs.h"
 #include "oracle_util.h"
 
 namespace oracle {
@@ -616,6 +617,155 @@ int oracle_sinkhorn_bcd(const double* M, int n, int m, const double* a, const do
             h.push(f, gnorm, h.last_time() + d);
         }
         finish(p, i, gamma, h, res);
+        return 0;
+    } catch (const std::exception& e) {
+        set_err(res, e.what());
+        return 1;
+    }
+}
+
+// sinkhorn_lbfgs_dual_internal: sinkhorn_lbfgs_dual.cpp:81-126 (SinkhornDual
+// 18-79): L-BFGS on the dual objective with LBFGSParam() defaults except
+// epsilon = tol, epsilon_rel = 0, max_iterations = max_iter (101-104).
+int oracle_sinkhorn_lbfgs_dual(const double* M, int n, int m, const double* a, const double* b,
+                               double reg, double tol, int max_iter, int verbose,
+                               const oracle_opts* opts, oracle_result* res) {
+    try {
+        Problem p(M, n, m, a, b, reg);
+        oracle::lbfgs::LbfgsParam param;
+        param.epsilon = tol;
+        param.epsilon_rel = 0.0;
+        param.max_iterations = max_iter;
+        Vec gamma;
+        init_gamma(p, opts, gamma);
+        std::vector<double> T((size_t)n * m);
+        History h(res);
+        Timer timer;
+        double last_obj = std::numeric_limits<double>::infinity();
+        int it = 0;
+        oracle::lbfgs::FunGrad fg = [&](const Vec& x, Vec& g) {
+            last_obj = dual_obj_grad(p, x.data(), g.data(), T.data(), true);
+            return last_obj;
+        };
+        // SinkhornDual::iterate (58-78): objective of the last evaluation,
+        // final_grad_norm, cumulative time; prim_vals are not recorded.
+        auto iterate = [&](const Vec&, double gnorm) {
+            const double d = timer.toc();
+            h.push(last_obj, gnorm, h.last_time() + d);
+            if (verbose >= 1)
+                std::printf("iter = %d, objval = %g, ||grad|| = %g\n", it, last_obj, gnorm);
+            it++;
+            timer.tic();
+        };
+        timer.tic();
+        double fx;
+        const int niter = oracle::lbfgs::lbfgs_minimize(fg, iterate, param, gamma, fx);
+        finish(p, niter, gamma, h, res);
+        return 0;
+    } catch (const std::invalid_argument& e) {
+        set_err(res, e.what());
+        return 2;
+    } catch (const std::exception& e) {
+        set_err(res, e.what());
+        return 1;
+    }
+}
+
+// sinkhorn_apdagd_internal: sinkhorn_apdagd.cpp:14-183. Accelerated
+// primal-dual adaptive gradient descent on phi = -f over dual = -gamma, with
+// the primal plan averaged over the iterations; stops when the duality gap
+// and the marginal error of the averaged plan are both <= tol. The reported
+// dual is -dualt of the last iteration and the plan is the averaged one.
+int oracle_sinkhorn_apdagd(const double* M, int n, int m, const double* a, const double* b,
+                           double reg, double tol, int max_iter, int verbose,
+                           const oracle_opts* opts, oracle_result* res) {
+    try {
+        constexpr double L0 = 1.0;
+        constexpr int max_inner = 20;
+        Problem p(M, n, m, a, b, reg);
+        const int N = n + m - 1;
+        Vec gamma, grad(N), dual(N), dual_new(N), dualp(N), dualp_new(N), dualt(N), diff(N);
+        std::vector<double> T((size_t)n * m);
+        // averaged plan and the plan of the current dualt, row-major
+        std::vector<double> plan((size_t)n * m), plan_t((size_t)n * m);
+        History h(res);
+        init_gamma(p, opts, gamma);
+        for (int q = 0; q < N; q++) dual[q] = -gamma[q];
+        dualp = dual;
+        dualt = dual;
+        get_plan(p, gamma.data(), plan.data());
+
+        Timer timer;
+        timer.tic();
+        double f = dual_obj_grad(p, gamma.data(), grad.data(), T.data(), true);
+        double gnorm = norm(grad);
+        h.push(f, gnorm, timer.toc());
+
+        int i;
+        double L = L0, pbeta = 0.0;
+        for (i = 0; i < max_iter; i++) {
+            timer.tic();
+            L *= 0.5;
+            double ptau = 0.0, phi_new = 0.0;
+            for (int j = 0; j < max_inner; j++) {
+                const double palpha = (1.0 + std::sqrt(4.0 * L * pbeta + 1.0)) / (2.0 * L);
+                const double pbeta_new = pbeta + palpha;
+                ptau = palpha / pbeta_new;
+                for (int q = 0; q < N; q++) dualt[q] = (1.0 - ptau) * dual[q] + ptau * dualp[q];
+                for (int q = 0; q < N; q++) gamma[q] = -dualt[q];
+                f = dual_obj_grad(p, gamma.data(), grad.data(), T.data(), true);
+                const double phit = -f;
+                for (int q = 0; q < N; q++) dualp_new[q] = dualp[q] + palpha * grad[q];
+                for (int q = 0; q < N; q++)
+                    dual_new[q] = (1.0 - ptau) * dual[q] + ptau * dualp_new[q];
+                for (int q = 0; q < N; q++) gamma[q] = -dual_new[q];
+                f = dual_obj(p, gamma.data(), T.data());
+                phi_new = -f;
+                for (int q = 0; q < N; q++) diff[q] = dual_new[q] - dualt[q];
+                const double rhs = phit + dot(grad, diff) - 0.5 * L * sqnorm(diff);
+                if (verbose >= 2)
+                    std::printf("j = %d, palpha = %g, pbeta = %g, phit = %g, phi_new = %g, rhs = %g\n",
+                                j, palpha, pbeta_new, phit, phi_new, rhs);
+                if (phi_new >= rhs || j >= max_inner - 1) {
+                    pbeta = pbeta_new;
+                    dualp.swap(dualp_new);
+                    dual.swap(dual_new);
+                    break;
+                }
+                L *= 2.0;
+            }
+            // plan = (1 - ptau) plan + ptau plan(-dualt)
+            for (int q = 0; q < N; q++) gamma[q] = -dualt[q];
+            get_plan(p, gamma.data(), plan_t.data());
+            for (size_t e = 0; e < plan.size(); e++)
+                plan[e] = (1.0 - ptau) * plan[e] + ptau * plan_t[e];
+            // statistics of the averaged plan (0 * log 0 gives NaN, as in
+            // the reference's array expression)
+            double entropy = 0.0, mp = 0.0;
+            std::vector<double> ra(n, 0.0), rb(m, 0.0);
+            for (int jj = 0; jj < m; jj++)
+                for (int ii = 0; ii < n; ii++) {
+                    const double x = plan[(size_t)ii * m + jj];
+                    entropy += x * (1.0 - std::log(x));
+                    mp += p.Mij(ii, jj) * x;
+                    ra[ii] += x;
+                    rb[jj] += x;
+                }
+            const double primal_obj = mp - reg * entropy;
+            double r2 = 0.0;
+            for (int ii = 0; ii < n; ii++) r2 += (ra[ii] - a[ii]) * (ra[ii] - a[ii]);
+            for (int jj = 0; jj < m; jj++) r2 += (rb[jj] - b[jj]) * (rb[jj] - b[jj]);
+            const double mar_err = std::sqrt(r2);
+            h.push(f, mar_err, h.last_time() + timer.toc());
+            if (verbose >= 1)
+                std::printf("iter = %d, primal_obj = %g, phi_new = %g, mar_err = %g\n", i,
+                            primal_obj, phi_new, mar_err);
+            if (primal_obj - phi_new <= tol && mar_err <= tol) break;
+        }
+        res->niter = i;
+        res->hist_len = h.len;
+        std::copy(gamma.begin(), gamma.end(), res->dual);
+        if (res->plan) std::copy(plan.begin(), plan.end(), res->plan);
         return 0;
     } catch (const std::exception& e) {
         set_err(res, e.what());

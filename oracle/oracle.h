@@ -9,6 +9,7 @@
  * the reference solvers of yixuan/regot-python:
  *   src/sinkhorn_problem_bcd.cpp, src/sinkhorn_problem_obj.cpp,
  *   src/sinkhorn_result.h, src/sinkhorn_bcd.cpp, src/sinkhorn_newton.cpp,
+ *   src/sinkhorn_lbfgs_dual.cpp, src/sinkhorn_apdagd.cpp,
  *   src/sinkhorn_ssns.cpp, src/sinkhorn_problem_ls.cpp, src/sinkhorn_hess.cpp,
  *   src/sinkhorn_sparsify3.cpp, src/sinkhorn_linsolve.cpp, src/sinkhorn_cg.cpp,
  *   src/qrot_problem.cpp, src/approx_proj.h, src/qrot_result.h,
@@ -106,6 +107,14 @@ int oracle_sinkhorn_ssns(const double* M, int n, int m, const double* a,
                          const double* b, double reg, double tol, int max_iter,
                          int verbose, const oracle_opts* opts,
                          oracle_result* res);
+int oracle_sinkhorn_lbfgs_dual(const double* M, int n, int m, const double* a,
+                               const double* b, double reg, double tol,
+                               int max_iter, int verbose,
+                               const oracle_opts* opts, oracle_result* res);
+int oracle_sinkhorn_apdagd(const double* M, int n, int m, const double* a,
+                           const double* b, double reg, double tol,
+                           int max_iter, int verbose, const oracle_opts* opts,
+                           oracle_result* res);
 
 /* ---- QROT problem pieces ---- */
 double oracle_qrot_dual_obj(const double* M, int n, int m, const double* a,

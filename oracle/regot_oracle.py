@@ -164,6 +164,16 @@ def sinkhorn_ssns(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
                 _EROT_DUAL, 1, with_dens=True, plan=kwargs.get("plan", True))
 
 
+def sinkhorn_lbfgs_dual(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
+    return _run(lib().oracle_sinkhorn_lbfgs_dual, M, a, b, reg, tol, max_iter, verbose, kwargs,
+                _EROT_DUAL, 1, plan=kwargs.get("plan", True))
+
+
+def sinkhorn_apdagd(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
+    return _run(lib().oracle_sinkhorn_apdagd, M, a, b, reg, tol, max_iter, verbose, kwargs,
+                _EROT_DUAL, 1, plan=kwargs.get("plan", True))
+
+
 def qrot_lbfgs_dual(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
     return _run(lib().oracle_qrot_lbfgs_dual, M, a, b, reg, tol, max_iter, verbose, kwargs,
                 _QROT_DUAL, 0, with_prim=True, plan=kwargs.get("plan", True))

@@ -447,6 +447,8 @@ void regot_problem_destroy(regot_dproblem* P) {
 REGOT_SOLVER_ENTRY(regot_sinkhorn_bcd, sinkhorn_bcd_gpu, P->n + P->m - 1)
 REGOT_SOLVER_ENTRY(regot_sinkhorn_newton, sinkhorn_newton_gpu, P->n + P->m - 1)
 REGOT_SOLVER_ENTRY(regot_sinkhorn_ssns, sinkhorn_ssns_gpu, P->n + P->m - 1)
+REGOT_SOLVER_ENTRY(regot_sinkhorn_lbfgs_dual, sinkhorn_lbfgs_dual_gpu, P->n + P->m - 1)
+REGOT_SOLVER_ENTRY(regot_sinkhorn_apdagd, sinkhorn_apdagd_gpu, P->n + P->m - 1)
 REGOT_SOLVER_ENTRY(regot_qrot_lbfgs_dual, qrot_lbfgs_dual_gpu, P->n + P->m)
 REGOT_SOLVER_ENTRY(regot_qrot_assn, qrot_assn_gpu, P->n + P->m)
 

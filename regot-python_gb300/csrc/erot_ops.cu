@@ -82,6 +82,15 @@ __global__ void k_merge_cols(const Acc* cp, int nrb, int m, int nc, double* out)
     }
 }
 
+// out[t] = sum of the per-CTA totals of a pass, in CTA order.
+__global__ void k_sum_totals(const double* totpart, int nblocks, int nt, double* out) {
+    const int t = threadIdx.x;
+    if (t >= nt) return;
+    double acc = 0.0;
+    for (int k = 0; k < nblocks; ++k) acc += totpart[(size_t)t * nblocks + k];
+    out[t] = acc;
+}
+
 }  // namespace
 
 ErotOps::ErotOps(regot_dproblem* P, double reg, cudaStream_t st)
@@ -235,6 +244,45 @@ void ErotOps::tmatvec(const double* alpha, const double* beta, const double* xr,
     pass(OP_E_HVP, p);
     merge_rows(1, yr);
     merge_cols(1, yc);
+}
+
+void ErotOps::merge_totals(int op, int nt, double* out) {
+    k_sum_totals<<<1, 32, 0, st_>>>(buf_.totpart.get(), pass_blocks(op, mixed_, n_, m_), nt, out);
+    count_launch();
+    REGOT_CHECK_LAUNCH();
+}
+
+void ErotOps::grad_ls(const double* alpha, const double* beta, const double* dr, const double* dc,
+                      double step, double* r, double* c, double* total, double* mx) {
+    PassParams p = base_params();
+    p.ra = alpha;
+    p.cb = beta;
+    p.rd = dr;
+    p.cd = dc;
+    p.steps[0] = step;
+    p.nsteps = 1;
+    maxabs(alpha, n_, beta, m_, mx);
+    p.grid = mx;
+    pass(OP_E_GRADLS, p);
+    merge_rows(1, r);
+    merge_cols(1, c);
+    merge_totals(OP_E_GRADLS, 1, total);
+}
+
+void ErotOps::avg_plan(const double* alpha, const double* beta, void* X, double tau, bool init,
+                       double* r, double* c, double* totals, double* mx) {
+    PassParams p = base_params();
+    p.ra = alpha;
+    p.cb = beta;
+    p.xavg = X;
+    p.steps[0] = tau;
+    p.nsteps = init ? 0 : 1;
+    maxabs(alpha, n_, beta, m_, mx);
+    p.grid = mx;
+    pass(OP_E_AVG, p);
+    merge_rows(1, r);
+    merge_cols(1, c);
+    merge_totals(OP_E_AVG, 2, totals);
 }
 
 void ErotOps::plan(const double* alpha, const double* beta, double* out, double* mx) {

@@ -73,6 +73,21 @@ public:
                  double* yr, double* yc, double* maxabs_scratch);
     // plan = T(alpha, beta) (device output, row-major, stride m).
     void plan(const double* alpha, const double* beta, double* out, double* maxabs_scratch);
+    // At the trial point (alpha, beta), reached from a base point by `step`
+    // along (dr, dc): row sums r[n] and column sums c[m] of T, and
+    // total[0] = sum T e^(-step w) phi(step w), w = (dr_i + dc_j)/reg,
+    // phi(x) = e^x - 1 - x. reg * total is the objective change from the
+    // base point minus its linear part step * g'd, with no cancellation.
+    void grad_ls(const double* alpha, const double* beta, const double* dr, const double* dc,
+                 double step, double* r, double* c, double* total, double* maxabs_scratch);
+    // Averaged plan X <- (1 - tau) X + tau T(alpha, beta) (X <- T when init):
+    // X is n x m row-major in the pass's element type (FP32 mixed, FP64
+    // otherwise). Row sums r[n], column sums c[m] of the new X, and
+    // totals[0] = sum M X, totals[1] = sum X (1 - log X).
+    void avg_plan(const double* alpha, const double* beta, void* X, double tau, bool init,
+                  double* r, double* c, double* totals, double* maxabs_scratch);
+    // out[t] = sum over the CTAs of total t of the last pass `op` (t < nt).
+    void merge_totals(int op, int nt, double* out);
 
     // Merge helpers (FP64 outputs).
     void merge_rows(int nr, double* out);  // out[r*n + i]

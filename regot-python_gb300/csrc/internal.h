@@ -84,6 +84,12 @@ enum PassOp : int {
     OP_Q_COLROOT,     // cols: count and sum of y = M - ra below cb (FP64)
     OP_Q_GRADLS,      // at C + s w (w = rd_i + cd_j): rows/cols sum Dn; totals sum Dn^2,
                       // sum of 0.5 (Dn^2 - D^2) - s w D (second-order part of the change)
+    OP_E_GRADLS,      // at the trial point (ra, cb), direction (rd, cd), step s: rows/cols
+                      // sum T; total sum T e^(-s w) phi(s w), w = (rd_i + cd_j)/reg,
+                      // phi(x) = e^x - 1 - x (change from the base point, minus s g'd, / reg)
+    OP_E_AVG,         // averaged plan X <- (1 - s) X + s T (X = T when nsteps == 0), X at
+                      // xavg (TM, row-major, stride m): rows/cols sum X; totals sum M X,
+                      // sum X (1 - log X)
     OP_COUNT
 };
 
@@ -116,6 +122,7 @@ struct PassParams {
     double* totpart = nullptr;     // [NT][nblocks]
     uint32_t* bitmask = nullptr;   // [n][nslabs][LC]
     double* out = nullptr;         // plan output, row-major, stride m
+    void* xavg = nullptr;          // averaged plan (OP_E_AVG), TM, row-major, stride m
     const int* done = nullptr;     // early-exit flag (device)
     int* err = nullptr;            // set to 1 if a bounded wait gave up (device)
 };

@@ -1,11 +1,12 @@
 // L-BFGS with the Nocedal-Wright strong-Wolfe line search, restating the
-// vendored LBFGS++ (MIT) that the reference's qrot_lbfgs_dual uses:
+// vendored LBFGS++ (MIT) that the reference's qrot_lbfgs_dual and
+// sinkhorn_lbfgs_dual use:
 // LBFGSSolver::minimize (src/LBFGSpp/LBFGS.h:79-175), the two-loop recursion
 // BFGSMat::apply_Hv (src/LBFGSpp/LBFGSpp/BFGSMat.h:61-100, 276-302),
 // LineSearchNocedalWright::LineSearch (LineSearchNocedalWright.h:30-280) and
 // the defaults of LBFGSParam (Param.h:168-182). The driver runs on the host in
 // FP64; every function evaluation is one dense GPU pass (the caller's
-// callback), and all vectors have n + m entries.
+// callback). Vectors have n + m entries (QROT) or n + m - 1 (EROT).
 #pragma once
 
 #include <algorithm>

@@ -173,16 +173,20 @@ template <> struct Vec<double> {
 __host__ __device__ constexpr int op_nr(int op) {
     return op == OP_E_ROW ? 1 : op == OP_E_ROWCOL ? 1 : op == OP_E_HVP ? 1 : op == OP_E_ROWMAX ? 1
          : op == OP_Q_GRAD ? 1 : op == OP_Q_GRADMASK ? 2 : op == OP_Q_P1 ? 1 : op == OP_Q_P3 ? 3
-         : op == OP_Q_GRADLS ? 1 : 0;
+         : op == OP_Q_GRADLS ? 1 : op == OP_E_GRADLS ? 1 : op == OP_E_AVG ? 1 : 0;
 }
 __host__ __device__ constexpr int op_nc(int op) {
     return op == OP_E_COL ? 1 : op == OP_E_ROWCOL ? 1 : op == OP_E_HVP ? 1 : op == OP_E_COLMAX ? 1
          : op == OP_Q_GRAD ? 1 : op == OP_Q_GRADMASK ? 2 : op == OP_Q_P2 ? 1 : op == OP_Q_COLROOT ? 2
-         : op == OP_Q_GRADLS ? 1 : 0;
+         : op == OP_Q_GRADLS ? 1 : op == OP_E_GRADLS ? 1 : op == OP_E_AVG ? 1 : 0;
 }
 __host__ __device__ constexpr int op_nt(int op) {
     return op == OP_E_LS ? 4 : op == OP_Q_GRAD ? 1 : op == OP_Q_GRADMASK ? 1 : op == OP_Q_OBJ ? 1
-         : op == OP_Q_P3 ? 2 : op == OP_Q_GRADLS ? 2 : 0;
+         : op == OP_Q_P3 ? 2 : op == OP_Q_GRADLS ? 2 : op == OP_E_GRADLS ? 1 : op == OP_E_AVG ? 2
+         : 0;
+}
+__host__ __device__ constexpr bool op_is_erot(int op) {
+    return op <= OP_E_COLMAX || op == OP_E_GRADLS || op == OP_E_AVG;
 }
 __host__ __device__ constexpr bool op_is_max(int op) {
     return op == OP_E_ROWMAX || op == OP_E_COLMAX;
@@ -226,13 +230,13 @@ __host__ __device__ constexpr bool op_uses_cx(int op) {
 }
 __host__ __device__ constexpr bool op_uses_cx2(int op) { return op == OP_Q_P3; }
 __host__ __device__ constexpr bool op_uses_cd(int op) {
-    return op == OP_E_LS || op == OP_Q_GRADLS;
+    return op == OP_E_LS || op == OP_Q_GRADLS || op == OP_E_GRADLS;
 }
 __host__ __device__ constexpr bool op_uses_rx(int op) {
     return op == OP_E_HVP || op == OP_Q_P2 || op == OP_Q_P3;
 }
 __host__ __device__ constexpr bool op_uses_rd(int op) {
-    return op == OP_E_LS || op == OP_Q_GRADLS;
+    return op == OP_E_LS || op == OP_Q_GRADLS || op == OP_E_GRADLS;
 }
 
 // Sum (or max) of the per-lane partials of a warp's N rows (N a power of
@@ -339,7 +343,7 @@ __global__ void __launch_bounds__(kThreads, 2) dense_pass(const PassParams p) {
     constexpr int NR = op_nr(OP), NC = op_nc(OP), NT = op_nt(OP);
     constexpr int NRa = NR > 0 ? NR : 1, NCa = NC > 0 ? NC : 1, NTa = NT > 0 ? NT : 1;
     constexpr bool ISMAX = op_is_max(OP);
-    constexpr bool EROT = (OP <= OP_E_COLMAX);
+    constexpr bool EROT = op_is_erot(OP);
     constexpr int RPW = kRB / kWarps;  // rows per warp per tile (4)
     constexpr int LOGR = RPW >= 8 ? 3 : RPW >= 4 ? 2 : RPW >= 2 ? 1 : 0;
     constexpr int NS = ring_stages<OP, Acc, CW>();
@@ -444,7 +448,10 @@ __global__ void __launch_bounds__(kThreads, 2) dense_pass(const PassParams p) {
     for (int t = 0; t < 4; ++t) steps[t] = (TM)p.steps[t];
     const int nsteps = p.nsteps;
 
-    Acc tot[NTa];
+    // The averaged-plan totals are accumulated per row in the pass's type and
+    // added into FP64 here (the duality-gap test needs them to ~1e-9).
+    using TotT = typename std::conditional<OP == OP_E_AVG, double, Acc>::type;
+    TotT tot[NTa];
 #pragma unroll
     for (int t = 0; t < NTa; ++t) tot[t] = 0;
     bool ok_wait = true;
@@ -621,6 +628,8 @@ __global__ void __launch_bounds__(kThreads, 2) dense_pass(const PassParams p) {
                     }
                     double pv[VW];  // plan values of one vector (plan passes)
                     (void)pv;
+                    Acc rchunk[2] = {(Acc)0, (Acc)0};  // this row's averaged-plan totals
+                    (void)rchunk;
     #pragma unroll
                     for (int q = 0; q < (PAIRED ? 0 : LC); ++q) {
                         const TM mval = Vec<TM>::get(mv[q / VW], q % VW);
@@ -667,6 +676,33 @@ __global__ void __launch_bounds__(kThreads, 2) dense_pass(const PassParams p) {
                                     if (s2 < nsteps) tot[s2] += T * expm1_minus_x(steps[s2] * w);
                             } else if constexpr (OP == OP_E_PLAN) {
                                 plan_put<VW>(pv, q, (double)T, p.out, i, m, c0, lane);
+                            } else if constexpr (OP == OP_E_GRADLS) {
+                                racc[0] += T;
+                                cacc[0][q] += T;
+                                if (cvalid[q]) {
+                                    // T e^(-s w) is T at the base point
+                                    const TM sw = steps[0] * ((rdv + cdv[q]) * inv_reg);
+                                    TM back;
+                                    if constexpr (MIXED) back = ex2_approx(-sw * 1.44269504f);
+                                    else back = exp(-sw);
+                                    tot[0] += (T * back) * expm1_minus_x(sw);
+                                }
+                            } else if constexpr (OP == OP_E_AVG) {
+                                if (cvalid[q]) {
+                                    const int j = c0 + ((q / VW) * 32 + lane) * VW + (q % VW);
+                                    TM* X = static_cast<TM*>(p.xavg) + (long long)i * m + j;
+                                    const TM xo = nsteps > 0 ? *X : (TM)0;
+                                    const TM xn = nsteps > 0 ? ((TM)1 - steps[0]) * xo + steps[0] * T : T;
+                                    *X = xn;
+                                    racc[0] += xn;
+                                    cacc[0][q] += xn;
+                                    rchunk[0] += mval * xn;
+                                    // FP64: 0 (1 - log 0) is NaN, as in the reference's
+                                    // array expression; an FP32 zero is an underflow of a
+                                    // positive value and contributes its limit 0
+                                    if constexpr (MIXED) rchunk[1] += xn > 0.f ? xn * (1.f - logf(xn)) : 0.f;
+                                    else rchunk[1] += xn * (1.0 - log(xn));
+                                }
                             }
                         } else {
                             TM arg;
@@ -721,6 +757,10 @@ __global__ void __launch_bounds__(kThreads, 2) dense_pass(const PassParams p) {
                     }
                     if constexpr (OP == OP_Q_GRADMASK) {
                         if (lane < LC) p.bitmask[((long long)i * nslabs + slab) * LC + lane] = bits;
+                    }
+                    if constexpr (OP == OP_E_AVG) {
+                        tot[0] += (double)rchunk[0];
+                        tot[1] += (double)rchunk[1];
                     }
 
 #pragma unroll

@@ -13,6 +13,10 @@ void sinkhorn_newton_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double t
                          const regot_opts& o, regot_result* res);
 void sinkhorn_ssns_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
                        const regot_opts& o, regot_result* res);
+void sinkhorn_lbfgs_dual_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol,
+                             int max_iter, const regot_opts& o, regot_result* res);
+void sinkhorn_apdagd_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
+                         const regot_opts& o, regot_result* res);
 // sparsify_mat3 of T(gamma) (sinkhorn_sparsify3.cpp:276-405): nnz as the
 // reference counts it (kept entries including exact zeros of T) and, if mask
 // is not NULL, the stored kept entries as a row-major n x (m - 1) 0/1 mask.

@@ -36,8 +36,8 @@ import numpy as np
 from . import _lib as L
 
 __all__ = [
-    "sinkhorn_bcd", "sinkhorn_newton", "sinkhorn_ssns", "qrot_lbfgs_dual", "qrot_assn",
-    "sinkhorn_result", "qrot_result", "Problem",
+    "sinkhorn_bcd", "sinkhorn_newton", "sinkhorn_ssns", "sinkhorn_lbfgs_dual", "sinkhorn_apdagd",
+    "qrot_lbfgs_dual", "qrot_assn", "sinkhorn_result", "qrot_result", "Problem",
 ]
 
 
@@ -234,6 +234,12 @@ class Problem:
     def sinkhorn_ssns(self, reg, tol=1e-6, max_iter=1000, verbose=0, **kw):
         return self._solve("regot_sinkhorn_ssns", reg, tol, max_iter, verbose, kw, False)
 
+    def sinkhorn_lbfgs_dual(self, reg, tol=1e-6, max_iter=1000, verbose=0, **kw):
+        return self._solve("regot_sinkhorn_lbfgs_dual", reg, tol, max_iter, verbose, kw, False)
+
+    def sinkhorn_apdagd(self, reg, tol=1e-6, max_iter=1000, verbose=0, **kw):
+        return self._solve("regot_sinkhorn_apdagd", reg, tol, max_iter, verbose, kw, False)
+
     def qrot_lbfgs_dual(self, reg, tol=1e-6, max_iter=1000, verbose=0, **kw):
         return self._solve("regot_qrot_lbfgs_dual", reg, tol, max_iter, verbose, kw, True)
 
@@ -352,6 +358,17 @@ def sinkhorn_newton(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
 def sinkhorn_ssns(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
     """Safe and sparse Newton for EROT; reference src/sinkhorn_ssns.cpp:16-234."""
     return _solve("sinkhorn_ssns", M, a, b, reg, tol, max_iter, verbose, kwargs)
+
+
+def sinkhorn_lbfgs_dual(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
+    """L-BFGS on the EROT dual; reference src/sinkhorn_lbfgs_dual.cpp:81-126."""
+    return _solve("sinkhorn_lbfgs_dual", M, a, b, reg, tol, max_iter, verbose, kwargs)
+
+
+def sinkhorn_apdagd(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
+    """Accelerated primal-dual adaptive gradient descent for EROT; reference
+    src/sinkhorn_apdagd.cpp:14-183. The plan is the averaged primal plan."""
+    return _solve("sinkhorn_apdagd", M, a, b, reg, tol, max_iter, verbose, kwargs)
 
 
 def qrot_lbfgs_dual(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):

@@ -83,8 +83,8 @@ EXPORTS = [
     "regot_opts_init", "regot_ctx_create", "regot_ctx_destroy", "regot_ctx_last_error",
     "regot_ctx_set_stream", "regot_ctx_own_stream", "regot_ctx_kernel_launches", "regot_problem_create",
     "regot_problem_destroy", "regot_sinkhorn_bcd", "regot_sinkhorn_newton",
-    "regot_sinkhorn_ssns", "regot_qrot_lbfgs_dual", "regot_qrot_assn",
-    "regot_erot_optimal_beta", "regot_erot_optimal_alpha", "regot_erot_dual_obj_grad",
+    "regot_sinkhorn_ssns", "regot_sinkhorn_lbfgs_dual", "regot_sinkhorn_apdagd",
+    "regot_qrot_lbfgs_dual", "regot_qrot_assn", "regot_erot_optimal_beta", "regot_erot_optimal_alpha", "regot_erot_dual_obj_grad",
     "regot_erot_hvp", "regot_erot_plan", "regot_erot_sparsify", "regot_qrot_dual_obj_grad",
     "regot_qrot_optimal_beta",
     "regot_qrot_primal_val", "regot_qrot_plan", "regot_time_pass",
@@ -123,6 +123,7 @@ def load() -> C.CDLL:
         lib.regot_problem_destroy.argtypes = [vp]
         lib.regot_problem_destroy.restype = None
         for name in ("regot_sinkhorn_bcd", "regot_sinkhorn_newton", "regot_sinkhorn_ssns",
+                     "regot_sinkhorn_lbfgs_dual", "regot_sinkhorn_apdagd",
                      "regot_qrot_lbfgs_dual", "regot_qrot_assn"):
             f = getattr(lib, name)
             f.argtypes = [vp, vp, C.c_double, C.c_double, C.c_int, C.POINTER(Opts),

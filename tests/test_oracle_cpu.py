@@ -114,6 +114,39 @@ def test_erot_solvers_agree_with_generic_minimiser():
         np.testing.assert_allclose(r.plan, _erot_dual_np(M, a, b, reg, r.dual)[2], rtol=1e-12)
 
 
+def test_erot_lbfgs_dual_matches_generic_minimiser():
+    # sinkhorn_lbfgs_dual minimises the same dual as BCD: same optimum as an
+    # independent minimiser of the numpy dual.
+    M, a, b = erot_points(40, 30, seed=8, dtype=np.float64)
+    reg = 0.05
+    n, m = M.shape
+    fun = lambda x: _erot_dual_np(M, a, b, reg, x)[:2]  # noqa: E731
+    res = minimize(fun, np.zeros(n + m - 1), jac=True, method="L-BFGS-B",
+                   options={"maxiter": 20000, "gtol": 1e-12, "ftol": 1e-15})
+    r = O.sinkhorn_lbfgs_dual(M, a, b, reg, tol=1e-8, max_iter=1000)
+    assert r.mar_errs[-1] < 1e-8 and len(r.mar_errs) == r.niter + 1
+    np.testing.assert_allclose(r.obj_vals[-1], res.fun, rtol=1e-9)
+    f, g, T = _erot_dual_np(M, a, b, reg, r.dual)
+    np.testing.assert_allclose(r.mar_errs[-1], np.linalg.norm(g), rtol=1e-9)
+    np.testing.assert_allclose(r.plan, T, rtol=1e-12)
+
+
+def test_erot_apdagd_averaged_plan_and_gap():
+    # APDAGD's plan is the running average of T along the extrapolated
+    # points; its marginal error falls and its duality gap closes.
+    M, a, b = erot_points(60, 50, seed=11, dtype=np.float64)
+    reg = 0.1
+    r = O.sinkhorn_apdagd(M, a, b, reg, tol=1e-4, max_iter=2000)
+    assert r.niter < 2000 and r.mar_errs[-1] <= 1e-4
+    P = r.plan
+    mar = np.sqrt(((P.sum(1) - a) ** 2).sum() + ((P.sum(0) - b) ** 2).sum())
+    np.testing.assert_allclose(r.mar_errs[-1], mar, rtol=1e-10)
+    primal = (M * P).sum() - reg * (P * (1 - np.log(P))).sum()
+    assert primal - (-r.obj_vals[-1]) <= 1e-4
+    rb = O.sinkhorn_bcd(M, a, b, reg, tol=1e-11, max_iter=20000)
+    np.testing.assert_allclose(P, rb.plan, rtol=0, atol=2e-3 * rb.plan.max())
+
+
 def test_erot_bcd_objective_is_monotone():
     M, a, b = erot_points(60, 50, seed=6, dtype=np.float64)
     r = O.sinkhorn_bcd(M, a, b, 0.05, tol=1e-10, max_iter=300)
