@@ -163,6 +163,26 @@ int regot_qrot_assn(regot_ctx* ctx, regot_dproblem* prob, double reg, double tol
 
 /* ---- Pass-level entry points (host vectors in and out) ---- */
 
+/* ---- Derivatives of EROT solves (no reference counterpart) ---- */
+
+/* Solve H x = rhs with the exact dual Hessian at gamma, the matrix that
+ * sinkhorn_newton factors (src/sinkhorn_newton.cpp:91-92; H from
+ * src/sinkhorn_problem_obj.cpp:396-418), by Jacobi-preconditioned CG to
+ * ||H x - rhs|| < tol ||rhs|| (max_iter <= 0: 2 (n + m - 1) steps). Host
+ * vectors of n + m - 1 entries; *iters receives the CG steps taken. */
+int regot_erot_hess_solve(regot_ctx* ctx, regot_dproblem* prob, double reg, const double* gamma,
+                          const double* rhs, double tol, int max_iter, double* x, int* iters);
+/* Weighted plan contraction without an n x m intermediate:
+ *   G_ij = T_ij                               (u == NULL), or
+ *   G_ij = T_ij (u_i + u_{n+j} - W_ij) / reg   (u given; W may be NULL),
+ *   rows_i = sum_j G_ij (rows may be NULL), Z = G Y (Y m x d, Z n x d, row-major),
+ * with T = exp((alpha (+) [beta~, 0] - M)/reg). gamma and u have n + m - 1
+ * entries, W is n x m row-major. mem (REGOT_MEM_HOST / DEVICE) applies to
+ * every array argument. */
+int regot_erot_tyy(regot_ctx* ctx, regot_dproblem* prob, double reg, const double* gamma,
+                   const double* u, const double* W, const double* Y, int d, double* rows,
+                   double* Z, int mem);
+
 /* Problem::optimal_beta / optimal_alpha (src/sinkhorn_problem_bcd.cpp:149-201). */
 int regot_erot_optimal_beta(regot_ctx* ctx, regot_dproblem* prob, double reg,
                             const double* alpha, double* beta);

@@ -544,6 +544,67 @@ int regot_erot_hvp(regot_ctx* ctx, regot_dproblem* P, double reg, const double* 
     });
 }
 
+int regot_erot_hess_solve(regot_ctx* ctx, regot_dproblem* P, double reg, const double* gamma,
+                          const double* rhs, double tol, int max_iter, double* x, int* iters) {
+    return guarded(ctx, [&] {
+        require(P && gamma && rhs && x, "NULL argument");
+        require(reg > 0.0, "reg must be positive");
+        require(tol >= 0.0, "tol must be non-negative");
+        erot_hess_solve_gpu(ctx, P, reg, gamma, rhs, tol, max_iter, x, iters);
+    });
+}
+
+int regot_erot_tyy(regot_ctx* ctx, regot_dproblem* P, double reg, const double* gamma,
+                   const double* u, const double* W, const double* Y, int d, double* rows,
+                   double* Z, int mem) {
+    return guarded(ctx, [&] {
+        require(P && gamma, "NULL argument");
+        require(reg > 0.0, "reg must be positive");
+        require(d >= 0 && (d == 0 || (Y && Z)), "Y and Z are required when d > 0");
+        require(mem == REGOT_MEM_HOST || mem == REGOT_MEM_DEVICE, "unknown memory kind");
+        cudaStream_t st = ctx->stream;
+        const int n = P->n, m = P->m;
+        const size_t nm1 = (size_t)(n + m - 1) * sizeof(double);
+        // duals and adjoint with beta_m = 0 appended, on the device
+        DBuf<double> g(n + m, st), uu(u ? n + m : 0, st);
+        g.zero();
+        const cudaMemcpyKind kin = mem == REGOT_MEM_HOST ? cudaMemcpyHostToDevice
+                                                         : cudaMemcpyDeviceToDevice;
+        REGOT_CUDA(cudaMemcpyAsync(g.get(), gamma, nm1, kin, st));
+        if (u) {
+            uu.zero();
+            REGOT_CUDA(cudaMemcpyAsync(uu.get(), u, nm1, kin, st));
+        }
+        const double *dW = W, *dY = Y;
+        DBuf<double> hW, hY, hZ, hR;
+        double *dZ = Z, *dR = rows;
+        if (mem == REGOT_MEM_HOST) {
+            if (W) {
+                hW.alloc((size_t)n * m, st);
+                h2d(hW.get(), W, (size_t)n * m * sizeof(double), st);
+                dW = hW.get();
+            }
+            if (d > 0) {
+                hY.alloc((size_t)m * d, st);
+                h2d(hY.get(), Y, (size_t)m * d * sizeof(double), st);
+                dY = hY.get();
+                hZ.alloc((size_t)n * d, st);
+                dZ = hZ.get();
+            }
+            if (rows) {
+                hR.alloc(n, st);
+                dR = hR.get();
+            }
+        }
+        erot_tyy_gpu(ctx, P, reg, g.get(), u ? uu.get() : nullptr, dW, dY, d, dR, dZ);
+        if (mem == REGOT_MEM_HOST) {
+            if (d > 0) d2h(Z, dZ, (size_t)n * d * sizeof(double), st);
+            if (rows) d2h(rows, dR, (size_t)n * sizeof(double), st);
+        }
+        sync(st);
+    });
+}
+
 int regot_erot_plan(regot_ctx* ctx, regot_dproblem* P, double reg, const double* gamma,
                     double* plan, int plan_mem) {
     return guarded(ctx, [&] {

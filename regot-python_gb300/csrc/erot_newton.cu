@@ -90,13 +90,15 @@ __global__ void k_newton_grad(const Acc* rp, int nslabs, const Acc* cp, int nrb,
     }
 }
 
-// CG set-up for H x = -g: x = 0, r = -g, z = r / diag(H), p = z.
-__global__ void k_cg_init(int N, const double* g, const double* hdiag, double tol, double* x,
-                          double* r, double* z, double* p, double* parts, NewtonState* st) {
+// CG set-up for H x = sign v (the Newton system: v = g, sign = -1): x = 0,
+// r = sign v, z = r / diag(H), p = z.
+__global__ void k_cg_init(int N, const double* g, double sign, const double* hdiag, double tol,
+                          double* x, double* r, double* z, double* p, double* parts,
+                          NewtonState* st) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     double v[2] = {0.0, 0.0};
     if (t < N) {
-        const double ri = -g[t];
+        const double ri = sign * g[t];
         const double zi = ri / hdiag[t];
         x[t] = 0.0;
         r[t] = ri;
@@ -368,8 +370,8 @@ void sinkhorn_newton_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double t
         if (hs.gnorm < tol || !std::isfinite(hs.f)) break;  // sinkhorn_newton.cpp:87-88
 
         // Newton direction: H x = -g by preconditioned CG.
-        k_cg_init<<<gv, kVecThreads, 0, st>>>(N, g.get(), hdiag.get(), cg_tol, x.get(), r.get(),
-                                              z.get(), pv.get(), parts.get(), S);
+        k_cg_init<<<gv, kVecThreads, 0, st>>>(N, g.get(), -1.0, hdiag.get(), cg_tol, x.get(),
+                                              r.get(), z.get(), pv.get(), parts.get(), S);
         count_launch();
         ops.maxabs(gamma.get(), N, pv.get(), N, &S->maxabs);
         int batch = 8;
@@ -429,6 +431,87 @@ void sinkhorn_newton_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double t
     cudaGraphDestroy(graph);
     finish_erot_result(ops, gamma.get(), hobj, hmar, htime, nullptr, hist_len, hist_cap, i,
                        passes, o, res);
+}
+
+// H x = rhs for the exact dual Hessian at gamma (the matrix the reference
+// factors in sinkhorn_newton.cpp:91-92), by the Jacobi-preconditioned CG of
+// the Newton solver above: one HVP pass per step, to
+// ||H x - rhs|| < tol ||rhs|| or max_iter steps. Vectors have n + m - 1
+// entries (host). Used for implicit derivatives of a solve.
+void erot_hess_solve_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, const double* gamma_h,
+                         const double* rhs_h, double tol, int max_iter, double* x_h, int* iters) {
+    cudaStream_t st = ctx->stream;
+    const int n = P->n, m = P->m, N = n + m;
+    const bool mixed = P->prec == REGOT_PREC_MIXED;
+    ErotOps ops(P, reg, st);
+    const PassShape sh = ops.buf().shape;
+    DBuf<double> gamma(N, st), g(N, st), hdiag(N, st), x(N, st), r(N, st), z(N, st), pv(N, st),
+        y(N, st), rhs(N, st);
+    DBuf<double> parts(4 * (size_t)cdiv(N, kVecThreads), st);
+    DBuf<NewtonState> dst(1, st);
+    NewtonState h0{};
+    h0.cg_max = max_iter > 0 ? max_iter : 2 * (n + m - 1);
+    h2d(dst.get(), &h0, sizeof(h0), st);
+    NewtonState* S = dst.get();
+    const int gv = cdiv(N, kVecThreads);
+    {
+        std::vector<double> h(N, 0.0);
+        std::copy(gamma_h, gamma_h + n + m - 1, h.begin());
+        h2d(gamma.get(), h.data(), N * sizeof(double), st);
+        std::copy(rhs_h, rhs_h + n + m - 1, h.begin());
+        h[N - 1] = 0.0;
+        h2d(rhs.get(), h.data(), N * sizeof(double), st);
+    }
+    ops.maxabs(gamma.get(), N, nullptr, 0, &S->maxabs);
+    PassParams pg = ops.base_params();
+    pg.ra = gamma.get();
+    pg.cb = gamma.get() + n;
+    pg.grid = &S->maxabs;
+    ops.pass(OP_E_ROWCOL, pg);  // diag(H) from the row and column sums
+    if (mixed)
+        k_newton_grad<float><<<gv, kVecThreads, 0, st>>>(
+            (const float*)ops.buf().rowpart.get(), sh.nslabs,
+            (const float*)ops.buf().colpart.get(), sh.nrb, n, m, gamma.get(), P->a, P->b, reg,
+            g.get(), hdiag.get(), parts.get(), S);
+    else
+        k_newton_grad<double><<<gv, kVecThreads, 0, st>>>(
+            (const double*)ops.buf().rowpart.get(), sh.nslabs,
+            (const double*)ops.buf().colpart.get(), sh.nrb, n, m, gamma.get(), P->a, P->b, reg,
+            g.get(), hdiag.get(), parts.get(), S);
+    k_cg_init<<<gv, kVecThreads, 0, st>>>(N, rhs.get(), 1.0, hdiag.get(), tol, x.get(), r.get(),
+                                          z.get(), pv.get(), parts.get(), S);
+    count_launch(2);
+    REGOT_CHECK_LAUNCH();
+    ops.maxabs(gamma.get(), N, pv.get(), N, &S->maxabs);
+    PassParams ph = pg;
+    ph.rx = pv.get();
+    ph.cx = pv.get() + n;
+    ph.done = &S->cg_done;
+    NewtonState hs{};
+    for (;;) {
+        read_small(ctx, &hs, S, sizeof(hs), st);
+        if (hs.cg_done) break;
+        for (int q = 0; q < 8; ++q) {  // steps between state reads
+            ops.pass(OP_E_HVP, ph);
+            if (mixed)
+                k_cg_a<float><<<gv, kVecThreads, 0, st>>>(
+                    (const float*)ops.buf().rowpart.get(), sh.nslabs,
+                    (const float*)ops.buf().colpart.get(), sh.nrb, n, m, hdiag.get(), pv.get(),
+                    reg, y.get(), parts.get(), S);
+            else
+                k_cg_a<double><<<gv, kVecThreads, 0, st>>>(
+                    (const double*)ops.buf().rowpart.get(), sh.nslabs,
+                    (const double*)ops.buf().colpart.get(), sh.nrb, n, m, hdiag.get(), pv.get(),
+                    reg, y.get(), parts.get(), S);
+            k_cg_b<<<gv, kVecThreads, 0, st>>>(N, pv.get(), y.get(), hdiag.get(), x.get(), r.get(),
+                                                 z.get(), parts.get(), S);
+            k_cg_c<<<gv, kVecThreads, 0, st>>>(N, z.get(), pv.get(), S);
+            count_launch(3);
+        }
+    }
+    read_small(ctx, x_h, x.get(), (size_t)(n + m - 1) * sizeof(double), st);
+    if (iters) *iters = hs.cg_it;
+    ops.check_err();
 }
 
 }  // namespace regot

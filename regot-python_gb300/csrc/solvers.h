@@ -22,6 +22,14 @@ void sinkhorn_apdagd_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double t
 // is not NULL, the stored kept entries as a row-major n x (m - 1) 0/1 mask.
 void erot_sparsify_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, const double* gamma,
                        double delta, double density_hint, long long* nnz, int* mask);
+// Z = G Y, rows = G 1 with G = T or T o (u_i + u_j - W_ij) / reg (erot_grad.cu);
+// all pointers device: gamma and u n + m (last 0), W n x m, Y m x d, Z n x d.
+void erot_tyy_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, const double* d_gamma,
+                  const double* d_u, const double* d_W, const double* d_Y, int d, double* d_rows,
+                  double* d_Z);
+// H x = rhs with the exact dual Hessian at gamma (host vectors, n + m - 1).
+void erot_hess_solve_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, const double* gamma,
+                         const double* rhs, double tol, int max_iter, double* x, int* iters);
 void qrot_lbfgs_dual_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
                          const regot_opts& o, regot_result* res);
 void qrot_assn_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,

@@ -78,6 +78,14 @@ def _is_torch_cuda(x) -> bool:
     return t.__module__.startswith("torch") and getattr(x, "is_cuda", False)
 
 
+def _check_cuda_f64(t, shape, name):
+    import torch
+
+    if not (_is_torch_cuda(t) and t.dtype == torch.float64 and t.is_contiguous()
+            and tuple(t.shape) == tuple(shape)):
+        raise ValueError(f"{name} must be a contiguous float64 CUDA tensor of shape {shape}")
+
+
 def _precision_code(precision, dtype) -> int:
     if precision is None:
         return L.REGOT_PREC_FP64 if dtype == np.float64 else L.REGOT_PREC_MIXED
@@ -285,13 +293,82 @@ class Problem:
             y.ctypes.data))
         return y
 
-    def erot_plan(self, reg, gamma):
+    def erot_plan(self, reg, gamma, out=None):
+        """T(gamma) as an n x m FP64 array (sinkhorn_result.h:32-50); with
+        `out` a contiguous float64 CUDA tensor of that shape, written there."""
         gamma = self._vec(gamma, self.n + self.m - 1)
+        if out is not None:
+            import torch
+
+            _check_cuda_f64(out, (self.n, self.m), "out")
+            torch.cuda.current_stream(out.device).synchronize()
+            self.ctx.check(self._lib.regot_erot_plan(
+                self.ctx.handle, self.handle, float(reg), gamma.ctypes.data, out.data_ptr(),
+                L.REGOT_MEM_DEVICE))
+            return out
         P = L.host_empty((self.n, self.m))
         self.ctx.check(self._lib.regot_erot_plan(
             self.ctx.handle, self.handle, float(reg), gamma.ctypes.data, P.ctypes.data,
             L.REGOT_MEM_HOST))
         return P
+
+    def erot_hess_solve(self, reg, gamma, rhs, tol=1e-10, max_iter=0):
+        """x with H x = rhs for the exact dual Hessian at gamma (the Newton
+        system of sinkhorn_newton.cpp:91-92), by preconditioned CG; returns
+        (x, CG steps)."""
+        gamma = self._vec(gamma, self.n + self.m - 1)
+        rhs = self._vec(rhs, self.n + self.m - 1)
+        x = np.zeros(self.n + self.m - 1)
+        it = C.c_int(0)
+        self.ctx.check(self._lib.regot_erot_hess_solve(
+            self.ctx.handle, self.handle, float(reg), gamma.ctypes.data, rhs.ctypes.data,
+            float(tol), int(max_iter), x.ctypes.data, C.byref(it)))
+        return x, int(it.value)
+
+    def erot_tyy(self, reg, gamma, Y, u=None, W=None):
+        """(rows, Z): rows = G 1 and Z = G Y for G = T(gamma), or
+        G = T o (u_i + u_j - W_ij) / reg when the adjoint u is given. numpy
+        arguments run through host memory; float64 CUDA tensors (gamma, u,
+        W, Y) stay on the device and the results are CUDA tensors."""
+        n, m = self.n, self.m
+        if _is_torch_cuda(Y):
+            import torch
+
+            d = int(Y.shape[1])
+            _check_cuda_f64(Y, (m, d), "Y")
+            for name, t, shape in (("gamma", gamma, (n + m - 1,)), ("u", u, (n + m - 1,)),
+                                   ("W", W, (n, m))):
+                if t is not None:
+                    _check_cuda_f64(t, shape, name)
+            rows = torch.empty(n, dtype=torch.float64, device=Y.device)
+            Z = torch.empty((n, d), dtype=torch.float64, device=Y.device)
+            torch.cuda.current_stream(Y.device).synchronize()
+            self.ctx.check(self._lib.regot_erot_tyy(
+                self.ctx.handle, self.handle, float(reg), gamma.data_ptr(),
+                u.data_ptr() if u is not None else None, W.data_ptr() if W is not None else None,
+                Y.data_ptr(), d, rows.data_ptr(), Z.data_ptr(), L.REGOT_MEM_DEVICE))
+            return rows, Z
+        gamma = self._vec(gamma, n + m - 1)
+        Y = np.ascontiguousarray(np.asarray(Y, dtype=np.float64))
+        if Y.ndim != 2 or Y.shape[0] != m:
+            raise ValueError(f"Y must be a {m} x d matrix")
+        d = Y.shape[1]
+        keep = []
+        if u is not None:
+            u = self._vec(u, n + m - 1)
+            keep.append(u)
+        if W is not None:
+            W = np.ascontiguousarray(np.asarray(W, dtype=np.float64))
+            if W.shape != (n, m):
+                raise ValueError(f"W must be {n} x {m}")
+            keep.append(W)
+        rows = np.zeros(n)
+        Z = np.zeros((n, d))
+        self.ctx.check(self._lib.regot_erot_tyy(
+            self.ctx.handle, self.handle, float(reg), gamma.ctypes.data,
+            u.ctypes.data if u is not None else None, W.ctypes.data if W is not None else None,
+            Y.ctypes.data, d, rows.ctypes.data, Z.ctypes.data, L.REGOT_MEM_HOST))
+        return rows, Z
 
     def erot_sparsify(self, reg, gamma, delta, density_hint, mask=True):
         """sparsify_mat3 of T(gamma) (sinkhorn_sparsify3.cpp:276-405): returns

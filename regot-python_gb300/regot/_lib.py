@@ -85,7 +85,8 @@ EXPORTS = [
     "regot_problem_destroy", "regot_sinkhorn_bcd", "regot_sinkhorn_newton",
     "regot_sinkhorn_ssns", "regot_sinkhorn_lbfgs_dual", "regot_sinkhorn_apdagd",
     "regot_qrot_lbfgs_dual", "regot_qrot_assn", "regot_erot_optimal_beta", "regot_erot_optimal_alpha", "regot_erot_dual_obj_grad",
-    "regot_erot_hvp", "regot_erot_plan", "regot_erot_sparsify", "regot_qrot_dual_obj_grad",
+    "regot_erot_hvp", "regot_erot_plan", "regot_erot_sparsify", "regot_erot_hess_solve",
+    "regot_erot_tyy", "regot_qrot_dual_obj_grad",
     "regot_qrot_optimal_beta",
     "regot_qrot_primal_val", "regot_qrot_plan", "regot_time_pass",
     "regot_erot_dual_obj_grad_noalloc", "regot_host_alloc", "regot_host_free",
@@ -140,6 +141,10 @@ def load() -> C.CDLL:
         lib.regot_qrot_primal_val.argtypes = [vp, vp, C.c_double, vp, vp]
         lib.regot_qrot_plan.argtypes = [vp, vp, C.c_double, vp, vp, C.c_int]
         lib.regot_time_pass.argtypes = [vp, vp, C.c_int, C.c_double, C.c_int]
+        lib.regot_erot_hess_solve.argtypes = [vp, vp, C.c_double, vp, vp, C.c_double, C.c_int,
+                                              vp, C.POINTER(C.c_int)]
+        lib.regot_erot_tyy.argtypes = [vp, vp, C.c_double, vp, vp, vp, vp, C.c_int, vp, vp,
+                                       C.c_int]
         lib.regot_erot_dual_obj_grad_noalloc.argtypes = [
             vp, C.c_longlong, C.c_int, C.c_int, vp, vp, vp, C.c_double, vp, vp, vp]
         lib.regot_host_alloc.argtypes = [C.c_size_t, C.POINTER(vp)]
