@@ -163,6 +163,51 @@ int regot_qrot_assn(regot_ctx* ctx, regot_dproblem* prob, double reg, double tol
 
 /* ---- Pass-level entry points (host vectors in and out) ---- */
 
+/* ---- Batched EROT (no reference counterpart: the reference solves one
+ * problem per call) ---- */
+
+/* `count` independent problems with squared-Euclidean costs computed on the
+ * fly from point clouds: M_ij = s_p sum_k (x_ik - y_jk)^2 in FP32, problem p
+ * with n_p rows, m_p columns, d_p <= REGOT_BATCH_MAX_DIM dimensions and cost
+ * scale s_p (NULL: 1). Points and marginals are concatenated over the
+ * problems: x holds sum n_p d_p floats (problem p's n_p x d_p row-major block
+ * after those of problems < p), y likewise, a sum n_p and b sum m_p doubles.
+ * Sizes and scales are host arrays; `mem` says where x, y, a and b live. */
+#define REGOT_BATCH_MAX_DIM 16
+typedef struct {
+    int count;
+    const int* n;
+    const int* m;
+    const int* d;
+    const double* cost_scale;
+    const float* x;
+    const float* y;
+    const double* a;
+    const double* b;
+    int mem;
+} regot_batch_desc;
+
+/* Results, host buffers: duals concatenated like a and b, gauge-fixed per
+ * problem as sinkhorn_bcd returns them (alpha + beta_m, beta - beta_m, so
+ * every problem's last beta is 0); per-problem iteration counts and final
+ * marginal errors. */
+typedef struct {
+    double* alpha;
+    double* beta;
+    int* niter;
+    double* mar_err;
+    long long sweeps;   /* out: sweeps run by the batch (the slowest problem) */
+    double solve_ms;    /* out: device time of the solve */
+} regot_batch_result;
+
+/* sinkhorn_bcd (src/sinkhorn_bcd.cpp:14-124) on every problem of the batch
+ * at once: one row and one column log-sum-exp kernel per sweep over all
+ * problems still running, each problem stopping at its own iteration with
+ * the reference's test (marginal error < tol, or max_iter). The sweeps run
+ * as a device-side loop. */
+int regot_erot_solve_batched(regot_ctx* ctx, const regot_batch_desc* desc, double reg, double tol,
+                             int max_iter, regot_batch_result* res);
+
 /* ---- Derivatives of EROT solves (no reference counterpart) ---- */
 
 /* Solve H x = rhs with the exact dual Hessian at gamma, the matrix that

@@ -544,6 +544,22 @@ int regot_erot_hvp(regot_ctx* ctx, regot_dproblem* P, double reg, const double* 
     });
 }
 
+int regot_erot_solve_batched(regot_ctx* ctx, const regot_batch_desc* desc, double reg, double tol,
+                             int max_iter, regot_batch_result* res) {
+    return guarded(ctx, [&] {
+        require(desc && res, "NULL argument");
+        require(desc->count > 0, "the batch is empty");
+        require(desc->n && desc->m && desc->d && desc->x && desc->y && desc->a && desc->b,
+                "NULL array in the batch description");
+        require(desc->mem == REGOT_MEM_HOST || desc->mem == REGOT_MEM_DEVICE,
+                "unknown memory kind");
+        require(std::isfinite(reg) && reg > 0.0, "reg must be a positive finite number");
+        require(!std::isnan(tol), "tol must not be NaN");
+        require(max_iter >= 0, "max_iter must be non-negative");
+        erot_solve_batched_gpu(ctx, desc, reg, tol, max_iter, res);
+    });
+}
+
 int regot_erot_hess_solve(regot_ctx* ctx, regot_dproblem* P, double reg, const double* gamma,
                           const double* rhs, double tol, int max_iter, double* x, int* iters) {
     return guarded(ctx, [&] {

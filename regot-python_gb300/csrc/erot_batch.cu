@@ -1,0 +1,642 @@
+// Batched sinkhorn_bcd: many independent EROT problems with squared-
+// Euclidean costs computed on the fly, solved together (the reference solves
+// one problem per call; its BCD is src/sinkhorn_bcd.cpp:14-124).
+//
+// Layout: the problems' points, marginals and duals are concatenated; per-
+// problem offsets locate them. A problem is assigned a dimension class
+// DP in {4, 8, 16} (d rounded up), its points are zero-padded to DP in
+// registers and shared memory, and each class has its own row and column
+// kernels, so a 3-D problem does not pay for 16 dimensions.
+//
+// One sweep = row kernels (one CTA per 32 rows of a problem: every CTA sees
+// whole rows, so the new alpha and the row sums of the iterate come out of
+// it directly), a finalize kernel (one warp per problem: marginal error,
+// stopping test, per-problem done mask), and column kernels (one CTA per 32
+// columns, new beta in place). Each element costs DP subtractions and FMAs
+// for the distance, one FMA for the exponent and one ex2: the sweep is bound
+// by FP32 issue and the SFU, not by memory (nothing n x m is stored).
+//
+// Log-sum-exp: each lane keeps a running (max, scaled sum) in base 2, so no
+// anchor has to be right in advance (the first sweep starts from alpha = 0,
+// where a row far from every column would underflow a fixed anchor); the
+// exponent is ((hi_i + hi_j) - M_ij) k + (lo_i + lo_j) k with the duals split
+// on a common FP32 grid as in the dense passes, so hi_i + hi_j is exact.
+//
+// The sweeps run as a device-side loop (a conditional WHILE graph node whose
+// body is two sweeps and a loop kernel): it continues while a problem is
+// running, no dual has left the split grid, and fewer than max_iter / 2 + 3
+// bodies have run.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "device_util.cuh"
+#include "solvers.h"
+
+namespace regot {
+
+namespace {
+
+constexpr int kBWarps = 8;
+constexpr int kBPer = 4;                    // rows (columns) per warp
+constexpr int kBItems = kBWarps * kBPer;    // rows (columns) per CTA
+constexpr int kBTile = 256;                 // columns (rows) staged per tile
+constexpr int kBClasses = 3;
+constexpr int kBClassDim[kBClasses] = {4, 8, 16};
+
+struct BatchDev {
+    const int* n;
+    const int* m;
+    const int* d;
+    const float* scale;
+    const long long* xo;  // offsets of the points of problem p (floats)
+    const long long* yo;
+    const int* ro;        // offsets into the concatenated row / column vectors
+    const int* co;
+    const int* rbo;       // offsets of the problem's row blocks (partials)
+    const float* X;
+    const float* Y;
+    const double* a;
+    const double* loga;
+    const double* logb;
+};
+
+struct BatchState {
+    int active;     // problems still running
+    int regrid;     // a dual reached the bound of the split grid
+    int loops;
+    int loop_cap;
+    double maxabs;  // max |dual| for the grid
+    double g, inv_g, bound;
+};
+
+__device__ __forceinline__ float bex2(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// Running log-sum-exp in base 2: sum 2^z = 2^mx * s.
+__device__ __forceinline__ void lse_add(float& mx, float& s, float z) {
+    if (z > mx) {
+        s = fmaf(s, bex2(mx - z), 1.f);
+        mx = z;
+    } else {
+        s += bex2(z - mx);
+    }
+}
+
+__device__ __forceinline__ void lse_merge(float& mx, float& s, float m2, float s2) {
+    const float m = fmaxf(mx, m2);
+    s = (m == -INFINITY) ? 0.f : s * bex2(mx - m) + s2 * bex2(m2 - m);
+    mx = m;
+}
+
+// Cost of one pair, identical in the row and column kernels.
+template <int DP>
+__device__ __forceinline__ float bcost(const float (&x)[DP], const float* y, float sc) {
+    float s = 0.f;
+#pragma unroll
+    for (int k = 0; k < DP; ++k) {
+        const float t = x[k] - y[k];
+        s = fmaf(t, t, s);
+    }
+    return s * sc;
+}
+
+__device__ __forceinline__ float2 bsplit(double v, const BatchState* st, int* regrid) {
+    if (!(fabs(v) < st->bound)) atomicOr(regrid, 1);
+    const double h = rint(v * st->inv_g) * st->g;
+    return make_float2((float)h, (float)(v - h));
+}
+
+
+// Row half-sweep of iterate k for the row blocks `items` (problem, block):
+// S_i = sum_j exp((alpha_i + beta_j - M_ij)/reg) at (alpha_k, beta_k), the
+// new alpha_i = alpha_i + reg (log a_i - log S_i) (sinkhorn_problem_bcd.cpp:
+// 177-201 with the current alpha as shift) with its split, and the block's
+// sum of (S_i - a_i)^2 for the marginal error.
+template <int DP>
+__global__ void __launch_bounds__(kBWarps * 32) k_brow(
+    const BatchDev B, const int2* __restrict__ items, const float2* __restrict__ as_cur,
+    const float2* __restrict__ bs, const double* __restrict__ alpha_cur, double* alpha_next,
+    float2* as_next, double* part, const int* __restrict__ done, BatchState* st, float k2,
+    double reg) {
+    const int2 it = items[blockIdx.x];
+    const int p = it.x;
+    if (done[p]) return;
+    const int n = B.n[p], m = B.m[p], d = B.d[p];
+    const float sc = B.scale[p];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i0 = it.y * kBItems + warp * kBPer;
+    const float* X = B.X + B.xo[p];
+    const float* Y = B.Y + B.yo[p];
+    const int ro = B.ro[p], co = B.co[p];
+
+    float xr[kBPer][DP], ah[kBPer], al[kBPer], mx[kBPer], sm[kBPer];
+#pragma unroll
+    for (int r = 0; r < kBPer; ++r) {
+        const int i = i0 + r;
+        const bool ok = i < n;
+#pragma unroll
+        for (int k = 0; k < DP; ++k) xr[r][k] = (ok && k < d) ? X[(long long)i * d + k] : 0.f;
+        const float2 s = ok ? as_cur[ro + i] : make_float2(0.f, 0.f);
+        ah[r] = s.x;
+        al[r] = __fmul_rn(s.y, k2);
+        mx[r] = -INFINITY;
+        sm[r] = 0.f;
+    }
+    __shared__ float sy[kBTile][DP + 1];
+    __shared__ float2 sb[kBTile];
+    for (int j0 = 0; j0 < m; j0 += kBTile) {
+        const int cnt = min(kBTile, m - j0);
+        for (int e = threadIdx.x; e < kBTile * DP; e += kBWarps * 32) {
+            const int jj = e / DP, k = e % DP;
+            sy[jj][k] = (jj < cnt && k < d) ? Y[(long long)(j0 + jj) * d + k] : 0.f;
+        }
+        for (int jj = threadIdx.x; jj < kBTile; jj += kBWarps * 32)
+            sb[jj] = jj < cnt ? bs[co + j0 + jj] : make_float2(0.f, 0.f);
+        __syncthreads();
+        for (int jj = lane; jj < cnt; jj += 32) {
+            float yv[DP];
+#pragma unroll
+            for (int k = 0; k < DP; ++k) yv[k] = sy[jj][k];
+            const float2 bj = sb[jj];
+            const float blk = __fmul_rn(bj.y, k2);
+#pragma unroll
+            for (int r = 0; r < kBPer; ++r) {
+                const float Mv = bcost<DP>(xr[r], yv, sc);
+                lse_add(mx[r], sm[r], fmaf((ah[r] + bj.x) - Mv, k2, __fadd_rn(al[r], blk)));
+            }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int r = 0; r < kBPer; ++r)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float m2 = __shfl_xor_sync(0xffffffffu, mx[r], o);
+            const float s2 = __shfl_xor_sync(0xffffffffu, sm[r], o);
+            lse_merge(mx[r], sm[r], m2, s2);
+        }
+    // lane r < kBPer finishes row i0 + r in FP64
+    double g2 = 0.0;
+    float mxr = mx[0], smr = sm[0];
+#pragma unroll
+    for (int r = 1; r < kBPer; ++r)
+        if (lane == r) {
+            mxr = mx[r];
+            smr = sm[r];
+        }
+    const int i = i0 + lane;
+    if (lane < kBPer && i < n) {
+        const double lg2 = (double)mxr + log2((double)smr);  // log2 S_i
+        const double S = exp2(lg2);
+        const double gi = S - B.a[ro + i];
+        g2 = gi * gi;
+        const double an = alpha_cur[ro + i] + reg * (B.loga[ro + i] - 0.69314718055994531 * lg2);
+        alpha_next[ro + i] = an;
+        as_next[ro + i] = bsplit(an, st, &st->regrid);
+    }
+    // block partial of sum (S_i - a_i)^2 in a fixed order
+    __shared__ double s_g2[kBWarps];
+    g2 += __shfl_xor_sync(0xffffffffu, g2, 1);
+    g2 += __shfl_xor_sync(0xffffffffu, g2, 2);
+    if (lane == 0) s_g2[warp] = g2;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+#pragma unroll
+        for (int w = 0; w < kBWarps; ++w) t += s_g2[w];
+        part[B.rbo[p] + it.y] = t;
+    }
+}
+
+
+// Column half-sweep for the column blocks `items`: with the new alpha,
+// S_j = sum_i exp((alpha_i + beta_j - M_ij)/reg) and beta_j += reg (log b_j -
+// log S_j) in place (sinkhorn_problem_bcd.cpp:149-174, current beta as
+// shift). write_split = 0 skips the split (first half-sweep, before the grid
+// is known).
+template <int DP>
+__global__ void __launch_bounds__(kBWarps * 32) k_bcol(
+    const BatchDev B, const int2* __restrict__ items, const float2* __restrict__ as,
+    float2* bs, double* beta, const int* __restrict__ done, BatchState* st, float k2, double reg,
+    int write_split) {
+    const int2 it = items[blockIdx.x];
+    const int p = it.x;
+    if (done[p]) return;
+    const int n = B.n[p], m = B.m[p], d = B.d[p];
+    const float sc = B.scale[p];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int j0c = it.y * kBItems + warp * kBPer;
+    const float* X = B.X + B.xo[p];
+    const float* Y = B.Y + B.yo[p];
+    const int ro = B.ro[p], co = B.co[p];
+
+    float yc[kBPer][DP], bh[kBPer], bl[kBPer], mx[kBPer], sm[kBPer];
+#pragma unroll
+    for (int r = 0; r < kBPer; ++r) {
+        const int j = j0c + r;
+        const bool ok = j < m;
+#pragma unroll
+        for (int k = 0; k < DP; ++k) yc[r][k] = (ok && k < d) ? Y[(long long)j * d + k] : 0.f;
+        const float2 s = ok ? bs[co + j] : make_float2(0.f, 0.f);
+        bh[r] = s.x;
+        bl[r] = __fmul_rn(s.y, k2);
+        mx[r] = -INFINITY;
+        sm[r] = 0.f;
+    }
+    __shared__ float sx[kBTile][DP + 1];
+    __shared__ float2 sa[kBTile];
+    for (int i0 = 0; i0 < n; i0 += kBTile) {
+        const int cnt = min(kBTile, n - i0);
+        for (int e = threadIdx.x; e < kBTile * DP; e += kBWarps * 32) {
+            const int ii = e / DP, k = e % DP;
+            sx[ii][k] = (ii < cnt && k < d) ? X[(long long)(i0 + ii) * d + k] : 0.f;
+        }
+        for (int ii = threadIdx.x; ii < kBTile; ii += kBWarps * 32)
+            sa[ii] = ii < cnt ? as[ro + i0 + ii] : make_float2(0.f, 0.f);
+        __syncthreads();
+        for (int ii = lane; ii < cnt; ii += 32) {
+            float xv[DP];
+#pragma unroll
+            for (int k = 0; k < DP; ++k) xv[k] = sx[ii][k];
+            const float2 ai = sa[ii];
+            const float alk = __fmul_rn(ai.y, k2);
+#pragma unroll
+            for (int r = 0; r < kBPer; ++r) {
+                // the same operations, in the same order, as the row kernel
+                const float Mv = bcost<DP>(xv, yc[r], sc);
+                lse_add(mx[r], sm[r], fmaf((ai.x + bh[r]) - Mv, k2, __fadd_rn(alk, bl[r])));
+            }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int r = 0; r < kBPer; ++r)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float m2 = __shfl_xor_sync(0xffffffffu, mx[r], o);
+            const float s2 = __shfl_xor_sync(0xffffffffu, sm[r], o);
+            lse_merge(mx[r], sm[r], m2, s2);
+        }
+    float mxr = mx[0], smr = sm[0];
+#pragma unroll
+    for (int r = 1; r < kBPer; ++r)
+        if (lane == r) {
+            mxr = mx[r];
+            smr = sm[r];
+        }
+    const int j = j0c + lane;
+    if (lane < kBPer && j < m) {
+        const double lg2 = (double)mxr + log2((double)smr);
+        const double bn = beta[co + j] + reg * (B.logb[co + j] - 0.69314718055994531 * lg2);
+        beta[co + j] = bn;
+        if (write_split) bs[co + j] = bsplit(bn, st, &st->regrid);
+    }
+}
+
+// Marginal error and stopping test of iterate k for every running problem
+// (one warp each): mar = sqrt(sum over the problem's row blocks), stop when
+// mar < tol or k >= max_iter (sinkhorn_bcd.cpp), the iterate's alpha being in
+// the buffers of `parity`.
+__global__ void k_bfin(const BatchDev B, int count, const double* part, int* done, int* iter,
+                       int* fpar, double* mar, int max_iter, double tol, BatchState* st,
+                       int parity) {
+    const int p = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (p >= count || done[p]) return;
+    const int nb = (B.n[p] + kBItems - 1) / kBItems;
+    double s = 0.0;
+    for (int k = lane; k < nb; k += 32) s += part[B.rbo[p] + k];
+    s = warp_sum_d(s);
+    if (lane == 0) {
+        const double g = sqrt(s);
+        const int k = iter[p];
+        mar[p] = g;
+        if (g < tol || k >= max_iter) {
+            done[p] = 1;
+            fpar[p] = parity;
+            atomicSub(&st->active, 1);
+        } else {
+            iter[p] = k + 1;
+        }
+    }
+}
+
+// Condition of the device-side loop, run once per body.
+__global__ void k_bloop(BatchState* st, cudaGraphConditionalHandle h) {
+    const int loops = ++st->loops;
+    const bool go = st->active > 0 && !st->regrid && loops < st->loop_cap;
+    cudaGraphSetConditional(h, go ? 1u : 0u);
+}
+
+__global__ void k_blog(const double* x, int len, double* y) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < len) y[t] = log(x[t]);
+}
+
+// st->maxabs = max |x|, |y| (zeroed by the caller), then the grid.
+__global__ void k_bmax(const double* x, int nx, const double* y, int ny, BatchState* st) {
+    unsigned long long v = 0ULL;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nx + ny; t += gridDim.x * blockDim.x) {
+        const unsigned long long q = abs_bits(t < nx ? x[t] : y[t - nx]);
+        v = q > v ? q : v;
+    }
+    block_atomic_max_bits(&st->maxabs, v);
+}
+
+// Grid of the split from max |dual|: g = 2^(e + 3 - 21), bound 2^(e + 4)
+// (8x headroom, as in the single-problem BCD).
+__global__ void k_bgrid(BatchState* st) {
+    const double m0 = st->maxabs;
+    const int e = (m0 > 0.0 && isfinite(m0)) ? ilogb(m0) : 0;
+    st->g = ldexp(1.0, e + 3 - 21);
+    st->inv_g = ldexp(1.0, -(e + 3 - 21));
+    st->bound = ldexp(1.0, e + 4);
+    st->regrid = 0;
+}
+
+__global__ void k_bsplit_all(const double* v, int len, float2* out, BatchState* st) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < len) out[t] = bsplit(v[t], st, &st->regrid);
+}
+
+
+struct BatchGraph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    ~BatchGraph() {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+    }
+};
+
+template <typename T>
+void upload_vec(DBuf<T>& buf, const std::vector<T>& v, cudaStream_t st) {
+    buf.alloc(v.size(), st);
+    h2d(buf.get(), v.data(), v.size() * sizeof(T), st);
+}
+
+}  // namespace
+
+void erot_solve_batched_gpu(regot_ctx* ctx, const regot_batch_desc* D, double reg, double tol,
+                            int max_iter, regot_batch_result* res) {
+    cudaStream_t st = ctx->stream;
+    const int P = D->count;
+    std::vector<int> hn(P), hm(P), hd(P), ro(P), co(P), rbo(P + 1), cls(P);
+    std::vector<long long> xo(P), yo(P);
+    std::vector<float> hsc(P);
+    long long NX = 0, NY = 0, NR = 0, NC = 0, NRB = 0;
+    for (int p = 0; p < P; ++p) {
+        const int n = D->n[p], m = D->m[p], d = D->d[p];
+        require(n > 0 && m > 0, "every problem needs at least one row and one column");
+        require(d >= 1 && d <= REGOT_BATCH_MAX_DIM, "point dimension must be in 1..16");
+        const double sc = D->cost_scale ? D->cost_scale[p] : 1.0;
+        require(std::isfinite(sc) && sc > 0.0, "cost scales must be positive and finite");
+        hn[p] = n;
+        hm[p] = m;
+        hd[p] = d;
+        hsc[p] = (float)sc;
+        ro[p] = (int)NR;
+        co[p] = (int)NC;
+        xo[p] = NX;
+        yo[p] = NY;
+        rbo[p] = (int)NRB;
+        NR += n;
+        NC += m;
+        NX += (long long)n * d;
+        NY += (long long)m * d;
+        NRB += cdiv(n, kBItems);
+        cls[p] = d <= kBClassDim[0] ? 0 : d <= kBClassDim[1] ? 1 : 2;
+    }
+    require(NR < (1LL << 31) && NC < (1LL << 31), "batch too large");
+    rbo[P] = (int)NRB;
+
+    // Work items per dimension class, the longest first (rows: by m, columns:
+    // by n) so that the large problems do not finish last.
+    std::vector<int> order(P);
+    for (int p = 0; p < P; ++p) order[p] = p;
+    std::vector<int2> ritems[kBClasses], citems[kBClasses];
+    std::stable_sort(order.begin(), order.end(), [&](int u, int v) { return hm[u] > hm[v]; });
+    for (int p : order)
+        for (int k = 0; k < cdiv(hn[p], kBItems); ++k) ritems[cls[p]].push_back(make_int2(p, k));
+    std::stable_sort(order.begin(), order.end(), [&](int u, int v) { return hn[u] > hn[v]; });
+    for (int p : order)
+        for (int k = 0; k < cdiv(hm[p], kBItems); ++k) citems[cls[p]].push_back(make_int2(p, k));
+
+    DBuf<int> dn, dm, dd, dro, dco, drbo;
+    DBuf<long long> dxo, dyo;
+    DBuf<float> dsc;
+    upload_vec(dn, hn, st);
+    upload_vec(dm, hm, st);
+    upload_vec(dd, hd, st);
+    upload_vec(dro, ro, st);
+    upload_vec(dco, co, st);
+    upload_vec(drbo, rbo, st);
+    upload_vec(dxo, xo, st);
+    upload_vec(dyo, yo, st);
+    upload_vec(dsc, hsc, st);
+    DBuf<int2> dri[kBClasses], dci[kBClasses];
+    for (int c = 0; c < kBClasses; ++c) {
+        if (!ritems[c].empty()) upload_vec(dri[c], ritems[c], st);
+        if (!citems[c].empty()) upload_vec(dci[c], citems[c], st);
+    }
+
+    // points and marginals on the device
+    DBuf<float> hX, hY;
+    DBuf<double> ha, hb, loga(NR, st), logb(NC, st);
+    const float* X = D->x;
+    const float* Y = D->y;
+    const double* a = D->a;
+    const double* b = D->b;
+    if (D->mem == REGOT_MEM_HOST) {
+        hX.alloc(NX, st);
+        hY.alloc(NY, st);
+        ha.alloc(NR, st);
+        hb.alloc(NC, st);
+        h2d(hX.get(), D->x, NX * sizeof(float), st);
+        h2d(hY.get(), D->y, NY * sizeof(float), st);
+        h2d(ha.get(), D->a, NR * sizeof(double), st);
+        h2d(hb.get(), D->b, NC * sizeof(double), st);
+        X = hX.get();
+        Y = hY.get();
+        a = ha.get();
+        b = hb.get();
+    }
+    k_blog<<<cdiv(NR, 256), 256, 0, st>>>(a, (int)NR, loga.get());
+    k_blog<<<cdiv(NC, 256), 256, 0, st>>>(b, (int)NC, logb.get());
+    count_launch(2);
+
+    DBuf<double> A[2] = {DBuf<double>(NR, st), DBuf<double>(NR, st)}, beta(NC, st);
+    DBuf<float2> AS[2] = {DBuf<float2>(NR, st), DBuf<float2>(NR, st)}, BS(NC, st);
+    DBuf<int> done(P, st), iter(P, st), fpar(P, st);
+    DBuf<double> mar(P, st), part(std::max<long long>(NRB, 1), st);
+    DBuf<BatchState> dstate(1, st);
+    for (int q = 0; q < 2; ++q) {
+        A[q].zero();
+        AS[q].zero();
+    }
+    beta.zero();
+    BS.zero();
+    done.zero();
+    iter.zero();
+    fpar.zero();
+    BatchState h0{};
+    h0.active = P;
+    h0.loop_cap = max_iter / 2 + 3;
+    h2d(dstate.get(), &h0, sizeof(h0), st);
+    BatchState* S = dstate.get();
+
+    BatchDev B{dn.get(), dm.get(), dd.get(), dsc.get(), dxo.get(), dyo.get(), dro.get(),
+               dco.get(), drbo.get(), X, Y, a, loga.get(), logb.get()};
+    const float k2 = (float)(1.4426950408889634 / reg);
+    auto launch_rows = [&](int q) {
+        for (int c = 0; c < kBClasses; ++c) {
+            const int nb = (int)ritems[c].size();
+            if (!nb) continue;
+            const dim3 grid(nb), block(kBWarps * 32);
+            if (c == 0)
+                k_brow<4><<<grid, block, 0, st>>>(B, dri[c].get(), AS[q].get(), BS.get(),
+                                                  A[q].get(), A[1 - q].get(), AS[1 - q].get(),
+                                                  part.get(), done.get(), S, k2, reg);
+            else if (c == 1)
+                k_brow<8><<<grid, block, 0, st>>>(B, dri[c].get(), AS[q].get(), BS.get(),
+                                                  A[q].get(), A[1 - q].get(), AS[1 - q].get(),
+                                                  part.get(), done.get(), S, k2, reg);
+            else
+                k_brow<16><<<grid, block, 0, st>>>(B, dri[c].get(), AS[q].get(), BS.get(),
+                                                   A[q].get(), A[1 - q].get(), AS[1 - q].get(),
+                                                   part.get(), done.get(), S, k2, reg);
+            count_launch();
+        }
+    };
+    auto launch_cols = [&](int q, int write_split) {
+        for (int c = 0; c < kBClasses; ++c) {
+            const int nb = (int)citems[c].size();
+            if (!nb) continue;
+            const dim3 grid(nb), block(kBWarps * 32);
+            if (c == 0)
+                k_bcol<4><<<grid, block, 0, st>>>(B, dci[c].get(), AS[q].get(), BS.get(),
+                                                  beta.get(), done.get(), S, k2, reg, write_split);
+            else if (c == 1)
+                k_bcol<8><<<grid, block, 0, st>>>(B, dci[c].get(), AS[q].get(), BS.get(),
+                                                  beta.get(), done.get(), S, k2, reg, write_split);
+            else
+                k_bcol<16><<<grid, block, 0, st>>>(B, dci[c].get(), AS[q].get(), BS.get(),
+                                                   beta.get(), done.get(), S, k2, reg,
+                                                   write_split);
+            count_launch();
+        }
+    };
+    // split of alpha (buffers q) and beta on a fresh grid from their max
+    auto regrid = [&](int q) {
+        REGOT_CUDA(cudaMemsetAsync(&S->maxabs, 0, sizeof(double), st));
+        k_bmax<<<64, 256, 0, st>>>(A[q].get(), (int)NR, beta.get(), (int)NC, S);
+        k_bgrid<<<1, 1, 0, st>>>(S);
+        k_bsplit_all<<<cdiv(NR, 256), 256, 0, st>>>(A[q].get(), (int)NR, AS[q].get(), S);
+        k_bsplit_all<<<cdiv(NC, 256), 256, 0, st>>>(beta.get(), (int)NC, BS.get(), S);
+        count_launch(4);
+        REGOT_CHECK_LAUNCH();
+    };
+
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    REGOT_CUDA(cudaEventCreate(&e0));
+    REGOT_CUDA(cudaEventCreate(&e1));
+    struct Events {
+        cudaEvent_t a, b;
+        ~Events() {
+            cudaEventDestroy(a);
+            cudaEventDestroy(b);
+        }
+    } events{e0, e1};
+    REGOT_CUDA(cudaEventRecord(e0, st));
+
+    // beta = optimal_beta(alpha = 0) (sinkhorn_bcd.cpp:38-47): one column
+    // half-sweep from zero duals, then the split grid from |beta|.
+    launch_cols(0, 0);
+    regrid(0);
+
+    // The sweeps: a graph whose only node is a conditional WHILE node; its
+    // body is two sweeps (alpha ping-pongs between A[0] and A[1]) and k_bloop.
+    BatchGraph lg;
+    REGOT_CUDA(cudaGraphCreate(&lg.graph, 0));
+    cudaGraphConditionalHandle loop_h;
+    REGOT_CUDA(cudaGraphConditionalHandleCreate(&loop_h, lg.graph, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+    cp.conditional.handle = loop_h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t loop_node;
+    REGOT_CUDA(cudaGraphAddNode(&loop_node, lg.graph, nullptr, nullptr, 0, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    long long* saved_counter = g_launch_counter;
+    long long body_kernels = 0;
+    g_launch_counter = &body_kernels;
+    const int fin_blocks = cdiv(P, 8);
+    REGOT_CUDA(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0,
+                                             cudaStreamCaptureModeThreadLocal));
+    try {
+        for (int q = 0; q < 2; ++q) {
+            launch_rows(q);
+            k_bfin<<<fin_blocks, 256, 0, st>>>(B, P, part.get(), done.get(), iter.get(),
+                                               fpar.get(), mar.get(), max_iter, tol, S, q);
+            count_launch();
+            launch_cols(1 - q, 1);
+        }
+        k_bloop<<<1, 1, 0, st>>>(S, loop_h);
+        count_launch();
+    } catch (...) {
+        cudaGraph_t g = nullptr;
+        cudaStreamEndCapture(st, &g);
+        g_launch_counter = saved_counter;
+        throw;
+    }
+    REGOT_CUDA(cudaStreamEndCapture(st, &body));
+    g_launch_counter = saved_counter;
+    REGOT_CUDA(cudaGraphInstantiate(&lg.exec, lg.graph, 0));
+
+    BatchState hs{};
+    int prev_loops = 0;
+    for (;;) {
+        REGOT_CUDA(cudaGraphLaunch(lg.exec, st));
+        read_small(ctx, &hs, S, sizeof(hs), st);
+        count_launch(body_kernels * (hs.loops - prev_loops));
+        prev_loops = hs.loops;
+        if (hs.active == 0) break;
+        if (!hs.regrid || hs.loops >= hs.loop_cap)
+            throw Error(REGOT_ERR_NUMERIC, "batched BCD did not terminate");
+        regrid(0);  // at a body boundary the running problems' alpha is in A[0]
+    }
+    REGOT_CUDA(cudaEventRecord(e1, st));
+
+    // results: each problem's alpha from the buffers of its last iterate,
+    // gauge-fixed with its last beta
+    std::vector<double> h0a(NR), h1a(NR), hbeta(NC), hmar(P);
+    std::vector<int> hfpar(P), hiter(P);
+    d2h(h0a.data(), A[0].get(), NR * sizeof(double), st);
+    d2h(h1a.data(), A[1].get(), NR * sizeof(double), st);
+    d2h(hbeta.data(), beta.get(), NC * sizeof(double), st);
+    d2h(hmar.data(), mar.get(), P * sizeof(double), st);
+    d2h(hfpar.data(), fpar.get(), P * sizeof(int), st);
+    d2h(hiter.data(), iter.get(), P * sizeof(int), st);
+    sync(st);
+    float ms = 0.f;
+    REGOT_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    for (int p = 0; p < P; ++p) {
+        const std::vector<double>& ap = hfpar[p] ? h1a : h0a;
+        const double bl = hbeta[co[p] + hm[p] - 1];
+        if (res->alpha)
+            for (int i = 0; i < hn[p]; ++i) res->alpha[ro[p] + i] = ap[ro[p] + i] + bl;
+        if (res->beta)
+            for (int j = 0; j < hm[p]; ++j) res->beta[co[p] + j] = hbeta[co[p] + j] - bl;
+        if (res->niter) res->niter[p] = hiter[p];
+        if (res->mar_err) res->mar_err[p] = hmar[p];
+    }
+    res->sweeps = 2LL * hs.loops;
+    res->solve_ms = ms;
+}
+
+}  // namespace regot

@@ -38,6 +38,7 @@ from . import _lib as L
 __all__ = [
     "sinkhorn_bcd", "sinkhorn_newton", "sinkhorn_ssns", "sinkhorn_lbfgs_dual", "sinkhorn_apdagd",
     "qrot_lbfgs_dual", "qrot_assn", "sinkhorn_result", "qrot_result", "Problem",
+    "sinkhorn_bcd_batched", "batch_result",
 ]
 
 
@@ -456,3 +457,82 @@ def qrot_lbfgs_dual(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
 def qrot_assn(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
     """Adaptive semi-smooth Newton for QROT; reference src/qrot_assn.cpp:16-170."""
     return _solve("qrot_assn", M, a, b, reg, tol, max_iter, verbose, kwargs)
+
+
+class batch_result:
+    """Result of sinkhorn_bcd_batched: per-problem iteration counts, final
+    marginal errors and gauge-fixed duals (alpha, beta~) as sinkhorn_bcd
+    returns them, plus the sweeps and device time of the whole batch."""
+
+    def __init__(self):
+        self.niter = None
+        self.mar_errs = None
+        self.duals = []
+        self.sweeps = 0
+        self.solve_ms = 0.0
+
+    def __repr__(self):
+        return (f"batch_result(problems={len(self.duals)}, sweeps={self.sweeps}, "
+                f"max niter={int(self.niter.max()) if len(self.duals) else 0})")
+
+
+def sinkhorn_bcd_batched(xs, ys, as_, bs, reg, tol=1e-6, max_iter=1000, cost_scale=None,
+                         device: int = 0):
+    """sinkhorn_bcd (reference src/sinkhorn_bcd.cpp:14-124) on many problems
+    at once, each with the squared-Euclidean cost M_ij = s_p |x_i - y_j|^2
+    computed on the fly in FP32 (no n x m matrix is stored). xs, ys: lists
+    of (n_p, d_p) and (m_p, d_p) point arrays (d_p <= 16); as_, bs: lists of
+    marginals; cost_scale: None, a number or one number per problem. Each
+    problem stops at its own iteration (marginal error < tol or max_iter)."""
+    P = len(xs)
+    if not (len(ys) == len(as_) == len(bs) == P) or P == 0:
+        raise ValueError("xs, ys, as_ and bs must be non-empty lists of the same length")
+    xs = [np.ascontiguousarray(np.asarray(x, dtype=np.float32)) for x in xs]
+    ys = [np.ascontiguousarray(np.asarray(y, dtype=np.float32)) for y in ys]
+    as_ = [np.ascontiguousarray(np.asarray(v, dtype=np.float64).ravel()) for v in as_]
+    bs = [np.ascontiguousarray(np.asarray(v, dtype=np.float64).ravel()) for v in bs]
+    n = np.array([x.shape[0] for x in xs], dtype=np.int32)
+    m = np.array([y.shape[0] for y in ys], dtype=np.int32)
+    d = np.array([x.shape[1] if x.ndim == 2 else 0 for x in xs], dtype=np.int32)
+    for p in range(P):
+        if xs[p].ndim != 2 or ys[p].ndim != 2 or ys[p].shape[1] != d[p]:
+            raise ValueError(f"problem {p}: x and y must be 2-D with the same dimension")
+        if as_[p].size != n[p] or bs[p].size != m[p]:
+            raise ValueError(f"problem {p}: a must have {n[p]} entries and b {m[p]}")
+        if not (1 <= d[p] <= L.BATCH_MAX_DIM):
+            raise ValueError(f"problem {p}: point dimension must be in 1..{L.BATCH_MAX_DIM}")
+    if cost_scale is None:
+        sc = None
+    else:
+        sc = np.ascontiguousarray(np.broadcast_to(np.asarray(cost_scale, dtype=np.float64),
+                                                  (P,)))
+    X = np.concatenate([x.ravel() for x in xs])
+    Y = np.concatenate([y.ravel() for y in ys])
+    A = np.concatenate(as_)
+    B = np.concatenate(bs)
+    ctx = L.context(device)
+    lib = L.load()
+    desc = L.BatchDesc()
+    desc.count = P
+    desc.n, desc.m, desc.d = n.ctypes.data, m.ctypes.data, d.ctypes.data
+    desc.cost_scale = sc.ctypes.data if sc is not None else None
+    desc.x, desc.y, desc.a, desc.b = X.ctypes.data, Y.ctypes.data, A.ctypes.data, B.ctypes.data
+    desc.mem = L.REGOT_MEM_HOST
+    alpha = np.zeros(A.size)
+    beta = np.zeros(B.size)
+    niter = np.zeros(P, dtype=np.int32)
+    mar = np.zeros(P)
+    r = L.BatchResult()
+    r.alpha, r.beta = alpha.ctypes.data, beta.ctypes.data
+    r.niter, r.mar_err = niter.ctypes.data, mar.ctypes.data
+    ctx.check(lib.regot_erot_solve_batched(ctx.handle, C.byref(desc), float(reg), float(tol),
+                                           int(max_iter), C.byref(r)))
+    out = batch_result()
+    out.niter = niter
+    out.mar_errs = mar
+    ro = np.r_[0, np.cumsum(n)]
+    co = np.r_[0, np.cumsum(m)]
+    out.duals = [np.r_[alpha[ro[p]:ro[p + 1]], beta[co[p]:co[p + 1] - 1]] for p in range(P)]
+    out.sweeps = int(r.sweeps)
+    out.solve_ms = float(r.solve_ms)
+    return out

@@ -78,6 +78,35 @@ class Result(C.Structure):
     ]
 
 
+class BatchDesc(C.Structure):
+    _fields_ = [
+        ("count", C.c_int),
+        ("n", C.c_void_p),
+        ("m", C.c_void_p),
+        ("d", C.c_void_p),
+        ("cost_scale", C.c_void_p),
+        ("x", C.c_void_p),
+        ("y", C.c_void_p),
+        ("a", C.c_void_p),
+        ("b", C.c_void_p),
+        ("mem", C.c_int),
+    ]
+
+
+class BatchResult(C.Structure):
+    _fields_ = [
+        ("alpha", C.c_void_p),
+        ("beta", C.c_void_p),
+        ("niter", C.c_void_p),
+        ("mar_err", C.c_void_p),
+        ("sweeps", C.c_longlong),
+        ("solve_ms", C.c_double),
+    ]
+
+
+BATCH_MAX_DIM = 16
+
+
 # Every symbol include/regot_gb300.h declares.
 EXPORTS = [
     "regot_opts_init", "regot_ctx_create", "regot_ctx_destroy", "regot_ctx_last_error",
@@ -86,7 +115,7 @@ EXPORTS = [
     "regot_sinkhorn_ssns", "regot_sinkhorn_lbfgs_dual", "regot_sinkhorn_apdagd",
     "regot_qrot_lbfgs_dual", "regot_qrot_assn", "regot_erot_optimal_beta", "regot_erot_optimal_alpha", "regot_erot_dual_obj_grad",
     "regot_erot_hvp", "regot_erot_plan", "regot_erot_sparsify", "regot_erot_hess_solve",
-    "regot_erot_tyy", "regot_qrot_dual_obj_grad",
+    "regot_erot_tyy", "regot_erot_solve_batched", "regot_qrot_dual_obj_grad",
     "regot_qrot_optimal_beta",
     "regot_qrot_primal_val", "regot_qrot_plan", "regot_time_pass",
     "regot_erot_dual_obj_grad_noalloc", "regot_host_alloc", "regot_host_free",
@@ -141,6 +170,8 @@ def load() -> C.CDLL:
         lib.regot_qrot_primal_val.argtypes = [vp, vp, C.c_double, vp, vp]
         lib.regot_qrot_plan.argtypes = [vp, vp, C.c_double, vp, vp, C.c_int]
         lib.regot_time_pass.argtypes = [vp, vp, C.c_int, C.c_double, C.c_int]
+        lib.regot_erot_solve_batched.argtypes = [vp, C.POINTER(BatchDesc), C.c_double,
+                                                 C.c_double, C.c_int, C.POINTER(BatchResult)]
         lib.regot_erot_hess_solve.argtypes = [vp, vp, C.c_double, vp, vp, C.c_double, C.c_int,
                                               vp, C.POINTER(C.c_int)]
         lib.regot_erot_tyy.argtypes = [vp, vp, C.c_double, vp, vp, vp, vp, C.c_int, vp, vp,

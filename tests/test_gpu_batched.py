@@ -1,0 +1,93 @@
+"""Batched BCD over point-cloud problems (regot_erot_solve_batched) against
+the FP64 oracle's sinkhorn_bcd run on each problem alone."""
+import numpy as np
+import pytest
+
+import regot_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+regot = pytest.importorskip("regot")
+
+
+def _batch(count, seed, nmin=16, nmax=200, dims=range(1, 17)):
+    """Uneven problems: n, m log-uniform, d uniform over `dims`, x ~ N(0, I),
+    y ~ N(mu, I) with mu ~ N(0, 0.25 I), uniform-random marginals."""
+    rng = np.random.default_rng(seed)
+    xs, ys, as_, bs, scales = [], [], [], [], []
+    dims = list(dims)
+    for _ in range(count):
+        n, m = np.exp(rng.uniform(np.log(nmin), np.log(nmax), 2)).round().astype(int)
+        d = int(rng.choice(dims))
+        mu = rng.normal(0.0, 0.5, d)
+        xs.append(rng.standard_normal((n, d)).astype(np.float32))
+        ys.append((rng.standard_normal((m, d)) + mu).astype(np.float32))
+        a = rng.uniform(0.5, 1.5, n)
+        b = rng.uniform(0.5, 1.5, m)
+        as_.append(a / a.sum())
+        bs.append(b / b.sum())
+        scales.append(1.0 / d)
+    return xs, ys, as_, bs, scales
+
+
+def _cost64(x, y, s):
+    x = x.astype(np.float64)
+    y = y.astype(np.float64)
+    return s * ((x[:, None, :] - y[None, :, :]) ** 2).sum(-1)
+
+
+def test_batched_matches_oracle_per_problem():
+    # tol 1e-6 as in the batched workload: the FP32 row sums carry relative
+    # errors of a few 1e-7, so much tighter tolerances stall in FP32
+    reg, tol = 0.05, 1e-6
+    xs, ys, as_, bs, sc = _batch(24, seed=5)
+    r = regot.sinkhorn_bcd_batched(xs, ys, as_, bs, reg, tol=tol, max_iter=5000, cost_scale=sc)
+    assert len(r.duals) == 24 and r.sweeps >= int(r.niter.max())
+    for p in range(24):
+        M = _cost64(xs[p], ys[p], sc[p])
+        o = O.sinkhorn_bcd(M, as_[p], bs[p], reg, tol=tol, max_iter=5000, plan=False)
+        assert r.mar_errs[p] < tol, (p, r.mar_errs[p])
+        # the FP32 cost differs from the FP64 one by an ulp of M: the same
+        # convergence up to a few iterations, duals to ~1e-6
+        assert abs(int(r.niter[p]) - o.niter) <= max(3, 0.05 * o.niter), (p, r.niter[p], o.niter)
+        np.testing.assert_allclose(r.duals[p], o.dual, rtol=0, atol=2e-5)
+        # the duals are optimal for the FP64 cost to the same accuracy
+        _, g = O.erot_dual_obj_grad(M, as_[p], bs[p], reg, r.duals[p])
+        assert np.linalg.norm(g) < 5 * tol
+
+
+def test_batched_max_iter_iterates():
+    # every problem stops at max_iter: the duals are the oracle's iterate
+    reg = 0.05
+    xs, ys, as_, bs, sc = _batch(10, seed=6, dims=(2, 3, 7, 12, 16))
+    r = regot.sinkhorn_bcd_batched(xs, ys, as_, bs, reg, tol=1e-14, max_iter=7, cost_scale=sc)
+    assert np.all(r.niter == 7)
+    for p in range(10):
+        M = _cost64(xs[p], ys[p], sc[p])
+        o = O.sinkhorn_bcd(M, as_[p], bs[p], reg, tol=1e-14, max_iter=7, plan=False)
+        assert o.niter == 7
+        np.testing.assert_allclose(r.duals[p], o.dual, rtol=0, atol=2e-5)
+        np.testing.assert_allclose(r.mar_errs[p], o.mar_errs[-1], rtol=2e-3, atol=1e-9)
+
+
+def test_batched_single_problem_equals_batch_member():
+    # a problem's result does not depend on the other problems of the batch
+    reg, tol = 0.05, 1e-7
+    xs, ys, as_, bs, sc = _batch(6, seed=7)
+    r = regot.sinkhorn_bcd_batched(xs, ys, as_, bs, reg, tol=tol, max_iter=3000, cost_scale=sc)
+    for p in (0, 3, 5):
+        r1 = regot.sinkhorn_bcd_batched([xs[p]], [ys[p]], [as_[p]], [bs[p]], reg, tol=tol,
+                                        max_iter=3000, cost_scale=sc[p])
+        assert r1.niter[0] == r.niter[p]
+        np.testing.assert_array_equal(r1.duals[0], r.duals[p])
+
+
+def test_batched_rejects_bad_input():
+    xs, ys, as_, bs, sc = _batch(2, seed=8)
+    with pytest.raises(ValueError):
+        regot.sinkhorn_bcd_batched(xs, ys[:1], as_, bs, 0.05)
+    with pytest.raises(ValueError):
+        regot.sinkhorn_bcd_batched([np.zeros((4, 17), np.float32)], [np.zeros((3, 17), np.float32)],
+                                   [np.full(4, 0.25)], [np.full(3, 1 / 3)], 0.05)
+    with pytest.raises(ValueError):
+        regot.sinkhorn_bcd_batched(xs, ys, as_, bs, -1.0)
