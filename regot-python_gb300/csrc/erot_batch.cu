@@ -29,6 +29,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <vector>
 
 #include "device_util.cuh"
@@ -67,6 +68,8 @@ struct BatchState {
     int regrid;     // a dual reached the bound of the split grid
     int loops;
     int loop_cap;
+    int stop_below;  // leave the device loop when this few problems still run
+    int pad;
     double maxabs;  // max |dual| for the grid
     double g, inv_g, bound;
 };
@@ -77,13 +80,31 @@ __device__ __forceinline__ float bex2(float x) {
     return y;
 }
 
-// Running log-sum-exp in base 2: sum 2^z = 2^mx * s.
+// Running log-sum-exp in base 2: sum 2^z = 2^mx * s. The reference point mx
+// only moves when a term exceeds it by 2^16, so terms stay below 2^16 and
+// the rescaling branch is rare after the first term (mx starts at -inf).
+constexpr float kLseSlack = 16.f;
+
 __device__ __forceinline__ void lse_add(float& mx, float& s, float z) {
-    if (z > mx) {
+    if (z > mx + kLseSlack) {
         s = fmaf(s, bex2(mx - z), 1.f);
         mx = z;
     } else {
         s += bex2(z - mx);
+    }
+}
+
+// Four terms (one per row or column of the lane): the common case adds
+// without a branch per term.
+__device__ __forceinline__ void lse_add4(float (&mx)[4], float (&s)[4], const float (&z)[4]) {
+    const bool slow = (z[0] > mx[0] + kLseSlack) | (z[1] > mx[1] + kLseSlack) |
+                      (z[2] > mx[2] + kLseSlack) | (z[3] > mx[3] + kLseSlack);
+    if (slow) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) lse_add(mx[r], s[r], z[r]);
+    } else {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) s[r] += bex2(z[r] - mx[r]);
     }
 }
 
@@ -93,16 +114,42 @@ __device__ __forceinline__ void lse_merge(float& mx, float& s, float m2, float s
     mx = m;
 }
 
-// Cost of one pair, identical in the row and column kernels.
+// Costs of two pairs at once, u = x and v = -y per dimension (the row
+// kernel pairs two rows with one column, the column kernel one row with two
+// columns). The packed FP32x2 instructions round each half exactly as the
+// scalar fadd / ffma / fmul would, so both kernels produce the same M_ij.
+// Four partial sums over the dimensions (k mod 4) keep the FMA chains short:
+// with one running sum the kernels were bound by its latency.
 template <int DP>
-__device__ __forceinline__ float bcost(const float (&x)[DP], const float* y, float sc) {
-    float s = 0.f;
+__device__ __forceinline__ float2 bcost2(const float2 (&u)[DP], const float2 (&v)[DP],
+                                         float2 sc2) {
+    float2 s[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) s[q] = make_float2(0.f, 0.f);
 #pragma unroll
     for (int k = 0; k < DP; ++k) {
-        const float t = x[k] - y[k];
-        s = fmaf(t, t, s);
+        const float2 t = __fadd2_rn(u[k], v[k]);
+        s[k & 3] = __ffma2_rn(t, t, s[k & 3]);
     }
-    return s * sc;
+    return __fmul2_rn(__fadd2_rn(__fadd2_rn(s[0], s[1]), __fadd2_rn(s[2], s[3])), sc2);
+}
+
+// Exponent of T in base 2 for two pairs: ((hi_i + hi_j) - M) k + (lo_i k + lo_j k).
+__device__ __forceinline__ float2 bexpo2(float2 hi_i, float2 hi_j, float2 lok_i, float2 lok_j,
+                                         float2 M, float2 k2) {
+    const float2 e = __fadd2_rn(__fadd2_rn(hi_i, hi_j), make_float2(-M.x, -M.y));
+    return __ffma2_rn(e, k2, __fadd2_rn(lok_i, lok_j));
+}
+
+// The row and column results are formed with FP32 transcendentals (log2f,
+// exp2f of the fractional part, the power of two applied in FP64): FP64
+// arithmetic issues at a small fraction of the FP32 rate on this part, and
+// the FP64 log / exp of the epilogues took as long as the element loop of a
+// small problem. log2f is accurate to about 1e-7 relative, which moves a
+// dual by ~1e-7 reg, far below what the 1e-6 marginal tolerance resolves.
+__device__ __forceinline__ double row_sum(float mx, float s) {
+    const float fl = floorf(mx);
+    return ldexp((double)(s * exp2f(mx - fl)), (int)fl);
 }
 
 __device__ __forceinline__ float2 bsplit(double v, const BatchState* st, int* regrid) {
@@ -118,14 +165,12 @@ __device__ __forceinline__ float2 bsplit(double v, const BatchState* st, int* re
 // 177-201 with the current alpha as shift) with its split, and the block's
 // sum of (S_i - a_i)^2 for the marginal error.
 template <int DP>
-__global__ void __launch_bounds__(kBWarps * 32) k_brow(
-    const BatchDev B, const int2* __restrict__ items, const float2* __restrict__ as_cur,
-    const float2* __restrict__ bs, const double* __restrict__ alpha_cur, double* alpha_next,
-    float2* as_next, double* part, const int* __restrict__ done, BatchState* st, float k2,
-    double reg) {
-    const int2 it = items[blockIdx.x];
+__device__ __forceinline__ void row_item(const BatchDev& B, int2 it, const float2* __restrict__ as_cur,
+                                         const float2* __restrict__ bs,
+                                         const double* __restrict__ alpha_cur, double* alpha_next,
+                                         float2* as_next, double* part, BatchState* st, float k2,
+                                         double reg) {
     const int p = it.x;
-    if (done[p]) return;
     const int n = B.n[p], m = B.m[p], d = B.d[p];
     const float sc = B.scale[p];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -134,41 +179,62 @@ __global__ void __launch_bounds__(kBWarps * 32) k_brow(
     const float* Y = B.Y + B.yo[p];
     const int ro = B.ro[p], co = B.co[p];
 
-    float xr[kBPer][DP], ah[kBPer], al[kBPer], mx[kBPer], sm[kBPer];
+    // rows in pairs: xp[h][k] = (x_{2h}[k], x_{2h+1}[k])
+    float2 xp[kBPer / 2][DP], ah[kBPer / 2], al[kBPer / 2];
+    float mx[kBPer], sm[kBPer];
 #pragma unroll
     for (int r = 0; r < kBPer; ++r) {
         const int i = i0 + r;
         const bool ok = i < n;
 #pragma unroll
-        for (int k = 0; k < DP; ++k) xr[r][k] = (ok && k < d) ? X[(long long)i * d + k] : 0.f;
+        for (int k = 0; k < DP; ++k) {
+            const float v = (ok && k < d) ? X[(long long)i * d + k] : 0.f;
+            if (r & 1) xp[r >> 1][k].y = v;
+            else xp[r >> 1][k].x = v;
+        }
         const float2 s = ok ? as_cur[ro + i] : make_float2(0.f, 0.f);
-        ah[r] = s.x;
-        al[r] = __fmul_rn(s.y, k2);
+        const float lk = __fmul_rn(s.y, k2);
+        if (r & 1) {
+            ah[r >> 1].y = s.x;
+            al[r >> 1].y = lk;
+        } else {
+            ah[r >> 1].x = s.x;
+            al[r >> 1].x = lk;
+        }
         mx[r] = -INFINITY;
         sm[r] = 0.f;
     }
-    __shared__ float sy[kBTile][DP + 1];
+    const float2 sc2 = make_float2(sc, sc), k22 = make_float2(k2, k2);
+    // columns staged negated and duplicated, (-y, -y), ready for the packed
+    // instructions (rows padded by one entry against bank conflicts)
+    __shared__ float2 sy[kBTile][DP + 1];
     __shared__ float2 sb[kBTile];
     for (int j0 = 0; j0 < m; j0 += kBTile) {
         const int cnt = min(kBTile, m - j0);
         for (int e = threadIdx.x; e < kBTile * DP; e += kBWarps * 32) {
             const int jj = e / DP, k = e % DP;
-            sy[jj][k] = (jj < cnt && k < d) ? Y[(long long)(j0 + jj) * d + k] : 0.f;
+            const float v = (jj < cnt && k < d) ? -Y[(long long)(j0 + jj) * d + k] : 0.f;
+            sy[jj][k] = make_float2(v, v);
         }
         for (int jj = threadIdx.x; jj < kBTile; jj += kBWarps * 32)
             sb[jj] = jj < cnt ? bs[co + j0 + jj] : make_float2(0.f, 0.f);
         __syncthreads();
         for (int jj = lane; jj < cnt; jj += 32) {
-            float yv[DP];
+            float2 ny[DP];
 #pragma unroll
-            for (int k = 0; k < DP; ++k) yv[k] = sy[jj][k];
+            for (int k = 0; k < DP; ++k) ny[k] = sy[jj][k];
             const float2 bj = sb[jj];
             const float blk = __fmul_rn(bj.y, k2);
+            float z[kBPer];
 #pragma unroll
-            for (int r = 0; r < kBPer; ++r) {
-                const float Mv = bcost<DP>(xr[r], yv, sc);
-                lse_add(mx[r], sm[r], fmaf((ah[r] + bj.x) - Mv, k2, __fadd_rn(al[r], blk)));
+            for (int h = 0; h < kBPer / 2; ++h) {
+                const float2 Mv = bcost2<DP>(xp[h], ny, sc2);
+                const float2 zz = bexpo2(ah[h], make_float2(bj.x, bj.x), al[h],
+                                         make_float2(blk, blk), Mv, k22);
+                z[2 * h] = zz.x;
+                z[2 * h + 1] = zz.y;
             }
+            lse_add4(mx, sm, z);
         }
         __syncthreads();
     }
@@ -191,8 +257,8 @@ __global__ void __launch_bounds__(kBWarps * 32) k_brow(
         }
     const int i = i0 + lane;
     if (lane < kBPer && i < n) {
-        const double lg2 = (double)mxr + log2((double)smr);  // log2 S_i
-        const double S = exp2(lg2);
+        const double lg2 = (double)mxr + (double)log2f(smr);  // log2 S_i
+        const double S = row_sum(mxr, smr);
         const double gi = S - B.a[ro + i];
         g2 = gi * gi;
         const double an = alpha_cur[ro + i] + reg * (B.loga[ro + i] - 0.69314718055994531 * lg2);
@@ -213,6 +279,21 @@ __global__ void __launch_bounds__(kBWarps * 32) k_brow(
     }
 }
 
+// One CTA per work item; the CTAs of finished problems return at once.
+// (Persistent CTAs fetching items from a counter measured 1.8x slower on the
+// batched workload: the hardware block scheduler balances these short
+// CTAs better.)
+template <int DP>
+__global__ void __launch_bounds__(kBWarps * 32) k_brow(
+    const BatchDev B, const int2* __restrict__ items, const float2* __restrict__ as_cur,
+    const float2* __restrict__ bs, const double* __restrict__ alpha_cur, double* alpha_next,
+    float2* as_next, double* part, const int* __restrict__ done, BatchState* st, float k2,
+    double reg) {
+    const int2 it = items[blockIdx.x];
+    if (done[it.x]) return;
+    row_item<DP>(B, it, as_cur, bs, alpha_cur, alpha_next, as_next, part, st, k2, reg);
+}
+
 
 // Column half-sweep for the column blocks `items`: with the new alpha,
 // S_j = sum_i exp((alpha_i + beta_j - M_ij)/reg) and beta_j += reg (log b_j -
@@ -220,13 +301,10 @@ __global__ void __launch_bounds__(kBWarps * 32) k_brow(
 // shift). write_split = 0 skips the split (first half-sweep, before the grid
 // is known).
 template <int DP>
-__global__ void __launch_bounds__(kBWarps * 32) k_bcol(
-    const BatchDev B, const int2* __restrict__ items, const float2* __restrict__ as,
-    float2* bs, double* beta, const int* __restrict__ done, BatchState* st, float k2, double reg,
-    int write_split) {
-    const int2 it = items[blockIdx.x];
+__device__ __forceinline__ void col_item(const BatchDev& B, int2 it, const float2* __restrict__ as,
+                                         float2* bs, double* beta, BatchState* st, float k2,
+                                         double reg, int write_split) {
     const int p = it.x;
-    if (done[p]) return;
     const int n = B.n[p], m = B.m[p], d = B.d[p];
     const float sc = B.scale[p];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -235,42 +313,62 @@ __global__ void __launch_bounds__(kBWarps * 32) k_bcol(
     const float* Y = B.Y + B.yo[p];
     const int ro = B.ro[p], co = B.co[p];
 
-    float yc[kBPer][DP], bh[kBPer], bl[kBPer], mx[kBPer], sm[kBPer];
+    // columns in pairs, negated: ny[h][k] = (-y_{2h}[k], -y_{2h+1}[k])
+    float2 ny[kBPer / 2][DP], bh[kBPer / 2], bl[kBPer / 2];
+    float mx[kBPer], sm[kBPer];
 #pragma unroll
     for (int r = 0; r < kBPer; ++r) {
         const int j = j0c + r;
         const bool ok = j < m;
 #pragma unroll
-        for (int k = 0; k < DP; ++k) yc[r][k] = (ok && k < d) ? Y[(long long)j * d + k] : 0.f;
+        for (int k = 0; k < DP; ++k) {
+            const float v = (ok && k < d) ? -Y[(long long)j * d + k] : 0.f;
+            if (r & 1) ny[r >> 1][k].y = v;
+            else ny[r >> 1][k].x = v;
+        }
         const float2 s = ok ? bs[co + j] : make_float2(0.f, 0.f);
-        bh[r] = s.x;
-        bl[r] = __fmul_rn(s.y, k2);
+        const float lk = __fmul_rn(s.y, k2);
+        if (r & 1) {
+            bh[r >> 1].y = s.x;
+            bl[r >> 1].y = lk;
+        } else {
+            bh[r >> 1].x = s.x;
+            bl[r >> 1].x = lk;
+        }
         mx[r] = -INFINITY;
         sm[r] = 0.f;
     }
-    __shared__ float sx[kBTile][DP + 1];
+    const float2 sc2 = make_float2(sc, sc), k22 = make_float2(k2, k2);
+    // rows staged duplicated, (x, x), for the packed instructions
+    __shared__ float2 sx[kBTile][DP + 1];
     __shared__ float2 sa[kBTile];
     for (int i0 = 0; i0 < n; i0 += kBTile) {
         const int cnt = min(kBTile, n - i0);
         for (int e = threadIdx.x; e < kBTile * DP; e += kBWarps * 32) {
             const int ii = e / DP, k = e % DP;
-            sx[ii][k] = (ii < cnt && k < d) ? X[(long long)(i0 + ii) * d + k] : 0.f;
+            const float v = (ii < cnt && k < d) ? X[(long long)(i0 + ii) * d + k] : 0.f;
+            sx[ii][k] = make_float2(v, v);
         }
         for (int ii = threadIdx.x; ii < kBTile; ii += kBWarps * 32)
             sa[ii] = ii < cnt ? as[ro + i0 + ii] : make_float2(0.f, 0.f);
         __syncthreads();
         for (int ii = lane; ii < cnt; ii += 32) {
-            float xv[DP];
+            float2 xv[DP];
 #pragma unroll
             for (int k = 0; k < DP; ++k) xv[k] = sx[ii][k];
             const float2 ai = sa[ii];
             const float alk = __fmul_rn(ai.y, k2);
+            float z[kBPer];
 #pragma unroll
-            for (int r = 0; r < kBPer; ++r) {
+            for (int h = 0; h < kBPer / 2; ++h) {
                 // the same operations, in the same order, as the row kernel
-                const float Mv = bcost<DP>(xv, yc[r], sc);
-                lse_add(mx[r], sm[r], fmaf((ai.x + bh[r]) - Mv, k2, __fadd_rn(alk, bl[r])));
+                const float2 Mv = bcost2<DP>(xv, ny[h], sc2);
+                const float2 zz = bexpo2(make_float2(ai.x, ai.x), bh[h], make_float2(alk, alk),
+                                         bl[h], Mv, k22);
+                z[2 * h] = zz.x;
+                z[2 * h + 1] = zz.y;
             }
+            lse_add4(mx, sm, z);
         }
         __syncthreads();
     }
@@ -291,11 +389,21 @@ __global__ void __launch_bounds__(kBWarps * 32) k_bcol(
         }
     const int j = j0c + lane;
     if (lane < kBPer && j < m) {
-        const double lg2 = (double)mxr + log2((double)smr);
+        const double lg2 = (double)mxr + (double)log2f(smr);
         const double bn = beta[co + j] + reg * (B.logb[co + j] - 0.69314718055994531 * lg2);
         beta[co + j] = bn;
         if (write_split) bs[co + j] = bsplit(bn, st, &st->regrid);
     }
+}
+
+template <int DP>
+__global__ void __launch_bounds__(kBWarps * 32) k_bcol(
+    const BatchDev B, const int2* __restrict__ items, const float2* __restrict__ as, float2* bs,
+    double* beta, const int* __restrict__ done, BatchState* st, float k2, double reg,
+    int write_split) {
+    const int2 it = items[blockIdx.x];
+    if (done[it.x]) return;
+    col_item<DP>(B, it, as, bs, beta, st, k2, reg, write_split);
 }
 
 // Marginal error and stopping test of iterate k for every running problem
@@ -329,7 +437,7 @@ __global__ void k_bfin(const BatchDev B, int count, const double* part, int* don
 // Condition of the device-side loop, run once per body.
 __global__ void k_bloop(BatchState* st, cudaGraphConditionalHandle h) {
     const int loops = ++st->loops;
-    const bool go = st->active > 0 && !st->regrid && loops < st->loop_cap;
+    const bool go = st->active > st->stop_below && !st->regrid && loops < st->loop_cap;
     cudaGraphSetConditional(h, go ? 1u : 0u);
 }
 
@@ -417,15 +525,31 @@ void erot_solve_batched_gpu(regot_ctx* ctx, const regot_batch_desc* D, double re
 
     // Work items per dimension class, the longest first (rows: by m, columns:
     // by n) so that the large problems do not finish last.
-    std::vector<int> order(P);
-    for (int p = 0; p < P; ++p) order[p] = p;
+    // The lists hold the running problems only: they are rebuilt, and the
+    // sweep graph captured again, each time the number of running problems
+    // has halved, so that the last sweeps of a few slow problems do not
+    // launch a CTA for every block of every problem.
     std::vector<int2> ritems[kBClasses], citems[kBClasses];
-    std::stable_sort(order.begin(), order.end(), [&](int u, int v) { return hm[u] > hm[v]; });
-    for (int p : order)
-        for (int k = 0; k < cdiv(hn[p], kBItems); ++k) ritems[cls[p]].push_back(make_int2(p, k));
-    std::stable_sort(order.begin(), order.end(), [&](int u, int v) { return hn[u] > hn[v]; });
-    for (int p : order)
-        for (int k = 0; k < cdiv(hm[p], kBItems); ++k) citems[cls[p]].push_back(make_int2(p, k));
+    auto build_items = [&](const std::vector<int>& running) {
+        std::vector<int> order(running);
+        for (int c = 0; c < kBClasses; ++c) {
+            ritems[c].clear();
+            citems[c].clear();
+        }
+        std::stable_sort(order.begin(), order.end(), [&](int u, int v) { return hm[u] > hm[v]; });
+        for (int p : order)
+            for (int k = 0; k < cdiv(hn[p], kBItems); ++k)
+                ritems[cls[p]].push_back(make_int2(p, k));
+        std::stable_sort(order.begin(), order.end(), [&](int u, int v) { return hn[u] > hn[v]; });
+        for (int p : order)
+            for (int k = 0; k < cdiv(hm[p], kBItems); ++k)
+                citems[cls[p]].push_back(make_int2(p, k));
+    };
+    {
+        std::vector<int> all(P);
+        for (int p = 0; p < P; ++p) all[p] = p;
+        build_items(all);
+    }
 
     DBuf<int> dn, dm, dd, dro, dco, drbo;
     DBuf<long long> dxo, dyo;
@@ -440,10 +564,13 @@ void erot_solve_batched_gpu(regot_ctx* ctx, const regot_batch_desc* D, double re
     upload_vec(dyo, yo, st);
     upload_vec(dsc, hsc, st);
     DBuf<int2> dri[kBClasses], dci[kBClasses];
-    for (int c = 0; c < kBClasses; ++c) {
-        if (!ritems[c].empty()) upload_vec(dri[c], ritems[c], st);
-        if (!citems[c].empty()) upload_vec(dci[c], citems[c], st);
-    }
+    auto upload_items = [&]() {
+        for (int c = 0; c < kBClasses; ++c) {
+            if (!ritems[c].empty()) upload_vec(dri[c], ritems[c], st);
+            if (!citems[c].empty()) upload_vec(dci[c], citems[c], st);
+        }
+    };
+    upload_items();
 
     // points and marginals on the device
     DBuf<float> hX, hY;
@@ -495,9 +622,9 @@ void erot_solve_batched_gpu(regot_ctx* ctx, const regot_batch_desc* D, double re
     const float k2 = (float)(1.4426950408889634 / reg);
     auto launch_rows = [&](int q) {
         for (int c = 0; c < kBClasses; ++c) {
-            const int nb = (int)ritems[c].size();
-            if (!nb) continue;
-            const dim3 grid(nb), block(kBWarps * 32);
+            const int ni = (int)ritems[c].size();
+            if (!ni) continue;
+            const dim3 grid(ni), block(kBWarps * 32);
             if (c == 0)
                 k_brow<4><<<grid, block, 0, st>>>(B, dri[c].get(), AS[q].get(), BS.get(),
                                                   A[q].get(), A[1 - q].get(), AS[1 - q].get(),
@@ -507,17 +634,18 @@ void erot_solve_batched_gpu(regot_ctx* ctx, const regot_batch_desc* D, double re
                                                   A[q].get(), A[1 - q].get(), AS[1 - q].get(),
                                                   part.get(), done.get(), S, k2, reg);
             else
-                k_brow<16><<<grid, block, 0, st>>>(B, dri[c].get(), AS[q].get(), BS.get(),
-                                                   A[q].get(), A[1 - q].get(), AS[1 - q].get(),
-                                                   part.get(), done.get(), S, k2, reg);
+                k_brow<16><<<grid, block, 0, st>>>(B, dri[c].get(), AS[q].get(),
+                                                   BS.get(), A[q].get(), A[1 - q].get(),
+                                                   AS[1 - q].get(), part.get(), done.get(), S, k2,
+                                                   reg);
             count_launch();
         }
     };
     auto launch_cols = [&](int q, int write_split) {
         for (int c = 0; c < kBClasses; ++c) {
-            const int nb = (int)citems[c].size();
-            if (!nb) continue;
-            const dim3 grid(nb), block(kBWarps * 32);
+            const int ni = (int)citems[c].size();
+            if (!ni) continue;
+            const dim3 grid(ni), block(kBWarps * 32);
             if (c == 0)
                 k_bcol<4><<<grid, block, 0, st>>>(B, dci[c].get(), AS[q].get(), BS.get(),
                                                   beta.get(), done.get(), S, k2, reg, write_split);
@@ -525,8 +653,8 @@ void erot_solve_batched_gpu(regot_ctx* ctx, const regot_batch_desc* D, double re
                 k_bcol<8><<<grid, block, 0, st>>>(B, dci[c].get(), AS[q].get(), BS.get(),
                                                   beta.get(), done.get(), S, k2, reg, write_split);
             else
-                k_bcol<16><<<grid, block, 0, st>>>(B, dci[c].get(), AS[q].get(), BS.get(),
-                                                   beta.get(), done.get(), S, k2, reg,
+                k_bcol<16><<<grid, block, 0, st>>>(B, dci[c].get(), AS[q].get(),
+                                                   BS.get(), beta.get(), done.get(), S, k2, reg,
                                                    write_split);
             count_launch();
         }
@@ -561,54 +689,81 @@ void erot_solve_batched_gpu(regot_ctx* ctx, const regot_batch_desc* D, double re
 
     // The sweeps: a graph whose only node is a conditional WHILE node; its
     // body is two sweeps (alpha ping-pongs between A[0] and A[1]) and k_bloop.
-    BatchGraph lg;
-    REGOT_CUDA(cudaGraphCreate(&lg.graph, 0));
-    cudaGraphConditionalHandle loop_h;
-    REGOT_CUDA(cudaGraphConditionalHandleCreate(&loop_h, lg.graph, 1, cudaGraphCondAssignDefault));
-    cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
-    cp.conditional.handle = loop_h;
-    cp.conditional.type = cudaGraphCondTypeWhile;
-    cp.conditional.size = 1;
-    cudaGraphNode_t loop_node;
-    REGOT_CUDA(cudaGraphAddNode(&loop_node, lg.graph, nullptr, nullptr, 0, &cp));
-    cudaGraph_t body = cp.conditional.phGraph_out[0];
-    long long* saved_counter = g_launch_counter;
     long long body_kernels = 0;
-    g_launch_counter = &body_kernels;
     const int fin_blocks = cdiv(P, 8);
-    REGOT_CUDA(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0,
-                                             cudaStreamCaptureModeThreadLocal));
-    try {
-        for (int q = 0; q < 2; ++q) {
-            launch_rows(q);
-            k_bfin<<<fin_blocks, 256, 0, st>>>(B, P, part.get(), done.get(), iter.get(),
-                                               fpar.get(), mar.get(), max_iter, tol, S, q);
+    auto make_graph = [&](BatchGraph& lg) {
+        REGOT_CUDA(cudaGraphCreate(&lg.graph, 0));
+        cudaGraphConditionalHandle loop_h;
+        REGOT_CUDA(cudaGraphConditionalHandleCreate(&loop_h, lg.graph, 1,
+                                                    cudaGraphCondAssignDefault));
+        cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+        cp.conditional.handle = loop_h;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t loop_node;
+        REGOT_CUDA(cudaGraphAddNode(&loop_node, lg.graph, nullptr, nullptr, 0, &cp));
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        long long* saved_counter = g_launch_counter;
+        body_kernels = 0;
+        g_launch_counter = &body_kernels;
+        REGOT_CUDA(cudaStreamBeginCaptureToGraph(st, body, nullptr, nullptr, 0,
+                                                 cudaStreamCaptureModeThreadLocal));
+        try {
+            for (int q = 0; q < 2; ++q) {
+                launch_rows(q);
+                k_bfin<<<fin_blocks, 256, 0, st>>>(B, P, part.get(), done.get(), iter.get(),
+                                                   fpar.get(), mar.get(), max_iter, tol, S, q);
+                count_launch();
+                launch_cols(1 - q, 1);
+            }
+            k_bloop<<<1, 1, 0, st>>>(S, loop_h);
             count_launch();
-            launch_cols(1 - q, 1);
+        } catch (...) {
+            cudaGraph_t g = nullptr;
+            cudaStreamEndCapture(st, &g);
+            g_launch_counter = saved_counter;
+            throw;
         }
-        k_bloop<<<1, 1, 0, st>>>(S, loop_h);
-        count_launch();
-    } catch (...) {
-        cudaGraph_t g = nullptr;
-        cudaStreamEndCapture(st, &g);
+        REGOT_CUDA(cudaStreamEndCapture(st, &body));
         g_launch_counter = saved_counter;
-        throw;
-    }
-    REGOT_CUDA(cudaStreamEndCapture(st, &body));
-    g_launch_counter = saved_counter;
-    REGOT_CUDA(cudaGraphInstantiate(&lg.exec, lg.graph, 0));
+        REGOT_CUDA(cudaGraphInstantiate(&lg.exec, lg.graph, 0));
+    };
+    auto set_stop_below = [&](int v) {
+        h2d(&S->stop_below, &v, sizeof(int), st);
+    };
+    std::vector<int> stop_host(1, P > 16 ? P / 2 : 0);
+    set_stop_below(stop_host[0]);
+    std::unique_ptr<BatchGraph> lg(new BatchGraph());
+    make_graph(*lg);
 
     BatchState hs{};
     int prev_loops = 0;
     for (;;) {
-        REGOT_CUDA(cudaGraphLaunch(lg.exec, st));
+        REGOT_CUDA(cudaGraphLaunch(lg->exec, st));
         read_small(ctx, &hs, S, sizeof(hs), st);
         count_launch(body_kernels * (hs.loops - prev_loops));
         prev_loops = hs.loops;
         if (hs.active == 0) break;
-        if (!hs.regrid || hs.loops >= hs.loop_cap)
-            throw Error(REGOT_ERR_NUMERIC, "batched BCD did not terminate");
-        regrid(0);  // at a body boundary the running problems' alpha is in A[0]
+        if (hs.loops >= hs.loop_cap) throw Error(REGOT_ERR_NUMERIC, "batched BCD did not terminate");
+        bool acted = false;
+        if (hs.regrid) {
+            regrid(0);  // at a body boundary the running problems' alpha is in A[0]
+            acted = true;
+        }
+        if (hs.active <= stop_host[0]) {
+            std::vector<int> hdone(P), running;
+            read_small(ctx, hdone.data(), done.get(), P * sizeof(int), st);
+            for (int p = 0; p < P; ++p)
+                if (!hdone[p]) running.push_back(p);
+            build_items(running);
+            upload_items();
+            stop_host[0] = hs.active > 16 ? hs.active / 2 : 0;
+            set_stop_below(stop_host[0]);
+            lg.reset(new BatchGraph());
+            make_graph(*lg);
+            acted = true;
+        }
+        if (!acted) throw Error(REGOT_ERR_NUMERIC, "batched BCD did not terminate");
     }
     REGOT_CUDA(cudaEventRecord(e1, st));
 
