@@ -157,6 +157,12 @@ int regot_sinkhorn_apdagd(regot_ctx* ctx, regot_dproblem* prob, double reg, doub
 /* qrot_lbfgs_dual (src/qrot_lbfgs_dual.cpp:81-126). */
 int regot_qrot_lbfgs_dual(regot_ctx* ctx, regot_dproblem* prob, double reg, double tol,
                           int max_iter, const regot_opts* opts, regot_result* res);
+/* qrot_bcd (src/qrot_bcd.cpp:14-103): exact alternating minimisation. */
+int regot_qrot_bcd(regot_ctx* ctx, regot_dproblem* prob, double reg, double tol, int max_iter,
+                   const regot_opts* opts, regot_result* res);
+/* qrot_gd (src/qrot_gd.cpp:14-120): gradient descent with Armijo backtracking. */
+int regot_qrot_gd(regot_ctx* ctx, regot_dproblem* prob, double reg, double tol, int max_iter,
+                  const regot_opts* opts, regot_result* res);
 /* qrot_assn (src/qrot_assn.cpp:16-170). */
 int regot_qrot_assn(regot_ctx* ctx, regot_dproblem* prob, double reg, double tol,
                     int max_iter, const regot_opts* opts, regot_result* res);
@@ -258,6 +264,9 @@ int regot_qrot_dual_obj_grad(regot_ctx* ctx, regot_dproblem* prob, double reg,
 /* QROT Problem::optimal_beta (src/qrot_problem.cpp:397-404). */
 int regot_qrot_optimal_beta(regot_ctx* ctx, regot_dproblem* prob, double reg,
                             const double* alpha, double* beta);
+/* QROT Problem::optimal_alpha (src/qrot_problem.cpp:409-419). */
+int regot_qrot_optimal_alpha(regot_ctx* ctx, regot_dproblem* prob, double reg,
+                             const double* beta, double* alpha);
 /* QROT Problem::primal_val (src/qrot_problem.cpp:10-24, src/approx_proj.h:6-26). */
 int regot_qrot_primal_val(regot_ctx* ctx, regot_dproblem* prob, double reg,
                           const double* gamma, double* value);

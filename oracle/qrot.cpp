@@ -101,6 +101,15 @@ static void optimal_beta(const Problem& p, const double* alpha, double* beta) {
     }
 }
 
+// optimal_alpha: qrot_problem.cpp:409-419, the row analogue.
+static void optimal_alpha(const Problem& p, const double* beta, double* alpha) {
+    std::vector<double> y(p.m);
+    for (int i = 0; i < p.n; i++) {
+        for (int j = 0; j < p.m; j++) y[j] = p.Mij(i, j) - beta[j];
+        alpha[i] = piecewise_linear_equation(y, p.reg * p.a[i]);
+    }
+}
+
 // primal_val: qrot_problem.cpp:10-24 with approx_proj (approx_proj.h:6-26).
 static double primal_val(const Problem& p, const double* gamma) {
     const int n = p.n, m = p.m;
@@ -362,6 +371,12 @@ double oracle_qrot_dual_obj_grad(const double* M, int n, int m, const double* a,
     return dual_obj_grad(make_problem(M, n, m, a, b, reg, tau), gamma, grad);
 }
 
+void oracle_qrot_optimal_alpha(const double* M, int n, int m, const double* a, double reg,
+                               const double* beta, double* alpha) {
+    Problem p = make_problem(M, n, m, a, a, reg, 0.0);
+    optimal_alpha(p, beta, alpha);
+}
+
 void oracle_qrot_optimal_beta(const double* M, int n, int m, const double* b, double reg,
                               const double* alpha, double* beta) {
     Problem p = make_problem(M, n, m, nullptr, b, reg, 0.0);
@@ -388,6 +403,95 @@ int oracle_qrot_hess_cg(const double* M, int n, int m, const double* gamma, cons
 void oracle_qrot_plan(const double* M, int n, int m, double reg, const double* gamma,
                       double* plan) {
     get_plan(make_problem(M, n, m, nullptr, nullptr, reg, 0.0), gamma, plan);
+}
+
+// qrot_bcd_internal: qrot_bcd.cpp:14-103 (block coordinate descent: alpha
+// then beta exactly; the problem is built with tau = 0).
+int oracle_qrot_bcd(const double* M, int n, int m, const double* a, const double* b, double reg,
+                    double tol, int max_iter, int verbose, const oracle_opts* opts,
+                    oracle_result* res) {
+    try {
+        Problem p = make_problem(M, n, m, a, b, reg, 0.0);
+        Vec gamma, grad(n + m);
+        init_gamma(p, opts, gamma);
+        History h(res);
+        Timer timer;
+        timer.tic();
+        double f = dual_obj_grad(p, gamma.data(), grad.data());
+        double gnorm = norm(grad);
+        h.push(f, gnorm / reg, timer.toc(), 0.0, primal_val(p, gamma.data()));
+        int i;
+        for (i = 0; i < max_iter; i++) {
+            if (verbose >= 1)
+                std::printf("iter = %d, objval = %g, ||grad|| = %g\n", i, f, gnorm);
+            timer.tic();
+            if (gnorm < tol) break;
+            optimal_alpha(p, gamma.data() + n, gamma.data());
+            optimal_beta(p, gamma.data(), gamma.data() + n);
+            f = dual_obj_grad(p, gamma.data(), grad.data());
+            gnorm = norm(grad);
+            const double d = timer.toc();
+            h.push(f, gnorm / reg, h.last_time() + d, 0.0, primal_val(p, gamma.data()));
+        }
+        res->niter = i;
+        res->hist_len = h.len;
+        std::copy(gamma.begin(), gamma.end(), res->dual);
+        if (res->plan) get_plan(p, gamma.data(), res->plan);
+        return 0;
+    } catch (const std::exception& e) {
+        set_err(res, e.what());
+        return 1;
+    }
+}
+
+// qrot_gd_internal: qrot_gd.cpp:14-120 (gradient descent with Armijo
+// backtracking: theta = kappa = 0.5, at most 20 trials; the last trial is
+// kept when none is accepted).
+int oracle_qrot_gd(const double* M, int n, int m, const double* a, const double* b, double reg,
+                   double tol, int max_iter, int verbose, const oracle_opts* opts,
+                   oracle_result* res) {
+    try {
+        constexpr double theta = 0.5, kappa = 0.5;
+        constexpr int nlinesearch = 20;
+        const double tau = opts ? opts->tau : 0.0;
+        Problem p = make_problem(M, n, m, a, b, reg, tau);
+        Vec gamma, newgamma(n + m), grad(n + m);
+        init_gamma(p, opts, gamma);
+        History h(res);
+        Timer timer;
+        timer.tic();
+        double f = dual_obj_grad(p, gamma.data(), grad.data());
+        double gnorm = norm(grad);
+        h.push(f, gnorm / reg, timer.toc(), 0.0, primal_val(p, gamma.data()));
+        int i;
+        for (i = 0; i < max_iter; i++) {
+            if (verbose >= 1)
+                std::printf("iter = %d, objval = %g, ||grad|| = %g\n", i, f, gnorm);
+            timer.tic();
+            if (gnorm < tol) break;
+            double step = 1.0;
+            const double thresh = theta * gnorm * gnorm;
+            for (int k = 0; k < nlinesearch; k++) {
+                for (int q = 0; q < n + m; q++) newgamma[q] = gamma[q] - step * grad[q];
+                const double newf = dual_obj(p, newgamma.data());
+                if (newf <= f - step * thresh) break;
+                step *= kappa;
+            }
+            gamma.swap(newgamma);
+            f = dual_obj_grad(p, gamma.data(), grad.data());
+            gnorm = norm(grad);
+            const double d = timer.toc();
+            h.push(f, gnorm / reg, h.last_time() + d, 0.0, primal_val(p, gamma.data()));
+        }
+        res->niter = i;
+        res->hist_len = h.len;
+        std::copy(gamma.begin(), gamma.end(), res->dual);
+        if (res->plan) get_plan(p, gamma.data(), res->plan);
+        return 0;
+    } catch (const std::exception& e) {
+        set_err(res, e.what());
+        return 1;
+    }
 }
 
 // qrot_lbfgs_dual_internal: qrot_lbfgs_dual.cpp:81-126 (QROTDual 18-79).

@@ -179,6 +179,25 @@ def qrot_lbfgs_dual(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
                 _QROT_DUAL, 0, with_prim=True, plan=kwargs.get("plan", True))
 
 
+def qrot_bcd(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
+    return _run(lib().oracle_qrot_bcd, M, a, b, reg, tol, max_iter, verbose, kwargs,
+                _QROT_DUAL, 0, with_prim=True, plan=kwargs.get("plan", True))
+
+
+def qrot_gd(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
+    return _run(lib().oracle_qrot_gd, M, a, b, reg, tol, max_iter, verbose, kwargs,
+                _QROT_DUAL, 0, with_prim=True, plan=kwargs.get("plan", True))
+
+
+def qrot_optimal_alpha(M, a, reg, beta):
+    M = _colmajor(M)
+    n, m = M.shape
+    alpha = np.zeros(n)
+    lib().oracle_qrot_optimal_alpha(_d(M), n, m, _d(_f64(a)), C.c_double(reg), _d(_f64(beta)),
+                                    _d(alpha))
+    return alpha
+
+
 def qrot_assn(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
     return _run(lib().oracle_qrot_assn, M, a, b, reg, tol, max_iter, verbose, kwargs,
                 _QROT_DUAL, 0, with_prim=True, plan=kwargs.get("plan", True))

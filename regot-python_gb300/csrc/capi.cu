@@ -451,6 +451,8 @@ REGOT_SOLVER_ENTRY(regot_sinkhorn_lbfgs_dual, sinkhorn_lbfgs_dual_gpu, P->n + P-
 REGOT_SOLVER_ENTRY(regot_sinkhorn_apdagd, sinkhorn_apdagd_gpu, P->n + P->m - 1)
 REGOT_SOLVER_ENTRY(regot_qrot_lbfgs_dual, qrot_lbfgs_dual_gpu, P->n + P->m)
 REGOT_SOLVER_ENTRY(regot_qrot_assn, qrot_assn_gpu, P->n + P->m)
+REGOT_SOLVER_ENTRY(regot_qrot_bcd, qrot_bcd_gpu, P->n + P->m)
+REGOT_SOLVER_ENTRY(regot_qrot_gd, qrot_gd_gpu, P->n + P->m)
 
 // ---------------------------------------------------------------- passes --
 

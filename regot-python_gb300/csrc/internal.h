@@ -90,6 +90,7 @@ enum PassOp : int {
     OP_E_AVG,         // averaged plan X <- (1 - s) X + s T (X = T when nsteps == 0), X at
                       // xavg (TM, row-major, stride m): rows/cols sum X; totals sum M X,
                       // sum X (1 - log X)
+    OP_Q_ROWROOT,     // rows: count and sum of y = M - cb below ra (FP64), optimal_alpha
     OP_COUNT
 };
 

@@ -173,7 +173,8 @@ template <> struct Vec<double> {
 __host__ __device__ constexpr int op_nr(int op) {
     return op == OP_E_ROW ? 1 : op == OP_E_ROWCOL ? 1 : op == OP_E_HVP ? 1 : op == OP_E_ROWMAX ? 1
          : op == OP_Q_GRAD ? 1 : op == OP_Q_GRADMASK ? 2 : op == OP_Q_P1 ? 1 : op == OP_Q_P3 ? 3
-         : op == OP_Q_GRADLS ? 1 : op == OP_E_GRADLS ? 1 : op == OP_E_AVG ? 1 : 0;
+         : op == OP_Q_GRADLS ? 1 : op == OP_E_GRADLS ? 1 : op == OP_E_AVG ? 1
+         : op == OP_Q_ROWROOT ? 2 : 0;
 }
 __host__ __device__ constexpr int op_nc(int op) {
     return op == OP_E_COL ? 1 : op == OP_E_ROWCOL ? 1 : op == OP_E_HVP ? 1 : op == OP_E_COLMAX ? 1
@@ -184,6 +185,10 @@ __host__ __device__ constexpr int op_nt(int op) {
     return op == OP_E_LS ? 4 : op == OP_Q_GRAD ? 1 : op == OP_Q_GRADMASK ? 1 : op == OP_Q_OBJ ? 1
          : op == OP_Q_P3 ? 2 : op == OP_Q_GRADLS ? 2 : op == OP_E_GRADLS ? 1 : op == OP_E_AVG ? 2
          : 0;
+}
+// Root-finding passes accumulate in FP64 in both storage modes.
+__host__ __device__ constexpr bool op_fp64_acc(int op) {
+    return op == OP_Q_COLROOT || op == OP_Q_ROWROOT;
 }
 __host__ __device__ constexpr bool op_is_erot(int op) {
     return op <= OP_E_COLMAX || op == OP_E_GRADLS || op == OP_E_AVG;
@@ -338,7 +343,9 @@ __global__ void __launch_bounds__(kThreads, 2) dense_pass(const PassParams p) {
     constexpr int VW = G::VW, LC = G::LC, CW = G::CW, NV = LC / VW;
     constexpr bool MIXED = std::is_same<TM, float>::value;
     constexpr bool COLROOT = (OP == OP_Q_COLROOT);
-    using Acc = typename std::conditional<COLROOT, double, TM>::type;
+    constexpr bool ROWROOT = (OP == OP_Q_ROWROOT);
+    constexpr bool ROOT = COLROOT || ROWROOT;
+    using Acc = typename std::conditional<ROOT, double, TM>::type;
     using VT = typename Vec<TM>::type;
     constexpr int NR = op_nr(OP), NC = op_nc(OP), NT = op_nt(OP);
     constexpr int NRa = NR > 0 ? NR : 1, NCa = NC > 0 ? NC : 1, NTa = NT > 0 ? NT : 1;
@@ -370,7 +377,7 @@ __global__ void __launch_bounds__(kThreads, 2) dense_pass(const PassParams p) {
     float4* s_rowp = s_colp + 2 * CW;                                      // [2][kRB]
     float* s_cdp = reinterpret_cast<float*>(s_rowp + 2 * kRB);             // [2][CW] (LS only)
     __shared__ __align__(8) uint64_t s_pbar[2];
-    constexpr bool STAGE_PARAMS = MIXED && !COLROOT;
+    constexpr bool STAGE_PARAMS = MIXED && !ROOT;
 
     if (STAGE_PARAMS && threadIdx.x == 0) {
         mbar_init(&s_pbar[0], 1);
@@ -470,7 +477,7 @@ __global__ void __launch_bounds__(kThreads, 2) dense_pass(const PassParams p) {
         // ---- per-column parameters of this slab (only what OP uses) ----
         TM ch[LC], clk[LC], cxv[op_uses_cx(OP) ? LC : 1], cx2v[op_uses_cx2(OP) ? LC : 1],
             cdv[op_uses_cd(OP) ? LC : 1];
-        double cbd[COLROOT ? LC : 1];
+        double cbd[ROOT ? LC : 1];
         bool cvalid[LC];
 #pragma unroll
         for (int q = 0; q < LC; ++q) {
@@ -478,7 +485,7 @@ __global__ void __launch_bounds__(kThreads, 2) dense_pass(const PassParams p) {
             const int j = c0 + (v * 32 + lane) * VW + e;
             const bool ok = j < m;
             cvalid[q] = ok;
-            if constexpr (COLROOT) {
+            if constexpr (ROOT) {
                 cbd[q] = ok ? p.cb[j] : -INFINITY;
                 ch[q] = 0;
                 clk[q] = 0;
@@ -542,7 +549,7 @@ __global__ void __launch_bounds__(kThreads, 2) dense_pass(const PassParams p) {
 #pragma unroll
                 for (int v = 0; v < NV; ++v) mvp[r2][v] = Vec<TM>::zero();
                 if (i < n) {
-                    if constexpr (COLROOT) {
+                    if constexpr (ROOT) {
                         prad[r2] = p.ra ? p.ra[i] : 0.0;
                     } else if constexpr (MIXED) {
                         const float4 r = p.rsplit ? s_rowp[(k & 1) * kRB + (i - r0)]
@@ -648,6 +655,12 @@ __global__ void __launch_bounds__(kThreads, 2) dense_pass(const PassParams p) {
                             if (cvalid[q] && y < cbd[q]) {
                                 cacc[0][q] += 1.0;
                                 cacc[1][q] += y;
+                            }
+                        } else if constexpr (ROWROOT) {
+                            const double y = (double)mval - cbd[q];
+                            if (cvalid[q] && y < rad) {
+                                racc[0] += 1.0;
+                                racc[1] += y;
                             }
                         } else if constexpr (EROT) {
                             // T = 2^((ra_i + cb_j - M_ij) log2(e) / reg): exact hi sum,
@@ -879,7 +892,7 @@ __global__ void k_split(const PassParams p, float4* rs, float4* cs, float* cds) 
 
 template <typename TM, int OP>
 void launch_one(const PassParams& p, cudaStream_t st) {
-    using Acc = typename std::conditional<OP == OP_Q_COLROOT, double, TM>::type;
+    using Acc = typename std::conditional<op_fp64_acc(OP), double, TM>::type;
     constexpr int CW = Geo<TM>::CW;
     constexpr int NS = ring_stages<OP, Acc, CW>();
     constexpr size_t smem = (size_t)kWarps * NS * CW * sizeof(TM) +
@@ -904,7 +917,7 @@ void launch_one(const PassParams& p, cudaStream_t st) {
 
 template <typename TM, int OP>
 int occupancy_of() {
-    using Acc = typename std::conditional<OP == OP_Q_COLROOT, double, TM>::type;
+    using Acc = typename std::conditional<op_fp64_acc(OP), double, TM>::type;
     constexpr int CW = Geo<TM>::CW;
     constexpr int NS = ring_stages<OP, Acc, CW>();
     constexpr size_t smem = (size_t)kWarps * NS * CW * sizeof(TM) +

@@ -127,6 +127,21 @@ __global__ void k_root_update(const double* cp, int nrb, int m, const double* b,
     }
 }
 
+// Row analogue for optimal_alpha (qrot_problem.cpp:409-419): rows' count
+// and sum of y = M_ij - beta_j below the current root x_i.
+__global__ void k_rowroot_update(const double* rp, int nslabs, int n, const double* a, double reg,
+                                 double* x, double* prev_cnt, QState* st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double cnt = merge_strided(rp + i, nslabs, (size_t)n);
+    const double sum = merge_strided(rp + (size_t)nslabs * n + i, nslabs, (size_t)n);
+    if (cnt != prev_cnt[i]) {
+        prev_cnt[i] = cnt;
+        x[i] = (reg * a[i] + sum) / cnt;
+        atomicOr(&st->changed, 1);
+    }
+}
+
 // ---- primal value (approx_proj) ----
 // P1 merge: x_i = min(a_i / (rowsum(D)_i / reg), 1)
 template <typename Acc>
@@ -534,6 +549,36 @@ public:
         throw Error(REGOT_ERR_NUMERIC, "optimal_beta did not converge");
     }
 
+    // alpha = optimal_alpha(beta) (qrot_problem.cpp:409-419), into alpha
+    // (device): Newton's method from above on each row's piecewise-linear
+    // equation, one OP_Q_ROWROOT pass per round, as optimal_beta for columns.
+    void optimal_alpha(const double* beta, double* alpha) {
+        double* prev = vec_.get();
+        const int gn = cdiv(n_, kVT);
+        k_root_init<<<gn, kVT, 0, st_>>>(n_, alpha, prev);
+        count_launch();
+        PassParams p = ops_.base_params();
+        p.ra = alpha;
+        p.cb = beta;
+        const PassShape sh = ops_.buf().shape;
+        for (int it = 0; it <= m_ + 1; ++it) {
+            const int zero = 0;
+            h2d(&state_.get()->changed, &zero, sizeof(int), st_);
+            ops_.pass(OP_Q_ROWROOT, p);
+            k_rowroot_update<<<gn, kVT, 0, st_>>>((const double*)ops_.buf().rowpart.get(),
+                                                   sh.nslabs, n_, P_->a, reg_, alpha, prev,
+                                                   state_.get());
+            count_launch();
+            REGOT_CHECK_LAUNCH();
+            int changed = 0;
+            d2h(&changed, &state_.get()->changed, sizeof(int), st_);
+            sync(st_);
+            ++passes_;
+            if (!changed) return;
+        }
+        throw Error(REGOT_ERR_NUMERIC, "optimal_alpha did not converge");
+    }
+
     // sigma x (n) with optional division by (h1 + mu)
     void sigma_rows(const double* x, double mu, bool divide, double* out, const int* done) {
         const int warps = 8;
@@ -900,6 +945,152 @@ void qrot_assn_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, in
     finish_qrot(E, E.gamma(), hobj, hmar, htime, hprim, i, o, res);
 }
 
+namespace {
+
+// Initial value shared by qrot_bcd and qrot_gd: x0, or (0, optimal_beta(0)).
+void qrot_initial(QrotEngine& E, const regot_opts& o, int n, int m) {
+    cudaStream_t st = E.stream();
+    if (o.x0 && o.x0_len == n + m) {
+        h2d(E.gamma(), o.x0, (n + m) * sizeof(double), st);
+        return;
+    }
+    REGOT_CUDA(cudaMemsetAsync(E.gamma(), 0, n * sizeof(double), st));
+    E.optimal_beta(E.gamma(), E.gamma() + n);
+}
+
+double host_norm(const std::vector<double>& g) {
+    double s = 0.0;
+    for (double v : g) s += v * v;
+    return std::sqrt(s);
+}
+
+}  // namespace
+
+// qrot_bcd_internal: qrot_bcd.cpp:14-103. alpha = optimal_alpha(beta), then
+// beta = optimal_beta(alpha), each by Newton's method from above on the
+// device (OP_Q_ROWROOT / OP_Q_COLROOT passes); the problem has tau = 0.
+void qrot_bcd_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
+                  const regot_opts& o, regot_result* res) {
+    cudaStream_t st = ctx->stream;
+    const int n = P->n, m = P->m, N = n + m;
+    QrotEngine E(P, reg, 0.0, st);
+    DevClock clock(st);
+    qrot_initial(E, o, n, m);
+    std::vector<double> g(N), hobj, hmar, htime, hprim;
+    auto grad = [&]() {
+        const double f = E.eval(E.gamma(), E.grad(), false);
+        d2h(g.data(), E.grad(), N * sizeof(double), st);
+        sync(st);
+        return f;
+    };
+    double t0 = clock.now_ms();
+    double f = grad();
+    double gnorm = host_norm(g);
+    hobj.push_back(f);
+    hmar.push_back(gnorm / reg);
+    htime.push_back(clock.now_ms() - t0);
+    hprim.push_back(o.prim_vals ? E.primal(E.gamma()) : 0.0);
+    int i;
+    for (i = 0; i < max_iter; i++) {
+        if (o.verbose >= 1) std::printf("iter = %d, objval = %g, ||grad|| = %g\n", i, f, gnorm);
+        t0 = clock.now_ms();
+        if (gnorm < tol) break;
+        E.optimal_alpha(E.gamma() + n, E.gamma());
+        E.optimal_beta(E.gamma(), E.gamma() + n);
+        f = grad();
+        gnorm = host_norm(g);
+        const double dur = clock.now_ms() - t0;
+        hobj.push_back(f);
+        hmar.push_back(gnorm / reg);
+        htime.push_back(htime.back() + dur);
+        hprim.push_back(o.prim_vals ? E.primal(E.gamma()) : 0.0);
+    }
+    finish_qrot(E, E.gamma(), hobj, hmar, htime, hprim, i, o, res);
+}
+
+// qrot_gd_internal: qrot_gd.cpp:14-120. Armijo backtracking along -g
+// (theta = kappa = 0.5, <= 20 trials, the last trial kept if none passes).
+// Mixed precision tests newf - f <= -step theta |g|^2 on the exact change
+// step g'd + sum rem (+ tau term) of the trial pass OP_Q_GRADLS; FP64
+// evaluates newf directly, as the reference does.
+void qrot_gd_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
+                 const regot_opts& o, regot_result* res) {
+    cudaStream_t st = ctx->stream;
+    const int n = P->n, m = P->m, N = n + m;
+    const bool mixed = P->prec == REGOT_PREC_MIXED;
+    constexpr double theta = 0.5, kappa = 0.5;
+    constexpr int nlinesearch = 20;
+    QrotEngine E(P, reg, o.tau, st);
+    DevClock clock(st);
+    qrot_initial(E, o, n, m);
+    std::vector<double> gamma(N), newgamma(N), g(N), d(N), hobj, hmar, htime, hprim;
+    d2h(gamma.data(), E.gamma(), N * sizeof(double), st);
+    sync(st);
+    DBuf<double> xp_d(N, st), d_d(N, st);
+    // f and the full gradient (tau term included) at the device gamma
+    auto grad = [&]() {
+        const double f = E.eval(E.gamma(), E.grad(), false);
+        d2h(g.data(), E.grad(), N * sizeof(double), st);
+        sync(st);
+        if (E.tau_grad() != 0.0) {
+            for (int q = 0; q < n; ++q) g[q] += E.tau_grad();
+            for (int q = 0; q < m; ++q) g[n + q] -= E.tau_grad();
+        }
+        return f;
+    };
+    double t0 = clock.now_ms();
+    double f = grad();
+    double gnorm = host_norm(g);
+    hobj.push_back(f);
+    hmar.push_back(gnorm / reg);
+    htime.push_back(clock.now_ms() - t0);
+    hprim.push_back(o.prim_vals ? E.primal(E.gamma()) : 0.0);
+    int i;
+    for (i = 0; i < max_iter; i++) {
+        if (o.verbose >= 1) std::printf("iter = %d, objval = %g, ||grad|| = %g\n", i, f, gnorm);
+        t0 = clock.now_ms();
+        if (gnorm < tol) break;
+        double step = 1.0;
+        const double g2 = gnorm * gnorm, thresh = theta * g2;
+        if (mixed) {
+            for (int q = 0; q < N; ++q) d[q] = -g[q];
+            h2d(xp_d.get(), gamma.data(), N * sizeof(double), st);
+            h2d(d_d.get(), d.data(), N * sizeof(double), st);
+        }
+        for (int k = 0; k < nlinesearch; k++) {
+            for (int q = 0; q < N; ++q) newgamma[q] = gamma[q] - step * g[q];
+            bool ok;
+            if (mixed) {
+                double sq = 0.0;
+                double change = -step * g2 + E.eval_step(xp_d.get(), d_d.get(), step, &sq);
+                if (o.tau > 0.0) {
+                    double e = 0.0;
+                    for (int q = 0; q < n; ++q) e += d[q];
+                    for (int q = 0; q < m; ++q) e -= d[n + q];
+                    change += 0.5 * o.tau * step * step * e * e;
+                }
+                ok = change <= -step * thresh;
+            } else {
+                h2d(E.gamma(), newgamma.data(), N * sizeof(double), st);
+                const double newf = E.eval(E.gamma(), E.grad(), false);
+                ok = newf <= f - step * thresh;
+            }
+            if (ok) break;
+            step *= kappa;
+        }
+        gamma.swap(newgamma);
+        h2d(E.gamma(), gamma.data(), N * sizeof(double), st);
+        f = grad();
+        gnorm = host_norm(g);
+        const double dur = clock.now_ms() - t0;
+        hobj.push_back(f);
+        hmar.push_back(gnorm / reg);
+        htime.push_back(htime.back() + dur);
+        hprim.push_back(o.prim_vals ? E.primal(E.gamma()) : 0.0);
+    }
+    finish_qrot(E, E.gamma(), hobj, hmar, htime, hprim, i, o, res);
+}
+
 }  // namespace regot
 
 // ------------------------------------------------------- pass-level C ABI --
@@ -953,6 +1144,19 @@ int regot_qrot_optimal_beta(regot_ctx* ctx, regot_dproblem* P, double reg, const
         h2d(E.gamma(), alpha, P->n * sizeof(double), ctx->stream);
         E.optimal_beta(E.gamma(), E.gamma() + P->n);
         d2h(beta, E.gamma() + P->n, P->m * sizeof(double), ctx->stream);
+        E.ops().check_err();
+    });
+}
+
+int regot_qrot_optimal_alpha(regot_ctx* ctx, regot_dproblem* P, double reg, const double* beta,
+                             double* alpha) {
+    return qguard(ctx, [&] {
+        require(P && alpha && beta, "NULL argument");
+        require(reg > 0.0, "reg must be positive");
+        QrotEngine E(P, reg, 0.0, ctx->stream);
+        h2d(E.gamma() + P->n, beta, P->m * sizeof(double), ctx->stream);
+        E.optimal_alpha(E.gamma() + P->n, E.gamma());
+        d2h(alpha, E.gamma(), P->n * sizeof(double), ctx->stream);
         E.ops().check_err();
     });
 }

@@ -35,6 +35,10 @@ void erot_hess_solve_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, const do
                          const double* rhs, double tol, int max_iter, double* x, int* iters);
 void qrot_lbfgs_dual_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
                          const regot_opts& o, regot_result* res);
+void qrot_bcd_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
+                  const regot_opts& o, regot_result* res);
+void qrot_gd_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
+                 const regot_opts& o, regot_result* res);
 void qrot_assn_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
                    const regot_opts& o, regot_result* res);
 

@@ -37,7 +37,8 @@ from . import _lib as L
 
 __all__ = [
     "sinkhorn_bcd", "sinkhorn_newton", "sinkhorn_ssns", "sinkhorn_lbfgs_dual", "sinkhorn_apdagd",
-    "qrot_lbfgs_dual", "qrot_assn", "sinkhorn_result", "qrot_result", "Problem",
+    "qrot_lbfgs_dual", "qrot_assn", "qrot_bcd", "qrot_gd", "sinkhorn_result", "qrot_result",
+    "Problem",
     "sinkhorn_bcd_batched", "batch_result",
 ]
 
@@ -255,6 +256,12 @@ class Problem:
     def qrot_assn(self, reg, tol=1e-6, max_iter=1000, verbose=0, **kw):
         return self._solve("regot_qrot_assn", reg, tol, max_iter, verbose, kw, True)
 
+    def qrot_bcd(self, reg, tol=1e-6, max_iter=1000, verbose=0, **kw):
+        return self._solve("regot_qrot_bcd", reg, tol, max_iter, verbose, kw, True)
+
+    def qrot_gd(self, reg, tol=1e-6, max_iter=1000, verbose=0, **kw):
+        return self._solve("regot_qrot_gd", reg, tol, max_iter, verbose, kw, True)
+
     # ---- pass-level calls --------------------------------------------
     def _vec(self, x, size):
         x = np.ascontiguousarray(np.asarray(x, dtype=np.float64).ravel())
@@ -399,6 +406,13 @@ class Problem:
             self.ctx.handle, self.handle, float(reg), alpha.ctypes.data, out.ctypes.data))
         return out
 
+    def qrot_optimal_alpha(self, reg, beta):
+        beta = self._vec(beta, self.m)
+        out = np.zeros(self.n)
+        self.ctx.check(self._lib.regot_qrot_optimal_alpha(
+            self.ctx.handle, self.handle, float(reg), beta.ctypes.data, out.ctypes.data))
+        return out
+
     def qrot_primal_val(self, reg, gamma):
         gamma = self._vec(gamma, self.n + self.m)
         out = np.zeros(1)
@@ -452,6 +466,16 @@ def sinkhorn_apdagd(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
 def qrot_lbfgs_dual(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
     """L-BFGS on the QROT dual; reference src/qrot_lbfgs_dual.cpp:81-126."""
     return _solve("qrot_lbfgs_dual", M, a, b, reg, tol, max_iter, verbose, kwargs)
+
+
+def qrot_bcd(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
+    """Block coordinate descent for QROT; reference src/qrot_bcd.cpp:14-103."""
+    return _solve("qrot_bcd", M, a, b, reg, tol, max_iter, verbose, kwargs)
+
+
+def qrot_gd(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
+    """Gradient descent for QROT; reference src/qrot_gd.cpp:14-120."""
+    return _solve("qrot_gd", M, a, b, reg, tol, max_iter, verbose, kwargs)
 
 
 def qrot_assn(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):

@@ -113,7 +113,8 @@ EXPORTS = [
     "regot_ctx_set_stream", "regot_ctx_own_stream", "regot_ctx_kernel_launches", "regot_problem_create",
     "regot_problem_destroy", "regot_sinkhorn_bcd", "regot_sinkhorn_newton",
     "regot_sinkhorn_ssns", "regot_sinkhorn_lbfgs_dual", "regot_sinkhorn_apdagd",
-    "regot_qrot_lbfgs_dual", "regot_qrot_assn", "regot_erot_optimal_beta", "regot_erot_optimal_alpha", "regot_erot_dual_obj_grad",
+    "regot_qrot_lbfgs_dual", "regot_qrot_assn", "regot_qrot_bcd", "regot_qrot_gd",
+    "regot_qrot_optimal_alpha", "regot_erot_optimal_beta", "regot_erot_optimal_alpha", "regot_erot_dual_obj_grad",
     "regot_erot_hvp", "regot_erot_plan", "regot_erot_sparsify", "regot_erot_hess_solve",
     "regot_erot_tyy", "regot_erot_solve_batched", "regot_qrot_dual_obj_grad",
     "regot_qrot_optimal_beta",
@@ -154,7 +155,8 @@ def load() -> C.CDLL:
         lib.regot_problem_destroy.restype = None
         for name in ("regot_sinkhorn_bcd", "regot_sinkhorn_newton", "regot_sinkhorn_ssns",
                      "regot_sinkhorn_lbfgs_dual", "regot_sinkhorn_apdagd",
-                     "regot_qrot_lbfgs_dual", "regot_qrot_assn"):
+                     "regot_qrot_lbfgs_dual", "regot_qrot_assn", "regot_qrot_bcd",
+                     "regot_qrot_gd"):
             f = getattr(lib, name)
             f.argtypes = [vp, vp, C.c_double, C.c_double, C.c_int, C.POINTER(Opts),
                           C.POINTER(Result)]
@@ -169,6 +171,7 @@ def load() -> C.CDLL:
         lib.regot_qrot_optimal_beta.argtypes = [vp, vp, C.c_double, vp, vp]
         lib.regot_qrot_primal_val.argtypes = [vp, vp, C.c_double, vp, vp]
         lib.regot_qrot_plan.argtypes = [vp, vp, C.c_double, vp, vp, C.c_int]
+        lib.regot_qrot_optimal_alpha.argtypes = [vp, vp, C.c_double, vp, vp]
         lib.regot_time_pass.argtypes = [vp, vp, C.c_int, C.c_double, C.c_int]
         lib.regot_erot_solve_batched.argtypes = [vp, C.POINTER(BatchDesc), C.c_double,
                                                  C.c_double, C.c_int, C.POINTER(BatchResult)]
