@@ -163,6 +163,22 @@ int regot_qrot_bcd(regot_ctx* ctx, regot_dproblem* prob, double reg, double tol,
 /* qrot_gd (src/qrot_gd.cpp:14-120): gradient descent with Armijo backtracking. */
 int regot_qrot_gd(regot_ctx* ctx, regot_dproblem* prob, double reg, double tol, int max_iter,
                   const regot_opts* opts, regot_result* res);
+/* qrot_apdagd (src/qrot_apdagd.cpp:14-179): accelerated primal-dual adaptive
+ * gradient descent; the plan output is the averaged plan. */
+int regot_qrot_apdagd(regot_ctx* ctx, regot_dproblem* prob, double reg, double tol,
+                      int max_iter, const regot_opts* opts, regot_result* res);
+/* qrot_pdaam (src/qrot_pdaam.cpp:14-188): primal-dual accelerated
+ * alternating minimisation; the plan output is the averaged plan. */
+int regot_qrot_pdaam(regot_ctx* ctx, regot_dproblem* prob, double reg, double tol,
+                     int max_iter, const regot_opts* opts, regot_result* res);
+/* qrot_grssn (src/qrot_grssn.cpp:16-133): regularized semi-smooth Newton with
+ * shift opts->shift (default 1e-3) and Armijo backtracking; tau must be 0. */
+int regot_qrot_grssn(regot_ctx* ctx, regot_dproblem* prob, double reg, double tol,
+                     int max_iter, const regot_opts* opts, regot_result* res);
+/* qrot_lbfgs_semi_dual (src/qrot_lbfgs_semi_dual.cpp:84-126): L-BFGS on the
+ * semi-dual in alpha, beta = optimal_beta(alpha); dual = (alpha, beta). */
+int regot_qrot_lbfgs_semi_dual(regot_ctx* ctx, regot_dproblem* prob, double reg, double tol,
+                               int max_iter, const regot_opts* opts, regot_result* res);
 /* qrot_assn (src/qrot_assn.cpp:16-170). */
 int regot_qrot_assn(regot_ctx* ctx, regot_dproblem* prob, double reg, double tol,
                     int max_iter, const regot_opts* opts, regot_result* res);

@@ -14,7 +14,8 @@
  *   src/sinkhorn_sparsify3.cpp, src/sinkhorn_linsolve.cpp, src/sinkhorn_cg.cpp,
  *   src/qrot_problem.cpp, src/approx_proj.h, src/qrot_result.h,
  *   src/qrot_lbfgs_dual.cpp, src/qrot_assn.cpp, src/qrot_hess.cpp,
- *   src/qrot_bcd.cpp, src/qrot_gd.cpp,
+ *   src/qrot_bcd.cpp, src/qrot_gd.cpp, src/qrot_apdagd.cpp, src/qrot_pdaam.cpp,
+ *   src/qrot_grssn.cpp, src/qrot_lbfgs_semi_dual.cpp,
  *   src/qrot_linsolve.cpp, src/qrot_cg.cpp, src/LBFGSpp/LBFGS.h,
  *   src/LBFGSpp/LBFGSpp/BFGSMat.h, src/LBFGSpp/LBFGSpp/LineSearchNocedalWright.h,
  *   src/LBFGSpp/LBFGSpp/Param.h, src/solvers.cpp (kwargs defaults).
@@ -148,6 +149,19 @@ int oracle_qrot_bcd(const double* M, int n, int m, const double* a,
 int oracle_qrot_gd(const double* M, int n, int m, const double* a,
                    const double* b, double reg, double tol, int max_iter,
                    int verbose, const oracle_opts* opts, oracle_result* res);
+int oracle_qrot_apdagd(const double* M, int n, int m, const double* a,
+                       const double* b, double reg, double tol, int max_iter,
+                       int verbose, const oracle_opts* opts, oracle_result* res);
+int oracle_qrot_pdaam(const double* M, int n, int m, const double* a,
+                      const double* b, double reg, double tol, int max_iter,
+                      int verbose, const oracle_opts* opts, oracle_result* res);
+int oracle_qrot_lbfgs_semi_dual(const double* M, int n, int m, const double* a,
+                                const double* b, double reg, double tol,
+                                int max_iter, int verbose, const oracle_opts* opts,
+                                oracle_result* res);
+int oracle_qrot_grssn(const double* M, int n, int m, const double* a,
+                      const double* b, double reg, double tol, int max_iter,
+                      int verbose, const oracle_opts* opts, oracle_result* res);
 /* optimal_alpha: qrot_problem.cpp:409-419. */
 void oracle_qrot_optimal_alpha(const double* M, int n, int m, const double* a,
                                double reg, const double* beta, double* alpha);

@@ -494,6 +494,316 @@ int oracle_qrot_gd(const double* M, int n, int m, const double* a, const double*
     }
 }
 
+// Primal objective <M, X> + reg/2 ||X||^2 and marginal error of an averaged
+// plan X (row-major), as qrot_apdagd.cpp:141-146 / qrot_pdaam.cpp:150-155.
+static void plan_stats(const Problem& p, const Vec& X, double* primal, double* mar_err) {
+    const int n = p.n, m = p.m;
+    Vec rs(n, 0.0), cs(m, 0.0);
+    double mx = 0.0, xx = 0.0;
+    for (int i = 0; i < n; i++)
+        for (int j = 0; j < m; j++) {
+            const double x = X[(size_t)i * m + j];
+            mx += p.Mij(i, j) * x;
+            xx += x * x;
+            rs[i] += x;
+            cs[j] += x;
+        }
+    double r2 = 0.0;
+    for (int i = 0; i < n; i++) r2 += (rs[i] - p.a[i]) * (rs[i] - p.a[i]);
+    for (int j = 0; j < m; j++) r2 += (cs[j] - p.b[j]) * (cs[j] - p.b[j]);
+    *primal = mx + 0.5 * p.reg * xx;
+    *mar_err = std::sqrt(r2);
+}
+
+// qrot_apdagd_internal: qrot_apdagd.cpp:14-179 (accelerated primal-dual
+// adaptive gradient descent on dual = -gamma, phi = -f / reg; L0 = 1, at
+// most 20 line-search trials, plan averaged with weight ptau).
+int oracle_qrot_apdagd(const double* M, int n, int m, const double* a, const double* b,
+                       double reg, double tol, int max_iter, int verbose,
+                       const oracle_opts* opts, oracle_result* res) {
+    try {
+        constexpr double L0 = 1.0;
+        constexpr int max_inner = 20;
+        const int N = n + m;
+        Problem p = make_problem(M, n, m, a, b, reg, 0.0);
+        Vec gamma, grad(N), dual(N), dual_new(N), dualp(N), dualp_new(N), dualt(N);
+        init_gamma(p, opts, gamma);
+        for (int q = 0; q < N; q++) dual[q] = -gamma[q];
+        dualp = dual;
+        dualt = dual;
+        Vec X((size_t)n * m), Xn((size_t)n * m);
+        get_plan(p, gamma.data(), X.data());
+        History h(res);
+        Timer timer;
+        timer.tic();
+        double f = dual_obj_grad(p, gamma.data(), grad.data());
+        h.push(f, norm(grad) / reg, timer.toc(), 0.0, primal_val(p, gamma.data()));
+        int i;
+        double L = L0, pbeta = 0.0;
+        for (i = 0; i < max_iter; i++) {
+            timer.tic();
+            L *= 0.5;
+            double ptau = 0.0, phi_new = 0.0;
+            for (int j = 0; j < max_inner; j++) {
+                const double palpha = (1.0 + std::sqrt(4.0 * L * pbeta + 1.0)) / (2.0 * L);
+                const double pbeta_new = pbeta + palpha;
+                ptau = palpha / pbeta_new;
+                for (int q = 0; q < N; q++) dualt[q] = (1.0 - ptau) * dual[q] + ptau * dualp[q];
+                for (int q = 0; q < N; q++) gamma[q] = -dualt[q];
+                f = dual_obj_grad(p, gamma.data(), grad.data());
+                const double phit = -f / reg;
+                for (int q = 0; q < N; q++) dualp_new[q] = dualp[q] + (palpha / reg) * grad[q];
+                for (int q = 0; q < N; q++)
+                    dual_new[q] = (1.0 - ptau) * dual[q] + ptau * dualp_new[q];
+                for (int q = 0; q < N; q++) gamma[q] = -dual_new[q];
+                f = dual_obj(p, gamma.data());
+                phi_new = -f / reg;
+                double gd = 0.0, dd = 0.0;
+                for (int q = 0; q < N; q++) {
+                    const double df = dual_new[q] - dualt[q];
+                    gd += grad[q] * df;
+                    dd += df * df;
+                }
+                const double rhs = phit + gd / reg - 0.5 * L * dd;
+                if (verbose >= 2)
+                    std::printf("j = %d, palpha = %g, pbeta = %g, phit = %g, phi_new = %g, "
+                                "rhs = %g\n", j, palpha, pbeta_new, phit, phi_new, rhs);
+                if (phi_new >= rhs || j >= max_inner - 1) {
+                    pbeta = pbeta_new;
+                    dualp.swap(dualp_new);
+                    dual.swap(dual_new);
+                    break;
+                }
+                L *= 2.0;
+            }
+            for (int q = 0; q < N; q++) gamma[q] = -dualt[q];
+            get_plan(p, gamma.data(), Xn.data());
+            for (size_t e = 0; e < X.size(); e++) X[e] = (1.0 - ptau) * X[e] + ptau * Xn[e];
+            double primal_obj, mar_err;
+            plan_stats(p, X, &primal_obj, &mar_err);
+            const double d = timer.toc();
+            h.push(f, mar_err, h.last_time() + d, 0.0, primal_val(p, gamma.data()));
+            if (verbose >= 1)
+                std::printf("iter = %d, primal_obj = %g, phi_new = %g, mar_err = %g\n", i,
+                            primal_obj, phi_new, mar_err);
+            if (primal_obj - phi_new <= tol && mar_err <= tol) break;
+        }
+        res->niter = i;
+        res->hist_len = h.len;
+        std::copy(gamma.begin(), gamma.end(), res->dual);
+        if (res->plan) std::copy(X.begin(), X.end(), res->plan);
+        return 0;
+    } catch (const std::exception& e) {
+        set_err(res, e.what());
+        return 1;
+    }
+}
+
+// qrot_pdaam_internal: qrot_pdaam.cpp:14-188 (primal-dual accelerated
+// alternating minimisation: the block with the larger gradient norm is
+// minimised exactly at the extrapolated point; L0 = 1, at most 20 trials).
+int oracle_qrot_pdaam(const double* M, int n, int m, const double* a, const double* b,
+                      double reg, double tol, int max_iter, int verbose,
+                      const oracle_opts* opts, oracle_result* res) {
+    try {
+        constexpr double L0 = 1.0;
+        constexpr int max_inner = 20;
+        const int N = n + m;
+        Problem p = make_problem(M, n, m, a, b, reg, 0.0);
+        Vec gamma, grad(N), dual(N), dual_new(N), dualp(N), dualt(N);
+        init_gamma(p, opts, gamma);
+        for (int q = 0; q < N; q++) dual[q] = -gamma[q];
+        dualp = dual;
+        dualt = dual;
+        Vec X((size_t)n * m), Xn((size_t)n * m);
+        get_plan(p, gamma.data(), X.data());
+        History h(res);
+        Timer timer;
+        timer.tic();
+        double f = dual_obj_grad(p, gamma.data(), grad.data());
+        h.push(f, norm(grad) / reg, timer.toc(), 0.0, primal_val(p, gamma.data()));
+        int i;
+        double L = L0, palpha = 0.0;
+        for (i = 0; i < max_iter; i++) {
+            timer.tic();
+            double L_new = 0.5 * L, phi_new = 0.0, tau_old = 0.0, tau_new = 0.0;
+            for (int j = 0; j < max_inner; j++) {
+                const double palpha_new =
+                    (1.0 + std::sqrt(4.0 * palpha * palpha * L * L_new + 1.0)) / (2.0 * L_new);
+                const double ptau = 1.0 / (palpha_new * L_new);
+                for (int q = 0; q < N; q++) dualt[q] = (1.0 - ptau) * dual[q] + ptau * dualp[q];
+                for (int q = 0; q < N; q++) gamma[q] = -dualt[q];
+                f = dual_obj_grad(p, gamma.data(), grad.data());
+                const double phit = -f / reg;
+                double lam = 0.0, mu = 0.0;
+                for (int q = 0; q < n; q++) lam += grad[q] * grad[q];
+                for (int q = 0; q < m; q++) mu += grad[n + q] * grad[n + q];
+                if (lam > mu) optimal_alpha(p, gamma.data() + n, gamma.data());
+                else optimal_beta(p, gamma.data(), gamma.data() + n);
+                for (int q = 0; q < N; q++) dual_new[q] = -gamma[q];
+                f = dual_obj(p, gamma.data());
+                phi_new = -f / reg;
+                const double rhs = phit + (lam + mu) / (2.0 * L_new * reg * reg);
+                if (verbose >= 2)
+                    std::printf("j = %d, L = %g, palpha = %g, phit = %g, phi_new = %g, rhs = %g\n",
+                                j, L_new, palpha, phit, phi_new, rhs);
+                if (phi_new >= rhs || j >= max_inner - 1) {
+                    const double ar = palpha / palpha_new, lr = L / L_new;
+                    tau_old = ar * ar * lr;
+                    tau_new = ptau;
+                    palpha = palpha_new;
+                    L = L_new;
+                    dual.swap(dual_new);
+                    break;
+                }
+                L_new *= 2.0;
+            }
+            for (int q = 0; q < N; q++) dualp[q] += (palpha / reg) * grad[q];
+            for (int q = 0; q < N; q++) gamma[q] = -dualt[q];
+            get_plan(p, gamma.data(), Xn.data());
+            for (size_t e = 0; e < X.size(); e++) X[e] = tau_old * X[e] + tau_new * Xn[e];
+            double primal_obj, mar_err;
+            plan_stats(p, X, &primal_obj, &mar_err);
+            const double d = timer.toc();
+            h.push(f, mar_err, h.last_time() + d, 0.0, primal_val(p, gamma.data()));
+            if (verbose >= 1)
+                std::printf("iter = %d, primal_obj = %g, phi_new = %g, mar_err = %g\n", i,
+                            primal_obj, phi_new, mar_err);
+            if (primal_obj - phi_new <= tol && mar_err <= tol) break;
+        }
+        res->niter = i;
+        res->hist_len = h.len;
+        std::copy(gamma.begin(), gamma.end(), res->dual);
+        if (res->plan) std::copy(X.begin(), X.end(), res->plan);
+        return 0;
+    } catch (const std::exception& e) {
+        set_err(res, e.what());
+        return 1;
+    }
+}
+
+// semi_dual_obj_grad: qrot_problem.cpp:420-442. beta = optimal_beta(alpha),
+// f = 0.5 ||D||^2 - reg (a'alpha + b'beta), grad = D 1 - reg a.
+static double semi_dual_obj_grad(const Problem& p, const double* alpha, double* grad,
+                                 double* beta) {
+    const int n = p.n, m = p.m;
+    optimal_beta(p, alpha, beta);
+    Vec gamma(n + m);
+    std::copy(alpha, alpha + n, gamma.begin());
+    std::copy(beta, beta + m, gamma.begin() + n);
+    const double sq = D_stats(p, gamma.data(), grad, nullptr);
+    for (int i = 0; i < n; i++) grad[i] -= p.reg * p.a[i];
+    return 0.5 * sq - p.reg * (dot(alpha, p.a, n) + dot(beta, p.b, m));
+}
+
+// qrot_lbfgs_semi_dual_internal: qrot_lbfgs_semi_dual.cpp:84-126
+// (QROTSemiDual 18-82): L-BFGS on alpha with epsilon = epsilon_rel = tol;
+// alpha0 = 0 or the first n entries of x0; the result is
+// (alpha, optimal_beta(alpha)).
+int oracle_qrot_lbfgs_semi_dual(const double* M, int n, int m, const double* a,
+                                const double* b, double reg, double tol, int max_iter,
+                                int verbose, const oracle_opts* opts, oracle_result* res) {
+    try {
+        Problem p = make_problem(M, n, m, a, b, reg, 0.0);
+        LbfgsParam param;
+        param.epsilon = tol;
+        param.epsilon_rel = tol;
+        param.max_iterations = max_iter;
+        Vec alpha(n, 0.0), beta(m);
+        if (opts && opts->x0 && opts->x0_len == n + m) std::copy(opts->x0, opts->x0 + n, alpha.begin());
+        History h(res);
+        Timer timer;
+        double last_obj = std::numeric_limits<double>::infinity();
+        int it = 0;
+        FunGrad fg = [&](const Vec& x, Vec& g) {
+            last_obj = semi_dual_obj_grad(p, x.data(), g.data(), beta.data());
+            return last_obj;
+        };
+        Vec gamma(n + m);
+        auto iterate = [&](const Vec& x, double gnorm) {
+            const double d = timer.toc();
+            std::copy(x.begin(), x.end(), gamma.begin());
+            optimal_beta(p, x.data(), gamma.data() + n);
+            const double prim = primal_val(p, gamma.data());
+            h.push(last_obj, gnorm / reg, h.last_time() + d, 0.0, prim);
+            if (verbose >= 1)
+                std::printf("iter = %d, objval = %g, ||grad|| = %g\n", it, last_obj, gnorm);
+            it++;
+            timer.tic();
+        };
+        timer.tic();
+        double fx;
+        const int niter = lbfgs_minimize(fg, iterate, param, alpha, fx);
+        std::copy(alpha.begin(), alpha.end(), gamma.begin());
+        optimal_beta(p, alpha.data(), gamma.data() + n);
+        res->niter = niter;
+        res->hist_len = h.len;
+        std::copy(gamma.begin(), gamma.end(), res->dual);
+        if (res->plan) get_plan(p, gamma.data(), res->plan);
+        return 0;
+    } catch (const std::invalid_argument& e) {
+        set_err(res, e.what());
+        return 2;
+    } catch (const std::exception& e) {
+        set_err(res, e.what());
+        return 1;
+    }
+}
+
+// qrot_grssn_internal: qrot_grssn.cpp:16-133 (regularized semi-smooth Newton:
+// direction (H + shift I)^{-1}(-g) by the Schur CG of hess_cg with tolerance
+// 1e-8, Armijo backtracking theta = kappa = 0.5, at most 20 trials).
+int oracle_qrot_grssn(const double* M, int n, int m, const double* a, const double* b,
+                      double reg, double tol, int max_iter, int verbose,
+                      const oracle_opts* opts, oracle_result* res) {
+    try {
+        constexpr double theta = 0.5, kappa = 0.5, cg_tol = 1e-8;
+        constexpr int nlinesearch = 20;
+        const double tau = opts ? opts->tau : 0.0;
+        const double shift = opts ? opts->shift : 1e-3;
+        Problem p = make_problem(M, n, m, a, b, reg, tau);
+        Vec gamma, newgamma(n + m), grad(n + m), direc, rhs(n + m);
+        init_gamma(p, opts, gamma);
+        History h(res);
+        Timer timer;
+        timer.tic();
+        Hessian H;
+        double f = dual_obj_grad_hess(p, gamma.data(), grad.data(), H);
+        double gnorm = norm(grad);
+        h.push(f, gnorm / reg, timer.toc(), 0.0, primal_val(p, gamma.data()));
+        int i;
+        for (i = 0; i < max_iter; i++) {
+            if (verbose >= 1)
+                std::printf("iter = %d, objval = %g, ||grad|| = %g\n", i, f, gnorm);
+            timer.tic();
+            if (gnorm < tol) break;
+            for (int q = 0; q < n + m; q++) rhs[q] = -grad[q];
+            hess_cg(H, rhs, shift, tau, cg_tol, direc);
+            double step = 1.0;
+            const double thresh = theta * dot(grad, direc);
+            for (int k = 0; k < nlinesearch; k++) {
+                for (int q = 0; q < n + m; q++) newgamma[q] = gamma[q] + step * direc[q];
+                const double newf = dual_obj(p, newgamma.data());
+                if (newf <= f + step * thresh) break;
+                step *= kappa;
+            }
+            gamma.swap(newgamma);
+            f = dual_obj_grad_hess(p, gamma.data(), grad.data(), H);
+            gnorm = norm(grad);
+            const double d = timer.toc();
+            h.push(f, gnorm / reg, h.last_time() + d, 0.0, primal_val(p, gamma.data()));
+        }
+        res->niter = i;
+        res->hist_len = h.len;
+        std::copy(gamma.begin(), gamma.end(), res->dual);
+        if (res->plan) get_plan(p, gamma.data(), res->plan);
+        return 0;
+    } catch (const std::exception& e) {
+        set_err(res, e.what());
+        return 1;
+    }
+}
+
 // qrot_lbfgs_dual_internal: qrot_lbfgs_dual.cpp:81-126 (QROTDual 18-79).
 int oracle_qrot_lbfgs_dual(const double* M, int n, int m, const double* a, const double* b,
                            double reg, double tol, int max_iter, int verbose,

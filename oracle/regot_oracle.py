@@ -189,6 +189,26 @@ def qrot_gd(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
                 _QROT_DUAL, 0, with_prim=True, plan=kwargs.get("plan", True))
 
 
+def qrot_apdagd(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
+    return _run(lib().oracle_qrot_apdagd, M, a, b, reg, tol, max_iter, verbose, kwargs,
+                _QROT_DUAL, 0, with_prim=True, plan=kwargs.get("plan", True))
+
+
+def qrot_pdaam(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
+    return _run(lib().oracle_qrot_pdaam, M, a, b, reg, tol, max_iter, verbose, kwargs,
+                _QROT_DUAL, 0, with_prim=True, plan=kwargs.get("plan", True))
+
+
+def qrot_grssn(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
+    return _run(lib().oracle_qrot_grssn, M, a, b, reg, tol, max_iter, verbose, kwargs,
+                _QROT_DUAL, 0, with_prim=True, plan=kwargs.get("plan", True))
+
+
+def qrot_lbfgs_semi_dual(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
+    return _run(lib().oracle_qrot_lbfgs_semi_dual, M, a, b, reg, tol, max_iter, verbose,
+                kwargs, _QROT_DUAL, 0, with_prim=True, plan=kwargs.get("plan", True))
+
+
 def qrot_optimal_alpha(M, a, reg, beta):
     M = _colmajor(M)
     n, m = M.shape

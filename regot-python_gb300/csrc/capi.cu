@@ -453,6 +453,10 @@ REGOT_SOLVER_ENTRY(regot_qrot_lbfgs_dual, qrot_lbfgs_dual_gpu, P->n + P->m)
 REGOT_SOLVER_ENTRY(regot_qrot_assn, qrot_assn_gpu, P->n + P->m)
 REGOT_SOLVER_ENTRY(regot_qrot_bcd, qrot_bcd_gpu, P->n + P->m)
 REGOT_SOLVER_ENTRY(regot_qrot_gd, qrot_gd_gpu, P->n + P->m)
+REGOT_SOLVER_ENTRY(regot_qrot_apdagd, qrot_apdagd_gpu, P->n + P->m)
+REGOT_SOLVER_ENTRY(regot_qrot_pdaam, qrot_pdaam_gpu, P->n + P->m)
+REGOT_SOLVER_ENTRY(regot_qrot_grssn, qrot_grssn_gpu, P->n + P->m)
+REGOT_SOLVER_ENTRY(regot_qrot_lbfgs_semi_dual, qrot_lbfgs_semi_dual_gpu, P->n + P->m)
 
 // ---------------------------------------------------------------- passes --
 

@@ -374,6 +374,14 @@ inline void sync(cudaStream_t st) { REGOT_CUDA(cudaStreamSynchronize(st)); }
 // directly (the transfer overlaps the computation and no device copy of the
 // plan is made); other host memory goes through a device buffer and one copy.
 // The caller synchronises the stream before reading the host result.
+// Averaged plans kept in FP32 to the FP64 plan output.
+template <typename T>
+__global__ void k_widen(const T* x, long long count, double* y) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < count;
+         t += (long long)gridDim.x * blockDim.x)
+        y[t] = (double)x[t];
+}
+
 template <typename F>
 void emit_plan(double* plan, int plan_mem, size_t count, cudaStream_t st, F&& compute) {
     if (plan_mem == REGOT_MEM_DEVICE) {

@@ -35,13 +35,6 @@ double ms_since(Clock::time_point t) {
     return std::chrono::duration<double, std::milli>(Clock::now() - t).count();
 }
 
-// FP32 averaged plan to the FP64 plan output.
-__global__ void k_widen(const float* x, long long count, double* y) {
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < count;
-         t += (long long)gridDim.x * blockDim.x)
-        y[t] = (double)x[t];
-}
-
 // Objective and gradient of the EROT dual from one row/column-sums pass.
 class ErotDual {
 public:
@@ -359,7 +352,7 @@ void sinkhorn_apdagd_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double t
     const long long count = (long long)n * m;
     finish_host(ops, gamma, hobj, hmar, htime, i, E.passes(), o, res, [&](double* dst) {
         if (mixed) {
-            k_widen<<<1024, 256, 0, st>>>(reinterpret_cast<const float*>(X.get()), count, dst);
+            k_widen<float><<<1024, 256, 0, st>>>(reinterpret_cast<const float*>(X.get()), count, dst);
             count_launch();
             REGOT_CHECK_LAUNCH();
         } else {

@@ -91,6 +91,9 @@ enum PassOp : int {
                       // xavg (TM, row-major, stride m): rows/cols sum X; totals sum M X,
                       // sum X (1 - log X)
     OP_Q_ROWROOT,     // rows: count and sum of y = M - cb below ra (FP64), optimal_alpha
+    OP_Q_AVG,         // averaged plan X <- steps[0] X + steps[1] D / reg (X = D / reg when
+                      // nsteps == 0), X at xavg (TM, row-major, stride m): rows/cols sum X;
+                      // totals sum M X, sum X^2
     OP_COUNT
 };
 
@@ -123,7 +126,7 @@ struct PassParams {
     double* totpart = nullptr;     // [NT][nblocks]
     uint32_t* bitmask = nullptr;   // [n][nslabs][LC]
     double* out = nullptr;         // plan output, row-major, stride m
-    void* xavg = nullptr;          // averaged plan (OP_E_AVG), TM, row-major, stride m
+    void* xavg = nullptr;          // averaged plan (OP_E_AVG, OP_Q_AVG), TM, row-major, stride m
     const int* done = nullptr;     // early-exit flag (device)
     int* err = nullptr;            // set to 1 if a bounded wait gave up (device)
 };

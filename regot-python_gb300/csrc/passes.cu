@@ -174,17 +174,18 @@ __host__ __device__ constexpr int op_nr(int op) {
     return op == OP_E_ROW ? 1 : op == OP_E_ROWCOL ? 1 : op == OP_E_HVP ? 1 : op == OP_E_ROWMAX ? 1
          : op == OP_Q_GRAD ? 1 : op == OP_Q_GRADMASK ? 2 : op == OP_Q_P1 ? 1 : op == OP_Q_P3 ? 3
          : op == OP_Q_GRADLS ? 1 : op == OP_E_GRADLS ? 1 : op == OP_E_AVG ? 1
-         : op == OP_Q_ROWROOT ? 2 : 0;
+         : op == OP_Q_ROWROOT ? 2 : op == OP_Q_AVG ? 1 : 0;
 }
 __host__ __device__ constexpr int op_nc(int op) {
     return op == OP_E_COL ? 1 : op == OP_E_ROWCOL ? 1 : op == OP_E_HVP ? 1 : op == OP_E_COLMAX ? 1
          : op == OP_Q_GRAD ? 1 : op == OP_Q_GRADMASK ? 2 : op == OP_Q_P2 ? 1 : op == OP_Q_COLROOT ? 2
-         : op == OP_Q_GRADLS ? 1 : op == OP_E_GRADLS ? 1 : op == OP_E_AVG ? 1 : 0;
+         : op == OP_Q_GRADLS ? 1 : op == OP_E_GRADLS ? 1 : op == OP_E_AVG ? 1
+         : op == OP_Q_AVG ? 1 : 0;
 }
 __host__ __device__ constexpr int op_nt(int op) {
     return op == OP_E_LS ? 4 : op == OP_Q_GRAD ? 1 : op == OP_Q_GRADMASK ? 1 : op == OP_Q_OBJ ? 1
          : op == OP_Q_P3 ? 2 : op == OP_Q_GRADLS ? 2 : op == OP_E_GRADLS ? 1 : op == OP_E_AVG ? 2
-         : 0;
+         : op == OP_Q_AVG ? 2 : 0;
 }
 // Root-finding passes accumulate in FP64 in both storage modes.
 __host__ __device__ constexpr bool op_fp64_acc(int op) {
@@ -457,7 +458,8 @@ __global__ void __launch_bounds__(kThreads, 2) dense_pass(const PassParams p) {
 
     // The averaged-plan totals are accumulated per row in the pass's type and
     // added into FP64 here (the duality-gap test needs them to ~1e-9).
-    using TotT = typename std::conditional<OP == OP_E_AVG, double, Acc>::type;
+    constexpr bool AVG = OP == OP_E_AVG || OP == OP_Q_AVG;
+    using TotT = typename std::conditional<AVG, double, Acc>::type;
     TotT tot[NTa];
 #pragma unroll
     for (int t = 0; t < NTa; ++t) tot[t] = 0;
@@ -765,13 +767,25 @@ __global__ void __launch_bounds__(kThreads, 2) dense_pass(const PassParams p) {
                                 tot[1] += R * R;
                             } else if constexpr (OP == OP_Q_PLAN) {
                                 plan_put<VW>(pv, q, (double)D * p.inv_reg_d, p.out, i, m, c0, lane);
+                            } else if constexpr (OP == OP_Q_AVG) {
+                                if (cvalid[q]) {
+                                    const int j = c0 + ((q / VW) * 32 + lane) * VW + (q % VW);
+                                    TM* X = static_cast<TM*>(p.xavg) + (long long)i * m + j;
+                                    const TM xd = D * inv_reg;
+                                    const TM xn = nsteps > 0 ? steps[0] * *X + steps[1] * xd : xd;
+                                    *X = xn;
+                                    racc[0] += xn;
+                                    cacc[0][q] += xn;
+                                    rchunk[0] += mval * xn;
+                                    rchunk[1] += xn * xn;
+                                }
                             }
                         }
                     }
                     if constexpr (OP == OP_Q_GRADMASK) {
                         if (lane < LC) p.bitmask[((long long)i * nslabs + slab) * LC + lane] = bits;
                     }
-                    if constexpr (OP == OP_E_AVG) {
+                    if constexpr (AVG) {
                         tot[0] += (double)rchunk[0];
                         tot[1] += (double)rchunk[1];
                     }

@@ -638,10 +638,13 @@ private:
 
 namespace {
 
-void finish_qrot(QrotEngine& E, const double* d_gamma, const std::vector<double>& hobj,
-                 const std::vector<double>& hmar, const std::vector<double>& htime,
-                 const std::vector<double>& hprim, int niter, const regot_opts& o,
-                 regot_result* res) {
+// Result from the device dual d_gamma and host histories; the plan is made by
+// plan_fn(dst) into an n x m FP64 destination (device or host view).
+template <typename F>
+void finish_qrot_with(QrotEngine& E, const double* d_gamma, const std::vector<double>& hobj,
+                      const std::vector<double>& hmar, const std::vector<double>& htime,
+                      const std::vector<double>& hprim, int niter, const regot_opts& o,
+                      regot_result* res, F&& plan_fn) {
     cudaStream_t st = E.stream();
     const int n = E.n(), m = E.m();
     const int L = (int)hobj.size();
@@ -654,10 +657,16 @@ void finish_qrot(QrotEngine& E, const double* d_gamma, const std::vector<double>
     if (res->mar_errs) std::memcpy(res->mar_errs, hmar.data(), L * sizeof(double));
     if (res->run_times) std::memcpy(res->run_times, htime.data(), L * sizeof(double));
     if (res->prim_vals) std::memcpy(res->prim_vals, hprim.data(), L * sizeof(double));
-    if (o.plan && res->plan)
-        emit_plan(res->plan, o.plan_mem, (size_t)n * m, st,
-                  [&](double* dst) { E.plan(d_gamma, dst); });
+    if (o.plan && res->plan) emit_plan(res->plan, o.plan_mem, (size_t)n * m, st, plan_fn);
     E.ops().check_err();
+}
+
+void finish_qrot(QrotEngine& E, const double* d_gamma, const std::vector<double>& hobj,
+                 const std::vector<double>& hmar, const std::vector<double>& htime,
+                 const std::vector<double>& hprim, int niter, const regot_opts& o,
+                 regot_result* res) {
+    finish_qrot_with(E, d_gamma, hobj, hmar, htime, hprim, niter, o, res,
+                     [&](double* dst) { E.plan(d_gamma, dst); });
 }
 
 // Wall clock in milliseconds on the device (globaltimer), like the
@@ -795,6 +804,212 @@ void qrot_lbfgs_dual_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double t
     finish_qrot(E, E.gamma(), hobj, hmar, htime, hprim, niter, o, res);
 }
 
+namespace {
+
+// (H + mu I)^{-1} rhs for the generalized Hessian H of the last masked
+// evaluation (sigma bitmask, h1, h2): hess_cg (qrot_cg.cpp:9-50) with the
+// Schur complement on the column block, identity preconditioner, relative
+// tolerance cg_tol and at most 2m steps, run on the device; the CG steps
+// are launched in batches between convergence checks.
+class QrotSchurCG {
+public:
+    QrotSchurCG(QrotEngine& E, double cg_tol)
+        : E_(E), st_(E.stream()), n_(E.n()), m_(E.m()), cg_tol_(cg_tol),
+          dvec_(8 * (size_t)std::max(n_, m_), st_), partial_((size_t)kColChunks * m_, st_),
+          rhs_d_(n_ + m_, st_) {
+        const size_t k = std::max(n_, m_);
+        t_d_ = dvec_.get() + k;
+        zy_ = t_d_ + k;
+        xs_ = zy_ + k;
+        rs_ = xs_ + k;
+        ps_ = rs_ + k;
+        ys_ = ps_ + k;
+        r1_ = ys_ + k;
+        QState hs;
+        d2h(&hs, E.state(), sizeof(hs), st_);
+        sync(st_);
+        hs.cg_max = 2 * m_;
+        h2d(E.state(), &hs, sizeof(hs), st_);
+    }
+
+    void solve(const std::vector<double>& rhs, double mu, std::vector<double>& out) {
+        QState* S = E_.state();
+        const int n = n_, m = m_, N = n + m;
+        const int gn = cdiv(n, kVT), gm = cdiv(m, kVT);
+        h2d(rhs_d_.get(), rhs.data(), N * sizeof(double), st_);
+        // v = w / (h1 + mu); zy = z - sigma' v
+        k_div_h1<<<gn, kVT, 0, st_>>>(n, rhs_d_.get(), E_.h1(), mu, t_d_);
+        count_launch();
+        E_.sigma_cols(t_d_, partial_.get(), nullptr);
+        k_sub_partial<<<gm, kVT, 0, st_>>>(m, rhs_d_.get() + n, partial_.get(), kColChunks, zy_);
+        k_acg_init<<<gm, kVT, 0, st_>>>(m, zy_, cg_tol_, xs_, rs_, ps_, E_.parts(), S);
+        count_launch(2);
+        int batch = 16;
+        for (;;) {
+            for (int q = 0; q < batch; ++q) step(mu);
+            int done = 0;
+            d2h(&done, &S->cg_done, sizeof(int), st_);
+            sync(st_);
+            if (done) break;
+            batch = std::min(batch * 2, 256);
+        }
+        // r1 = (w - sigma r2) / (h1 + mu)
+        E_.sigma_rows(xs_, mu, false, t_d_, nullptr);
+        k_backsub<<<gn, kVT, 0, st_>>>(n, rhs_d_.get(), t_d_, E_.h1(), mu, r1_);
+        count_launch();
+        out.resize(N);
+        d2h(out.data(), r1_, n * sizeof(double), st_);
+        d2h(out.data() + n, xs_, m * sizeof(double), st_);
+        sync(st_);
+    }
+
+private:
+    // One CG step on Delta = h2 o x + mu x - sigma' ((sigma x) / (h1 + mu));
+    // a no-op once the device flag cg_done is set.
+    void step(double mu) {
+        QState* S = E_.state();
+        const int gm = cdiv(m_, kVT);
+        E_.sigma_rows(ps_, mu, true, t_d_, &S->cg_done);
+        E_.sigma_cols(t_d_, partial_.get(), &S->cg_done);
+        k_acg_a<<<gm, kVT, 0, st_>>>(m_, partial_.get(), kColChunks, E_.h2(), mu, ps_, ys_,
+                                     E_.parts(), S);
+        k_acg_b<<<gm, kVT, 0, st_>>>(m_, ps_, ys_, xs_, rs_, E_.parts(), S);
+        k_acg_c<<<gm, kVT, 0, st_>>>(m_, rs_, ps_, S);
+        count_launch(3);
+    }
+
+    QrotEngine& E_;
+    cudaStream_t st_;
+    int n_, m_;
+    double cg_tol_;
+    DBuf<double> dvec_, partial_, rhs_d_;
+    double *t_d_, *zy_, *xs_, *rs_, *ps_, *ys_, *r1_;
+};
+
+}  // namespace
+
+// qrot_lbfgs_semi_dual_internal: qrot_lbfgs_semi_dual.cpp:84-126
+// (QROTSemiDual 18-82). L-BFGS on alpha (epsilon = epsilon_rel = tol) of the
+// semi-dual f(alpha) = 0.5 ||D||^2 - reg (a'alpha + b'beta(alpha)),
+// beta(alpha) = optimal_beta(alpha) (semi_dual_obj_grad,
+// qrot_problem.cpp:420-442): every evaluation is the optimal_beta root
+// passes plus one gradient pass. In mixed precision a line-search trial
+// forms f(x) - f(xp) without cancellation: with d = (x - xp, beta(x) -
+// beta(xp)) and the full dual gradient (g_alpha, g_beta) at (xp, beta(xp)),
+// the change is g_alpha'd_alpha + g_beta'd_beta + sum rem (OP_Q_GRADLS at
+// the base point along d); g_beta vanishes up to rounding at an exact beta.
+void qrot_lbfgs_semi_dual_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol,
+                              int max_iter, const regot_opts& o, regot_result* res) {
+    cudaStream_t st = ctx->stream;
+    const int n = P->n, m = P->m, N = n + m;
+    const bool mixed = P->prec == REGOT_PREC_MIXED;
+    QrotEngine E(P, reg, 0.0, st);
+    DevClock clock(st);
+    lbfgs::Param param;
+    param.epsilon = tol;
+    param.epsilon_rel = tol;
+    param.max_iterations = max_iter;
+    std::vector<double> alpha(n, 0.0);
+    if (o.x0 && o.x0_len == n + m) std::copy(o.x0, o.x0 + n, alpha.begin());
+
+    // The last few evaluations: alpha, beta(alpha) and the beta block of the
+    // full gradient there (the base points of later line searches).
+    struct Rec {
+        std::vector<double> alpha, beta, gbeta;
+    };
+    std::vector<Rec> recs;
+    auto find = [&](const std::vector<double>& x) -> const Rec* {
+        for (auto it = recs.rbegin(); it != recs.rend(); ++it)
+            if (it->alpha == x) return &*it;
+        return nullptr;
+    };
+    std::vector<double> gfull(N), beta(m);
+    auto record = [&](const std::vector<double>& x) {
+        if (recs.size() >= 4) recs.erase(recs.begin());
+        recs.push_back(Rec{x, beta, std::vector<double>(gfull.begin() + n, gfull.end())});
+    };
+    // f and g at x: beta = optimal_beta(x) on the device, then one pass
+    double last_obj = std::numeric_limits<double>::infinity();
+    lbfgs::FunGrad fg = [&](const lbfgs::Vec& x, lbfgs::Vec& g) {
+        h2d(E.gamma(), x.data(), n * sizeof(double), st);
+        E.optimal_beta(E.gamma(), E.gamma() + n);
+        last_obj = E.eval(E.gamma(), E.grad(), false);
+        d2h(gfull.data(), E.grad(), N * sizeof(double), st);
+        d2h(beta.data(), E.gamma() + n, m * sizeof(double), st);
+        sync(st);
+        std::copy(gfull.begin(), gfull.begin() + n, g.begin());
+        record(x);
+        return last_obj;
+    };
+    DBuf<double> xp_d(N, st), d_d(N, st);
+    std::vector<double> xpf(N), dv(N), gtmp(n);
+    const std::vector<double>& ha = P->ha;
+    const std::vector<double>& hb = P->hb;
+    lbfgs::TrialFn trial = [&](const lbfgs::Vec& xp, const lbfgs::Vec& drt, double step,
+                               double fx_init, double dg_init, lbfgs::Vec& x, lbfgs::Vec& g) {
+        for (int k = 0; k < n; ++k) x[k] = xp[k] + step * drt[k];
+        if (!mixed) return fg(x, g);
+        if (!find(xp)) fg(xp, gtmp);  // not expected: the base point is an evaluated one
+        const Rec base = *find(xp);
+        h2d(E.gamma(), x.data(), n * sizeof(double), st);
+        E.optimal_beta(E.gamma(), E.gamma() + n);
+        d2h(beta.data(), E.gamma() + n, m * sizeof(double), st);
+        sync(st);
+        double gb = 0.0;
+        for (int k = 0; k < n; ++k) {
+            xpf[k] = xp[k];
+            dv[k] = x[k] - xp[k];
+        }
+        for (int j = 0; j < m; ++j) {
+            xpf[n + j] = base.beta[j];
+            dv[n + j] = beta[j] - base.beta[j];
+            gb += base.gbeta[j] * dv[n + j];
+        }
+        h2d(xp_d.get(), xpf.data(), N * sizeof(double), st);
+        h2d(d_d.get(), dv.data(), N * sizeof(double), st);
+        double sq = 0.0;
+        const double rem = E.eval_step(xp_d.get(), d_d.get(), 1.0, &sq);
+        d2h(gfull.data(), E.grad(), N * sizeof(double), st);
+        sync(st);
+        std::copy(gfull.begin(), gfull.begin() + n, g.begin());
+        double dab = 0.0;
+        for (int i = 0; i < n; ++i) dab += x[i] * ha[i];
+        for (int j = 0; j < m; ++j) dab += beta[j] * hb[j];
+        last_obj = 0.5 * sq - reg * dab;  // history: f(x) evaluated directly
+        record(x);
+        return fx_init + (step * dg_init + gb + rem);
+    };
+    std::vector<double> hobj, hmar, htime, hprim;
+    int it = 0;
+    double t_prev = clock.now_ms();
+    // gamma = (alpha, optimal_beta(alpha)) on the device
+    auto full_dual = [&](const std::vector<double>& x) {
+        h2d(E.gamma(), x.data(), n * sizeof(double), st);
+        if (const Rec* r = find(x)) h2d(E.gamma() + n, r->beta.data(), m * sizeof(double), st);
+        else E.optimal_beta(E.gamma(), E.gamma() + n);
+    };
+    auto iterate = [&](const lbfgs::Vec& x, double gnorm) {
+        const double d = clock.now_ms() - t_prev;
+        double prim = 0.0;
+        if (o.prim_vals) {
+            full_dual(x);
+            prim = E.primal(E.gamma());
+        }
+        hobj.push_back(last_obj);
+        hmar.push_back(gnorm / reg);
+        htime.push_back((htime.empty() ? 0.0 : htime.back()) + d);
+        hprim.push_back(prim);
+        if (o.verbose >= 1)
+            std::printf("iter = %d, objval = %g, ||grad|| = %g\n", it, last_obj, gnorm);
+        it++;
+        t_prev = clock.now_ms();
+    };
+    double fx;
+    const int niter = lbfgs::minimize(fg, trial, iterate, param, alpha, fx);
+    full_dual(alpha);
+    finish_qrot(E, E.gamma(), hobj, hmar, htime, hprim, niter, o, res);
+}
+
 // qrot_assn_internal (qrot_assn.cpp:16-170) with the CG solve of
 // QROTLinearSolver (method 0, qrot_linsolve.cpp:72-105; qrot_cg.cpp:9-50).
 void qrot_assn_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
@@ -810,67 +1025,9 @@ void qrot_assn_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, in
 
     std::vector<double> gamma, g(N), u(N), gu(N), v(N), gv(N), direc(N);
     init_gamma(E, o, gamma);
-    DBuf<double> dvec(8 * (size_t)std::max(n, m), st), partial((size_t)kColChunks * m, st);
-    double* w_d = dvec.get();                  // rhs alpha part (n)
-    double* t_d = w_d + std::max(n, m);        // temp (n)
-    double* zy = t_d + std::max(n, m);         // Schur rhs (m)
-    double* xs = zy + std::max(n, m);          // CG solution r2 (m)
-    double* rs = xs + std::max(n, m);          // CG residual (m)
-    double* ps = rs + std::max(n, m);          // CG direction (m)
-    double* ys = ps + std::max(n, m);          // Delta p (m)
-    double* r1 = ys + std::max(n, m);          // back-substitution (n)
-    DBuf<double> rhs_d(N, st);
-    QState* S = E.state();
-    const int gn = cdiv(n, kVT), gm = cdiv(m, kVT);
-    const int cg_max = 2 * m;
-    {
-        QState hs;
-        d2h(&hs, S, sizeof(hs), st);
-        sync(st);
-        hs.cg_max = cg_max;
-        h2d(S, &hs, sizeof(hs), st);
-    }
-
-    double mu_cur = 0.0;
-    // One CG step on Delta (captured once per distinct mu is not possible:
-    // mu changes every iteration, so it is read from device memory).
-    DBuf<double> mu_d(1, st);
-    auto cg_step_launch = [&](double mu) {
-        E.sigma_rows(ps, mu, true, t_d, &S->cg_done);
-        E.sigma_cols(t_d, partial.get(), &S->cg_done);
-        k_acg_a<<<gm, kVT, 0, st>>>(m, partial.get(), kColChunks, E.h2(), mu, ps, ys, E.parts(), S);
-        k_acg_b<<<gm, kVT, 0, st>>>(m, ps, ys, xs, rs, E.parts(), S);
-        k_acg_c<<<gm, kVT, 0, st>>>(m, rs, ps, S);
-        count_launch(3);
-    };
-
-    // (H + mu I)^{-1} rhs with H the generalized Hessian (hess_cg, qrot_cg.cpp:9-50).
+    QrotSchurCG cg(E, cg_tol);
     auto solve = [&](const std::vector<double>& rhs, double mu, std::vector<double>& out) {
-        h2d(rhs_d.get(), rhs.data(), N * sizeof(double), st);
-        // v = w / (h1 + mu); zy = z - sigma' v
-        k_div_h1<<<gn, kVT, 0, st>>>(n, rhs_d.get(), E.h1(), mu, t_d);
-        count_launch();
-        E.sigma_cols(t_d, partial.get(), nullptr);
-        k_sub_partial<<<gm, kVT, 0, st>>>(m, rhs_d.get() + n, partial.get(), kColChunks, zy);
-        k_acg_init<<<gm, kVT, 0, st>>>(m, zy, cg_tol, xs, rs, ps, E.parts(), S);
-        count_launch(2);
-        int batch = 16;
-        for (;;) {
-            for (int q = 0; q < batch; ++q) cg_step_launch(mu);
-            int done = 0;
-            d2h(&done, &S->cg_done, sizeof(int), st);
-            sync(st);
-            if (done) break;
-            batch = std::min(batch * 2, 256);
-        }
-        // r1 = (w - sigma r2) / (h1 + mu)
-        E.sigma_rows(xs, mu, false, t_d, nullptr);
-        k_backsub<<<gn, kVT, 0, st>>>(n, rhs_d.get(), t_d, E.h1(), mu, r1);
-        count_launch();
-        out.resize(N);
-        d2h(out.data(), r1, n * sizeof(double), st);
-        d2h(out.data() + n, xs, m * sizeof(double), st);
-        sync(st);
+        cg.solve(rhs, mu, out);
     };
     auto grad_at = [&](const std::vector<double>& x, std::vector<double>& gr, bool mask) {
         h2d(E.gamma(), x.data(), N * sizeof(double), st);
@@ -884,9 +1041,6 @@ void qrot_assn_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, in
         h2d(E.gamma(), x.data(), N * sizeof(double), st);
         return E.primal(E.gamma());
     };
-    (void)mu_cur;
-    (void)w_d;
-
     std::vector<double> hobj, hmar, htime, hprim;
     double t0 = clock.now_ms();
     double f = grad_at(gamma, g, true);
@@ -942,6 +1096,89 @@ void qrot_assn_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, in
         hprim.push_back(primal(gamma));
     }
     h2d(E.gamma(), gamma.data(), N * sizeof(double), st);
+    finish_qrot(E, E.gamma(), hobj, hmar, htime, hprim, i, o, res);
+}
+
+// qrot_grssn_internal: qrot_grssn.cpp:16-133. Regularized semi-smooth Newton:
+// direction (H + shift I)^{-1} (-g) by the Schur CG of hess_cg (CG tolerance
+// 1e-8; the reference's sparse direct factorizations, methods 1-3, solve
+// the same system), then Armijo backtracking (theta = kappa = 0.5, <= 20
+// trials, the last trial kept if none passes). Mixed precision tests
+// f(x + s d) - f(x) <= s theta g'd on the exact change s g'd + sum rem of
+// the trial pass OP_Q_GRADLS; FP64 evaluates the objective directly, as
+// the reference does.
+void qrot_grssn_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
+                    const regot_opts& o, regot_result* res) {
+    require(o.tau == 0.0, "qrot_grssn: tau > 0 is not supported");
+    cudaStream_t st = ctx->stream;
+    const int n = P->n, m = P->m, N = n + m;
+    const bool mixed = P->prec == REGOT_PREC_MIXED;
+    constexpr double theta = 0.5, kappa = 0.5, cg_tol = 1e-8;
+    constexpr int nlinesearch = 20;
+    const double shift = o.shift;
+    QrotEngine E(P, reg, 0.0, st);
+    DevClock clock(st);
+    std::vector<double> gamma, newgamma(N), g(N), direc(N), rhs(N);
+    init_gamma(E, o, gamma);
+    QrotSchurCG cg(E, cg_tol);
+    DBuf<double> xp_d(N, st), d_d(N, st);
+    // f, g and the generalized Hessian (sigma bitmask, h1, h2) at gamma
+    auto grad_hess = [&]() {
+        h2d(E.gamma(), gamma.data(), N * sizeof(double), st);
+        const double f = E.eval(E.gamma(), E.grad(), true);
+        d2h(g.data(), E.grad(), N * sizeof(double), st);
+        sync(st);
+        return f;
+    };
+    auto primal = [&]() { return o.prim_vals ? E.primal(E.gamma()) : 0.0; };
+
+    std::vector<double> hobj, hmar, htime, hprim;
+    double t0 = clock.now_ms();
+    double f = grad_hess();
+    double gnorm = lbfgs::norm(g);
+    hobj.push_back(f);
+    hmar.push_back(gnorm / reg);
+    htime.push_back(clock.now_ms() - t0);
+    hprim.push_back(primal());
+    int i;
+    for (i = 0; i < max_iter; i++) {
+        if (o.verbose >= 1) std::printf("iter = %d, objval = %g, ||grad|| = %g\n", i, f, gnorm);
+        t0 = clock.now_ms();
+        if (gnorm < tol) break;
+        for (int q = 0; q < N; ++q) rhs[q] = -g[q];
+        cg.solve(rhs, shift, direc);
+        double step = 1.0;
+        double gd = 0.0;
+        for (int q = 0; q < N; ++q) gd += g[q] * direc[q];
+        const double thresh = theta * gd;
+        if (mixed) {
+            h2d(xp_d.get(), gamma.data(), N * sizeof(double), st);
+            h2d(d_d.get(), direc.data(), N * sizeof(double), st);
+        }
+        for (int k = 0; k < nlinesearch; k++) {
+            for (int q = 0; q < N; ++q) newgamma[q] = gamma[q] + step * direc[q];
+            bool ok;
+            if (mixed) {
+                double sq = 0.0;
+                const double rem = E.eval_step(xp_d.get(), d_d.get(), step, &sq);
+                ok = step * gd + rem <= step * thresh;
+            } else {
+                h2d(E.gamma(), newgamma.data(), N * sizeof(double), st);
+                const double newf = E.eval(E.gamma(), E.grad(), false);
+                ok = newf <= f + step * thresh;
+            }
+            if (ok) break;
+            step *= kappa;
+        }
+        gamma.swap(newgamma);
+        f = grad_hess();
+        gnorm = lbfgs::norm(g);
+        const double dur = clock.now_ms() - t0;
+        hobj.push_back(f);
+        hmar.push_back(gnorm / reg);
+        htime.push_back(htime.back() + dur);
+        hprim.push_back(primal());
+    }
     finish_qrot(E, E.gamma(), hobj, hmar, htime, hprim, i, o, res);
 }
 
@@ -1089,6 +1326,305 @@ void qrot_gd_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int 
         hprim.push_back(o.prim_vals ? E.primal(E.gamma()) : 0.0);
     }
     finish_qrot(E, E.gamma(), hobj, hmar, htime, hprim, i, o, res);
+}
+
+namespace {
+
+using HVec = std::vector<double>;
+
+// Averaged plan of qrot_apdagd / qrot_pdaam, kept on the device in the pass's
+// element type: X <- c_old X + c_new D(gamma) / reg (X <- D / reg at the
+// start), with the primal objective <M, X> + reg/2 ||X||^2 and the marginal
+// error of X (qrot_apdagd.cpp:133-146, qrot_pdaam.cpp:142-155), one pass
+// (OP_Q_AVG).
+class QrotAvgPlan {
+public:
+    QrotAvgPlan(regot_ctx* ctx, QrotEngine& E, regot_dproblem* P)
+        : ctx_(ctx), E_(E), P_(P), n_(P->n), m_(P->m), st_(E.stream()),
+          mixed_(P->prec == REGOT_PREC_MIXED),
+          X_((size_t)n_ * m_ * (mixed_ ? sizeof(float) : sizeof(double)), st_),
+          sums_(n_ + m_ + 2, st_), mx_(1, st_) {}
+
+    void update(const double* gamma, double c_old, double c_new, bool init, double* primal,
+                double* mar_err) {
+        ErotOps& ops = E_.ops();
+        PassParams p = ops.base_params();
+        p.ra = gamma;
+        p.cb = gamma + n_;
+        p.xavg = X_.get();
+        p.steps[0] = c_old;
+        p.steps[1] = c_new;
+        p.nsteps = init ? 0 : 2;
+        ops.maxabs(gamma, n_ + m_, nullptr, 0, mx_.get());
+        p.grid = mx_.get();
+        ops.pass(OP_Q_AVG, p);
+        ops.merge_rows(1, sums_.get());
+        ops.merge_cols(1, sums_.get() + n_);
+        ops.merge_totals(OP_Q_AVG, 2, sums_.get() + n_ + m_);
+        E_.add_passes(1);
+        const int cnt = n_ + m_ + 2;
+        const double* h = static_cast<const double*>(ctx_stage(ctx_, cnt * sizeof(double)));
+        d2h(const_cast<double*>(h), sums_.get(), cnt * sizeof(double), st_);
+        sync(st_);
+        double r2 = 0.0;
+        for (int i = 0; i < n_; ++i) r2 += (h[i] - P_->ha[i]) * (h[i] - P_->ha[i]);
+        for (int j = 0; j < m_; ++j) r2 += (h[n_ + j] - P_->hb[j]) * (h[n_ + j] - P_->hb[j]);
+        *mar_err = std::sqrt(r2);
+        *primal = h[n_ + m_] + 0.5 * E_.ops().reg() * h[n_ + m_ + 1];
+    }
+
+    // X to an n x m FP64 destination (device or mapped host).
+    void emit(double* dst) {
+        const long long count = (long long)n_ * m_;
+        if (mixed_) {
+            k_widen<float><<<1024, 256, 0, st_>>>(reinterpret_cast<const float*>(X_.get()),
+                                                  count, dst);
+            count_launch();
+            REGOT_CHECK_LAUNCH();
+        } else {
+            REGOT_CUDA(cudaMemcpyAsync(dst, X_.get(), (size_t)count * sizeof(double),
+                                       cudaMemcpyDefault, st_));
+        }
+    }
+
+private:
+    regot_ctx* ctx_;
+    QrotEngine& E_;
+    regot_dproblem* P_;
+    int n_, m_;
+    cudaStream_t st_;
+    bool mixed_;
+    DBuf<char> X_;
+    DBuf<double> sums_, mx_;
+};
+
+// obj and gradient at the host point x (uploaded to the engine's gamma).
+double qrot_grad_at(QrotEngine& E, const HVec& x, HVec& g) {
+    cudaStream_t st = E.stream();
+    const size_t bytes = x.size() * sizeof(double);
+    h2d(E.gamma(), x.data(), bytes, st);
+    const double f = E.eval(E.gamma(), E.grad(), false);
+    d2h(g.data(), E.grad(), bytes, st);
+    sync(st);
+    return f;
+}
+
+// f(xp + d) - f(xp) - g'd (>= 0) at the device points xp, d, from the
+// trial pass; the caller adds g'd. Uploads both host vectors.
+double qrot_change_rem(QrotEngine& E, DBuf<double>& xp_d, DBuf<double>& d_d, const HVec& xp,
+                       const HVec& d) {
+    cudaStream_t st = E.stream();
+    h2d(xp_d.get(), xp.data(), xp.size() * sizeof(double), st);
+    h2d(d_d.get(), d.data(), d.size() * sizeof(double), st);
+    double sq = 0.0;
+    return E.eval_step(xp_d.get(), d_d.get(), 1.0, &sq);
+}
+
+}  // namespace
+
+// qrot_apdagd_internal: qrot_apdagd.cpp:14-179. dual = -gamma, phi = -f / reg;
+// the averaged plan lives on the device. The line-search test
+// phi_new >= phit + g'diff / reg - L/2 |diff|^2 (diff = dual_new - dualt) is,
+// with f_new - f_t = -g'diff + rem, the test rem <= reg L/2 |diff|^2: mixed
+// precision takes rem from the trial pass (no cancellation); FP64 evaluates
+// f_new directly, as the reference does.
+void qrot_apdagd_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
+                     const regot_opts& o, regot_result* res) {
+    cudaStream_t st = ctx->stream;
+    const int n = P->n, m = P->m, N = n + m;
+    const bool mixed = P->prec == REGOT_PREC_MIXED;
+    constexpr double L0 = 1.0;
+    constexpr int max_inner = 20;
+    QrotEngine E(P, reg, 0.0, st);
+    QrotAvgPlan X(ctx, E, P);
+    DevClock clock(st);
+    qrot_initial(E, o, n, m);
+    HVec gamma(N), g(N), dual(N), dual_new(N), dualp(N), dualp_new(N), dualt(N), d(N);
+    d2h(gamma.data(), E.gamma(), N * sizeof(double), st);
+    sync(st);
+    for (int q = 0; q < N; ++q) dual[q] = -gamma[q];
+    dualp = dual;
+    dualt = dual;
+    double primal_obj = 0.0, mar_err = 0.0;
+    X.update(E.gamma(), 0.0, 1.0, true, &primal_obj, &mar_err);
+    DBuf<double> xp_d(N, st), d_d(N, st);
+    HVec hobj, hmar, htime, hprim;
+
+    double t0 = clock.now_ms();
+    double f = qrot_grad_at(E, gamma, g);
+    hobj.push_back(f);
+    hmar.push_back(host_norm(g) / reg);
+    htime.push_back(clock.now_ms() - t0);
+    hprim.push_back(o.prim_vals ? E.primal(E.gamma()) : 0.0);
+    int i;
+    double L = L0, pbeta = 0.0;
+    for (i = 0; i < max_iter; i++) {
+        t0 = clock.now_ms();
+        L *= 0.5;
+        double ptau = 0.0, phi_new = 0.0;
+        for (int j = 0; j < max_inner; j++) {
+            const double palpha = (1.0 + std::sqrt(4.0 * L * pbeta + 1.0)) / (2.0 * L);
+            const double pbeta_new = pbeta + palpha;
+            ptau = palpha / pbeta_new;
+            for (int q = 0; q < N; ++q) {
+                dualt[q] = (1.0 - ptau) * dual[q] + ptau * dualp[q];
+                gamma[q] = -dualt[q];
+            }
+            const double ft = qrot_grad_at(E, gamma, g);
+            const double phit = -ft / reg;
+            double gd = 0.0, dd = 0.0;
+            for (int q = 0; q < N; ++q) {
+                dualp_new[q] = dualp[q] + (palpha / reg) * g[q];
+                dual_new[q] = (1.0 - ptau) * dual[q] + ptau * dualp_new[q];
+                const double df = dual_new[q] - dualt[q];
+                gd += g[q] * df;
+                dd += df * df;
+            }
+            bool accept;
+            if (mixed) {
+                for (int q = 0; q < N; ++q) d[q] = -(dual_new[q] - dualt[q]);
+                const double rem = qrot_change_rem(E, xp_d, d_d, gamma, d);
+                f = ft - gd + rem;
+                phi_new = -f / reg;
+                accept = rem <= 0.5 * L * reg * dd;
+            } else {
+                for (int q = 0; q < N; ++q) d[q] = -dual_new[q];
+                h2d(E.gamma(), d.data(), N * sizeof(double), st);
+                f = E.eval(E.gamma(), E.grad(), false);
+                phi_new = -f / reg;
+                accept = phi_new >= phit + gd / reg - 0.5 * L * dd;
+            }
+            if (o.verbose >= 2)
+                std::printf("j = %d, palpha = %g, pbeta = %g, phit = %g, phi_new = %g\n", j,
+                            palpha, pbeta_new, phit, phi_new);
+            if (accept || j >= max_inner - 1) {
+                pbeta = pbeta_new;
+                dualp.swap(dualp_new);
+                dual.swap(dual_new);
+                break;
+            }
+            L *= 2.0;
+        }
+        // plan = (1 - ptau) plan + ptau plan(-dualt) and its statistics
+        for (int q = 0; q < N; ++q) gamma[q] = -dualt[q];
+        h2d(E.gamma(), gamma.data(), N * sizeof(double), st);
+        X.update(E.gamma(), 1.0 - ptau, ptau, false, &primal_obj, &mar_err);
+        hobj.push_back(f);
+        hmar.push_back(mar_err);
+        htime.push_back(htime.back() + (clock.now_ms() - t0));
+        hprim.push_back(o.prim_vals ? E.primal(E.gamma()) : 0.0);
+        if (o.verbose >= 1)
+            std::printf("iter = %d, primal_obj = %g, phi_new = %g, mar_err = %g\n", i,
+                        primal_obj, phi_new, mar_err);
+        if (primal_obj - phi_new <= tol && mar_err <= tol) break;
+    }
+    finish_qrot_with(E, E.gamma(), hobj, hmar, htime, hprim, i, o, res,
+                     [&](double* dst) { X.emit(dst); });
+}
+
+// qrot_pdaam_internal: qrot_pdaam.cpp:14-188. At the extrapolated point
+// dualt, the block (alpha or beta) with the larger gradient norm is
+// minimised exactly on the device (optimal_alpha / optimal_beta passes);
+// the test phi_new >= phit + |g|^2 / (2 L reg^2) is, with
+// f_new - f_t = g'd + rem (d = gamma_new - gamma_t), the test
+// g'd + rem <= -|g|^2 / (2 L reg): mixed precision takes rem from the
+// trial pass, FP64 evaluates f_new directly, as the reference does.
+void qrot_pdaam_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
+                    const regot_opts& o, regot_result* res) {
+    cudaStream_t st = ctx->stream;
+    const int n = P->n, m = P->m, N = n + m;
+    const bool mixed = P->prec == REGOT_PREC_MIXED;
+    constexpr double L0 = 1.0;
+    constexpr int max_inner = 20;
+    QrotEngine E(P, reg, 0.0, st);
+    QrotAvgPlan X(ctx, E, P);
+    DevClock clock(st);
+    qrot_initial(E, o, n, m);
+    HVec gamma(N), gt(N), g(N), dual(N), dualp(N), dualt(N), d(N);
+    d2h(gamma.data(), E.gamma(), N * sizeof(double), st);
+    sync(st);
+    for (int q = 0; q < N; ++q) dual[q] = -gamma[q];
+    dualp = dual;
+    dualt = dual;
+    double primal_obj = 0.0, mar_err = 0.0;
+    X.update(E.gamma(), 0.0, 1.0, true, &primal_obj, &mar_err);
+    DBuf<double> xp_d(N, st), d_d(N, st);
+    HVec hobj, hmar, htime, hprim;
+
+    double t0 = clock.now_ms();
+    double f = qrot_grad_at(E, gamma, g);
+    hobj.push_back(f);
+    hmar.push_back(host_norm(g) / reg);
+    htime.push_back(clock.now_ms() - t0);
+    hprim.push_back(o.prim_vals ? E.primal(E.gamma()) : 0.0);
+    int i;
+    double L = L0, palpha = 0.0;
+    for (i = 0; i < max_iter; i++) {
+        t0 = clock.now_ms();
+        double L_new = 0.5 * L, phi_new = 0.0, tau_old = 0.0, tau_new = 0.0;
+        for (int j = 0; j < max_inner; j++) {
+            const double palpha_new =
+                (1.0 + std::sqrt(4.0 * palpha * palpha * L * L_new + 1.0)) / (2.0 * L_new);
+            const double ptau = 1.0 / (palpha_new * L_new);
+            for (int q = 0; q < N; ++q) {
+                dualt[q] = (1.0 - ptau) * dual[q] + ptau * dualp[q];
+                gt[q] = -dualt[q];
+            }
+            const double ft = qrot_grad_at(E, gt, g);  // E.gamma() = gamma_t
+            const double phit = -ft / reg;
+            double lam = 0.0, mu = 0.0;
+            for (int q = 0; q < n; ++q) lam += g[q] * g[q];
+            for (int q = 0; q < m; ++q) mu += g[n + q] * g[n + q];
+            if (lam > mu) E.optimal_alpha(E.gamma() + n, E.gamma());
+            else E.optimal_beta(E.gamma(), E.gamma() + n);
+            d2h(gamma.data(), E.gamma(), N * sizeof(double), st);
+            sync(st);
+            bool accept;
+            if (mixed) {
+                double gd = 0.0;
+                for (int q = 0; q < N; ++q) {
+                    d[q] = gamma[q] - gt[q];
+                    gd += g[q] * d[q];
+                }
+                const double rem = qrot_change_rem(E, xp_d, d_d, gt, d);
+                f = ft + (gd + rem);
+                phi_new = -f / reg;
+                accept = gd + rem <= -(lam + mu) / (2.0 * L_new * reg);
+            } else {
+                f = E.eval(E.gamma(), E.grad(), false);
+                phi_new = -f / reg;
+                accept = phi_new >= phit + (lam + mu) / (2.0 * L_new * reg * reg);
+            }
+            if (o.verbose >= 2)
+                std::printf("j = %d, L = %g, palpha = %g, phit = %g, phi_new = %g\n", j, L_new,
+                            palpha, phit, phi_new);
+            if (accept || j >= max_inner - 1) {
+                const double ar = palpha / palpha_new, lr = L / L_new;
+                tau_old = ar * ar * lr;
+                tau_new = ptau;
+                palpha = palpha_new;
+                L = L_new;
+                for (int q = 0; q < N; ++q) dual[q] = -gamma[q];
+                break;
+            }
+            L_new *= 2.0;
+        }
+        for (int q = 0; q < N; ++q) dualp[q] += (palpha / reg) * g[q];
+        // plan = tau_old plan + tau_new plan(-dualt) and its statistics
+        for (int q = 0; q < N; ++q) gamma[q] = -dualt[q];
+        h2d(E.gamma(), gamma.data(), N * sizeof(double), st);
+        X.update(E.gamma(), tau_old, tau_new, false, &primal_obj, &mar_err);
+        hobj.push_back(f);
+        hmar.push_back(mar_err);
+        htime.push_back(htime.back() + (clock.now_ms() - t0));
+        hprim.push_back(o.prim_vals ? E.primal(E.gamma()) : 0.0);
+        if (o.verbose >= 1)
+            std::printf("iter = %d, primal_obj = %g, phi_new = %g, mar_err = %g\n", i,
+                        primal_obj, phi_new, mar_err);
+        if (primal_obj - phi_new <= tol && mar_err <= tol) break;
+    }
+    finish_qrot_with(E, E.gamma(), hobj, hmar, htime, hprim, i, o, res,
+                     [&](double* dst) { X.emit(dst); });
 }
 
 }  // namespace regot

@@ -39,6 +39,14 @@ void qrot_bcd_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int
                   const regot_opts& o, regot_result* res);
 void qrot_gd_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
                  const regot_opts& o, regot_result* res);
+void qrot_apdagd_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
+                     const regot_opts& o, regot_result* res);
+void qrot_pdaam_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
+                    const regot_opts& o, regot_result* res);
+void qrot_grssn_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
+                    const regot_opts& o, regot_result* res);
+void qrot_lbfgs_semi_dual_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol,
+                              int max_iter, const regot_opts& o, regot_result* res);
 void qrot_assn_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
                    const regot_opts& o, regot_result* res);
 

@@ -37,7 +37,8 @@ from . import _lib as L
 
 __all__ = [
     "sinkhorn_bcd", "sinkhorn_newton", "sinkhorn_ssns", "sinkhorn_lbfgs_dual", "sinkhorn_apdagd",
-    "qrot_lbfgs_dual", "qrot_assn", "qrot_bcd", "qrot_gd", "sinkhorn_result", "qrot_result",
+    "qrot_lbfgs_dual", "qrot_assn", "qrot_bcd", "qrot_gd", "qrot_apdagd", "qrot_pdaam",
+    "qrot_grssn", "qrot_lbfgs_semi_dual", "sinkhorn_result", "qrot_result",
     "Problem",
     "sinkhorn_bcd_batched", "batch_result",
 ]
@@ -262,6 +263,18 @@ class Problem:
     def qrot_gd(self, reg, tol=1e-6, max_iter=1000, verbose=0, **kw):
         return self._solve("regot_qrot_gd", reg, tol, max_iter, verbose, kw, True)
 
+    def qrot_apdagd(self, reg, tol=1e-6, max_iter=1000, verbose=0, **kw):
+        return self._solve("regot_qrot_apdagd", reg, tol, max_iter, verbose, kw, True)
+
+    def qrot_pdaam(self, reg, tol=1e-6, max_iter=1000, verbose=0, **kw):
+        return self._solve("regot_qrot_pdaam", reg, tol, max_iter, verbose, kw, True)
+
+    def qrot_grssn(self, reg, tol=1e-6, max_iter=1000, verbose=0, **kw):
+        return self._solve("regot_qrot_grssn", reg, tol, max_iter, verbose, kw, True)
+
+    def qrot_lbfgs_semi_dual(self, reg, tol=1e-6, max_iter=1000, verbose=0, **kw):
+        return self._solve("regot_qrot_lbfgs_semi_dual", reg, tol, max_iter, verbose, kw, True)
+
     # ---- pass-level calls --------------------------------------------
     def _vec(self, x, size):
         x = np.ascontiguousarray(np.asarray(x, dtype=np.float64).ravel())
@@ -476,6 +489,29 @@ def qrot_bcd(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
 def qrot_gd(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
     """Gradient descent for QROT; reference src/qrot_gd.cpp:14-120."""
     return _solve("qrot_gd", M, a, b, reg, tol, max_iter, verbose, kwargs)
+
+
+def qrot_apdagd(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
+    """Accelerated primal-dual adaptive gradient descent for QROT; reference
+    src/qrot_apdagd.cpp:14-179. The plan is the averaged primal plan."""
+    return _solve("qrot_apdagd", M, a, b, reg, tol, max_iter, verbose, kwargs)
+
+
+def qrot_pdaam(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
+    """Primal-dual accelerated alternating minimisation for QROT; reference
+    src/qrot_pdaam.cpp:14-188. The plan is the averaged primal plan."""
+    return _solve("qrot_pdaam", M, a, b, reg, tol, max_iter, verbose, kwargs)
+
+
+def qrot_grssn(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
+    """Regularized semi-smooth Newton for QROT; reference src/qrot_grssn.cpp:16-133.
+    kwargs: ``shift`` (1e-3), ``method`` (the system is solved by CG)."""
+    return _solve("qrot_grssn", M, a, b, reg, tol, max_iter, verbose, kwargs)
+
+
+def qrot_lbfgs_semi_dual(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
+    """L-BFGS on the QROT semi-dual; reference src/qrot_lbfgs_semi_dual.cpp:84-126."""
+    return _solve("qrot_lbfgs_semi_dual", M, a, b, reg, tol, max_iter, verbose, kwargs)
 
 
 def qrot_assn(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):

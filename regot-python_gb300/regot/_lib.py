@@ -114,6 +114,7 @@ EXPORTS = [
     "regot_problem_destroy", "regot_sinkhorn_bcd", "regot_sinkhorn_newton",
     "regot_sinkhorn_ssns", "regot_sinkhorn_lbfgs_dual", "regot_sinkhorn_apdagd",
     "regot_qrot_lbfgs_dual", "regot_qrot_assn", "regot_qrot_bcd", "regot_qrot_gd",
+    "regot_qrot_apdagd", "regot_qrot_pdaam", "regot_qrot_grssn", "regot_qrot_lbfgs_semi_dual",
     "regot_qrot_optimal_alpha", "regot_erot_optimal_beta", "regot_erot_optimal_alpha", "regot_erot_dual_obj_grad",
     "regot_erot_hvp", "regot_erot_plan", "regot_erot_sparsify", "regot_erot_hess_solve",
     "regot_erot_tyy", "regot_erot_solve_batched", "regot_qrot_dual_obj_grad",
@@ -156,7 +157,8 @@ def load() -> C.CDLL:
         for name in ("regot_sinkhorn_bcd", "regot_sinkhorn_newton", "regot_sinkhorn_ssns",
                      "regot_sinkhorn_lbfgs_dual", "regot_sinkhorn_apdagd",
                      "regot_qrot_lbfgs_dual", "regot_qrot_assn", "regot_qrot_bcd",
-                     "regot_qrot_gd"):
+                     "regot_qrot_gd", "regot_qrot_apdagd", "regot_qrot_pdaam",
+                     "regot_qrot_grssn", "regot_qrot_lbfgs_semi_dual"):
             f = getattr(lib, name)
             f.argtypes = [vp, vp, C.c_double, C.c_double, C.c_int, C.POINTER(Opts),
                           C.POINTER(Result)]

@@ -292,3 +292,55 @@ def test_qrot_assn_matches_numpy_restatement():
         errs.append(gn / reg)
     r = O.qrot_assn(M, a, b, reg, tol=1e-12, max_iter=len(errs) - 1, plan=False)
     np.testing.assert_allclose(r.mar_errs[:len(errs)], errs, rtol=1e-5)
+
+
+@pytest.mark.parametrize("solver", ["qrot_apdagd", "qrot_pdaam"])
+def test_qrot_accelerated_averaged_plan_and_gap(solver):
+    # The plan of the accelerated QROT methods is the running average of
+    # D/reg along the extrapolated points: its marginal error is the recorded
+    # one, its duality gap against the last dual value closes, and it tends
+    # to the optimal plan.
+    M, a, b = qrot_points(40, 30, seed=7, dtype=np.float64)
+    reg = 0.1
+    r = getattr(O, solver)(M, a, b, reg, tol=1e-5, max_iter=5000)
+    assert r.niter < 5000 and r.mar_errs[-1] <= 1e-5
+    P = r.plan
+    mar = np.sqrt(((P.sum(1) - a) ** 2).sum() + ((P.sum(0) - b) ** 2).sum())
+    np.testing.assert_allclose(r.mar_errs[-1], mar, rtol=1e-10)
+    primal = (M * P).sum() + 0.5 * reg * (P * P).sum()
+    assert primal - (-r.obj_vals[-1] / reg) <= 1e-5
+    rl = O.qrot_lbfgs_dual(M, a, b, reg, tol=1e-8, max_iter=20000)
+    P_opt = O.qrot_plan(M, reg, rl.dual)
+    np.testing.assert_allclose(P, P_opt, rtol=0, atol=0.05 * P_opt.max())
+    np.testing.assert_allclose(r.obj_vals[-1], rl.obj_vals[-1], rtol=1e-4)
+
+
+def test_qrot_grssn_and_semi_dual_reach_the_optimum():
+    # Both reach the optimum of the generic minimiser; GRSSN's first step is
+    # the Newton direction of the shifted generalized Jacobian, and the
+    # semi-dual's dual is (alpha, optimal_beta(alpha)).
+    M, a, b = qrot_points(25, 20, seed=6, dtype=np.float64)
+    reg = 0.1
+    fun = lambda x: _qrot_dual_np(M, a, b, reg, x)[:2]  # noqa: E731
+    res = minimize(fun, np.zeros(45), jac=True, method="L-BFGS-B",
+                   options={"maxiter": 50000, "gtol": 1e-13, "ftol": 1e-16})
+    rg = O.qrot_grssn(M, a, b, reg, tol=1e-9, max_iter=500)
+    assert rg.niter < 500 and rg.mar_errs[-1] * reg < 1e-9
+    np.testing.assert_allclose(rg.obj_vals[-1], res.fun, rtol=1e-7)
+    rs = O.qrot_lbfgs_semi_dual(M, a, b, reg, tol=1e-8, max_iter=2000)
+    np.testing.assert_allclose(rs.obj_vals[-1], res.fun, rtol=1e-7)
+    beta = O.qrot_optimal_beta(M, b, reg, rs.dual[:25])
+    np.testing.assert_allclose(rs.dual[25:], beta, rtol=0, atol=0)
+    # first GRSSN step: (H + shift I) d = -g with H the generalized Jacobian
+    gam = np.r_[np.zeros(25), O.qrot_optimal_beta(M, b, reg, np.zeros(25))]
+    f, g, D = _qrot_dual_np(M, a, b, reg, gam)
+    s = (D > 0).astype(float)
+    H = np.block([[np.diag(s.sum(1)), s], [s.T, np.diag(s.sum(0))]]) + 1e-3 * np.eye(45)
+    d = np.linalg.solve(H, -g)
+    step = 1.0
+    for _ in range(20):
+        if _qrot_dual_np(M, a, b, reg, gam + step * d)[0] <= f + step * 0.5 * (g @ d):
+            break
+        step *= 0.5
+    r1 = O.qrot_grssn(M, a, b, reg, tol=1e-14, max_iter=1, plan=False)
+    np.testing.assert_allclose(r1.dual, gam + step * d, rtol=0, atol=1e-7)
