@@ -1,6 +1,9 @@
-// QROT on the GPU: qrot_lbfgs_dual (reference src/qrot_lbfgs_dual.cpp:81-126)
-// and qrot_assn (src/qrot_assn.cpp:16-170), with the dense passes of
-// src/qrot_problem.cpp and src/qrot_hess.cpp.
+// QROT on the GPU: qrot_lbfgs_dual (reference src/qrot_lbfgs_dual.cpp:81-126),
+// qrot_assn (src/qrot_assn.cpp:16-170), qrot_grssn (src/qrot_grssn.cpp:16-133),
+// qrot_lbfgs_semi_dual (src/qrot_lbfgs_semi_dual.cpp:84-126), qrot_bcd
+// (src/qrot_bcd.cpp:14-103), qrot_gd (src/qrot_gd.cpp:14-120), qrot_apdagd
+// (src/qrot_apdagd.cpp:14-179) and qrot_pdaam (src/qrot_pdaam.cpp:14-188),
+// with the dense passes of src/qrot_problem.cpp and src/qrot_hess.cpp.
 //
 //   grad / obj   one pass: D = (alpha_i + beta_j - M_ij)+, row and column sums
 //                of D and sum D^2 (compute_D_stats, qrot_problem.cpp:36-94).
