@@ -147,6 +147,15 @@ int regot_sinkhorn_newton(regot_ctx* ctx, regot_dproblem* prob, double reg, doub
 /* sinkhorn_ssns (src/sinkhorn_ssns.cpp:16-234). */
 int regot_sinkhorn_ssns(regot_ctx* ctx, regot_dproblem* prob, double reg, double tol,
                         int max_iter, const regot_opts* opts, regot_result* res);
+/* sinkhorn_sparse_newton (src/sinkhorn_sparse_newton.cpp:24-171): Newton
+ * steps on the density-sparsified Hessian (opts->density, default 0.01;
+ * shift min(||g||, opts->shift)) with the More-Thuente line search. */
+int regot_sinkhorn_sparse_newton(regot_ctx* ctx, regot_dproblem* prob, double reg, double tol,
+                                 int max_iter, const regot_opts* opts, regot_result* res);
+/* sinkhorn_splr (src/sinkhorn_splr.cpp:24-200): sparse-plus-low-rank
+ * quasi-Newton steps (BFGS correction of the sparsified Hessian). */
+int regot_sinkhorn_splr(regot_ctx* ctx, regot_dproblem* prob, double reg, double tol,
+                        int max_iter, const regot_opts* opts, regot_result* res);
 /* sinkhorn_lbfgs_dual (src/sinkhorn_lbfgs_dual.cpp:81-126). */
 int regot_sinkhorn_lbfgs_dual(regot_ctx* ctx, regot_dproblem* prob, double reg, double tol,
                               int max_iter, const regot_opts* opts, regot_result* res);
@@ -274,6 +283,14 @@ int regot_erot_plan(regot_ctx* ctx, regot_dproblem* prob, double reg, const doub
  * receives the kept nonzero entries as a row-major n x (m-1) array of 0/1. */
 int regot_erot_sparsify(regot_ctx* ctx, regot_dproblem* prob, double reg, const double* gamma,
                         double delta, double density_hint, long long* nnz, int* mask);
+/* sparsify_mat_with_density (src/sinkhorn_sparsify4.cpp:77-174, preserve =
+ * true) of T(gamma), as dual_sparsified_hess_with_density calls it
+ * (src/sinkhorn_problem_obj.cpp:446-457): the largest floor(n (m-1) density)
+ * entries of the first m-1 columns plus the first row and column. Entries
+ * tied with the threshold value are all kept. *nnz = number of kept nonzero
+ * entries; mask as for regot_erot_sparsify. */
+int regot_erot_sparsify_density(regot_ctx* ctx, regot_dproblem* prob, double reg,
+                                const double* gamma, double density, long long* nnz, int* mask);
 /* QROT Problem::dual_obj_grad (src/qrot_problem.cpp:226-253). */
 int regot_qrot_dual_obj_grad(regot_ctx* ctx, regot_dproblem* prob, double reg,
                              const double* gamma, double* obj, double* grad);

@@ -488,6 +488,222 @@ static void finish(const Problem& p, int niter, const Vec& gamma, History& h, or
     if (r->plan) get_plan(p, gamma.data(), r->plan);
 }
 
+// ------------- sparsify_mat_with_density (sinkhorn_sparsify4.cpp) -------------
+// sinkhorn_sparsify4.cpp:77-174 with preserve = true (sinkhorn_sparsify.h:22):
+// the largest k = floor(n (m-1) density) entries of T[:, :m-1] (selected with
+// std::nth_element, the reference's non-AVX2 path), plus the first column and
+// the first row of T[:, :m-1].
+static CSC sparsify_with_density(const double* T, int n, int m, double density) {
+    const size_t len = (size_t)n * (m - 1);
+    density = std::min(std::max(density, 0.0), 1.0);
+    const size_t k = (size_t)(len * density);
+    std::vector<size_t> ind(len);
+    for (size_t q = 0; q < len; q++) ind[q] = q;
+    if (k > 0 && k < len)
+        std::nth_element(ind.begin(), ind.begin() + (len - k), ind.end(),
+                         [T](size_t x, size_t y) { return T[x] < T[y]; });
+    std::vector<char> keep(len, 0);
+    for (int i = 0; i < n; i++) keep[i] = 1;                          // column 0
+    for (int j = 1; j < m - 1; j++) keep[(size_t)j * n] = 1;          // row 0
+    for (size_t q = len - k; q < len; q++) keep[ind[q]] = 1;
+    CSC sp;
+    sp.n = n;
+    sp.ncol = m - 1;
+    sp.outer.assign(m, 0);
+    for (int j = 0; j < m - 1; j++) {
+        for (int i = 0; i < n; i++) {
+            const size_t q = (size_t)j * n + i;
+            if (keep[q]) {
+                sp.val.push_back(T[q]);
+                sp.inner.push_back(i);
+            }
+        }
+        sp.outer[j + 1] = (int)sp.val.size();
+    }
+    return sp;
+}
+
+// dual_sparsified_hess_with_density: sinkhorn_problem_obj.cpp:446-457 with
+// compute_hess_with_density (sinkhorn_hess.cpp:37-55).
+static void sparsified_hess_density(const Problem& p, const double* T, const Vec& grad,
+                                    double density, Hessian& H) {
+    const int n = p.n, m = p.m;
+    H.n = n;
+    H.m = m;
+    H.h1.resize(n);
+    H.h2.resize(m - 1);
+    for (int i = 0; i < n; i++) H.h1[i] = (grad[i] + p.a[i]) / p.reg;
+    for (int j = 0; j < m - 1; j++) H.h2[j] = (grad[n + j] + p.b[j]) / p.reg;
+    H.sigmad = sparsify_with_density(T, n, m, density);
+    for (auto& v : H.sigmad.val) v /= p.reg;
+}
+
+// density_T2H: sinkhorn_sparse_newton.cpp:17-22 (sinkhorn_splr.cpp:16-21).
+static double density_T2H(double denT, int n, int m) {
+    const double nnz = 2.0 * denT * n * (m - 1) + n + m - 1;
+    return nnz / double(n + m - 1) / double(n + m - 1);
+}
+
+// ---------------- More-Thuente line search (sinkhorn_problem_ls.cpp) ----------------
+// quadratic_minimizer (fa, ga, fb): lines 68-75.
+static double qmin_fgf(double a, double b, double fa, double ga, double fb) {
+    const double ba = b - a;
+    const double w = 0.5 * ba * ga / (fa - fb + ba * ga);
+    return a + w * ba;
+}
+// quadratic_minimizer (ga, gb): lines 83-87.
+static double qmin_gg(double a, double b, double ga, double gb) {
+    const double w = ga / (ga - gb);
+    return a + w * (b - a);
+}
+// cubic_minimizer: lines 92-150.
+static double cmin(double a, double b, double fa, double fb, double ga, double gb, bool& exists) {
+    const double apb = a + b, ba = b - a, ba2 = ba * ba;
+    const double fba = fb - fa, gba = gb - ga;
+    const double z3 = (ga + gb) * ba - 2.0 * fba;
+    const double z2 = 0.5 * (gba * ba2 - 3.0 * apb * z3);
+    const double z1 = fba * ba2 - apb * z2 - (a * apb + b * b) * z3;
+    const double eps = std::numeric_limits<double>::epsilon();
+    if (std::abs(z3) < eps * std::abs(z2) || std::abs(z3) < eps * std::abs(z1)) {
+        exists = (z2 * ba > 0.0);
+        return exists ? (-0.5 * z1 / z2) : b;
+    }
+    const double u = z2 / (3.0 * z3), v = z1 / z2;
+    const double vu = v / u;
+    exists = (vu <= 1.0);
+    if (!exists) return b;
+    double r1, r2;
+    if (std::abs(u) >= std::abs(v)) {
+        const double w = 1.0 + std::sqrt(1.0 - vu);
+        r1 = -u * w;
+        r2 = -v / w;
+    } else {
+        const double sd = std::sqrt(std::abs(u)) * std::sqrt(std::abs(v)) * std::sqrt(1 - u / v);
+        r1 = -u - sd;
+        r2 = -u + sd;
+    }
+    return (z3 * ba > 0.0) ? std::max(r1, r2) : std::min(r1, r2);
+}
+// step_selection: lines 154-222.
+static double step_select(double al, double au, double at, double fl, double fu, double ft,
+                          double gl, double gu, double gt) {
+    if (al == au) return al;
+    if (!std::isfinite(ft) || !std::isfinite(gt)) return (al + at) / 2.0;
+    bool ac_ok;
+    const double ac = cmin(al, at, fl, ft, gl, gt, ac_ok);
+    const double aq = qmin_fgf(al, at, fl, gl, ft);
+    if (ft > fl) {
+        if (!ac_ok) return aq;
+        return (std::abs(ac - al) < std::abs(aq - al)) ? ac : ((aq + ac) / 2.0);
+    }
+    const double as = qmin_gg(al, at, gl, gt);
+    if (gt * gl < 0.0) return (std::abs(ac - at) >= std::abs(as - at)) ? ac : as;
+    const double deltal = 1.1, deltau = 0.66;
+    if (std::abs(gt) < std::abs(gl)) {
+        const bool use_ac = ac_ok && ((ac - at) * (at - al) > 0.0) &&
+                            (std::abs(ac - at) < std::abs(as - at));
+        const double r = use_ac ? ac : as;
+        return (at > al) ? std::min(at + deltau * (au - at), r)
+                         : std::max(at + deltau * (au - at), r);
+    }
+    if (!std::isfinite(au) || !std::isfinite(fu) || !std::isfinite(gu))
+        return at + deltal * (at - al);
+    bool ae_ok;
+    const double ae = cmin(at, au, ft, fu, gt, gu, ae_ok);
+    return (at > al) ? std::min(at + deltau * (au - at), ae) : std::max(at + deltau * (au - at), ae);
+}
+
+// line_search_wolfe: sinkhorn_problem_ls.cpp:226-436 (c1 = 1e-4, c2 = 0.9,
+// 20 trials, steps in [1e-10, 2]). eval(step, &f, &dg) evaluates the
+// objective and its directional derivative at gamma + step d (leaving T
+// there). Sets recompute when the returned step is not the last evaluated.
+template <typename Eval>
+static double wolfe_search(double init_step, double f0, double dg0, Eval&& eval,
+                           bool& recompute) {
+    const double c1 = 1e-4, c2 = 0.9;
+    const int max_iter = 20;
+    recompute = false;
+    const double step_min = 1e-10, step_max = 2.0;
+    init_step = std::min(std::max(init_step, step_min), step_max);
+    double step = init_step;
+    if (dg0 > 0.0) {
+        recompute = true;
+        return init_step;
+    }
+    const double test_decr = c1 * dg0, test_curv = -c2 * dg0;
+    const double Inf = std::numeric_limits<double>::infinity();
+    double I_lo = 0.0, I_hi = Inf, fI_lo = 0.0, fI_hi = Inf;
+    double gI_lo = (1.0 - c1) * dg0, gI_hi = Inf, psiI_lo = 0.0;
+    bool bracketed = false, guard_min = true;
+    double width = Inf, width_prev = Inf;
+    int shrink_fails = 0;
+    const double delta_max = 1.1, delta_min = 7.0 / 12, shrink = 0.66;
+    double fx = f0;
+    for (int it = 0; it < max_iter; it++) {
+        double dg;
+        eval(step, &fx, &dg);
+        const double psit = fx - f0 - step * test_decr;
+        const double dpsit = dg - test_decr;
+        if (psit <= 0.0 && std::abs(dg) <= test_curv) return step;
+        if (step <= step_min && (psit > 0.0 || dpsit >= 0.0)) return step;
+        if (step >= step_max && (psit <= 0.0 && dpsit < 0.0)) return step;
+        const double ft = psit, gt = dpsit;  // f is psi throughout (line 329)
+        if (guard_min && (psit <= 0.0 && dpsit < 0.0)) guard_min = false;
+        double next;
+        const bool case2 = (psit <= psiI_lo) && (dpsit * (I_lo - step) > 0.0);
+        if (case2) {
+            next = std::min(step_max, step + delta_max * (step - I_lo));
+        } else {
+            next = step_select(I_lo, I_hi, step, fI_lo, fI_hi, ft, gI_lo, gI_hi, gt);
+            next = std::min(std::max(next, step_min), step_max);
+            if (guard_min) {
+                next = std::max(next, step_min);
+                next = std::min(next, std::max(step_min, delta_min * step));
+            }
+        }
+        if (psit > psiI_lo) {
+            I_hi = step;
+            fI_hi = ft;
+            gI_hi = gt;
+        } else if (case2) {
+            I_lo = step;
+            fI_lo = ft;
+            gI_lo = gt;
+            psiI_lo = psit;
+        } else {
+            I_hi = I_lo;
+            fI_hi = fI_lo;
+            gI_hi = gI_lo;
+            I_lo = step;
+            fI_lo = ft;
+            gI_lo = gt;
+            psiI_lo = psit;
+        }
+        if (!bracketed && !case2) {
+            const double l = std::min(I_lo, I_hi), r = std::max(I_lo, I_hi);
+            bracketed = (l >= step_min && r <= step_max);
+        }
+        if (bracketed) {
+            width_prev = width;
+            width = std::abs(I_hi - I_lo);
+            if (width_prev < Inf && width > shrink * width_prev) shrink_fails += 1;
+            else shrink_fails = 0;
+            if (shrink_fails >= 2) {
+                next = (I_lo + I_hi) / 2.0;
+                shrink_fails = 0;
+            }
+        }
+        step = next;
+    }
+    // Trials used up (lines 417-435): the psi of the last evaluated value at
+    // the step chosen next decides between that step and I_lo.
+    const double psit = fx - f0 - step * test_decr;
+    if (psit <= psiI_lo) return step;
+    recompute = true;
+    if (I_lo <= 0.0) return init_step;
+    return I_lo;
+}
+
 }  // namespace erot
 }  // namespace oracle
 
@@ -892,6 +1108,150 @@ int oracle_sinkhorn_ssns(const double* M, int n, int m, const double* a, const d
         set_err(res, e.what());
         return 1;
     }
+}
+
+
+// Shared loop of sinkhorn_sparse_newton (sinkhorn_sparse_newton.cpp:24-171)
+// and sinkhorn_splr (sinkhorn_splr.cpp:24-200): sparsified Hessian with a
+// target density, shift min(gnorm, shift), More-Thuente line search from
+// min(1, 1.5 alpha). SPLR adds the BFGS correction of solve_low_rank
+// (sinkhorn_linsolve.cpp:160-225, always a direct factorization) when
+// y's > 1e-6 y'y, and adapts the density more gently.
+static int sparse_newton_loop(bool splr, const double* M, int n, int m, const double* a,
+                              const double* b, double reg, double tol, int max_iter, int verbose,
+                              const oracle_opts* opts, oracle_result* res) {
+    try {
+        const int method = opts ? opts->method : 1;
+        const double density_max = opts ? opts->density : 0.01;
+        const double density_min = 0.01 * density_max;
+        double density = 0.1 * density_max;
+        const double shift_max = opts ? opts->shift : 1e-3;
+        const double cg_tol = 1e-8, eps = 1e-6;
+        const int N = n + m - 1;
+        Problem p(M, n, m, a, b, reg);
+        Vec gamma, gamma_pre(N, 0.0), g(N), g_pre(N, 0.0), direc(N), x(N), gx(N), rhs(N);
+        std::vector<double> T((size_t)n * m);
+        History h(res);
+        init_gamma(p, opts, gamma);
+        Timer timer;
+        timer.tic();
+        double f = dual_obj_grad(p, gamma.data(), g.data(), T.data(), true);
+        double gnorm = norm(g);
+        const double gnorm_init = gnorm;
+        Hessian H;
+        sparsified_hess_density(p, T.data(), g, density, H);
+        h.push(f, gnorm, timer.toc(), density_T2H(density, n, m));
+        double alpha = 1.0;
+        int i;
+        for (i = 0; i < max_iter; i++) {
+            if (verbose >= 1)
+                std::printf("iter = %d, objval = %g, ||grad|| = %g\n", i, f, gnorm);
+            timer.tic();
+            if (gnorm < tol || !std::isfinite(f)) break;
+            for (int q = 0; q < N; q++) rhs[q] = -g[q];
+            const double shift = std::min(gnorm, shift_max);
+            bool low_rank = false;
+            Vec y(N), sv(N);
+            double ys = 0.0;
+            if (splr) {
+                double yy = 0.0;
+                for (int q = 0; q < N; q++) {
+                    y[q] = g[q] - g_pre[q];
+                    sv[q] = gamma[q] - gamma_pre[q];
+                    ys += y[q] * sv[q];
+                    yy += y[q] * y[q];
+                }
+                low_rank = (i > 0) && (ys > eps * yy);
+            }
+            if (low_rank) {
+                Vec ir, iy;
+                if (!hess_direct(H, rhs, shift, ir) || !hess_direct(H, y, shift, iy))
+                    throw std::runtime_error("sparse factorization failed");
+                const double rs = dot(sv, rhs), yiy = dot(y, iy), yir = dot(y, ir);
+                const double rs_ys = rs / ys;
+                const double cs = (1.0 + yiy / ys) * rs_ys - yir / ys;
+                for (int q = 0; q < N; q++) direc[q] = ir[q] + cs * sv[q] - rs_ys * iy[q];
+            } else if (method == 0) {
+                hess_cg(H, rhs, shift, nullptr, cg_tol, direc);
+            } else if (!hess_direct(H, rhs, shift, direc)) {
+                throw std::runtime_error("sparse factorization failed");
+            }
+            bool recompute = true;
+            auto eval = [&](double st, double* fx, double* dg) {
+                for (int q = 0; q < N; q++) x[q] = gamma[q] + st * direc[q];
+                *fx = dual_obj_grad(p, x.data(), gx.data(), T.data(), true);
+                *dg = dot(gx, direc);
+            };
+            alpha = wolfe_search(std::min(1.0, 1.5 * alpha), f, dot(g, direc), eval, recompute);
+            gamma_pre = gamma;
+            for (int q = 0; q < N; q++) gamma[q] += alpha * direc[q];
+            g_pre = g;
+            // T is the last line-search evaluation unless recompute is set
+            f = dual_obj_grad(p, gamma.data(), g.data(), T.data(), recompute);
+            const double gnorm_pre = gnorm;
+            gnorm = norm(g);
+            if (splr) {
+                const bool bad = (gnorm_pre < gnorm_init) && (gnorm > gnorm_pre);
+                density *= bad ? 1.1 : 0.99;
+            } else {
+                const bool bad = (gnorm_pre < gnorm_init) && (gnorm > 1.1 * gnorm_pre);
+                density *= bad ? 2.0 : 0.9;
+            }
+            density = std::min(density_max, std::max(density_min, density));
+            sparsified_hess_density(p, T.data(), g, density, H);
+            const double d = timer.toc();
+            h.push(f, gnorm, h.last_time() + d, density_T2H(density, n, m));
+        }
+        finish(p, i, gamma, h, res);
+        return 0;
+    } catch (const std::exception& e) {
+        set_err(res, e.what());
+        return 1;
+    }
+}
+
+int oracle_sinkhorn_sparse_newton(const double* M, int n, int m, const double* a,
+                                  const double* b, double reg, double tol, int max_iter,
+                                  int verbose, const oracle_opts* opts, oracle_result* res) {
+    return sparse_newton_loop(false, M, n, m, a, b, reg, tol, max_iter, verbose, opts, res);
+}
+
+int oracle_sinkhorn_splr(const double* M, int n, int m, const double* a, const double* b,
+                         double reg, double tol, int max_iter, int verbose,
+                         const oracle_opts* opts, oracle_result* res) {
+    return sparse_newton_loop(true, M, n, m, a, b, reg, tol, max_iter, verbose, opts, res);
+}
+
+// sparsify_mat_with_density (sinkhorn_sparsify4.cpp:77-174, preserve = true)
+// of a column-major n x m T into CSC of its first m-1 columns; returns nnz or
+// -1 if cap is too small.
+long oracle_sparsify_density(const double* T, int n, int m, double density, int* outer,
+                             int* inner, double* values, long cap) {
+    const CSC sp = sparsify_with_density(T, n, m, density);
+    if (sp.nnz() > cap) return -1;
+    std::copy(sp.outer.begin(), sp.outer.end(), outer);
+    std::copy(sp.inner.begin(), sp.inner.end(), inner);
+    std::copy(sp.val.begin(), sp.val.end(), values);
+    return sp.nnz();
+}
+
+// line_search_wolfe on f(s) = c0 + c1 s + c2 s^2 + c3 s^3 + c4 s^4 (tests of
+// the More-Thuente restatement); returns the step, recompute in *flag and the
+// number of evaluations in *nev.
+double oracle_wolfe_poly(const double* c, double init_step, int* flag, int* nev) {
+    auto poly = [c](double s) { return c[0] + s * (c[1] + s * (c[2] + s * (c[3] + s * c[4]))); };
+    auto dpoly = [c](double s) { return c[1] + s * (2 * c[2] + s * (3 * c[3] + s * 4 * c[4])); };
+    int count = 0;
+    auto eval = [&](double st, double* fx, double* dg) {
+        *fx = poly(st);
+        *dg = dpoly(st);
+        count++;
+    };
+    bool recompute = false;
+    const double step = wolfe_search(init_step, poly(0.0), dpoly(0.0), eval, recompute);
+    *flag = recompute ? 1 : 0;
+    *nev = count;
+    return step;
 }
 
 }  // extern "C"

@@ -10,6 +10,7 @@
  *   src/sinkhorn_problem_bcd.cpp, src/sinkhorn_problem_obj.cpp,
  *   src/sinkhorn_result.h, src/sinkhorn_bcd.cpp, src/sinkhorn_newton.cpp,
  *   src/sinkhorn_lbfgs_dual.cpp, src/sinkhorn_apdagd.cpp,
+ *   src/sinkhorn_sparse_newton.cpp, src/sinkhorn_splr.cpp, src/sinkhorn_sparsify4.cpp,
  *   src/sinkhorn_ssns.cpp, src/sinkhorn_problem_ls.cpp, src/sinkhorn_hess.cpp,
  *   src/sinkhorn_sparsify3.cpp, src/sinkhorn_linsolve.cpp, src/sinkhorn_cg.cpp,
  *   src/qrot_problem.cpp, src/approx_proj.h, src/qrot_result.h,
@@ -93,6 +94,14 @@ double oracle_erot_compute_T(const double* M, int n, int m, double reg,
 long oracle_sparsify_mat3(const double* T, int n, int m, double delta,
                           double density_hint, int* outer, int* inner,
                           double* values, long cap);
+/* sparsify_mat_with_density (sinkhorn_sparsify4.cpp:77-174, preserve =
+ * true), same output convention as oracle_sparsify_mat3. */
+long oracle_sparsify_density(const double* T, int n, int m, double density,
+                             int* outer, int* inner, double* values, long cap);
+/* line_search_wolfe (sinkhorn_problem_ls.cpp:226-436) on the quartic with
+ * coefficients c[0..4]. */
+double oracle_wolfe_poly(const double* c, double init_step, int* recompute,
+                         int* nev);
 void oracle_erot_plan(const double* M, int n, int m, double reg,
                       const double* gamma, double* plan_rowmajor);
 
@@ -113,6 +122,13 @@ int oracle_sinkhorn_lbfgs_dual(const double* M, int n, int m, const double* a,
                                const double* b, double reg, double tol,
                                int max_iter, int verbose,
                                const oracle_opts* opts, oracle_result* res);
+int oracle_sinkhorn_sparse_newton(const double* M, int n, int m,
+                                  const double* a, const double* b, double reg,
+                                  double tol, int max_iter, int verbose,
+                                  const oracle_opts* opts, oracle_result* res);
+int oracle_sinkhorn_splr(const double* M, int n, int m, const double* a,
+                         const double* b, double reg, double tol, int max_iter,
+                         int verbose, const oracle_opts* opts, oracle_result* res);
 int oracle_sinkhorn_apdagd(const double* M, int n, int m, const double* a,
                            const double* b, double reg, double tol,
                            int max_iter, int verbose, const oracle_opts* opts,

@@ -71,6 +71,8 @@ def lib():
         _lib.oracle_erot_dual_obj_grad.restype = C.c_double
         _lib.oracle_erot_compute_T.restype = C.c_double
         _lib.oracle_sparsify_mat3.restype = C.c_long
+        _lib.oracle_sparsify_density.restype = C.c_long
+        _lib.oracle_wolfe_poly.restype = C.c_double
         _lib.oracle_qrot_dual_obj.restype = C.c_double
         _lib.oracle_qrot_dual_obj_grad.restype = C.c_double
         _lib.oracle_qrot_primal_val.restype = C.c_double
@@ -161,6 +163,16 @@ def sinkhorn_newton(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
 
 def sinkhorn_ssns(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
     return _run(lib().oracle_sinkhorn_ssns, M, a, b, reg, tol, max_iter, verbose, kwargs,
+                _EROT_DUAL, 1, with_dens=True, plan=kwargs.get("plan", True))
+
+
+def sinkhorn_sparse_newton(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
+    return _run(lib().oracle_sinkhorn_sparse_newton, M, a, b, reg, tol, max_iter, verbose,
+                kwargs, _EROT_DUAL, 1, with_dens=True, plan=kwargs.get("plan", True))
+
+
+def sinkhorn_splr(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
+    return _run(lib().oracle_sinkhorn_splr, M, a, b, reg, tol, max_iter, verbose, kwargs,
                 _EROT_DUAL, 1, with_dens=True, plan=kwargs.get("plan", True))
 
 
@@ -302,6 +314,29 @@ def sparsify_mat3(T, delta, density_hint):
                                      outer.ctypes.data_as(_ip), inner.ctypes.data_as(_ip),
                                      _d(vals), C.c_long(cap))
     return outer, inner[:nnz].copy(), vals[:nnz].copy()
+
+
+def sparsify_density(T, density):
+    """sparsify_mat_with_density: (outer[m], inner[nnz], values[nnz]) CSC."""
+    T = _colmajor(T)
+    n, m = T.shape
+    cap = n * max(m - 1, 0) + 1
+    outer = np.zeros(m, dtype=np.int32)
+    inner = np.zeros(cap, dtype=np.int32)
+    vals = np.zeros(cap)
+    nnz = lib().oracle_sparsify_density(_d(T), n, m, C.c_double(density),
+                                        outer.ctypes.data_as(_ip), inner.ctypes.data_as(_ip),
+                                        _d(vals), C.c_long(cap))
+    return outer, inner[:nnz].copy(), vals[:nnz].copy()
+
+
+def wolfe_poly(coefs, init_step):
+    """More-Thuente line search on a quartic: (step, recompute, evaluations)."""
+    c = _f64(coefs).ravel()
+    flag = C.c_int(0)
+    nev = C.c_int(0)
+    step = lib().oracle_wolfe_poly(_d(c), C.c_double(init_step), C.byref(flag), C.byref(nev))
+    return step, bool(flag.value), nev.value
 
 
 def erot_plan(M, reg, gamma):

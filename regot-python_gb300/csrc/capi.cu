@@ -447,6 +447,8 @@ void regot_problem_destroy(regot_dproblem* P) {
 REGOT_SOLVER_ENTRY(regot_sinkhorn_bcd, sinkhorn_bcd_gpu, P->n + P->m - 1)
 REGOT_SOLVER_ENTRY(regot_sinkhorn_newton, sinkhorn_newton_gpu, P->n + P->m - 1)
 REGOT_SOLVER_ENTRY(regot_sinkhorn_ssns, sinkhorn_ssns_gpu, P->n + P->m - 1)
+REGOT_SOLVER_ENTRY(regot_sinkhorn_sparse_newton, sinkhorn_sparse_newton_gpu, P->n + P->m - 1)
+REGOT_SOLVER_ENTRY(regot_sinkhorn_splr, sinkhorn_splr_gpu, P->n + P->m - 1)
 REGOT_SOLVER_ENTRY(regot_sinkhorn_lbfgs_dual, sinkhorn_lbfgs_dual_gpu, P->n + P->m - 1)
 REGOT_SOLVER_ENTRY(regot_sinkhorn_apdagd, sinkhorn_apdagd_gpu, P->n + P->m - 1)
 REGOT_SOLVER_ENTRY(regot_qrot_lbfgs_dual, qrot_lbfgs_dual_gpu, P->n + P->m)
@@ -649,6 +651,15 @@ int regot_erot_sparsify(regot_ctx* ctx, regot_dproblem* P, double reg, const dou
         require(reg > 0.0, "reg must be positive");
         require(delta >= 0.0, "delta must be non-negative");
         erot_sparsify_gpu(ctx, P, reg, gamma, delta, density_hint, nnz, mask);
+    });
+}
+
+int regot_erot_sparsify_density(regot_ctx* ctx, regot_dproblem* P, double reg,
+                                const double* gamma, double density, long long* nnz, int* mask) {
+    return guarded(ctx, [&] {
+        require(P && gamma && nnz, "NULL argument");
+        require(reg > 0.0, "reg must be positive");
+        erot_sparsify_density_gpu(ctx, P, reg, gamma, density, nnz, mask);
     });
 }
 

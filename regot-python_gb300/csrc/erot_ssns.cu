@@ -62,6 +62,7 @@
 #include "device_util.cuh"
 #include "erot_ops.cuh"
 #include "solvers.h"
+#include "wolfe.h"
 
 namespace regot {
 
@@ -452,6 +453,7 @@ struct RowStageArgs {
     int ldr;          // CSR row stride (m - 1)
     int cache;        // rows of T and d in shared memory
     long long lds;    // per-block scratch stride (2 rows) when not cached
+    int keep_row0;    // keep every entry of row 0 (sparsify_mat_with_density)
 };
 
 // Row stage and CSR rows (see the file comment).
@@ -484,6 +486,7 @@ __global__ void __launch_bounds__(kSelThreads) k_row_stage(DenseArgs a, RowStage
             // the dropped mass exceeds 2 delta: re-keep down to y
             if (block_select(dbuf, m1, fix_target(delta2, k), k, sh, yy)) y = yy;
         }
+        if (r.keep_row0 && i == 0) y = (TM)0;
         int* cols = rcols + (size_t)i * r.ldr;
         TM* vals = rvals + (size_t)i * r.ldr;
         const int total = block_compact(
@@ -821,6 +824,106 @@ __global__ void k_ls_sum(const double* totpart, int nblocks, int nsteps, double*
     out[s] = acc;
 }
 
+// ---- global top-k threshold of T[:, :m-1] (sparsify_mat_with_density) ----
+// The k-th largest value is found by a radix select over the bit patterns of
+// T' (non-negative values order like their patterns): per digit, a grid-wide
+// histogram of the candidates (entries whose higher digits match the prefix
+// chosen so far), then one block picks the bin holding the k-th largest.
+struct TopK {
+    unsigned long long prefix, mask;
+    unsigned long long rank;  // position of the threshold among the candidates, from the top
+    int empty;                // k == 0: nothing but the preserved row and column
+};
+
+template <typename TM>
+__global__ void __launch_bounds__(256) k_topk_hist(const TM* TT, long long ldt, int n, int m1,
+                                                   const TopK* tk, int lo, int nb,
+                                                   unsigned* ghist) {
+    using K = KeyOf<TM>;
+    using U = typename K::U;
+    __shared__ unsigned s_h[kBins];
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) s_h[b] = 0u;
+    __syncthreads();
+    const U prefix = (U)tk->prefix, mask = (U)tk->mask;
+    constexpr int VW = 16 / (int)sizeof(TM);
+    const long long vpr = ldt / VW;  // ldt is a multiple of VW
+    const long long total = vpr * m1;
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < total;
+         v += (long long)gridDim.x * blockDim.x) {
+        const long long j = v / vpr;
+        const int i0 = (int)(v - j * vpr) * VW;
+        const float4 raw = *reinterpret_cast<const float4*>(TT + j * ldt + i0);
+        const TM* e = reinterpret_cast<const TM*>(&raw);
+#pragma unroll
+        for (int q = 0; q < VW; ++q) {
+            const U key = K::key(e[q]);
+            if (i0 + q < n && (key & mask) == prefix)
+                atomicAdd(&s_h[(int)((key >> lo) & (U)(nb - 1))], 1u);
+        }
+    }
+    __syncthreads();
+    for (int b = threadIdx.x; b < nb; b += blockDim.x)
+        if (s_h[b]) atomicAdd(&ghist[b], s_h[b]);
+}
+
+// One block of 256 threads: thread t owns nb / 256 consecutive bins counted
+// from the top; a scan over the threads gives the count above each bin.
+__global__ void __launch_bounds__(256) k_topk_pick(TopK* tk, const unsigned* ghist, int lo,
+                                                   int nb) {
+    __shared__ unsigned long long s_w[8];
+    __shared__ int s_bin;
+    __shared__ unsigned long long s_above;
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const int per = nb / 256;
+    const int btop = nb - t * per;  // this thread's bins: btop - 1 down to btop - per
+    unsigned long long loc = 0;
+    for (int q = 0; q < per; ++q) loc += ghist[btop - 1 - q];
+    unsigned long long inc = loc;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const unsigned long long o = __shfl_up_sync(kFull, inc, d);
+        if (lane >= d) inc += o;
+    }
+    if (lane == 31) s_w[w] = inc;
+    if (t == 0) s_bin = -1;
+    __syncthreads();
+    unsigned long long run = inc - loc;
+    for (int q = 0; q < w; ++q) run += s_w[q];
+    const unsigned long long r = tk->rank;
+    for (int q = 0; q < per; ++q) {
+        const int b = btop - 1 - q;
+        const unsigned long long c = ghist[b];
+        if (run < r && run + c >= r) {
+            s_bin = b;
+            s_above = run;
+        }
+        run += c;
+    }
+    __syncthreads();
+    if (t == 0 && !tk->empty && s_bin >= 0) {
+        tk->prefix |= (unsigned long long)s_bin << lo;
+        tk->mask |= (unsigned long long)(nb - 1) << lo;
+        tk->rank -= s_above;
+    }
+}
+
+// Column thresholds of the density sparsification: column 0 keeps every
+// entry, the others keep T >= the k-th largest value (all of its ties).
+template <typename TM>
+__global__ void k_topk_finish(const TopK* tk, int m1, TM* xcol) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= m1) return;
+    using K = KeyOf<TM>;
+    const TM thr = tk->empty ? (TM)INFINITY : K::val((typename K::U)tk->prefix);
+    xcol[j] = j == 0 ? (TM)0 : thr;
+}
+
+// out = base + s d (n + m entries)
+__global__ void k_axpy_to(int N, const double* base, double s, const double* d, double* out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < N) out[t] = base[t] + s * d[t];
+}
+
 template <typename TM>
 class SsnsEngine {
 public:
@@ -829,11 +932,11 @@ public:
           reg_(reg), mixed_(P->prec == REGOT_PREC_MIXED) {
         const int N = n_ + m_;
         const int method = o.method < 0 ? 1 : o.method;
-        require(method == 0 || method == 1, "sinkhorn_ssns: method must be 0 (CG) or 1 (direct)");
-        jacobi_ = method == 1;
-        cg_tol_ = method == 0 ? 1e-8 : (o.cg_tol > 0.0 ? o.cg_tol : 1e-10);
-        cg_max_ = o.cg_max_iter > 0 ? o.cg_max_iter : 2 * std::max(m1_, 1);
-        if (jacobi_ && o.cg_max_iter <= 0) cg_max_ = 10 * std::max(m1_, 1);
+        jacobi_ = method != 0;
+        tol_direct_ = o.cg_tol > 0.0 ? o.cg_tol : 1e-10;
+        max_cg_ = o.cg_max_iter > 0 ? o.cg_max_iter : 2 * std::max(m1_, 1);
+        max_direct_ = o.cg_max_iter > 0 ? o.cg_max_iter : 10 * std::max(m1_, 1);
+        cg_max_ = jacobi_ ? max_direct_ : max_cg_;
         gamma_.alloc(N, st_);
         g_.alloc(N, st_);
         h_.alloc(N, st_);
@@ -963,6 +1066,7 @@ public:
         r.ldr = m1_;
         r.cache = row_cache_ ? 1 : 0;
         r.lds = lds_;
+        r.keep_row0 = 0;
         k_row_stage<TM><<<row_grid_, kSelThreads, row_smem_, st_>>>(
             a, r, xcol_.get(), 2.0 * delta, row_scratch_.get(), yrow_.get(), rcount_.get(),
             rcols_.get(), rvals_.get());
@@ -981,15 +1085,26 @@ public:
         return (2.0 * nnz + dim) / dim / dim;
     }
 
-    // direction = -(H_s + shift I)^{-1} g into dir (sinkhorn_ssns.cpp:118-140).
-    void direction(double shift) {
+    // direction = -(H_s + shift I)^{-1} gv into dir (sinkhorn_ssns.cpp:118-140);
+    // gv = g unless given. mode -1 follows the method (0: CG with relative
+    // tolerance 1e-8; otherwise the direct-solve stand-in, Jacobi PCG to
+    // tol_direct_), mode 0 / 1 forces one of them.
+    void direction(double shift, const double* gv = nullptr, int mode = -1) {
         SsnState* S = state_.get();
+        const bool jac = mode < 0 ? jacobi_ : mode == 1;
+        const double* gsrc = gv ? gv : g_.get();
+        cg_tol_ = jac ? tol_direct_ : 1e-8;
+        const int maxit = jac ? max_direct_ : max_cg_;
+        if (maxit != cg_max_) {
+            cg_max_ = maxit;
+            REGOT_CUDA(cudaMemcpyAsync(&S->max_it, &cg_max_, sizeof(int), cudaMemcpyHostToDevice,
+                                       st_));
+        }
         REGOT_CUDA(cudaMemcpyAsync(&S->shift, &shift, sizeof(double), cudaMemcpyHostToDevice,
                                    st_));
         REGOT_CUDA(cudaMemsetAsync(dir_.get(), 0, (size_t)(n_ + m_) * sizeof(double), st_));
         if (m1_ <= 0) {
-            k_schur_rhs_rows<<<cdiv(n_, kVT), kVT, 0, st_>>>(n_, g_.get(), h_.get(), S,
-                                                             dir_.get());
+            k_schur_rhs_rows<<<cdiv(n_, kVT), kVT, 0, st_>>>(n_, gsrc, h_.get(), S, dir_.get());
             count_launch();
             return;
         }
@@ -997,18 +1112,18 @@ public:
         const int gc = cdiv((long long)m1_ * 32, 32 * kSpWarps);
         const int bt = 32 * kSpWarps;
         const double* diag = nullptr;
-        if (jacobi_) {
+        if (jac) {
             k_schur_diag<TM><<<gc, bt, 0, st_>>>(S_, h_.get(), S, diag_.get());
             count_launch();
             diag = diag_.get();
         }
-        k_schur_rhs_rows<<<cdiv(n_, kVT), kVT, 0, st_>>>(n_, g_.get(), h_.get(), S, u_.get());
+        k_schur_rhs_rows<<<cdiv(n_, kVT), kVT, 0, st_>>>(n_, gsrc, h_.get(), S, u_.get());
         double* x = dir_.get() + n_;
-        k_schur_init<TM><<<gc, bt, 0, st_>>>(S_, g_.get(), u_.get(), diag, cg_tol_, x, rv_.get(),
+        k_schur_init<TM><<<gc, bt, 0, st_>>>(S_, gsrc, u_.get(), diag, cg_tol_, x, rv_.get(),
                                              z_.get(), p_.get(), parts_.get(), S);
         count_launch(2);
         REGOT_CHECK_LAUNCH();
-        if (!exec_ || graph_jacobi_ != jacobi_) build_graph(diag);
+        if (!exec_ || graph_jacobi_ != jac) build_graph(diag, jac);
         int batch = 8;
         for (;;) {
             for (int q = 0; q < batch; ++q) REGOT_CUDA(cudaGraphLaunch(exec_, st_));
@@ -1019,7 +1134,7 @@ public:
             if (done) break;
             batch = std::min(batch * 2, 64);
         }
-        k_schur_back<TM><<<gr, bt, 0, st_>>>(S_, g_.get(), h_.get(), dir_.get(), S);
+        k_schur_back<TM><<<gr, bt, 0, st_>>>(S_, gsrc, h_.get(), dir_.get(), S);
         count_launch();
         REGOT_CHECK_LAUNCH();
     }
@@ -1092,13 +1207,119 @@ public:
         return (long long)zc;
     }
 
+    // ---- sinkhorn_sparse_newton / sinkhorn_splr pieces ----
+    double* g() { return g_.get(); }
+    double* dir() { return dir_.get(); }
+
+    // sparsify_mat_with_density of T(gamma) with preserve = true
+    // (sinkhorn_sparsify4.cpp:77-174), right after grad(): the largest
+    // k = floor(n (m-1) density) entries of T[:, :m-1] (every entry tied with
+    // the k-th largest value is kept too; the reference's nth_element keeps
+    // an arbitrary subset of such ties), the first column and the first row.
+    void sparsify_density(double density) {
+        if (m1_ <= 0) return;
+        const DenseArgs a = dense_args();
+        if (!topk_.get()) {
+            topk_.alloc(1, st_);
+            hist_.alloc(kBins, st_);
+        }
+        zeros_.zero();
+        dim3 tgrid(cdiv(m1_, 32), cdiv(n_, 32));
+        k_tt<TM><<<tgrid, dim3(32, 8), 0, st_>>>(a, tt_.get(), ldt_, zeros_.get());
+        count_launch();
+        const double dd = std::min(std::max(density, 0.0), 1.0);
+        const unsigned long long len = (unsigned long long)n_ * (unsigned long long)m1_;
+        const unsigned long long k = (unsigned long long)((double)len * dd);
+        TopK t0{0ull, 0ull, k, k == 0 ? 1 : 0};
+        h2d(topk_.get(), &t0, sizeof(TopK), st_);
+        if (k > 0) {
+            const int grid = std::max(1, device_sm_count() * 4);
+            int hi = Digits<TM>::kTop;
+            bool first = true;
+            while (hi >= 0) {
+                const int width = first ? 11 : ((hi + 1) % 11 == 0 ? 11 : 10);
+                const int lo = hi - width + 1 > 0 ? hi - width + 1 : 0;
+                const int nb = 1 << (hi - lo + 1);
+                REGOT_CUDA(cudaMemsetAsync(hist_.get(), 0, (size_t)nb * sizeof(unsigned), st_));
+                k_topk_hist<TM><<<grid, 256, 0, st_>>>(tt_.get(), ldt_, n_, m1_, topk_.get(), lo,
+                                                       nb, hist_.get());
+                k_topk_pick<<<1, 256, 0, st_>>>(topk_.get(), hist_.get(), lo, nb);
+                count_launch(2);
+                passes_ += 1;
+                hi = lo - 1;
+                first = false;
+            }
+        }
+        k_topk_finish<TM><<<cdiv(m1_, kVT), kVT, 0, st_>>>(topk_.get(), m1_, xcol_.get());
+        RowStageArgs r;
+        r.ldr = m1_;
+        r.cache = row_cache_ ? 1 : 0;
+        r.lds = lds_;
+        r.keep_row0 = 1;
+        k_row_stage<TM><<<row_grid_, kSelThreads, row_smem_, st_>>>(
+            a, r, xcol_.get(), (double)INFINITY, row_scratch_.get(), yrow_.get(), rcount_.get(),
+            rcols_.get(), rvals_.get());
+        k_csc_fill<TM><<<col_grid_, kSelThreads, col_smem_, st_>>>(
+            tt_.get(), ldt_, n_, m1_, xcol_.get(), yrow_.get(), n_, col_cache_ ? 1 : 0,
+            ccount_.get(), crows_.get(), cvals_.get());
+        k_nnz<<<cdiv(n_, kVT), kVT, 0, st_>>>(rcount_.get(), n_, parts_.get(), state_.get());
+        count_launch(4);
+        REGOT_CHECK_LAUNCH();
+        passes_ += 3;
+    }
+
+    // Objective and gradient (host, n + m - 1 entries) at the host point x
+    // (n + m entries, beta_m = 0), one pass. FP64 forms f directly; mixed
+    // precision returns f0 + step g0'd + reg sum T(x) e^(-s w) phi(s w)
+    // (OP_E_GRADLS at x along dir with step s), the change from the base
+    // point without cancellation.
+    double trial(const std::vector<double>& x, double step, double f0, double g0d,
+                 std::vector<double>& gx) {
+        const int N = n_ + m_;
+        if (!xt_.get()) {
+            xt_.alloc(N, st_);
+            tsum_.alloc(N + 1, st_);
+            tmx_.alloc(1, st_);
+        }
+        h2d(xt_.get(), x.data(), N * sizeof(double), st_);
+        double* r = tsum_.get();
+        double* c = r + n_;
+        if (mixed_)
+            ops_.grad_ls(xt_.get(), xt_.get() + n_, dir_.get(), dir_.get() + n_, step, r, c,
+                         r + N, tmx_.get());
+        else
+            ops_.row_col_sums(xt_.get(), xt_.get() + n_, r, c, tmx_.get());
+        ++passes_;
+        const int cnt = mixed_ ? N + 1 : N;
+        double* h = static_cast<double*>(ctx_stage(P_->ctx, (size_t)cnt * sizeof(double)));
+        d2h(h, r, (size_t)cnt * sizeof(double), st_);
+        sync(st_);
+        double tsum = 0.0, lin = 0.0;
+        for (int i = 0; i < n_; ++i) {
+            gx[i] = h[i] - P_->ha[i];
+            tsum += h[i];
+            lin += x[i] * P_->ha[i];
+        }
+        for (int j = 0; j < m1_; ++j) {
+            gx[n_ + j] = h[n_ + j] - P_->hb[j];
+            lin += x[n_ + j] * P_->hb[j];
+        }
+        if (mixed_) return f0 + (step * g0d + reg_ * h[N]);
+        return reg_ * tsum - lin;
+    }
+
+    // gamma <- the host point x (n + m entries)
+    void set_gamma(const std::vector<double>& x) {
+        h2d(gamma_.get(), x.data(), (size_t)(n_ + m_) * sizeof(double), st_);
+    }
+
     ~SsnsEngine() {
         if (exec_) cudaGraphExecDestroy(exec_);
         if (graph_) cudaGraphDestroy(graph_);
     }
 
 private:
-    void build_graph(const double* diag) {
+    void build_graph(const double* diag, bool jac) {
         if (exec_) cudaGraphExecDestroy(exec_);
         if (graph_) cudaGraphDestroy(graph_);
         exec_ = nullptr;
@@ -1123,7 +1344,7 @@ private:
         REGOT_CUDA(cudaStreamEndCapture(st_, &graph_));
         g_launch_counter = saved;
         REGOT_CUDA(cudaGraphInstantiate(&exec_, graph_, 0));
-        graph_jacobi_ = jacobi_;
+        graph_jacobi_ = jac;
     }
 
     regot_dproblem* P_;
@@ -1133,9 +1354,12 @@ private:
     double reg_;
     bool mixed_;
     bool jacobi_ = true;
-    double cg_tol_ = 1e-10;
-    int cg_max_ = 0;
+    double cg_tol_ = 1e-10, tol_direct_ = 1e-10;
+    int cg_max_ = 0, max_cg_ = 0, max_direct_ = 0;
     DBuf<double> gamma_, g_, h_, dir_, u_, rv_, z_, p_, q_, diag_, parts_, lsout_;
+    DBuf<double> xt_, tsum_, tmx_;
+    DBuf<TopK> topk_;
+    DBuf<unsigned> hist_;
     DBuf<SsnState> state_;
     DBuf<unsigned long long> zeros_;
     long long ldt_ = 0, lds_ = 0;
@@ -1162,6 +1386,8 @@ void run_ssns(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max
     constexpr double rho_t1 = 0.25, rho_t2 = 0.75, mu_s1 = 4.0, mu_s2 = 0.5, kappa = 0.001,
                      nu0 = 0.01;
     double mu = o.mu0 > 0.0 ? o.mu0 : 1.0;
+    require(o.method < 0 || o.method == 0 || o.method == 1,
+            "sinkhorn_ssns: method must be 0 (CG) or 1 (direct)");
     SsnsEngine<TM> E(ctx, P, reg, o);
     ErotOps& ops = E.ops();
 
@@ -1252,6 +1478,183 @@ void run_ssns(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max
                        hist.get() + 3 * L, L, L, i, E.passes(), o, res);
 }
 
+// sinkhorn_sparse_newton_internal (sinkhorn_sparse_newton.cpp:24-171) and
+// sinkhorn_splr_internal (sinkhorn_splr.cpp:24-200). Each iteration: the
+// direction from the density-sparsified Hessian with shift
+// min(gnorm, shift) (SPLR: plus the BFGS correction of solve_low_rank,
+// sinkhorn_linsolve.cpp:160-225, when y's > 1e-6 y'y), the More-Thuente
+// line search from min(1, 1.5 alpha) with one dense pass per trial, the
+// gradient pass at the new point, the density update and the
+// sparsification. The driver keeps gamma, g and the direction on the host
+// in FP64 (n + m entries each).
+template <typename TM>
+void run_sparse_newton(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
+                       const regot_opts& o, regot_result* res, bool splr) {
+    using clock = std::chrono::steady_clock;
+    cudaStream_t st = ctx->stream;
+    const int n = P->n, m = P->m, N = n + m, N1 = n + m - 1;
+    const double density_max = o.density > 0.0 ? o.density : 0.01;
+    const double density_min = 0.01 * density_max;
+    double density = 0.1 * density_max;
+    const double shift_max = o.shift;
+    constexpr double eps = 1e-6;
+    SsnsEngine<TM> E(ctx, P, reg, o);
+    ErotOps& ops = E.ops();
+    auto density_T2H = [&](double d) {  // sinkhorn_sparse_newton.cpp:17-22
+        const double nnz = 2.0 * d * n * (m - 1) + n + m - 1;
+        return nnz / double(n + m - 1) / double(n + m - 1);
+    };
+    std::vector<double> gamma(N, 0.0), gamma_pre(N, 0.0), g(N, 0.0), g_pre(N, 0.0),
+        dir(N, 0.0), x(N, 0.0), gx(N, 0.0), y(N, 0.0), sv(N, 0.0), ir(N, 0.0), iy(N, 0.0);
+    // Initial value (sinkhorn_sparse_newton.cpp:56-65)
+    if (o.x0 && o.x0_len == N1) {
+        std::copy(o.x0, o.x0 + N1, gamma.begin());
+    } else {
+        DBuf<double> beta(m, st), zero(n, st), mx(1, st);
+        zero.zero();
+        ops.optimal_beta(zero.get(), beta.get(), mx.get());
+        std::vector<double> hb(m);
+        read_small(ctx, hb.data(), beta.get(), m * sizeof(double), st);
+        for (int i = 0; i < n; ++i) gamma[i] = hb[m - 1];
+        for (int j = 0; j < m - 1; ++j) gamma[n + j] = hb[j] - hb[m - 1];
+    }
+    E.set_gamma(gamma);
+    auto lin = [&](const std::vector<double>& v) {  // alpha'a + beta~'b~
+        double s = 0.0;
+        for (int i = 0; i < n; ++i) s += v[i] * P->ha[i];
+        for (int j = 0; j < m - 1; ++j) s += v[n + j] * P->hb[j];
+        return s;
+    };
+    auto read_g = [&]() {
+        d2h(g.data(), E.g(), (size_t)N * sizeof(double), st);
+        sync(st);
+    };
+    auto dot = [&](const std::vector<double>& u, const std::vector<double>& v) {
+        double s = 0.0;
+        for (int q = 0; q < N1; ++q) s += u[q] * v[q];
+        return s;
+    };
+    auto ms_since = [](clock::time_point t) {
+        return std::chrono::duration<double, std::milli>(clock::now() - t).count();
+    };
+
+    std::vector<double> hobj, hmar, htime, hdens;
+    auto t0 = clock::now();
+    E.grad();
+    SsnState hs = E.read_state();
+    double f = hs.f, gnorm = hs.gnorm;
+    const double gnorm_init = gnorm;
+    read_g();
+    E.sparsify_density(density);
+    sync(st);
+    hobj.push_back(f);
+    hmar.push_back(gnorm);
+    htime.push_back(ms_since(t0));
+    hdens.push_back(density_T2H(density));
+    double alpha = 1.0;
+    DBuf<double> ny(N, st);
+    int i;
+    for (i = 0; i < max_iter; i++) {
+        if (o.verbose >= 1) std::printf("iter = %d, objval = %g, ||grad|| = %g\n", i, f, gnorm);
+        const auto t_it = clock::now();
+        if (gnorm < tol || !std::isfinite(f)) break;
+        const double shift = std::min(gnorm, shift_max);
+        bool low_rank = false;
+        double ys = 0.0;
+        if (splr) {
+            double yy = 0.0;
+            for (int q = 0; q < N1; ++q) {
+                y[q] = g[q] - g_pre[q];
+                sv[q] = gamma[q] - gamma_pre[q];
+                ys += y[q] * sv[q];
+                yy += y[q] * y[q];
+            }
+            low_rank = i > 0 && ys > eps * yy;
+        }
+        if (low_rank) {
+            // res = A^-1 r + ((1 + y'A^-1 y / y's) r's / y's - y'A^-1 r / y's) s
+            //       - (r's / y's) A^-1 y, r = -g, A = H_s + shift I, both
+            // solves by the direct-solve stand-in (the reference factors A)
+            std::vector<double> negy(N, 0.0);
+            for (int q = 0; q < N1; ++q) negy[q] = -y[q];
+            h2d(ny.get(), negy.data(), (size_t)N * sizeof(double), st);
+            E.direction(shift, ny.get(), 1);
+            d2h(iy.data(), E.dir(), (size_t)N * sizeof(double), st);
+            E.direction(shift, nullptr, 1);
+            d2h(ir.data(), E.dir(), (size_t)N * sizeof(double), st);
+            sync(st);
+            double rs = 0.0, yiy = 0.0, yir = 0.0;
+            for (int q = 0; q < N1; ++q) {
+                rs -= sv[q] * g[q];
+                yiy += y[q] * iy[q];
+                yir += y[q] * ir[q];
+            }
+            const double rs_ys = rs / ys;
+            const double cs = (1.0 + yiy / ys) * rs_ys - yir / ys;
+            for (int q = 0; q < N1; ++q) dir[q] = ir[q] + cs * sv[q] - rs_ys * iy[q];
+            dir[N1] = 0.0;
+            h2d(E.dir(), dir.data(), (size_t)N * sizeof(double), st);
+        } else {
+            E.direction(shift);
+            d2h(dir.data(), E.dir(), (size_t)N * sizeof(double), st);
+            sync(st);
+        }
+        // Wolfe line search: one pass per trial
+        const double g0d = dot(g, dir);
+        auto eval = [&](double step, double* fx, double* dg) {
+            for (int q = 0; q < N; ++q) x[q] = gamma[q] + step * dir[q];
+            *fx = E.trial(x, step, f, g0d, gx);
+            *dg = dot(gx, dir);
+        };
+        const wolfe::Outcome ls = wolfe::search(std::min(1.0, 1.5 * alpha), f, g0d, eval);
+        alpha = ls.step;
+        gamma_pre = gamma;
+        for (int q = 0; q < N; ++q) gamma[q] = gamma_pre[q] + alpha * dir[q];
+        g_pre = g;
+        if (!ls.recompute && ls.last_eval != alpha) {
+            // The reference keeps T of the last trial (sinkhorn_splr.cpp:147):
+            // sums and the sparsification come from T there, the objective's
+            // linear terms from the new point.
+            for (int q = 0; q < N; ++q) x[q] = gamma_pre[q] + ls.last_eval * dir[q];
+            E.set_gamma(x);
+            E.grad();
+            hs = E.read_state();
+            f = hs.f + (lin(x) - lin(gamma));
+        } else {
+            E.set_gamma(gamma);
+            E.grad();
+            hs = E.read_state();
+            f = hs.f;
+        }
+        const double gnorm_pre = gnorm;
+        gnorm = hs.gnorm;
+        read_g();
+        if (splr) {
+            const bool bad = gnorm_pre < gnorm_init && gnorm > gnorm_pre;
+            density *= bad ? 1.1 : 0.99;
+        } else {
+            const bool bad = gnorm_pre < gnorm_init && gnorm > 1.1 * gnorm_pre;
+            density *= bad ? 2.0 : 0.9;
+        }
+        density = std::min(density_max, std::max(density_min, density));
+        E.sparsify_density(density);
+        E.set_gamma(gamma);
+        sync(st);
+        hobj.push_back(f);
+        hmar.push_back(gnorm);
+        htime.push_back(htime.back() + ms_since(t_it));
+        hdens.push_back(density_T2H(density));
+    }
+    const int L = (int)hobj.size();
+    DBuf<double> hist(4 * (size_t)std::max(L, 1), st);
+    h2d(hist.get(), hobj.data(), L * sizeof(double), st);
+    h2d(hist.get() + L, hmar.data(), L * sizeof(double), st);
+    h2d(hist.get() + 2 * L, htime.data(), L * sizeof(double), st);
+    h2d(hist.get() + 3 * L, hdens.data(), L * sizeof(double), st);
+    finish_erot_result(ops, E.gamma(), hist.get(), hist.get() + L, hist.get() + 2 * L,
+                       hist.get() + 3 * L, L, L, i, E.passes(), o, res);
+}
+
 template <typename TM>
 void sparsify_at(regot_ctx* ctx, regot_dproblem* P, double reg, const double* gamma,
                  double delta, double density_hint, long long* nnz, int* mask) {
@@ -1263,12 +1666,18 @@ void sparsify_at(regot_ctx* ctx, regot_dproblem* P, double reg, const double* ga
     std::copy(gamma, gamma + n + m - 1, h.begin());
     h2d(E.gamma(), h.data(), (n + m) * sizeof(double), ctx->stream);
     E.grad();
-    E.sparsify(delta, density_hint);
+    // delta < 0 selects the density sparsification (density in density_hint)
+    if (delta < 0.0) {
+        E.sparsify_density(density_hint);
+        E.read_state();
+    } else {
+        E.sparsify(delta, density_hint);
+    }
     const SsnState hs = E.read_state();
     const long long stored = (long long)hs.nnz;
     require(E.csc_nnz() == stored, "CSR and CSC copies of the sparsified matrix differ",
             REGOT_ERR_NUMERIC);
-    *nnz = stored + E.zero_count();
+    *nnz = delta < 0.0 ? stored : stored + E.zero_count();
     if (mask) E.kept_mask(mask);
     E.ops().check_err();
 }
@@ -1289,6 +1698,30 @@ void sinkhorn_ssns_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol
         run_ssns<float>(ctx, P, reg, tol, max_iter, o, res);
     else
         run_ssns<double>(ctx, P, reg, tol, max_iter, o, res);
+}
+
+void erot_sparsify_density_gpu(regot_ctx* ctx, regot_dproblem* P, double reg,
+                               const double* gamma, double density, long long* nnz, int* mask) {
+    if (P->prec == REGOT_PREC_MIXED)
+        sparsify_at<float>(ctx, P, reg, gamma, -1.0, density, nnz, mask);
+    else
+        sparsify_at<double>(ctx, P, reg, gamma, -1.0, density, nnz, mask);
+}
+
+void sinkhorn_sparse_newton_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol,
+                                int max_iter, const regot_opts& o, regot_result* res) {
+    if (P->prec == REGOT_PREC_MIXED)
+        run_sparse_newton<float>(ctx, P, reg, tol, max_iter, o, res, false);
+    else
+        run_sparse_newton<double>(ctx, P, reg, tol, max_iter, o, res, false);
+}
+
+void sinkhorn_splr_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
+                       const regot_opts& o, regot_result* res) {
+    if (P->prec == REGOT_PREC_MIXED)
+        run_sparse_newton<float>(ctx, P, reg, tol, max_iter, o, res, true);
+    else
+        run_sparse_newton<double>(ctx, P, reg, tol, max_iter, o, res, true);
 }
 
 }  // namespace regot

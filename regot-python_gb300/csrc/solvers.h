@@ -13,6 +13,12 @@ void sinkhorn_newton_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double t
                          const regot_opts& o, regot_result* res);
 void sinkhorn_ssns_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
                        const regot_opts& o, regot_result* res);
+void sinkhorn_sparse_newton_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol,
+                                int max_iter, const regot_opts& o, regot_result* res);
+void sinkhorn_splr_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
+                       const regot_opts& o, regot_result* res);
+void erot_sparsify_density_gpu(regot_ctx* ctx, regot_dproblem* P, double reg,
+                               const double* gamma, double density, long long* nnz, int* mask);
 void sinkhorn_lbfgs_dual_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol,
                              int max_iter, const regot_opts& o, regot_result* res);
 void sinkhorn_apdagd_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,

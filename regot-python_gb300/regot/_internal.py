@@ -37,6 +37,7 @@ from . import _lib as L
 
 __all__ = [
     "sinkhorn_bcd", "sinkhorn_newton", "sinkhorn_ssns", "sinkhorn_lbfgs_dual", "sinkhorn_apdagd",
+    "sinkhorn_sparse_newton", "sinkhorn_splr",
     "qrot_lbfgs_dual", "qrot_assn", "qrot_bcd", "qrot_gd", "qrot_apdagd", "qrot_pdaam",
     "qrot_grssn", "qrot_lbfgs_semi_dual", "sinkhorn_result", "qrot_result",
     "Problem",
@@ -227,7 +228,8 @@ class Problem:
         res.run_times = hist[2, :k].tolist()
         if qrot:
             res.prim_vals = hist[4, :k].tolist()
-        elif fname == "regot_sinkhorn_ssns":
+        elif fname in ("regot_sinkhorn_ssns", "regot_sinkhorn_sparse_newton",
+                       "regot_sinkhorn_splr"):
             res.densities = hist[3, :k].tolist()
         res.passes = int(r.passes)
         res.solve_ms = float(r.solve_ms)
@@ -244,6 +246,12 @@ class Problem:
 
     def sinkhorn_ssns(self, reg, tol=1e-6, max_iter=1000, verbose=0, **kw):
         return self._solve("regot_sinkhorn_ssns", reg, tol, max_iter, verbose, kw, False)
+
+    def sinkhorn_sparse_newton(self, reg, tol=1e-6, max_iter=1000, verbose=0, **kw):
+        return self._solve("regot_sinkhorn_sparse_newton", reg, tol, max_iter, verbose, kw, False)
+
+    def sinkhorn_splr(self, reg, tol=1e-6, max_iter=1000, verbose=0, **kw):
+        return self._solve("regot_sinkhorn_splr", reg, tol, max_iter, verbose, kw, False)
 
     def sinkhorn_lbfgs_dual(self, reg, tol=1e-6, max_iter=1000, verbose=0, **kw):
         return self._solve("regot_sinkhorn_lbfgs_dual", reg, tol, max_iter, verbose, kw, False)
@@ -403,6 +411,17 @@ class Problem:
             float(density_hint), nnz.ctypes.data, K.ctypes.data if mask else None))
         return int(nnz[0]), (K.astype(bool) if mask else None)
 
+    def erot_sparsify_density(self, reg, gamma, density, mask=True):
+        """sparsify_mat_with_density of T(gamma) (sinkhorn_sparsify4.cpp:77-174,
+        first row and column preserved): returns (nnz, kept) as erot_sparsify."""
+        gamma = self._vec(gamma, self.n + self.m - 1)
+        nnz = np.zeros(1, dtype=np.int64)
+        K = np.zeros((self.n, self.m - 1), dtype=np.int32) if mask else None
+        self.ctx.check(self._lib.regot_erot_sparsify_density(
+            self.ctx.handle, self.handle, float(reg), gamma.ctypes.data, float(density),
+            nnz.ctypes.data, K.ctypes.data if mask else None))
+        return int(nnz[0]), (K.astype(bool) if mask else None)
+
     def qrot_dual_obj_grad(self, reg, gamma):
         gamma = self._vec(gamma, self.n + self.m)
         obj = np.zeros(1)
@@ -463,6 +482,20 @@ def sinkhorn_newton(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
 def sinkhorn_ssns(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
     """Safe and sparse Newton for EROT; reference src/sinkhorn_ssns.cpp:16-234."""
     return _solve("sinkhorn_ssns", M, a, b, reg, tol, max_iter, verbose, kwargs)
+
+
+def sinkhorn_sparse_newton(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
+    """Newton's method with a density-sparsified Hessian for EROT; reference
+    src/sinkhorn_sparse_newton.cpp:24-171. kwargs: ``density`` (0.01),
+    ``shift`` (1e-3), ``method`` (1)."""
+    return _solve("sinkhorn_sparse_newton", M, a, b, reg, tol, max_iter, verbose, kwargs)
+
+
+def sinkhorn_splr(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
+    """Sparse-plus-low-rank quasi-Newton method for EROT; reference
+    src/sinkhorn_splr.cpp:24-200. kwargs: ``density`` (0.01), ``shift``
+    (1e-3), ``method`` (1)."""
+    return _solve("sinkhorn_splr", M, a, b, reg, tol, max_iter, verbose, kwargs)
 
 
 def sinkhorn_lbfgs_dual(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):

@@ -113,10 +113,12 @@ EXPORTS = [
     "regot_ctx_set_stream", "regot_ctx_own_stream", "regot_ctx_kernel_launches", "regot_problem_create",
     "regot_problem_destroy", "regot_sinkhorn_bcd", "regot_sinkhorn_newton",
     "regot_sinkhorn_ssns", "regot_sinkhorn_lbfgs_dual", "regot_sinkhorn_apdagd",
+    "regot_sinkhorn_sparse_newton", "regot_sinkhorn_splr",
     "regot_qrot_lbfgs_dual", "regot_qrot_assn", "regot_qrot_bcd", "regot_qrot_gd",
     "regot_qrot_apdagd", "regot_qrot_pdaam", "regot_qrot_grssn", "regot_qrot_lbfgs_semi_dual",
     "regot_qrot_optimal_alpha", "regot_erot_optimal_beta", "regot_erot_optimal_alpha", "regot_erot_dual_obj_grad",
-    "regot_erot_hvp", "regot_erot_plan", "regot_erot_sparsify", "regot_erot_hess_solve",
+    "regot_erot_hvp", "regot_erot_plan", "regot_erot_sparsify", "regot_erot_sparsify_density",
+    "regot_erot_hess_solve",
     "regot_erot_tyy", "regot_erot_solve_batched", "regot_qrot_dual_obj_grad",
     "regot_qrot_optimal_beta",
     "regot_qrot_primal_val", "regot_qrot_plan", "regot_time_pass",
@@ -155,6 +157,7 @@ def load() -> C.CDLL:
         lib.regot_problem_destroy.argtypes = [vp]
         lib.regot_problem_destroy.restype = None
         for name in ("regot_sinkhorn_bcd", "regot_sinkhorn_newton", "regot_sinkhorn_ssns",
+                     "regot_sinkhorn_sparse_newton", "regot_sinkhorn_splr",
                      "regot_sinkhorn_lbfgs_dual", "regot_sinkhorn_apdagd",
                      "regot_qrot_lbfgs_dual", "regot_qrot_assn", "regot_qrot_bcd",
                      "regot_qrot_gd", "regot_qrot_apdagd", "regot_qrot_pdaam",
@@ -169,6 +172,7 @@ def load() -> C.CDLL:
         lib.regot_erot_plan.argtypes = [vp, vp, C.c_double, vp, vp, C.c_int]
         lib.regot_erot_sparsify.argtypes = [vp, vp, C.c_double, vp, C.c_double, C.c_double, vp,
                                              vp]
+        lib.regot_erot_sparsify_density.argtypes = [vp, vp, C.c_double, vp, C.c_double, vp, vp]
         lib.regot_qrot_dual_obj_grad.argtypes = [vp, vp, C.c_double, vp, vp, vp]
         lib.regot_qrot_optimal_beta.argtypes = [vp, vp, C.c_double, vp, vp]
         lib.regot_qrot_primal_val.argtypes = [vp, vp, C.c_double, vp, vp]

@@ -344,3 +344,78 @@ def test_qrot_grssn_and_semi_dual_reach_the_optimum():
         step *= 0.5
     r1 = O.qrot_grssn(M, a, b, reg, tol=1e-14, max_iter=1, plan=False)
     np.testing.assert_allclose(r1.dual, gam + step * d, rtol=0, atol=1e-7)
+
+
+def _sparsify_density_np(T, density):
+    """sparsify_mat_with_density restated in numpy (distinct values)."""
+    n, m = T.shape
+    Tt = T[:, :-1]
+    k = int(Tt.size * min(max(density, 0.0), 1.0))
+    K = np.zeros(Tt.shape, dtype=bool)
+    if k > 0:
+        order = np.argsort(Tt.ravel(order="F"), kind="stable")
+        K.ravel(order="F")[order[Tt.size - k:]] = True
+        K = K.reshape(Tt.shape, order="F") if not K.flags.f_contiguous else K
+        flat = np.zeros(Tt.size, dtype=bool)
+        flat[order[Tt.size - k:]] = True
+        K = flat.reshape(Tt.shape, order="F")
+    K[:, 0] = True
+    K[0, :] = True
+    return K
+
+
+@pytest.mark.parametrize("density", [0.0, 0.003, 0.05, 0.4, 1.0])
+def test_sparsify_density_matches_definition(density):
+    rng = np.random.default_rng(17)
+    for trial in range(3):
+        n, m = rng.integers(20, 90), rng.integers(20, 90)
+        T = np.exp(rng.standard_normal((n, m)) * 4.0 - 6.0) / (n * m)
+        outer, inner, vals = O.sparsify_density(T, density)
+        K = np.zeros((n, m - 1), dtype=bool)
+        for j in range(m - 1):
+            K[inner[outer[j]:outer[j + 1]], j] = True
+        np.testing.assert_array_equal(K, _sparsify_density_np(T, density))
+        np.testing.assert_array_equal(vals, T[:, :-1].T[K.T])
+
+
+@pytest.mark.parametrize("coefs,init", [
+    ([0.0, -1.0, 0.5, 0.0, 0.0], 1.0),     # minimiser at 1: accepted at once
+    ([0.0, -1.0, 50.0, 0.0, 0.0], 1.0),    # minimiser at 0.01: interpolation
+    ([0.0, -1.0, 0.01, 0.0, 0.0], 1.0),    # minimiser at 50: extrapolation to 2
+    ([0.0, -1.0, 0.3, -0.4, 0.2], 0.5),    # quartic
+    ([1.0, -3.0, 0.0, 2.0, 0.5], 1.5),
+])
+def test_wolfe_line_search_conditions(coefs, init):
+    """line_search_wolfe (sinkhorn_problem_ls.cpp:226-436): the returned step
+    satisfies the strong Wolfe conditions, or is the upper bound 2 with
+    sufficient decrease."""
+    c = np.array(coefs, dtype=float)
+    f = np.polynomial.Polynomial(c)
+    df = f.deriv()
+    step, recompute, nev = O.wolfe_poly(c, init)
+    assert 1 <= nev <= 20 and not recompute
+    suff = f(step) <= f(0) + 1e-4 * step * df(0)
+    curv = abs(df(step)) <= 0.9 * abs(df(0))
+    assert suff and (curv or step == 2.0)
+
+
+def test_wolfe_line_search_ascent_direction():
+    step, recompute, nev = O.wolfe_poly([0.0, 1.0, 1.0, 0.0, 0.0], 0.7)
+    assert step == 0.7 and recompute and nev == 0
+
+
+@pytest.mark.parametrize("solver,tol", [("sinkhorn_sparse_newton", 1e-7), ("sinkhorn_splr", 1e-8)])
+def test_erot_sparse_newton_and_splr_reach_the_optimum(solver, tol):
+    # The sparsified Newton steps converge linearly (the density falls to
+    # 1 % of its maximum); SPLR's low-rank correction converges much faster.
+    M, a, b = erot_points(40, 30, seed=12, dtype=np.float64)
+    reg = 0.1
+    rn = O.sinkhorn_newton(M, a, b, reg, tol=1e-11, max_iter=100)
+    r = getattr(O, solver)(M, a, b, reg, tol=tol, max_iter=2000, density=0.5)
+    assert r.niter < 2000 and r.mar_errs[-1] < tol
+    np.testing.assert_allclose(r.obj_vals[-1], rn.obj_vals[-1], rtol=1e-9)
+    np.testing.assert_allclose(r.plan, rn.plan, rtol=0, atol=1e-5 * rn.plan.max())
+    # densities record density_T2H of the density parameter
+    n, m = M.shape
+    d0 = 0.1 * 0.5
+    np.testing.assert_allclose(r.densities[0], (2 * d0 * n * (m - 1) + n + m - 1) / (n + m - 1) ** 2)
