@@ -188,6 +188,27 @@ int regot_qrot_grssn(regot_ctx* ctx, regot_dproblem* prob, double reg, double to
  * semi-dual in alpha, beta = optimal_beta(alpha); dual = (alpha, beta). */
 int regot_qrot_lbfgs_semi_dual(regot_ctx* ctx, regot_dproblem* prob, double reg, double tol,
                                int max_iter, const regot_opts* opts, regot_result* res);
+/* Options of qrot_pdip (PDIPSolverOpts, src/pdip_solvers.h:16-35, as parsed
+ * by parse_pdip_opts, src/solvers.cpp:203-239). */
+typedef struct {
+    int inner_solver;         /* 0 = "cg" (default), 1 = "fp" */
+    int cg_max_iter;          /* 1000 */
+    double fixed_threshold;   /* 1e-9 */
+    int fp_max_iter;          /* 800 */
+    double fp_exit_scale;     /* 1e-2 */
+    int fp_stop_gap_mu_only;  /* 1 */
+    int cg_stop_gap_mu_only;  /* 0 */
+    double cg_mar_tol;        /* 1e-10 */
+} regot_pdip_opts;
+void regot_pdip_opts_init(regot_pdip_opts* popts);
+/* qrot_pdip (src/solvers.cpp:268-292; pdip_cg.cpp:206-413 and
+ * pdip_fp.cpp:278-667): primal-dual interior point for QROT. Fills niter,
+ * hist_len, obj_vals, mar_errs, run_times and the plan (the primal x) of
+ * res (res->dual is not used); *converged (may be NULL) receives the
+ * converged flag. Only opts->verbose, plan and plan_mem are read. */
+int regot_qrot_pdip(regot_ctx* ctx, regot_dproblem* prob, double reg, double tol, int max_iter,
+                    const regot_pdip_opts* popts, const regot_opts* opts, regot_result* res,
+                    int* converged);
 /* qrot_assn (src/qrot_assn.cpp:16-170). */
 int regot_qrot_assn(regot_ctx* ctx, regot_dproblem* prob, double reg, double tol,
                     int max_iter, const regot_opts* opts, regot_result* res);

@@ -16,7 +16,8 @@
  *   src/qrot_problem.cpp, src/approx_proj.h, src/qrot_result.h,
  *   src/qrot_lbfgs_dual.cpp, src/qrot_assn.cpp, src/qrot_hess.cpp,
  *   src/qrot_bcd.cpp, src/qrot_gd.cpp, src/qrot_apdagd.cpp, src/qrot_pdaam.cpp,
- *   src/qrot_grssn.cpp, src/qrot_lbfgs_semi_dual.cpp,
+ *   src/qrot_grssn.cpp, src/qrot_lbfgs_semi_dual.cpp, src/pdip_cg.cpp, src/pdip_fp.cpp,
+ *   src/pdip_transport_ops.hpp, src/pdip_block_operator.h, src/pdip_sparse_chol.cpp,
  *   src/qrot_linsolve.cpp, src/qrot_cg.cpp, src/LBFGSpp/LBFGS.h,
  *   src/LBFGSpp/LBFGSpp/BFGSMat.h, src/LBFGSpp/LBFGSpp/LineSearchNocedalWright.h,
  *   src/LBFGSpp/LBFGSpp/Param.h, src/solvers.cpp (kwargs defaults).
@@ -178,6 +179,13 @@ int oracle_qrot_lbfgs_semi_dual(const double* M, int n, int m, const double* a,
 int oracle_qrot_grssn(const double* M, int n, int m, const double* a,
                       const double* b, double reg, double tol, int max_iter,
                       int verbose, const oracle_opts* opts, oracle_result* res);
+/* qrot_pdip (pdip_cg.cpp:206-413, pdip_fp.cpp:278-667): inner_solver 0 =
+ * "cg", 1 = "fp". Plan row-major; res->dual[0] = converged flag. popts
+ * (NULL for the defaults): cg_max_iter, fixed_threshold, fp_max_iter,
+ * fp_exit_scale, fp_stop_gap_mu_only, cg_stop_gap_mu_only, cg_mar_tol. */
+int oracle_qrot_pdip(const double* M, int n, int m, const double* a,
+                     const double* b, double reg, double tol, int max_iter,
+                     int inner_solver, const double* popts, oracle_result* res);
 /* optimal_alpha: qrot_problem.cpp:409-419. */
 void oracle_qrot_optimal_alpha(const double* M, int n, int m, const double* a,
                                double reg, const double* beta, double* alpha);

@@ -221,6 +221,41 @@ def qrot_lbfgs_semi_dual(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwa
                 kwargs, _QROT_DUAL, 0, with_prim=True, plan=kwargs.get("plan", True))
 
 
+_PDIP_KEYS = ("cg_max_iter", "fixed_threshold", "fp_max_iter", "fp_exit_scale",
+              "fp_stop_gap_mu_only", "cg_stop_gap_mu_only", "cg_mar_tol")
+_PDIP_DEFAULTS = (1000, 1e-9, 800, 1e-2, True, False, 1e-10)
+
+
+def qrot_pdip(M, a, b, reg, tol=1e-8, max_iter=1000, verbose=0, **kwargs):
+    """qrot_pdip restated: namespace(niter, converged, plan, obj_vals,
+    mar_errs, run_times)."""
+    M = _colmajor(M)
+    n, m = M.shape
+    a = _f64(a).ravel()
+    b = _f64(b).ravel()
+    mode = str(kwargs.get("inner_solver", "cg")).lower()
+    popts = np.array([float(kwargs.get(k, dflt)) for k, dflt in zip(_PDIP_KEYS, _PDIP_DEFAULTS)])
+    cap = max_iter + 2
+    hist = np.zeros((3, cap))
+    plan = np.zeros((n, m))
+    flag = np.zeros(1)
+    r = _Result()
+    r.hist_cap = cap
+    r.dual = _d(flag)
+    r.plan = _d(plan)
+    r.obj_vals = _d(hist[0])
+    r.mar_errs = _d(hist[1])
+    r.run_times = _d(hist[2])
+    rc = lib().oracle_qrot_pdip(_d(M), n, m, _d(a), _d(b), C.c_double(reg), C.c_double(tol),
+                                int(max_iter), 1 if mode == "fp" else 0, _d(popts), C.byref(r))
+    if rc != 0:
+        raise RuntimeError(r.err.decode())
+    k = r.hist_len
+    return SimpleNamespace(niter=r.niter, converged=bool(flag[0]), plan=plan,
+                           obj_vals=hist[0, :k].tolist(), mar_errs=hist[1, :k].tolist(),
+                           run_times=hist[2, :k].tolist())
+
+
 def qrot_optimal_alpha(M, a, reg, beta):
     M = _colmajor(M)
     n, m = M.shape

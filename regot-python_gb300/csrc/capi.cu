@@ -460,6 +460,50 @@ REGOT_SOLVER_ENTRY(regot_qrot_pdaam, qrot_pdaam_gpu, P->n + P->m)
 REGOT_SOLVER_ENTRY(regot_qrot_grssn, qrot_grssn_gpu, P->n + P->m)
 REGOT_SOLVER_ENTRY(regot_qrot_lbfgs_semi_dual, qrot_lbfgs_semi_dual_gpu, P->n + P->m)
 
+void regot_pdip_opts_init(regot_pdip_opts* p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->inner_solver = 0;
+    p->cg_max_iter = 1000;
+    p->fixed_threshold = 1e-9;
+    p->fp_max_iter = 800;
+    p->fp_exit_scale = 1e-2;
+    p->fp_stop_gap_mu_only = 1;
+    p->cg_stop_gap_mu_only = 0;
+    p->cg_mar_tol = 1e-10;
+}
+
+int regot_qrot_pdip(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
+                    const regot_pdip_opts* popts, const regot_opts* opts, regot_result* res,
+                    int* converged) {
+    return guarded(ctx, [&] {
+        require(P != nullptr, "problem is NULL");
+        require(res != nullptr, "result is NULL");
+        require(!std::isnan(reg), "reg must not be NaN");
+        require(!std::isnan(tol), "tol must not be NaN");
+        require(max_iter >= 0, "max_iter must be non-negative");
+        require(res->hist_cap >= max_iter + 2 || (!res->obj_vals && !res->mar_errs &&
+                                                  !res->run_times),
+                "history capacity must be at least max_iter + 2");
+        regot_pdip_opts po;
+        regot_pdip_opts_init(&po);
+        if (popts) po = *popts;
+        const regot_opts o = effective_opts(opts);
+        cudaEvent_t e0, e1;
+        REGOT_CUDA(cudaEventCreate(&e0));
+        REGOT_CUDA(cudaEventCreate(&e1));
+        REGOT_CUDA(cudaEventRecord(e0, ctx->stream));
+        qrot_pdip_gpu(ctx, P, reg, tol, max_iter, po, o, res, converged);
+        REGOT_CUDA(cudaEventRecord(e1, ctx->stream));
+        REGOT_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        res->solve_ms = ms;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    });
+}
+
 // ---------------------------------------------------------------- passes --
 
 int regot_erot_optimal_beta(regot_ctx* ctx, regot_dproblem* P, double reg, const double* alpha,

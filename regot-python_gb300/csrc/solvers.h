@@ -53,6 +53,9 @@ void qrot_grssn_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, i
                     const regot_opts& o, regot_result* res);
 void qrot_lbfgs_semi_dual_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol,
                               int max_iter, const regot_opts& o, regot_result* res);
+void qrot_pdip_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
+                   const regot_pdip_opts& po, const regot_opts& o, regot_result* res,
+                   int* converged);
 void qrot_assn_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
                    const regot_opts& o, regot_result* res);
 

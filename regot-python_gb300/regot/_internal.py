@@ -39,7 +39,7 @@ __all__ = [
     "sinkhorn_bcd", "sinkhorn_newton", "sinkhorn_ssns", "sinkhorn_lbfgs_dual", "sinkhorn_apdagd",
     "sinkhorn_sparse_newton", "sinkhorn_splr",
     "qrot_lbfgs_dual", "qrot_assn", "qrot_bcd", "qrot_gd", "qrot_apdagd", "qrot_pdaam",
-    "qrot_grssn", "qrot_lbfgs_semi_dual", "sinkhorn_result", "qrot_result",
+    "qrot_grssn", "qrot_lbfgs_semi_dual", "qrot_pdip", "pdip_cg", "pdip_fp", "pdip_result", "sinkhorn_result", "qrot_result",
     "Problem",
     "sinkhorn_bcd_batched", "batch_result",
 ]
@@ -75,6 +75,27 @@ class qrot_result:
 
     def __repr__(self):
         return f"<qrot_result niter={self.niter}>"
+
+
+class pdip_result:
+    """Result of qrot_pdip (src/pdip_result.h:13-33). The per-phase timing
+    fields are filled only by the reference's developer build; they are 0."""
+
+    def __init__(self):
+        self.niter = 0
+        self.converged = False
+        self.plan = np.zeros((0, 0))
+        self.obj_vals = []
+        self.mar_errs = []
+        self.run_times = []
+        self.t_build_B = 0.0
+        self.t_chol_factor = 0.0
+        self.t_chol_solve = 0.0
+        self.t_eq_matvec = 0.0
+        self.t_other = 0.0
+
+    def __repr__(self):
+        return f"<pdip_result niter={self.niter} converged={self.converged}>"
 
 
 def _is_torch_cuda(x) -> bool:
@@ -276,6 +297,58 @@ class Problem:
 
     def qrot_pdaam(self, reg, tol=1e-6, max_iter=1000, verbose=0, **kw):
         return self._solve("regot_qrot_pdaam", reg, tol, max_iter, verbose, kw, True)
+
+    def qrot_pdip(self, reg, tol=1e-8, max_iter=1000, verbose=0, **kw):
+        """qrot_pdip (solvers.cpp:268-292): kwargs inner_solver ("cg" | "fp")
+        and the PDIPSolverOpts fields parsed by parse_pdip_opts (203-239)."""
+        mode = kw.get("inner_solver", "cg")
+        if not isinstance(mode, str):
+            raise RuntimeError(
+                'qrot_pdip: inner_solver must be a string, e.g. "cg" or "fp"')
+        mode = mode.lower()
+        if mode not in ("cg", "fp"):
+            raise RuntimeError('qrot_pdip: inner_solver must be "cg" or "fp"')
+        n, m = self.n, self.m
+        po = L.PdipOpts()
+        self._lib.regot_pdip_opts_init(C.byref(po))
+        po.inner_solver = 1 if mode == "fp" else 0
+        for key, conv in (("cg_max_iter", int), ("fixed_threshold", float),
+                          ("fp_max_iter", int), ("fp_exit_scale", float),
+                          ("fp_stop_gap_mu_only", bool), ("cg_stop_gap_mu_only", bool),
+                          ("cg_mar_tol", float)):
+            if key in kw:
+                setattr(po, key, conv(kw[key]))
+        o = L.Opts()
+        self._lib.regot_opts_init(C.byref(o))
+        o.verbose = int(verbose)
+        want_plan = bool(kw.get("plan", True))
+        o.plan = 1 if want_plan else 0
+        max_iter = int(max_iter)
+        if max_iter < 0:
+            raise ValueError("max_iter must be non-negative")
+        cap = max_iter + 2
+        hist = np.zeros((3, cap))
+        plan = L.host_empty((n, m)) if want_plan else None
+        r = L.Result()
+        r.hist_cap = cap
+        r.plan = plan.ctypes.data if want_plan else None
+        r.obj_vals = hist[0].ctypes.data
+        r.mar_errs = hist[1].ctypes.data
+        r.run_times = hist[2].ctypes.data
+        conv = C.c_int(0)
+        self.ctx.check(self._lib.regot_qrot_pdip(
+            self.ctx.handle, self.handle, float(reg), float(tol), max_iter, C.byref(po),
+            C.byref(o), C.byref(r), C.byref(conv)))
+        k = r.hist_len
+        res = pdip_result()
+        res.niter = int(r.niter)
+        res.converged = bool(conv.value)
+        res.plan = plan
+        res.obj_vals = hist[0, :k].tolist()
+        res.mar_errs = hist[1, :k].tolist()
+        res.run_times = hist[2, :k].tolist()
+        res.solve_ms = float(r.solve_ms)
+        return res
 
     def qrot_grssn(self, reg, tol=1e-6, max_iter=1000, verbose=0, **kw):
         return self._solve("regot_qrot_grssn", reg, tol, max_iter, verbose, kw, True)
@@ -545,6 +618,27 @@ def qrot_grssn(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
 def qrot_lbfgs_semi_dual(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
     """L-BFGS on the QROT semi-dual; reference src/qrot_lbfgs_semi_dual.cpp:84-126."""
     return _solve("qrot_lbfgs_semi_dual", M, a, b, reg, tol, max_iter, verbose, kwargs)
+
+
+def qrot_pdip(M, a, b, reg, tol=1e-8, max_iter=1000, verbose=0, **kwargs):
+    """Primal-dual interior point for QROT; reference src/solvers.cpp:268-292
+    (pdip_cg.cpp:206-413, pdip_fp.cpp:278-667). kwargs: ``inner_solver``
+    ("cg" or "fp"), ``cg_max_iter``, ``fixed_threshold``, ``fp_max_iter``,
+    ``fp_exit_scale``, ``fp_stop_gap_mu_only``, ``cg_stop_gap_mu_only``,
+    ``cg_mar_tol``. Returns a ``pdip_result``."""
+    return _solve("qrot_pdip", M, a, b, reg, tol, max_iter, verbose, kwargs)
+
+
+def pdip_cg(M, a, b, reg, tol=1e-8, max_iter=1000, verbose=0, **kwargs):
+    """``qrot_pdip`` with the CG inner solver (solvers.cpp:294-300)."""
+    kwargs = dict(kwargs, inner_solver="cg")
+    return _solve("qrot_pdip", M, a, b, reg, tol, max_iter, verbose, kwargs)
+
+
+def pdip_fp(M, a, b, reg, tol=1e-8, max_iter=1000, verbose=0, **kwargs):
+    """``qrot_pdip`` with the fixed-point inner solver (solvers.cpp:302-308)."""
+    kwargs = dict(kwargs, inner_solver="fp")
+    return _solve("qrot_pdip", M, a, b, reg, tol, max_iter, verbose, kwargs)
 
 
 def qrot_assn(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):

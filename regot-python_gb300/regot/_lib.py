@@ -78,6 +78,19 @@ class Result(C.Structure):
     ]
 
 
+class PdipOpts(C.Structure):
+    _fields_ = [
+        ("inner_solver", C.c_int),
+        ("cg_max_iter", C.c_int),
+        ("fixed_threshold", C.c_double),
+        ("fp_max_iter", C.c_int),
+        ("fp_exit_scale", C.c_double),
+        ("fp_stop_gap_mu_only", C.c_int),
+        ("cg_stop_gap_mu_only", C.c_int),
+        ("cg_mar_tol", C.c_double),
+    ]
+
+
 class BatchDesc(C.Structure):
     _fields_ = [
         ("count", C.c_int),
@@ -116,7 +129,7 @@ EXPORTS = [
     "regot_sinkhorn_sparse_newton", "regot_sinkhorn_splr",
     "regot_qrot_lbfgs_dual", "regot_qrot_assn", "regot_qrot_bcd", "regot_qrot_gd",
     "regot_qrot_apdagd", "regot_qrot_pdaam", "regot_qrot_grssn", "regot_qrot_lbfgs_semi_dual",
-    "regot_qrot_optimal_alpha", "regot_erot_optimal_beta", "regot_erot_optimal_alpha", "regot_erot_dual_obj_grad",
+    "regot_qrot_optimal_alpha", "regot_qrot_pdip", "regot_pdip_opts_init", "regot_erot_optimal_beta", "regot_erot_optimal_alpha", "regot_erot_dual_obj_grad",
     "regot_erot_hvp", "regot_erot_plan", "regot_erot_sparsify", "regot_erot_sparsify_density",
     "regot_erot_hess_solve",
     "regot_erot_tyy", "regot_erot_solve_batched", "regot_qrot_dual_obj_grad",
@@ -172,6 +185,11 @@ def load() -> C.CDLL:
         lib.regot_erot_plan.argtypes = [vp, vp, C.c_double, vp, vp, C.c_int]
         lib.regot_erot_sparsify.argtypes = [vp, vp, C.c_double, vp, C.c_double, C.c_double, vp,
                                              vp]
+        lib.regot_pdip_opts_init.argtypes = [C.POINTER(PdipOpts)]
+        lib.regot_pdip_opts_init.restype = None
+        lib.regot_qrot_pdip.argtypes = [vp, vp, C.c_double, C.c_double, C.c_int,
+                                        C.POINTER(PdipOpts), C.POINTER(Opts), C.POINTER(Result),
+                                        C.POINTER(C.c_int)]
         lib.regot_erot_sparsify_density.argtypes = [vp, vp, C.c_double, vp, C.c_double, vp, vp]
         lib.regot_qrot_dual_obj_grad.argtypes = [vp, vp, C.c_double, vp, vp, vp]
         lib.regot_qrot_optimal_beta.argtypes = [vp, vp, C.c_double, vp, vp]

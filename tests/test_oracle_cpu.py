@@ -419,3 +419,26 @@ def test_erot_sparse_newton_and_splr_reach_the_optimum(solver, tol):
     n, m = M.shape
     d0 = 0.1 * 0.5
     np.testing.assert_allclose(r.densities[0], (2 * d0 * n * (m - 1) + n + m - 1) / (n + m - 1) ** 2)
+
+
+@pytest.mark.parametrize("mode", ["cg", "fp"])
+@pytest.mark.parametrize("reg", [0.1, 0.01])
+def test_qrot_pdip_reaches_the_qrot_optimum(mode, reg):
+    """qrot_pdip (pdip_cg.cpp / pdip_fp.cpp): the interior-point plan is
+    feasible to the stopping tolerance and tends to the QROT optimum found
+    by the dual Newton method."""
+    M, a, b = qrot_points(40, 30, seed=3, dtype=np.float64)
+    r = O.qrot_pdip(M, a, b, reg, tol=1e-8, max_iter=200, inner_solver=mode)
+    assert r.converged and r.niter < 200
+    assert len(r.obj_vals) == len(r.mar_errs) == r.niter
+    P = r.plan
+    mar = max(np.linalg.norm(P.sum(1) - a), np.linalg.norm(P.sum(0) - b))
+    np.testing.assert_allclose(r.mar_errs[-1], mar, rtol=1e-6, atol=1e-14)
+    np.testing.assert_allclose(r.obj_vals[-1], (M * P).sum() + reg / 2 * (P * P).sum(), rtol=1e-12)
+    assert P.min() > 0
+    rg = O.qrot_grssn(M, a, b, reg, tol=1e-11, max_iter=2000)
+    Pg = O.qrot_plan(M, reg, rg.dual)
+    # the barrier stop leaves a few entries near the support boundary off
+    np.testing.assert_allclose(P, Pg, rtol=0, atol=2e-2 * Pg.max())
+    np.testing.assert_allclose(r.obj_vals[-1], (M * Pg).sum() + reg / 2 * (Pg * Pg).sum(),
+                               rtol=2e-3)
