@@ -79,7 +79,8 @@ def test_qrot_semi_dual_fp64_matches_oracle(case):
     # dual at reg = 0.01
     np.testing.assert_allclose(r.prim_vals, o.prim_vals, rtol=1e-6, atol=1e-12)
     np.testing.assert_allclose(r.dual, o.dual, rtol=0, atol=1e-8)
-    np.testing.assert_allclose(r.plan, o.plan, rtol=0, atol=1e-7 * o.plan.max())
+    # plan = (alpha + beta - M)+ / reg: dual rounding over reg
+    np.testing.assert_allclose(r.plan, o.plan, rtol=0, atol=1e-6 * o.plan.max())
 
 
 def test_qrot_semi_dual_mixed_converges():
