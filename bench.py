@@ -282,6 +282,88 @@ def run_batched(args):
     print(json.dumps(line))
 
 
+def solver_problems(seed=3):
+    """The problems of the solver table: EROT n = m = 2048 (3-D Gaussian
+    clouds, sqeuclid / max, uniform-ish weights, as the headline workload);
+    QROT n = m = 2048 (uniform points in the unit square, sqeuclid, Dirichlet(1)
+    weights floored at 1e-6); PDIP n = m = 256 (its inner factorizations are
+    dense in the reference)."""
+    from problems import erot_points, qrot_points
+
+    erot = erot_points(2048, 2048, seed=seed, dtype=np.float32)
+    qrot = qrot_points(2048, 2048, seed=seed, dtype=np.float32)
+    pdip = qrot_points(256, 256, seed=seed, dtype=np.float64)
+    return erot, qrot, pdip
+
+
+SOLVER_TABLE = [
+    # (solver, problem, reg, tol, max_iter, precision, kwargs)
+    ("sinkhorn_bcd", "erot", 0.05, 1e-6, 5000, "mixed", {}),
+    ("sinkhorn_newton", "erot", 0.05, 1e-6, 200, "mixed", {}),
+    ("sinkhorn_ssns", "erot", 0.05, 1e-6, 500, "mixed", {}),
+    ("sinkhorn_sparse_newton", "erot", 0.05, 1e-6, 3000, "mixed", {"density": 0.05}),
+    ("sinkhorn_splr", "erot", 0.05, 1e-6, 3000, "mixed", {"density": 0.05}),
+    ("sinkhorn_lbfgs_dual", "erot", 0.05, 1e-6, 3000, "mixed", {}),
+    ("sinkhorn_apdagd", "erot", 0.05, 1e-4, 3000, "mixed", {}),
+    ("qrot_lbfgs_dual", "qrot", 0.1, 1e-6, 3000, "mixed", {"prim_vals": False}),
+    ("qrot_assn", "qrot", 0.1, 1e-6, 500, "mixed", {"prim_vals": False}),
+    ("qrot_grssn", "qrot", 0.1, 1e-6, 500, "mixed", {"prim_vals": False}),
+    ("qrot_lbfgs_semi_dual", "qrot", 0.1, 1e-6, 3000, "mixed", {"prim_vals": False}),
+    ("qrot_bcd", "qrot", 0.1, 1e-6, 3000, "mixed", {"prim_vals": False}),
+    ("qrot_gd", "qrot", 0.1, 1e-6, 3000, "mixed", {"prim_vals": False}),
+    ("qrot_apdagd", "qrot", 0.1, 1e-6, 3000, "mixed", {"prim_vals": False}),
+    ("qrot_pdaam", "qrot", 0.1, 1e-6, 3000, "mixed", {"prim_vals": False}),
+    ("qrot_pdip", "pdip", 0.1, 1e-8, 200, "fp64", {"inner_solver": "cg"}),
+    ("qrot_pdip", "pdip", 0.1, 1e-8, 200, "fp64", {"inner_solver": "fp"}),
+]
+
+
+def run_solvers(args):
+    """One JSON line per solver of the table: device time of a solve from a
+    resident problem (median of `steps` after `warmup`), iterations, final
+    marginal error, passes over M; and the FP64 oracle's time for the
+    initial value and one iteration on one host core (a bounded sample)."""
+    import regot
+    import regot_oracle as O
+
+    erot, qrot, pdip = solver_problems()
+    probs = {"erot": erot, "qrot": qrot, "pdip": pdip}
+    resident = {}
+    for name, key, reg, tol, max_iter, prec, kw in SOLVER_TABLE:
+        M, a, b = probs[key]
+        if (key, prec) not in resident:
+            resident[(key, prec)] = regot.Problem(M, a, b, precision=prec)
+        P = resident[(key, prec)]
+        fn = getattr(P, name)
+        for _ in range(args.warmup):
+            r = fn(reg, tol=tol, max_iter=max_iter, plan=False, **kw)
+        ms = []
+        for _ in range(args.steps):
+            r = fn(reg, tol=tol, max_iter=max_iter, plan=False, **kw)
+            ms.append(r.solve_ms)
+        dev = statistics.median(ms)
+        line = {"workload": "solver table", "solver": name, "problem": key,
+                "n": int(M.shape[0]), "m": int(M.shape[1]), "reg": reg, "tol": tol,
+                "precision": prec, "options": {k: v for k, v in kw.items()},
+                "ms": round(dev, 3), "niter": int(r.niter),
+                "final_mar_err": float(r.mar_errs[-1]) if len(r.mar_errs) else None,
+                "passes": int(getattr(r, "passes", 0) or 0)}
+        if getattr(r, "converged", None) is not None:
+            line["converged"] = bool(r.converged)
+        if not args.no_cpu_baseline:
+            # FP64 oracle, one host core: a few iterations, per-iteration time
+            okw = {k: v for k, v in kw.items() if k != "prim_vals"}
+            Mq = M.astype(np.float64) if prec == "fp64" else M.astype(np.float32).astype(np.float64)
+            t = time.perf_counter()
+            if name == "qrot_pdip":
+                O.qrot_pdip(Mq, a, b, reg, tol=0.0, max_iter=1, **okw)
+            else:
+                getattr(O, name)(Mq, a, b, reg, tol=0.0, max_iter=1, plan=False, **okw)
+            line["cpu_oracle_ms_init_plus_1_iter"] = round((time.perf_counter() - t) * 1e3, 1)
+            line["gpu_ms_per_iter"] = round(dev / max(int(r.niter), 1), 4)
+        print(json.dumps(line), flush=True)
+
+
 def run_probe(kind, n):
     """Ceilings on this GPU, printed as one JSON line.
 
@@ -372,8 +454,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ncu-case", action="store_true",
                     help="a few passes for an ncu capture (no timing, no JSON)")
-    ap.add_argument("--workload", choices=["bcd", "batched"], default="bcd",
-                    help="batched: the batched uneven-problem workload (its own JSON line)")
+    ap.add_argument("--workload", choices=["bcd", "batched", "solvers"], default="bcd",
+                    help="batched: the batched uneven-problem workload (its own JSON line); "
+                         "solvers: one line per solver of the solver table")
     ap.add_argument("--probe", choices=["hbm-read", "host-link"],
                     help="measure the ceilings the numbers are read against (no JSON line)")
     args = ap.parse_args()
@@ -415,6 +498,9 @@ def main():
         return
     if args.workload == "batched" and not args.ncu_case:
         run_batched(args)
+        return
+    if args.workload == "solvers":
+        run_solvers(args)
         return
 
     import torch
