@@ -8,6 +8,7 @@ regressions (tests/test_golden_cpu.py) and give the GPU tests a fixed target
 
     python tests/golden/make_golden.py
 """
+import json
 import os
 import sys
 
@@ -35,6 +36,33 @@ CASES = {
                                 "qrot_lbfgs_dual", 0.1, 1e-8, 3000, {}),
     "assn_points_32x24_r0.1": (lambda: qrot_points(32, 24, seed=24, dtype=np.float64),
                                "qrot_assn", 0.1, 1e-10, 20, {}),
+    # fixed iteration counts (tol 1e-14): the histories follow step for step
+    "lbfgsdual_readme_40x30_r0.1": (lambda: readme_example(40, 30), "sinkhorn_lbfgs_dual", 0.1,
+                                    1e-14, 15, {}),
+    "apdagd_readme_40x30_r0.1": (lambda: readme_example(40, 30), "sinkhorn_apdagd", 0.1,
+                                 1e-14, 30, {}),
+    "sparsenewton_points_48x36_r0.05": (lambda: erot_points(48, 36, seed=25, dtype=np.float64),
+                                        "sinkhorn_sparse_newton", 0.05, 1e-14, 10,
+                                        {"density": 0.3}),
+    "splr_points_48x36_r0.05": (lambda: erot_points(48, 36, seed=26, dtype=np.float64),
+                                "sinkhorn_splr", 0.05, 1e-14, 10, {"density": 0.3}),
+    "qbcd_points_32x24_r0.1": (lambda: qrot_points(32, 24, seed=27, dtype=np.float64),
+                               "qrot_bcd", 0.1, 1e-14, 20, {}),
+    "qgd_points_32x24_r0.1": (lambda: qrot_points(32, 24, seed=28, dtype=np.float64),
+                              "qrot_gd", 0.1, 1e-14, 20, {}),
+    "qapdagd_points_32x24_r0.1": (lambda: qrot_points(32, 24, seed=29, dtype=np.float64),
+                                  "qrot_apdagd", 0.1, 1e-14, 20, {}),
+    "qpdaam_points_32x24_r0.1": (lambda: qrot_points(32, 24, seed=30, dtype=np.float64),
+                                 "qrot_pdaam", 0.1, 1e-14, 20, {}),
+    "grssn_points_32x24_r0.1": (lambda: qrot_points(32, 24, seed=31, dtype=np.float64),
+                                "qrot_grssn", 0.1, 1e-14, 6, {}),
+    "semidual_points_32x24_r0.1": (lambda: qrot_points(32, 24, seed=32, dtype=np.float64),
+                                   "qrot_lbfgs_semi_dual", 0.1, 1e-14, 15, {}),
+    # converged interior-point solves
+    "pdipcg_points_30x25_r0.1": (lambda: qrot_points(30, 25, seed=33, dtype=np.float64),
+                                 "qrot_pdip", 0.1, 1e-8, 200, {"inner_solver": "cg"}),
+    "pdipfp_points_30x25_r0.1": (lambda: qrot_points(30, 25, seed=34, dtype=np.float64),
+                                 "qrot_pdip", 0.1, 1e-8, 200, {"inner_solver": "fp"}),
 }
 
 
@@ -43,8 +71,12 @@ def solve(name):
     M, a, b = make()
     r = getattr(O, solver)(M, a, b, reg, tol=tol, max_iter=max_iter, **kw)
     out = dict(M=M, a=a, b=b, reg=reg, tol=tol, max_iter=max_iter, solver=solver,
-               niter=r.niter, dual=r.dual, plan=r.plan, obj_vals=np.array(r.obj_vals),
-               mar_errs=np.array(r.mar_errs))
+               kwargs=json.dumps(kw), niter=r.niter, plan=r.plan,
+               obj_vals=np.array(r.obj_vals), mar_errs=np.array(r.mar_errs))
+    if hasattr(r, "dual"):
+        out["dual"] = r.dual
+    if hasattr(r, "converged"):
+        out["converged"] = r.converged
     if hasattr(r, "densities"):
         out["densities"] = np.array(r.densities)
     if hasattr(r, "prim_vals"):
