@@ -51,11 +51,6 @@ __global__ void k_convert(const TS* src, long long lds, TD* dst, long long ldd, 
     }
 }
 
-__global__ void k_check_finite(const double* x, int len, int* bad) {
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < len; i += gridDim.x * blockDim.x)
-        if (!isfinite(x[i])) atomicOr(bad, 1);
-}
-
 void check_solver_args(regot_dproblem* P, double reg, double tol, int max_iter, regot_result* res,
                        int dual_len) {
     require(P != nullptr, "problem is NULL");

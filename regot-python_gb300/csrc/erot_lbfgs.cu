@@ -46,8 +46,6 @@ public:
         d_.zero();
     }
 
-    int n() const { return n_; }
-    int m() const { return m_; }
     double* alpha() { return g_.get(); }
     double* beta() { return g_.get() + n_; }
     double* dir_alpha() { return d_.get(); }

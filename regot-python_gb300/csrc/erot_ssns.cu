@@ -121,14 +121,12 @@ struct KeyOf;
 template <>
 struct KeyOf<float> {
     using U = unsigned;
-    static constexpr int kBits = 32;
     __device__ static U key(float v) { return __float_as_uint(v); }
     __device__ static float val(U k) { return __uint_as_float(k); }
 };
 template <>
 struct KeyOf<double> {
     using U = unsigned long long;
-    static constexpr int kBits = 64;
     __device__ static U key(double v) { return (U)__double_as_longlong(v); }
     __device__ static double val(U k) { return __longlong_as_double((long long)k); }
 };
@@ -916,12 +914,6 @@ __global__ void k_topk_finish(const TopK* tk, int m1, TM* xcol) {
     using K = KeyOf<TM>;
     const TM thr = tk->empty ? (TM)INFINITY : K::val((typename K::U)tk->prefix);
     xcol[j] = j == 0 ? (TM)0 : thr;
-}
-
-// out = base + s d (n + m entries)
-__global__ void k_axpy_to(int N, const double* base, double s, const double* d, double* out) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < N) out[t] = base[t] + s * d[t];
 }
 
 template <typename TM>

@@ -204,14 +204,6 @@ __host__ __device__ constexpr bool op_needs_cb(int op) {
     return op != OP_E_COLMAX;
 }
 
-// Power-of-two grid for the hi/lo split, from a bound on |ra|, |cb|.
-__device__ __forceinline__ double split_grid(const double* maxabs) {
-    if (!maxabs) return 1.0;
-    const double mx = *maxabs;
-    if (!(mx > 0.0) || !isfinite(mx)) return 1.0;
-    return ldexp(1.0, ilogb(mx) - 21);
-}
-
 __device__ __forceinline__ void split(double v, double g, double inv_g, float& hi, float& lo) {
     if (!isfinite(v)) {
         hi = (float)v;

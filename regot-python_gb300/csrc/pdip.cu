@@ -384,8 +384,6 @@ public:
         const long long want = (nv_ + kEw - 1) / kEw;
         return (int)std::max(1LL, std::min<long long>(want, (long long)device_sm_count() * 8));
     }
-    int n() const { return n_; }
-    int m() const { return m_; }
     long long nv() const { return nv_; }
     cudaStream_t stream() const { return st_; }
     double* c() { return c_.get(); }
