@@ -60,6 +60,7 @@ struct QState {
     double thresh2;
     double prim[6];  // primal-value scalars
     double maxabs;
+    double mu;       // shift of the Schur CG (read by its captured steps)
 };
 
 // ---- gradient / objective merge ----
@@ -208,8 +209,10 @@ __device__ __forceinline__ int bit_col(int s, int q, int L) {
 // out_i = scale_i * sum_j sigma_ij x_j, scale_i = 1 / (h1_i + mu) (or 1).
 template <int CW, int VW, int LC>
 __global__ void k_sigma_rows(const uint32_t* bm, int n, int m, int nslabs, const double* x,
-                             const double* h1, double mu, int divide, double* out, const int* done) {
+                             const double* h1, double mu, const double* mu_dev, int divide,
+                             double* out, const int* done) {
     if (done && *done) return;
+    if (mu_dev) mu = *mu_dev;
     const int lane = threadIdx.x & 31;
     const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (i >= n) return;
@@ -271,9 +274,10 @@ __global__ void k_acg_init(int m, const double* zy, double tol, double* x, doubl
     }
 }
 
-__global__ void k_acg_a(int m, const double* partial, int chunks, const double* h2, double mu,
+__global__ void k_acg_a(int m, const double* partial, int chunks, const double* h2,
                         const double* p, double* y, double* parts, QState* st) {
     if (st->cg_done) return;
+    const double mu = st->mu;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     double v[1] = {0.0};
     if (j < m) {
@@ -582,17 +586,18 @@ public:
         throw Error(REGOT_ERR_NUMERIC, "optimal_alpha did not converge");
     }
 
-    // sigma x (n) with optional division by (h1 + mu)
-    void sigma_rows(const double* x, double mu, bool divide, double* out, const int* done) {
+    // sigma x (n) with optional division by (h1 + mu); mu from *mu_dev when given
+    void sigma_rows(const double* x, double mu, bool divide, double* out, const int* done,
+                    const double* mu_dev = nullptr) {
         const int warps = 8;
         if (mixed_)
             k_sigma_rows<Geo<float>::CW, Geo<float>::VW, Geo<float>::LC>
                 <<<cdiv(n_, warps), warps * 32, 0, st_>>>(bm_.get(), n_, m_, nslabs(), x, h_.get(),
-                                                          mu, divide ? 1 : 0, out, done);
+                                                          mu, mu_dev, divide ? 1 : 0, out, done);
         else
             k_sigma_rows<Geo<double>::CW, Geo<double>::VW, Geo<double>::LC>
                 <<<cdiv(n_, warps), warps * 32, 0, st_>>>(bm_.get(), n_, m_, nslabs(), x, h_.get(),
-                                                          mu, divide ? 1 : 0, out, done);
+                                                          mu, mu_dev, divide ? 1 : 0, out, done);
         count_launch();
     }
     // partial sums of sigma' y over kColChunks row chunks
@@ -847,14 +852,19 @@ public:
         k_sub_partial<<<gm, kVT, 0, st_>>>(m, rhs_d_.get() + n, partial_.get(), kColChunks, zy_);
         k_acg_init<<<gm, kVT, 0, st_>>>(m, zy_, cg_tol_, xs_, rs_, ps_, E_.parts(), S);
         count_launch(2);
-        int batch = 16;
+        h2d(&S->mu, &mu, sizeof(double), st_);
+        if (!exec_) build_graph();
+        // kGraphSteps CG steps per graph launch; every kernel returns at once
+        // after convergence (cg_done)
+        int batch = 2;
         for (;;) {
-            for (int q = 0; q < batch; ++q) step(mu);
+            for (int q = 0; q < batch; ++q) REGOT_CUDA(cudaGraphLaunch(exec_, st_));
+            count_launch(graph_kernels_ * batch);
             int done = 0;
             d2h(&done, &S->cg_done, sizeof(int), st_);
             sync(st_);
             if (done) break;
-            batch = std::min(batch * 2, 256);
+            batch = std::min(batch * 2, 32);
         }
         // r1 = (w - sigma r2) / (h1 + mu)
         E_.sigma_rows(xs_, mu, false, t_d_, nullptr);
@@ -866,20 +876,52 @@ public:
         sync(st_);
     }
 
+    ~QrotSchurCG() {
+        if (exec_) cudaGraphExecDestroy(exec_);
+        if (graph_) cudaGraphDestroy(graph_);
+    }
+
 private:
-    // One CG step on Delta = h2 o x + mu x - sigma' ((sigma x) / (h1 + mu));
-    // a no-op once the device flag cg_done is set.
-    void step(double mu) {
+    static constexpr int kGraphSteps = 8;
+
+    // One CG step on Delta = h2 o x + mu x - sigma' ((sigma x) / (h1 + mu)),
+    // mu from the state; a no-op once the device flag cg_done is set.
+    void step() {
         QState* S = E_.state();
         const int gm = cdiv(m_, kVT);
-        E_.sigma_rows(ps_, mu, true, t_d_, &S->cg_done);
+        E_.sigma_rows(ps_, 0.0, true, t_d_, &S->cg_done, &S->mu);
         E_.sigma_cols(t_d_, partial_.get(), &S->cg_done);
-        k_acg_a<<<gm, kVT, 0, st_>>>(m_, partial_.get(), kColChunks, E_.h2(), mu, ps_, ys_,
+        k_acg_a<<<gm, kVT, 0, st_>>>(m_, partial_.get(), kColChunks, E_.h2(), ps_, ys_,
                                      E_.parts(), S);
         k_acg_b<<<gm, kVT, 0, st_>>>(m_, ps_, ys_, xs_, rs_, E_.parts(), S);
         k_acg_c<<<gm, kVT, 0, st_>>>(m_, rs_, ps_, S);
         count_launch(3);
     }
+
+    // kGraphSteps steps captured once per solver call: the shift is read
+    // from the state, so the graph serves every solve.
+    void build_graph() {
+        long long* saved = g_launch_counter;
+        graph_kernels_ = 0;
+        g_launch_counter = &graph_kernels_;
+        REGOT_CUDA(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
+        try {
+            for (int q = 0; q < kGraphSteps; ++q) step();
+        } catch (...) {
+            cudaGraph_t g = nullptr;
+            cudaStreamEndCapture(st_, &g);
+            if (g) cudaGraphDestroy(g);
+            g_launch_counter = saved;
+            throw;
+        }
+        REGOT_CUDA(cudaStreamEndCapture(st_, &graph_));
+        g_launch_counter = saved;
+        REGOT_CUDA(cudaGraphInstantiate(&exec_, graph_, 0));
+    }
+
+    cudaGraph_t graph_ = nullptr;
+    cudaGraphExec_t exec_ = nullptr;
+    long long graph_kernels_ = 0;
 
     QrotEngine& E_;
     cudaStream_t st_;
