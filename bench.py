@@ -364,6 +364,56 @@ def run_solvers(args):
         print(json.dumps(line), flush=True)
 
 
+def run_autograd(args):
+    """One JSON line for the autograd workload: x, y in R^{4096 x 64} ~ N(0, I)
+    (seed 3, FP32 on the device), M = |x - y|^2 / 64, uniform weights, reg 0.05;
+    the differentiable cost sqeuclid_ot_cost (forward sinkhorn_newton to
+    tol 1e-6, backward dL/dx = 2 (r o x - T y) / 64 by the fused contraction)
+    and the plan loss sqeuclid_plan_loss with W ~ N(0, 1) (backward through
+    the implicit adjoint: one CG solve over the HVP passes). Time of forward
+    plus backward, CUDA events, median of `steps`."""
+    import torch
+
+    import regot.torch as rt
+
+    n, d, reg, tol = 4096, 64, 0.05, 1e-6
+    g = torch.Generator(device="cuda").manual_seed(3)
+    x0 = torch.randn(n, d, device="cuda", generator=g)
+    y = torch.randn(n, d, device="cuda", generator=g)
+    W = torch.randn(n, n, device="cuda", generator=g, dtype=torch.float64)
+    a = torch.full((n,), 1.0 / n, device="cuda", dtype=torch.float64)
+    b = torch.full((n,), 1.0 / n, device="cuda", dtype=torch.float64)
+    out = {}
+    for name in ("sqeuclid_ot_cost", "sqeuclid_plan_loss"):
+        def step():
+            x = x0.clone().requires_grad_(True)
+            if name == "sqeuclid_ot_cost":
+                loss = rt.sqeuclid_ot_cost(x, y, a, b, reg, scale=float(d), tol=tol)
+            else:
+                loss = rt.sqeuclid_plan_loss(x, y, a, b, reg, W, scale=float(d), tol=tol)
+            loss.backward()
+            return x.grad
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(args.steps):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+            gx = step()
+            e1.record()
+            torch.cuda.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        out[name] = {"ms_fwd_bwd": round(statistics.median(ms), 3),
+                     "grad_norm": float(gx.norm())}
+    line = {"workload": "autograd", "config": "x, y in R^{4096 x 64} ~ N(0, I) (seed 3), "
+                                              "M = |x - y|^2 / 64, uniform a, b, reg 0.05, "
+                                              "forward sinkhorn_newton tol 1e-6",
+            "steps": args.steps, "warmup": args.warmup, "results": out}
+    print(json.dumps(line), flush=True)
+
+
 def run_probe(kind, n):
     """Ceilings on this GPU, printed as one JSON line.
 
@@ -454,7 +504,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ncu-case", action="store_true",
                     help="a few passes for an ncu capture (no timing, no JSON)")
-    ap.add_argument("--workload", choices=["bcd", "batched", "solvers"], default="bcd",
+    ap.add_argument("--workload", choices=["bcd", "batched", "solvers", "autograd"],
+                    default="bcd",
                     help="batched: the batched uneven-problem workload (its own JSON line); "
                          "solvers: one line per solver of the solver table")
     ap.add_argument("--probe", choices=["hbm-read", "host-link"],
@@ -501,6 +552,9 @@ def main():
         return
     if args.workload == "solvers":
         run_solvers(args)
+        return
+    if args.workload == "autograd":
+        run_autograd(args)
         return
 
     import torch
