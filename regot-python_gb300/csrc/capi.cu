@@ -593,6 +593,13 @@ int regot_erot_hvp(regot_ctx* ctx, regot_dproblem* P, double reg, const double* 
 
 int regot_erot_solve_batched(regot_ctx* ctx, const regot_batch_desc* desc, double reg, double tol,
                              int max_iter, regot_batch_result* res) {
+    return regot_erot_solve_batched_grad(ctx, desc, reg, tol, max_iter, res, nullptr, nullptr,
+                                         nullptr);
+}
+
+int regot_erot_solve_batched_grad(regot_ctx* ctx, const regot_batch_desc* desc, double reg,
+                                  double tol, int max_iter, regot_batch_result* res, double* cost,
+                                  double* grad_x, double* grad_y) {
     return guarded(ctx, [&] {
         require(desc && res, "NULL argument");
         require(desc->count > 0, "the batch is empty");
@@ -603,7 +610,7 @@ int regot_erot_solve_batched(regot_ctx* ctx, const regot_batch_desc* desc, doubl
         require(std::isfinite(reg) && reg > 0.0, "reg must be a positive finite number");
         require(!std::isnan(tol), "tol must not be NaN");
         require(max_iter >= 0, "max_iter must be non-negative");
-        erot_solve_batched_gpu(ctx, desc, reg, tol, max_iter, res);
+        erot_solve_batched_gpu(ctx, desc, reg, tol, max_iter, res, cost, grad_x, grad_y);
     });
 }
 

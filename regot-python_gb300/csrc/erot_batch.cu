@@ -441,6 +441,145 @@ __global__ void k_bloop(BatchState* st, cudaGraphConditionalHandle h) {
     cudaGraphSetConditional(h, go ? 1u : 0u);
 }
 
+// Backward of the batch: for each problem, the gradient of its regularised
+// OT cost L = a'alpha + b'beta - reg sum T at the returned duals with respect
+// to the points. By the envelope theorem dL/dM = T, and M_ij = s |x_i - y_j|^2
+// gives dL/dx_i = 2 s sum_j T_ij (x_i - y_j) and dL/dy_j = 2 s sum_i T_ij
+// (y_j - x_i). One warp per own point (a row for dL/dx, a column for dL/dy),
+// lanes over the other side's points staged in shared memory. T_ij comes out
+// as in the sweeps (the same FP32 cost, the split exponent) and the weighted
+// differences are summed against a running base-2 reference like the
+// log-sum-exp, so no term overflows whatever the duals. Summing T (x_i - y_j)
+// instead of forming r_i x_i - (T y)_i avoids cancelling the two terms.
+// side 0 also writes the row sums of T (for the cost).
+constexpr int kGWarps = 8;  // own points per CTA
+
+template <int DP>
+__global__ void __launch_bounds__(kGWarps * 32) k_bgrad(
+    const BatchDev B, const int2* __restrict__ items, int side, const float2* __restrict__ as,
+    const float2* __restrict__ bs, float k2, double* __restrict__ grad,
+    double* __restrict__ tsum) {
+    const int2 it = items[blockIdx.x];
+    const int p = it.x;
+    const int d = B.d[p];
+    const int n_own = side ? B.m[p] : B.n[p];
+    const int n_oth = side ? B.n[p] : B.m[p];
+    const float* Po = side ? B.Y + B.yo[p] : B.X + B.xo[p];
+    const float* Pt = side ? B.X + B.xo[p] : B.Y + B.yo[p];
+    const float2* so = side ? bs + B.co[p] : as + B.ro[p];
+    const float2* sx = side ? as + B.ro[p] : bs + B.co[p];
+    const float sc = B.scale[p];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i = it.y * kGWarps + warp;
+    const bool ok = i < n_own;  // the same for the whole warp
+    float u[DP], acc[DP];
+#pragma unroll
+    for (int k = 0; k < DP; ++k) {
+        u[k] = (ok && k < d) ? Po[(long long)i * d + k] : 0.f;
+        acc[k] = 0.f;
+    }
+    const float2 s_own = ok ? so[i] : make_float2(0.f, 0.f);
+    const float lk_own = __fmul_rn(s_own.y, k2);
+    float mx = -INFINITY, ts = 0.f;
+    __shared__ float sv[kBTile][DP + 1];
+    __shared__ float2 sd[kBTile];
+    for (int j0 = 0; j0 < n_oth; j0 += kBTile) {
+        const int cnt = min(kBTile, n_oth - j0);
+        for (int e = threadIdx.x; e < kBTile * DP; e += kGWarps * 32) {
+            const int jj = e / DP, k = e % DP;
+            sv[jj][k] = (jj < cnt && k < d) ? Pt[(long long)(j0 + jj) * d + k] : 0.f;
+        }
+        for (int jj = threadIdx.x; jj < kBTile; jj += kGWarps * 32)
+            sd[jj] = jj < cnt ? sx[j0 + jj] : make_float2(0.f, 0.f);
+        __syncthreads();
+        if (ok) {
+            for (int jj = lane; jj < cnt; jj += 32) {
+                float t[DP], q[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+                for (int k = 0; k < DP; ++k) {
+                    t[k] = __fsub_rn(u[k], sv[jj][k]);
+                    q[k & 3] = __fmaf_rn(t[k], t[k], q[k & 3]);
+                }
+                const float M = __fmul_rn(__fadd_rn(__fadd_rn(q[0], q[1]), __fadd_rn(q[2], q[3])), sc);
+                const float2 sj = sd[jj];
+                const float e = __fadd_rn(__fadd_rn(s_own.x, sj.x), -M);
+                const float z = __fmaf_rn(e, k2, __fadd_rn(lk_own, __fmul_rn(sj.y, k2)));
+                if (z > mx + kLseSlack) {
+                    const float f = bex2(mx - z);
+#pragma unroll
+                    for (int k = 0; k < DP; ++k) acc[k] *= f;
+                    ts *= f;
+                    mx = z;
+                }
+                const float w = bex2(z - mx);
+#pragma unroll
+                for (int k = 0; k < DP; ++k) acc[k] = __fmaf_rn(w, t[k], acc[k]);
+                ts += w;
+            }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float m2 = __shfl_xor_sync(0xffffffffu, mx, o);
+        const float t2 = __shfl_xor_sync(0xffffffffu, ts, o);
+        float a2[DP];
+#pragma unroll
+        for (int k = 0; k < DP; ++k) a2[k] = __shfl_xor_sync(0xffffffffu, acc[k], o);
+        const float m = fmaxf(mx, m2);
+        if (m != -INFINITY) {
+            const float f1 = bex2(mx - m), f2 = bex2(m2 - m);
+#pragma unroll
+            for (int k = 0; k < DP; ++k) acc[k] = acc[k] * f1 + a2[k] * f2;
+            ts = ts * f1 + t2 * f2;
+        }
+        mx = m;
+    }
+    if (!ok) return;
+    const float fl = floorf(mx);
+    const float fr = exp2f(mx - fl);
+    float v = 0.f;
+#pragma unroll
+    for (int k = 0; k < DP; ++k)
+        if (lane == k) v = acc[k];
+    if (grad && lane < d) {
+        const long long off = side ? B.yo[p] : B.xo[p];
+        grad[off + (long long)i * d + lane] = 2.0 * (double)sc * ldexp((double)(v * fr), (int)fl);
+    }
+    if (side == 0 && lane == 0) tsum[B.ro[p] + i] = ldexp((double)(ts * fr), (int)fl);
+}
+
+// Each problem's alpha from the buffer of its last iterate.
+__global__ void k_bfinal(const BatchDev B, const int* __restrict__ fpar,
+                         const double* __restrict__ a0, const double* __restrict__ a1, double* af) {
+    const int p = blockIdx.x;
+    const int ro = B.ro[p], n = B.n[p];
+    const double* src = fpar[p] ? a1 : a0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) af[ro + i] = src[ro + i];
+}
+
+// L_p = sum a_i (alpha_i + c) + sum b_j (beta_j - c) - reg sum T, with the
+// gauge c = beta_m of the returned duals (one block of 256 per problem).
+__global__ void k_bcost(const BatchDev B, const double* __restrict__ b,
+                        const double* __restrict__ af, const double* __restrict__ beta,
+                        const double* __restrict__ tsum, double reg, double* cost) {
+    const int p = blockIdx.x;
+    const int ro = B.ro[p], co = B.co[p], n = B.n[p], m = B.m[p];
+    const double c = beta[co + m - 1];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        s += B.a[ro + i] * (af[ro + i] + c) - reg * tsum[ro + i];
+    for (int j = threadIdx.x; j < m; j += blockDim.x) s += b[co + j] * (beta[co + j] - c);
+    __shared__ double red[256];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) cost[p] = red[0];
+}
+
 __global__ void k_blog(const double* x, int len, double* y) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t < len) y[t] = log(x[t]);
@@ -491,7 +630,8 @@ void upload_vec(DBuf<T>& buf, const std::vector<T>& v, cudaStream_t st) {
 }  // namespace
 
 void erot_solve_batched_gpu(regot_ctx* ctx, const regot_batch_desc* D, double reg, double tol,
-                            int max_iter, regot_batch_result* res) {
+                            int max_iter, regot_batch_result* res, double* cost, double* grad_x,
+                            double* grad_y) {
     cudaStream_t st = ctx->stream;
     const int P = D->count;
     std::vector<int> hn(P), hm(P), hd(P), ro(P), co(P), rbo(P + 1), cls(P);
@@ -765,6 +905,61 @@ void erot_solve_batched_gpu(regot_ctx* ctx, const regot_batch_desc* D, double re
         }
         if (!acted) throw Error(REGOT_ERR_NUMERIC, "batched BCD did not terminate");
     }
+
+    // Backward: costs and point gradients at every problem's last iterate,
+    // its alpha gathered into one buffer and both duals split on a common
+    // grid from their max.
+    DBuf<double> Af, tsum, gxd, gyd, dcost;
+    if (cost || grad_x || grad_y) {
+        Af.alloc(NR, st);
+        tsum.alloc(NR, st);
+        k_bfinal<<<P, 256, 0, st>>>(B, fpar.get(), A[0].get(), A[1].get(), Af.get());
+        REGOT_CUDA(cudaMemsetAsync(&S->maxabs, 0, sizeof(double), st));
+        k_bmax<<<64, 256, 0, st>>>(Af.get(), (int)NR, beta.get(), (int)NC, S);
+        k_bgrid<<<1, 1, 0, st>>>(S);
+        k_bsplit_all<<<cdiv(NR, 256), 256, 0, st>>>(Af.get(), (int)NR, AS[0].get(), S);
+        k_bsplit_all<<<cdiv(NC, 256), 256, 0, st>>>(beta.get(), (int)NC, BS.get(), S);
+        count_launch(5);
+        if (grad_x) gxd.alloc(NX, st);
+        if (grad_y) gyd.alloc(NY, st);
+        std::vector<int> order(P);
+        for (int p = 0; p < P; ++p) order[p] = p;
+        for (int side = 0; side < 2; ++side) {
+            double* out = side ? gyd.get() : gxd.get();
+            if (side == 1 && !grad_y) break;  // side 0 runs for the row sums of T
+            std::stable_sort(order.begin(), order.end(), [&](int u, int v) {
+                return side ? hn[u] > hn[v] : hm[u] > hm[v];
+            });
+            std::vector<int2> gi[kBClasses];
+            for (int p : order)
+                for (int k = 0; k < cdiv(side ? hm[p] : hn[p], kGWarps); ++k)
+                    gi[cls[p]].push_back(make_int2(p, k));
+            for (int c = 0; c < kBClasses; ++c) {
+                const int ni = (int)gi[c].size();
+                if (!ni) continue;
+                DBuf<int2> items;
+                upload_vec(items, gi[c], st);
+                const dim3 grid(ni), block(kGWarps * 32);
+                if (c == 0)
+                    k_bgrad<4><<<grid, block, 0, st>>>(B, items.get(), side, AS[0].get(), BS.get(),
+                                                       k2, out, tsum.get());
+                else if (c == 1)
+                    k_bgrad<8><<<grid, block, 0, st>>>(B, items.get(), side, AS[0].get(), BS.get(),
+                                                       k2, out, tsum.get());
+                else
+                    k_bgrad<16><<<grid, block, 0, st>>>(B, items.get(), side, AS[0].get(),
+                                                        BS.get(), k2, out, tsum.get());
+                count_launch();
+                REGOT_CHECK_LAUNCH();  // the item list is freed in stream order
+            }
+        }
+        if (cost) {
+            dcost.alloc(P, st);
+            k_bcost<<<P, 256, 0, st>>>(B, b, Af.get(), beta.get(), tsum.get(), reg, dcost.get());
+            count_launch();
+        }
+        REGOT_CHECK_LAUNCH();
+    }
     REGOT_CUDA(cudaEventRecord(e1, st));
 
     // results: each problem's alpha from the buffers of its last iterate,
@@ -777,6 +972,9 @@ void erot_solve_batched_gpu(regot_ctx* ctx, const regot_batch_desc* D, double re
     d2h(hmar.data(), mar.get(), P * sizeof(double), st);
     d2h(hfpar.data(), fpar.get(), P * sizeof(int), st);
     d2h(hiter.data(), iter.get(), P * sizeof(int), st);
+    if (grad_x) d2h(grad_x, gxd.get(), NX * sizeof(double), st);
+    if (grad_y) d2h(grad_y, gyd.get(), NY * sizeof(double), st);
+    if (cost) d2h(cost, dcost.get(), P * sizeof(double), st);
     sync(st);
     float ms = 0.f;
     REGOT_CUDA(cudaEventElapsedTime(&ms, e0, e1));

@@ -649,7 +649,10 @@ def qrot_assn(M, a, b, reg, tol=1e-6, max_iter=1000, verbose=0, **kwargs):
 class batch_result:
     """Result of sinkhorn_bcd_batched: per-problem iteration counts, final
     marginal errors and gauge-fixed duals (alpha, beta~) as sinkhorn_bcd
-    returns them, plus the sweeps and device time of the whole batch."""
+    returns them, plus the sweeps and device time of the whole batch. With
+    grad=True also each problem's regularised OT cost (costs) and its
+    gradients with respect to the points (grad_x, grad_y: lists of (n_p, d_p)
+    and (m_p, d_p) arrays)."""
 
     def __init__(self):
         self.niter = None
@@ -657,6 +660,9 @@ class batch_result:
         self.duals = []
         self.sweeps = 0
         self.solve_ms = 0.0
+        self.costs = None
+        self.grad_x = None
+        self.grad_y = None
 
     def __repr__(self):
         return (f"batch_result(problems={len(self.duals)}, sweeps={self.sweeps}, "
@@ -664,13 +670,17 @@ class batch_result:
 
 
 def sinkhorn_bcd_batched(xs, ys, as_, bs, reg, tol=1e-6, max_iter=1000, cost_scale=None,
-                         device: int = 0):
+                         device: int = 0, grad: bool = False):
     """sinkhorn_bcd (reference src/sinkhorn_bcd.cpp:14-124) on many problems
     at once, each with the squared-Euclidean cost M_ij = s_p |x_i - y_j|^2
     computed on the fly in FP32 (no n x m matrix is stored). xs, ys: lists
     of (n_p, d_p) and (m_p, d_p) point arrays (d_p <= 16); as_, bs: lists of
     marginals; cost_scale: None, a number or one number per problem. Each
-    problem stops at its own iteration (marginal error < tol or max_iter)."""
+    problem stops at its own iteration (marginal error < tol or max_iter).
+    grad=True adds the backward in the same call: each problem's cost
+    L = a'alpha + b'beta - reg sum T and dL/dx = 2 s sum_j T_ij (x_i - y_j),
+    dL/dy = 2 s sum_i T_ij (y_j - x_i) at the returned duals (the envelope
+    theorem, dL/dM = T)."""
     P = len(xs)
     if not (len(ys) == len(as_) == len(bs) == P) or P == 0:
         raise ValueError("xs, ys, as_ and bs must be non-empty lists of the same length")
@@ -712,9 +722,23 @@ def sinkhorn_bcd_batched(xs, ys, as_, bs, reg, tol=1e-6, max_iter=1000, cost_sca
     r = L.BatchResult()
     r.alpha, r.beta = alpha.ctypes.data, beta.ctypes.data
     r.niter, r.mar_err = niter.ctypes.data, mar.ctypes.data
-    ctx.check(lib.regot_erot_solve_batched(ctx.handle, C.byref(desc), float(reg), float(tol),
-                                           int(max_iter), C.byref(r)))
+    if grad:
+        costs = np.zeros(P)
+        gx = np.zeros(X.size)
+        gy = np.zeros(Y.size)
+        ctx.check(lib.regot_erot_solve_batched_grad(
+            ctx.handle, C.byref(desc), float(reg), float(tol), int(max_iter), C.byref(r),
+            costs.ctypes.data, gx.ctypes.data, gy.ctypes.data))
+    else:
+        ctx.check(lib.regot_erot_solve_batched(ctx.handle, C.byref(desc), float(reg),
+                                               float(tol), int(max_iter), C.byref(r)))
     out = batch_result()
+    if grad:
+        xo = np.r_[0, np.cumsum(n.astype(np.int64) * d)]
+        yo = np.r_[0, np.cumsum(m.astype(np.int64) * d)]
+        out.costs = costs
+        out.grad_x = [gx[xo[p]:xo[p + 1]].reshape(n[p], d[p]) for p in range(P)]
+        out.grad_y = [gy[yo[p]:yo[p + 1]].reshape(m[p], d[p]) for p in range(P)]
     out.niter = niter
     out.mar_errs = mar
     ro = np.r_[0, np.cumsum(n)]

@@ -132,7 +132,8 @@ EXPORTS = [
     "regot_qrot_optimal_alpha", "regot_qrot_pdip", "regot_pdip_opts_init", "regot_erot_optimal_beta", "regot_erot_optimal_alpha", "regot_erot_dual_obj_grad",
     "regot_erot_hvp", "regot_erot_plan", "regot_erot_sparsify", "regot_erot_sparsify_density",
     "regot_erot_hess_solve",
-    "regot_erot_tyy", "regot_erot_solve_batched", "regot_qrot_dual_obj_grad",
+    "regot_erot_tyy", "regot_erot_solve_batched", "regot_erot_solve_batched_grad",
+    "regot_qrot_dual_obj_grad",
     "regot_qrot_optimal_beta",
     "regot_qrot_primal_val", "regot_qrot_plan", "regot_time_pass",
     "regot_erot_dual_obj_grad_noalloc", "regot_host_alloc", "regot_host_free",
@@ -199,6 +200,9 @@ def load() -> C.CDLL:
         lib.regot_time_pass.argtypes = [vp, vp, C.c_int, C.c_double, C.c_int]
         lib.regot_erot_solve_batched.argtypes = [vp, C.POINTER(BatchDesc), C.c_double,
                                                  C.c_double, C.c_int, C.POINTER(BatchResult)]
+        lib.regot_erot_solve_batched_grad.argtypes = [vp, C.POINTER(BatchDesc), C.c_double,
+                                                      C.c_double, C.c_int,
+                                                      C.POINTER(BatchResult), vp, vp, vp]
         lib.regot_erot_hess_solve.argtypes = [vp, vp, C.c_double, vp, vp, C.c_double, C.c_int,
                                               vp, C.POINTER(C.c_int)]
         lib.regot_erot_tyy.argtypes = [vp, vp, C.c_double, vp, vp, vp, vp, C.c_int, vp, vp,

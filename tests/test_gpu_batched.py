@@ -91,3 +91,38 @@ def test_batched_rejects_bad_input():
                                    [np.full(4, 0.25)], [np.full(3, 1 / 3)], 0.05)
     with pytest.raises(ValueError):
         regot.sinkhorn_bcd_batched(xs, ys, as_, bs, -1.0)
+
+
+def test_batched_backward_matches_fp64_at_the_returned_duals():
+    # grad=True: each problem's cost a'alpha + b'beta - reg sum T (the negated
+    # dual objective of the oracle) and dL/dx = 2 s sum_j T_ij (x_i - y_j),
+    # dL/dy = 2 s sum_i T_ij (y_j - x_i), checked in FP64 at the duals the
+    # call returned. The kernels evaluate T from the FP32 cost: a relative
+    # error of ~1e-7 in M moves the exponent by ~1e-7 M / reg, a few 1e-5 of
+    # T at these sizes, hence 3e-4 of the largest gradient entry.
+    reg, tol = 0.05, 1e-6
+    xs, ys, as_, bs, sc = _batch(14, seed=9, nmin=20, nmax=700, dims=(1, 3, 4, 5, 8, 9, 16))
+    r0 = regot.sinkhorn_bcd_batched(xs, ys, as_, bs, reg, tol=tol, max_iter=5000, cost_scale=sc)
+    r = regot.sinkhorn_bcd_batched(xs, ys, as_, bs, reg, tol=tol, max_iter=5000, cost_scale=sc,
+                                   grad=True)
+    np.testing.assert_array_equal(r.niter, r0.niter)
+    assert len(r.grad_x) == len(r.grad_y) == len(r.costs) == 14
+    for p in range(14):
+        np.testing.assert_array_equal(r.duals[p], r0.duals[p])
+        x = xs[p].astype(np.float64)
+        y = ys[p].astype(np.float64)
+        n, m = x.shape[0], y.shape[0]
+        M = _cost64(xs[p], ys[p], sc[p])
+        f, _ = O.erot_dual_obj_grad(M, as_[p], bs[p], reg, r.duals[p])
+        assert abs(r.costs[p] + f) < 5e-6, (p, r.costs[p], -f)
+        alpha = r.duals[p][:n]
+        beta = np.r_[r.duals[p][n:], 0.0]
+        T = np.exp((alpha[:, None] + beta[None, :] - M) / reg)
+        gx = 2 * sc[p] * (T.sum(1)[:, None] * x - T @ y)
+        gy = 2 * sc[p] * (T.sum(0)[:, None] * y - T.T @ x)
+        assert r.grad_x[p].shape == x.shape and r.grad_y[p].shape == y.shape
+        np.testing.assert_allclose(r.grad_x[p], gx, rtol=0, atol=3e-4 * np.abs(gx).max())
+        np.testing.assert_allclose(r.grad_y[p], gy, rtol=0, atol=3e-4 * np.abs(gy).max())
+        # translating both clouds leaves the cost unchanged: the gradients sum to 0
+        np.testing.assert_allclose(r.grad_x[p].sum(0) + r.grad_y[p].sum(0), 0.0,
+                                   atol=1e-4 * np.abs(gx).sum())
