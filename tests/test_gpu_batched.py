@@ -126,3 +126,29 @@ def test_batched_backward_matches_fp64_at_the_returned_duals():
         # translating both clouds leaves the cost unchanged: the gradients sum to 0
         np.testing.assert_allclose(r.grad_x[p].sum(0) + r.grad_y[p].sum(0), 0.0,
                                    atol=1e-4 * np.abs(gx).sum())
+
+
+def test_batched_backward_at_max_iter_iterates():
+    # problems stopped by max_iter (odd and even counts, so the last alpha
+    # sits in either ping-pong buffer): the backward still uses exactly the
+    # returned iterate, whose row sums are still off a by up to 0.1
+    reg = 0.05
+    xs, ys, as_, bs, sc = _batch(8, seed=10, nmin=40, nmax=400, dims=(2, 6, 11, 16))
+    for it in (4, 7):
+        r = regot.sinkhorn_bcd_batched(xs, ys, as_, bs, reg, tol=1e-14, max_iter=it,
+                                       cost_scale=sc, grad=True)
+        assert np.all(r.niter == it)
+        for p in range(8):
+            n = xs[p].shape[0]
+            M = _cost64(xs[p], ys[p], sc[p])
+            f, _ = O.erot_dual_obj_grad(M, as_[p], bs[p], reg, r.duals[p])
+            assert abs(r.costs[p] + f) < 5e-6 * max(1.0, abs(f)), (it, p)
+            alpha = r.duals[p][:n]
+            beta = np.r_[r.duals[p][n:], 0.0]
+            T = np.exp((alpha[:, None] + beta[None, :] - M) / reg)
+            x = xs[p].astype(np.float64)
+            y = ys[p].astype(np.float64)
+            gx = 2 * sc[p] * (T.sum(1)[:, None] * x - T @ y)
+            gy = 2 * sc[p] * (T.sum(0)[:, None] * y - T.T @ x)
+            np.testing.assert_allclose(r.grad_x[p], gx, rtol=0, atol=3e-4 * np.abs(gx).max())
+            np.testing.assert_allclose(r.grad_y[p], gy, rtol=0, atol=3e-4 * np.abs(gy).max())
