@@ -297,7 +297,7 @@ def run_batched(args):
             "backward_ms": round(statistics.median(fb_dev) - dev, 3),
             "e2e": round(P / (statistics.median(fb_wall) * 1e-3), 1),
             "d2h_bytes_per_step": int(sum(a.nbytes + b.nbytes for a, b in zip(as_, bs))
-                                      + 2 * sum(x.nbytes + y.nbytes for x, y in zip(xs, ys))
+                                      + sum(x.nbytes + y.nbytes for x, y in zip(xs, ys))
                                       + 8 * P),
             "what": "cost a'alpha + b'beta - reg sum T and dL/dx, dL/dy per problem "
                     "in the same call as the solve"},

@@ -266,11 +266,12 @@ int regot_erot_solve_batched(regot_ctx* ctx, const regot_batch_desc* desc, doubl
  * negated dual objective of src/sinkhorn_problem_obj.cpp:324-342) and, by
  * the envelope theorem dL/dM = T with M_ij = s |x_i - y_j|^2,
  * grad_x = 2 s sum_j T_ij (x_i - y_j), grad_y = 2 s sum_i T_ij (y_j - x_i),
- * laid out like desc->x and desc->y. Host buffers, each optional (NULL);
- * res->solve_ms then covers the solve and the backward. */
+ * laid out like desc->x and desc->y and, like the points, FP32 (they are
+ * accumulated in FP32). Host buffers, each optional (NULL); res->solve_ms
+ * then covers the solve and the backward. */
 int regot_erot_solve_batched_grad(regot_ctx* ctx, const regot_batch_desc* desc, double reg,
                                   double tol, int max_iter, regot_batch_result* res, double* cost,
-                                  double* grad_x, double* grad_y);
+                                  float* grad_x, float* grad_y);
 
 /* ---- Derivatives of EROT solves (no reference counterpart) ---- */
 

@@ -599,7 +599,7 @@ int regot_erot_solve_batched(regot_ctx* ctx, const regot_batch_desc* desc, doubl
 
 int regot_erot_solve_batched_grad(regot_ctx* ctx, const regot_batch_desc* desc, double reg,
                                   double tol, int max_iter, regot_batch_result* res, double* cost,
-                                  double* grad_x, double* grad_y) {
+                                  float* grad_x, float* grad_y) {
     return guarded(ctx, [&] {
         require(desc && res, "NULL argument");
         require(desc->count > 0, "the batch is empty");

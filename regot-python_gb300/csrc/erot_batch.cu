@@ -451,13 +451,14 @@ __global__ void k_bloop(BatchState* st, cudaGraphConditionalHandle h) {
 // differences are summed against a running base-2 reference like the
 // log-sum-exp, so no term overflows whatever the duals. Summing T (x_i - y_j)
 // instead of forming r_i x_i - (T y)_i avoids cancelling the two terms.
-// side 0 also writes the row sums of T (for the cost).
+// The gradients are accumulated in FP32 and stored as FP32, the type of the
+// points. side 0 also writes the row sums of T (for the cost).
 constexpr int kGWarps = 8;  // own points per CTA
 
 template <int DP>
 __global__ void __launch_bounds__(kGWarps * 32) k_bgrad(
     const BatchDev B, const int2* __restrict__ items, int side, const float2* __restrict__ as,
-    const float2* __restrict__ bs, float k2, double* __restrict__ grad,
+    const float2* __restrict__ bs, float k2, float* __restrict__ grad,
     double* __restrict__ tsum) {
     const int2 it = items[blockIdx.x];
     const int p = it.x;
@@ -544,7 +545,8 @@ __global__ void __launch_bounds__(kGWarps * 32) k_bgrad(
         if (lane == k) v = acc[k];
     if (grad && lane < d) {
         const long long off = side ? B.yo[p] : B.xo[p];
-        grad[off + (long long)i * d + lane] = 2.0 * (double)sc * ldexp((double)(v * fr), (int)fl);
+        grad[off + (long long)i * d + lane] =
+            (float)(2.0 * (double)sc * ldexp((double)(v * fr), (int)fl));
     }
     if (side == 0 && lane == 0) tsum[B.ro[p] + i] = ldexp((double)(ts * fr), (int)fl);
 }
@@ -630,8 +632,8 @@ void upload_vec(DBuf<T>& buf, const std::vector<T>& v, cudaStream_t st) {
 }  // namespace
 
 void erot_solve_batched_gpu(regot_ctx* ctx, const regot_batch_desc* D, double reg, double tol,
-                            int max_iter, regot_batch_result* res, double* cost, double* grad_x,
-                            double* grad_y) {
+                            int max_iter, regot_batch_result* res, double* cost, float* grad_x,
+                            float* grad_y) {
     cudaStream_t st = ctx->stream;
     const int P = D->count;
     std::vector<int> hn(P), hm(P), hd(P), ro(P), co(P), rbo(P + 1), cls(P);
@@ -909,7 +911,8 @@ void erot_solve_batched_gpu(regot_ctx* ctx, const regot_batch_desc* D, double re
     // Backward: costs and point gradients at every problem's last iterate,
     // its alpha gathered into one buffer and both duals split on a common
     // grid from their max.
-    DBuf<double> Af, tsum, gxd, gyd, dcost;
+    DBuf<double> Af, tsum, dcost;
+    DBuf<float> gxd, gyd;
     if (cost || grad_x || grad_y) {
         Af.alloc(NR, st);
         tsum.alloc(NR, st);
@@ -925,7 +928,7 @@ void erot_solve_batched_gpu(regot_ctx* ctx, const regot_batch_desc* D, double re
         std::vector<int> order(P);
         for (int p = 0; p < P; ++p) order[p] = p;
         for (int side = 0; side < 2; ++side) {
-            double* out = side ? gyd.get() : gxd.get();
+            float* out = side ? gyd.get() : gxd.get();
             if (side == 1 && !grad_y) break;  // side 0 runs for the row sums of T
             std::stable_sort(order.begin(), order.end(), [&](int u, int v) {
                 return side ? hn[u] > hn[v] : hm[u] > hm[v];
@@ -972,8 +975,8 @@ void erot_solve_batched_gpu(regot_ctx* ctx, const regot_batch_desc* D, double re
     d2h(hmar.data(), mar.get(), P * sizeof(double), st);
     d2h(hfpar.data(), fpar.get(), P * sizeof(int), st);
     d2h(hiter.data(), iter.get(), P * sizeof(int), st);
-    if (grad_x) d2h(grad_x, gxd.get(), NX * sizeof(double), st);
-    if (grad_y) d2h(grad_y, gyd.get(), NY * sizeof(double), st);
+    if (grad_x) d2h(grad_x, gxd.get(), NX * sizeof(float), st);
+    if (grad_y) d2h(grad_y, gyd.get(), NY * sizeof(float), st);
     if (cost) d2h(cost, dcost.get(), P * sizeof(double), st);
     sync(st);
     float ms = 0.f;

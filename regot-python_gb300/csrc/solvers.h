@@ -35,10 +35,11 @@ void erot_tyy_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, const double* d
                   double* d_Z);
 // Batched BCD over point-cloud problems (erot_batch.cu).
 // cost, grad_x, grad_y (host, optional): each problem's regularised OT cost
-// and its gradients with respect to the points, at the returned duals.
+// and its gradients with respect to the points (FP32, like the points), at
+// the returned duals.
 void erot_solve_batched_gpu(regot_ctx* ctx, const regot_batch_desc* D, double reg, double tol,
                             int max_iter, regot_batch_result* res, double* cost = nullptr,
-                            double* grad_x = nullptr, double* grad_y = nullptr);
+                            float* grad_x = nullptr, float* grad_y = nullptr);
 // H x = rhs with the exact dual Hessian at gamma (host vectors, n + m - 1).
 void erot_hess_solve_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, const double* gamma,
                          const double* rhs, double tol, int max_iter, double* x, int* iters);

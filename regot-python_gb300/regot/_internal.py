@@ -680,7 +680,7 @@ def sinkhorn_bcd_batched(xs, ys, as_, bs, reg, tol=1e-6, max_iter=1000, cost_sca
     grad=True adds the backward in the same call: each problem's cost
     L = a'alpha + b'beta - reg sum T and dL/dx = 2 s sum_j T_ij (x_i - y_j),
     dL/dy = 2 s sum_i T_ij (y_j - x_i) at the returned duals (the envelope
-    theorem, dL/dM = T)."""
+    theorem, dL/dM = T), as float32 arrays like the points."""
     P = len(xs)
     if not (len(ys) == len(as_) == len(bs) == P) or P == 0:
         raise ValueError("xs, ys, as_ and bs must be non-empty lists of the same length")
@@ -724,8 +724,8 @@ def sinkhorn_bcd_batched(xs, ys, as_, bs, reg, tol=1e-6, max_iter=1000, cost_sca
     r.niter, r.mar_err = niter.ctypes.data, mar.ctypes.data
     if grad:
         costs = np.zeros(P)
-        gx = np.zeros(X.size)
-        gy = np.zeros(Y.size)
+        gx = np.zeros(X.size, dtype=np.float32)
+        gy = np.zeros(Y.size, dtype=np.float32)
         ctx.check(lib.regot_erot_solve_batched_grad(
             ctx.handle, C.byref(desc), float(reg), float(tol), int(max_iter), C.byref(r),
             costs.ctypes.data, gx.ctypes.data, gy.ctypes.data))

@@ -121,6 +121,7 @@ def test_batched_backward_matches_fp64_at_the_returned_duals():
         gx = 2 * sc[p] * (T.sum(1)[:, None] * x - T @ y)
         gy = 2 * sc[p] * (T.sum(0)[:, None] * y - T.T @ x)
         assert r.grad_x[p].shape == x.shape and r.grad_y[p].shape == y.shape
+        assert r.grad_x[p].dtype == np.float32 and r.grad_y[p].dtype == np.float32
         np.testing.assert_allclose(r.grad_x[p], gx, rtol=0, atol=3e-4 * np.abs(gx).max())
         np.testing.assert_allclose(r.grad_y[p], gy, rtol=0, atol=3e-4 * np.abs(gy).max())
         # translating both clouds leaves the cost unchanged: the gradients sum to 0
