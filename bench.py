@@ -437,6 +437,67 @@ def run_autograd(args):
     print(json.dumps(line), flush=True)
 
 
+def pass_table(ctx, prob, reg, reps=20, kinds=None):
+    """Per-op roofline of every dense pass over `prob` (regot_time_pass):
+    device time per launch from CUDA events around `reps` back-to-back
+    launches on the library's stream, algorithmic bytes (regot_pass_bytes:
+    one read of M plus the plan / averaged-plan / bitmask traffic the pass
+    writes) and their ratio against the measured HBM copy peak."""
+    import ctypes as C
+
+    import torch
+
+    from regot import _lib
+
+    lib = _lib.load()
+    peak, _ = measured_peaks()
+    stream = torch.cuda.current_stream()
+    rows = {}
+    for kind, (name, op) in enumerate(_lib.PASS_KINDS):
+        if kinds is not None and name not in kinds:
+            continue
+        ctx.check(lib.regot_time_pass(ctx.handle, prob.handle, kind, reg, 1))  # prepares
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.check(lib.regot_time_pass(ctx.handle, prob.handle, kind, reg, reps))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        us = e0.elapsed_time(e1) * 1e3 / reps
+        nbytes = int(lib.regot_pass_bytes(prob.handle, kind))
+        gbs = nbytes / (us * 1e-6) / 1e9
+        rows[name] = {"kernel": f"dense_pass<{op}>", "us": round(us, 2), "bytes": nbytes,
+                      "gbs": round(gbs, 1), "frac": round(gbs / peak, 4)}
+    return rows
+
+
+def run_passes(args):
+    """One JSON line: the per-op roofline table at n = m = args.n in mixed
+    (FP32 M) and plain FP64 storage."""
+    import torch
+
+    import regot
+    from problems import erot_points
+    from regot import _lib
+
+    n = args.n
+    M, a, b = erot_points(n, n, seed=0, dtype=np.float32)
+    ctx = _lib.context(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx.set_stream(stream.cuda_stream)
+    out = {}
+    for prec in ("mixed", "fp64"):
+        prob = regot.Problem(M, a, b, precision=prec)
+        out[prec] = pass_table(ctx, prob, REG)
+        prob.close()
+    peak, src = measured_peaks()
+    print(json.dumps({"workload": "dense passes", "n": n, "m": n, "reg": REG,
+                      "peak_gbs": peak, "peak_source": src, "passes": out}), flush=True)
+    ctx.set_stream(None)
+
+
 def run_probe(kind, n):
     """Ceilings on this GPU, printed as one JSON line.
 
@@ -527,7 +588,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ncu-case", action="store_true",
                     help="a few passes for an ncu capture (no timing, no JSON)")
-    ap.add_argument("--workload", choices=["bcd", "batched", "solvers", "autograd"],
+    ap.add_argument("--workload", choices=["bcd", "batched", "solvers", "autograd", "passes"],
                     default="bcd",
                     help="batched: the batched uneven-problem workload (its own JSON line); "
                          "solvers: one line per solver of the solver table")
@@ -579,6 +640,9 @@ def main():
         return
     if args.workload == "autograd":
         run_autograd(args)
+        return
+    if args.workload == "passes":
+        run_passes(args)
         return
 
     import torch

@@ -292,6 +292,23 @@ int regot_erot_hess_solve(regot_ctx* ctx, regot_dproblem* prob, double reg, cons
 int regot_erot_tyy(regot_ctx* ctx, regot_dproblem* prob, double reg, const double* gamma,
                    const double* u, const double* W, const double* Y, int d, double* rows,
                    double* Z, int mem);
+/* M = scale * (squared Euclidean distance of row i of x and row j of y), by
+ * direct differences (no |x|^2 + |y|^2 - 2 x.y cancellation): x n x d, y
+ * m x d, M n x m with row stride ldm, all row-major DEVICE arrays of dtype
+ * (REGOT_F32 or REGOT_F64). Enqueued on the context's stream, not
+ * synchronised. The cost of the point-cloud losses of the torch wrapper; no
+ * counterpart in the reference, which takes M as given. */
+int regot_sqeuclid_cost(regot_ctx* ctx, const void* x, const void* y, int n, int m, int d,
+                        double scale, int dtype, void* M, long long ldm);
+/* The column-side contraction of the same G: cols_j = sum_i G_ij (cols may
+ * be NULL) and Z = G'X (X n x d, Z m x d, row-major); the dL/dy of a
+ * squared-Euclidean cost is 2 (cols o y - Z) / scale. FP32 storage runs both
+ * contractions on the tensor cores (tcgen05, BF16 hi/lo split operands,
+ * FP32 accumulation: about 1e-5 relative per product); FP64 storage on the
+ * CUDA cores in FP64. No counterpart in the reference. */
+int regot_erot_tty(regot_ctx* ctx, regot_dproblem* prob, double reg, const double* gamma,
+                   const double* u, const double* W, const double* X, int d, double* cols,
+                   double* Z, int mem);
 
 /* Problem::optimal_beta / optimal_alpha (src/sinkhorn_problem_bcd.cpp:149-201). */
 int regot_erot_optimal_beta(regot_ctx* ctx, regot_dproblem* prob, double reg,
@@ -343,22 +360,52 @@ int regot_qrot_plan(regot_ctx* ctx, regot_dproblem* prob, double reg, const doub
 
 /* ---- Measurement ---- */
 
-/* Kinds of dense pass for regot_time_pass. */
+/* Kinds of dense pass for regot_time_pass (each is one streamed read of M,
+ * plus the writes noted). */
 enum {
-    REGOT_PASS_EROT_ROW = 0,   /* row log-sum-exp pass of sinkhorn_bcd */
-    REGOT_PASS_EROT_COL = 1,   /* column log-sum-exp pass of sinkhorn_bcd */
-    REGOT_PASS_EROT_GRAD = 2,  /* fused row+column sums (objective / gradient) */
-    REGOT_PASS_EROT_HVP = 3,   /* Hessian-vector product */
-    REGOT_PASS_QROT_GRAD = 4   /* QROT relu objective / gradient */
+    REGOT_PASS_EROT_ROW = 0,      /* row log-sum-exp pass of sinkhorn_bcd */
+    REGOT_PASS_EROT_COL = 1,      /* column log-sum-exp pass of sinkhorn_bcd */
+    REGOT_PASS_EROT_GRAD = 2,     /* fused row+column sums (objective / gradient) */
+    REGOT_PASS_EROT_HVP = 3,      /* Hessian-vector product */
+    REGOT_PASS_QROT_GRAD = 4,     /* QROT relu objective / gradient */
+    REGOT_PASS_EROT_LS = 5,       /* objective changes at 4 step sizes (Armijo, line_selection) */
+    REGOT_PASS_EROT_GRADLS = 6,   /* L-BFGS / More-Thuente trial: gradient + exact change */
+    REGOT_PASS_EROT_AVG = 7,      /* APDAGD averaged plan (X read and written) */
+    REGOT_PASS_EROT_PLAN = 8,     /* FP64 plan written to device memory */
+    REGOT_PASS_EROT_ROWMAX = 9,   /* optimal_alpha anchor (row max) */
+    REGOT_PASS_EROT_COLMAX = 10,  /* optimal_beta anchor (column max) */
+    REGOT_PASS_QROT_GRADMASK = 11,/* QROT gradient + Jacobian bitmask written */
+    REGOT_PASS_QROT_GRADLS = 12,  /* QROT line-search trial */
+    REGOT_PASS_QROT_OBJ = 13,     /* QROT objective only */
+    REGOT_PASS_QROT_P1 = 14,      /* primal_val pass 1 (row sums) */
+    REGOT_PASS_QROT_P2 = 15,      /* primal_val pass 2 (weighted column sums) */
+    REGOT_PASS_QROT_P3 = 16,      /* primal_val pass 3 (value terms) */
+    REGOT_PASS_QROT_COLROOT = 17, /* optimal_beta Newton round (FP64 accumulation) */
+    REGOT_PASS_QROT_ROWROOT = 18, /* optimal_alpha Newton round (FP64 accumulation) */
+    REGOT_PASS_QROT_AVG = 19,     /* QROT averaged plan (X read and written) */
+    REGOT_PASS_QROT_PLAN = 20,    /* FP64 QROT plan written to device memory */
+    REGOT_PASS_COUNT = 21
 };
 /* Enqueue `reps` launches of one dense pass over M on the context's stream
- * (duals zero, beta = 0) and return without synchronising, so that the
- * caller can bracket them with its own events. The first call for a
- * (problem, kind, reg) also prepares the pass inputs (in mixed precision the
- * FP32 split and one pass) and synchronises before enqueueing; later calls
- * enqueue the `reps` passes only. No counterpart in the reference: it
+ * and return without synchronising, so that the caller can bracket them
+ * with its own events. The inputs are fixed, deterministic vectors (duals 0
+ * for the EROT passes and 0.1 for the QROT passes). The first call for a
+ * (problem, kind, reg) also prepares the pass inputs (in mixed precision
+ * the FP32 split and one pass) and synchronises before enqueueing; later
+ * calls enqueue the `reps` passes only. No counterpart in the reference: it
  * measures the kernels behind the solvers above. */
 int regot_time_pass(regot_ctx* ctx, regot_dproblem* prob, int kind, double reg, int reps);
+/* Algorithmic bytes of one pass of `kind` over prob (M read once in its
+ * storage type, plus the plan, averaged-plan or bitmask traffic the pass
+ * writes); -1 for an invalid argument. */
+long long regot_pass_bytes(regot_dproblem* prob, int kind);
+/* Limit (polls of about 200 us) of the dense passes' bounded waits on their
+ * parameter copies; returns the previous limit, and a negative value
+ * restores the default (16384). A pass whose wait gives up drains the copy
+ * under the default limit, marks its result invalid and the call returns
+ * REGOT_ERR_TIMEOUT; 0 makes every such wait give up at once. Process-wide;
+ * for exercising the timeout path. No counterpart in the reference. */
+long long regot_set_wait_limit(long long spins);
 
 /* ---- Allocation-free variant ----
  * No counterpart in the reference. regot_erot_dual_obj_grad for callers that
@@ -368,15 +415,19 @@ int regot_time_pass(regot_ctx* ctx, regot_dproblem* prob, int kind, double reg, 
  * cannot afford cudaMalloc's implicit device synchronisation. It allocates
  * nothing: its scratch is one static device array of
  * REGOT_NOALLOC_SCRATCH_BYTES (16 MiB) that every GPU loading the library
- * holds until exit; a problem that needs more (beyond about n = m = 14000)
- * returns REGOT_ERR_TOO_LARGE. All pointers are device pointers: M is n x m
+ * holds until exit; a problem that needs more (about 32 (n + m) +
+ * 4 n m (1/512 + 1/64) bytes: beyond about n = m = 15400, while n = m = 14000
+ * always fits) returns REGOT_ERR_TOO_LARGE. All pointers are device pointers: M is n x m
  * FP32 row-major with row stride ldm (a multiple of 4, 16-byte aligned
  * base), gamma = (alpha, beta~) has n+m-1 entries (beta_m = 0), grad has
  * n+m-1 entries, obj one. The work is enqueued on `stream` (a cudaStream_t,
  * NULL = legacy default) and not synchronised. The first call on a device
  * looks up the scratch address (cudaGetSymbolAddress) and should come before
  * any stream capture. All calls share the scratch: calls that overlap on the
- * GPU race and must be serialised by the caller. */
+ * GPU race and must be serialised by the caller. A failure on the GPU after
+ * the call has returned (a bounded wait of the dense pass that gave up)
+ * shows as NaN in grad and *obj; the status only reports argument, size and
+ * launch errors. */
 #define REGOT_NOALLOC_SCRATCH_BYTES (16u << 20)
 int regot_erot_dual_obj_grad_noalloc(const float* M, long long ldm, int n, int m,
                                      const double* gamma, const double* a, const double* b,

@@ -2,6 +2,31 @@
 // Nocedal-Wright line search of the vendored LBFGS++ (MIT), shared by the
 // qrot_lbfgs_dual and sinkhorn_lbfgs_dual restatements. Test infrastructure
 // only (see oracle.h).
+// The L-BFGS control flow, line search and error messages below follow
+// LBFGS++, which carries this notice:
+//
+//   Copyright (C) 2016-2026 Yixuan Qiu <yixuan.qiu@cos.name>
+//   Copyright (C) 2016-2026 Dirk Toewe <DirkToewe@GoogleMail.com>
+//   MIT License
+//
+//   Permission is hereby granted, free of charge, to any person obtaining a
+//   copy of this software and associated documentation files (the
+//   "Software"), to deal in the Software without restriction, including
+//   without limitation the rights to use, copy, modify, merge, publish,
+//   distribute, sublicense, and/or sell copies of the Software, and to
+//   permit persons to whom the Software is furnished to do so, subject to
+//   the following conditions:
+//
+//   The above copyright notice and this permission notice shall be included
+//   in all copies or substantial portions of the Software.
+//
+//   THE SOFTWARE IS PROVIDED "AS IS", WITHOUT WARRANTY OF ANY KIND, EXPRESS
+//   OR IMPLIED, INCLUDING BUT NOT LIMITED TO THE WARRANTIES OF
+//   MERCHANTABILITY, FITNESS FOR A PARTICULAR PURPOSE AND NONINFRINGEMENT.
+//   IN NO EVENT SHALL THE AUTHORS OR COPYRIGHT HOLDERS BE LIABLE FOR ANY
+//   CLAIM, DAMAGES OR OTHER LIABILITY, WHETHER IN AN ACTION OF CONTRACT,
+//   TORT OR OTHERWISE, ARISING FROM, OUT OF OR IN CONNECTION WITH THE
+//   SOFTWARE OR THE USE OR OTHER DEALINGS IN THE SOFTWARE.
 #ifndef REGOT_ORACLE_LBFGS_H
 #define REGOT_ORACLE_LBFGS_H
 

@@ -9,6 +9,7 @@
 #include <mutex>
 #include <string>
 #include <unordered_map>
+#include <type_traits>
 #include <vector>
 
 #include "device_util.cuh"
@@ -49,6 +50,24 @@ __global__ void k_convert(const TS* src, long long lds, TD* dst, long long ldd, 
         const long long i = t / ldd, j = t - i * ldd;
         dst[t] = j < m ? (TD)src[i * lds + j] : (TD)0;
     }
+}
+
+// *flag = 1 if any of the `nvec` 16-byte vectors of M holds a NaN or an
+// infinity (padding columns are zero).
+template <typename TM>
+__global__ void k_nonfinite(const void* M, long long nvec, int* flag) {
+    using V = typename std::conditional<sizeof(TM) == 4, float4, double2>::type;
+    const V* v = static_cast<const V*>(M);
+    bool bad = false;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < nvec;
+         t += (long long)gridDim.x * blockDim.x) {
+        const V x = v[t];
+        if constexpr (sizeof(TM) == 4)
+            bad |= !(isfinite(x.x) && isfinite(x.y) && isfinite(x.z) && isfinite(x.w));
+        else
+            bad |= !(isfinite(x.x) && isfinite(x.y));
+    }
+    if (__syncthreads_or(bad) && threadIdx.x == 0) atomicOr(flag, 1);
 }
 
 void check_solver_args(regot_dproblem* P, double reg, double tol, int max_iter, regot_result* res,
@@ -389,6 +408,23 @@ int regot_problem_create(regot_ctx* ctx, const regot_problem_desc* d, int precis
                 REGOT_CHECK_LAUNCH();
                 if (stage) REGOT_CUDA(cudaFreeAsync(stage, st));
             }
+            // M must be finite in its storage type (an FP64 entry beyond the
+            // FP32 range becomes an infinity in mixed storage).
+            {
+                DBuf<int> flag(1, st);
+                flag.zero();
+                const long long nvec = (long long)n * P->ldm * (long long)es / 16;
+                const int blocks = (int)std::min<long long>(cdiv(nvec, 256), 4LL * device_sm_count());
+                if (es == 4) k_nonfinite<float><<<blocks, 256, 0, st>>>(P->M, nvec, flag.get());
+                else k_nonfinite<double><<<blocks, 256, 0, st>>>(P->M, nvec, flag.get());
+                count_launch();
+                REGOT_CHECK_LAUNCH();
+                int bad = 0;
+                read_small(ctx, &bad, flag.get(), sizeof(int), st);
+                require(!bad, precision == REGOT_PREC_MIXED && d->M_dtype == REGOT_F64
+                                  ? "M must be finite (and within the FP32 range in mixed precision)"
+                                  : "M must be finite");
+            }
             sync(st);
         } catch (...) {
             if (P->M) cudaFreeAsync(P->M, st);
@@ -624,54 +660,82 @@ int regot_erot_hess_solve(regot_ctx* ctx, regot_dproblem* P, double reg, const d
     });
 }
 
+static void erot_contract_entry(regot_ctx* ctx, regot_dproblem* P, double reg,
+                                const double* gamma, const double* u, const double* W,
+                                const double* Y, int d, double* sums, double* Z, int mem,
+                                bool cols) {
+    require(P && gamma, "NULL argument");
+    require(reg > 0.0, "reg must be positive");
+    require(d >= 0 && (d == 0 || (Y && Z)), "Y and Z are required when d > 0");
+    require(mem == REGOT_MEM_HOST || mem == REGOT_MEM_DEVICE, "unknown memory kind");
+    cudaStream_t st = ctx->stream;
+    const int n = P->n, m = P->m;
+    const int nown = cols ? m : n, K = cols ? n : m;
+    const size_t nm1 = (size_t)(n + m - 1) * sizeof(double);
+    // duals and adjoint with beta_m = 0 appended, on the device
+    DBuf<double> g(n + m, st), uu(u ? n + m : 0, st);
+    g.zero();
+    const cudaMemcpyKind kin = mem == REGOT_MEM_HOST ? cudaMemcpyHostToDevice
+                                                     : cudaMemcpyDeviceToDevice;
+    REGOT_CUDA(cudaMemcpyAsync(g.get(), gamma, nm1, kin, st));
+    if (u) {
+        uu.zero();
+        REGOT_CUDA(cudaMemcpyAsync(uu.get(), u, nm1, kin, st));
+    }
+    const double *dW = W, *dY = Y;
+    DBuf<double> hW, hY, hZ, hS;
+    double *dZ = Z, *dS = sums;
+    if (mem == REGOT_MEM_HOST) {
+        if (W) {
+            hW.alloc((size_t)n * m, st);
+            h2d(hW.get(), W, (size_t)n * m * sizeof(double), st);
+            dW = hW.get();
+        }
+        if (d > 0) {
+            hY.alloc((size_t)K * d, st);
+            h2d(hY.get(), Y, (size_t)K * d * sizeof(double), st);
+            dY = hY.get();
+            hZ.alloc((size_t)nown * d, st);
+            dZ = hZ.get();
+        }
+        if (sums) {
+            hS.alloc(nown, st);
+            dS = hS.get();
+        }
+    }
+    erot_contract_gpu(ctx, P, reg, g.get(), u ? uu.get() : nullptr, dW, d > 0 ? dY : nullptr, d,
+                      cols, dS, d > 0 ? dZ : nullptr);
+    if (mem == REGOT_MEM_HOST) {
+        if (d > 0) d2h(Z, dZ, (size_t)nown * d * sizeof(double), st);
+        if (sums) d2h(sums, dS, (size_t)nown * sizeof(double), st);
+    }
+    sync(st);
+}
+
 int regot_erot_tyy(regot_ctx* ctx, regot_dproblem* P, double reg, const double* gamma,
                    const double* u, const double* W, const double* Y, int d, double* rows,
                    double* Z, int mem) {
     return guarded(ctx, [&] {
-        require(P && gamma, "NULL argument");
-        require(reg > 0.0, "reg must be positive");
-        require(d >= 0 && (d == 0 || (Y && Z)), "Y and Z are required when d > 0");
-        require(mem == REGOT_MEM_HOST || mem == REGOT_MEM_DEVICE, "unknown memory kind");
-        cudaStream_t st = ctx->stream;
-        const int n = P->n, m = P->m;
-        const size_t nm1 = (size_t)(n + m - 1) * sizeof(double);
-        // duals and adjoint with beta_m = 0 appended, on the device
-        DBuf<double> g(n + m, st), uu(u ? n + m : 0, st);
-        g.zero();
-        const cudaMemcpyKind kin = mem == REGOT_MEM_HOST ? cudaMemcpyHostToDevice
-                                                         : cudaMemcpyDeviceToDevice;
-        REGOT_CUDA(cudaMemcpyAsync(g.get(), gamma, nm1, kin, st));
-        if (u) {
-            uu.zero();
-            REGOT_CUDA(cudaMemcpyAsync(uu.get(), u, nm1, kin, st));
-        }
-        const double *dW = W, *dY = Y;
-        DBuf<double> hW, hY, hZ, hR;
-        double *dZ = Z, *dR = rows;
-        if (mem == REGOT_MEM_HOST) {
-            if (W) {
-                hW.alloc((size_t)n * m, st);
-                h2d(hW.get(), W, (size_t)n * m * sizeof(double), st);
-                dW = hW.get();
-            }
-            if (d > 0) {
-                hY.alloc((size_t)m * d, st);
-                h2d(hY.get(), Y, (size_t)m * d * sizeof(double), st);
-                dY = hY.get();
-                hZ.alloc((size_t)n * d, st);
-                dZ = hZ.get();
-            }
-            if (rows) {
-                hR.alloc(n, st);
-                dR = hR.get();
-            }
-        }
-        erot_tyy_gpu(ctx, P, reg, g.get(), u ? uu.get() : nullptr, dW, dY, d, dR, dZ);
-        if (mem == REGOT_MEM_HOST) {
-            if (d > 0) d2h(Z, dZ, (size_t)n * d * sizeof(double), st);
-            if (rows) d2h(rows, dR, (size_t)n * sizeof(double), st);
-        }
-        sync(st);
+        erot_contract_entry(ctx, P, reg, gamma, u, W, Y, d, rows, Z, mem, false);
+    });
+}
+
+int regot_sqeuclid_cost(regot_ctx* ctx, const void* x, const void* y, int n, int m, int d,
+                        double scale, int dtype, void* M, long long ldm) {
+    return guarded(ctx, [&] {
+        require(x && y && M, "NULL argument");
+        require(n > 0 && m > 0 && d > 0 && ldm >= m, "invalid sizes");
+        require(dtype == REGOT_F32 || dtype == REGOT_F64, "unsupported dtype");
+        require(std::isfinite(scale), "scale must be finite");
+        sqeuclid_gpu(x, y, n, m, d, scale, dtype == REGOT_F64, M, ldm, ctx->stream);
+    });
+}
+
+int regot_erot_tty(regot_ctx* ctx, regot_dproblem* P, double reg, const double* gamma,
+                   const double* u, const double* W, const double* X, int d, double* cols,
+                   double* Z, int mem) {
+    return guarded(ctx, [&] {
+        erot_contract_entry(ctx, P, reg, gamma, u, W, X, d, cols, Z, mem, true);
     });
 }
 
@@ -718,10 +782,33 @@ struct TimePassState {
     double reg = 0.0;
     cudaStream_t stream = nullptr;
     ErotOps* ops = nullptr;
-    DBuf<double> vec, mx;
+    DBuf<double> vec, mx, plan;
+    DBuf<char> xavg;
+    DBuf<uint32_t> bitmask;
     int prepared_op = -1;  // pass whose inputs (split) are in place
 };
 TimePassState* g_tp = nullptr;
+
+// Pass kinds of regot_time_pass, in the order of the REGOT_PASS_* enum.
+constexpr int kTimedOps[REGOT_PASS_COUNT] = {
+    OP_E_ROW, OP_E_COL, OP_E_ROWCOL, OP_E_HVP, OP_Q_GRAD, OP_E_LS, OP_E_GRADLS, OP_E_AVG,
+    OP_E_PLAN, OP_E_ROWMAX, OP_E_COLMAX, OP_Q_GRADMASK, OP_Q_GRADLS, OP_Q_OBJ, OP_Q_P1,
+    OP_Q_P2, OP_Q_P3, OP_Q_COLROOT, OP_Q_ROWROOT, OP_Q_AVG, OP_Q_PLAN};
+
+// Deterministic pass inputs: duals (0.1 for the QROT passes, so that a part
+// of the entries is positive; 0 for EROT), weights and directions of a few
+// hundredths, as in the solvers' late iterations.
+__global__ void k_time_pass_inputs(double* v, int n, int m, bool qrot) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int len = 4 * (n + m);
+    if (t >= len) return;
+    const int block = t / (n + m);  // 0: ra|cb, 1: rx|cx, 2: cx2 (cols), 3: rd|cd
+    const int k = t % (n + m);
+    double x = 0.0;
+    if (block == 0) x = qrot ? 0.1 : 0.0;
+    else x = 0.01 * (1 + (k * 7919) % 5) * (block == 3 ? 0.1 : 1.0);
+    v[t] = x;
+}
 }  // namespace
 
 static void drop_time_pass_state(regot_dproblem* P) {
@@ -732,12 +819,30 @@ static void drop_time_pass_state(regot_dproblem* P) {
     }
 }
 
+extern "C" long long regot_set_wait_limit(long long spins) { return set_wait_limit(spins); }
+
+extern "C" long long regot_pass_bytes(regot_dproblem* P, int kind) {
+    if (!P || kind < 0 || kind >= REGOT_PASS_COUNT) return -1;
+    const long long nm = (long long)P->n * P->m;
+    const long long es = P->prec == REGOT_PREC_MIXED ? 4 : 8;
+    const int op = kTimedOps[kind];
+    long long bytes = nm * es;  // one read of M
+    if (op == OP_E_PLAN || op == OP_Q_PLAN) bytes += nm * 8;  // FP64 plan written
+    if (op == OP_E_AVG || op == OP_Q_AVG) bytes += 2 * nm * es;  // averaged plan read + written
+    if (op == OP_Q_GRADMASK) bytes += nm / 8;  // bitmask written
+    return bytes;
+}
+
 extern "C" int regot_time_pass(regot_ctx* ctx, regot_dproblem* P, int kind, double reg,
                                int reps) {
     return guarded(ctx, [&] {
         require(P != nullptr && reps >= 0, "invalid argument");
-        require(kind >= REGOT_PASS_EROT_ROW && kind <= REGOT_PASS_QROT_GRAD, "unknown pass kind");
+        require(kind >= 0 && kind < REGOT_PASS_COUNT, "unknown pass kind");
+        require(reg > 0.0 && std::isfinite(reg), "reg must be a positive finite number");
         cudaStream_t st = ctx->stream;
+        const int n = P->n, m = P->m;
+        const int op = kTimedOps[kind];
+        const bool qrot = op >= OP_Q_GRAD && op != OP_E_GRADLS && op != OP_E_AVG;
         // Workspace kept between calls for the same problem (the timed region
         // should contain the passes only).
         if (!g_tp || g_tp->P != P || g_tp->reg != reg || g_tp->stream != st) {
@@ -750,26 +855,59 @@ extern "C" int regot_time_pass(regot_ctx* ctx, regot_dproblem* P, int kind, doub
             g_tp->reg = reg;
             g_tp->stream = st;
             g_tp->ops = new ErotOps(P, reg, st);
-            g_tp->vec.alloc(2 * ((size_t)P->n + P->m), st);
-            g_tp->vec.zero();
+            g_tp->vec.alloc(4 * ((size_t)n + m), st);
             g_tp->mx.alloc(1, st);
-            g_tp->mx.zero();
             sync(st);
         }
         ErotOps& ops = *g_tp->ops;
-        const int n = P->n;
-        PassParams p = ops.base_params();
+        if (g_tp->prepared_op != op) {
+            double* v = g_tp->vec.get();
+            k_time_pass_inputs<<<cdiv(4LL * (n + m), 256), 256, 0, st>>>(v, n, m, qrot);
+            count_launch();
+            REGOT_CHECK_LAUNCH();
+            ops.maxabs(v, n + m, nullptr, 0, g_tp->mx.get());
+            const size_t es = P->prec == REGOT_PREC_MIXED ? 4 : 8;
+            if ((op == OP_E_PLAN || op == OP_Q_PLAN) && !g_tp->plan.get())
+                g_tp->plan.alloc((size_t)n * m, st);
+            if ((op == OP_E_AVG || op == OP_Q_AVG) && !g_tp->xavg.get()) {
+                g_tp->xavg.alloc((size_t)n * m * es, st);
+                g_tp->xavg.zero();
+            }
+            if (op == OP_Q_GRADMASK && !g_tp->bitmask.get()) {
+                const PassShape sh = P->prec == REGOT_PREC_MIXED ? pass_shape<float>(n, m)
+                                                                 : pass_shape<double>(n, m);
+                const int lc = P->prec == REGOT_PREC_MIXED ? Geo<float>::LC : Geo<double>::LC;
+                g_tp->bitmask.alloc((size_t)n * sh.nslabs * lc, st);
+            }
+        }
         double* v = g_tp->vec.get();
+        PassParams p = ops.base_params();
         p.ra = v;
         p.cb = v + n;
-        p.rx = v + n + P->m;
-        p.cx = v + 2 * n + P->m;
+        p.rx = v + (n + m);
+        p.cx = v + (n + m) + n;
+        p.cx2 = v + 2 * (n + m) + n;
+        p.rd = v + 3 * (n + m);
+        p.cd = v + 3 * (n + m) + n;
         p.grid = g_tp->mx.get();
-        int op = OP_E_ROW;
-        if (kind == REGOT_PASS_EROT_COL) op = OP_E_COL;
-        if (kind == REGOT_PASS_EROT_GRAD) op = OP_E_ROWCOL;
-        if (kind == REGOT_PASS_EROT_HVP) op = OP_E_HVP;
-        if (kind == REGOT_PASS_QROT_GRAD) op = OP_Q_GRAD;
+        p.out = g_tp->plan.get();
+        p.xavg = g_tp->xavg.get();
+        p.bitmask = g_tp->bitmask.get();
+        if (op == OP_E_LS) {
+            const double s4[4] = {1.0, 0.5, 0.25, 0.1};
+            for (int k = 0; k < 4; ++k) p.steps[k] = s4[k];
+            p.nsteps = 4;
+        } else if (op == OP_E_GRADLS || op == OP_Q_GRADLS) {
+            p.steps[0] = 0.5;
+            p.nsteps = 1;
+        } else if (op == OP_E_AVG) {
+            p.steps[0] = 0.1;
+            p.nsteps = 1;  // X read and written (an APDAGD iteration after the first)
+        } else if (op == OP_Q_AVG) {
+            p.steps[0] = 0.9;
+            p.steps[1] = 0.1;
+            p.nsteps = 1;
+        }
         if (g_tp->prepared_op != op) {
             // split once (mixed), run the pass once, then time the dense
             // kernel alone on later calls

@@ -129,7 +129,18 @@ struct PassParams {
     void* xavg = nullptr;          // averaged plan (OP_E_AVG, OP_Q_AVG), TM, row-major, stride m
     const int* done = nullptr;     // early-exit flag (device)
     int* err = nullptr;            // set to 1 if a bounded wait gave up (device)
+    long long wait_limit = 0;      // polls before a wait gives up (filled by launch_pass)
 };
+
+// Polls (each suspended for up to 200 us) before a bounded wait on a copy
+// barrier gives up: a few seconds at most.
+constexpr long long kDefaultWaitSpins = 1LL << 14;
+// Current limit of the dense passes' bounded waits, and a setter that
+// returns the previous value (negative: back to kDefaultWaitSpins). A lower
+// limit makes the waits give up early; the tests use it to exercise the
+// timeout path without a fault.
+long long wait_limit();
+long long set_wait_limit(long long spins);
 
 struct PassShape {
     int nslabs, nrb, ntiles;

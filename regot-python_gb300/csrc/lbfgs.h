@@ -7,6 +7,31 @@
 // the defaults of LBFGSParam (Param.h:168-182). The driver runs on the host in
 // FP64; every function evaluation is one dense GPU pass (the caller's
 // callback). Vectors have n + m entries (QROT) or n + m - 1 (EROT).
+// The L-BFGS control flow, line search and error messages below follow
+// LBFGS++, which carries this notice:
+//
+//   Copyright (C) 2016-2026 Yixuan Qiu <yixuan.qiu@cos.name>
+//   Copyright (C) 2016-2026 Dirk Toewe <DirkToewe@GoogleMail.com>
+//   MIT License
+//
+//   Permission is hereby granted, free of charge, to any person obtaining a
+//   copy of this software and associated documentation files (the
+//   "Software"), to deal in the Software without restriction, including
+//   without limitation the rights to use, copy, modify, merge, publish,
+//   distribute, sublicense, and/or sell copies of the Software, and to
+//   permit persons to whom the Software is furnished to do so, subject to
+//   the following conditions:
+//
+//   The above copyright notice and this permission notice shall be included
+//   in all copies or substantial portions of the Software.
+//
+//   THE SOFTWARE IS PROVIDED "AS IS", WITHOUT WARRANTY OF ANY KIND, EXPRESS
+//   OR IMPLIED, INCLUDING BUT NOT LIMITED TO THE WARRANTIES OF
+//   MERCHANTABILITY, FITNESS FOR A PARTICULAR PURPOSE AND NONINFRINGEMENT.
+//   IN NO EVENT SHALL THE AUTHORS OR COPYRIGHT HOLDERS BE LIABLE FOR ANY
+//   CLAIM, DAMAGES OR OTHER LIABILITY, WHETHER IN AN ACTION OF CONTRACT,
+//   TORT OR OTHERWISE, ARISING FROM, OUT OF OR IN CONNECTION WITH THE
+//   SOFTWARE OR THE USE OR OTHER DEALINGS IN THE SOFTWARE.
 #pragma once
 
 #include <algorithm>

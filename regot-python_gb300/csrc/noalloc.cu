@@ -13,8 +13,15 @@
 // The caller passes device pointers for every input and output. All calls
 // share the array: calls that overlap on the GPU (on different streams, or
 // from different host threads) race on it and must be serialised by the
-// caller. Nothing in it has to start at zero: each call overwrites every
-// word it reads.
+// caller. The only word that has to start at zero, the pass's error word,
+// is cleared by each call before the pass; every other word is overwritten
+// before it is read.
+//
+// Errors on the GPU: the dense pass waits for its parameter copies with a
+// bounded wait. If one gives up, the pass sets the error word in the scratch
+// and the finishing kernels write NaN into grad and *obj, so the failure
+// shows in the outputs without a host synchronisation (the call itself has
+// already returned REGOT_OK by then).
 //
 // The first call on a device resolves the array's device address with
 // cudaGetSymbolAddress (with that device current); make that first call
@@ -28,7 +35,9 @@
 namespace regot {
 namespace {
 
-// 16 MiB: enough for n = m = 14000 (about 32 (n+m) + 4 n m (1/256 + 1/64) bytes).
+// 16 MiB. A problem needs about 32 (n + m) + 4 n m (1/512 + 1/64) bytes
+// (FP32 row partials per 512-column slab and column partials per 64-row
+// block): up to about n = m = 15400; n = m = 14000 always fits.
 constexpr size_t kNoallocScratchBytes = REGOT_NOALLOC_SCRATCH_BYTES;
 constexpr int kMaxDevices = 64;
 
@@ -57,8 +66,9 @@ size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 // Single block: bound on |alpha|, |beta~| (for the hi/lo grid), then the
 // FP32 split of alpha and of beta = (beta~, 0).
 __global__ void k_noalloc_split(const double* gamma, int n, int m, double* maxabs, float4* rs,
-                                float4* cs) {
+                                float4* cs, int* err) {
     __shared__ double s_max[32];
+    if (threadIdx.x == 0) *err = 0;
     double v = 0.0;
     for (int t = threadIdx.x; t < n + m - 1; t += blockDim.x) {
         const double x = gamma[t];
@@ -97,20 +107,24 @@ __global__ void k_noalloc_split(const double* gamma, int n, int m, double* maxab
 
 // Merge the pass partials: grad = [T 1 - a ; (T' 1 - b)_{j<m-1}], and per-block
 // partials of sum(T 1), gamma_a . a, gamma_b . b.
+// A pass whose bounded wait gave up (*err != 0) produced no valid partials:
+// grad is then NaN.
 __global__ void k_noalloc_grad(const float* rowpart, int nslabs, const float* colpart, int nrb,
                                int n, int m, const double* gamma, const double* a,
-                               const double* b, double* grad, double* blockpart) {
+                               const double* b, double* grad, double* blockpart,
+                               const int* err) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool failed = *err != 0;
     double v[3] = {0.0, 0.0, 0.0};
     if (t < n) {
         const double r = merge_strided(rowpart + t, nslabs, (size_t)n);
-        grad[t] = r - a[t];
+        grad[t] = failed ? NAN : r - a[t];
         v[0] = r;
         v[1] = gamma[t] * a[t];
     } else if (t < n + m - 1) {
         const int j = t - n;
         const double c = merge_strided(colpart + j, nrb, (size_t)m);
-        grad[t] = c - b[j];
+        grad[t] = failed ? NAN : c - b[j];
         v[2] = gamma[t] * b[j];
     }
     __shared__ double s[3][32];
@@ -129,8 +143,13 @@ __global__ void k_noalloc_grad(const float* rowpart, int nslabs, const float* co
 }
 
 // obj = reg * sum(T) - gamma_a . a - gamma_b . b~ (sinkhorn_problem_obj.cpp:389-390).
-__global__ void k_noalloc_obj(const double* blockpart, int nblocks, double reg, double* obj) {
+__global__ void k_noalloc_obj(const double* blockpart, int nblocks, double reg, double* obj,
+                              const int* err) {
     if (threadIdx.x != 0) return;
+    if (*err) {
+        *obj = NAN;
+        return;
+    }
     double s0 = 0.0, s1 = 0.0, s2 = 0.0;
     for (int k = 0; k < nblocks; ++k) {
         s0 += blockpart[(size_t)k * 3 + 0];
@@ -164,6 +183,8 @@ extern "C" int regot_erot_dual_obj_grad_noalloc(const float* M, long long ldm, i
         size_t off = 0;
         const size_t o_max = off;
         off = align256(off + sizeof(double));
+        const size_t o_err = off;
+        off = align256(off + sizeof(int));
         const size_t o_rs = off;
         off = align256(off + (size_t)n * sizeof(float4));
         const size_t o_cs = off;
@@ -184,8 +205,9 @@ extern "C" int regot_erot_dual_obj_grad_noalloc(const float* M, long long ldm, i
         float* rowpart = reinterpret_cast<float*>(base + o_row);
         float* colpart = reinterpret_cast<float*>(base + o_col);
         double* blk = reinterpret_cast<double*>(base + o_blk);
+        int* err = reinterpret_cast<int*>(base + o_err);
 
-        k_noalloc_split<<<1, 1024, 0, st>>>(gamma, n, m, maxabs, rs, cs);
+        k_noalloc_split<<<1, 1024, 0, st>>>(gamma, n, m, maxabs, rs, cs, err);
         REGOT_CHECK_LAUNCH();
         PassParams p;
         p.M = M;
@@ -198,11 +220,12 @@ extern "C" int regot_erot_dual_obj_grad_noalloc(const float* M, long long ldm, i
         p.csplit = cs;
         p.rowpart = rowpart;
         p.colpart = colpart;
+        p.err = err;
         launch_pass<float>(OP_E_ROWCOL, p, st);
         k_noalloc_grad<<<fin_blocks, fin_threads, 0, st>>>(rowpart, sh.nslabs, colpart, sh.nrb, n,
-                                                           m, gamma, a, b, grad, blk);
+                                                           m, gamma, a, b, grad, blk, err);
         REGOT_CHECK_LAUNCH();
-        k_noalloc_obj<<<1, 32, 0, st>>>(blk, fin_blocks, reg, obj);
+        k_noalloc_obj<<<1, 32, 0, st>>>(blk, fin_blocks, reg, obj, err);
         REGOT_CHECK_LAUNCH();
         return REGOT_OK;
     } catch (const Error& e) {

@@ -16,6 +16,7 @@
 //                  arg = ((rh + ch) - M_ij) + (rl + cl) has a hi sum that is
 //                  exact and an error relative to |arg| instead of |ra|+|cb|;
 //                  T = 2^(arg * log2(e)/reg) by ex2.approx.
+#include <atomic>
 #include <cfloat>
 #include <cmath>
 #include <type_traits>
@@ -29,13 +30,24 @@ thread_local long long* g_launch_counter = nullptr;
 int device_sm_count() {
     int dev = 0, count = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return 1;
-    static int cache[64] = {0};
-    if (dev < 64 && cache[dev]) return cache[dev];
+    static std::atomic<int> cache[64] = {};
+    if (dev < 64) {
+        const int c = cache[dev].load(std::memory_order_relaxed);
+        if (c) return c;
+    }
     if (cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
         count <= 0)
         count = 1;
-    if (dev < 64) cache[dev] = count;
+    if (dev < 64) cache[dev].store(count, std::memory_order_relaxed);
     return count;
+}
+
+namespace {
+std::atomic<long long> g_wait_limit{kDefaultWaitSpins};
+}
+long long wait_limit() { return g_wait_limit.load(std::memory_order_relaxed); }
+long long set_wait_limit(long long spins) {
+    return g_wait_limit.exchange(spins < 0 ? kDefaultWaitSpins : spins);
 }
 
 namespace {
@@ -83,13 +95,18 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
         ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar))
         : "memory");
 }
-// Bounded wait: gives up after kMaxSpins suspended polls (a few seconds at
-// most) and reports it through *err.
-constexpr long long kMaxSpins = 1LL << 14;
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* err) {
-    for (long long s = 0; s < kMaxSpins; ++s)
+// Bounded wait: gives up after `limit` suspended polls (kDefaultWaitSpins:
+// a few seconds at most) and reports it through *err. A wait that gave up
+// still drains the copy under the default limit before returning, so that
+// the buffer is not refilled, and the CTA does not exit, while the copy is
+// in flight; the caller treats the data as missing either way.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity, int* err,
+                                                  long long limit) {
+    for (long long s = 0; s < limit; ++s)
         if (mbar_try_wait(bar, parity)) return true;
     if (err) atomicOr(err, 1);
+    for (long long s = 0; s < kDefaultWaitSpins; ++s)
+        if (mbar_try_wait(bar, parity)) break;
     return false;
 }
 
@@ -465,7 +482,8 @@ __global__ void __launch_bounds__(kThreads, 2) dense_pass(const PassParams p) {
         const int seg = (int)((ldm - c0) < CW ? (ldm - c0) : CW);
 
         if constexpr (STAGE_PARAMS) {
-            const bool got = mbar_wait_bounded(&s_pbar[k & 1], (uint32_t)((k >> 1) & 1), p.err);
+            const bool got = mbar_wait_bounded(&s_pbar[k & 1], (uint32_t)((k >> 1) & 1), p.err,
+                                               p.wait_limit);
             ok_wait = ok_wait && got;
         }
         // ---- per-column parameters of this slab (only what OP uses) ----
@@ -905,13 +923,15 @@ void launch_one(const PassParams& p, cudaStream_t st) {
                             (size_t)(op_nc(OP) > 0 ? op_nc(OP) : 0) * (kWarps / 2) * CW * sizeof(Acc) +
                             2 * ((size_t)CW * 16 + (size_t)kRB * 16 +
                                  (op_uses_cd(OP) ? (size_t)CW * 4 : 0));
-    static unsigned long long configured = 0;  // per instantiation, one bit per device
+    // per instantiation, one bit per device; host threads may race to set
+    // the attribute, which is idempotent
+    static std::atomic<unsigned long long> configured{0};
     int dev = 0;
     REGOT_CUDA(cudaGetDevice(&dev));
-    if (dev >= 64 || !(configured & (1ULL << dev))) {
+    if (dev >= 64 || !(configured.load(std::memory_order_acquire) & (1ULL << dev))) {
         REGOT_CUDA(cudaFuncSetAttribute(dense_pass<TM, OP>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        if (dev < 64) configured |= (1ULL << dev);
+        if (dev < 64) configured.fetch_or(1ULL << dev, std::memory_order_acq_rel);
     }
     const PassShape s = pass_shape<TM>(p.n, p.m);
     const int blocks = pass_blocks(OP, std::is_same<TM, float>::value, p.n, p.m);
@@ -971,17 +991,20 @@ void launch_pass(int op, const PassParams& p, cudaStream_t st) {
     q.inv_reg_f = (float)(1.0 / p.reg);
     q.kexp_d = 1.0 / p.reg;
     q.inv_reg_d = 1.0 / p.reg;
+    q.wait_limit = wait_limit();
     Dispatch<TM>::template go<0>(op, q, st);
 }
 
 int pass_blocks(int op, bool mixed, int n, int m) {
     int dev = 0;
     REGOT_CUDA(cudaGetDevice(&dev));
-    static int cache[64][2][OP_COUNT] = {};
-    int occ = (dev < 64 && op >= 0 && op < OP_COUNT) ? cache[dev][mixed][op] : 0;
+    static std::atomic<int> cache[64][2][OP_COUNT] = {};
+    int occ = (dev < 64 && op >= 0 && op < OP_COUNT)
+                  ? cache[dev][mixed][op].load(std::memory_order_relaxed) : 0;
     if (!occ) {
         occ = mixed ? OccTable<float>::get<0>(op) : OccTable<double>::get<0>(op);
-        if (dev < 64 && op >= 0 && op < OP_COUNT) cache[dev][mixed][op] = occ;
+        if (dev < 64 && op >= 0 && op < OP_COUNT)
+            cache[dev][mixed][op].store(occ, std::memory_order_relaxed);
     }
     const PassShape s = mixed ? pass_shape<float>(n, m) : pass_shape<double>(n, m);
     const int cap = device_sm_count() * occ;

@@ -28,11 +28,21 @@ void sinkhorn_apdagd_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double t
 // is not NULL, the stored kept entries as a row-major n x (m - 1) 0/1 mask.
 void erot_sparsify_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, const double* gamma,
                        double delta, double density_hint, long long* nnz, int* mask);
-// Z = G Y, rows = G 1 with G = T or T o (u_i + u_j - W_ij) / reg (erot_grad.cu);
-// all pointers device: gamma and u n + m (last 0), W n x m, Y m x d, Z n x d.
-void erot_tyy_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, const double* d_gamma,
-                  const double* d_u, const double* d_W, const double* d_Y, int d, double* d_rows,
-                  double* d_Z);
+// Contraction of G = T or T o (u_i + u_j - W_ij) / reg (erot_grad.cu): rows
+// (cols = false) sums = G 1, Z = G Y with Y m x d, Z n x d; columns
+// (cols = true) sums = G'1, Z = G'Y with Y n x d, Z m x d. All pointers
+// device: gamma and u n + m (last 0), W n x m; Z and Y may be NULL when
+// d == 0. FP32 storage runs the tensor-core kernel (erot_tc.cu).
+void erot_contract_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, const double* d_gamma,
+                       const double* d_u, const double* d_W, const double* d_Y, int d, bool cols,
+                       double* d_sums, double* d_Z);
+// M = scale * squared Euclidean distances of the rows of x (n x d) and y
+// (m x d), row-major with stride ldm, FP32 or FP64 (fp64) throughout.
+void sqeuclid_gpu(const void* x, const void* y, int n, int m, int d, double scale, bool fp64,
+                  void* M, long long ldm, cudaStream_t st);
+void erot_contract_tc(regot_ctx* ctx, regot_dproblem* P, double reg, const double* d_gamma,
+                      const double* d_u, const double* d_W, const double* d_Y, int d, bool cols,
+                      double* d_sums, double* d_Z);
 // Batched BCD over point-cloud problems (erot_batch.cu).
 // cost, grad_x, grad_y (host, optional): each problem's regularised OT cost
 // and its gradients with respect to the points (FP32, like the points), at

@@ -432,28 +432,38 @@ class Problem:
         G = T o (u_i + u_j - W_ij) / reg when the adjoint u is given. numpy
         arguments run through host memory; float64 CUDA tensors (gamma, u,
         W, Y) stay on the device and the results are CUDA tensors."""
+        return self._contract(reg, gamma, Y, u, W, cols=False)
+
+    def erot_tty(self, reg, gamma, X, u=None, W=None):
+        """(cols, Z): cols = G'1 and Z = G'X (X n x d) for the same G as
+        erot_tyy."""
+        return self._contract(reg, gamma, X, u, W, cols=True)
+
+    def _contract(self, reg, gamma, Y, u, W, cols):
         n, m = self.n, self.m
+        K, nown = (n, m) if cols else (m, n)
+        fn = self._lib.regot_erot_tty if cols else self._lib.regot_erot_tyy
         if _is_torch_cuda(Y):
             import torch
 
             d = int(Y.shape[1])
-            _check_cuda_f64(Y, (m, d), "Y")
+            _check_cuda_f64(Y, (K, d), "Y")
             for name, t, shape in (("gamma", gamma, (n + m - 1,)), ("u", u, (n + m - 1,)),
                                    ("W", W, (n, m))):
                 if t is not None:
                     _check_cuda_f64(t, shape, name)
-            rows = torch.empty(n, dtype=torch.float64, device=Y.device)
-            Z = torch.empty((n, d), dtype=torch.float64, device=Y.device)
+            sums = torch.empty(nown, dtype=torch.float64, device=Y.device)
+            Z = torch.empty((nown, d), dtype=torch.float64, device=Y.device)
             torch.cuda.current_stream(Y.device).synchronize()
-            self.ctx.check(self._lib.regot_erot_tyy(
+            self.ctx.check(fn(
                 self.ctx.handle, self.handle, float(reg), gamma.data_ptr(),
                 u.data_ptr() if u is not None else None, W.data_ptr() if W is not None else None,
-                Y.data_ptr(), d, rows.data_ptr(), Z.data_ptr(), L.REGOT_MEM_DEVICE))
-            return rows, Z
+                Y.data_ptr(), d, sums.data_ptr(), Z.data_ptr(), L.REGOT_MEM_DEVICE))
+            return sums, Z
         gamma = self._vec(gamma, n + m - 1)
         Y = np.ascontiguousarray(np.asarray(Y, dtype=np.float64))
-        if Y.ndim != 2 or Y.shape[0] != m:
-            raise ValueError(f"Y must be a {m} x d matrix")
+        if Y.ndim != 2 or Y.shape[0] != K:
+            raise ValueError(f"the contracted matrix must be {K} x d")
         d = Y.shape[1]
         keep = []
         if u is not None:
@@ -464,13 +474,13 @@ class Problem:
             if W.shape != (n, m):
                 raise ValueError(f"W must be {n} x {m}")
             keep.append(W)
-        rows = np.zeros(n)
-        Z = np.zeros((n, d))
-        self.ctx.check(self._lib.regot_erot_tyy(
+        sums = np.zeros(nown)
+        Z = np.zeros((nown, d))
+        self.ctx.check(fn(
             self.ctx.handle, self.handle, float(reg), gamma.ctypes.data,
             u.ctypes.data if u is not None else None, W.ctypes.data if W is not None else None,
-            Y.ctypes.data, d, rows.ctypes.data, Z.ctypes.data, L.REGOT_MEM_HOST))
-        return rows, Z
+            Y.ctypes.data, d, sums.ctypes.data, Z.ctypes.data, L.REGOT_MEM_HOST))
+        return sums, Z
 
     def erot_sparsify(self, reg, gamma, delta, density_hint, mask=True):
         """sparsify_mat3 of T(gamma) (sinkhorn_sparsify3.cpp:276-405): returns

@@ -119,6 +119,19 @@ class BatchResult(C.Structure):
 
 BATCH_MAX_DIM = 16
 
+# Dense pass kinds of regot_time_pass / regot_pass_bytes (REGOT_PASS_*), with
+# the name of the kernel instance each one launches.
+PASS_KINDS = [
+    ("EROT_ROW", "OP_E_ROW"), ("EROT_COL", "OP_E_COL"), ("EROT_GRAD", "OP_E_ROWCOL"),
+    ("EROT_HVP", "OP_E_HVP"), ("QROT_GRAD", "OP_Q_GRAD"), ("EROT_LS", "OP_E_LS"),
+    ("EROT_GRADLS", "OP_E_GRADLS"), ("EROT_AVG", "OP_E_AVG"), ("EROT_PLAN", "OP_E_PLAN"),
+    ("EROT_ROWMAX", "OP_E_ROWMAX"), ("EROT_COLMAX", "OP_E_COLMAX"),
+    ("QROT_GRADMASK", "OP_Q_GRADMASK"), ("QROT_GRADLS", "OP_Q_GRADLS"), ("QROT_OBJ", "OP_Q_OBJ"),
+    ("QROT_P1", "OP_Q_P1"), ("QROT_P2", "OP_Q_P2"), ("QROT_P3", "OP_Q_P3"),
+    ("QROT_COLROOT", "OP_Q_COLROOT"), ("QROT_ROWROOT", "OP_Q_ROWROOT"), ("QROT_AVG", "OP_Q_AVG"),
+    ("QROT_PLAN", "OP_Q_PLAN"),
+]
+
 
 # Every symbol include/regot_gb300.h declares.
 EXPORTS = [
@@ -132,10 +145,11 @@ EXPORTS = [
     "regot_qrot_optimal_alpha", "regot_qrot_pdip", "regot_pdip_opts_init", "regot_erot_optimal_beta", "regot_erot_optimal_alpha", "regot_erot_dual_obj_grad",
     "regot_erot_hvp", "regot_erot_plan", "regot_erot_sparsify", "regot_erot_sparsify_density",
     "regot_erot_hess_solve",
-    "regot_erot_tyy", "regot_erot_solve_batched", "regot_erot_solve_batched_grad",
+    "regot_erot_tyy", "regot_erot_tty", "regot_sqeuclid_cost", "regot_erot_solve_batched", "regot_erot_solve_batched_grad",
     "regot_qrot_dual_obj_grad",
     "regot_qrot_optimal_beta",
-    "regot_qrot_primal_val", "regot_qrot_plan", "regot_time_pass",
+    "regot_qrot_primal_val", "regot_qrot_plan", "regot_time_pass", "regot_pass_bytes",
+    "regot_set_wait_limit",
     "regot_erot_dual_obj_grad_noalloc", "regot_host_alloc", "regot_host_free",
 ]
 
@@ -198,6 +212,10 @@ def load() -> C.CDLL:
         lib.regot_qrot_plan.argtypes = [vp, vp, C.c_double, vp, vp, C.c_int]
         lib.regot_qrot_optimal_alpha.argtypes = [vp, vp, C.c_double, vp, vp]
         lib.regot_time_pass.argtypes = [vp, vp, C.c_int, C.c_double, C.c_int]
+        lib.regot_pass_bytes.argtypes = [vp, C.c_int]
+        lib.regot_pass_bytes.restype = C.c_longlong
+        lib.regot_set_wait_limit.argtypes = [C.c_longlong]
+        lib.regot_set_wait_limit.restype = C.c_longlong
         lib.regot_erot_solve_batched.argtypes = [vp, C.POINTER(BatchDesc), C.c_double,
                                                  C.c_double, C.c_int, C.POINTER(BatchResult)]
         lib.regot_erot_solve_batched_grad.argtypes = [vp, C.POINTER(BatchDesc), C.c_double,
@@ -207,6 +225,10 @@ def load() -> C.CDLL:
                                               vp, C.POINTER(C.c_int)]
         lib.regot_erot_tyy.argtypes = [vp, vp, C.c_double, vp, vp, vp, vp, C.c_int, vp, vp,
                                        C.c_int]
+        lib.regot_erot_tty.argtypes = [vp, vp, C.c_double, vp, vp, vp, vp, C.c_int, vp, vp,
+                                       C.c_int]
+        lib.regot_sqeuclid_cost.argtypes = [vp, vp, vp, C.c_int, C.c_int, C.c_int, C.c_double,
+                                            C.c_int, vp, C.c_longlong]
         lib.regot_erot_dual_obj_grad_noalloc.argtypes = [
             vp, C.c_longlong, C.c_int, C.c_int, vp, vp, vp, C.c_double, vp, vp, vp]
         lib.regot_host_alloc.argtypes = [C.c_size_t, C.POINTER(vp)]

@@ -13,13 +13,18 @@ ot_plan(M, a, b, reg)      the optimal plan T*; the backward of a loss on it is
                            passes), dL/dM_ij = T_ij (u_i + u_j - W_ij) / reg,
                            dL/da = u_alpha, dL/db = (u_beta~, 0), W = dL/dT.
 sqeuclid_ot_cost(x, y, a, b, reg, scale)
-                           ot_cost with M_ij = |x_i - y_j|^2 / scale; the
-                           backward dL/dx = 2 g (r o x - T y) / scale runs the
-                           fused contraction regot_erot_tyy (no n x m array).
+                           ot_cost with M_ij = |x_i - y_j|^2 / scale (formed by
+                           the library's direct-difference kernel); the
+                           backward dL/dx = 2 g (r o x - T y) / scale and
+                           dL/dy = 2 g (c o y - T'x) / scale run the fused
+                           contractions regot_erot_tyy / regot_erot_tty (no
+                           n x m array; tensor cores for float32 points).
 sqeuclid_plan_loss(x, y, a, b, reg, W, scale)
                            <T*, W> for that cost; dL/dx = 2 g (rG o x - G y) /
-                           scale with G = dL/dM of ot_plan, again through
-                           regot_erot_tyy with the adjoint u and W.
+                           scale and dL/dy likewise with G = dL/dM of ot_plan,
+                           through the same contractions with the adjoint u
+                           and W; the loss and the adjoint right-hand side are
+                           contractions too.
 
 The solve runs on the GPU of the inputs through regot.Problem (float32 M:
 mixed precision; float64: FP64). Forward tolerances are the caller's; the
@@ -61,10 +66,9 @@ def _center(v):
 
 
 def _dual_tensors(prob, gamma, device):
-    n, m = prob.n, prob.m
-    alpha = torch.from_numpy(gamma[:n].copy()).to(device)
-    beta = torch.from_numpy(np.r_[gamma[n:], 0.0]).to(device)
-    return alpha, beta
+    n = prob.n
+    g = torch.from_numpy(np.r_[gamma, 0.0]).to(device)  # beta_m = 0 appended
+    return g[:n], g[n:]
 
 
 class _OTCost(torch.autograd.Function):
@@ -138,16 +142,39 @@ class _OTPlan(torch.autograd.Function):
 
 
 def _sqeuclid(x, y, scale):
-    return ((x * x).sum(1)[:, None] + (y * y).sum(1)[None, :] - 2.0 * x @ y.T).clamp_min(0) / scale
+    """M_ij = |x_i - y_j|^2 / scale by the library's direct-difference kernel
+    (regot_sqeuclid_cost) in the points' precision (float32 or float64)."""
+    import ctypes as C
+
+    dt = torch.float64 if x.dtype == torch.float64 else torch.float32
+    xd = x.detach().to(dt).contiguous()
+    yd = y.detach().to(dt).contiguous()
+    n, d = xd.shape
+    m = yd.shape[0]
+    if yd.shape[1] != d:
+        raise ValueError("x and y must have the same number of columns")
+    M = torch.empty((n, m), dtype=dt, device=x.device)
+    ctx = I.L.context(x.device.index or 0)
+    torch.cuda.current_stream(x.device).synchronize()
+    ctx.check(ctx._lib.regot_sqeuclid_cost(
+        ctx.handle, C.c_void_p(xd.data_ptr()), C.c_void_p(yd.data_ptr()), n, m, d,
+        1.0 / float(scale), I.L.REGOT_F64 if dt == torch.float64 else I.L.REGOT_F32,
+        C.c_void_p(M.data_ptr()), m))
+    return M
+
+
+def _gamma_tensor(gamma, device):
+    return torch.from_numpy(np.ascontiguousarray(gamma)).to(device)
 
 
 class _SqEuclidCost(torch.autograd.Function):
     @staticmethod
     def forward(ctx, x, y, a, b, reg, scale, solver, tol, max_iter, kwargs):
-        with torch.no_grad():
-            M = _sqeuclid(x, y, scale)
+        M = _sqeuclid(x, y, scale)
         prob, r = _solve(M, a, b, reg, solver, tol, max_iter, dict(kwargs))
+        del M
         ctx.prob, ctx.gamma, ctx.reg, ctx.scale = prob, r.dual, reg, scale
+        ctx.gam = _gamma_tensor(r.dual, x.device)
         ctx.save_for_backward(x, y)
         ctx.dtypes = (x.dtype, y.dtype, a.dtype, b.dtype)
         return torch.tensor(-r.obj_vals[-1], dtype=torch.float64, device=x.device)
@@ -157,18 +184,16 @@ class _SqEuclidCost(torch.autograd.Function):
         x, y = ctx.saved_tensors
         prob, gamma, reg, scale = ctx.prob, ctx.gamma, ctx.reg, ctx.scale
         dx = dy = da = db = None
+        xd = x.detach().to(torch.float64).contiguous()
+        yd = y.detach().to(torch.float64).contiguous()
         if ctx.needs_input_grad[0]:
-            gam = torch.from_numpy(gamma).to(x.device)
-            Y = y.detach().to(torch.float64).contiguous()
-            rows, TY = prob.erot_tyy(reg, gam, Y)
-            xd = x.detach().to(torch.float64)
+            # dL/dx = 2 (rows o x - T y) / scale, T y on the tensor cores (FP32 storage)
+            rows, TY = prob.erot_tyy(reg, ctx.gam, yd)
             dx = (g * 2.0 * (rows[:, None] * xd - TY) / scale).to(ctx.dtypes[0])
         if ctx.needs_input_grad[1]:
-            T = torch.empty((prob.n, prob.m), dtype=torch.float64, device=y.device)
-            prob.erot_plan(reg, gamma, out=T)
-            yd = y.detach().to(torch.float64)
-            xd = x.detach().to(torch.float64)
-            dy = (g * 2.0 * (T.sum(0)[:, None] * yd - T.T @ xd) / scale).to(ctx.dtypes[1])
+            # dL/dy = 2 (cols o y - T'x) / scale, the column-side contraction
+            cols, TX = prob.erot_tty(reg, ctx.gam, xd)
+            dy = (g * 2.0 * (cols[:, None] * yd - TX) / scale).to(ctx.dtypes[1])
         alpha, beta = _dual_tensors(prob, gamma, x.device)
         if ctx.needs_input_grad[2]:
             da = (g * _center(alpha)).to(ctx.dtypes[2])
@@ -180,39 +205,47 @@ class _SqEuclidCost(torch.autograd.Function):
 class _SqEuclidPlanLoss(torch.autograd.Function):
     @staticmethod
     def forward(ctx, x, y, a, b, reg, W, scale, solver, tol, max_iter, cg_tol, kwargs):
-        with torch.no_grad():
-            M = _sqeuclid(x, y, scale)
+        M = _sqeuclid(x, y, scale)
         prob, r = _solve(M, a, b, reg, solver, tol, max_iter, dict(kwargs))
-        T = torch.empty((prob.n, prob.m), dtype=torch.float64, device=x.device)
-        prob.erot_plan(reg, r.dual, out=T)
+        del M
+        n, m = prob.n, prob.m
         W64 = W.detach().to(torch.float64).contiguous()
+        gam = _gamma_tensor(r.dual, x.device)
+        zero = torch.zeros(n + m - 1, dtype=torch.float64, device=x.device)
+        # with u = 0 the contraction's G is -W o T / reg: its row and column
+        # sums give the loss sum W o T and the adjoint right-hand side
+        # dL/dgamma = (rows, cols~) of W o T / reg, without an n x m array
+        e0 = torch.empty((n, 0), dtype=torch.float64, device=x.device)
+        e1 = torch.empty((m, 0), dtype=torch.float64, device=x.device)
+        rows0, _ = prob.erot_tyy(reg, gam, e1, u=zero, W=W64)
+        cols0, _ = prob.erot_tty(reg, gam, e0, u=zero, W=W64)
         ctx.prob, ctx.gamma, ctx.reg, ctx.scale, ctx.cg_tol = prob, r.dual, reg, scale, cg_tol
-        ctx.save_for_backward(x, y, T, W64)
+        ctx.gam = gam
+        ctx.dgamma = -torch.cat([rows0, cols0[: m - 1]])
+        ctx.save_for_backward(x, y, W64)
         ctx.dtypes = (x.dtype, y.dtype, a.dtype, b.dtype)
-        return (W64 * T).sum()
+        return -reg * rows0.sum()
 
     @staticmethod
     def backward(ctx, g):
-        x, y, T, W = ctx.saved_tensors
+        x, y, W = ctx.saved_tensors
         prob, gamma, reg, scale = ctx.prob, ctx.gamma, ctx.reg, ctx.scale
         n, m = prob.n, prob.m
-        u = _adjoint(prob, gamma, reg, T, W, ctx.cg_tol)
+        u, _ = prob.erot_hess_solve(reg, gamma, ctx.dgamma.cpu().numpy(),
+                                    tol=_cg_tol(prob, ctx.cg_tol))
+        ut = torch.from_numpy(u).to(x.device)
+        xd = x.detach().to(torch.float64).contiguous()
+        yd = y.detach().to(torch.float64).contiguous()
         dx = dy = da = db = None
+        # G = T o (u_i + u_j - W_ij) / reg contracted on the fly (no n x m array)
         if ctx.needs_input_grad[0]:
-            # G = T o (u_i + u_j - W_ij) / reg contracted with y on the fly
-            gam = torch.from_numpy(gamma).to(x.device)
-            ut = torch.from_numpy(u).to(x.device)
-            Y = y.detach().to(torch.float64).contiguous()
-            rows, GY = prob.erot_tyy(reg, gam, Y, u=ut, W=W)
-            xd = x.detach().to(torch.float64)
+            rows, GY = prob.erot_tyy(reg, ctx.gam, yd, u=ut, W=W)
             dx = (g * 2.0 * (rows[:, None] * xd - GY) / scale).to(ctx.dtypes[0])
-        ua = torch.from_numpy(u[:n].copy()).to(x.device)
-        ub = torch.from_numpy(np.r_[u[n:], 0.0]).to(x.device)
         if ctx.needs_input_grad[1]:
-            G = T / reg * (ua[:, None] + ub[None, :] - W)
-            yd = y.detach().to(torch.float64)
-            xd = x.detach().to(torch.float64)
-            dy = (g * 2.0 * (G.sum(0)[:, None] * yd - G.T @ xd) / scale).to(ctx.dtypes[1])
+            cols, GX = prob.erot_tty(reg, ctx.gam, xd, u=ut, W=W)
+            dy = (g * 2.0 * (cols[:, None] * yd - GX) / scale).to(ctx.dtypes[1])
+        ua = ut[:n]
+        ub = torch.cat([ut[n:], ut.new_zeros(1)])
         if ctx.needs_input_grad[2]:
             da = (g * ua).to(ctx.dtypes[2])
         if ctx.needs_input_grad[3]:
