@@ -50,13 +50,14 @@ TOL = 1e-6
 MAX_ITER = 1000
 
 
-def workload_config(n):
+def workload_config(n, world=1):
     return {"workload": f"large dense EROT n=m={n}, sqeuclid/max of 3-D Gaussian clouds "
                         f"(seed 0), FP32 M, FP64 duals, reg={REG}, tol={TOL}",
             "solver": "sinkhorn_bcd", "n": n, "m": n, "reg": REG, "tol": TOL,
             "precision": "mixed", "l2": "M (4*n*m bytes) larger than L2; no flush needed",
             "value": "device-resident solve, duals only",
-            "e2e": "regot.sinkhorn_bcd on pinned host M incl. upload, plan and D2H"}
+            "e2e": "regot.sinkhorn_bcd on pinned host M incl. upload, plan and D2H",
+            "parallelism": f"replicas x{world}"}
 
 
 def max_over_ranks(x, dist=None, device="cpu"):
@@ -144,16 +145,16 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def profiled_traffic():
-    """DRAM bytes per launch of the row pass from the committed ncu summary."""
-    path = os.path.join(REPO, "profiles", "dense_pass_erot_row_8192.md")
+def profiled_traffic(kernel):
+    """DRAM bytes per launch of `kernel` at n = m = 8192 from the committed
+    ncu figures (profiles/dense_pass_dram_traffic.json), or None."""
+    path = os.path.join(REPO, "profiles", "dense_pass_dram_traffic.json")
     try:
-        for line in open(path):
-            if line.startswith("traffic_bytes_per_launch:"):
-                return int(line.split(":")[1].strip())
-    except OSError:
-        pass
-    return None
+        with open(path) as f:
+            v = json.load(f).get(kernel)
+        return int(v) if v is not None else None
+    except (OSError, ValueError):
+        return None
 
 
 def cpu_solve_sample(M64, a, b, iters):
@@ -171,6 +172,12 @@ def cpu_solve_sample(M64, a, b, iters):
 
 
 def run_reference(args, n):
+    """The reference arm: the FP64 oracle restatement of sinkhorn_bcd (the
+    reference itself cannot be built here) on the same problem, on one host
+    core like the reference's BCD (no OpenMP on that path). Each timed step
+    is one full measured solve to tolerance; at about 18 s a solve, the run
+    times min(steps, 3) of them. Warm-up steps are bounded samples (the
+    initial value and one iteration)."""
     rank, world, _ = rank_env()
     if rank != 0:
         return
@@ -180,26 +187,27 @@ def run_reference(args, n):
 
     M, a, b = erot_points(n, n, seed=0, dtype=np.float32)
     M64 = np.asfortranarray(M.astype(np.float64))
-    t = time.perf_counter()
-    full = O.sinkhorn_bcd(M64, a, b, REG, tol=TOL, max_iter=MAX_ITER, plan=False)
-    full_ms = (time.perf_counter() - t) * 1e3
-    niter = full.niter
-    samples = []
-    for step in range(args.warmup + args.steps):
-        t_init, t_iter = cpu_solve_sample(M64, a, b, 1)
-        if step >= args.warmup:
-            samples.append(t_init + niter * t_iter)
+    for _ in range(args.warmup):
+        cpu_solve_sample(M64, a, b, 1)
+    steps = max(1, min(args.steps, 3))
+    samples, niter, mar = [], None, None
+    for _ in range(steps):
+        t = time.perf_counter()
+        full = O.sinkhorn_bcd(M64, a, b, REG, tol=TOL, max_iter=MAX_ITER, plan=False)
+        samples.append((time.perf_counter() - t) * 1e3)
+        niter, mar = full.niter, full.mar_errs[-1]
     value = statistics.median(samples)
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "impl": "reference",
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "n_gpus": args.gpus, "steps": steps, "warmup": args.warmup,
         "ms_per_step": round(value, 3), "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": workload_config(n),
         "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": 1, "kind": "port",
-                         "sample": f"FP64 oracle restatement of sinkhorn_bcd (single-threaded "
-                                   f"like the reference): init + 1 iteration per step, "
-                                   f"extrapolated to the {niter} iterations of one full oracle "
-                                   f"solve ({full_ms:.0f} ms wall)"},
+                         "sample": f"FP64 oracle restatement of sinkhorn_bcd, single-threaded "
+                                   f"like the reference's BCD: {steps} full solves to "
+                                   f"mar_err <= {TOL} measured ({niter} iterations, final "
+                                   f"mar_err {mar:.3e}), median; warm-up steps are the "
+                                   f"initial value plus one iteration"},
         "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
@@ -209,8 +217,9 @@ def run_reference(args, n):
 def batched_workload(count=512, seed=2):
     """Batched uneven EROT: n, m log-uniform in [64, 2048], d uniform in
     {2..16}, x ~ N(0, I_d), y ~ N(mu, I_d) with mu ~ N(0, 0.25 I_d), uniform
-    marginals; cost |x - y|^2 / d computed on the fly (the 1/d keeps costs
-    O(1): unscaled costs need tens of thousands of sweeps at reg 0.05)."""
+    marginals; squared-Euclidean costs computed on the fly. Returns the
+    points, marginals and the per-problem 1/d cost scales (used by the
+    scaled variant of the workload)."""
     rng = np.random.default_rng(seed)
     xs, ys, as_, bs, sc = [], [], [], [], []
     for _ in range(count):
@@ -225,84 +234,115 @@ def batched_workload(count=512, seed=2):
     return xs, ys, as_, bs, sc
 
 
-def run_batched(args):
-    """One JSON line for the batched workload: solves/s of the batched BCD
-    against the plain FP64 single-problem solver (sinkhorn_bcd on each
-    problem's FP64 cost matrix, timed on a sample of the problems)."""
+def batched_measure(steps, warmup, scaled, max_iter, sample_stride=32):
+    """Solves/s of the batched BCD (forward, and forward + backward in the
+    same call) against the plain FP64 single-problem solver on the same
+    problems: regot.Problem (FP64 M built before the timed region, resident
+    on the device), sinkhorn_bcd's device time, plus, for forward + backward,
+    the cost and both point gradients through the FP64 contractions
+    (erot_tyy / erot_tty), timed with CUDA events on the library's stream.
+    The plain solver is timed on every `sample_stride`-th problem."""
     import torch
 
     import regot
+    from regot import _lib
 
     reg, tol = 0.05, 1e-6
     xs, ys, as_, bs, sc = batched_workload()
+    if not scaled:
+        sc = [1.0] * len(sc)
     P = len(xs)
-    solve = lambda: regot.sinkhorn_bcd_batched(xs, ys, as_, bs, reg, tol=tol,  # noqa: E731
-                                               max_iter=20000, cost_scale=sc)
-    for _ in range(args.warmup):
-        r = solve()
-    torch.cuda.synchronize()
-    dev_ms, wall_ms = [], []
-    for _ in range(args.steps):
-        t = time.perf_counter()
-        r = solve()
-        wall_ms.append((time.perf_counter() - t) * 1e3)
-        dev_ms.append(r.solve_ms)
-    elems = sum(2 * (int(k) + 1) * x.shape[0] * y.shape[0] for k, x, y in zip(r.niter, xs, ys))
-    # forward + backward: the same solves with each problem's cost and point
-    # gradients computed in the same call
-    solve_fb = lambda: regot.sinkhorn_bcd_batched(xs, ys, as_, bs, reg, tol=tol,  # noqa: E731
-                                                  max_iter=20000, cost_scale=sc, grad=True)
-    for _ in range(args.warmup):
-        solve_fb()
-    torch.cuda.synchronize()
-    fb_dev, fb_wall = [], []
-    for _ in range(args.steps):
-        t = time.perf_counter()
-        rf = solve_fb()
-        fb_wall.append((time.perf_counter() - t) * 1e3)
-        fb_dev.append(rf.solve_ms)
-    sample = list(range(0, P, 32))
-    t = time.perf_counter()
-    for p in sample:
-        x = xs[p].astype(np.float64)
-        y = ys[p].astype(np.float64)
-        M = sc[p] * ((x[:, None, :] - y[None, :, :]) ** 2).sum(-1)
-        regot.sinkhorn_bcd(M, as_[p], bs[p], reg, tol=tol, max_iter=20000, precision="fp64",
-                           plan=False)
-    plain_s = (time.perf_counter() - t) / len(sample)
-    dev = statistics.median(dev_ms)
-    wall = statistics.median(wall_ms)
-    line = {
-        "metric": "batched EROT solves/s (512 uneven problems, tol 1e-6)",
-        "value": round(P / (dev * 1e-3), 1), "unit": "solves/s", "n_gpus": 1,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dev, 3),
-        "higher_is_better": True, "dtype": "f32 cost, f64 duals", "data": "synthetic",
-        "config": {"workload": "512 problems, n, m log-uniform in [64, 2048], d in 2..16, "
-                               "cost |x - y|^2 / d on the fly, reg 0.05, tol 1e-6, seed 2",
-                   "solver": "sinkhorn_bcd_batched"},
-        "e2e": {"value": round(P / (wall * 1e-3), 1), "unit": "solves/s",
-                "h2d_bytes_per_step": int(sum(x.nbytes + y.nbytes for x, y in zip(xs, ys))
-                                          + sum(a.nbytes + b.nbytes for a, b in zip(as_, bs))),
-                "d2h_bytes_per_step": int(sum(a.nbytes + b.nbytes for a, b in zip(as_, bs)))},
+    solve = lambda grad: regot.sinkhorn_bcd_batched(xs, ys, as_, bs, reg, tol=tol,  # noqa: E731
+                                                    max_iter=max_iter, cost_scale=sc, grad=grad)
+    out = {}
+    for grad in (False, True):
+        for _ in range(warmup):
+            r = solve(grad)
+        torch.cuda.synchronize()
+        dev, wall = [], []
+        for _ in range(steps):
+            t = time.perf_counter()
+            r = solve(grad)
+            wall.append((time.perf_counter() - t) * 1e3)
+            dev.append(r.solve_ms)
+        out[grad] = (statistics.median(dev), statistics.median(wall), r)
+    r = out[False][2]
+    # plain FP64 single-problem solver, forward and backward, device time
+    ctx = _lib.context(0)
+    stream = torch.cuda.Stream()
+    ctx.set_stream(stream.cuda_stream)
+    sample = list(range(0, P, sample_stride))
+    fwd_ms, bwd_ms, plain_niter, plain_conv = [], [], [], 0
+    with torch.cuda.stream(stream):
+        for p in sample:
+            x = xs[p].astype(np.float64)
+            y = ys[p].astype(np.float64)
+            M = sc[p] * ((x[:, None, :] - y[None, :, :]) ** 2).sum(-1)
+            prob = regot.Problem(M, as_[p], bs[p], precision="fp64")
+            xd = torch.from_numpy(x).cuda()
+            yd = torch.from_numpy(y).cuda()
+            torch.cuda.synchronize()
+            rp = prob.sinkhorn_bcd(reg, tol=tol, max_iter=max_iter, plan=False)
+            fwd_ms.append(rp.solve_ms)
+            plain_niter.append(rp.niter)
+            plain_conv += int(rp.mar_errs[-1] < tol)
+            gam = torch.from_numpy(rp.dual).cuda()
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            prob.erot_tyy(reg, gam, yd)
+            prob.erot_tty(reg, gam, xd)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            bwd_ms.append(e0.elapsed_time(e1))
+            prob.close()
+    ctx.set_stream(None)
+    plain_fwd = statistics.mean(fwd_ms)
+    plain_fb = statistics.mean(f + b for f, b in zip(fwd_ms, bwd_ms))
+    dev, wall = out[False][0], out[False][1]
+    fb_dev, fb_wall = out[True][0], out[True][1]
+    conv = int((np.asarray(r.mar_errs) < tol).sum())
+    h2d = int(sum(x.nbytes + y.nbytes for x, y in zip(xs, ys))
+              + sum(a.nbytes + b.nbytes for a, b in zip(as_, bs)))
+    d2h = int(sum(a.nbytes + b.nbytes for a, b in zip(as_, bs)))
+    return {
+        "workload": f"{P} problems, n, m log-uniform in [64, 2048], d in 2..16, cost "
+                    + ("|x - y|^2 / d" if scaled else "|x - y|^2 (unscaled)")
+                    + f" on the fly, reg {reg}, tol {tol}, max_iter {max_iter}, seed 2",
+        "fwd": {"solves_per_s": round(P / (dev * 1e-3), 1), "ms": round(dev, 3),
+                "e2e_solves_per_s": round(P / (wall * 1e-3), 1)},
+        "fwd_bwd": {"solves_per_s": round(P / (fb_dev * 1e-3), 1), "ms": round(fb_dev, 3),
+                    "e2e_solves_per_s": round(P / (fb_wall * 1e-3), 1),
+                    "what": "cost a'alpha + b'beta - reg sum T and dL/dx, dL/dy per problem "
+                            "in the same call as the solve"},
         "sweeps": int(r.sweeps), "niter_median": float(np.median(r.niter)),
-        "niter_max": int(r.niter.max()), "max_final_mar_err": float(r.mar_errs.max()),
-        "element_evaluations_per_s": round(elems / (dev * 1e-3), 1),
-        "plain_fp64_single_problem": {"s_per_problem": round(plain_s, 5),
-                                      "sample": f"{len(sample)} of the {P} problems",
-                                      "solves_per_s": round(1.0 / plain_s, 2)},
-        "batched_vs_plain": round((P / (dev * 1e-3)) * plain_s, 1),
-        "fwd_bwd": {
-            "value": round(P / (statistics.median(fb_dev) * 1e-3), 1), "unit": "solves/s",
-            "ms_per_step": round(statistics.median(fb_dev), 3),
-            "backward_ms": round(statistics.median(fb_dev) - dev, 3),
-            "e2e": round(P / (statistics.median(fb_wall) * 1e-3), 1),
-            "d2h_bytes_per_step": int(sum(a.nbytes + b.nbytes for a, b in zip(as_, bs))
-                                      + sum(x.nbytes + y.nbytes for x, y in zip(xs, ys))
-                                      + 8 * P),
-            "what": "cost a'alpha + b'beta - reg sum T and dL/dx, dL/dy per problem "
-                    "in the same call as the solve"},
+        "niter_max": int(np.max(r.niter)), "converged": conv, "problems": P,
+        "max_final_mar_err": float(np.max(r.mar_errs)),
+        "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+        "plain_fp64_single_problem": {
+            "sample": f"{len(sample)} of the {P} problems, resident FP64 problems, device time",
+            "fwd_ms_per_problem": round(plain_fwd, 3),
+            "fwd_bwd_ms_per_problem": round(plain_fb, 3),
+            "fwd_solves_per_s": round(1e3 / plain_fwd, 2),
+            "fwd_bwd_solves_per_s": round(1e3 / plain_fb, 2),
+            "niter_median": float(np.median(plain_niter)), "converged": plain_conv},
+        "batched_vs_plain_fwd": round((P / (dev * 1e-3)) / (1e3 / plain_fwd), 1),
+        "batched_vs_plain_fwd_bwd": round((P / (fb_dev * 1e-3)) / (1e3 / plain_fb), 1),
     }
-    print(json.dumps(line))
+
+
+def run_batched(args):
+    """One JSON line per variant of the batched workload: the cost as the
+    workload states it (|x - y|^2) and the 1/d-scaled one."""
+    for scaled, max_iter in ((False, args.batched_max_iter), (True, 20000)):
+        res = batched_measure(args.steps, args.warmup, scaled, max_iter)
+        line = {"metric": "batched EROT fwd+bwd solves/s vs plain FP64 single-problem",
+                "value": res["fwd_bwd"]["solves_per_s"], "unit": "solves/s", "n_gpus": 1,
+                "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": res["fwd_bwd"]["ms"], "higher_is_better": True,
+                "dtype": "f32 cost, f64 duals", "data": "synthetic", **res}
+        print(json.dumps(line), flush=True)
 
 
 def solver_problems(seed=3):
@@ -488,10 +528,19 @@ def run_passes(args):
     torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
     out = {}
+    lib = _lib.load()
     for prec in ("mixed", "fp64"):
+        code = _lib.REGOT_PREC_MIXED if prec == "mixed" else _lib.REGOT_PREC_FP64
+        tables = {}
         prob = regot.Problem(M, a, b, precision=prec)
-        out[prec] = pass_table(ctx, prob, REG)
+        for label, cfg in (("config0", 0), ("config1", 1)):
+            lib.regot_force_pass_config(cfg)
+            tables[label] = pass_table(ctx, prob, REG)
+        lib.regot_force_pass_config(-1)
+        ctx.check(lib.regot_autotune(ctx.handle, n, n, code, 10))
+        tables["tuned"] = pass_table(ctx, prob, REG)
         prob.close()
+        out[prec] = tables
     peak, src = measured_peaks()
     print(json.dumps({"workload": "dense passes", "n": n, "m": n, "reg": REG,
                       "peak_gbs": peak, "peak_source": src, "passes": out}), flush=True)
@@ -586,6 +635,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--headline-only", action="store_true",
+                    help="skip the nested measurements (plain FP64, solvers, batched)")
+    ap.add_argument("--batched-max-iter", type=int, default=20000,
+                    help="iteration cap of the unscaled batched workload")
     ap.add_argument("--ncu-case", action="store_true",
                     help="a few passes for an ncu capture (no timing, no JSON)")
     ap.add_argument("--workload", choices=["bcd", "batched", "solvers", "autograd", "passes"],
@@ -668,60 +721,97 @@ def main():
     torch.cuda.set_stream(stream)
     ctx.set_stream(stream.cuda_stream)
 
+    # ---- the autotuner: launch configuration of every dense pass at this
+    # size (timed on a synthetic problem of the size; untimed here) ----
+    lib = _lib.load()
+    t_tune = time.perf_counter()
+    ctx.check(lib.regot_autotune(ctx.handle, n, n, _lib.REGOT_PREC_MIXED, 10))
+    tune_s = time.perf_counter() - t_tune
+    tuned = {}
+    for kind, (name, _op) in enumerate(_lib.PASS_KINDS):
+        tuned[name] = int(lib.regot_pass_config(ctx.handle, kind, _lib.REGOT_PREC_MIXED, n, n))
+
     # ---- device-resident value ----
     prob = regot.Problem(M, a, b, precision="mixed", device=local)
     for _ in range(args.warmup):
         r = prob.sinkhorn_bcd(REG, tol=TOL, max_iter=MAX_ITER, plan=False)
-    launches0 = ctx.kernel_launches()
     if dist:
         dist.barrier()
     torch.cuda.synchronize(dev)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
+        # keep the GPU loaded for about 1.5 s before the timed steps, so that
+        # the clock samples cover a loaded, steady state
+        t_load = time.perf_counter()
+        while time.perf_counter() - t_load < 1.5:
+            prob.sinkhorn_bcd(REG, tol=TOL, max_iter=MAX_ITER, plan=False)
+        torch.cuda.synchronize(dev)
+        if dist:
+            dist.barrier()
+        launches0 = ctx.kernel_launches()
         e0.record(stream)
         for _ in range(args.steps):
             r = prob.sinkhorn_bcd(REG, tol=TOL, max_iter=MAX_ITER, plan=False)
         e1.record(stream)
         torch.cuda.synchronize(dev)
+        launches = ctx.kernel_launches() - launches0
     if dist:
         dist.barrier()
-    launches = ctx.kernel_launches() - launches0
     elapsed = max_over_ranks(e0.elapsed_time(e1), dist, dev)
     ms_per_step = elapsed / args.steps
     value = elapsed / (args.steps * world)
     niter, mar = r.niter, r.mar_errs[-1]
 
-    # ---- roofline of the dominant kernel (row / column LSE pass) ----
-    reps = 20
-    torch.cuda.synchronize(dev)
-    k0 = torch.cuda.Event(enable_timing=True)
-    k1 = torch.cuda.Event(enable_timing=True)
-    _lib.load().regot_time_pass(ctx.handle, prob.handle, 0, REG, 1)  # warm
-    torch.cuda.synchronize(dev)
-    k0.record(stream)
-    ctx.check(_lib.load().regot_time_pass(ctx.handle, prob.handle, 0, REG, reps))
-    k1.record(stream)
-    torch.cuda.synchronize(dev)
-    row_ms = k0.elapsed_time(k1) / reps
-    _lib.load().regot_time_pass(ctx.handle, prob.handle, 1, REG, 1)  # warm, prepares the split
-    torch.cuda.synchronize(dev)
-    k0.record(stream)
-    ctx.check(_lib.load().regot_time_pass(ctx.handle, prob.handle, 1, REG, reps))
-    k1.record(stream)
-    torch.cuda.synchronize(dev)
-    col_ms = k0.elapsed_time(k1) / reps
-    alg_bytes = 4 * n * n
-    achieved = alg_bytes / (row_ms * 1e-3) / 1e9
+    # ---- roofline of the dominant kernel (row / column LSE pass) and the
+    # per-op table of every dense pass ----
+    passes = pass_table(ctx, prob, REG)
+    row, col = passes["EROT_ROW"], passes["EROT_COL"]
+    alg_bytes = row["bytes"]
     peak, peak_src = measured_peaks()
-    traffic = profiled_traffic()
-    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                "frac": round(achieved / peak, 4), "traffic": traffic,
+    roofline = {"bound": "hbm", "achieved": row["gbs"], "peak": peak, "unit": "GB/s",
+                "frac": row["frac"],
+                "traffic": profiled_traffic(f"dense_pass<float, OP_E_ROW> n=m={n}"),
                 "kernel": "dense_pass<float, OP_E_ROW> (row log-sum-exp pass)",
-                "algorithmic_bytes_per_launch": alg_bytes, "launch_ms": round(row_ms, 5),
-                "col_pass_launch_ms": round(col_ms, 5),
-                "col_pass_frac": round(alg_bytes / (col_ms * 1e-3) / 1e9 / peak, 4),
-                "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)"}
+                "algorithmic_bytes_per_launch": alg_bytes, "launch_ms": round(row["us"] * 1e-3, 5),
+                "col_pass_launch_ms": round(col["us"] * 1e-3, 5), "col_pass_frac": col["frac"],
+                "peak_source": f"{peak_src} (MEASURED_PEAKS.json hbm_gbs)",
+                "per_op": {k: {"us": v["us"], "frac": v["frac"]} for k, v in passes.items()}}
+
+    # ---- the returned duals' marginal error in FP64 on the same FP32 M ----
+    prob64 = regot.Problem(M, a, b, precision="fp64", device=local)
+    _, g64 = prob64.erot_dual_obj_grad(REG, r.dual)
+    solve = {"niter": int(niter), "final_mar_err": float(mar),
+             "final_mar_err_fp64": float(np.linalg.norm(g64))}
+
+    extra = {}
+    if rank == 0 and world == 1 and not args.headline_only:
+        # ---- the plain FP64 GPU solver on the same problem ----
+        ms64 = []
+        for _ in range(3):
+            r64 = prob64.sinkhorn_bcd(REG, tol=TOL, max_iter=MAX_ITER, plan=False)
+            ms64.append(r64.solve_ms)
+        extra["plain_fp64"] = {"ms": round(statistics.median(ms64), 3), "niter": int(r64.niter),
+                               "what": "sinkhorn_bcd with FP64 M and FP64 arithmetic on the "
+                                       "GPU, device-resident, median of 3"}
+        # ---- the second-order solvers at both regularisations ----
+        solvers = {}
+        for reg in (0.05, 0.01):
+            for name in ("sinkhorn_bcd", "sinkhorn_newton", "sinkhorn_ssns"):
+                fn = getattr(prob, name)
+                fn(reg, tol=TOL, max_iter=200 if name != "sinkhorn_bcd" else MAX_ITER, plan=False)
+                ms, rr = [], None
+                for _ in range(3):
+                    rr = fn(reg, tol=TOL, max_iter=200 if name != "sinkhorn_bcd" else MAX_ITER,
+                            plan=False)
+                    ms.append(rr.solve_ms)
+                _, gg = prob64.erot_dual_obj_grad(reg, rr.dual)
+                solvers[f"{name} reg={reg}"] = {
+                    "ms": round(statistics.median(ms), 3), "niter": int(rr.niter),
+                    "passes": int(rr.passes), "final_mar_err": float(rr.mar_errs[-1]),
+                    "final_mar_err_fp64": float(np.linalg.norm(gg))}
+        extra["large_erot_solvers"] = solvers
+    prob64.close()
     prob.close()
 
     # ---- end to end through the public API (pinned host M) ----
@@ -742,30 +832,41 @@ def main():
     h2d = M.nbytes + a.nbytes + b.nbytes
     d2h = re.plan.nbytes + re.dual.nbytes + 3 * 8 * len(re.mar_errs)
 
-    # ---- CPU baseline (rank 0, N = 1) ----
+    if rank == 0 and world == 1 and not args.headline_only:
+        # ---- the batched workload (512 uneven problems), forward and
+        # forward + backward, against the plain FP64 single-problem solver ----
+        torch.cuda.set_stream(torch.cuda.default_stream(dev))
+        ctx.set_stream(None)
+        extra["batched"] = batched_measure(3, 2, scaled=False, max_iter=args.batched_max_iter)
+        extra["batched_cost_over_d"] = batched_measure(3, 2, scaled=True, max_iter=20000)
+
+    # ---- CPU baseline (rank 0, N = 1): one full oracle solve, measured ----
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        prob64 = regot.Problem(M, a, b, precision="fp64", device=local)
-        n64 = prob64.sinkhorn_bcd(REG, tol=TOL, max_iter=MAX_ITER, plan=False).niter
-        prob64.close()
+        from regot_oracle import sinkhorn_bcd as oracle_bcd
+
         M64 = np.asfortranarray(M.astype(np.float64))
-        iters = 3
-        t_init, t_iter = cpu_solve_sample(M64, a, b, iters)
-        cpu = {"value": round(t_init + n64 * t_iter, 1), "unit": UNIT, "cores": 1, "kind": "port",
-               "sample": f"FP64 oracle sinkhorn_bcd on the same problem: init + {iters} "
-                         f"iterations timed ({t_init:.0f} ms + {t_iter:.0f} ms/iter), "
-                         f"extrapolated to the {n64} iterations the FP64 algorithm needs"}
+        t = time.perf_counter()
+        o = oracle_bcd(M64, a, b, REG, tol=TOL, max_iter=MAX_ITER, plan=False)
+        cpu_ms = (time.perf_counter() - t) * 1e3
+        cpu = {"value": round(cpu_ms, 1), "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"FP64 oracle sinkhorn_bcd (single-threaded, like the reference's BCD) "
+                         f"on the same problem: one full solve to mar_err <= {TOL} measured "
+                         f"({o.niter} iterations)"}
 
     line = {
         "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_per_step, 4),
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
-        "data": "synthetic", "config": dict(workload_config(n), parallelism=f"replicas x{world}",
-                                            niter=niter, final_mar_err=mar),
+        "data": "synthetic", "config": workload_config(n, world), "solve": solve,
         "e2e": {"value": round(e2e_ms, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "roofline": roofline, "cpu_baseline": cpu, "clocks": clk.summary(),
         "gpu_launches": int(launches),
+        "autotune": {"configs": tuned, "seconds": round(tune_s, 2),
+                     "what": "per dense pass: 0 = 2 CTAs/SM, 4-deep row ring; "
+                             "1 = 1 CTA/SM, 8-deep row ring (regot_autotune)"},
+        **extra,
     }
     if rank == 0:
         print(json.dumps(line))

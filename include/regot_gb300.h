@@ -407,6 +407,35 @@ long long regot_pass_bytes(regot_dproblem* prob, int kind);
  * for exercising the timeout path. No counterpart in the reference. */
 long long regot_set_wait_limit(long long spins);
 
+/* ---- Autotuner of the dense passes (no counterpart in the reference,
+ * whose passes are fixed Eigen loops, e.g. src/sinkhorn_problem_bcd.cpp:82-146
+ * and src/sinkhorn_problem_obj.cpp:16-136) ----
+ * Every dense pass has two launch configurations with the same tile shape:
+ * 0 = two CTAs per SM (128 registers a thread) with a 4-deep ring of row
+ * buffers per warp, 1 = one CTA per SM (255 registers) with an 8-deep ring.
+ * regot_autotune times every pass kind under both on a synthetic n x m
+ * problem of the given storage precision (`reps` back-to-back launches,
+ * CUDA events) and keeps the faster one for (this GPU, precision, pass,
+ * size class floor(log2(n m))); later passes of that class (or of the
+ * nearest tuned class within two) use it. Choices persist through
+ * regot_autotune_save / _load (NULL path: $REGOT_GB300_AUTOTUNE, else
+ * ~/.cache/regot_gb300_autotune.tsv, read on the first launch of a process).
+ * Untuned passes use configuration 0. */
+int regot_autotune(regot_ctx* ctx, int n, int m, int precision, int reps);
+int regot_autotune_save(const char* path);   /* entries written, or -1 */
+int regot_autotune_load(const char* path);   /* entries read */
+void regot_autotune_clear(void);
+/* The table as text (one tab-separated line per entry: device, precision,
+ * pass, size class, configuration, microseconds of each configuration);
+ * copies at most len - 1 bytes and returns the full length. */
+size_t regot_autotune_entries(char* buf, size_t len);
+/* Force configuration cfg (0 or 1) for every pass; -1 restores the tuned
+ * choices. Returns the previous forced value. */
+int regot_force_pass_config(int cfg);
+/* The configuration a pass of `kind` (REGOT_PASS_*) would use now for an
+ * n x m problem of `precision`; -1 on error. */
+int regot_pass_config(regot_ctx* ctx, int kind, int precision, int n, int m);
+
 /* ---- Allocation-free variant ----
  * No counterpart in the reference. regot_erot_dual_obj_grad for callers that
  * cannot allocate device memory: code running while another framework

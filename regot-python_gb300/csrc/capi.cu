@@ -2,7 +2,10 @@
 // include/regot_gb300.h): contexts, device-resident problems, the solver
 // entry points and the pass-level entry points. Every entry point converts
 // exceptions into a status code and a per-context message.
+#include <sys/stat.h>
+
 #include <algorithm>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -820,6 +823,113 @@ static void drop_time_pass_state(regot_dproblem* P) {
 }
 
 extern "C" long long regot_set_wait_limit(long long spins) { return set_wait_limit(spins); }
+
+extern "C" int regot_force_pass_config(int cfg) { return force_pass_config(cfg); }
+
+extern "C" int regot_pass_config(regot_ctx* ctx, int kind, int precision, int n, int m) {
+    int cfg = -1;
+    const int rc = guarded(ctx, [&] {
+        require(kind >= 0 && kind < REGOT_PASS_COUNT, "unknown pass kind");
+        require(n > 0 && m > 0, "invalid sizes");
+        cfg = pass_config(kTimedOps[kind], precision == REGOT_PREC_MIXED, n, m);
+    });
+    return rc == REGOT_OK ? cfg : -1;
+}
+
+extern "C" int regot_autotune_save(const char* path) {
+    if (path == nullptr || *path == '\0') {
+        // the default location: create its directory
+        if (const char* h = std::getenv("HOME")) {
+            if (!std::getenv("REGOT_GB300_AUTOTUNE"))
+                mkdir((std::string(h) + "/.cache").c_str(), 0755);
+        }
+    }
+    return save_tuning(path);
+}
+extern "C" int regot_autotune_load(const char* path) { return load_tuning(path); }
+extern "C" void regot_autotune_clear(void) { clear_tuning(); }
+extern "C" size_t regot_autotune_entries(char* buf, size_t len) {
+    const std::string s = tuning_entries();
+    if (buf && len) {
+        const size_t k = std::min(len - 1, s.size());
+        std::memcpy(buf, s.data(), k);
+        buf[k] = '\0';
+    }
+    return s.size();
+}
+
+extern "C" int regot_autotune(regot_ctx* ctx, int n, int m, int precision, int reps) {
+    int rc = guarded(ctx, [&] {
+        require(n > 0 && m > 1, "invalid sizes");
+        require(precision == REGOT_PREC_FP64 || precision == REGOT_PREC_MIXED,
+                "unsupported precision");
+        require(reps > 0, "reps must be positive");
+    });
+    if (rc != REGOT_OK) return rc;
+    // A synthetic problem of the size: M uniform on [0, 1), uniform marginals.
+    std::vector<float> M((size_t)n * m);
+    unsigned long long x = 0x9E3779B97F4A7C15ULL;
+    for (auto& v : M) {
+        x ^= x << 13;
+        x ^= x >> 7;
+        x ^= x << 17;
+        v = (float)((x >> 40) * (1.0 / (1ULL << 24)));
+    }
+    std::vector<double> a(n, 1.0 / n), b(m, 1.0 / m);
+    regot_problem_desc d{};
+    d.M = M.data();
+    d.M_dtype = REGOT_F32;
+    d.M_mem = REGOT_MEM_HOST;
+    d.ldm = m;
+    d.n = n;
+    d.m = m;
+    d.a = a.data();
+    d.b = b.data();
+    d.ab_mem = REGOT_MEM_HOST;
+    regot_dproblem* P = nullptr;
+    rc = regot_problem_create(ctx, &d, precision, &P);
+    if (rc != REGOT_OK) return rc;
+    const int prev = force_pass_config(-1);
+    rc = guarded(ctx, [&] {
+        cudaStream_t st = ctx->stream;
+        cudaEvent_t e0, e1;
+        REGOT_CUDA(cudaEventCreate(&e0));
+        REGOT_CUDA(cudaEventCreate(&e1));
+        const double reg = 0.01;
+        try {
+            for (int kind = 0; kind < REGOT_PASS_COUNT; ++kind) {
+                double us[kPassConfigs];
+                for (int cfg = 0; cfg < kPassConfigs; ++cfg) {
+                    force_pass_config(cfg);
+                    int r = regot_time_pass(ctx, P, kind, reg, 1);  // prepares, warms
+                    if (r != REGOT_OK) throw Error(r, ctx->last_error);
+                    sync(st);
+                    REGOT_CUDA(cudaEventRecord(e0, st));
+                    r = regot_time_pass(ctx, P, kind, reg, reps);
+                    if (r != REGOT_OK) throw Error(r, ctx->last_error);
+                    REGOT_CUDA(cudaEventRecord(e1, st));
+                    REGOT_CUDA(cudaEventSynchronize(e1));
+                    float ms = 0.f;
+                    REGOT_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                    us[cfg] = 1e3 * ms / reps;
+                }
+                int best = 0;
+                for (int cfg = 1; cfg < kPassConfigs; ++cfg)
+                    if (us[cfg] < us[best]) best = cfg;
+                record_tuning(kTimedOps[kind], precision == REGOT_PREC_MIXED, n, m, best, us);
+            }
+        } catch (...) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            throw;
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    });
+    force_pass_config(prev);
+    regot_problem_destroy(P);
+    return rc;
+}
 
 extern "C" long long regot_pass_bytes(regot_dproblem* P, int kind) {
     if (!P || kind < 0 || kind >= REGOT_PASS_COUNT) return -1;

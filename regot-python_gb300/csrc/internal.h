@@ -147,6 +147,34 @@ struct PassShape {
     int nblocks;  // capacity for per-CTA totals (>= the grid of any dense pass)
 };
 
+// Launch configurations of the dense passes (dense_pass.cuh): CTAs per SM
+// (the register budget: 128 registers a thread with 2, 255 with 1) and the
+// depth of each warp's ring of row buffers. The autotuner (passes.cu)
+// chooses one per (device, precision, pass, size class of n m).
+template <int CFG> struct PassCfg;
+template <> struct PassCfg<0> { static constexpr int kMinBlocks = 2, kStages = 4; };
+template <> struct PassCfg<1> { static constexpr int kMinBlocks = 1, kStages = 8; };
+constexpr int kPassConfigs = 2;
+template <typename TM, int CFG>
+void launch_pass_cfg(int op, const PassParams& p, cudaStream_t st, int blocks);
+template <typename TM, int CFG>
+int occupancy_cfg(int op);
+// The configuration the passes use for (op, precision, n, m): a forced
+// choice (tests, the tuner), else the tuned one, else 0.
+int pass_config(int op, bool mixed, int n, int m);
+// Force one configuration for every pass (-1: back to the tuned choices);
+// returns the previous forced value.
+int force_pass_config(int cfg);
+// The autotuner's table (passes.cu): record a measured choice for the
+// current device, save / load the cache file (NULL or "": the default path,
+// $REGOT_GB300_AUTOTUNE or ~/.cache/regot_gb300_autotune.tsv), clear it,
+// and list it (one line per entry, as in the file).
+void record_tuning(int op, bool mixed, int n, int m, int cfg, const double* us);
+int save_tuning(const char* path);
+int load_tuning(const char* path);
+void clear_tuning();
+std::string tuning_entries();
+
 constexpr int kMaxPassCtasPerSm = 4;
 int device_sm_count();
 // Grid of the persistent dense pass `op` (SMs x resident CTAs, at most the

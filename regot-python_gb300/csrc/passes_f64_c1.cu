@@ -1,0 +1,7 @@
+// Dense passes over FP64 M in launch configuration 1 (dense_pass.cuh).
+#include "dense_pass.cuh"
+
+namespace regot {
+template void launch_pass_cfg<double, 1>(int, const PassParams&, cudaStream_t, int);
+template int occupancy_cfg<double, 1>(int);
+}  // namespace regot

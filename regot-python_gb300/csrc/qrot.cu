@@ -27,6 +27,7 @@
 // relative tolerance 1e-8, at most 2m steps) runs on the device, captured in
 // a CUDA graph.
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -715,9 +716,602 @@ void init_gamma(QrotEngine& E, const regot_opts& o, std::vector<double>& gamma) 
 
 }  // namespace
 
+namespace {
+
+// ---- L-BFGS on the device (qrot_lbfgs_dual) ----
+// LBFGS++'s minimize and Nocedal-Wright line search (restated in lbfgs.h)
+// keep their control flow on the host, but every vector of the algorithm
+// stays on the device: the iterates x, the gradients, the direction, and the
+// ring of m = 6 correction pairs (s, y). The two-loop recursion
+// (BFGSMat::apply_Hv, src/LBFGSpp/LBFGSpp/BFGSMat.h:276-302) is carried out
+// on scalars: with the Gram matrices S'Y and Y'Y of the stored pairs, kept
+// up to date as pairs are added, and the products S'g, Y'g, every alpha_j
+// and beta_j of the recursion follows from scalar recurrences, and the
+// direction is one linear combination of g and the pairs. A line-search
+// trial is an axpy, one dense pass and one merge kernel whose last block
+// writes every scalar the host needs (objective terms, g'd, |g|^2, |x|^2)
+// into one 64-byte record: one small copy and one synchronisation per trial.
+constexpr int kLbM = 6;          // LBFGSParam m (Param.h:168-182)
+constexpr int kLbBlock = 256;
+constexpr int kLbPairSums = 5 * kLbM + 4;
+
+struct LbScal {
+    double sq;   // sum D^2 at the trial point
+    double rem;  // mixed trial: sum of the second-order remainders
+    double dab;  // x'(a, b)
+    double dg;   // grad(x)' drt
+    double gg;   // |grad(x)|^2
+    double xx;   // |x|^2
+    double dg0;  // grad' drt of a new direction
+    double pad;
+};
+
+struct LbState {
+    unsigned counter;
+    int ncorr, ptr;
+    int phys[kLbM + 1];  // logical slot -> physical pair buffer; [kLbM] is the staging buffer
+    double theta;
+    double ys[kLbM];
+    double SY[kLbM][kLbM];  // s_i' y_j (logical slots)
+    double YY[kLbM][kLbM];
+    double cv, cy[kLbM], cs[kLbM];  // direction = cv g + sum_k cy[k] y_k + cs[k] s_k
+};
+
+// Block sums of K values, then the last block to arrive adds the block sums
+// in block order: true in every thread of that block, with the totals in
+// s_out (shared, K entries).
+template <int K>
+__device__ bool lb_reduce(const double (&v)[K], double* parts, unsigned* counter, double* s_out) {
+    __shared__ double s_red[K][kLbBlock / 32];
+    __shared__ int s_last;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+#pragma unroll
+    for (int k = 0; k < K; ++k) {
+        const double x = warp_sum_d(v[k]);
+        if (lane == 0) s_red[k][warp] = x;
+    }
+    __syncthreads();
+    if (tid < K) {
+        double s = 0.0;
+        for (int w = 0; w < kLbBlock / 32; ++w) s += s_red[tid][w];
+        parts[(size_t)blockIdx.x * K + tid] = s;
+        __threadfence();
+    }
+    __syncthreads();
+    if (tid == 0) s_last = atomicAdd(counter, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (!s_last) return false;
+    __threadfence();
+    if (tid < K) {
+        double s = 0.0;
+        for (unsigned b = 0; b < gridDim.x; ++b) s += __ldcg(&parts[(size_t)b * K + tid]);
+        s_out[tid] = s;
+    }
+    if (tid == 0) *counter = 0u;
+    __syncthreads();
+    return true;
+}
+
+__global__ void k_lb_axpy(const double* __restrict__ xp, const double* __restrict__ d,
+                          double step, int N, double* __restrict__ x) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < N) x[t] = xp[t] + step * d[t];
+}
+
+// Gradient of the last dense pass at x (rows, then columns: D1 - reg a,
+// D'1 - reg b), the record's dot products, and the pass totals (sum D^2 and,
+// with nt == 2, the remainder sum).
+template <typename Acc>
+__global__ void __launch_bounds__(kLbBlock) k_lb_merge(
+    const Acc* __restrict__ rp, int nslabs, const Acc* __restrict__ cp, int nrb, int n, int m,
+    const double* __restrict__ totpart, int nblocks, int nt, const double* __restrict__ x,
+    const double* __restrict__ drt, const double* __restrict__ a, const double* __restrict__ b,
+    double reg, double* __restrict__ grad, double* parts, LbState* st, LbScal* out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[4] = {0.0, 0.0, 0.0, 0.0};
+    if (t < n + m) {
+        double g, w;
+        if (t < n) {
+            g = merge_strided(rp + t, nslabs, (size_t)n) - reg * a[t];
+            w = a[t];
+        } else {
+            const int j = t - n;
+            g = merge_strided(cp + j, nrb, (size_t)m) - reg * b[j];
+            w = b[j];
+        }
+        grad[t] = g;
+        const double xt = x[t];
+        v[0] = xt * w;
+        v[1] = g * drt[t];
+        v[2] = g * g;
+        v[3] = xt * xt;
+    }
+    __shared__ double s_sum[4];
+    if (!lb_reduce<4>(v, parts, &st->counter, s_sum)) return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    __shared__ double s_tot[2];
+    if (warp < 2) {
+        double s = 0.0;
+        if (warp < nt)
+            for (int k = lane; k < nblocks; k += 32) s += totpart[(size_t)warp * nblocks + k];
+        s = warp_sum_d(s);
+        if (lane == 0) s_tot[warp] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        out->sq = s_tot[0];
+        out->rem = nt > 1 ? s_tot[1] : 0.0;
+        out->dab = s_sum[0];
+        out->dg = s_sum[1];
+        out->gg = s_sum[2];
+        out->xx = s_sum[3];
+    }
+}
+
+// New correction pair s = x - xp, y = g - gp into the staging buffer, its
+// products with every stored pair and with g; the last block adds the pair
+// to the ring when s'y > eps y'y (BFGSMat::add_correction,
+// BFGSMat.h:81-100, as LBFGS.h:160-161 calls it), updates the Gram
+// matrices, and turns the two-loop recursion of apply_Hv(g, -1)
+// (BFGSMat.h:276-302) into the coefficients of the new direction.
+__global__ void __launch_bounds__(kLbBlock) k_lb_pair(
+    const double* __restrict__ x, const double* __restrict__ xp, const double* __restrict__ g,
+    const double* __restrict__ gp, double* __restrict__ pairs, int N, double* parts, LbState* st) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[kLbPairSums];
+#pragma unroll
+    for (int k = 0; k < kLbPairSums; ++k) v[k] = 0.0;
+    if (t < N) {
+        const double s = x[t] - xp[t], y = g[t] - gp[t], gt = g[t];
+        const int stg = st->phys[kLbM];
+        pairs[(size_t)(2 * stg) * N + t] = s;
+        pairs[(size_t)(2 * stg + 1) * N + t] = y;
+#pragma unroll
+        for (int k = 0; k < kLbM; ++k) {
+            const int ph = st->phys[k];
+            const double sk = pairs[(size_t)(2 * ph) * N + t];
+            const double yk = pairs[(size_t)(2 * ph + 1) * N + t];
+            v[5 * k + 0] = s * yk;
+            v[5 * k + 1] = sk * y;
+            v[5 * k + 2] = y * yk;
+            v[5 * k + 3] = sk * gt;
+            v[5 * k + 4] = yk * gt;
+        }
+        v[5 * kLbM + 0] = s * y;
+        v[5 * kLbM + 1] = y * y;
+        v[5 * kLbM + 2] = s * gt;
+        v[5 * kLbM + 3] = y * gt;
+    }
+    __shared__ double r[kLbPairSums];
+    if (!lb_reduce<kLbPairSums>(v, parts, &st->counter, r)) return;
+    if (threadIdx.x != 0) return;
+    constexpr int M = kLbM;
+    double SV[M], YV[M];
+    for (int k = 0; k < M; ++k) {
+        SV[k] = r[5 * k + 3];
+        YV[k] = r[5 * k + 4];
+    }
+    const double ys = r[5 * M + 0], yy = r[5 * M + 1];
+    if (ys > DBL_EPSILON * yy) {
+        const int loc = st->ptr % M;
+        for (int k = 0; k < M; ++k) {
+            if (k == loc) continue;
+            st->SY[loc][k] = r[5 * k + 0];
+            st->SY[k][loc] = r[5 * k + 1];
+            st->YY[loc][k] = r[5 * k + 2];
+            st->YY[k][loc] = r[5 * k + 2];
+        }
+        st->SY[loc][loc] = ys;
+        st->YY[loc][loc] = yy;
+        st->ys[loc] = ys;
+        st->theta = yy / ys;
+        const int old = st->phys[loc];
+        st->phys[loc] = st->phys[M];
+        st->phys[M] = old;
+        SV[loc] = r[5 * M + 2];
+        YV[loc] = r[5 * M + 3];
+        if (st->ncorr < M) st->ncorr++;
+        st->ptr = loc + 1;
+    }
+    // apply_Hv(g, a = -1, res): res = a g; newest to oldest:
+    // alpha_j = s_j'res / ys_j, res -= alpha_j y_j; res /= theta; oldest to
+    // newest: beta_j = y_j'res / ys_j, res += (alpha_j - beta_j) s_j.
+    const double av = -1.0, theta = st->theta;
+    const int ncorr = st->ncorr;
+    double alpha[M], beta[M];
+    int order[M];
+    int j = st->ptr % M;
+    for (int i = 0; i < ncorr; ++i) {
+        j = (j + M - 1) % M;
+        double sres = av * SV[j];
+        for (int q = 0; q < i; ++q) sres -= alpha[order[q]] * st->SY[j][order[q]];
+        alpha[j] = sres / st->ys[j];
+        order[i] = j;
+    }
+    for (int i = 0; i < ncorr; ++i) {
+        // j is the oldest pair here, then moves to newer ones
+        double yres = av * YV[j];
+        for (int q = 0; q < ncorr; ++q) yres -= alpha[order[q]] * st->YY[j][order[q]];
+        yres /= theta;
+        for (int q = 0; q < i; ++q) {
+            const int k = (j + M - 1 - q) % M;  // the pairs already added, newest first
+            yres += (alpha[k] - beta[k]) * st->SY[k][j];
+        }
+        beta[j] = yres / st->ys[j];
+        j = (j + 1) % M;
+    }
+    st->cv = av / theta;
+    for (int k = 0; k < M; ++k) {
+        st->cy[k] = 0.0;
+        st->cs[k] = 0.0;
+    }
+    for (int q = 0; q < ncorr; ++q) {
+        const int k = order[q];
+        st->cy[k] = -alpha[k] / theta;
+        st->cs[k] = alpha[k] - beta[k];
+    }
+}
+
+// drt = cv g + sum_k cy[k] y_k + cs[k] s_k over the stored pairs, and g'drt.
+__global__ void __launch_bounds__(kLbBlock) k_lb_dir(const double* __restrict__ g,
+                                                     const double* __restrict__ pairs, int N,
+                                                     double* __restrict__ drt, double* parts,
+                                                     LbState* st, LbScal* out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    double v[1] = {0.0};
+    if (t < N) {
+        const double gt = g[t];
+        double d = st->cv * gt;
+        const int ncorr = st->ncorr;
+        for (int k = 0; k < ncorr; ++k) {
+            const int ph = st->phys[k];
+            d += st->cy[k] * pairs[(size_t)(2 * ph + 1) * N + t];
+            d += st->cs[k] * pairs[(size_t)(2 * ph) * N + t];
+        }
+        drt[t] = d;
+        v[0] = gt * d;
+    }
+    __shared__ double r[1];
+    if (!lb_reduce<1>(v, parts, &st->counter, r)) return;
+    if (threadIdx.x == 0) out->dg0 = r[0];
+}
+
+// Page-locked record for the per-trial readback.
+struct PinnedScal {
+    LbScal* p = nullptr;
+    PinnedScal() { REGOT_CUDA(cudaHostAlloc((void**)&p, sizeof(LbScal), cudaHostAllocDefault)); }
+    ~PinnedScal() {
+        if (p) cudaFreeHost(p);
+    }
+    PinnedScal(const PinnedScal&) = delete;
+    PinnedScal& operator=(const PinnedScal&) = delete;
+};
+
+__global__ void k_lb_stamp(unsigned long long* out) {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    *out = t;
+}
+
+}  // namespace
+
+// qrot_lbfgs_dual_internal (qrot_lbfgs_dual.cpp:81-126) with LBFGSSolver::
+// minimize (LBFGS.h:79-175) and LineSearchNocedalWright::LineSearch
+// (LineSearchNocedalWright.h:85-280) on device vectors; tau = 0.
+void qrot_lbfgs_dual_device(regot_ctx* ctx, regot_dproblem* P, double reg, double tol,
+                            int max_iter, const regot_opts& o, regot_result* res) {
+    cudaStream_t st = ctx->stream;
+    const int n = P->n, m = P->m, N = n + m;
+    QrotEngine E(P, reg, 0.0, st);
+    ErotOps& ops = E.ops();
+    const bool mixed = P->prec == REGOT_PREC_MIXED;
+    const PassShape sh = ops.buf().shape;
+    constexpr int M = kLbM;
+    const int gN = cdiv(N, kLbBlock);
+
+    DBuf<double> X(3 * (size_t)N, st), G(3 * (size_t)N, st), drt(N, st);
+    DBuf<double> pairs((size_t)(M + 1) * 2 * N, st), parts((size_t)gN * kLbPairSums, st);
+    DBuf<LbState> dstate(1, st);
+    DBuf<LbScal> dscal(1, st);
+    DBuf<double> grid(1, st);
+    pairs.zero();
+    {
+        LbState s0{};
+        s0.ncorr = 0;
+        s0.ptr = M;  // BFGSMat::reset: m_ptr = m
+        for (int k = 0; k <= M; ++k) s0.phys[k] = k;
+        s0.theta = 1.0;
+        s0.cv = -1.0;  // the first direction is -g (LBFGS.h:104)
+        h2d(dstate.get(), &s0, sizeof(s0), st);
+    }
+    PinnedScal pin;
+    LbScal* hs = pin.p;
+    auto xbuf = [&](int i) { return X.get() + (size_t)i * N; };
+    auto gbuf = [&](int i) { return G.get() + (size_t)i * N; };
+
+    const int cap = max_iter + 2;
+    DBuf<unsigned long long> stamps(2 * (size_t)cap + 2, st);
+    std::vector<double> hobj, hmar, hprim;
+    int nstamp = 0;
+    auto stamp = [&]() {
+        k_lb_stamp<<<1, 1, 0, st>>>(stamps.get() + nstamp++);
+        count_launch();
+    };
+
+    // Initial point: alpha = 0, beta = optimal_beta(0), or x0.
+    std::vector<double> gamma0;
+    stamp();  // the reference's timer starts before the first evaluation
+    init_gamma(E, o, gamma0);
+    d2d(xbuf(0), E.gamma(), (size_t)N * sizeof(double), st);
+
+    // Merge of the last pass at x into grad, plus the record; returns after
+    // the record has reached the host.
+    auto merge = [&](int op, int nt, const double* x, double* g) {
+        const int blocks = pass_blocks(op, mixed, n, m);
+        if (mixed)
+            k_lb_merge<float><<<gN, kLbBlock, 0, st>>>(
+                (const float*)ops.buf().rowpart.get(), sh.nslabs,
+                (const float*)ops.buf().colpart.get(), sh.nrb, n, m, ops.buf().totpart.get(),
+                blocks, nt, x, drt.get(), P->a, P->b, reg, g, parts.get(), dstate.get(),
+                dscal.get());
+        else
+            k_lb_merge<double><<<gN, kLbBlock, 0, st>>>(
+                (const double*)ops.buf().rowpart.get(), sh.nslabs,
+                (const double*)ops.buf().colpart.get(), sh.nrb, n, m, ops.buf().totpart.get(),
+                blocks, nt, x, drt.get(), P->a, P->b, reg, g, parts.get(), dstate.get(),
+                dscal.get());
+        count_launch();
+        REGOT_CHECK_LAUNCH();
+        E.add_passes(1);
+        d2h(hs, dscal.get(), sizeof(LbScal), st);
+        sync(st);
+    };
+    // f and grad at x (the Q_GRAD pass), as Problem::dual_obj_grad.
+    auto eval_at = [&](const double* x, double* g) {
+        ops.maxabs(x, N, nullptr, 0, grid.get());
+        PassParams p = ops.base_params();
+        p.ra = x;
+        p.cb = x + n;
+        p.grid = grid.get();
+        ops.pass(OP_Q_GRAD, p);
+        merge(OP_Q_GRAD, 1, x, g);
+        return 0.5 * hs->sq - reg * hs->dab;
+    };
+
+    int ix = 0, ig = 0;
+    double fx = eval_at(xbuf(ix), gbuf(ig));
+    double last_obj = fx;
+    double gg = hs->gg, xx = hs->xx;
+    int it = 0;
+    auto iterate = [&](int xi, double gnorm) {
+        stamp();
+        double prim = 0.0;
+        if (o.prim_vals) prim = E.primal(xbuf(xi));
+        hobj.push_back(last_obj);
+        hmar.push_back(gnorm / reg);
+        hprim.push_back(prim);
+        if (o.verbose >= 1)
+            std::printf("iter = %d, objval = %g, ||grad|| = %g\n", it, last_obj, gnorm);
+        it++;
+        stamp();
+    };
+
+    lbfgs::Param param;
+    param.epsilon = tol;
+    param.epsilon_rel = tol;
+    param.max_iterations = max_iter;
+    int niter = 0;
+    double gnorm = std::sqrt(gg);
+    iterate(ix, gnorm);
+    if (gnorm <= param.epsilon || gnorm <= param.epsilon_rel * std::sqrt(xx)) {
+        niter = 1;
+    } else {
+        // drt = -g (LBFGS.h:104), its g'drt; step = 1 / |drt|
+        k_lb_dir<<<gN, kLbBlock, 0, st>>>(gbuf(ig), pairs.get(), N, drt.get(), parts.get(),
+                                          dstate.get(), dscal.get());
+        count_launch();
+        REGOT_CHECK_LAUNCH();
+        double step = 1.0 / gnorm;
+        bool dg_known = true;  // the first g'drt is -|g|^2
+        double dg = -gg;
+        int k = 1;
+        for (;;) {
+            const int ixp = ix, igp = ig;
+            // ---- line search (LineSearchNocedalWright.h:85-280) ----
+            if (step <= 0.0) throw Error(REGOT_ERR_INVALID_ARG, "'step' must be positive");
+            const double fx_init = fx;
+            bool split_done = false;
+            int ixl = ixp, igl = igp;  // x_lo, grad_lo (start as xp, gradp)
+            int ixt = (ixp + 1) % 3, igt = (igp + 1) % 3;  // trial targets
+            double dg_init = dg, test_decr = 0.0, test_curv = 0.0;
+            auto free_of = [](int a, int b) { return 3 - a - b; };
+            // One trial at step: x = xp + step drt into buffer ixt, grad into
+            // igt; returns f and sets dgt, ggt, xxt.
+            double dgt = 0.0, ggt = 0.0, xxt = 0.0;
+            auto trial = [&](double s) {
+                k_lb_axpy<<<gN, kLbBlock, 0, st>>>(xbuf(ixp), drt.get(), s, N, xbuf(ixt));
+                count_launch();
+                double f;
+                if (mixed) {
+                    PassParams p = ops.base_params();
+                    p.ra = xbuf(ixp);
+                    p.cb = xbuf(ixp) + n;
+                    p.rd = drt.get();
+                    p.cd = drt.get() + n;
+                    p.steps[0] = s;
+                    p.nsteps = 1;
+                    p.grid = grid.get();
+                    if (!split_done) {
+                        ops.maxabs(xbuf(ixp), N, nullptr, 0, grid.get());
+                        ops.pass(OP_Q_GRADLS, p);
+                        split_done = true;
+                    } else {
+                        ops.pass_presplit(OP_Q_GRADLS, p);
+                    }
+                    merge(OP_Q_GRADLS, 2, xbuf(ixt), gbuf(igt));
+                    if (!dg_known) dg_init = hs->dg0;
+                    last_obj = 0.5 * hs->sq - reg * hs->dab;
+                    f = fx_init + s * dg_init + hs->rem;
+                } else {
+                    f = eval_at(xbuf(ixt), gbuf(igt));
+                    if (!dg_known) dg_init = hs->dg0;
+                    last_obj = f;
+                }
+                if (!dg_known) {
+                    dg_known = true;
+                    if (dg_init > 0.0)
+                        throw Error(REGOT_ERR_LINESEARCH,
+                                    "the moving direction increases the objective function value");
+                }
+                test_decr = param.ftol * dg_init;
+                test_curv = -param.wolfe * dg_init;
+                dgt = hs->dg;
+                ggt = hs->gg;
+                xxt = hs->xx;
+                return f;
+            };
+            double step_hi = 0.0, fx_hi = 0.0, step_lo = 0.0, fx_lo = fx_init, dg_lo = 0.0;
+            double gg_lo = gg, xx_lo = xx;
+            bool lo_is_init = true;
+            int lsit = 0;
+            bool done = false;
+            // expansion phase
+            for (;;) {
+                fx = trial(step);
+                dg = dgt;
+                if (lo_is_init) dg_lo = dg_init;
+                if (fx - fx_init > step * test_decr || (0.0 < step_lo && fx >= fx_lo)) {
+                    step_hi = step;
+                    fx_hi = fx;
+                    break;
+                }
+                if (std::abs(dg) <= test_curv) {
+                    done = true;
+                    break;
+                }
+                step_hi = step_lo;
+                fx_hi = fx_lo;
+                step_lo = step;
+                fx_lo = fx;
+                dg_lo = dg;
+                lo_is_init = false;
+                std::swap(ixl, ixt);  // x_lo.swap(x)
+                std::swap(igl, igt);
+                gg_lo = ggt;
+                xx_lo = xxt;
+                if (ixt == ixp) ixt = free_of(ixp, ixl);
+                if (igt == igp) igt = free_of(igp, igl);
+                if (dg >= 0.0) break;
+                lsit++;
+                if (lsit >= param.max_linesearch) {
+                    // x.swap(x_lo): the accepted point is x_lo
+                    std::swap(ixl, ixt);
+                    std::swap(igl, igt);
+                    ggt = gg_lo;
+                    xxt = xx_lo;
+                    done = true;
+                    break;
+                }
+                step *= 2.0;
+            }
+            if (!done) {
+                // zoom phase
+                for (;;) {
+                    step = lbfgs::quad_interp(step_lo, step_hi, fx_lo, fx_hi,
+                                              lo_is_init ? dg_init : dg_lo);
+                    fx = trial(step);
+                    dg = dgt;
+                    if (lo_is_init) dg_lo = dg_init;
+                    if (fx - fx_init > step * test_decr || fx >= fx_lo) {
+                        if (step == step_hi)
+                            throw Error(REGOT_ERR_LINESEARCH,
+                                        "the line search routine failed, possibly due to "
+                                        "insufficient numeric precision");
+                        step_hi = step;
+                        fx_hi = fx;
+                    } else {
+                        if (std::abs(dg) <= test_curv) break;
+                        if (dg * (step_hi - step_lo) >= 0.0) {
+                            step_hi = step_lo;
+                            fx_hi = fx_lo;
+                        }
+                        if (step == step_lo)
+                            throw Error(REGOT_ERR_LINESEARCH,
+                                        "the line search routine failed, possibly due to "
+                                        "insufficient numeric precision");
+                        step_lo = step;
+                        fx_lo = fx;
+                        dg_lo = dg;
+                        lo_is_init = false;
+                        std::swap(ixl, ixt);
+                        std::swap(igl, igt);
+                        gg_lo = ggt;
+                        xx_lo = xxt;
+                        if (ixt == ixp) ixt = free_of(ixp, ixl);
+                        if (igt == igp) igt = free_of(igp, igl);
+                    }
+                    lsit++;
+                    if (lsit >= param.max_linesearch) {
+                        if (step_lo <= 0.0)
+                            throw Error(REGOT_ERR_LINESEARCH,
+                                        "the line search routine failed, unable to sufficiently "
+                                        "decrease the function value");
+                        step = step_lo;
+                        fx = fx_lo;
+                        dg = dg_lo;
+                        std::swap(ixl, ixt);
+                        std::swap(igl, igt);
+                        ggt = gg_lo;
+                        xxt = xx_lo;
+                        break;
+                    }
+                }
+            }
+            // the accepted point is in (ixt, igt)
+            ix = ixt;
+            ig = igt;
+            gg = ggt;
+            xx = xxt;
+            gnorm = std::sqrt(gg);
+            iterate(ix, gnorm);
+            if (gnorm <= param.epsilon || gnorm <= param.epsilon_rel * std::sqrt(xx)) break;
+            if (param.max_iterations != 0 && k >= param.max_iterations) break;
+            // correction pair and the next direction
+            k_lb_pair<<<gN, kLbBlock, 0, st>>>(xbuf(ix), xbuf(ixp), gbuf(ig), gbuf(igp),
+                                               pairs.get(), N, parts.get(), dstate.get());
+            k_lb_dir<<<gN, kLbBlock, 0, st>>>(gbuf(ig), pairs.get(), N, drt.get(), parts.get(),
+                                              dstate.get(), dscal.get());
+            count_launch(2);
+            REGOT_CHECK_LAUNCH();
+            dg_known = false;  // read with the first trial's record
+            step = 1.0;
+            k++;
+        }
+        niter = k;
+    }
+    // run_times from the device stamps (each iteration: from the end of the
+    // previous iterate call, or the start, to the start of this one)
+    std::vector<unsigned long long> hst(nstamp);
+    d2h(hst.data(), stamps.get(), nstamp * sizeof(unsigned long long), st);
+    sync(st);
+    std::vector<double> htime(hobj.size());
+    double cum = 0.0;
+    for (size_t q = 0; q < hobj.size(); ++q) {
+        cum += (double)(hst[2 * q + 1] - hst[2 * q]) * 1e-6;
+        htime[q] = cum;
+    }
+    finish_qrot(E, xbuf(ix), hobj, hmar, htime, hprim, niter, o, res);
+}
+
 // qrot_lbfgs_dual_internal (qrot_lbfgs_dual.cpp:81-126, QROTDual 18-79).
 void qrot_lbfgs_dual_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max_iter,
                          const regot_opts& o, regot_result* res) {
+    if (o.tau == 0.0) {
+        qrot_lbfgs_dual_device(ctx, P, reg, tol, max_iter, o, res);
+        return;
+    }
+    // tau > 0 (only reachable through the C ABI: the reference's Python
+    // layer never sets it): the host-vector driver with the exact tau terms.
     cudaStream_t st = ctx->stream;
     const int n = P->n, m = P->m, N = n + m;
     QrotEngine E(P, reg, o.tau, st);

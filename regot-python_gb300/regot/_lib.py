@@ -149,7 +149,9 @@ EXPORTS = [
     "regot_qrot_dual_obj_grad",
     "regot_qrot_optimal_beta",
     "regot_qrot_primal_val", "regot_qrot_plan", "regot_time_pass", "regot_pass_bytes",
-    "regot_set_wait_limit",
+    "regot_set_wait_limit", "regot_autotune", "regot_autotune_save", "regot_autotune_load",
+    "regot_autotune_clear", "regot_autotune_entries", "regot_force_pass_config",
+    "regot_pass_config",
     "regot_erot_dual_obj_grad_noalloc", "regot_host_alloc", "regot_host_free",
 ]
 
@@ -216,6 +218,15 @@ def load() -> C.CDLL:
         lib.regot_pass_bytes.restype = C.c_longlong
         lib.regot_set_wait_limit.argtypes = [C.c_longlong]
         lib.regot_set_wait_limit.restype = C.c_longlong
+        lib.regot_autotune.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int]
+        lib.regot_autotune_save.argtypes = [C.c_char_p]
+        lib.regot_autotune_load.argtypes = [C.c_char_p]
+        lib.regot_autotune_clear.argtypes = []
+        lib.regot_autotune_clear.restype = None
+        lib.regot_autotune_entries.argtypes = [C.c_char_p, C.c_size_t]
+        lib.regot_autotune_entries.restype = C.c_size_t
+        lib.regot_force_pass_config.argtypes = [C.c_int]
+        lib.regot_pass_config.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int]
         lib.regot_erot_solve_batched.argtypes = [vp, C.POINTER(BatchDesc), C.c_double,
                                                  C.c_double, C.c_int, C.POINTER(BatchResult)]
         lib.regot_erot_solve_batched_grad.argtypes = [vp, C.POINTER(BatchDesc), C.c_double,
@@ -278,6 +289,17 @@ class Context:
                 self.handle = None
         except Exception:
             pass
+
+
+def autotune_entries() -> list[list[str]]:
+    """The autotuner's table: one list of fields per entry (device,
+    precision, pass, size class, configuration, microseconds of each
+    configuration)."""
+    lib = load()
+    size = lib.regot_autotune_entries(None, 0)
+    buf = C.create_string_buffer(size + 1)
+    lib.regot_autotune_entries(buf, size + 1)
+    return [ln.split("\t") for ln in buf.value.decode().splitlines() if ln]
 
 
 _contexts: dict[int, Context] = {}
