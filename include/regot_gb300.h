@@ -259,6 +259,19 @@ typedef struct {
  * as a device-side loop. */
 int regot_erot_solve_batched(regot_ctx* ctx, const regot_batch_desc* desc, double reg, double tol,
                              int max_iter, regot_batch_result* res);
+/* The half-sweeps of a dimension class (d <= 4, <= 8, <= 16) run either on
+ * the CUDA cores (direct differences, FP32) or with the cost tile x y' on
+ * the tensor cores (tcgen05, TF32 hi/lo split operands, FP32 accumulation,
+ * M = s (|x|^2 + |y|^2 - 2 x.y)): about 2^-21 s (|x|^2 + |y|^2) absolute
+ * error in M instead of the direct difference's relative FP32 rounding.
+ * The first batch with problems of a class on a device times one row
+ * half-sweep of each and keeps the faster for the process.
+ * regot_force_batch_variant(0 | 1) forces one for every class (-1: the timed
+ * choice) and returns the previous forced value; regot_batch_variants
+ * fills out[3] with the timed choices so far (-1: not yet timed). No
+ * counterpart in the reference. */
+int regot_force_batch_variant(int variant);
+int regot_batch_variants(regot_ctx* ctx, int* out);
 
 /* regot_erot_solve_batched followed by its backward (no counterpart in the
  * reference, which has no derivatives): at each problem's returned duals,

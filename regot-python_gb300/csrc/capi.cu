@@ -826,6 +826,16 @@ extern "C" long long regot_set_wait_limit(long long spins) { return set_wait_lim
 
 extern "C" int regot_force_pass_config(int cfg) { return force_pass_config(cfg); }
 
+extern "C" int regot_force_batch_variant(int variant) { return force_batch_variant(variant); }
+
+extern "C" int regot_batch_variants(regot_ctx* ctx, int* out) {
+    return guarded(ctx, [&] {
+        require(out != nullptr, "NULL argument");
+        const std::vector<int> v = batch_variants();
+        for (size_t c = 0; c < v.size(); ++c) out[c] = v[c];
+    });
+}
+
 extern "C" int regot_pass_config(regot_ctx* ctx, int kind, int precision, int n, int m) {
     int cfg = -1;
     const int rc = guarded(ctx, [&] {

@@ -27,12 +27,17 @@
 // running, no dual has left the split grid, and fewer than max_iter / 2 + 3
 // bodies have run.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <memory>
+#include <mutex>
+#include <string>
 #include <vector>
 
 #include "device_util.cuh"
+#include "sm100_util.cuh"
 #include "solvers.h"
 
 namespace regot {
@@ -69,7 +74,7 @@ struct BatchState {
     int loops;
     int loop_cap;
     int stop_below;  // leave the device loop when this few problems still run
-    int pad;
+    int err;         // a bounded wait of a tensor-core sweep gave up
     double maxabs;  // max |dual| for the grid
     double g, inv_g, bound;
 };
@@ -406,6 +411,232 @@ __global__ void __launch_bounds__(kBWarps * 32) k_bcol(
     col_item<DP>(B, it, as, bs, beta, st, k2, reg, write_split);
 }
 
+// ---- tensor-core variant of the half-sweeps ----
+// The cost tile x y' on the fifth-generation tensor cores: a CTA owns 128
+// points of one side of a problem (the MMA's M = 128 rows, one TMEM lane
+// each) and walks the other side in tiles of 256 points (N = 256). Both
+// sides' points, zero-padded to 16 dimensions, are split into TF32 hi + lo
+// parts (hi = x rounded to TF32, lo = the rest rounded to TF32: x = hi + lo
+// to about 2^-22 relative) and stored K-major in shared memory; one thread
+// issues, per 8-wide K step, hi*hi + hi*lo + lo*hi (TF32x3) into an FP32
+// accumulator of 128 lanes x 256 columns in tensor memory. The epilogue
+// reads each thread's row of the tile (tcgen05.ld) and forms
+// M_ij = s (|x_i|^2 + |y_j|^2 - 2 x_i.y_j) before the same split exponent
+// and running log-sum-exp as the CUDA-core kernels. The expansion loses the
+// direct difference's relative accuracy on small distances: M carries an
+// absolute error of about 2^-21 s (|x_i|^2 + |y_j|^2), which the batched
+// tests measure against the direct difference. Which variant a dimension
+// class uses is chosen by timing (see the host code).
+constexpr int kTcOwn = 128;
+constexpr int kTcTile = 256;
+constexpr int kTcK = 16;
+constexpr uint32_t kTcLbo = 128, kTcSbo = 512;  // K-major TF32 core matrices (8 rows x 16 B)
+constexpr uint32_t kTcABytes = (kTcOwn / 8) * kTcSbo;
+constexpr uint32_t kTcBBytes = (kTcTile / 8) * kTcSbo;
+// Dynamic shared memory per CTA: the tiles and the per-point parameters;
+// requested at 100 KB so that at most two CTAs share an SM, whose tensor
+// memory (512 columns) then holds both accumulators.
+constexpr size_t kTcSmem = 100 * 1024;
+static_assert(2 * (size_t)kTcABytes + 2 * (size_t)kTcBBytes + kTcTile * 16 + 1024 <= kTcSmem,
+              "tensor-core sweep tiles exceed the requested shared memory");
+constexpr uint32_t kTcTmemCols = 256;
+constexpr long long kTcPolls = 1LL << 14;
+
+__device__ __forceinline__ float tf32_rna(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+
+// Point row r (16 values) into the hi / lo tiles.
+__device__ __forceinline__ void tc_put_point(unsigned char* hi, unsigned char* lo, int r,
+                                             const float (&v)[kTcK]) {
+#pragma unroll
+    for (int kg = 0; kg < kTcK / 4; ++kg) {
+        float h[4], l[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            h[e] = tf32_rna(v[4 * kg + e]);
+            l[e] = tf32_rna(v[4 * kg + e] - h[e]);
+        }
+        const uint32_t off = (uint32_t)(r >> 3) * kTcSbo + (uint32_t)kg * kTcLbo + (uint32_t)(r & 7) * 16;
+        *reinterpret_cast<float4*>(hi + off) = make_float4(h[0], h[1], h[2], h[3]);
+        *reinterpret_cast<float4*>(lo + off) = make_float4(l[0], l[1], l[2], l[3]);
+    }
+}
+
+// Half-sweep with the cost tile on the tensor cores. COLS = false: the row
+// half-sweep of row_item (items are blocks of 128 rows; each warp of the
+// first four writes the marginal-error partial of its 32 rows, the layout
+// k_bfin reads); COLS = true: the column half-sweep of col_item.
+template <bool COLS>
+__global__ void __launch_bounds__(256, 1) k_bsweep_tc(
+    const BatchDev B, const int2* __restrict__ items, const float2* __restrict__ own_split,
+    const float2* __restrict__ oth_split, const double* __restrict__ own_cur, double* own_next,
+    float2* own_split_next, double* part, const int* __restrict__ done, BatchState* st, float k2,
+    double reg, int write_split) {
+    const int2 it = items[blockIdx.x];
+    const int p = it.x;
+    if (done[p]) return;
+    extern __shared__ unsigned char tc_raw[];
+    unsigned char* smem = tc_raw + ((1024 - (sm100::smem_u32(tc_raw) & 1023)) & 1023);
+    unsigned char* Ahi = smem;
+    unsigned char* Alo = Ahi + kTcABytes;
+    unsigned char* Bhi = Alo + kTcABytes;
+    unsigned char* Blo = Bhi + kTcBBytes;
+    float4* sp = reinterpret_cast<float4*>(Blo + kTcBBytes);  // other point: |y|^2, hi, lo k
+    __shared__ __align__(8) uint64_t s_bar;
+    __shared__ uint32_t s_tmem;
+    __shared__ float s_mx[kTcOwn], s_sm[kTcOwn];
+
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int r = tid & (kTcOwn - 1), half = tid >> 7;
+    const int n = B.n[p], m = B.m[p], d = B.d[p];
+    const int n_own = COLS ? m : n, n_oth = COLS ? n : m;
+    const float* Po = COLS ? B.Y + B.yo[p] : B.X + B.xo[p];
+    const float* Pt = COLS ? B.X + B.xo[p] : B.Y + B.yo[p];
+    const int oo = COLS ? B.co[p] : B.ro[p], ot = COLS ? B.ro[p] : B.co[p];
+    const float sc = B.scale[p];
+    const int o = it.y * kTcOwn + r;
+    const bool own_ok = o < n_own;
+
+    // own point: row r of A (written by the first 128 threads), its squared
+    // norm and split dual (both halves keep them)
+    float v[kTcK];
+    float own_sq = 0.f;
+#pragma unroll
+    for (int k = 0; k < kTcK; ++k) {
+        v[k] = (own_ok && k < d) ? Po[(long long)o * d + k] : 0.f;
+        own_sq = __fmaf_rn(v[k], v[k], own_sq);
+    }
+    if (half == 0) tc_put_point(Ahi, Alo, r, v);
+    const float2 osp = own_ok ? own_split[oo + o] : make_float2(0.f, 0.f);
+    const float oh = osp.x, olk = __fmul_rn(osp.y, k2);
+
+    if (tid == 0) {
+        sm100::mbar_init(&s_bar, 1);
+        sm100::fence_mbar_init();
+    }
+    if (warp == 0) {
+        sm100::tmem_alloc(&s_tmem, kTcTmemCols);
+        sm100::tmem_relinquish();
+    }
+    sm100::tc_fence_before();
+    __syncthreads();
+    sm100::tc_fence_after();
+    const uint32_t tmem = s_tmem;
+    constexpr uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(kTcTile >> 3) << 17) |
+                               ((uint32_t)(kTcOwn >> 4) << 24);
+    const uint32_t ah = sm100::smem_u32(Ahi), al = sm100::smem_u32(Alo);
+    const uint32_t bh = sm100::smem_u32(Bhi), bl = sm100::smem_u32(Blo);
+
+    float mx = -INFINITY, sm = 0.f;
+    bool failed = false;
+    int tile = 0;
+    for (int j0 = 0; j0 < n_oth; j0 += kTcTile, ++tile) {
+        // other points of the tile: row tid of B and its parameters
+        {
+            const int j = j0 + tid;
+            const bool ok = j < n_oth;
+            float w[kTcK];
+            float sq = 0.f;
+#pragma unroll
+            for (int k = 0; k < kTcK; ++k) {
+                w[k] = (ok && k < d) ? Pt[(long long)j * d + k] : 0.f;
+                sq = __fmaf_rn(w[k], w[k], sq);
+            }
+            tc_put_point(Bhi, Blo, tid, w);
+            const float2 s2 = ok ? oth_split[ot + j] : make_float2(0.f, 0.f);
+            sp[tid] = make_float4(sq, s2.x, __fmul_rn(s2.y, k2), 0.f);
+        }
+        sm100::fence_proxy_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+#pragma unroll
+            for (int ks = 0; ks < kTcK / 8; ++ks) {
+                const uint64_t dah = sm100::smem_desc(ah + ks * 2 * kTcLbo, kTcLbo, kTcSbo);
+                const uint64_t dal = sm100::smem_desc(al + ks * 2 * kTcLbo, kTcLbo, kTcSbo);
+                const uint64_t dbh = sm100::smem_desc(bh + ks * 2 * kTcLbo, kTcLbo, kTcSbo);
+                const uint64_t dbl = sm100::smem_desc(bl + ks * 2 * kTcLbo, kTcLbo, kTcSbo);
+                sm100::mma_tf32(tmem, dah, dbh, idesc, ks != 0 ? 1u : 0u);
+                sm100::mma_tf32(tmem, dah, dbl, idesc, 1u);
+                sm100::mma_tf32(tmem, dal, dbh, idesc, 1u);
+            }
+            sm100::mma_commit(&s_bar);
+        }
+        const bool ok = sm100::mbar_wait(&s_bar, (uint32_t)(tile & 1), kTcPolls);
+        if (__syncthreads_or(!ok)) {
+            failed = true;
+            break;
+        }
+        sm100::tc_fence_after();
+        const uint32_t trow = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
+#pragma unroll 1
+        for (int x = 0; x < 8; ++x) {
+            const int c0 = half * 128 + 16 * x;
+            float dv[16];
+            sm100::tmem_ld16(trow + (uint32_t)c0, dv);
+            if (!own_ok) continue;
+#pragma unroll
+            for (int e = 0; e < 16; ++e) {
+                const int jj = c0 + e;
+                if (j0 + jj < n_oth) {
+                    const float4 q = sp[jj];
+                    const float Mij = __fmul_rn(__fmaf_rn(-2.f, dv[e], __fadd_rn(own_sq, q.x)), sc);
+                    const float ex = __fadd_rn(__fadd_rn(oh, q.y), -Mij);
+                    const float z = __fmaf_rn(ex, k2, __fadd_rn(olk, q.z));
+                    lse_add(mx, sm, z);
+                }
+            }
+        }
+        sm100::tc_fence_before();
+        __syncthreads();
+    }
+    if (failed) {
+        // the commit covers every MMA this CTA issued; wait for it (bounded)
+        // before the tensor memory is freed
+        if (tid == 0) {
+            atomicOr(&st->err, 1);
+            sm100::mbar_wait(&s_bar, (uint32_t)(tile & 1), kTcPolls);
+        }
+        sm100::tc_fence_before();
+        __syncthreads();
+        if (warp == 0) sm100::tmem_dealloc(tmem, kTcTmemCols);
+        return;
+    }
+    if (warp == 0) sm100::tmem_dealloc(tmem, kTcTmemCols);
+    // merge the two column halves of each owner
+    if (half == 1) {
+        s_mx[r] = mx;
+        s_sm[r] = sm;
+    }
+    __syncthreads();
+    if (half == 1) return;
+    lse_merge(mx, sm, s_mx[r], s_sm[r]);
+    double g2 = 0.0;
+    if (own_ok) {
+        const double lg2 = (double)mx + (double)log2f(sm);
+        if constexpr (!COLS) {
+            const double S = row_sum(mx, sm);
+            const double gi = S - B.a[oo + o];
+            g2 = gi * gi;
+            const double an = own_cur[oo + o] + reg * (B.loga[oo + o] - 0.69314718055994531 * lg2);
+            own_next[oo + o] = an;
+            own_split_next[oo + o] = bsplit(an, st, &st->regrid);
+        } else {
+            const double bn = own_cur[oo + o] + reg * (B.logb[oo + o] - 0.69314718055994531 * lg2);
+            own_next[oo + o] = bn;
+            if (write_split) own_split_next[oo + o] = bsplit(bn, st, &st->regrid);
+        }
+    }
+    if constexpr (!COLS) {
+        // partial of sum (S_i - a_i)^2 per 32 rows, in the 32-row layout
+        g2 = warp_sum_d(g2);
+        const int blk = it.y * (kTcOwn / kBItems) + warp;
+        if (lane == 0 && blk * kBItems < n) part[B.rbo[p] + blk] = g2;
+    }
+}
+
 // Marginal error and stopping test of iterate k for every running problem
 // (one warp each): mar = sqrt(sum over the problem's row blocks), stop when
 // mar < tol or k >= max_iter (sinkhorn_bcd.cpp), the iterate's alpha being in
@@ -629,7 +860,49 @@ void upload_vec(DBuf<T>& buf, const std::vector<T>& v, cudaStream_t st) {
     h2d(buf.get(), v.data(), v.size() * sizeof(T), st);
 }
 
+// Which half-sweep kernels a dimension class uses: 0 = CUDA-core direct
+// differences (k_brow / k_bcol), 1 = tensor-core cost tile (k_bsweep_tc).
+// Chosen per device and class by timing one row half-sweep of each on the
+// first batch that has problems of the class; a forced choice overrides.
+std::mutex g_bvar_mutex;
+std::map<std::pair<std::string, int>, int> g_bvar;
+std::atomic<int> g_bvar_force{-1};
+
+std::string bdevice_name() {
+    int dev = 0;
+    cudaDeviceProp prop;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&prop, dev) != cudaSuccess)
+        return "unknown";
+    return std::string(prop.name) + " sm" + std::to_string(prop.multiProcessorCount);
+}
+
+template <bool COLS>
+void configure_tc_sweep() {
+    static std::atomic<unsigned long long> configured{0};
+    int dev = 0;
+    REGOT_CUDA(cudaGetDevice(&dev));
+    if (dev >= 64 || !(configured.load() & (1ULL << dev))) {
+        REGOT_CUDA(cudaFuncSetAttribute(k_bsweep_tc<COLS>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)kTcSmem));
+        if (dev < 64) configured.fetch_or(1ULL << dev);
+    }
+}
+
 }  // namespace
+
+int force_batch_variant(int v) { return g_bvar_force.exchange(v == 0 || v == 1 ? v : -1); }
+
+std::vector<int> batch_variants() {
+    std::vector<int> out(kBClasses, -1);
+    const std::string dev = bdevice_name();
+    std::lock_guard<std::mutex> lock(g_bvar_mutex);
+    for (int c = 0; c < kBClasses; ++c) {
+        auto it = g_bvar.find({dev, c});
+        if (it != g_bvar.end()) out[c] = it->second;
+    }
+    return out;
+}
 
 void erot_solve_batched_gpu(regot_ctx* ctx, const regot_batch_desc* D, double reg, double tol,
                             int max_iter, regot_batch_result* res, double* cost, float* grad_x,
@@ -672,20 +945,27 @@ void erot_solve_batched_gpu(regot_ctx* ctx, const regot_batch_desc* D, double re
     // has halved, so that the last sweeps of a few slow problems do not
     // launch a CTA for every block of every problem.
     std::vector<int2> ritems[kBClasses], citems[kBClasses];
+    std::vector<int2> rtc[kBClasses], ctc[kBClasses];  // blocks of 128 (tensor-core sweeps)
     auto build_items = [&](const std::vector<int>& running) {
         std::vector<int> order(running);
         for (int c = 0; c < kBClasses; ++c) {
             ritems[c].clear();
             citems[c].clear();
+            rtc[c].clear();
+            ctc[c].clear();
         }
         std::stable_sort(order.begin(), order.end(), [&](int u, int v) { return hm[u] > hm[v]; });
-        for (int p : order)
+        for (int p : order) {
             for (int k = 0; k < cdiv(hn[p], kBItems); ++k)
                 ritems[cls[p]].push_back(make_int2(p, k));
+            for (int k = 0; k < cdiv(hn[p], kTcOwn); ++k) rtc[cls[p]].push_back(make_int2(p, k));
+        }
         std::stable_sort(order.begin(), order.end(), [&](int u, int v) { return hn[u] > hn[v]; });
-        for (int p : order)
+        for (int p : order) {
             for (int k = 0; k < cdiv(hm[p], kBItems); ++k)
                 citems[cls[p]].push_back(make_int2(p, k));
+            for (int k = 0; k < cdiv(hm[p], kTcOwn); ++k) ctc[cls[p]].push_back(make_int2(p, k));
+        }
     };
     {
         std::vector<int> all(P);
@@ -705,11 +985,13 @@ void erot_solve_batched_gpu(regot_ctx* ctx, const regot_batch_desc* D, double re
     upload_vec(dxo, xo, st);
     upload_vec(dyo, yo, st);
     upload_vec(dsc, hsc, st);
-    DBuf<int2> dri[kBClasses], dci[kBClasses];
+    DBuf<int2> dri[kBClasses], dci[kBClasses], drt[kBClasses], dct[kBClasses];
     auto upload_items = [&]() {
         for (int c = 0; c < kBClasses; ++c) {
             if (!ritems[c].empty()) upload_vec(dri[c], ritems[c], st);
             if (!citems[c].empty()) upload_vec(dci[c], citems[c], st);
+            if (!rtc[c].empty()) upload_vec(drt[c], rtc[c], st);
+            if (!ctc[c].empty()) upload_vec(dct[c], ctc[c], st);
         }
     };
     upload_items();
@@ -762,10 +1044,25 @@ void erot_solve_batched_gpu(regot_ctx* ctx, const regot_batch_desc* D, double re
     BatchDev B{dn.get(), dm.get(), dd.get(), dsc.get(), dxo.get(), dyo.get(), dro.get(),
                dco.get(), drbo.get(), X, Y, a, loga.get(), logb.get()};
     const float k2 = (float)(1.4426950408889634 / reg);
+    int use_tc[kBClasses] = {0, 0, 0};
+    configure_tc_sweep<false>();
+    configure_tc_sweep<true>();
+    auto launch_rows_class = [&](int q, int c, int tc) {
+        if (tc) {
+            k_bsweep_tc<false><<<(int)rtc[c].size(), 256, kTcSmem, st>>>(
+                B, drt[c].get(), AS[q].get(), BS.get(), A[q].get(), A[1 - q].get(),
+                AS[1 - q].get(), part.get(), done.get(), S, k2, reg, 1);
+            count_launch();
+            return true;
+        }
+        return false;
+    };
     auto launch_rows = [&](int q) {
         for (int c = 0; c < kBClasses; ++c) {
             const int ni = (int)ritems[c].size();
             if (!ni) continue;
+            if (use_tc[c] < -1) continue;
+            if (launch_rows_class(q, c, use_tc[c] == 1)) continue;
             const dim3 grid(ni), block(kBWarps * 32);
             if (c == 0)
                 k_brow<4><<<grid, block, 0, st>>>(B, dri[c].get(), AS[q].get(), BS.get(),
@@ -787,6 +1084,13 @@ void erot_solve_batched_gpu(regot_ctx* ctx, const regot_batch_desc* D, double re
         for (int c = 0; c < kBClasses; ++c) {
             const int ni = (int)citems[c].size();
             if (!ni) continue;
+            if (use_tc[c] == 1) {
+                k_bsweep_tc<true><<<(int)ctc[c].size(), 256, kTcSmem, st>>>(
+                    B, dct[c].get(), BS.get(), AS[q].get(), beta.get(), beta.get(), BS.get(),
+                    part.get(), done.get(), S, k2, reg, write_split);
+                count_launch();
+                continue;
+            }
             const dim3 grid(ni), block(kBWarps * 32);
             if (c == 0)
                 k_bcol<4><<<grid, block, 0, st>>>(B, dci[c].get(), AS[q].get(), BS.get(),
@@ -826,8 +1130,52 @@ void erot_solve_batched_gpu(regot_ctx* ctx, const regot_batch_desc* D, double re
 
     // beta = optimal_beta(alpha = 0) (sinkhorn_bcd.cpp:38-47): one column
     // half-sweep from zero duals, then the split grid from |beta|.
-    launch_cols(0, 0);
+    // Variant per class: forced, known for this device, or timed now (one
+    // row half-sweep of each variant from the current iterate; row sweeps
+    // write only the next-iterate buffers, so the solve is unaffected).
+    const int forced = g_bvar_force.load();
+    const std::string devname = bdevice_name();
+    for (int c = 0; c < kBClasses; ++c) {
+        if (forced >= 0) {
+            use_tc[c] = forced;
+            continue;
+        }
+        std::lock_guard<std::mutex> lock(g_bvar_mutex);
+        auto it = g_bvar.find({devname, c});
+        use_tc[c] = it != g_bvar.end() ? it->second : -1;
+    }
+    launch_cols(0, 0);  // the untuned classes run the CUDA-core kernels here
     regrid(0);
+    for (int c = 0; c < kBClasses; ++c) {
+        if (use_tc[c] >= 0) continue;
+        if (ritems[c].empty()) {
+            use_tc[c] = 0;
+            continue;
+        }
+        float ms[2] = {0.f, 0.f};
+        cudaEvent_t t0, t1;
+        REGOT_CUDA(cudaEventCreate(&t0));
+        REGOT_CUDA(cudaEventCreate(&t1));
+        for (int v = 0; v < 2; ++v) {
+            for (int rep = 0; rep < 2; ++rep) {  // warm, then timed
+                const int keep[kBClasses] = {use_tc[0], use_tc[1], use_tc[2]};
+                REGOT_CUDA(cudaEventRecord(t0, st));
+                if (!launch_rows_class(0, c, v)) {
+                    for (int k = 0; k < kBClasses; ++k) use_tc[k] = (k == c) ? 0 : -2;
+                    launch_rows(0);
+                    for (int k = 0; k < kBClasses; ++k) use_tc[k] = keep[k];
+                }
+                REGOT_CUDA(cudaEventRecord(t1, st));
+            }
+            REGOT_CUDA(cudaEventSynchronize(t1));
+            REGOT_CUDA(cudaEventElapsedTime(&ms[v], t0, t1));
+        }
+        cudaEventDestroy(t0);
+        cudaEventDestroy(t1);
+        use_tc[c] = ms[1] < ms[0] ? 1 : 0;
+        std::lock_guard<std::mutex> lock(g_bvar_mutex);
+        g_bvar[{devname, c}] = use_tc[c];
+    }
 
     // The sweeps: a graph whose only node is a conditional WHILE node; its
     // body is two sweeps (alpha ping-pongs between A[0] and A[1]) and k_bloop.
@@ -885,6 +1233,8 @@ void erot_solve_batched_gpu(regot_ctx* ctx, const regot_batch_desc* D, double re
         read_small(ctx, &hs, S, sizeof(hs), st);
         count_launch(body_kernels * (hs.loops - prev_loops));
         prev_loops = hs.loops;
+        if (hs.err)
+            throw Error(REGOT_ERR_TIMEOUT, "a tensor-core half-sweep gave up waiting for its MMAs");
         if (hs.active == 0) break;
         if (hs.loops >= hs.loop_cap) throw Error(REGOT_ERR_NUMERIC, "batched BCD did not terminate");
         bool acted = false;

@@ -395,8 +395,13 @@ void sinkhorn_newton_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double t
         read_small(ctx, &hs, S, sizeof(hs), st);
         const double thresh = theta * hs.gtd;
         double step = 1.0, accepted = -1.0;
-        for (int k0 = 0; k0 < nlinesearch && accepted < 0.0; k0 += 4) {
-            const int ns = std::min(4, nlinesearch - k0);
+        // The first pass tries the full step alone (accepted in most Newton
+        // iterations; one phi per entry instead of four), later passes four
+        // steps at a time. The accepted step is the reference's first
+        // acceptable one either way.
+        for (int k0 = 0; k0 < nlinesearch && accepted < 0.0;) {
+            const int ns = std::min(k0 == 0 ? 1 : 4, nlinesearch - k0);
+            k0 += ns;
             double steps[4] = {0, 0, 0, 0};
             for (int s = 0; s < ns; ++s) steps[s] = step * std::pow(kappa, s);
             PassParams q = pl;

@@ -43,6 +43,12 @@ void sqeuclid_gpu(const void* x, const void* y, int n, int m, int d, double scal
 void erot_contract_tc(regot_ctx* ctx, regot_dproblem* P, double reg, const double* d_gamma,
                       const double* d_u, const double* d_W, const double* d_Y, int d, bool cols,
                       double* d_sums, double* d_Z);
+// Half-sweep variant of the batched BCD per dimension class (erot_batch.cu):
+// force one for every class (0 CUDA cores, 1 tensor cores, -1 timed
+// choice; returns the previous forced value), and the timed choices made on
+// this device so far (-1: none yet) for the classes d <= 4, 8, 16.
+int force_batch_variant(int v);
+std::vector<int> batch_variants();
 // Batched BCD over point-cloud problems (erot_batch.cu).
 // cost, grad_x, grad_y (host, optional): each problem's regularised OT cost
 // and its gradients with respect to the points (FP32, like the points), at

@@ -153,3 +153,54 @@ def test_batched_backward_at_max_iter_iterates():
             gy = 2 * sc[p] * (T.sum(0)[:, None] * y - T.T @ x)
             np.testing.assert_allclose(r.grad_x[p], gx, rtol=0, atol=3e-4 * np.abs(gx).max())
             np.testing.assert_allclose(r.grad_y[p], gy, rtol=0, atol=3e-4 * np.abs(gy).max())
+
+
+def _force(v):
+    from regot import _lib
+
+    return _lib.load().regot_force_batch_variant(v)
+
+
+@pytest.mark.parametrize("scaled", [True, False])
+def test_batched_tensor_core_cost_tile(scaled):
+    """The tensor-core variant of the half-sweeps (cost tile x y' on tcgen05
+    in TF32x3, M = s (|x|^2 + |y|^2 - 2 x.y)) against the CUDA-core direct
+    differences and the FP64 oracle. The expansion carries an absolute error
+    of about 2^-21 s (|x|^2 + |y|^2) in M, i.e. about 1e-6 s d; at reg 0.05
+    that moves T by up to about 1e-4 relative for the unscaled costs of
+    d = 16 and the duals by a few 1e-6, which the bounds below state.
+    Fixed-iteration runs compare the two variants without the stopping test;
+    converged runs check the marginal error of the tensor-core duals in FP64
+    on the FP64 cost."""
+    reg, tol = 0.05, 1e-6
+    xs, ys, as_, bs, sc = _batch(20, seed=8, nmin=40, nmax=400, dims=(3, 6, 8, 11, 16))
+    if not scaled:
+        sc = [1.0] * len(sc)
+    old = _force(1)
+    try:
+        r_tc = regot.sinkhorn_bcd_batched(xs, ys, as_, bs, reg, tol=1e-14, max_iter=6,
+                                          cost_scale=sc)
+        _force(0)
+        r_cc = regot.sinkhorn_bcd_batched(xs, ys, as_, bs, reg, tol=1e-14, max_iter=6,
+                                          cost_scale=sc)
+        _force(1)
+        r_conv = regot.sinkhorn_bcd_batched(xs, ys, as_, bs, reg, tol=tol, max_iter=20000,
+                                            cost_scale=sc)
+    finally:
+        _force(old)
+    worst = 0.0
+    for p in range(len(xs)):
+        assert r_tc.niter[p] == r_cc.niter[p] == 6
+        d = xs[p].shape[1]
+        # the cost tile's absolute error (~1e-6 s d) passes into the duals
+        # about one to one; 64x headroom
+        bound = 6.4e-5 * sc[p] * d
+        err = np.abs(r_tc.duals[p] - r_cc.duals[p]).max()
+        worst = max(worst, err / bound)
+        assert err <= bound, (p, err, bound)
+        M = _cost64(xs[p], ys[p], sc[p])
+        assert r_conv.mar_errs[p] < tol, (p, r_conv.mar_errs[p])
+        _, g = O.erot_dual_obj_grad(M, as_[p], bs[p], reg, r_conv.duals[p])
+        # marginal error on the FP64 cost: tol plus the cost tile's perturbation
+        assert np.linalg.norm(g) < tol + 2e-4 * sc[p] * d, (p, np.linalg.norm(g))
+    print(f"tensor-core vs CUDA-core duals after 6 sweeps: worst error / bound = {worst:.3f}")
