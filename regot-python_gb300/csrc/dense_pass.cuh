@@ -466,8 +466,15 @@ __global__ void __launch_bounds__(kThreads, PassCfg<CFG>::kMinBlocks) dense_pass
             ok_wait = ok_wait && got;
         }
         // ---- per-column parameters of this slab (only what OP uses) ----
-        TM ch[LC], clk[LC], cxv[op_uses_cx(OP) ? LC : 1], cx2v[op_uses_cx2(OP) ? LC : 1],
-            cdv[op_uses_cd(OP) ? LC : 1];
+        // The mixed HVP reads its CG-vector entries from the staged column
+        // parameters in the element loop instead of holding 16 more
+        // registers (with them the pass spilled at 128 registers a thread).
+        constexpr bool CX_SMEM = MIXED && OP == OP_E_HVP;
+        // Likewise the line-search direction of the mixed trial passes.
+        constexpr bool CD_SMEM = MIXED && op_uses_cd(OP);
+        TM ch[LC], clk[LC], cxv[(op_uses_cx(OP) && !CX_SMEM) ? LC : 1],
+            cx2v[op_uses_cx2(OP) ? LC : 1],
+            cdv[(op_uses_cd(OP) && !CD_SMEM) ? LC : 1];
         double cbd[ROOT ? LC : 1];
         bool cvalid[LC];
 #pragma unroll
@@ -486,16 +493,9 @@ __global__ void __launch_bounds__(kThreads, PassCfg<CFG>::kMinBlocks) dense_pass
                 ch[q] = ok ? c.x : -INFINITY;
                 // EROT folds the exp2 scale into the low part: lo * kexp.
                 clk[q] = ok ? (EROT ? __fmul_rn(c.y, kexp) : c.y) : 0.f;
-                if constexpr (op_uses_cx(OP)) cxv[q] = c.z;
+                if constexpr (op_uses_cx(OP) && !CX_SMEM) cxv[q] = c.z;
                 if constexpr (op_uses_cx2(OP)) cx2v[q] = c.w;
-                if constexpr (op_uses_cd(OP)) {
-                    // entries past the last group of four were not staged
-                    const int jj = j - c0;
-                    const int ncol = (m - c0) < CW ? (m - c0) : CW;
-                    cdv[q] = (ok && p.cdsplit)
-                                 ? (jj < (ncol / 4) * 4 ? s_cdp[(k & 1) * CW + jj] : p.cdsplit[j])
-                                 : 0.f;
-                }
+
             } else {
                 ch[q] = ok ? ((p.cb && op_needs_cb(OP)) ? (TM)p.cb[j] : (TM)0) : (TM)(-INFINITY);
                 clk[q] = 0;
@@ -504,6 +504,18 @@ __global__ void __launch_bounds__(kThreads, PassCfg<CFG>::kMinBlocks) dense_pass
                 if constexpr (op_uses_cd(OP)) cdv[q] = (ok && p.cd) ? (TM)p.cd[j] : (TM)0;
             }
         }
+        // direction entry of the lane's column q (mixed: from the staged
+        // copy; entries past the last group of four were not staged)
+        auto cd_at = [&](int q) -> TM {
+            if constexpr (CD_SMEM) {
+                const int jj = ((q / VW) * 32 + lane) * VW + (q % VW);
+                const int ncol = (m - c0) < CW ? (m - c0) : CW;
+                if (jj >= ncol || !p.cdsplit) return (TM)0;
+                return jj < (ncol / 4) * 4 ? s_cdp[(k & 1) * CW + jj] : p.cdsplit[c0 + jj];
+            } else {
+                return cdv[q];
+            }
+        };
         Acc cacc[NCa][LC];
 #pragma unroll
         for (int c = 0; c < NCa; ++c)
@@ -615,7 +627,9 @@ __global__ void __launch_bounds__(kThreads, PassCfg<CFG>::kMinBlocks) dense_pass
                                 cacc[0][q + 1] = c.y;
                             }
                             if constexpr (OP == OP_E_HVP) {
-                                racc2 = __ffma2_rn(T, make_float2(cxv[q], cxv[q + 1]), racc2);
+                                const float4* cpar = s_colp + (k & 1) * CW +
+                                                     ((q / VW) * 32 + lane) * VW + q % VW;
+                                racc2 = __ffma2_rn(T, make_float2(cpar[0].z, cpar[1].z), racc2);
                                 const float2 c = __ffma2_rn(T, make_float2(rxv, rxv),
                                                             make_float2(cacc[0][q], cacc[0][q + 1]));
                                 cacc[0][q] = c.x;
@@ -674,7 +688,7 @@ __global__ void __launch_bounds__(kThreads, PassCfg<CFG>::kMinBlocks) dense_pass
                                 racc[0] += T * cxv[q];
                                 cacc[0][q] += T * rxv;
                             } else if constexpr (OP == OP_E_LS) {
-                                const TM w = (rdv + cdv[q]) * inv_reg;
+                                const TM w = (rdv + cd_at(q)) * inv_reg;
     #pragma unroll
                                 for (int s2 = 0; s2 < 4; ++s2)
                                     if (s2 < nsteps) tot[s2] += T * expm1_minus_x(steps[s2] * w);
@@ -685,7 +699,7 @@ __global__ void __launch_bounds__(kThreads, PassCfg<CFG>::kMinBlocks) dense_pass
                                 cacc[0][q] += T;
                                 if (cvalid[q]) {
                                     // T e^(-s w) is T at the base point
-                                    const TM sw = steps[0] * ((rdv + cdv[q]) * inv_reg);
+                                    const TM sw = steps[0] * ((rdv + cd_at(q)) * inv_reg);
                                     TM back;
                                     if constexpr (MIXED) back = ex2_approx(-sw * 1.44269504f);
                                     else back = exp(-sw);
@@ -729,7 +743,7 @@ __global__ void __launch_bounds__(kThreads, PassCfg<CFG>::kMinBlocks) dense_pass
                             } else if constexpr (OP == OP_Q_GRADLS) {
                             // objective change along s w without cancellation:
                             // 0.5 (Dn^2 - D^2) - s w D >= 0 in every case
-                            const TM sw = steps[0] * (rdv + cdv[q]);
+                            const TM sw = steps[0] * (rdv + cd_at(q));
                             const TM Cn = arg + sw;
                             const TM Dn = Cn > (TM)0 ? Cn : (TM)0;
                             TM rem;

@@ -530,7 +530,9 @@ __global__ void __launch_bounds__(256, 1) k_bsweep_tc(
     const uint32_t ah = sm100::smem_u32(Ahi), al = sm100::smem_u32(Alo);
     const uint32_t bh = sm100::smem_u32(Bhi), bl = sm100::smem_u32(Blo);
 
-    float mx = -INFINITY, sm = 0.f;
+    // running log-sum-exp: one reference point, four partial sums (four
+    // independent add chains per thread)
+    float mx = -INFINITY, sm4[4] = {0.f, 0.f, 0.f, 0.f};
     bool failed = false;
     int tile = 0;
     for (int j0 = 0; j0 < n_oth; j0 += kTcTile, ++tile) {
@@ -571,23 +573,31 @@ __global__ void __launch_bounds__(256, 1) k_bsweep_tc(
         }
         sm100::tc_fence_after();
         const uint32_t trow = tmem + ((uint32_t)(32 * (warp & 3)) << 16);
+        const int cnt = min(kTcTile, n_oth - j0);  // valid columns of the tile
 #pragma unroll 1
         for (int x = 0; x < 8; ++x) {
             const int c0 = half * 128 + 16 * x;
             float dv[16];
             sm100::tmem_ld16(trow + (uint32_t)c0, dv);
-            if (!own_ok) continue;
+            if (!own_ok || c0 >= cnt) continue;
+            float z[16];
+            float zmax = -INFINITY;
 #pragma unroll
             for (int e = 0; e < 16; ++e) {
-                const int jj = c0 + e;
-                if (j0 + jj < n_oth) {
-                    const float4 q = sp[jj];
-                    const float Mij = __fmul_rn(__fmaf_rn(-2.f, dv[e], __fadd_rn(own_sq, q.x)), sc);
-                    const float ex = __fadd_rn(__fadd_rn(oh, q.y), -Mij);
-                    const float z = __fmaf_rn(ex, k2, __fadd_rn(olk, q.z));
-                    lse_add(mx, sm, z);
-                }
+                const float4 q = sp[c0 + e];
+                const float Mij = __fmul_rn(__fmaf_rn(-2.f, dv[e], __fadd_rn(own_sq, q.x)), sc);
+                const float ex = __fadd_rn(__fadd_rn(oh, q.y), -Mij);
+                z[e] = (c0 + e < cnt) ? __fmaf_rn(ex, k2, __fadd_rn(olk, q.z)) : -INFINITY;
+                zmax = fmaxf(zmax, z[e]);
             }
+            if (zmax > mx + kLseSlack) {  // move the reference point (rare after the first)
+                const float f = bex2(mx - zmax);
+#pragma unroll
+                for (int h = 0; h < 4; ++h) sm4[h] *= f;
+                mx = zmax;
+            }
+#pragma unroll
+            for (int e = 0; e < 16; ++e) sm4[e & 3] += bex2(z[e] - mx);
         }
         sm100::tc_fence_before();
         __syncthreads();
@@ -605,6 +615,7 @@ __global__ void __launch_bounds__(256, 1) k_bsweep_tc(
         return;
     }
     if (warp == 0) sm100::tmem_dealloc(tmem, kTcTmemCols);
+    float sm = (sm4[0] + sm4[1]) + (sm4[2] + sm4[3]);
     // merge the two column halves of each owner
     if (half == 1) {
         s_mx[r] = mx;
@@ -1130,9 +1141,10 @@ void erot_solve_batched_gpu(regot_ctx* ctx, const regot_batch_desc* D, double re
 
     // beta = optimal_beta(alpha = 0) (sinkhorn_bcd.cpp:38-47): one column
     // half-sweep from zero duals, then the split grid from |beta|.
-    // Variant per class: forced, known for this device, or timed now (one
-    // row half-sweep of each variant from the current iterate; row sweeps
-    // write only the next-iterate buffers, so the solve is unaffected).
+    // Variant per class: forced, known for this device, or timed now (a row
+    // and a column half-sweep of each variant from the current iterate: the
+    // row sweeps write only the next-iterate buffers and the column sweeps a
+    // scratch copy of beta, so the solve is unaffected).
     const int forced = g_bvar_force.load();
     const std::string devname = bdevice_name();
     for (int c = 0; c < kBClasses; ++c) {
@@ -1156,15 +1168,41 @@ void erot_solve_batched_gpu(regot_ctx* ctx, const regot_batch_desc* D, double re
         cudaEvent_t t0, t1;
         REGOT_CUDA(cudaEventCreate(&t0));
         REGOT_CUDA(cudaEventCreate(&t1));
+        // the column half-sweeps update a scratch copy of beta (write_split
+        // 0), so the timing leaves the solve's state as it was
+        DBuf<double> beta_t(NC, st);
+        const int nr = (int)ritems[c].size(), nc = (int)citems[c].size();
         for (int v = 0; v < 2; ++v) {
             for (int rep = 0; rep < 2; ++rep) {  // warm, then timed
-                const int keep[kBClasses] = {use_tc[0], use_tc[1], use_tc[2]};
+                d2d(beta_t.get(), beta.get(), NC * sizeof(double), st);
                 REGOT_CUDA(cudaEventRecord(t0, st));
-                if (!launch_rows_class(0, c, v)) {
-                    for (int k = 0; k < kBClasses; ++k) use_tc[k] = (k == c) ? 0 : -2;
-                    launch_rows(0);
-                    for (int k = 0; k < kBClasses; ++k) use_tc[k] = keep[k];
+                if (v == 1) {
+                    launch_rows_class(0, c, 1);
+                    k_bsweep_tc<true><<<(int)ctc[c].size(), 256, kTcSmem, st>>>(
+                        B, dct[c].get(), BS.get(), AS[1].get(), beta_t.get(), beta_t.get(),
+                        BS.get(), part.get(), done.get(), S, k2, reg, 0);
+                } else if (c == 0) {
+                    k_brow<4><<<nr, kBWarps * 32, 0, st>>>(B, dri[c].get(), AS[0].get(), BS.get(),
+                                                            A[0].get(), A[1].get(), AS[1].get(),
+                                                            part.get(), done.get(), S, k2, reg);
+                    k_bcol<4><<<nc, kBWarps * 32, 0, st>>>(B, dci[c].get(), AS[1].get(), BS.get(),
+                                                            beta_t.get(), done.get(), S, k2, reg, 0);
+                } else if (c == 1) {
+                    k_brow<8><<<nr, kBWarps * 32, 0, st>>>(B, dri[c].get(), AS[0].get(), BS.get(),
+                                                            A[0].get(), A[1].get(), AS[1].get(),
+                                                            part.get(), done.get(), S, k2, reg);
+                    k_bcol<8><<<nc, kBWarps * 32, 0, st>>>(B, dci[c].get(), AS[1].get(), BS.get(),
+                                                            beta_t.get(), done.get(), S, k2, reg, 0);
+                } else {
+                    k_brow<16><<<nr, kBWarps * 32, 0, st>>>(B, dri[c].get(), AS[0].get(),
+                                                             BS.get(), A[0].get(), A[1].get(),
+                                                             AS[1].get(), part.get(), done.get(), S,
+                                                             k2, reg);
+                    k_bcol<16><<<nc, kBWarps * 32, 0, st>>>(B, dci[c].get(), AS[1].get(),
+                                                             BS.get(), beta_t.get(), done.get(), S,
+                                                             k2, reg, 0);
                 }
+                count_launch(2);
                 REGOT_CUDA(cudaEventRecord(t1, st));
             }
             REGOT_CUDA(cudaEventSynchronize(t1));

@@ -109,7 +109,7 @@ __global__ void k_tc_tile_b(const double* __restrict__ Y, int ldy, int dk, int K
 }
 
 template <bool COLS, bool ADJ>
-__global__ void __launch_bounds__(kTcThreads) k_contract_tc(
+__global__ void __launch_bounds__(kTcThreads, 3) k_contract_tc(
     const float* __restrict__ M, long long ldm, int n, int m, const float4* __restrict__ rs,
     const float4* __restrict__ cs, float kexp, float inv_reg, const double* __restrict__ u,
     const double* __restrict__ W, const __nv_bfloat16* __restrict__ Bt, int nch, int per,
@@ -178,6 +178,41 @@ __global__ void __launch_bounds__(kTcThreads) k_contract_tc(
         }
     }
 
+    // M values of a chunk for this thread (row mode: two adjacent columns of
+    // 8 rows; column mode: one column of 8 row pairs in the rotated order),
+    // loaded one chunk ahead so that the loads of chunk k + 1 are in flight
+    // while chunk k's tile is formed and multiplied.
+    auto load_m = [&](int c, float2 (&mv)[8]) {
+        if constexpr (!COLS) {
+            const int j = c * kTcKC + 2 * (lane & 15);
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+                const int i = o0 + warp * 16 + 2 * t + (lane >> 4);
+                mv[t] = make_float2(0.f, 0.f);
+                if (i < n) {
+                    const float* row = M + (long long)i * ldm + j;
+                    if (j + 1 < m) mv[t] = *reinterpret_cast<const float2*>(row);
+                    else if (j < m) mv[t].x = row[0];
+                }
+            }
+        } else {
+            const int j = o0 + 32 * (warp & 3) + lane;
+            const bool jv = j < m;
+            const int g8 = lane >> 3;
+            const int kbase = 16 * (warp >> 2);
+#pragma unroll
+            for (int pp = 0; pp < 8; ++pp) {
+                const int q = (pp & ~3) | ((pp + g8) & 3);
+                const int i = c * kTcKC + kbase + 2 * q;
+                mv[pp] = make_float2(0.f, 0.f);
+                if (jv && i < n) mv[pp].x = M[(long long)i * ldm + j];
+                if (jv && i + 1 < n) mv[pp].y = M[(long long)(i + 1) * ldm + j];
+            }
+        }
+    };
+    float2 mv[8], mv_next[8];
+    load_m(c0, mv);
+
     bool failed = false;
     int ncommit = 0;        // thread 0: chunks whose MMAs were committed
     int bpending = -1;      // thread 0: chunk whose B copy it gave up waiting for
@@ -214,17 +249,7 @@ __global__ void __launch_bounds__(kTcThreads) k_contract_tc(
                     clk[e] = __fmul_rn(cc.y, kexp);
                     if constexpr (ADJ) cu[e] = u[n + j + e];
                 }
-            float2 mv[8];
-#pragma unroll
-            for (int t = 0; t < 8; ++t) {
-                const int i = o0 + warp * 16 + 2 * t + (lane >> 4);
-                mv[t] = make_float2(0.f, 0.f);
-                if (i < n) {
-                    const float* row = M + (long long)i * ldm + j;
-                    if (cv[1]) mv[t] = *reinterpret_cast<const float2*>(row);
-                    else if (cv[0]) mv[t].x = row[0];
-                }
-            }
+            if (it + 1 < nloc) load_m(c + 1, mv_next);
 #pragma unroll
             for (int t = 0; t < 8; ++t) {
                 const int r = warp * 16 + 2 * t + (lane >> 4);
@@ -253,15 +278,7 @@ __global__ void __launch_bounds__(kTcThreads) k_contract_tc(
             const bool jv = j < m;
             const int g8 = lane >> 3;
             const int kbase = 16 * (warp >> 2);
-            float2 mv[8];
-#pragma unroll
-            for (int pp = 0; pp < 8; ++pp) {
-                const int q = (pp & ~3) | ((pp + g8) & 3);
-                const int i = c * kTcKC + kbase + 2 * q;
-                mv[pp] = make_float2(0.f, 0.f);
-                if (jv && i < n) mv[pp].x = M[(long long)i * ldm + j];
-                if (jv && i + 1 < n) mv[pp].y = M[(long long)(i + 1) * ldm + j];
-            }
+            if (it + 1 < nloc) load_m(c + 1, mv_next);
 #pragma unroll
             for (int pp = 0; pp < 8; ++pp) {
                 const int q = (pp & ~3) | ((pp + g8) & 3);
@@ -295,6 +312,8 @@ __global__ void __launch_bounds__(kTcThreads) k_contract_tc(
                 *reinterpret_cast<uint32_t*>(Alo + off) = lo;
             }
         }
+#pragma unroll
+        for (int t = 0; t < 8; ++t) mv[t] = mv_next[t];
         fence_proxy_async_smem();
         __syncthreads();
         if (tid == 0) {
@@ -415,8 +434,9 @@ void erot_contract_tc(regot_ctx* ctx, regot_dproblem* P, double reg, const doubl
     }
     const int nch = cdiv(K, kTcKC);
     const int nob = cdiv(nown, kTcOwners);
+    // one wave of 3 CTAs per SM (their shared memory allows three)
     const int target = 3 * device_sm_count();
-    int S = std::max(1, std::min(nch, cdiv(target, nob)));
+    int S = std::max(1, std::min(nch, target / nob));
     const int per = cdiv(nch, S);
     S = cdiv(nch, per);
     const int owners_pad = nob * kTcOwners;
