@@ -466,15 +466,13 @@ __global__ void __launch_bounds__(kThreads, PassCfg<CFG>::kMinBlocks) dense_pass
             ok_wait = ok_wait && got;
         }
         // ---- per-column parameters of this slab (only what OP uses) ----
-        // The mixed HVP reads its CG-vector entries from the staged column
-        // parameters in the element loop instead of holding 16 more
-        // registers (with them the pass spilled at 128 registers a thread).
-        constexpr bool CX_SMEM = MIXED && OP == OP_E_HVP;
-        // Likewise the line-search direction of the mixed trial passes.
-        constexpr bool CD_SMEM = MIXED && op_uses_cd(OP);
-        TM ch[LC], clk[LC], cxv[(op_uses_cx(OP) && !CX_SMEM) ? LC : 1],
-            cx2v[op_uses_cx2(OP) ? LC : 1],
-            cdv[(op_uses_cd(OP) && !CD_SMEM) ? LC : 1];
+        // Per-column vectors stay in registers, loaded once per tile. Reading
+        // them from the staged parameters in the element loop instead (no
+        // spills at 128 registers) was measured slower: a lane's columns are
+        // 16 bytes apart in the staged arrays, so those reads conflict on
+        // the shared-memory banks (HVP 0.64 -> 0.26 of peak).
+        TM ch[LC], clk[LC], cxv[op_uses_cx(OP) ? LC : 1], cx2v[op_uses_cx2(OP) ? LC : 1],
+            cdv[op_uses_cd(OP) ? LC : 1];
         double cbd[ROOT ? LC : 1];
         bool cvalid[LC];
 #pragma unroll
@@ -493,9 +491,16 @@ __global__ void __launch_bounds__(kThreads, PassCfg<CFG>::kMinBlocks) dense_pass
                 ch[q] = ok ? c.x : -INFINITY;
                 // EROT folds the exp2 scale into the low part: lo * kexp.
                 clk[q] = ok ? (EROT ? __fmul_rn(c.y, kexp) : c.y) : 0.f;
-                if constexpr (op_uses_cx(OP) && !CX_SMEM) cxv[q] = c.z;
+                if constexpr (op_uses_cx(OP)) cxv[q] = c.z;
                 if constexpr (op_uses_cx2(OP)) cx2v[q] = c.w;
-
+                if constexpr (op_uses_cd(OP)) {
+                    // entries past the last group of four were not staged
+                    const int jj = j - c0;
+                    const int ncol = (m - c0) < CW ? (m - c0) : CW;
+                    cdv[q] = (ok && p.cdsplit)
+                                 ? (jj < (ncol / 4) * 4 ? s_cdp[(k & 1) * CW + jj] : p.cdsplit[j])
+                                 : 0.f;
+                }
             } else {
                 ch[q] = ok ? ((p.cb && op_needs_cb(OP)) ? (TM)p.cb[j] : (TM)0) : (TM)(-INFINITY);
                 clk[q] = 0;
@@ -504,18 +509,7 @@ __global__ void __launch_bounds__(kThreads, PassCfg<CFG>::kMinBlocks) dense_pass
                 if constexpr (op_uses_cd(OP)) cdv[q] = (ok && p.cd) ? (TM)p.cd[j] : (TM)0;
             }
         }
-        // direction entry of the lane's column q (mixed: from the staged
-        // copy; entries past the last group of four were not staged)
-        auto cd_at = [&](int q) -> TM {
-            if constexpr (CD_SMEM) {
-                const int jj = ((q / VW) * 32 + lane) * VW + (q % VW);
-                const int ncol = (m - c0) < CW ? (m - c0) : CW;
-                if (jj >= ncol || !p.cdsplit) return (TM)0;
-                return jj < (ncol / 4) * 4 ? s_cdp[(k & 1) * CW + jj] : p.cdsplit[c0 + jj];
-            } else {
-                return cdv[q];
-            }
-        };
+        auto cd_at = [&](int q) -> TM { return cdv[q]; };
         Acc cacc[NCa][LC];
 #pragma unroll
         for (int c = 0; c < NCa; ++c)
@@ -627,9 +621,7 @@ __global__ void __launch_bounds__(kThreads, PassCfg<CFG>::kMinBlocks) dense_pass
                                 cacc[0][q + 1] = c.y;
                             }
                             if constexpr (OP == OP_E_HVP) {
-                                const float4* cpar = s_colp + (k & 1) * CW +
-                                                     ((q / VW) * 32 + lane) * VW + q % VW;
-                                racc2 = __ffma2_rn(T, make_float2(cpar[0].z, cpar[1].z), racc2);
+                                racc2 = __ffma2_rn(T, make_float2(cxv[q], cxv[q + 1]), racc2);
                                 const float2 c = __ffma2_rn(T, make_float2(rxv, rxv),
                                                             make_float2(cacc[0][q], cacc[0][q + 1]));
                                 cacc[0][q] = c.x;
@@ -638,12 +630,64 @@ __global__ void __launch_bounds__(kThreads, PassCfg<CFG>::kMinBlocks) dense_pass
                         }
                         racc[0] = racc2.x + racc2.y;
                     }
+                    // QROT objective / gradient and line-search trial, two
+                    // columns per packed FP32x2 instruction: the argument is
+                    // formed in the scalar path's order, and the relu, the
+                    // trial shift and the second-order remainder of the
+                    // objective change follow it per component.
+                    constexpr bool QPAIRED = MIXED && (OP == OP_Q_GRAD || OP == OP_Q_GRADLS);
+                    if constexpr (QPAIRED) {
+                        const float2 rh2 = make_float2(rh, rh), rl2 = make_float2(rlk, rlk);
+                        const float2 neg1 = make_float2(-1.f, -1.f), half2 = make_float2(0.5f, 0.5f);
+                        const float2 st2 = make_float2(steps[0], steps[0]), rd2 = make_float2(rdv, rdv);
+                        float2 racc2 = make_float2(0.f, 0.f), t0 = make_float2(0.f, 0.f),
+                               t1 = make_float2(0.f, 0.f);
+    #pragma unroll
+                        for (int q = 0; q < LC; q += 2) {
+                            const float2 mv2 = make_float2(Vec<TM>::get(mv[q / VW], q % VW),
+                                                           Vec<TM>::get(mv[q / VW], (q + 1) % VW));
+                            float2 sv = __fadd2_rn(rh2, make_float2(ch[q], ch[q + 1]));
+                            sv = __ffma2_rn(mv2, neg1, sv);
+                            const float2 arg =
+                                __fadd2_rn(sv, __fadd2_rn(rl2, make_float2(clk[q], clk[q + 1])));
+                            if constexpr (OP == OP_Q_GRAD) {
+                                const float2 D = make_float2(fmaxf(arg.x, 0.f), fmaxf(arg.y, 0.f));
+                                racc2 = __fadd2_rn(racc2, D);
+                                const float2 c = __fadd2_rn(make_float2(cacc[0][q], cacc[0][q + 1]), D);
+                                cacc[0][q] = c.x;
+                                cacc[0][q + 1] = c.y;
+                                t0 = __ffma2_rn(D, D, t0);
+                            } else {
+                                const float2 sw =
+                                    __fmul2_rn(st2, __fadd2_rn(rd2, make_float2(cd_at(q), cd_at(q + 1))));
+                                const float2 Cn = __fadd2_rn(arg, sw);
+                                const float2 Dn = make_float2(fmaxf(Cn.x, 0.f), fmaxf(Cn.y, 0.f));
+                                // 0.5 (Dn^2 - D^2) - s w D >= 0 in every case
+                                const float2 ra = __fmul2_rn(half2, __fmul2_rn(sw, sw));
+                                const float2 rb = __fmul2_rn(make_float2(-arg.x, -arg.y),
+                                                             __ffma2_rn(half2, arg, sw));
+                                const float2 rc = __fmul2_rn(half2, __fmul2_rn(Cn, Cn));
+                                const float2 rem = make_float2(
+                                    arg.x > 0.f ? (Cn.x > 0.f ? ra.x : rb.x) : (Cn.x > 0.f ? rc.x : 0.f),
+                                    arg.y > 0.f ? (Cn.y > 0.f ? ra.y : rb.y) : (Cn.y > 0.f ? rc.y : 0.f));
+                                racc2 = __fadd2_rn(racc2, Dn);
+                                const float2 c = __fadd2_rn(make_float2(cacc[0][q], cacc[0][q + 1]), Dn);
+                                cacc[0][q] = c.x;
+                                cacc[0][q + 1] = c.y;
+                                t0 = __ffma2_rn(Dn, Dn, t0);
+                                t1 = __fadd2_rn(t1, rem);
+                            }
+                        }
+                        racc[0] = racc2.x + racc2.y;
+                        tot[0] += t0.x + t0.y;
+                        if constexpr (OP == OP_Q_GRADLS) tot[1] += t1.x + t1.y;
+                    }
                     double pv[VW];  // plan values of one vector (plan passes)
                     (void)pv;
                     Acc rchunk[2] = {(Acc)0, (Acc)0};  // this row's averaged-plan totals
                     (void)rchunk;
     #pragma unroll
-                    for (int q = 0; q < (PAIRED ? 0 : LC); ++q) {
+                    for (int q = 0; q < ((PAIRED || QPAIRED) ? 0 : LC); ++q) {
                         const TM mval = Vec<TM>::get(mv[q / VW], q % VW);
                         if constexpr (OP == OP_E_ROWMAX) {
                             TM a;

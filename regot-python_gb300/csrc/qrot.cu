@@ -30,6 +30,7 @@
 #include <cfloat>
 #include <cmath>
 #include <cstring>
+#include <map>
 #include <vector>
 
 #include "device_util.cuh"
@@ -1046,7 +1047,9 @@ void qrot_lbfgs_dual_device(regot_ctx* ctx, regot_dproblem* P, double reg, doubl
 
     // Merge of the last pass at x into grad, plus the record; returns after
     // the record has reached the host.
-    auto merge = [&](int op, int nt, const double* x, double* g) {
+    // Merge of the last pass at x into grad and the record, and its copy to
+    // the host (not waited for).
+    auto merge_launch = [&](int op, int nt, const double* x, double* g) {
         const int blocks = pass_blocks(op, mixed, n, m);
         if (mixed)
             k_lb_merge<float><<<gN, kLbBlock, 0, st>>>(
@@ -1062,20 +1065,95 @@ void qrot_lbfgs_dual_device(regot_ctx* ctx, regot_dproblem* P, double reg, doubl
                 dscal.get());
         count_launch();
         REGOT_CHECK_LAUNCH();
-        E.add_passes(1);
         d2h(hs, dscal.get(), sizeof(LbScal), st);
-        sync(st);
     };
-    // f and grad at x (the Q_GRAD pass), as Problem::dual_obj_grad.
-    auto eval_at = [&](const double* x, double* g) {
+    // f and grad at x (the Q_GRAD pass), as Problem::dual_obj_grad: enqueued.
+    auto eval_launch = [&](const double* x, double* g) {
         ops.maxabs(x, N, nullptr, 0, grid.get());
         PassParams p = ops.base_params();
         p.ra = x;
         p.cb = x + n;
         p.grid = grid.get();
         ops.pass(OP_Q_GRAD, p);
-        merge(OP_Q_GRAD, 1, x, g);
+        merge_launch(OP_Q_GRAD, 1, x, g);
+    };
+    auto eval_at = [&](const double* x, double* g) {
+        eval_launch(x, g);
+        sync(st);
+        E.add_passes(1);
         return 0.5 * hs->sq - reg * hs->dab;
+    };
+    // Trial at xp + s drt into buffers (xt, gt): the axpy, the trial pass
+    // (mixed: OP_Q_GRADLS from the split of xp and drt, made here when
+    // `split` is set; FP64: OP_Q_GRAD at the trial point) and the merge;
+    // enqueued, not waited for.
+    auto trial_launch = [&](int xpi, int xti, int gti, double s, bool split) {
+        k_lb_axpy<<<gN, kLbBlock, 0, st>>>(xbuf(xpi), drt.get(), s, N, xbuf(xti));
+        count_launch();
+        if (mixed) {
+            PassParams p = ops.base_params();
+            p.ra = xbuf(xpi);
+            p.cb = xbuf(xpi) + n;
+            p.rd = drt.get();
+            p.cd = drt.get() + n;
+            p.steps[0] = s;
+            p.nsteps = 1;
+            p.grid = grid.get();
+            if (split) {
+                ops.maxabs(xbuf(xpi), N, nullptr, 0, grid.get());
+                ops.pass(OP_Q_GRADLS, p);
+            } else {
+                ops.pass_presplit(OP_Q_GRADLS, p);
+            }
+            merge_launch(OP_Q_GRADLS, 2, xbuf(xti), gbuf(gti));
+        } else {
+            eval_launch(xbuf(xti), gbuf(gti));
+        }
+    };
+    // From the second iteration on, the correction pair, the new direction
+    // and the first trial of the next line search (step 1, base = the
+    // accepted point) are the same kernels every iteration: one CUDA graph
+    // per assignment of the rotating buffers, captured on first use.
+    std::map<int, cudaGraphExec_t> iter_graphs;
+    long long iter_graph_kernels = 0;
+    struct GraphSet {
+        std::map<int, cudaGraphExec_t>& g;
+        ~GraphSet() {
+            for (auto& kv : g) cudaGraphExecDestroy(kv.second);
+        }
+    } graph_set{iter_graphs};
+    auto iter_graph = [&](int xi, int gi, int xpi, int gpi) {
+        const int key = ((xi * 3 + gi) * 3 + xpi) * 3 + gpi;
+        auto it = iter_graphs.find(key);
+        if (it != iter_graphs.end()) return it->second;
+        long long* saved = g_launch_counter;
+        long long kernels = 0;
+        g_launch_counter = &kernels;
+        cudaGraph_t graph = nullptr;
+        REGOT_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        try {
+            k_lb_pair<<<gN, kLbBlock, 0, st>>>(xbuf(xi), xbuf(xpi), gbuf(gi), gbuf(gpi),
+                                               pairs.get(), N, parts.get(), dstate.get());
+            k_lb_dir<<<gN, kLbBlock, 0, st>>>(gbuf(gi), pairs.get(), N, drt.get(), parts.get(),
+                                              dstate.get(), dscal.get());
+            count_launch(2);
+            trial_launch(xi, (xi + 1) % 3, (gi + 1) % 3, 1.0, true);
+        } catch (...) {
+            cudaGraph_t g = nullptr;
+            cudaStreamEndCapture(st, &g);
+            if (g) cudaGraphDestroy(g);
+            g_launch_counter = saved;
+            throw;
+        }
+        REGOT_CUDA(cudaStreamEndCapture(st, &graph));
+        g_launch_counter = saved;
+        cudaGraphExec_t exec = nullptr;
+        const cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        REGOT_CUDA(e);
+        iter_graph_kernels = kernels;
+        iter_graphs[key] = exec;
+        return exec;
     };
 
     int ix = 0, ig = 0;
@@ -1113,6 +1191,7 @@ void qrot_lbfgs_dual_device(regot_ctx* ctx, regot_dproblem* P, double reg, doubl
         REGOT_CHECK_LAUNCH();
         double step = 1.0 / gnorm;
         bool dg_known = true;  // the first g'drt is -|g|^2
+        bool pre_launched = false;
         double dg = -gg;
         int k = 1;
         for (;;) {
@@ -1129,31 +1208,22 @@ void qrot_lbfgs_dual_device(regot_ctx* ctx, regot_dproblem* P, double reg, doubl
             // igt; returns f and sets dgt, ggt, xxt.
             double dgt = 0.0, ggt = 0.0, xxt = 0.0;
             auto trial = [&](double s) {
-                k_lb_axpy<<<gN, kLbBlock, 0, st>>>(xbuf(ixp), drt.get(), s, N, xbuf(ixt));
-                count_launch();
+                if (pre_launched) {
+                    // the first trial (step 1) ran in the iteration's graph
+                    pre_launched = false;
+                } else {
+                    trial_launch(ixp, ixt, igt, s, !split_done);
+                }
+                split_done = true;
+                sync(st);
+                E.add_passes(1);
                 double f;
                 if (mixed) {
-                    PassParams p = ops.base_params();
-                    p.ra = xbuf(ixp);
-                    p.cb = xbuf(ixp) + n;
-                    p.rd = drt.get();
-                    p.cd = drt.get() + n;
-                    p.steps[0] = s;
-                    p.nsteps = 1;
-                    p.grid = grid.get();
-                    if (!split_done) {
-                        ops.maxabs(xbuf(ixp), N, nullptr, 0, grid.get());
-                        ops.pass(OP_Q_GRADLS, p);
-                        split_done = true;
-                    } else {
-                        ops.pass_presplit(OP_Q_GRADLS, p);
-                    }
-                    merge(OP_Q_GRADLS, 2, xbuf(ixt), gbuf(igt));
                     if (!dg_known) dg_init = hs->dg0;
                     last_obj = 0.5 * hs->sq - reg * hs->dab;
                     f = fx_init + s * dg_init + hs->rem;
                 } else {
-                    f = eval_at(xbuf(ixt), gbuf(igt));
+                    f = 0.5 * hs->sq - reg * hs->dab;
                     if (!dg_known) dg_init = hs->dg0;
                     last_obj = f;
                 }
@@ -1276,13 +1346,11 @@ void qrot_lbfgs_dual_device(regot_ctx* ctx, regot_dproblem* P, double reg, doubl
             iterate(ix, gnorm);
             if (gnorm <= param.epsilon || gnorm <= param.epsilon_rel * std::sqrt(xx)) break;
             if (param.max_iterations != 0 && k >= param.max_iterations) break;
-            // correction pair and the next direction
-            k_lb_pair<<<gN, kLbBlock, 0, st>>>(xbuf(ix), xbuf(ixp), gbuf(ig), gbuf(igp),
-                                               pairs.get(), N, parts.get(), dstate.get());
-            k_lb_dir<<<gN, kLbBlock, 0, st>>>(gbuf(ig), pairs.get(), N, drt.get(), parts.get(),
-                                              dstate.get(), dscal.get());
-            count_launch(2);
-            REGOT_CHECK_LAUNCH();
+            // correction pair, next direction and the next line search's
+            // first trial at step 1 (the graph of this buffer assignment)
+            REGOT_CUDA(cudaGraphLaunch(iter_graph(ix, ig, ixp, igp), st));
+            count_launch(iter_graph_kernels);
+            pre_launched = true;
             dg_known = false;  // read with the first trial's record
             step = 1.0;
             k++;
