@@ -427,6 +427,84 @@ def run_solvers(args):
         print(json.dumps(line), flush=True)
 
 
+CONFIG_RUNS = [
+    # (config, problem, solver, reg, tol, max_iter, kwargs): the solvers the
+    # configurations name, with the reference's default options
+    ("C1", "readme", "sinkhorn_bcd", 0.1, 1e-8, 1000, {}),
+    ("C1", "readme", "sinkhorn_bcd", 0.01, 1e-8, 1000, {}),
+    ("C1", "readme", "sinkhorn_ssns", 0.1, 1e-8, 1000, {}),
+    ("C1", "readme", "sinkhorn_ssns", 0.01, 1e-8, 1000, {}),
+    ("C1", "readme", "qrot_lbfgs_dual", 0.1, 1e-8, 1000, {}),
+    ("C3", "qrot4096", "qrot_lbfgs_dual", 0.1, 1e-6, 1000, {}),
+    ("C3", "qrot4096", "qrot_lbfgs_dual", 0.01, 1e-6, 1000, {}),
+    ("C3", "qrot4096", "qrot_assn", 0.1, 1e-6, 1000, {}),
+    ("C3", "qrot4096", "qrot_assn", 0.01, 1e-6, 1000, {}),
+]
+
+
+def run_configs(args):
+    """One JSON line per (configuration, solver, reg) of CONFIG_RUNS: the
+    README example (n = 1000, m = 800, FP64 M) and the large QROT problem
+    (n = m = 4096, seed 1). GPU: device time of a solve from a resident
+    problem, median of `steps` after `warmup`, in FP64 and in mixed
+    precision. CPU: the FP64 oracle on one host core (the reference's solvers
+    on these paths are single-threaded), timed over min(niter, K) iterations
+    with K bounded to about 10 s of work; the total is measured when K covers
+    the whole solve and extrapolated (init + niter x per-iteration time,
+    marked) otherwise."""
+    import regot
+    import regot_oracle as O
+    from problems import qrot_points, readme_example
+
+    probs = {"readme": readme_example(1000, 800),
+             "qrot4096": qrot_points(4096, 4096, seed=1, dtype=np.float32)}
+    resident = {}
+    for cfg, key, name, reg, tol, max_iter, kw in CONFIG_RUNS:
+        M, a, b = probs[key]
+        line = {"workload": "configs", "config": cfg, "solver": name, "n": int(M.shape[0]),
+                "m": int(M.shape[1]), "reg": reg, "tol": tol, "max_iter": max_iter,
+                "options": dict(kw)}
+        niter64 = None
+        for prec in ("fp64", "mixed"):
+            if (key, prec) not in resident:
+                resident[(key, prec)] = regot.Problem(M, a, b, precision=prec)
+            fn = getattr(resident[(key, prec)], name)
+            for _ in range(args.warmup):
+                r = fn(reg, tol=tol, max_iter=max_iter, plan=False, **kw)
+            ms = []
+            for _ in range(args.steps):
+                r = fn(reg, tol=tol, max_iter=max_iter, plan=False, **kw)
+                ms.append(r.solve_ms)
+            line[prec] = {"ms": round(statistics.median(ms), 3), "niter": int(r.niter),
+                          "final_mar_err": float(r.mar_errs[-1]) if len(r.mar_errs) else None,
+                          "passes": int(getattr(r, "passes", 0) or 0)}
+            if prec == "fp64":
+                niter64 = int(r.niter)
+        if not args.no_cpu_baseline:
+            M64 = M.astype(np.float64)
+            ofn = getattr(O, name)
+
+            def timed(k):
+                t = time.perf_counter()
+                ofn(M64, a, b, reg, tol=0.0, max_iter=k, plan=False)
+                return time.perf_counter() - t
+
+            t1 = timed(1)
+            t2 = timed(2)
+            per = max(t2 - t1, 1e-6)
+            init = max(t1 - per, 0.0)
+            k = int(min(niter64, max(2, 10.0 / per)))
+            if k > 2:
+                tk = timed(k)
+                per = (tk - t1) / (k - 1)
+                init = max(t1 - per, 0.0)
+            total = init + per * niter64
+            line["cpu_oracle"] = {"ms": round(total * 1e3, 1), "iterations_timed": k,
+                                  "niter": niter64, "ms_per_iter": round(per * 1e3, 3),
+                                  "extrapolated": k < niter64, "cores": 1}
+        print(json.dumps(line), flush=True)
+
+
 def run_autograd(args):
     """One JSON line for the autograd workload: x, y in R^{4096 x 64} ~ N(0, I)
     (seed 3, FP32 on the device), M = |x - y|^2 / 64, uniform weights, reg 0.05;
@@ -641,10 +719,13 @@ def main():
                     help="iteration cap of the unscaled batched workload")
     ap.add_argument("--ncu-case", action="store_true",
                     help="a few passes for an ncu capture (no timing, no JSON)")
-    ap.add_argument("--workload", choices=["bcd", "batched", "solvers", "autograd", "passes"],
+    ap.add_argument("--workload",
+                    choices=["bcd", "batched", "solvers", "autograd", "passes", "configs"],
                     default="bcd",
                     help="batched: the batched uneven-problem workload (its own JSON line); "
-                         "solvers: one line per solver of the solver table")
+                         "solvers: one line per solver of the solver table; "
+                         "configs: the README-example and large-QROT configurations, GPU "
+                         "beside the FP64 oracle")
     ap.add_argument("--probe", choices=["hbm-read", "host-link"],
                     help="measure the ceilings the numbers are read against (no JSON line)")
     args = ap.parse_args()
@@ -696,6 +777,9 @@ def main():
         return
     if args.workload == "passes":
         run_passes(args)
+        return
+    if args.workload == "configs":
+        run_configs(args)
         return
 
     import torch

@@ -355,6 +355,13 @@ int regot_erot_sparsify(regot_ctx* ctx, regot_dproblem* prob, double reg, const 
  * entries; mask as for regot_erot_sparsify. */
 int regot_erot_sparsify_density(regot_ctx* ctx, regot_dproblem* prob, double reg,
                                 const double* gamma, double density, long long* nnz, int* mask);
+/* The selection stages of both sparsifications run with each row and column
+ * in registers when n and m - 1 are at most 16384 (FP32) or 8192 (FP64),
+ * else from shared memory; the two give the same thresholds and the same
+ * kept entries. regot_force_sparsify_path(1) makes every later
+ * sparsification take the shared-memory path (0: the default choice) and
+ * returns the previous setting. No counterpart in the reference. */
+int regot_force_sparsify_path(int shared_memory);
 /* QROT Problem::dual_obj_grad (src/qrot_problem.cpp:226-253). */
 int regot_qrot_dual_obj_grad(regot_ctx* ctx, regot_dproblem* prob, double reg,
                              const double* gamma, double* obj, double* grad);

@@ -98,6 +98,48 @@ __device__ __forceinline__ double merge_strided(const Acc* p, int count, size_t 
     return (s0 + s1) + (s2 + s3);
 }
 
+// Knuth's TwoSum in FP32: s + e == a + b exactly (no FMA can be formed, so
+// contraction does not change it).
+__device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) {
+    s = a + b;
+    const float z = s - a;
+    e = (a - (s - z)) + (b - z);
+}
+
+// FP32 partials: compensated FP32 sums (TwoSum, two independent
+// accumulators with their rounding errors beside them), converted to FP64
+// once. FP64 arithmetic issues at a small fraction of the FP32 rate on this
+// part; converting and adding every partial in FP64 made the merge kernels
+// of the solver loops FP64-bound. The error stays at about count * 2^-48
+// relative, the level of the FP64 sum.
+template <>
+__device__ __forceinline__ double merge_strided<float>(const float* p, int count, size_t stride) {
+    float s0 = 0.f, c0 = 0.f, s1 = 0.f, c1 = 0.f;
+    int k = 0;
+    for (; k + 8 <= count; k += 8) {
+        float v[8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) v[q] = p[(size_t)(k + q) * stride];
+#pragma unroll
+        for (int q = 0; q < 8; q += 2) {
+            float t, e;
+            two_sum_f(s0, v[q], t, e);
+            s0 = t;
+            c0 += e;
+            two_sum_f(s1, v[q + 1], t, e);
+            s1 = t;
+            c1 += e;
+        }
+    }
+    for (; k < count; ++k) {
+        float t, e;
+        two_sum_f(s0, p[(size_t)k * stride], t, e);
+        s0 = t;
+        c0 += e;
+    }
+    return ((double)s0 + (double)s1) + ((double)c0 + (double)c1);
+}
+
 template <typename Acc>
 __device__ __forceinline__ double max_strided(const Acc* p, int count, size_t stride) {
     double s0 = -INFINITY, s1 = -INFINITY;
@@ -197,14 +239,6 @@ __device__ __forceinline__ double merge_2d(const Acc* p, int count, size_t strid
         for (int q = 0; q < 8; ++q) S += s_m2[q][threadIdx.x];
     }
     return S;
-}
-
-// Knuth's TwoSum in FP32: s + e == a + b exactly (no FMA can be formed, so
-// contraction does not change it).
-__device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) {
-    s = a + b;
-    const float z = s - a;
-    e = (a - (s - z)) + (b - z);
 }
 
 // FP32 partials: the same merge with compensated FP32 sums (TwoSum, the

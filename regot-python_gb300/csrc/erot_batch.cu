@@ -1317,7 +1317,9 @@ void erot_solve_batched_gpu(regot_ctx* ctx, const regot_batch_desc* D, double re
         for (int p = 0; p < P; ++p) order[p] = p;
         for (int side = 0; side < 2; ++side) {
             float* out = side ? gyd.get() : gxd.get();
-            if (side == 1 && !grad_y) break;  // side 0 runs for the row sums of T
+            if (side == 1 && !grad_y) break;
+            // side 0 gives grad_x and the row sums of T that the cost needs
+            if (side == 0 && !cost && !grad_x) continue;
             std::stable_sort(order.begin(), order.end(), [&](int u, int v) {
                 return side ? hn[u] > hn[v] : hm[u] > hm[v];
             });

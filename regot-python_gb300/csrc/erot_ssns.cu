@@ -53,10 +53,12 @@
 // can differ from the reference's sequential FP64 sums only where a partial
 // sum lies within about 1e-15 (relative) of delta.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <limits>
+#include <type_traits>
 #include <vector>
 
 #include "device_util.cuh"
@@ -541,6 +543,410 @@ __global__ void __launch_bounds__(kSelThreads) k_csc_fill(const TM* TT, long lon
     }
 }
 
+// ---- register-resident sparsification (rows and columns up to 256 x VPT) ----
+// The same selections as k_col_select / k_row_stage / k_csc_fill, with each
+// row (column) held in registers: thread t owns the VPT entries
+// W (t + 256 c) + e (c < VPT / W, e < W, W entries per 16-byte vector), all
+// loaded up front by vector loads, so that a row's loads are in flight at
+// once and the radix rounds, the threshold tests and the ordered compaction
+// read registers. The first radix digit has 11 bits (the exponent and the
+// leading mantissa bits: 2048 bins), the later ones 8; the answer of the
+// select does not depend on the digit widths. Bin sums are exact 64-bit
+// integers kept as two 32-bit words and added by 32-bit shared-memory
+// atomics with an explicit carry.
+// Blocks of 256 threads; the register bounds aim at three blocks per SM
+// where the row fits in 32 words per thread without spills (two for the
+// row stage, which also keeps the kept mask and the thresholds).
+constexpr int kRT = 256;  // threads
+constexpr int kRW = kRT / 32;
+constexpr int kRBins = 2048;
+
+struct RSmem {
+    unsigned hlo[kRBins];
+    unsigned hhi[kRBins];
+    unsigned hcnt[kRBins];
+    unsigned long long wtot[kRW];
+    double red[kRW];
+    double red2[kRW];
+    int wcnt[16][kRW];  // compaction: per chunk and warp (VPT / W <= 16)
+    unsigned long long base;
+    double result;
+    int bin;
+    unsigned count;
+};
+
+// Exact 64-bit add into (hi, lo) by 32-bit atomics: the carry out of the low
+// word is read from the value the atomic returns.
+__device__ __forceinline__ void bin_add(unsigned* lo, unsigned* hi, unsigned long long v) {
+    const unsigned vl = (unsigned)v, vh = (unsigned)(v >> 32);
+    const unsigned old = atomicAdd(lo, vl);
+    const unsigned up = vh + ((old + vl < old) ? 1u : 0u);
+    if (up) atomicAdd(hi, up);
+}
+
+template <typename TM>
+struct VecOf;
+template <>
+struct VecOf<float> {
+    static constexpr int W = 4;
+    using V = float4;
+};
+template <>
+struct VecOf<double> {
+    static constexpr int W = 2;
+    using V = double2;
+};
+
+template <typename TM, int VPT>
+__device__ __forceinline__ int r_index(int k) {
+    constexpr int W = VecOf<TM>::W;
+    return W * ((int)threadIdx.x + kRT * (k / W)) + (k % W);
+}
+
+// v[k] = src[r_index(k)] for indices < len, else 0. `vec`: src is 16-byte
+// aligned and readable up to the end of the last vector that holds an index
+// < len (rows padded to whole vectors).
+template <typename TM, int VPT>
+__device__ __forceinline__ void r_load(const TM* __restrict__ src, int len, bool vec,
+                                       TM (&v)[VPT]) {
+    constexpr int W = VecOf<TM>::W;
+    using V = typename VecOf<TM>::V;
+#pragma unroll
+    for (int c = 0; c < VPT / W; ++c) {
+        const int i0 = W * ((int)threadIdx.x + kRT * c);
+        if (vec && i0 < len) {
+            const V q = __ldg(reinterpret_cast<const V*>(src + i0));
+            const TM* e = reinterpret_cast<const TM*>(&q);
+#pragma unroll
+            for (int w = 0; w < W; ++w) v[c * W + w] = (i0 + w < len) ? e[w] : (TM)0;
+        } else {
+#pragma unroll
+            for (int w = 0; w < W; ++w) v[c * W + w] = (i0 + w < len) ? src[i0 + w] : (TM)0;
+        }
+    }
+}
+
+// Block sum estimate (as block_est_max: TM sums per thread and warp, FP64
+// over warps, with headroom for their rounding) and maximum of the entries
+// v[k] with bit k of `use` set (the others count as 0).
+template <typename TM, int VPT>
+__device__ void r_est_max(const TM (&v)[VPT], unsigned long long use, RSmem& sh, double& est,
+                          double& mx) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    TM s = 0, m = 0;
+#pragma unroll
+    for (int k = 0; k < VPT; ++k) {
+        const TM x = ((use >> k) & 1ull) ? v[k] : (TM)0;
+        s += x;
+        m = x > m ? x : m;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        s += __shfl_xor_sync(kFull, s, o);
+        const TM mo = __shfl_xor_sync(kFull, m, o);
+        m = mo > m ? mo : m;
+    }
+    if (lane == 0) {
+        sh.red[w] = (double)s;
+        sh.red2[w] = (double)m;
+    }
+    __syncthreads();
+    double t = 0.0, mm = 0.0;
+#pragma unroll
+    for (int q = 0; q < kRW; ++q) {
+        t += sh.red[q];
+        mm = fmax(mm, sh.red2[q]);
+    }
+    est = t * (1.0 + 1e-3) + mm;
+    mx = mm;
+    __syncthreads();
+}
+
+// Block-wide select of block_select's threshold over the register values
+// v[k] with bit k of `use` set (zeros ignored), most significant digit first.
+template <typename TM, int VPT>
+__device__ bool r_select(const TM (&v)[VPT], unsigned long long use, unsigned long long target,
+                         int kscale, RSmem& sh, TM& out) {
+    using K = KeyOf<TM>;
+    using U = typename K::U;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    U prefix = 0, mask = 0;
+    unsigned long long base = 0;
+    int hi = Digits<TM>::kTop;
+    bool first = true;
+    while (hi >= 0) {
+        const int width = first ? 11 : 8;
+        const int lo = hi - width + 1 > 0 ? hi - width + 1 : 0;
+        const int nb = 1 << (hi - lo + 1);
+        for (int b = tid; b < nb; b += kRT) {
+            sh.hlo[b] = 0u;
+            sh.hhi[b] = 0u;
+            sh.hcnt[b] = 0u;
+        }
+        if (tid == 0) sh.bin = -1;
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < VPT; ++k) {
+            const U key = K::key(v[k]);
+            if (((use >> k) & 1ull) && key != 0 && (key & mask) == prefix) {
+                const int b = (int)((key >> lo) & (U)(nb - 1));
+                bin_add(&sh.hlo[b], &sh.hhi[b], fix_of(v[k], kscale));
+                atomicAdd(&sh.hcnt[b], 1u);
+            }
+        }
+        __syncthreads();
+        // exclusive scan of the bin sums: thread t owns `per` consecutive bins
+        const int per = nb > kRT ? nb / kRT : 1;
+        const int b0 = tid * per;
+        const bool owner = b0 < nb;
+        unsigned long long ls = 0;
+        if (owner)
+            for (int q = 0; q < per; ++q)
+                ls += ((unsigned long long)sh.hhi[b0 + q] << 32) | sh.hlo[b0 + q];
+        unsigned long long inc = ls;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const unsigned long long o = __shfl_up_sync(kFull, inc, d);
+            if (lane >= d) inc += o;
+        }
+        if (lane == 31) sh.wtot[w] = inc;
+        __syncthreads();
+        unsigned long long run = base + (inc - ls);
+#pragma unroll
+        for (int q = 0; q < kRW; ++q) run += q < w ? sh.wtot[q] : 0ull;
+        if (owner) {
+            for (int q = 0; q < per; ++q) {
+                const int b = b0 + q;
+                const unsigned long long nx =
+                    run + (((unsigned long long)sh.hhi[b] << 32) | sh.hlo[b]);
+                if (run <= target && nx > target && sh.hcnt[b] > 0) {
+                    sh.bin = b;
+                    sh.base = run;
+                    sh.count = sh.hcnt[b];
+                }
+                run = nx;
+            }
+        }
+        __syncthreads();
+        const int sb = sh.bin;
+        const unsigned cnt = sh.count;
+        const unsigned long long nbase = sh.base;
+        __syncthreads();
+        if (sb < 0) return false;
+        prefix |= (U)sb << lo;
+        mask |= (U)(nb - 1) << lo;
+        base = nbase;
+        if (cnt == 1 && lo > 0) {
+            // a single candidate left: it is the answer
+#pragma unroll
+            for (int k = 0; k < VPT; ++k)
+                if (((use >> k) & 1ull) && K::key(v[k]) != 0 && (K::key(v[k]) & mask) == prefix)
+                    sh.result = (double)v[k];
+            __syncthreads();
+            out = (TM)sh.result;
+            __syncthreads();
+            return true;
+        }
+        hi = lo - 1;
+        first = false;
+    }
+    out = K::val(prefix);
+    return true;
+}
+
+// Ordered compaction of the register entries with bit k of `keep` set:
+// emit(k, slot) with consecutive slots in index order. Returns the total.
+template <typename TM, int VPT, typename Emit>
+__device__ int r_compact(unsigned long long keep, RSmem& sh, Emit emit) {
+    constexpr int W = VecOf<TM>::W;
+    constexpr int NC = VPT / W;
+    static_assert(NC <= 16, "compaction chunks");
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int incl[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+        const int cnt = __popcll((keep >> (c * W)) & ((1ull << W) - 1ull));
+        int x = cnt;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int o = __shfl_up_sync(kFull, x, d);
+            if (lane >= d) x += o;
+        }
+        incl[c] = x - cnt;  // exclusive within the warp
+        if (lane == 31) sh.wcnt[c][w] = x;
+    }
+    __syncthreads();
+    int before = 0;
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+        int woff = 0, ctot = 0;
+#pragma unroll
+        for (int q = 0; q < kRW; ++q) {
+            const int x = sh.wcnt[c][q];
+            ctot += x;
+            woff += q < w ? x : 0;
+        }
+        int slot = before + woff + incl[c];
+#pragma unroll
+        for (int e = 0; e < W; ++e) {
+            const int k = c * W + e;
+            if ((keep >> k) & 1ull) emit(k, slot++);
+        }
+        before += ctot;
+    }
+    __syncthreads();
+    return before;
+}
+
+// Column thresholds x_j from the rows of T' (k_col_select).
+template <typename TM, int VPT>
+__global__ void __launch_bounds__(kRT, VPT * sizeof(TM) <= 128 ? 3 : 1) k_col_select_r(const TM* __restrict__ TT, long long ldt,
+                                                      int n, int m1, double delta, int from_large,
+                                                      TM* __restrict__ xout) {
+    __shared__ RSmem sh;
+    for (int j = blockIdx.x; j < m1; j += gridDim.x) {
+        TM v[VPT];
+        r_load<TM, VPT>(TT + (size_t)j * ldt, n, true, v);
+        double est, mx;
+        r_est_max<TM, VPT>(v, ~0ull, sh, est, mx);
+        const int k = fix_scale(est);
+        TM x;
+        if (!r_select<TM, VPT>(v, ~0ull, fix_target(delta, k), k, sh, x))
+            x = from_large ? (TM)mx : (TM)INFINITY;  // column sum <= delta
+        if (threadIdx.x == 0) xout[j] = x;
+    }
+}
+
+// Row stage and CSR rows (k_row_stage): T of row i from M, its dropped
+// entries (below the column thresholds), the row threshold y_i where their
+// sum exceeds delta2, and the kept entries in column order.
+template <typename TM, int VPT>
+__global__ void __launch_bounds__(kRT, VPT * sizeof(TM) <= 64 ? 3 : VPT * sizeof(TM) <= 128 ? 2 : 1) k_row_stage_r(DenseArgs a, int ldr, int keep_row0,
+                                                     int vec, const TM* __restrict__ xcol,
+                                                     double delta2, TM* __restrict__ yout,
+                                                     int* __restrict__ rcount,
+                                                     int* __restrict__ rcols,
+                                                     TM* __restrict__ rvals) {
+    __shared__ RSmem sh;
+    const TM* M = static_cast<const TM*>(a.M);
+    const int m1 = a.m1;
+    for (int i = blockIdx.x; i < a.n; i += gridDim.x) {
+        TM t[VPT];
+        r_load<TM, VPT>(M + (size_t)i * a.ldm, m1, vec != 0, t);
+        unsigned long long drop = 0ull;
+#pragma unroll
+        for (int k = 0; k < VPT; ++k) {
+            const int j = r_index<TM, VPT>(k);
+            TM tk = 0;
+            if (j < m1) {
+                bool z64;
+                tk = t_at<TM>(a, i, j, t[k], z64);
+                if (tk < __ldg(xcol + j)) drop |= 1ull << k;
+            }
+            t[k] = tk;
+        }
+        double est, mx;
+        r_est_max<TM, VPT>(t, drop, sh, est, mx);
+        TM y = (TM)INFINITY;
+        if (est > delta2) {  // est bounds the dropped mass from above
+            const int ks = fix_scale(est);
+            TM yy;
+            if (r_select<TM, VPT>(t, drop, fix_target(delta2, ks), ks, sh, yy)) y = yy;
+        }
+        if (keep_row0 && i == 0) y = (TM)0;
+        unsigned long long keep = 0ull;
+#pragma unroll
+        for (int k = 0; k < VPT; ++k)
+            if (t[k] != (TM)0 && (!((drop >> k) & 1ull) || t[k] >= y)) keep |= 1ull << k;
+        int* cols = rcols + (size_t)i * ldr;
+        TM* vals = rvals + (size_t)i * ldr;
+        const int total = r_compact<TM, VPT>(keep, sh, [&](int k, int slot) {
+            cols[slot] = r_index<TM, VPT>(k);
+            vals[slot] = t[k];
+        });
+        if (threadIdx.x == 0) {
+            rcount[i] = total;
+            yout[i] = y;
+        }
+    }
+}
+
+// CSC columns from T' with the column and row thresholds (k_csc_fill).
+template <typename TM, int VPT>
+__global__ void __launch_bounds__(kRT, VPT * sizeof(TM) <= 128 ? 3 : 1) k_csc_fill_r(const TM* __restrict__ TT, long long ldt,
+                                                    int n, int m1, const TM* __restrict__ xcol,
+                                                    const TM* __restrict__ yrow, int ldc,
+                                                    int* __restrict__ ccount,
+                                                    int* __restrict__ crows,
+                                                    TM* __restrict__ cvals) {
+    __shared__ RSmem sh;
+    for (int j = blockIdx.x; j < m1; j += gridDim.x) {
+        TM v[VPT];
+        r_load<TM, VPT>(TT + (size_t)j * ldt, n, true, v);
+        const TM xj = xcol[j];
+        unsigned long long keep = 0ull;
+#pragma unroll
+        for (int k = 0; k < VPT; ++k) {
+            const int i = r_index<TM, VPT>(k);
+            if (i < n && v[k] != (TM)0 && (v[k] >= xj || v[k] >= __ldg(yrow + i)))
+                keep |= 1ull << k;
+        }
+        int* rows = crows + (size_t)j * ldc;
+        TM* vals = cvals + (size_t)j * ldc;
+        const int total = r_compact<TM, VPT>(keep, sh, [&](int k, int slot) {
+            rows[slot] = r_index<TM, VPT>(k);
+            vals[slot] = v[k];
+        });
+        if (threadIdx.x == 0) ccount[j] = total;
+    }
+}
+
+// Values per thread of the register path for rows of length len (a power
+// of two, at least one vector), or 0 when the row is too long for it.
+template <typename TM>
+int r_vpt(int len) {
+    constexpr int W = VecOf<TM>::W;
+    constexpr int kMax = sizeof(TM) == 4 ? 64 : 32;
+    int v = W;
+    while ((long long)v * kRT < len) v *= 2;
+    return v <= kMax ? v : 0;
+}
+
+template <typename TM, int V>
+constexpr bool r_valid() {
+    return V >= VecOf<TM>::W && V <= (sizeof(TM) == 4 ? 64 : 32);
+}
+
+// f(std::integral_constant<int, vpt>) for a valid vpt of the register path.
+template <typename TM, typename F>
+void r_dispatch(int vpt, F&& f) {
+    auto go = [&](auto c) {
+        if constexpr (r_valid<TM, decltype(c)::value>()) f(c);
+    };
+    switch (vpt) {
+        case 2: go(std::integral_constant<int, 2>{}); break;
+        case 4: go(std::integral_constant<int, 4>{}); break;
+        case 8: go(std::integral_constant<int, 8>{}); break;
+        case 16: go(std::integral_constant<int, 16>{}); break;
+        case 32: go(std::integral_constant<int, 32>{}); break;
+        case 64: go(std::integral_constant<int, 64>{}); break;
+        default: break;
+    }
+}
+
+// Grid of a register-path kernel: every block resident at once (the blocks
+// loop over rows or columns), at most one block per row or column.
+template <typename Kern>
+int r_grid(Kern kern, int count) {
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kRT, 0) != cudaSuccess ||
+        occ < 1)
+        occ = 1;
+    return std::max(1, std::min(count, device_sm_count() * occ));
+}
+
+std::atomic<int> g_sparsify_legacy{0};
+
 // Number of stored entries (sum of the row counts).
 __global__ void k_nnz(const int* rcount, int n, double* parts, SsnState* st) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -550,7 +956,14 @@ __global__ void k_nnz(const int* rcount, int n, double* parts, SsnState* st) {
     if (grid_reduce<1>(v, parts, &st->counter, out)) st->nnz = out[0];
 }
 
-// ---- sparse products (one warp per row or column; FP64 accumulation) ----
+// ---- sparse products (one warp per row or column) ----
+// FP64 engine: FP64 products and sums. Mixed engine (FP32 values): the
+// vector operand comes as FP32 (hi, lo) pairs and every product and sum is
+// formed in compensated FP32 (the exact product error by an FMA, TwoSum for
+// the running sum), converted to FP64 once per row. FP64 instructions issue
+// at a small fraction of the FP32 rate on this part, and one FP64 FMA (plus
+// a conversion) per stored entry made the CG products FP64-bound; the
+// compensated sums stay within about 2^-44 of sum |v x| per row.
 struct Sparse {
     const int* rcount;
     const int* rcols;
@@ -562,34 +975,91 @@ struct Sparse {
     int ldc;
     int n, m1;
     double inv_reg;
+    // mixed engine: FP32 (hi, lo) copies of the CG vectors, written by the
+    // kernels that produce them, and 1 / (h1 + shift) in FP32 for the
+    // preconditioner
+    float2* u2;  // rows (n)
+    float2* p2;  // columns (m - 1)
+    float2* x2;  // columns: the beta part of the direction
+    float2* d2;  // rows: the alpha part of the direction
+    float* w32;  // rows
 };
 
 template <typename TM>
-__device__ __forceinline__ double row_dot(const Sparse& S, int i, const double* x) {
+using SpVec = typename std::conditional<std::is_same<TM, float>::value, float2, double>::type;
+
+__device__ __forceinline__ float2 split_df(double v) {
+    const float h = __double2float_rn(v);
+    return make_float2(h, __double2float_rn(v - (double)h));
+}
+
+__device__ __forceinline__ double sp_dot(const double* v, const int* c, int cnt,
+                                         const double* x) {
     const int lane = threadIdx.x & 31;
-    const int cnt = S.rcount[i];
-    const int* c = S.rcols + (size_t)i * S.ldr;
-    const TM* v = static_cast<const TM*>(S.rvals) + (size_t)i * S.ldr;
     double s = 0.0;
-    for (int k = lane; k < cnt; k += 32) s += (double)v[k] * x[c[k]];
-    return warp_sum_d(s) * S.inv_reg;
+    for (int k = lane; k < cnt; k += 32) s += v[k] * x[c[k]];
+    return warp_sum_d(s);
+}
+
+__device__ __forceinline__ double sp_dot(const float* v, const int* c, int cnt, const float2* x) {
+    const int lane = threadIdx.x & 31;
+    float s = 0.f, e = 0.f;
+    for (int k = lane; k < cnt; k += 32) {
+        const float vv = v[k];
+        const float2 xx = x[c[k]];
+        const float p = vv * xx.x;
+        const float pe = fmaf(vv, xx.x, -p);  // exact: vv xx.x = p + pe
+        float t, te;
+        two_sum_f(s, p, t, te);
+        s = t;
+        e += te + fmaf(vv, xx.y, pe);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float so = __shfl_xor_sync(kFull, s, o);
+        const float eo = __shfl_xor_sync(kFull, e, o);
+        float t, te;
+        two_sum_f(s, so, t, te);
+        s = t;
+        e += eo + te;
+    }
+    return (double)s + (double)e;
 }
 
 template <typename TM>
-__device__ __forceinline__ double col_dot(const Sparse& S, int j, const double* x) {
-    const int lane = threadIdx.x & 31;
+__device__ __forceinline__ double row_dot(const Sparse& S, int i, const SpVec<TM>* x) {
+    const int cnt = S.rcount[i];
+    const int* c = S.rcols + (size_t)i * S.ldr;
+    const TM* v = static_cast<const TM*>(S.rvals) + (size_t)i * S.ldr;
+    return sp_dot(v, c, cnt, x) * S.inv_reg;
+}
+
+template <typename TM>
+__device__ __forceinline__ double col_dot(const Sparse& S, int j, const SpVec<TM>* x) {
     const int cnt = S.ccount[j];
     const int* r = S.crows + (size_t)j * S.ldc;
     const TM* v = static_cast<const TM*>(S.cvals) + (size_t)j * S.ldc;
-    double s = 0.0;
-    for (int k = lane; k < cnt; k += 32) s += (double)v[k] * x[r[k]];
-    return warp_sum_d(s) * S.inv_reg;
+    return sp_dot(v, r, cnt, x) * S.inv_reg;
+}
+
+// The operand of a sparse product: the FP64 vector itself, or (mixed) its
+// FP32 (hi, lo) copy.
+template <typename TM>
+__device__ __forceinline__ const SpVec<TM>* sp_arg(const double* x, const float2* x2) {
+    if constexpr (std::is_same<TM, float>::value) return x2;
+    else return x;
+}
+
+template <typename TM>
+__device__ __forceinline__ void put_split(float2* dst, int k, double v) {
+    if constexpr (std::is_same<TM, float>::value) dst[k] = split_df(v);
 }
 
 // Vectors: h = (h1 [n], h2 [m - 1]) from the gradient pass, g, direction
 // dir = (d_alpha [n], d_beta~ [m - 1], 0). The Schur CG works on x = d_beta~.
 
-// Jacobi diagonal of the Schur complement (method 1).
+// Jacobi diagonal of the Schur complement (method 1). It only preconditions,
+// so the mixed engine forms it in FP32 from w32 = 1 / (h1 + shift).
 template <typename TM>
 __global__ void k_schur_diag(Sparse S, const double* h, SsnState* st, double* diag) {
     const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -599,12 +1069,21 @@ __global__ void k_schur_diag(Sparse S, const double* h, SsnState* st, double* di
     const int cnt = S.ccount[j];
     const int* r = S.crows + (size_t)j * S.ldc;
     const TM* v = static_cast<const TM*>(S.cvals) + (size_t)j * S.ldc;
-    double s = 0.0;
-    for (int k = lane; k < cnt; k += 32) {
-        const double sv = (double)v[k] * S.inv_reg;
-        s += sv * sv / (h[r[k]] + shift);
+    double s;
+    if constexpr (std::is_same<TM, float>::value) {
+        float sf = 0.f;
+        for (int k = lane; k < cnt; k += 32) sf = fmaf(v[k] * v[k], S.w32[r[k]], sf);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) sf += __shfl_xor_sync(kFull, sf, o);
+        s = (double)sf * S.inv_reg * S.inv_reg;
+    } else {
+        s = 0.0;
+        for (int k = lane; k < cnt; k += 32) {
+            const double sv = v[k] * S.inv_reg;
+            s += sv * sv / (h[r[k]] + shift);
+        }
+        s = warp_sum_d(s);
     }
-    s = warp_sum_d(s);
     if (lane == 0) {
         const double dj = h[S.n + j] + shift;
         const double dd = dj - s;
@@ -612,11 +1091,18 @@ __global__ void k_schur_diag(Sparse S, const double* h, SsnState* st, double* di
     }
 }
 
-// u_i = rhs_alpha_i / (h1_i + shift) with rhs = -g.
+// u_i = rhs_alpha_i / (h1_i + shift) with rhs = -g; with u2 / w32 given (the
+// mixed engine) also u's FP32 pair and 1 / (h1_i + shift) in FP32.
 __global__ void k_schur_rhs_rows(int n, const double* g, const double* h, SsnState* st,
-                                 double* u) {
+                                 double* u, float2* u2, float* w32) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) u[i] = -g[i] / (h[i] + st->shift);
+    if (i < n) {
+        const double w = 1.0 / (h[i] + st->shift);
+        const double ui = -g[i] * w;
+        u[i] = ui;
+        if (u2) u2[i] = split_df(ui);
+        if (w32) w32[i] = (float)w;
+    }
 }
 
 // CG set-up on Delta x = rhs_beta - S' u: x = 0, r = that, z = r / diag, p = z.
@@ -628,14 +1114,16 @@ __global__ void k_schur_init(Sparse S, const double* g, const double* u, const d
     const int lane = threadIdx.x & 31;
     double v[2] = {0.0, 0.0};
     if (j < S.m1) {
-        const double w = col_dot<TM>(S, j, u);
+        const double w = col_dot<TM>(S, j, sp_arg<TM>(u, S.u2));
         if (lane == 0) {
             const double rj = -g[S.n + j] - w;
             const double zj = diag ? rj / diag[j] : rj;
             x[j] = 0.0;
+            put_split<TM>(S.x2, j, 0.0);
             rv[j] = rj;
             z[j] = zj;
             p[j] = zj;
+            put_split<TM>(S.p2, j, zj);
             v[0] = rj * rj;
             v[1] = rj * zj;
         }
@@ -658,8 +1146,12 @@ __global__ void k_schur_rows(Sparse S, const double* p, const double* h, double*
     if (st->done) return;
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (i >= S.n) return;
-    const double s = row_dot<TM>(S, i, p);
-    if ((threadIdx.x & 31) == 0) u[i] = s / (h[i] + st->shift);
+    const double s = row_dot<TM>(S, i, sp_arg<TM>(p, S.p2));
+    if ((threadIdx.x & 31) == 0) {
+        const double ui = s / (h[i] + st->shift);
+        u[i] = ui;
+        put_split<TM>(S.u2, i, ui);
+    }
 }
 
 // q_j = (h2_j + shift) p_j - (S' u)_j; alpha = r'z / p'q.
@@ -670,7 +1162,7 @@ __global__ void k_schur_cols(Sparse S, const double* p, const double* u, const d
     const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     double v[1] = {0.0};
     if (j < S.m1) {
-        const double w = col_dot<TM>(S, j, u);
+        const double w = col_dot<TM>(S, j, sp_arg<TM>(u, S.u2));
         if ((threadIdx.x & 31) == 0) {
             const double qj = (h[S.n + j] + st->shift) * p[j] - w;
             q[j] = qj;
@@ -683,15 +1175,19 @@ __global__ void k_schur_cols(Sparse S, const double* p, const double* u, const d
 }
 
 // x += alpha p, r -= alpha q, z = r / diag; stop on ||r||^2 < thresh2 or
-// at the iteration limit (Eigen's ConjugateGradient loop).
+// at the iteration limit (Eigen's ConjugateGradient loop). x2 (mixed): x's
+// FP32 pair.
 __global__ void k_schur_b(int m1, const double* p, const double* q, const double* diag,
-                          double* x, double* rv, double* z, double* parts, SsnState* st) {
+                          double* x, double* rv, double* z, double* parts, SsnState* st,
+                          float2* x2) {
     if (st->done) return;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const double al = st->alpha;
     double v[2] = {0.0, 0.0};
     if (j < m1) {
-        x[j] += al * p[j];
+        const double xj = x[j] + al * p[j];
+        x[j] = xj;
+        if (x2) x2[j] = split_df(xj);
         const double rj = rv[j] - al * q[j];
         rv[j] = rj;
         const double zj = diag ? rj / diag[j] : rj;
@@ -713,10 +1209,14 @@ __global__ void k_schur_b(int m1, const double* p, const double* q, const double
     }
 }
 
-__global__ void k_schur_c(int m1, const double* z, double* p, SsnState* st) {
+__global__ void k_schur_c(int m1, const double* z, double* p, SsnState* st, float2* p2) {
     if (st->done) return;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j < m1) p[j] = z[j] + st->beta * p[j];
+    if (j < m1) {
+        const double pj = z[j] + st->beta * p[j];
+        p[j] = pj;
+        if (p2) p2[j] = split_df(pj);
+    }
 }
 
 // d_alpha_i = (rhs_alpha_i - (S d_beta)_i) / (h1_i + shift).
@@ -725,8 +1225,12 @@ __global__ void k_schur_back(Sparse S, const double* g, const double* h, double*
                              SsnState* st) {
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (i >= S.n) return;
-    const double s = row_dot<TM>(S, i, dir + S.n);
-    if ((threadIdx.x & 31) == 0) dir[i] = (-g[i] - s) / (h[i] + st->shift);
+    const double s = row_dot<TM>(S, i, sp_arg<TM>(dir + S.n, S.x2));
+    if ((threadIdx.x & 31) == 0) {
+        const double di = (-g[i] - s) / (h[i] + st->shift);
+        dir[i] = di;
+        put_split<TM>(S.d2, i, di);
+    }
 }
 
 // d'H_s d and g'd: rows give d_a (h1 d_a + S d_b), cols d_b (h2 d_b + S' d_a).
@@ -736,7 +1240,7 @@ __global__ void k_dhd_rows(Sparse S, const double* dir, const double* g, const d
     const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     double v[2] = {0.0, 0.0};
     if (i < S.n) {
-        const double s = row_dot<TM>(S, i, dir + S.n);
+        const double s = row_dot<TM>(S, i, sp_arg<TM>(dir + S.n, S.x2));
         if ((threadIdx.x & 31) == 0) {
             const double di = dir[i];
             v[0] = di * (h[i] * di + s);
@@ -757,7 +1261,7 @@ __global__ void k_dhd_cols(Sparse S, const double* dir, const double* g, const d
     const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     double v[2] = {0.0, 0.0};
     if (j < S.m1) {
-        const double s = col_dot<TM>(S, j, dir);
+        const double s = col_dot<TM>(S, j, sp_arg<TM>(dir, S.d2));
         if ((threadIdx.x & 31) == 0) {
             const double dj = dir[S.n + j];
             v[0] = dj * (h[S.n + j] * dj + s);
@@ -991,6 +1495,20 @@ public:
         S_.n = n_;
         S_.m1 = m1_;
         S_.inv_reg = 1.0 / reg;
+        S_.u2 = S_.p2 = S_.x2 = S_.d2 = nullptr;
+        S_.w32 = nullptr;
+        if (mixed_) {
+            u2_.alloc(n_, st_);
+            d2_.alloc(n_, st_);
+            w32_.alloc(n_, st_);
+            p2_.alloc(mm, st_);
+            x2_.alloc(mm, st_);
+            S_.u2 = u2_.get();
+            S_.d2 = d2_.get();
+            S_.w32 = w32_.get();
+            S_.p2 = p2_.get();
+            S_.x2 = x2_.get();
+        }
     }
 
     double* gamma() { return gamma_.get(); }
@@ -1051,22 +1569,11 @@ public:
         zeros_.zero();
         dim3 tgrid(cdiv(m1_, 32), cdiv(n_, 32));
         k_tt<TM><<<tgrid, dim3(32, 8), 0, st_>>>(a, tt_.get(), ldt_, zeros_.get());
-        k_col_select<TM><<<col_grid_, kSelThreads, col_smem_, st_>>>(
-            tt_.get(), ldt_, n_, m1_, delta, density_hint > 0.2 ? 0 : 1, col_cache_ ? 1 : 0,
-            xcol_.get());
-        RowStageArgs r;
-        r.ldr = m1_;
-        r.cache = row_cache_ ? 1 : 0;
-        r.lds = lds_;
-        r.keep_row0 = 0;
-        k_row_stage<TM><<<row_grid_, kSelThreads, row_smem_, st_>>>(
-            a, r, xcol_.get(), 2.0 * delta, row_scratch_.get(), yrow_.get(), rcount_.get(),
-            rcols_.get(), rvals_.get());
-        k_csc_fill<TM><<<col_grid_, kSelThreads, col_smem_, st_>>>(
-            tt_.get(), ldt_, n_, m1_, xcol_.get(), yrow_.get(), n_, col_cache_ ? 1 : 0,
-            ccount_.get(), crows_.get(), cvals_.get());
+        col_select(delta, density_hint > 0.2 ? 0 : 1);
+        row_stage(a, 2.0 * delta, 0);
+        csc_fill();
         k_nnz<<<cdiv(n_, kVT), kVT, 0, st_>>>(rcount_.get(), n_, parts_.get(), state_.get());
-        count_launch(5);
+        count_launch(2);
         REGOT_CHECK_LAUNCH();
         passes_ += 4;
         unsigned long long zc = 0;
@@ -1075,6 +1582,64 @@ public:
         const double nnz = hs.nnz + (double)zc;
         const double dim = (double)(n_ + m_ - 1);
         return (2.0 * nnz + dim) / dim / dim;
+    }
+
+    // The selection stages of a sparsification: the register path when the
+    // rows and the columns fit it, else the shared-memory path.
+    bool rpath() const {
+        return g_sparsify_legacy.load(std::memory_order_relaxed) == 0 && r_vpt<TM>(n_) > 0 &&
+               r_vpt<TM>(m1_) > 0;
+    }
+    void col_select(double delta, int from_large) {
+        if (rpath()) {
+            r_dispatch<TM>(r_vpt<TM>(n_), [&](auto c) {
+                constexpr int V = decltype(c)::value;
+                k_col_select_r<TM, V><<<r_grid(k_col_select_r<TM, V>, m1_), kRT, 0, st_>>>(
+                    tt_.get(), ldt_, n_, m1_, delta, from_large, xcol_.get());
+            });
+        } else {
+            k_col_select<TM><<<col_grid_, kSelThreads, col_smem_, st_>>>(
+                tt_.get(), ldt_, n_, m1_, delta, from_large, col_cache_ ? 1 : 0, xcol_.get());
+        }
+        count_launch();
+    }
+    void row_stage(const DenseArgs& a, double delta2, int keep_row0) {
+        if (rpath()) {
+            constexpr int W = VecOf<TM>::W;
+            const int vec = (reinterpret_cast<uintptr_t>(P_->M) % 16 == 0 && P_->ldm % W == 0)
+                                ? 1 : 0;
+            r_dispatch<TM>(r_vpt<TM>(m1_), [&](auto c) {
+                constexpr int V = decltype(c)::value;
+                k_row_stage_r<TM, V><<<r_grid(k_row_stage_r<TM, V>, n_), kRT, 0, st_>>>(
+                    a, m1_, keep_row0, vec, xcol_.get(), delta2, yrow_.get(), rcount_.get(),
+                    rcols_.get(), rvals_.get());
+            });
+        } else {
+            RowStageArgs r;
+            r.ldr = m1_;
+            r.cache = row_cache_ ? 1 : 0;
+            r.lds = lds_;
+            r.keep_row0 = keep_row0;
+            k_row_stage<TM><<<row_grid_, kSelThreads, row_smem_, st_>>>(
+                a, r, xcol_.get(), delta2, row_scratch_.get(), yrow_.get(), rcount_.get(),
+                rcols_.get(), rvals_.get());
+        }
+        count_launch();
+    }
+    void csc_fill() {
+        if (rpath()) {
+            r_dispatch<TM>(r_vpt<TM>(n_), [&](auto c) {
+                constexpr int V = decltype(c)::value;
+                k_csc_fill_r<TM, V><<<r_grid(k_csc_fill_r<TM, V>, m1_), kRT, 0, st_>>>(
+                    tt_.get(), ldt_, n_, m1_, xcol_.get(), yrow_.get(), n_, ccount_.get(),
+                    crows_.get(), cvals_.get());
+            });
+        } else {
+            k_csc_fill<TM><<<col_grid_, kSelThreads, col_smem_, st_>>>(
+                tt_.get(), ldt_, n_, m1_, xcol_.get(), yrow_.get(), n_, col_cache_ ? 1 : 0,
+                ccount_.get(), crows_.get(), cvals_.get());
+        }
+        count_launch();
     }
 
     // direction = -(H_s + shift I)^{-1} gv into dir (sinkhorn_ssns.cpp:118-140);
@@ -1096,7 +1661,8 @@ public:
                                    st_));
         REGOT_CUDA(cudaMemsetAsync(dir_.get(), 0, (size_t)(n_ + m_) * sizeof(double), st_));
         if (m1_ <= 0) {
-            k_schur_rhs_rows<<<cdiv(n_, kVT), kVT, 0, st_>>>(n_, gsrc, h_.get(), S, dir_.get());
+            k_schur_rhs_rows<<<cdiv(n_, kVT), kVT, 0, st_>>>(n_, gsrc, h_.get(), S, dir_.get(),
+                                                             nullptr, nullptr);
             count_launch();
             return;
         }
@@ -1104,12 +1670,13 @@ public:
         const int gc = cdiv((long long)m1_ * 32, 32 * kSpWarps);
         const int bt = 32 * kSpWarps;
         const double* diag = nullptr;
+        k_schur_rhs_rows<<<cdiv(n_, kVT), kVT, 0, st_>>>(n_, gsrc, h_.get(), S, u_.get(), S_.u2,
+                                                         S_.w32);
         if (jac) {
             k_schur_diag<TM><<<gc, bt, 0, st_>>>(S_, h_.get(), S, diag_.get());
             count_launch();
             diag = diag_.get();
         }
-        k_schur_rhs_rows<<<cdiv(n_, kVT), kVT, 0, st_>>>(n_, gsrc, h_.get(), S, u_.get());
         double* x = dir_.get() + n_;
         k_schur_init<TM><<<gc, bt, 0, st_>>>(S_, gsrc, u_.get(), diag, cg_tol_, x, rv_.get(),
                                              z_.get(), p_.get(), parts_.get(), S);
@@ -1243,19 +1810,10 @@ public:
             }
         }
         k_topk_finish<TM><<<cdiv(m1_, kVT), kVT, 0, st_>>>(topk_.get(), m1_, xcol_.get());
-        RowStageArgs r;
-        r.ldr = m1_;
-        r.cache = row_cache_ ? 1 : 0;
-        r.lds = lds_;
-        r.keep_row0 = 1;
-        k_row_stage<TM><<<row_grid_, kSelThreads, row_smem_, st_>>>(
-            a, r, xcol_.get(), (double)INFINITY, row_scratch_.get(), yrow_.get(), rcount_.get(),
-            rcols_.get(), rvals_.get());
-        k_csc_fill<TM><<<col_grid_, kSelThreads, col_smem_, st_>>>(
-            tt_.get(), ldt_, n_, m1_, xcol_.get(), yrow_.get(), n_, col_cache_ ? 1 : 0,
-            ccount_.get(), crows_.get(), cvals_.get());
+        row_stage(a, (double)INFINITY, 1);
+        csc_fill();
         k_nnz<<<cdiv(n_, kVT), kVT, 0, st_>>>(rcount_.get(), n_, parts_.get(), state_.get());
-        count_launch(4);
+        count_launch(2);
         REGOT_CHECK_LAUNCH();
         passes_ += 3;
     }
@@ -1330,8 +1888,8 @@ private:
         k_schur_cols<TM><<<gc, bt, 0, st_>>>(S_, p_.get(), u_.get(), h_.get(), q_.get(),
                                              parts_.get(), S);
         k_schur_b<<<gv, kVT, 0, st_>>>(m1_, p_.get(), q_.get(), diag, x, rv_.get(), z_.get(),
-                                       parts_.get(), S);
-        k_schur_c<<<gv, kVT, 0, st_>>>(m1_, z_.get(), p_.get(), S);
+                                       parts_.get(), S, S_.x2);
+        k_schur_c<<<gv, kVT, 0, st_>>>(m1_, z_.get(), p_.get(), S, S_.p2);
         count_launch(4);
         REGOT_CUDA(cudaStreamEndCapture(st_, &graph_));
         g_launch_counter = saved;
@@ -1350,6 +1908,8 @@ private:
     int cg_max_ = 0, max_cg_ = 0, max_direct_ = 0;
     DBuf<double> gamma_, g_, h_, dir_, u_, rv_, z_, p_, q_, diag_, parts_, lsout_;
     DBuf<double> xt_, tsum_, tmx_;
+    DBuf<float2> u2_, d2_, p2_, x2_;  // mixed: FP32 (hi, lo) copies of the CG vectors
+    DBuf<float> w32_;
     DBuf<TopK> topk_;
     DBuf<unsigned> hist_;
     DBuf<SsnState> state_;
@@ -1675,6 +2235,10 @@ void sparsify_at(regot_ctx* ctx, regot_dproblem* P, double reg, const double* ga
 }
 
 }  // namespace
+
+int force_sparsify_path(int shared_memory) {
+    return g_sparsify_legacy.exchange(shared_memory ? 1 : 0);
+}
 
 void erot_sparsify_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, const double* gamma,
                        double delta, double density_hint, long long* nnz, int* mask) {

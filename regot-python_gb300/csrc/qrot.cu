@@ -733,7 +733,10 @@ namespace {
 // writes every scalar the host needs (objective terms, g'd, |g|^2, |x|^2)
 // into one 64-byte record: one small copy and one synchronisation per trial.
 constexpr int kLbM = 6;          // LBFGSParam m (Param.h:168-182)
-constexpr int kLbBlock = 256;
+// Blocks of two warps: the vector kernels are FP64 work on n + m entries,
+// which this part issues at a small fraction of its FP32 rate per SM, so
+// they are spread over as many SMs as the vector length allows.
+constexpr int kLbBlock = 64;
 constexpr int kLbPairSums = 5 * kLbM + 4;
 
 struct LbScal {
@@ -760,10 +763,15 @@ struct LbState {
 
 // Block sums of K values, then the last block to arrive adds the block sums
 // in block order: true in every thread of that block, with the totals in
-// s_out (shared, K entries).
+// s_out (shared, K entries). The last block's sums are spread over its
+// warps (value k to warp k mod warps, blocks to lanes) with every load of a
+// lane issued before its adds, so that they take a few memory latencies
+// instead of one per block.
 template <int K>
 __device__ bool lb_reduce(const double (&v)[K], double* parts, unsigned* counter, double* s_out) {
-    __shared__ double s_red[K][kLbBlock / 32];
+    constexpr int NW = kLbBlock / 32;
+    constexpr int PER = (K + NW - 1) / NW;
+    __shared__ double s_red[K][NW];
     __shared__ int s_last;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
 #pragma unroll
@@ -774,7 +782,7 @@ __device__ bool lb_reduce(const double (&v)[K], double* parts, unsigned* counter
     __syncthreads();
     if (tid < K) {
         double s = 0.0;
-        for (int w = 0; w < kLbBlock / 32; ++w) s += s_red[tid][w];
+        for (int w = 0; w < NW; ++w) s += s_red[tid][w];
         parts[(size_t)blockIdx.x * K + tid] = s;
         __threadfence();
     }
@@ -783,10 +791,24 @@ __device__ bool lb_reduce(const double (&v)[K], double* parts, unsigned* counter
     __syncthreads();
     if (!s_last) return false;
     __threadfence();
-    if (tid < K) {
-        double s = 0.0;
-        for (unsigned b = 0; b < gridDim.x; ++b) s += __ldcg(&parts[(size_t)b * K + tid]);
-        s_out[tid] = s;
+    double acc[PER];
+#pragma unroll
+    for (int q = 0; q < PER; ++q) acc[q] = 0.0;
+    for (unsigned b = lane; b < gridDim.x; b += 32) {
+        double x[PER];
+#pragma unroll
+        for (int q = 0; q < PER; ++q) {
+            const int k = warp + q * NW;
+            x[q] = k < K ? __ldcg(&parts[(size_t)b * K + k]) : 0.0;
+        }
+#pragma unroll
+        for (int q = 0; q < PER; ++q) acc[q] += x[q];
+    }
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+        const int k = warp + q * NW;
+        const double t = warp_sum_d(acc[q]);
+        if (lane == 0 && k < K) s_out[k] = t;
     }
     if (tid == 0) *counter = 0u;
     __syncthreads();
@@ -807,9 +829,11 @@ __global__ void __launch_bounds__(kLbBlock) k_lb_merge(
     const Acc* __restrict__ rp, int nslabs, const Acc* __restrict__ cp, int nrb, int n, int m,
     const double* __restrict__ totpart, int nblocks, int nt, const double* __restrict__ x,
     const double* __restrict__ drt, const double* __restrict__ a, const double* __restrict__ b,
-    double reg, double* __restrict__ grad, double* parts, LbState* st, LbScal* out) {
+    double reg, double* __restrict__ grad, double* parts, LbState* st, LbScal* out,
+    unsigned long long* __restrict__ mxparts, double* __restrict__ xmax) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     double v[4] = {0.0, 0.0, 0.0, 0.0};
+    unsigned long long xbits = 0ULL;
     if (t < n + m) {
         double g, w;
         if (t < n) {
@@ -822,19 +846,44 @@ __global__ void __launch_bounds__(kLbBlock) k_lb_merge(
         }
         grad[t] = g;
         const double xt = x[t];
+        xbits = abs_bits(xt);
         v[0] = xt * w;
         v[1] = g * drt[t];
         v[2] = g * g;
         v[3] = xt * xt;
     }
+    // max |x| of this block (bit patterns of non-negative doubles order like
+    // the values), for the split grid of a line search from x
+    {
+        __shared__ unsigned long long s_wmax[kLbBlock / 32];
+        const unsigned long long wm = warp_max_u64(xbits);
+        if ((threadIdx.x & 31) == 0) s_wmax[threadIdx.x >> 5] = wm;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            unsigned long long bm = 0ULL;
+            for (int w = 0; w < kLbBlock / 32; ++w) bm = s_wmax[w] > bm ? s_wmax[w] : bm;
+            mxparts[blockIdx.x] = bm;
+        }
+    }
     __shared__ double s_sum[4];
     if (!lb_reduce<4>(v, parts, &st->counter, s_sum)) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (warp == 0) {
+        unsigned long long bm = 0ULL;
+        for (unsigned b = lane; b < gridDim.x; b += 32) {
+            const unsigned long long q = __ldcg(&mxparts[b]);
+            bm = q > bm ? q : bm;
+        }
+        bm = warp_max_u64(bm);
+        if (lane == 0) *xmax = __longlong_as_double((long long)bm);
+    }
     __shared__ double s_tot[2];
     if (warp < 2) {
         double s = 0.0;
-        if (warp < nt)
+        if (warp < nt) {
+#pragma unroll 4
             for (int k = lane; k < nblocks; k += 32) s += totpart[(size_t)warp * nblocks + k];
+        }
         s = warp_sum_d(s);
         if (lane == 0) s_tot[warp] = s;
     }
@@ -886,6 +935,12 @@ __global__ void __launch_bounds__(kLbBlock) k_lb_pair(
     __shared__ double r[kLbPairSums];
     if (!lb_reduce<kLbPairSums>(v, parts, &st->counter, r)) return;
     if (threadIdx.x != 0) return;
+    // The scalar recursion works on a shared-memory copy of the state: its
+    // chains of dependent reads then wait on shared memory, not on L2.
+    __shared__ LbState s_st;
+    s_st = *st;
+    LbState* const gst = st;
+    st = &s_st;
     constexpr int M = kLbM;
     double SV[M], YV[M];
     for (int k = 0; k < M; ++k) {
@@ -917,47 +972,65 @@ __global__ void __launch_bounds__(kLbBlock) k_lb_pair(
     // apply_Hv(g, a = -1, res): res = a g; newest to oldest:
     // alpha_j = s_j'res / ys_j, res -= alpha_j y_j; res /= theta; oldest to
     // newest: beta_j = y_j'res / ys_j, res += (alpha_j - beta_j) s_j.
+    // The recursion runs in age order (age 0 = the newest pair) with every
+    // index known at compile time, so alpha and beta stay in registers and
+    // the Gram-matrix reads (shared memory) do not wait on the chain.
     const double av = -1.0, theta = st->theta;
     const int ncorr = st->ncorr;
+    const int newest = (st->ptr + M - 1) % M;
+    int slot[M];
+#pragma unroll
+    for (int a = 0; a < M; ++a) slot[a] = (newest + M - a) % M;
     double alpha[M], beta[M];
-    int order[M];
-    int j = st->ptr % M;
-    for (int i = 0; i < ncorr; ++i) {
-        j = (j + M - 1) % M;
-        double sres = av * SV[j];
-        for (int q = 0; q < i; ++q) sres -= alpha[order[q]] * st->SY[j][order[q]];
-        alpha[j] = sres / st->ys[j];
-        order[i] = j;
-    }
-    for (int i = 0; i < ncorr; ++i) {
-        // j is the oldest pair here, then moves to newer ones
-        double yres = av * YV[j];
-        for (int q = 0; q < ncorr; ++q) yres -= alpha[order[q]] * st->YY[j][order[q]];
-        yres /= theta;
-        for (int q = 0; q < i; ++q) {
-            const int k = (j + M - 1 - q) % M;  // the pairs already added, newest first
-            yres += (alpha[k] - beta[k]) * st->SY[k][j];
+#pragma unroll
+    for (int i = 0; i < M; ++i) {
+        alpha[i] = 0.0;
+        if (i < ncorr) {
+            double sres = av * SV[slot[i]];
+#pragma unroll
+            for (int q = 0; q < i; ++q) sres -= alpha[q] * st->SY[slot[i]][slot[q]];
+            alpha[i] = sres / st->ys[slot[i]];
         }
-        beta[j] = yres / st->ys[j];
-        j = (j + 1) % M;
+    }
+#pragma unroll
+    for (int i = M - 1; i >= 0; --i) {
+        beta[i] = 0.0;
+        if (i < ncorr) {
+            // pair i, then newer ones; the older ones (q > i) are added
+            double yres = av * YV[slot[i]];
+#pragma unroll
+            for (int q = 0; q < M; ++q)
+                if (q < ncorr) yres -= alpha[q] * st->YY[slot[i]][slot[q]];
+            yres /= theta;
+#pragma unroll
+            for (int q = i + 1; q < M; ++q)
+                if (q < ncorr) yres += (alpha[q] - beta[q]) * st->SY[slot[q]][slot[i]];
+            beta[i] = yres / st->ys[slot[i]];
+        }
     }
     st->cv = av / theta;
     for (int k = 0; k < M; ++k) {
         st->cy[k] = 0.0;
         st->cs[k] = 0.0;
     }
-    for (int q = 0; q < ncorr; ++q) {
-        const int k = order[q];
-        st->cy[k] = -alpha[k] / theta;
-        st->cs[k] = alpha[k] - beta[k];
+#pragma unroll
+    for (int a = 0; a < M; ++a) {
+        if (a < ncorr) {
+            st->cy[slot[a]] = -alpha[a] / theta;
+            st->cs[slot[a]] = alpha[a] - beta[a];
+        }
     }
+    *gst = s_st;
 }
 
 // drt = cv g + sum_k cy[k] y_k + cs[k] s_k over the stored pairs, and g'drt.
+// With xt given, also the first trial point xt = xp + step drt.
 __global__ void __launch_bounds__(kLbBlock) k_lb_dir(const double* __restrict__ g,
                                                      const double* __restrict__ pairs, int N,
                                                      double* __restrict__ drt, double* parts,
-                                                     LbState* st, LbScal* out) {
+                                                     LbState* st, LbScal* out,
+                                                     const double* __restrict__ xp, double step,
+                                                     double* __restrict__ xt) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     double v[1] = {0.0};
     if (t < N) {
@@ -970,6 +1043,7 @@ __global__ void __launch_bounds__(kLbBlock) k_lb_dir(const double* __restrict__ 
             d += st->cs[k] * pairs[(size_t)(2 * ph) * N + t];
         }
         drt[t] = d;
+        if (xt) xt[t] = xp[t] + step * d;
         v[0] = gt * d;
     }
     __shared__ double r[1];
@@ -1015,6 +1089,10 @@ void qrot_lbfgs_dual_device(regot_ctx* ctx, regot_dproblem* P, double reg, doubl
     DBuf<LbState> dstate(1, st);
     DBuf<LbScal> dscal(1, st);
     DBuf<double> grid(1, st);
+    // max |x| of each iterate buffer, written by the merge of the pass at x
+    // (the split grid of a line search from x)
+    DBuf<double> xmax(3, st);
+    DBuf<unsigned long long> mxparts(gN, st);
     pairs.zero();
     {
         LbState s0{};
@@ -1049,66 +1127,65 @@ void qrot_lbfgs_dual_device(regot_ctx* ctx, regot_dproblem* P, double reg, doubl
     // the record has reached the host.
     // Merge of the last pass at x into grad and the record, and its copy to
     // the host (not waited for).
-    auto merge_launch = [&](int op, int nt, const double* x, double* g) {
+    auto merge_launch = [&](int op, int nt, const double* x, double* g, double* xm) {
         const int blocks = pass_blocks(op, mixed, n, m);
         if (mixed)
             k_lb_merge<float><<<gN, kLbBlock, 0, st>>>(
                 (const float*)ops.buf().rowpart.get(), sh.nslabs,
                 (const float*)ops.buf().colpart.get(), sh.nrb, n, m, ops.buf().totpart.get(),
                 blocks, nt, x, drt.get(), P->a, P->b, reg, g, parts.get(), dstate.get(),
-                dscal.get());
+                dscal.get(), mxparts.get(), xm);
         else
             k_lb_merge<double><<<gN, kLbBlock, 0, st>>>(
                 (const double*)ops.buf().rowpart.get(), sh.nslabs,
                 (const double*)ops.buf().colpart.get(), sh.nrb, n, m, ops.buf().totpart.get(),
                 blocks, nt, x, drt.get(), P->a, P->b, reg, g, parts.get(), dstate.get(),
-                dscal.get());
+                dscal.get(), mxparts.get(), xm);
         count_launch();
         REGOT_CHECK_LAUNCH();
         d2h(hs, dscal.get(), sizeof(LbScal), st);
     };
-    // f and grad at x (the Q_GRAD pass), as Problem::dual_obj_grad: enqueued.
-    auto eval_launch = [&](const double* x, double* g) {
-        ops.maxabs(x, N, nullptr, 0, grid.get());
+    // f and grad at x in buffer xi (the Q_GRAD pass), as
+    // Problem::dual_obj_grad: enqueued. Only a mixed pass splits x, on the
+    // grid of max |x|.
+    auto eval_launch = [&](int xi, double* g) {
+        const double* x = xbuf(xi);
+        if (mixed) ops.maxabs(x, N, nullptr, 0, grid.get());
         PassParams p = ops.base_params();
         p.ra = x;
         p.cb = x + n;
         p.grid = grid.get();
         ops.pass(OP_Q_GRAD, p);
-        merge_launch(OP_Q_GRAD, 1, x, g);
+        merge_launch(OP_Q_GRAD, 1, x, g, xmax.get() + xi);
     };
-    auto eval_at = [&](const double* x, double* g) {
-        eval_launch(x, g);
+    auto eval_at = [&](int xi, double* g) {
+        eval_launch(xi, g);
         sync(st);
         E.add_passes(1);
         return 0.5 * hs->sq - reg * hs->dab;
     };
-    // Trial at xp + s drt into buffers (xt, gt): the axpy, the trial pass
-    // (mixed: OP_Q_GRADLS from the split of xp and drt, made here when
-    // `split` is set; FP64: OP_Q_GRAD at the trial point) and the merge;
-    // enqueued, not waited for.
-    auto trial_launch = [&](int xpi, int xti, int gti, double s, bool split) {
-        k_lb_axpy<<<gN, kLbBlock, 0, st>>>(xbuf(xpi), drt.get(), s, N, xbuf(xti));
-        count_launch();
-        if (mixed) {
-            PassParams p = ops.base_params();
-            p.ra = xbuf(xpi);
-            p.cb = xbuf(xpi) + n;
-            p.rd = drt.get();
-            p.cd = drt.get() + n;
-            p.steps[0] = s;
-            p.nsteps = 1;
-            p.grid = grid.get();
-            if (split) {
-                ops.maxabs(xbuf(xpi), N, nullptr, 0, grid.get());
-                ops.pass(OP_Q_GRADLS, p);
-            } else {
-                ops.pass_presplit(OP_Q_GRADLS, p);
-            }
-            merge_launch(OP_Q_GRADLS, 2, xbuf(xti), gbuf(gti));
-        } else {
-            eval_launch(xbuf(xti), gbuf(gti));
+    // Trial at xp + s drt into buffers (xt, gt): the axpy (unless the
+    // direction kernel wrote the point), the trial pass OP_Q_GRADLS (the
+    // gradient at the trial point and the objective change from xp without
+    // cancellation; mixed: from the split of xp and drt, made here when
+    // `split` is set, on the grid of max |xp| from xp's merge) and the
+    // merge; enqueued, not waited for.
+    auto trial_launch = [&](int xpi, int xti, int gti, double s, bool split, bool have_x) {
+        if (!have_x) {
+            k_lb_axpy<<<gN, kLbBlock, 0, st>>>(xbuf(xpi), drt.get(), s, N, xbuf(xti));
+            count_launch();
         }
+        PassParams p = ops.base_params();
+        p.ra = xbuf(xpi);
+        p.cb = xbuf(xpi) + n;
+        p.rd = drt.get();
+        p.cd = drt.get() + n;
+        p.steps[0] = s;
+        p.nsteps = 1;
+        p.grid = xmax.get() + xpi;
+        if (split) ops.pass(OP_Q_GRADLS, p);
+        else ops.pass_presplit(OP_Q_GRADLS, p);
+        merge_launch(OP_Q_GRADLS, 2, xbuf(xti), gbuf(gti), xmax.get() + xti);
     };
     // From the second iteration on, the correction pair, the new direction
     // and the first trial of the next line search (step 1, base = the
@@ -1135,9 +1212,10 @@ void qrot_lbfgs_dual_device(regot_ctx* ctx, regot_dproblem* P, double reg, doubl
             k_lb_pair<<<gN, kLbBlock, 0, st>>>(xbuf(xi), xbuf(xpi), gbuf(gi), gbuf(gpi),
                                                pairs.get(), N, parts.get(), dstate.get());
             k_lb_dir<<<gN, kLbBlock, 0, st>>>(gbuf(gi), pairs.get(), N, drt.get(), parts.get(),
-                                              dstate.get(), dscal.get());
+                                              dstate.get(), dscal.get(), xbuf(xi), 1.0,
+                                              xbuf((xi + 1) % 3));
             count_launch(2);
-            trial_launch(xi, (xi + 1) % 3, (gi + 1) % 3, 1.0, true);
+            trial_launch(xi, (xi + 1) % 3, (gi + 1) % 3, 1.0, true, true);
         } catch (...) {
             cudaGraph_t g = nullptr;
             cudaStreamEndCapture(st, &g);
@@ -1157,7 +1235,7 @@ void qrot_lbfgs_dual_device(regot_ctx* ctx, regot_dproblem* P, double reg, doubl
     };
 
     int ix = 0, ig = 0;
-    double fx = eval_at(xbuf(ix), gbuf(ig));
+    double fx = eval_at(ix, gbuf(ig));
     double last_obj = fx;
     double gg = hs->gg, xx = hs->xx;
     int it = 0;
@@ -1186,7 +1264,7 @@ void qrot_lbfgs_dual_device(regot_ctx* ctx, regot_dproblem* P, double reg, doubl
     } else {
         // drt = -g (LBFGS.h:104), its g'drt; step = 1 / |drt|
         k_lb_dir<<<gN, kLbBlock, 0, st>>>(gbuf(ig), pairs.get(), N, drt.get(), parts.get(),
-                                          dstate.get(), dscal.get());
+                                          dstate.get(), dscal.get(), nullptr, 0.0, nullptr);
         count_launch();
         REGOT_CHECK_LAUNCH();
         double step = 1.0 / gnorm;
@@ -1212,21 +1290,19 @@ void qrot_lbfgs_dual_device(regot_ctx* ctx, regot_dproblem* P, double reg, doubl
                     // the first trial (step 1) ran in the iteration's graph
                     pre_launched = false;
                 } else {
-                    trial_launch(ixp, ixt, igt, s, !split_done);
+                    trial_launch(ixp, ixt, igt, s, !split_done, false);
                 }
                 split_done = true;
                 sync(st);
                 E.add_passes(1);
-                double f;
-                if (mixed) {
-                    if (!dg_known) dg_init = hs->dg0;
-                    last_obj = 0.5 * hs->sq - reg * hs->dab;
-                    f = fx_init + s * dg_init + hs->rem;
-                } else {
-                    f = 0.5 * hs->sq - reg * hs->dab;
-                    if (!dg_known) dg_init = hs->dg0;
-                    last_obj = f;
-                }
+                // The decrease tests use the exact change f(xp + s d) - f(xp)
+                // = s g'd + rem: near the solution the change falls below the
+                // rounding of f itself, where a difference of two evaluated
+                // objectives is noise and the line search fails by chance.
+                // The reported objective is the evaluated one.
+                if (!dg_known) dg_init = hs->dg0;
+                last_obj = 0.5 * hs->sq - reg * hs->dab;
+                const double f = fx_init + s * dg_init + hs->rem;
                 if (!dg_known) {
                     dg_known = true;
                     if (dg_init > 0.0)

@@ -48,6 +48,7 @@ void erot_contract_tc(regot_ctx* ctx, regot_dproblem* P, double reg, const doubl
 // choice; returns the previous forced value), and the timed choices made on
 // this device so far (-1: none yet) for the classes d <= 4, 8, 16.
 int force_batch_variant(int v);
+int force_sparsify_path(int shared_memory);
 std::vector<int> batch_variants();
 // Batched BCD over point-cloud problems (erot_batch.cu).
 // cost, grad_x, grad_y (host, optional): each problem's regularised OT cost

@@ -152,6 +152,7 @@ EXPORTS = [
     "regot_set_wait_limit", "regot_autotune", "regot_autotune_save", "regot_autotune_load",
     "regot_autotune_clear", "regot_autotune_entries", "regot_force_pass_config",
     "regot_pass_config", "regot_force_batch_variant", "regot_batch_variants",
+    "regot_force_sparsify_path",
     "regot_erot_dual_obj_grad_noalloc", "regot_host_alloc", "regot_host_free",
 ]
 
@@ -228,6 +229,7 @@ def load() -> C.CDLL:
         lib.regot_force_pass_config.argtypes = [C.c_int]
         lib.regot_pass_config.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int]
         lib.regot_force_batch_variant.argtypes = [C.c_int]
+        lib.regot_force_sparsify_path.argtypes = [C.c_int]
         lib.regot_batch_variants.argtypes = [vp, C.POINTER(C.c_int)]
         lib.regot_erot_solve_batched.argtypes = [vp, C.POINTER(BatchDesc), C.c_double,
                                                  C.c_double, C.c_int, C.POINTER(BatchResult)]

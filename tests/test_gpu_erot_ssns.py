@@ -57,6 +57,45 @@ def test_sparsify_pattern(precision, hint):
             assert abs(nnz_g - nnz_o) <= max(3, 2e-3 * nnz_o)
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("shape", [(300, 257), (1000, 1537), (2100, 700)])
+def test_sparsify_register_path_matches_shared_memory_path(precision, shape):
+    # The selection stages have two implementations (rows and columns in
+    # registers, or in shared memory for longer ones); on the same T they
+    # keep exactly the same entries, in both sparsifications. The shapes give
+    # 4, 8 and 16 register values per thread.
+    from regot import _lib
+
+    lib = _lib.load()
+    n, m = shape
+    M, a, b = erot_points(n, m, seed=6, dtype=np.float64)
+    Mq = _as_precision(M, precision)
+    reg = 0.02
+    gamma = _partial_duals(Mq, a, b, reg, 4)
+    _, g = O.erot_dual_obj_grad(Mq, a, b, reg, gamma)
+    gn = np.linalg.norm(g)
+    P = regot.Problem(M, a, b, precision=precision)
+
+    def both(fn):
+        first = fn()
+        old = lib.regot_force_sparsify_path(1)
+        try:
+            second = fn()
+        finally:
+            assert lib.regot_force_sparsify_path(old) == 1
+        return first, second
+
+    for delta, hint in [(0.01 * gn, 0.001), (0.3 * gn, 0.5), (1e-4, 0.001), (0.0, 0.5)]:
+        (nr, Kr), (ns, Ks) = both(lambda: P.erot_sparsify(reg, gamma, delta, hint))
+        assert nr == ns, delta
+        assert np.array_equal(Kr, Ks), (delta, np.count_nonzero(Kr != Ks))
+    for density in (0.02, 0.3):
+        (nr, Kr), (ns, Ks) = both(lambda: P.erot_sparsify_density(reg, gamma, density))
+        assert nr == ns, density
+        assert np.array_equal(Kr, Ks), (density, np.count_nonzero(Kr != Ks))
+    P.close()
+
+
 @pytest.mark.parametrize("hint", [0.001, 0.5])
 def test_sparsify_large_delta_branches(hint):
     # Column sums below delta: find_small drops every entry, find_large keeps
