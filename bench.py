@@ -505,6 +505,56 @@ def run_configs(args):
         print(json.dumps(line), flush=True)
 
 
+def ncu_case_more(kind):
+    """Small invocations of the solver kernels for ncu captures (no timing).
+
+    sparsify: the SSNS sparsification at n = m = 8192 (mixed, reg 0.01, at
+    the duals of a BCD solve to 1e-4), then two SSNS iterations (their
+    Schur-complement CG steps). qrot: qrot_lbfgs_dual (20 iterations) and
+    qrot_assn (10 iterations) on the large QROT problem (n = m = 4096,
+    seed 1, reg 0.1, mixed). contract: the tensor-core contractions T Y and
+    T'X at n = m = 4096, d = 64 (mixed, at the duals of a BCD solve).
+    newton: three sinkhorn_newton iterations at n = m = 8192 (mixed,
+    reg 0.01) from the duals of a BCD solve to 1e-4."""
+    import regot
+    from problems import erot_points, qrot_points
+
+    if kind == "newton":
+        M, a, b = erot_points(N, N, seed=0, dtype=np.float32)
+        P = regot.Problem(M, a, b, precision="mixed")
+        r = P.sinkhorn_bcd(REG, tol=1e-4, max_iter=3000, plan=False)
+        g0 = np.asarray(r.dual)
+        rn = P.sinkhorn_newton(REG, tol=1e-6, max_iter=3, plan=False, x0=g0)
+        print("ncu case (newton): niter", rn.niter, "passes", rn.passes)
+    elif kind == "sparsify":
+        M, a, b = erot_points(N, N, seed=0, dtype=np.float32)
+        P = regot.Problem(M, a, b, precision="mixed")
+        r = P.sinkhorn_bcd(REG, tol=1e-4, max_iter=3000, plan=False)
+        _, g = P.erot_dual_obj_grad(REG, np.asarray(r.dual))
+        nnz, _ = P.erot_sparsify(REG, r.dual, 0.01 * float(np.linalg.norm(g)), 0.001, mask=False)
+        rs = P.sinkhorn_ssns(REG, tol=1e-6, max_iter=2, plan=False)
+        print("ncu case (sparsify): nnz", nnz, "ssns niter", rs.niter)
+    elif kind == "qrot":
+        M, a, b = qrot_points(4096, 4096, seed=1, dtype=np.float32)
+        P = regot.Problem(M, a, b, precision="mixed")
+        rl = P.qrot_lbfgs_dual(0.1, tol=0.0, max_iter=20, prim_vals=False, plan=False)
+        ra = P.qrot_assn(0.1, tol=1e-6, max_iter=10, prim_vals=False, plan=False)
+        print("ncu case (qrot): lbfgs niter", rl.niter, "assn niter", ra.niter)
+    else:
+        n, d, reg = 4096, 64, 0.05
+        rng = np.random.default_rng(3)
+        x = rng.standard_normal((n, d)).astype(np.float32)
+        y = rng.standard_normal((n, d)).astype(np.float32)
+        M = (((x[:, None, :] - y[None, :, :]) ** 2).sum(-1) / d).astype(np.float32)
+        a = np.full(n, 1.0 / n)
+        P = regot.Problem(M, a, a, precision="mixed")
+        r = P.sinkhorn_bcd(reg, tol=1e-6, max_iter=500, plan=False)
+        s1, _ = P.erot_tyy(reg, r.dual, y.astype(np.float64))
+        s2, _ = P.erot_tty(reg, r.dual, x.astype(np.float64))
+        print("ncu case (contract): row sums err", float(np.abs(s1 - a).max()))
+    P.close()
+
+
 def run_autograd(args):
     """One JSON line for the autograd workload: x, y in R^{4096 x 64} ~ N(0, I)
     (seed 3, FP32 on the device), M = |x - y|^2 / 64, uniform weights, reg 0.05;
@@ -720,12 +770,14 @@ def main():
     ap.add_argument("--ncu-case", action="store_true",
                     help="a few passes for an ncu capture (no timing, no JSON)")
     ap.add_argument("--workload",
-                    choices=["bcd", "batched", "solvers", "autograd", "passes", "configs"],
+                    choices=["bcd", "batched", "solvers", "autograd", "passes", "configs",
+                             "sparsify", "qrot", "contract", "newton"],
                     default="bcd",
                     help="batched: the batched uneven-problem workload (its own JSON line); "
                          "solvers: one line per solver of the solver table; "
                          "configs: the README-example and large-QROT configurations, GPU "
-                         "beside the FP64 oracle")
+                         "beside the FP64 oracle; sparsify, qrot, contract, newton: ncu "
+                         "cases only")
     ap.add_argument("--probe", choices=["hbm-read", "host-link"],
                     help="measure the ceilings the numbers are read against (no JSON line)")
     args = ap.parse_args()
@@ -754,6 +806,9 @@ def main():
             r = regot.sinkhorn_bcd_batched(xs, ys, as_, bs, 0.05, tol=1e-6, max_iter=2,
                                            cost_scale=sc, grad=True)
             print("ncu case (batched): sweeps", r.sweeps)
+            return
+        if args.workload in ("sparsify", "qrot", "contract", "newton"):
+            ncu_case_more(args.workload)
             return
         M, a, b = erot_points(n, n, seed=0, dtype=np.float32)
         prob = regot.Problem(M, a, b, precision="mixed")

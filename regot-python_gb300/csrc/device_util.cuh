@@ -160,7 +160,10 @@ __device__ __forceinline__ double max_strided(const Acc* p, int count, size_t st
 // per-block partials with all its threads (thread t takes blocks t, t + bs,
 // ... in order, then a fixed butterfly and warp order), so the result does
 // not depend on which block finishes last.
-template <int K>
+// LANE0: only lane 0 of each warp holds nonzero values (warp-per-item
+// kernels); the warp sums are then lane 0's values, read without the
+// FP64 butterfly (adding the other lanes' zeros would not change them).
+template <int K, bool LANE0 = false>
 __device__ bool grid_reduce(const double (&vals)[K], double* block_parts, unsigned* counter,
                             double (&out)[K]) {
     __shared__ double s_red[K][32];
@@ -171,7 +174,7 @@ __device__ bool grid_reduce(const double (&vals)[K], double* block_parts, unsign
     const int nw = (nthreads + 31) >> 5;
 #pragma unroll
     for (int k = 0; k < K; ++k) {
-        const double v = warp_sum_d(vals[k]);
+        const double v = LANE0 ? vals[k] : warp_sum_d(vals[k]);
         if (lane == 0) s_red[k][warp] = v;
     }
     __syncthreads();

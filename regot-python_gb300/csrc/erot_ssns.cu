@@ -1130,7 +1130,7 @@ __global__ void k_schur_init(Sparse S, const double* g, const double* u, const d
     }
     double out[2];
     __threadfence();
-    if (grid_reduce<2>(v, parts, &st->counter, out)) {
+    if (grid_reduce<2, true>(v, parts, &st->counter, out)) {
         st->thresh2 = fmax(tol * tol * out[0], 2.2250738585072014e-308);
         st->rr = out[0];
         st->absnew = out[1];
@@ -1171,7 +1171,7 @@ __global__ void k_schur_cols(Sparse S, const double* p, const double* u, const d
     }
     double out[1];
     __threadfence();
-    if (grid_reduce<1>(v, parts, &st->counter, out)) st->alpha = st->absnew / out[0];
+    if (grid_reduce<1, true>(v, parts, &st->counter, out)) st->alpha = st->absnew / out[0];
 }
 
 // x += alpha p, r -= alpha q, z = r / diag; stop on ||r||^2 < thresh2 or
@@ -1249,7 +1249,7 @@ __global__ void k_dhd_rows(Sparse S, const double* dir, const double* g, const d
     }
     double out[2];
     __threadfence();
-    if (grid_reduce<2>(v, parts, &st->counter, out)) {
+    if (grid_reduce<2, true>(v, parts, &st->counter, out)) {
         st->dhd = out[0];
         st->gtd = out[1];
     }
@@ -1270,7 +1270,7 @@ __global__ void k_dhd_cols(Sparse S, const double* dir, const double* g, const d
     }
     double out[2];
     __threadfence();
-    if (grid_reduce<2>(v, parts, &st->counter, out)) {
+    if (grid_reduce<2, true>(v, parts, &st->counter, out)) {
         st->dhd += out[0];
         st->gtd += out[1];
     }
@@ -1986,11 +1986,15 @@ void run_ssns(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, int max
         E.dir_dots();
         hs = E.read_state();
         const double gtd = hs.gtd, dhd = hs.dhd;
-        // line_selection: first candidate below f, else the best.
+        // line_selection: first candidate below f, else the best. The full
+        // step is evaluated alone first (one series per entry instead of
+        // four); the other three only when it does not decrease f. The
+        // per-step totals of a pass do not depend on which steps share it.
         double tots[4];
-        E.ls_pass(cands, 4, tots);
+        E.ls_pass(cands, 1, tots);
         double best = 1.0, best_df = std::numeric_limits<double>::infinity();
         for (int s = 0; s < 4; ++s) {
+            if (s == 1) E.ls_pass(cands + 1, 3, tots + 1);
             const double df = cands[s] * gtd + reg * tots[s];
             if (df < best_df) {
                 best = cands[s];

@@ -234,6 +234,90 @@ __global__ void k_sigma_rows(const uint32_t* bm, int n, int m, int nslabs, const
     if (lane == 0) out[i] = divide ? acc / (h1[i] + mu) : acc;
 }
 
+// Mixed engine: the same products with the vector given as FP32 (hi, lo)
+// pairs and summed in compensated FP32 (TwoSum), converted to FP64 once per
+// row. One FP64 add per set bit made these products FP64-bound on this part;
+// the compensated sums stay within about 2^-44 of sum |x_j| over the row.
+__device__ __forceinline__ float2 split_f2(double v) {
+    const float h = __double2float_rn(v);
+    return make_float2(h, __double2float_rn(v - (double)h));
+}
+__device__ __forceinline__ void cadd(float& s, float& e, float2 x) {
+    float t, te;
+    two_sum_f(s, x.x, t, te);
+    s = t;
+    e += te + x.y;
+}
+
+template <int CW, int VW, int LC>
+__global__ void k_sigma_rows_f(const uint32_t* bm, int n, int m, int nslabs, const float2* x2,
+                               const double* h1, double mu, const double* mu_dev, int divide,
+                               double* out, float2* out2, const int* done) {
+    if (done && *done) return;
+    if (mu_dev) mu = *mu_dev;
+    const int lane = threadIdx.x & 31;
+    const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (i >= n) return;
+    float s = 0.f, e = 0.f;
+    const uint32_t* row = bm + (size_t)i * nslabs * LC;
+    for (int sl = 0; sl < nslabs; ++sl) {
+#pragma unroll
+        for (int q = 0; q < LC; ++q) {
+            const uint32_t w = row[sl * LC + q];
+            if ((w >> lane) & 1u) cadd(s, e, x2[bit_col<CW, VW, LC>(sl, q, lane)]);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const float so = __shfl_xor_sync(0xffffffffu, s, o);
+        const float eo = __shfl_xor_sync(0xffffffffu, e, o);
+        float t, te;
+        two_sum_f(s, so, t, te);
+        s = t;
+        e += eo + te;
+    }
+    if (lane == 0) {
+        const double acc = (double)s + (double)e;
+        const double r = divide ? acc / (h1[i] + mu) : acc;
+        out[i] = r;
+        if (out2) out2[i] = split_f2(r);
+    }
+}
+
+template <int CW, int VW, int LC>
+__global__ void k_sigma_cols_f(const uint32_t* bm, int n, int m, int nslabs, const float2* y2,
+                               double* partial, const int* done) {
+    if (done && *done) return;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = blockIdx.y;
+    if (j >= m) return;
+    const int sl = j / CW, o = j - sl * CW;
+    const int L = (o % (32 * VW)) / VW;
+    const int q = (o / (32 * VW)) * VW + (o % VW);
+    const int rows_per = (n + gridDim.y - 1) / gridDim.y;
+    const int i0 = c * rows_per, i1 = min(n, i0 + rows_per);
+    float s = 0.f, e = 0.f;
+    int i = i0;
+    for (; i + 8 <= i1; i += 8) {
+        // eight rows' words and values in flight at once
+        uint32_t w[8];
+        float2 yv[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            w[u] = bm[((size_t)(i + u) * nslabs + sl) * LC + q];
+            yv[u] = y2[i + u];
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+            if ((w[u] >> L) & 1u) cadd(s, e, yv[u]);
+    }
+    for (; i < i1; ++i) {
+        const uint32_t w = bm[((size_t)i * nslabs + sl) * LC + q];
+        if ((w >> L) & 1u) cadd(s, e, y2[i]);
+    }
+    partial[(size_t)c * m + j] = (double)s + (double)e;
+}
+
 // partial[c][j] = sum_{i in chunk c} sigma_ij y_i
 template <int CW, int VW, int LC>
 __global__ void k_sigma_cols(const uint32_t* bm, int n, int m, int nslabs, const double* y,
@@ -248,7 +332,20 @@ __global__ void k_sigma_cols(const uint32_t* bm, int n, int m, int nslabs, const
     const int rows_per = (n + gridDim.y - 1) / gridDim.y;
     const int i0 = c * rows_per, i1 = min(n, i0 + rows_per);
     double acc = 0.0;
-    for (int i = i0; i < i1; ++i) {
+    int i = i0;
+    for (; i + 8 <= i1; i += 8) {
+        uint32_t w[8];
+        double yv[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            w[u] = bm[((size_t)(i + u) * nslabs + s) * LC + q];
+            yv[u] = y[i + u];
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+            if ((w[u] >> L) & 1u) acc += yv[u];
+    }
+    for (; i < i1; ++i) {
         const uint32_t w = bm[((size_t)i * nslabs + s) * LC + q];
         if ((w >> L) & 1u) acc += y[i];
     }
@@ -256,14 +353,18 @@ __global__ void k_sigma_cols(const uint32_t* bm, int n, int m, int nslabs, const
 }
 
 // ---- ASSN Schur-complement CG: Delta x = h2 o x + mu x - sigma' ((sigma x) / (h1 + mu)) ----
+// The float2 arguments (mixed engine, else null) receive the FP32 (hi, lo)
+// copies of the vectors the sigma products read.
 __global__ void k_acg_init(int m, const double* zy, double tol, double* x, double* r, double* p,
-                           double* parts, QState* st) {
+                           double* parts, QState* st, float2* x2, float2* p2) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     double v[1] = {0.0};
     if (j < m) {
         x[j] = 0.0;
         r[j] = zy[j];
         p[j] = zy[j];
+        if (x2) x2[j] = make_float2(0.f, 0.f);
+        if (p2) p2[j] = split_f2(zy[j]);
         v[0] = zy[j] * zy[j];
     }
     double out[1];
@@ -284,6 +385,7 @@ __global__ void k_acg_a(int m, const double* partial, int chunks, const double* 
     double v[1] = {0.0};
     if (j < m) {
         double u = 0.0;
+#pragma unroll 8
         for (int c = 0; c < chunks; ++c) u += partial[(size_t)c * m + j];
         const double yj = h2[j] * p[j] + mu * p[j] - u;
         y[j] = yj;
@@ -295,13 +397,15 @@ __global__ void k_acg_a(int m, const double* partial, int chunks, const double* 
 }
 
 __global__ void k_acg_b(int m, const double* p, const double* y, double* x, double* r,
-                        double* parts, QState* st) {
+                        double* parts, QState* st, float2* x2) {
     if (st->cg_done) return;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const double al = st->alpha;
     double v[1] = {0.0};
     if (j < m) {
-        x[j] += al * p[j];
+        const double xj = x[j] + al * p[j];
+        x[j] = xj;
+        if (x2) x2[j] = split_f2(xj);
         const double rj = r[j] - al * y[j];
         r[j] = rj;
         v[0] = rj * rj;
@@ -319,16 +423,25 @@ __global__ void k_acg_b(int m, const double* p, const double* y, double* x, doub
     }
 }
 
-__global__ void k_acg_c(int m, const double* r, double* p, QState* st) {
+__global__ void k_acg_c(int m, const double* r, double* p, QState* st, float2* p2) {
     if (st->cg_done) return;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j < m) p[j] = r[j] + st->beta * p[j];
+    if (j < m) {
+        const double pj = r[j] + st->beta * p[j];
+        p[j] = pj;
+        if (p2) p2[j] = split_f2(pj);
+    }
 }
 
 // w / (h1 + mu) for the Schur right-hand side
-__global__ void k_div_h1(int n, const double* w, const double* h1, double mu, double* out) {
+__global__ void k_div_h1(int n, const double* w, const double* h1, double mu, double* out,
+                         float2* out2) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] = w[i] / (h1[i] + mu);
+    if (i < n) {
+        const double v = w[i] / (h1[i] + mu);
+        out[i] = v;
+        if (out2) out2[i] = split_f2(v);
+    }
 }
 // zy_j = rhs_j - sum_c partial[c][j]
 __global__ void k_sub_partial(int m, const double* rhs, const double* partial, int chunks,
@@ -336,6 +449,7 @@ __global__ void k_sub_partial(int m, const double* rhs, const double* partial, i
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= m) return;
     double u = 0.0;
+#pragma unroll 8
     for (int c = 0; c < chunks; ++c) u += partial[(size_t)c * m + j];
     out[j] = rhs[j] - u;
 }
@@ -588,11 +702,18 @@ public:
         throw Error(REGOT_ERR_NUMERIC, "optimal_alpha did not converge");
     }
 
-    // sigma x (n) with optional division by (h1 + mu); mu from *mu_dev when given
-    void sigma_rows(const double* x, double mu, bool divide, double* out, const int* done,
-                    const double* mu_dev = nullptr) {
+    // sigma x (n) with optional division by (h1 + mu); mu from *mu_dev when
+    // given. With x2 (the FP32 pairs of x; mixed engine) the compensated
+    // FP32 kernel runs and out2, if given, receives the pairs of the result.
+    void sigma_rows(const double* x, const float2* x2, double mu, bool divide, double* out,
+                    float2* out2, const int* done, const double* mu_dev = nullptr) {
         const int warps = 8;
-        if (mixed_)
+        if (mixed_ && x2)
+            k_sigma_rows_f<Geo<float>::CW, Geo<float>::VW, Geo<float>::LC>
+                <<<cdiv(n_, warps), warps * 32, 0, st_>>>(bm_.get(), n_, m_, nslabs(), x2,
+                                                          h_.get(), mu, mu_dev, divide ? 1 : 0,
+                                                          out, out2, done);
+        else if (mixed_)
             k_sigma_rows<Geo<float>::CW, Geo<float>::VW, Geo<float>::LC>
                 <<<cdiv(n_, warps), warps * 32, 0, st_>>>(bm_.get(), n_, m_, nslabs(), x, h_.get(),
                                                           mu, mu_dev, divide ? 1 : 0, out, done);
@@ -602,10 +723,13 @@ public:
                                                           mu, mu_dev, divide ? 1 : 0, out, done);
         count_launch();
     }
-    // partial sums of sigma' y over kColChunks row chunks
-    void sigma_cols(const double* y, double* partial, const int* done) {
+    // partial sums of sigma' y over kColChunks row chunks (y2 as for x2 above)
+    void sigma_cols(const double* y, const float2* y2, double* partial, const int* done) {
         dim3 grid(cdiv(m_, 128), kColChunks);
-        if (mixed_)
+        if (mixed_ && y2)
+            k_sigma_cols_f<Geo<float>::CW, Geo<float>::VW, Geo<float>::LC>
+                <<<grid, 128, 0, st_>>>(bm_.get(), n_, m_, nslabs(), y2, partial, done);
+        else if (mixed_)
             k_sigma_cols<Geo<float>::CW, Geo<float>::VW, Geo<float>::LC>
                 <<<grid, 128, 0, st_>>>(bm_.get(), n_, m_, nslabs(), y, partial, done);
         else
@@ -613,6 +737,7 @@ public:
                 <<<grid, 128, 0, st_>>>(bm_.get(), n_, m_, nslabs(), y, partial, done);
         count_launch();
     }
+    bool mixed() const { return mixed_; }
     const double* h1() const { return h_.get(); }
     const double* h2() const { return h_.get() + n_; }
     double* parts() { return parts_.get(); }
@@ -719,47 +844,93 @@ void init_gamma(QrotEngine& E, const regot_opts& o, std::vector<double>& gamma) 
 
 namespace {
 
-// ---- L-BFGS on the device (qrot_lbfgs_dual) ----
+// ---- L-BFGS with device vectors (qrot_lbfgs_dual) ----
 // LBFGS++'s minimize and Nocedal-Wright line search (restated in lbfgs.h)
-// keep their control flow on the host, but every vector of the algorithm
+// keep their control flow on the host, and every vector of the algorithm
 // stays on the device: the iterates x, the gradients, the direction, and the
-// ring of m = 6 correction pairs (s, y). The two-loop recursion
-// (BFGSMat::apply_Hv, src/LBFGSpp/LBFGSpp/BFGSMat.h:276-302) is carried out
-// on scalars: with the Gram matrices S'Y and Y'Y of the stored pairs, kept
-// up to date as pairs are added, and the products S'g, Y'g, every alpha_j
-// and beta_j of the recursion follows from scalar recurrences, and the
-// direction is one linear combination of g and the pairs. A line-search
-// trial is an axpy, one dense pass and one merge kernel whose last block
-// writes every scalar the host needs (objective terms, g'd, |g|^2, |x|^2)
-// into one 64-byte record: one small copy and one synchronisation per trial.
+// ring of m = 6 correction pairs (s, y). A line-search trial is the trial
+// point, one dense pass and one merge kernel. The merge's last block writes
+// every scalar the host needs into one record: the objective terms, g'd,
+// |g|^2, |x|^2 and the 34 products of the trial's correction pair
+// (s = x - xp, y = g - gp, staged on the device) with the stored pairs and
+// with g. One small copy and one synchronisation per trial. The two-loop
+// recursion (BFGSMat::apply_Hv, src/LBFGSpp/LBFGSpp/BFGSMat.h:276-302) then
+// runs on the host on scalars: with the Gram matrices S'Y and Y'Y of the
+// stored pairs, kept up to date as pairs are added, every alpha_j and beta_j
+// follows from scalar recurrences, and the next direction is one linear
+// combination of g and the pairs, formed by one kernel from coefficients
+// the host copies to the device. (A single device thread ran this scalar
+// chain an order of magnitude slower: FP64 latency on this part.)
 constexpr int kLbM = 6;          // LBFGSParam m (Param.h:168-182)
 // Blocks of two warps: the vector kernels are FP64 work on n + m entries,
 // which this part issues at a small fraction of its FP32 rate per SM, so
 // they are spread over as many SMs as the vector length allows.
 constexpr int kLbBlock = 64;
 constexpr int kLbPairSums = 5 * kLbM + 4;
+constexpr int kLbBufs = 3;       // rotating iterate / gradient buffers
 
 struct LbScal {
     double sq;   // sum D^2 at the trial point
-    double rem;  // mixed trial: sum of the second-order remainders
+    double rem;  // sum of the second-order remainders of the change from xp
     double dab;  // x'(a, b)
     double dg;   // grad(x)' drt
     double gg;   // |grad(x)|^2
     double xx;   // |x|^2
     double dg0;  // grad' drt of a new direction
     double pad;
+    // products of the trial's pair (s, y) with the stored pairs (s_k, y_k)
+    // and the trial gradient g: [5k..5k+4] = s'y_k, s_k'y, y'y_k, s_k'g,
+    // y_k'g for ring slot k; then s'y, y'y, s'g, y'g
+    double prod[kLbPairSums];
 };
 
-struct LbState {
-    unsigned counter;
-    int ncorr, ptr;
-    int phys[kLbM + 1];  // logical slot -> physical pair buffer; [kLbM] is the staging buffer
-    double theta;
-    double ys[kLbM];
-    double SY[kLbM][kLbM];  // s_i' y_j (logical slots)
-    double YY[kLbM][kLbM];
+// Direction coefficients and buffer maps, written by the host.
+struct LbCoef {
     double cv, cy[kLbM], cs[kLbM];  // direction = cv g + sum_k cy[k] y_k + cs[k] s_k
+    int ncorr;
+    int phys[kLbM];      // ring slot -> physical pair buffer
+    int stage[kLbBufs];  // iterate buffer -> physical staging pair buffer
 };
+
+// Warp sums of K values per lane with about 1.1 K FP64 adds per lane instead
+// of 5 K: three halving exchanges (at lane distances 16, 8, 4 each lane
+// keeps half of its values and adds the partner's copy of that half), then
+// two plain exchanges on the K8 = ceil(K / 8) values left. Lane l then holds
+// the totals of values off(l) .. off(l) + K8 - 1 (off from lane bits 4, 3,
+// 2); put(k, total) is called once per value, from the lanes with bits 1
+// and 0 clear.
+template <int K, typename Put>
+__device__ __forceinline__ void warp_sums_multi(const double (&v)[K], int lane, Put put) {
+    constexpr int K8 = (K + 7) / 8;
+    constexpr int KP = 8 * K8;
+    double a[KP];
+#pragma unroll
+    for (int k = 0; k < KP; ++k) a[k] = k < K ? v[k] : 0.0;
+    int off = 0;
+#pragma unroll
+    for (int lev = 0; lev < 3; ++lev) {
+        const int o = 16 >> lev;
+        const int H = KP >> (lev + 1);  // values kept after this level
+        const bool upper = (lane & o) != 0;
+#pragma unroll
+        for (int i = 0; i < H; ++i) {
+            const double mine = upper ? a[i + H] : a[i];
+            const double send = upper ? a[i] : a[i + H];
+            a[i] = mine + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+        off += upper ? H : 0;
+    }
+#pragma unroll
+    for (int i = 0; i < K8; ++i) {
+        a[i] += __shfl_xor_sync(0xffffffffu, a[i], 2);
+        a[i] += __shfl_xor_sync(0xffffffffu, a[i], 1);
+    }
+    if ((lane & 3) == 0) {
+#pragma unroll
+        for (int i = 0; i < K8; ++i)
+            if (off + i < K) put(off + i, a[i]);
+    }
+}
 
 // Block sums of K values, then the last block to arrive adds the block sums
 // in block order: true in every thread of that block, with the totals in
@@ -774,11 +945,7 @@ __device__ bool lb_reduce(const double (&v)[K], double* parts, unsigned* counter
     __shared__ double s_red[K][NW];
     __shared__ int s_last;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-        const double x = warp_sum_d(v[k]);
-        if (lane == 0) s_red[k][warp] = x;
-    }
+    warp_sums_multi<K>(v, lane, [&](int k, double x) { s_red[k][warp] = x; });
     __syncthreads();
     if (tid < K) {
         double s = 0.0;
@@ -821,20 +988,29 @@ __global__ void k_lb_axpy(const double* __restrict__ xp, const double* __restric
     if (t < N) x[t] = xp[t] + step * d[t];
 }
 
-// Gradient of the last dense pass at x (rows, then columns: D1 - reg a,
-// D'1 - reg b), the record's dot products, and the pass totals (sum D^2 and,
-// with nt == 2, the remainder sum).
+// Gradient of the last dense pass at the trial point x (rows, then
+// columns: D1 - reg a, D'1 - reg b), the trial's correction pair s = x - xp,
+// y = g - gp into the staging buffer of x's buffer, the record's dot
+// products (with the pair products), the pass totals (sum D^2 and, with
+// nt == 2, the remainder sum) and max |x| beside x's buffer. Without gp
+// (the first evaluation) no pair is formed.
 template <typename Acc>
 __global__ void __launch_bounds__(kLbBlock) k_lb_merge(
     const Acc* __restrict__ rp, int nslabs, const Acc* __restrict__ cp, int nrb, int n, int m,
     const double* __restrict__ totpart, int nblocks, int nt, const double* __restrict__ x,
     const double* __restrict__ drt, const double* __restrict__ a, const double* __restrict__ b,
-    double reg, double* __restrict__ grad, double* parts, LbState* st, LbScal* out,
+    double reg, double* __restrict__ grad, const double* __restrict__ xp,
+    const double* __restrict__ gp, double* __restrict__ pairs, const LbCoef* __restrict__ cf,
+    int xbuf, double* parts, unsigned* counter, LbScal* out,
     unsigned long long* __restrict__ mxparts, double* __restrict__ xmax) {
+    constexpr int K = 4 + kLbPairSums;
+    const int N = n + m;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    double v[4] = {0.0, 0.0, 0.0, 0.0};
+    double v[K];
+#pragma unroll
+    for (int k = 0; k < K; ++k) v[k] = 0.0;
     unsigned long long xbits = 0ULL;
-    if (t < n + m) {
+    if (t < N) {
         double g, w;
         if (t < n) {
             g = merge_strided(rp + t, nslabs, (size_t)n) - reg * a[t];
@@ -851,6 +1027,29 @@ __global__ void __launch_bounds__(kLbBlock) k_lb_merge(
         v[1] = g * drt[t];
         v[2] = g * g;
         v[3] = xt * xt;
+        if (gp) {
+        const double sn = xt - xp[t], yn = g - gp[t];
+        const int stg = cf->stage[xbuf];
+        pairs[(size_t)(2 * stg) * N + t] = sn;
+        pairs[(size_t)(2 * stg + 1) * N + t] = yn;
+        int ph[kLbM];
+#pragma unroll
+        for (int k = 0; k < kLbM; ++k) ph[k] = cf->phys[k];
+#pragma unroll
+        for (int k = 0; k < kLbM; ++k) {
+            const double sk = pairs[(size_t)(2 * ph[k]) * N + t];
+            const double yk = pairs[(size_t)(2 * ph[k] + 1) * N + t];
+            v[4 + 5 * k + 0] = sn * yk;
+            v[4 + 5 * k + 1] = sk * yn;
+            v[4 + 5 * k + 2] = yn * yk;
+            v[4 + 5 * k + 3] = sk * g;
+            v[4 + 5 * k + 4] = yk * g;
+        }
+        v[4 + 5 * kLbM + 0] = sn * yn;
+        v[4 + 5 * kLbM + 1] = yn * yn;
+        v[4 + 5 * kLbM + 2] = sn * g;
+        v[4 + 5 * kLbM + 3] = yn * g;
+        }
     }
     // max |x| of this block (bit patterns of non-negative doubles order like
     // the values), for the split grid of a line search from x
@@ -865,8 +1064,8 @@ __global__ void __launch_bounds__(kLbBlock) k_lb_merge(
             mxparts[blockIdx.x] = bm;
         }
     }
-    __shared__ double s_sum[4];
-    if (!lb_reduce<4>(v, parts, &st->counter, s_sum)) return;
+    __shared__ double s_sum[K];
+    if (!lb_reduce<K>(v, parts, counter, s_sum)) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     if (warp == 0) {
         unsigned long long bm = 0ULL;
@@ -896,51 +1095,87 @@ __global__ void __launch_bounds__(kLbBlock) k_lb_merge(
         out->gg = s_sum[2];
         out->xx = s_sum[3];
     }
+    if (threadIdx.x < kLbPairSums) out->prod[threadIdx.x] = s_sum[4 + threadIdx.x];
 }
 
-// New correction pair s = x - xp, y = g - gp into the staging buffer, its
-// products with every stored pair and with g; the last block adds the pair
-// to the ring when s'y > eps y'y (BFGSMat::add_correction,
-// BFGSMat.h:81-100, as LBFGS.h:160-161 calls it), updates the Gram
-// matrices, and turns the two-loop recursion of apply_Hv(g, -1)
-// (BFGSMat.h:276-302) into the coefficients of the new direction.
-__global__ void __launch_bounds__(kLbBlock) k_lb_pair(
-    const double* __restrict__ x, const double* __restrict__ xp, const double* __restrict__ g,
-    const double* __restrict__ gp, double* __restrict__ pairs, int N, double* parts, LbState* st) {
+// drt = cv g + sum_k cy[k] y_k + cs[k] s_k over the stored pairs, and g'drt.
+// With xt given, also the first trial point xt = xp + step drt.
+__global__ void __launch_bounds__(kLbBlock) k_lb_dir(const double* __restrict__ g,
+                                                     const double* __restrict__ pairs, int N,
+                                                     double* __restrict__ drt, double* parts,
+                                                     unsigned* counter,
+                                                     const LbCoef* __restrict__ cf, LbScal* out,
+                                                     const double* __restrict__ xp, double step,
+                                                     double* __restrict__ xt) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    double v[kLbPairSums];
-#pragma unroll
-    for (int k = 0; k < kLbPairSums; ++k) v[k] = 0.0;
+    double v[1] = {0.0};
     if (t < N) {
-        const double s = x[t] - xp[t], y = g[t] - gp[t], gt = g[t];
-        const int stg = st->phys[kLbM];
-        pairs[(size_t)(2 * stg) * N + t] = s;
-        pairs[(size_t)(2 * stg + 1) * N + t] = y;
+        const double gt = g[t];
+        double d = cf->cv * gt;
+        const int ncorr = cf->ncorr;
+        int ph[kLbM];
+        double cy[kLbM], cs[kLbM];
 #pragma unroll
         for (int k = 0; k < kLbM; ++k) {
-            const int ph = st->phys[k];
-            const double sk = pairs[(size_t)(2 * ph) * N + t];
-            const double yk = pairs[(size_t)(2 * ph + 1) * N + t];
-            v[5 * k + 0] = s * yk;
-            v[5 * k + 1] = sk * y;
-            v[5 * k + 2] = y * yk;
-            v[5 * k + 3] = sk * gt;
-            v[5 * k + 4] = yk * gt;
+            ph[k] = cf->phys[k];
+            cy[k] = cf->cy[k];
+            cs[k] = cf->cs[k];
         }
-        v[5 * kLbM + 0] = s * y;
-        v[5 * kLbM + 1] = y * y;
-        v[5 * kLbM + 2] = s * gt;
-        v[5 * kLbM + 3] = y * gt;
+#pragma unroll
+        for (int k = 0; k < kLbM; ++k) {
+            if (k < ncorr) {
+                d += cy[k] * pairs[(size_t)(2 * ph[k] + 1) * N + t];
+                d += cs[k] * pairs[(size_t)(2 * ph[k]) * N + t];
+            }
+        }
+        drt[t] = d;
+        if (xt) xt[t] = xp[t] + step * d;
+        v[0] = gt * d;
     }
-    __shared__ double r[kLbPairSums];
-    if (!lb_reduce<kLbPairSums>(v, parts, &st->counter, r)) return;
-    if (threadIdx.x != 0) return;
-    // The scalar recursion works on a shared-memory copy of the state: its
-    // chains of dependent reads then wait on shared memory, not on L2.
-    __shared__ LbState s_st;
-    s_st = *st;
-    LbState* const gst = st;
-    st = &s_st;
+    __shared__ double r[1];
+    if (!lb_reduce<1>(v, parts, counter, r)) return;
+    if (threadIdx.x == 0) out->dg0 = r[0];
+}
+
+// Page-locked host copy of one T (the per-trial record, the coefficients).
+template <typename T>
+struct Pinned {
+    T* p = nullptr;
+    Pinned() { REGOT_CUDA(cudaHostAlloc((void**)&p, sizeof(T), cudaHostAllocDefault)); }
+    ~Pinned() {
+        if (p) cudaFreeHost(p);
+    }
+    Pinned(const Pinned&) = delete;
+    Pinned& operator=(const Pinned&) = delete;
+};
+
+// The host side of the pair ring: Gram matrices of the stored pairs in ring
+// slots (logical order of BFGSMat), s'y of each, theta, and the maps of the
+// device buffers.
+struct LbHost {
+    int ncorr = 0;
+    int ptr = kLbM;  // BFGSMat::reset: m_ptr = m
+    int phys[kLbM];
+    int stage[kLbBufs];
+    double theta = 1.0;
+    double ys[kLbM] = {};
+    double SY[kLbM][kLbM] = {};  // s_i' y_j
+    double YY[kLbM][kLbM] = {};
+    LbHost() {
+        for (int k = 0; k < kLbM; ++k) phys[k] = k;
+        for (int b = 0; b < kLbBufs; ++b) stage[b] = kLbM + b;
+    }
+};
+
+// BFGSMat::add_correction (BFGSMat.h:81-100, as LBFGS.h:160-161 calls it:
+// the pair is stored when s'y > eps y'y) for the pair staged with iterate
+// buffer xb, whose products with the ring and the new gradient are r (the
+// record's prod), then the coefficients of apply_Hv(g, -1)
+// (BFGSMat.h:276-302) by the scalar two-loop recursion: newest to oldest
+// alpha_j = s_j'res / ys_j, res -= alpha_j y_j; res /= theta; oldest to
+// newest beta_j = y_j'res / ys_j, res += (alpha_j - beta_j) s_j, with res
+// kept as coefficients of g and the pairs.
+void lb_host_step(LbHost& H, const double* r, int xb, LbCoef& c) {
     constexpr int M = kLbM;
     double SV[M], YV[M];
     for (int k = 0; k < M; ++k) {
@@ -949,118 +1184,62 @@ __global__ void __launch_bounds__(kLbBlock) k_lb_pair(
     }
     const double ys = r[5 * M + 0], yy = r[5 * M + 1];
     if (ys > DBL_EPSILON * yy) {
-        const int loc = st->ptr % M;
+        const int loc = H.ptr % M;
         for (int k = 0; k < M; ++k) {
             if (k == loc) continue;
-            st->SY[loc][k] = r[5 * k + 0];
-            st->SY[k][loc] = r[5 * k + 1];
-            st->YY[loc][k] = r[5 * k + 2];
-            st->YY[k][loc] = r[5 * k + 2];
+            H.SY[loc][k] = r[5 * k + 0];
+            H.SY[k][loc] = r[5 * k + 1];
+            H.YY[loc][k] = r[5 * k + 2];
+            H.YY[k][loc] = r[5 * k + 2];
         }
-        st->SY[loc][loc] = ys;
-        st->YY[loc][loc] = yy;
-        st->ys[loc] = ys;
-        st->theta = yy / ys;
-        const int old = st->phys[loc];
-        st->phys[loc] = st->phys[M];
-        st->phys[M] = old;
+        H.SY[loc][loc] = ys;
+        H.YY[loc][loc] = yy;
+        H.ys[loc] = ys;
+        H.theta = yy / ys;
+        std::swap(H.phys[loc], H.stage[xb]);
         SV[loc] = r[5 * M + 2];
         YV[loc] = r[5 * M + 3];
-        if (st->ncorr < M) st->ncorr++;
-        st->ptr = loc + 1;
+        if (H.ncorr < M) H.ncorr++;
+        H.ptr = loc + 1;
     }
-    // apply_Hv(g, a = -1, res): res = a g; newest to oldest:
-    // alpha_j = s_j'res / ys_j, res -= alpha_j y_j; res /= theta; oldest to
-    // newest: beta_j = y_j'res / ys_j, res += (alpha_j - beta_j) s_j.
-    // The recursion runs in age order (age 0 = the newest pair) with every
-    // index known at compile time, so alpha and beta stay in registers and
-    // the Gram-matrix reads (shared memory) do not wait on the chain.
-    const double av = -1.0, theta = st->theta;
-    const int ncorr = st->ncorr;
-    const int newest = (st->ptr + M - 1) % M;
-    int slot[M];
-#pragma unroll
-    for (int a = 0; a < M; ++a) slot[a] = (newest + M - a) % M;
-    double alpha[M], beta[M];
-#pragma unroll
-    for (int i = 0; i < M; ++i) {
-        alpha[i] = 0.0;
-        if (i < ncorr) {
-            double sres = av * SV[slot[i]];
-#pragma unroll
-            for (int q = 0; q < i; ++q) sres -= alpha[q] * st->SY[slot[i]][slot[q]];
-            alpha[i] = sres / st->ys[slot[i]];
+    const double av = -1.0, theta = H.theta;
+    const int ncorr = H.ncorr;
+    double alpha[M] = {}, beta[M] = {};
+    int order[M];
+    int j = H.ptr % M;
+    for (int i = 0; i < ncorr; ++i) {
+        j = (j + M - 1) % M;
+        double sres = av * SV[j];
+        for (int q = 0; q < i; ++q) sres -= alpha[order[q]] * H.SY[j][order[q]];
+        alpha[j] = sres / H.ys[j];
+        order[i] = j;
+    }
+    for (int i = 0; i < ncorr; ++i) {
+        // j is the oldest pair here, then moves to newer ones
+        double yres = av * YV[j];
+        for (int q = 0; q < ncorr; ++q) yres -= alpha[order[q]] * H.YY[j][order[q]];
+        yres /= theta;
+        for (int q = 0; q < i; ++q) {
+            const int k = (j + M - 1 - q) % M;  // the pairs already added, newest first
+            yres += (alpha[k] - beta[k]) * H.SY[k][j];
         }
+        beta[j] = yres / H.ys[j];
+        j = (j + 1) % M;
     }
-#pragma unroll
-    for (int i = M - 1; i >= 0; --i) {
-        beta[i] = 0.0;
-        if (i < ncorr) {
-            // pair i, then newer ones; the older ones (q > i) are added
-            double yres = av * YV[slot[i]];
-#pragma unroll
-            for (int q = 0; q < M; ++q)
-                if (q < ncorr) yres -= alpha[q] * st->YY[slot[i]][slot[q]];
-            yres /= theta;
-#pragma unroll
-            for (int q = i + 1; q < M; ++q)
-                if (q < ncorr) yres += (alpha[q] - beta[q]) * st->SY[slot[q]][slot[i]];
-            beta[i] = yres / st->ys[slot[i]];
-        }
-    }
-    st->cv = av / theta;
+    c.cv = av / theta;
     for (int k = 0; k < M; ++k) {
-        st->cy[k] = 0.0;
-        st->cs[k] = 0.0;
+        c.cy[k] = 0.0;
+        c.cs[k] = 0.0;
     }
-#pragma unroll
-    for (int a = 0; a < M; ++a) {
-        if (a < ncorr) {
-            st->cy[slot[a]] = -alpha[a] / theta;
-            st->cs[slot[a]] = alpha[a] - beta[a];
-        }
+    for (int q = 0; q < ncorr; ++q) {
+        const int k = order[q];
+        c.cy[k] = -alpha[k] / theta;
+        c.cs[k] = alpha[k] - beta[k];
     }
-    *gst = s_st;
+    c.ncorr = ncorr;
+    for (int k = 0; k < M; ++k) c.phys[k] = H.phys[k];
+    for (int b = 0; b < kLbBufs; ++b) c.stage[b] = H.stage[b];
 }
-
-// drt = cv g + sum_k cy[k] y_k + cs[k] s_k over the stored pairs, and g'drt.
-// With xt given, also the first trial point xt = xp + step drt.
-__global__ void __launch_bounds__(kLbBlock) k_lb_dir(const double* __restrict__ g,
-                                                     const double* __restrict__ pairs, int N,
-                                                     double* __restrict__ drt, double* parts,
-                                                     LbState* st, LbScal* out,
-                                                     const double* __restrict__ xp, double step,
-                                                     double* __restrict__ xt) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    double v[1] = {0.0};
-    if (t < N) {
-        const double gt = g[t];
-        double d = st->cv * gt;
-        const int ncorr = st->ncorr;
-        for (int k = 0; k < ncorr; ++k) {
-            const int ph = st->phys[k];
-            d += st->cy[k] * pairs[(size_t)(2 * ph + 1) * N + t];
-            d += st->cs[k] * pairs[(size_t)(2 * ph) * N + t];
-        }
-        drt[t] = d;
-        if (xt) xt[t] = xp[t] + step * d;
-        v[0] = gt * d;
-    }
-    __shared__ double r[1];
-    if (!lb_reduce<1>(v, parts, &st->counter, r)) return;
-    if (threadIdx.x == 0) out->dg0 = r[0];
-}
-
-// Page-locked record for the per-trial readback.
-struct PinnedScal {
-    LbScal* p = nullptr;
-    PinnedScal() { REGOT_CUDA(cudaHostAlloc((void**)&p, sizeof(LbScal), cudaHostAllocDefault)); }
-    ~PinnedScal() {
-        if (p) cudaFreeHost(p);
-    }
-    PinnedScal(const PinnedScal&) = delete;
-    PinnedScal& operator=(const PinnedScal&) = delete;
-};
 
 __global__ void k_lb_stamp(unsigned long long* out) {
     unsigned long long t;
@@ -1084,27 +1263,31 @@ void qrot_lbfgs_dual_device(regot_ctx* ctx, regot_dproblem* P, double reg, doubl
     constexpr int M = kLbM;
     const int gN = cdiv(N, kLbBlock);
 
-    DBuf<double> X(3 * (size_t)N, st), G(3 * (size_t)N, st), drt(N, st);
-    DBuf<double> pairs((size_t)(M + 1) * 2 * N, st), parts((size_t)gN * kLbPairSums, st);
-    DBuf<LbState> dstate(1, st);
+    DBuf<double> X(kLbBufs * (size_t)N, st), G(kLbBufs * (size_t)N, st), drt(N, st);
+    // pair buffers: the ring's M plus one staging pair per iterate buffer
+    DBuf<double> pairs((size_t)(M + kLbBufs) * 2 * N, st);
+    DBuf<double> parts((size_t)gN * (4 + kLbPairSums), st);
+    DBuf<unsigned> counter(1, st);
+    DBuf<LbCoef> dcoef(1, st);
     DBuf<LbScal> dscal(1, st);
     DBuf<double> grid(1, st);
     // max |x| of each iterate buffer, written by the merge of the pass at x
     // (the split grid of a line search from x)
-    DBuf<double> xmax(3, st);
+    DBuf<double> xmax(kLbBufs, st);
     DBuf<unsigned long long> mxparts(gN, st);
     pairs.zero();
-    {
-        LbState s0{};
-        s0.ncorr = 0;
-        s0.ptr = M;  // BFGSMat::reset: m_ptr = m
-        for (int k = 0; k <= M; ++k) s0.phys[k] = k;
-        s0.theta = 1.0;
-        s0.cv = -1.0;  // the first direction is -g (LBFGS.h:104)
-        h2d(dstate.get(), &s0, sizeof(s0), st);
-    }
-    PinnedScal pin;
+    counter.zero();
+    LbHost ring;
+    Pinned<LbCoef> pcoef;
+    LbCoef* coef = pcoef.p;
+    std::memset(coef, 0, sizeof(LbCoef));
+    coef->cv = -1.0;  // the first direction is -g (LBFGS.h:104)
+    for (int k = 0; k < M; ++k) coef->phys[k] = ring.phys[k];
+    for (int b = 0; b < kLbBufs; ++b) coef->stage[b] = ring.stage[b];
+    Pinned<LbScal> pin;
     LbScal* hs = pin.p;
+    // the pair products of the last trial written into each iterate buffer
+    double hprod[kLbBufs][kLbPairSums] = {};
     auto xbuf = [&](int i) { return X.get() + (size_t)i * N; };
     auto gbuf = [&](int i) { return G.get() + (size_t)i * N; };
 
@@ -1125,22 +1308,28 @@ void qrot_lbfgs_dual_device(regot_ctx* ctx, regot_dproblem* P, double reg, doubl
 
     // Merge of the last pass at x into grad, plus the record; returns after
     // the record has reached the host.
-    // Merge of the last pass at x into grad and the record, and its copy to
-    // the host (not waited for).
-    auto merge_launch = [&](int op, int nt, const double* x, double* g, double* xm) {
+    // Merge of the last pass at x (buffer xi) into grad (buffer gi) and the
+    // record, and its copy to the host (not waited for). With xpi >= 0 the
+    // trial's correction pair from (xpi, gpi) is staged and its products
+    // enter the record.
+    auto merge_launch = [&](int op, int nt, int xi, int gi, int xpi, int gpi) {
         const int blocks = pass_blocks(op, mixed, n, m);
+        const double* xp = xpi >= 0 ? xbuf(xpi) : xbuf(xi);
+        const double* gp = gpi >= 0 ? gbuf(gpi) : nullptr;
         if (mixed)
             k_lb_merge<float><<<gN, kLbBlock, 0, st>>>(
                 (const float*)ops.buf().rowpart.get(), sh.nslabs,
                 (const float*)ops.buf().colpart.get(), sh.nrb, n, m, ops.buf().totpart.get(),
-                blocks, nt, x, drt.get(), P->a, P->b, reg, g, parts.get(), dstate.get(),
-                dscal.get(), mxparts.get(), xm);
+                blocks, nt, xbuf(xi), drt.get(), P->a, P->b, reg, gbuf(gi), xp, gp, pairs.get(),
+                dcoef.get(), xi, parts.get(), counter.get(), dscal.get(), mxparts.get(),
+                xmax.get() + xi);
         else
             k_lb_merge<double><<<gN, kLbBlock, 0, st>>>(
                 (const double*)ops.buf().rowpart.get(), sh.nslabs,
                 (const double*)ops.buf().colpart.get(), sh.nrb, n, m, ops.buf().totpart.get(),
-                blocks, nt, x, drt.get(), P->a, P->b, reg, g, parts.get(), dstate.get(),
-                dscal.get(), mxparts.get(), xm);
+                blocks, nt, xbuf(xi), drt.get(), P->a, P->b, reg, gbuf(gi), xp, gp, pairs.get(),
+                dcoef.get(), xi, parts.get(), counter.get(), dscal.get(), mxparts.get(),
+                xmax.get() + xi);
         count_launch();
         REGOT_CHECK_LAUNCH();
         d2h(hs, dscal.get(), sizeof(LbScal), st);
@@ -1148,7 +1337,7 @@ void qrot_lbfgs_dual_device(regot_ctx* ctx, regot_dproblem* P, double reg, doubl
     // f and grad at x in buffer xi (the Q_GRAD pass), as
     // Problem::dual_obj_grad: enqueued. Only a mixed pass splits x, on the
     // grid of max |x|.
-    auto eval_launch = [&](int xi, double* g) {
+    auto eval_launch = [&](int xi, int gi) {
         const double* x = xbuf(xi);
         if (mixed) ops.maxabs(x, N, nullptr, 0, grid.get());
         PassParams p = ops.base_params();
@@ -1156,21 +1345,22 @@ void qrot_lbfgs_dual_device(regot_ctx* ctx, regot_dproblem* P, double reg, doubl
         p.cb = x + n;
         p.grid = grid.get();
         ops.pass(OP_Q_GRAD, p);
-        merge_launch(OP_Q_GRAD, 1, x, g, xmax.get() + xi);
+        merge_launch(OP_Q_GRAD, 1, xi, gi, -1, -1);
     };
-    auto eval_at = [&](int xi, double* g) {
-        eval_launch(xi, g);
+    auto eval_at = [&](int xi, int gi) {
+        eval_launch(xi, gi);
         sync(st);
         E.add_passes(1);
         return 0.5 * hs->sq - reg * hs->dab;
     };
-    // Trial at xp + s drt into buffers (xt, gt): the axpy (unless the
-    // direction kernel wrote the point), the trial pass OP_Q_GRADLS (the
-    // gradient at the trial point and the objective change from xp without
-    // cancellation; mixed: from the split of xp and drt, made here when
-    // `split` is set, on the grid of max |xp| from xp's merge) and the
-    // merge; enqueued, not waited for.
-    auto trial_launch = [&](int xpi, int xti, int gti, double s, bool split, bool have_x) {
+    // Trial at xp + s drt into buffers (xt, gt) from the line search's base
+    // (xp, gp): the axpy (unless the direction kernel wrote the point), the
+    // trial pass OP_Q_GRADLS (the gradient at the trial point and the
+    // objective change from xp without cancellation; mixed: from the split
+    // of xp and drt, made here when `split` is set, on the grid of max |xp|
+    // from xp's merge) and the merge; enqueued, not waited for.
+    auto trial_launch = [&](int xpi, int gpi, int xti, int gti, double s, bool split,
+                            bool have_x) {
         if (!have_x) {
             k_lb_axpy<<<gN, kLbBlock, 0, st>>>(xbuf(xpi), drt.get(), s, N, xbuf(xti));
             count_launch();
@@ -1185,12 +1375,13 @@ void qrot_lbfgs_dual_device(regot_ctx* ctx, regot_dproblem* P, double reg, doubl
         p.grid = xmax.get() + xpi;
         if (split) ops.pass(OP_Q_GRADLS, p);
         else ops.pass_presplit(OP_Q_GRADLS, p);
-        merge_launch(OP_Q_GRADLS, 2, xbuf(xti), gbuf(gti), xmax.get() + xti);
+        merge_launch(OP_Q_GRADLS, 2, xti, gti, xpi, gpi);
     };
-    // From the second iteration on, the correction pair, the new direction
-    // and the first trial of the next line search (step 1, base = the
-    // accepted point) are the same kernels every iteration: one CUDA graph
-    // per assignment of the rotating buffers, captured on first use.
+    // From the second iteration on, the copy of the coefficients, the new
+    // direction and the first trial of the next line search (step 1, base =
+    // the accepted point) are the same operations every iteration: one CUDA
+    // graph per assignment of the rotating buffers, captured on first use.
+    // The coefficient copy reads the page-locked block at each replay.
     std::map<int, cudaGraphExec_t> iter_graphs;
     long long iter_graph_kernels = 0;
     struct GraphSet {
@@ -1199,8 +1390,8 @@ void qrot_lbfgs_dual_device(regot_ctx* ctx, regot_dproblem* P, double reg, doubl
             for (auto& kv : g) cudaGraphExecDestroy(kv.second);
         }
     } graph_set{iter_graphs};
-    auto iter_graph = [&](int xi, int gi, int xpi, int gpi) {
-        const int key = ((xi * 3 + gi) * 3 + xpi) * 3 + gpi;
+    auto iter_graph = [&](int xi, int gi) {
+        const int key = xi * kLbBufs + gi;
         auto it = iter_graphs.find(key);
         if (it != iter_graphs.end()) return it->second;
         long long* saved = g_launch_counter;
@@ -1209,13 +1400,13 @@ void qrot_lbfgs_dual_device(regot_ctx* ctx, regot_dproblem* P, double reg, doubl
         cudaGraph_t graph = nullptr;
         REGOT_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         try {
-            k_lb_pair<<<gN, kLbBlock, 0, st>>>(xbuf(xi), xbuf(xpi), gbuf(gi), gbuf(gpi),
-                                               pairs.get(), N, parts.get(), dstate.get());
+            REGOT_CUDA(cudaMemcpyAsync(dcoef.get(), coef, sizeof(LbCoef),
+                                       cudaMemcpyHostToDevice, st));
             k_lb_dir<<<gN, kLbBlock, 0, st>>>(gbuf(gi), pairs.get(), N, drt.get(), parts.get(),
-                                              dstate.get(), dscal.get(), xbuf(xi), 1.0,
-                                              xbuf((xi + 1) % 3));
-            count_launch(2);
-            trial_launch(xi, (xi + 1) % 3, (gi + 1) % 3, 1.0, true, true);
+                                              counter.get(), dcoef.get(), dscal.get(), xbuf(xi),
+                                              1.0, xbuf((xi + 1) % kLbBufs));
+            count_launch();
+            trial_launch(xi, gi, (xi + 1) % kLbBufs, (gi + 1) % kLbBufs, 1.0, true, true);
         } catch (...) {
             cudaGraph_t g = nullptr;
             cudaStreamEndCapture(st, &g);
@@ -1235,7 +1426,7 @@ void qrot_lbfgs_dual_device(regot_ctx* ctx, regot_dproblem* P, double reg, doubl
     };
 
     int ix = 0, ig = 0;
-    double fx = eval_at(ix, gbuf(ig));
+    double fx = eval_at(ix, ig);
     double last_obj = fx;
     double gg = hs->gg, xx = hs->xx;
     int it = 0;
@@ -1263,8 +1454,10 @@ void qrot_lbfgs_dual_device(regot_ctx* ctx, regot_dproblem* P, double reg, doubl
         niter = 1;
     } else {
         // drt = -g (LBFGS.h:104), its g'drt; step = 1 / |drt|
+        h2d(dcoef.get(), coef, sizeof(LbCoef), st);
         k_lb_dir<<<gN, kLbBlock, 0, st>>>(gbuf(ig), pairs.get(), N, drt.get(), parts.get(),
-                                          dstate.get(), dscal.get(), nullptr, 0.0, nullptr);
+                                          counter.get(), dcoef.get(), dscal.get(), nullptr, 0.0,
+                                          nullptr);
         count_launch();
         REGOT_CHECK_LAUNCH();
         double step = 1.0 / gnorm;
@@ -1290,11 +1483,12 @@ void qrot_lbfgs_dual_device(regot_ctx* ctx, regot_dproblem* P, double reg, doubl
                     // the first trial (step 1) ran in the iteration's graph
                     pre_launched = false;
                 } else {
-                    trial_launch(ixp, ixt, igt, s, !split_done, false);
+                    trial_launch(ixp, igp, ixt, igt, s, !split_done, false);
                 }
                 split_done = true;
                 sync(st);
                 E.add_passes(1);
+                std::memcpy(hprod[ixt], hs->prod, sizeof(hprod[ixt]));
                 // The decrease tests use the exact change f(xp + s d) - f(xp)
                 // = s g'd + rem: near the solution the change falls below the
                 // rounding of f itself, where a difference of two evaluated
@@ -1422,9 +1616,11 @@ void qrot_lbfgs_dual_device(regot_ctx* ctx, regot_dproblem* P, double reg, doubl
             iterate(ix, gnorm);
             if (gnorm <= param.epsilon || gnorm <= param.epsilon_rel * std::sqrt(xx)) break;
             if (param.max_iterations != 0 && k >= param.max_iterations) break;
-            // correction pair, next direction and the next line search's
-            // first trial at step 1 (the graph of this buffer assignment)
-            REGOT_CUDA(cudaGraphLaunch(iter_graph(ix, ig, ixp, igp), st));
+            // correction pair and direction coefficients (host), then the
+            // next direction and the next line search's first trial at
+            // step 1 (the graph of this buffer assignment)
+            lb_host_step(ring, hprod[ix], ix, *coef);
+            REGOT_CUDA(cudaGraphLaunch(iter_graph(ix, ig), st));
             count_launch(iter_graph_kernels);
             pre_launched = true;
             dg_known = false;  // read with the first trial's record
@@ -1563,6 +1759,13 @@ public:
         : E_(E), st_(E.stream()), n_(E.n()), m_(E.m()), cg_tol_(cg_tol),
           dvec_(8 * (size_t)std::max(n_, m_), st_), partial_((size_t)kColChunks * m_, st_),
           rhs_d_(n_ + m_, st_) {
+        if (E.mixed()) {
+            const size_t k2 = std::max(n_, m_);
+            f2vec_.alloc(3 * k2, st_);
+            p2_ = f2vec_.get();
+            t2_ = p2_ + k2;
+            x2_ = t2_ + k2;
+        }
         const size_t k = std::max(n_, m_);
         t_d_ = dvec_.get() + k;
         zy_ = t_d_ + k;
@@ -1584,11 +1787,11 @@ public:
         const int gn = cdiv(n, kVT), gm = cdiv(m, kVT);
         h2d(rhs_d_.get(), rhs.data(), N * sizeof(double), st_);
         // v = w / (h1 + mu); zy = z - sigma' v
-        k_div_h1<<<gn, kVT, 0, st_>>>(n, rhs_d_.get(), E_.h1(), mu, t_d_);
+        k_div_h1<<<gn, kVT, 0, st_>>>(n, rhs_d_.get(), E_.h1(), mu, t_d_, t2_);
         count_launch();
-        E_.sigma_cols(t_d_, partial_.get(), nullptr);
+        E_.sigma_cols(t_d_, t2_, partial_.get(), nullptr);
         k_sub_partial<<<gm, kVT, 0, st_>>>(m, rhs_d_.get() + n, partial_.get(), kColChunks, zy_);
-        k_acg_init<<<gm, kVT, 0, st_>>>(m, zy_, cg_tol_, xs_, rs_, ps_, E_.parts(), S);
+        k_acg_init<<<gm, kVT, 0, st_>>>(m, zy_, cg_tol_, xs_, rs_, ps_, E_.parts(), S, x2_, p2_);
         count_launch(2);
         h2d(&S->mu, &mu, sizeof(double), st_);
         if (!exec_) build_graph();
@@ -1605,7 +1808,7 @@ public:
             batch = std::min(batch * 2, 32);
         }
         // r1 = (w - sigma r2) / (h1 + mu)
-        E_.sigma_rows(xs_, mu, false, t_d_, nullptr);
+        E_.sigma_rows(xs_, x2_, mu, false, t_d_, nullptr, nullptr);
         k_backsub<<<gn, kVT, 0, st_>>>(n, rhs_d_.get(), t_d_, E_.h1(), mu, r1_);
         count_launch();
         out.resize(N);
@@ -1627,12 +1830,12 @@ private:
     void step() {
         QState* S = E_.state();
         const int gm = cdiv(m_, kVT);
-        E_.sigma_rows(ps_, 0.0, true, t_d_, &S->cg_done, &S->mu);
-        E_.sigma_cols(t_d_, partial_.get(), &S->cg_done);
+        E_.sigma_rows(ps_, p2_, 0.0, true, t_d_, t2_, &S->cg_done, &S->mu);
+        E_.sigma_cols(t_d_, t2_, partial_.get(), &S->cg_done);
         k_acg_a<<<gm, kVT, 0, st_>>>(m_, partial_.get(), kColChunks, E_.h2(), ps_, ys_,
                                      E_.parts(), S);
-        k_acg_b<<<gm, kVT, 0, st_>>>(m_, ps_, ys_, xs_, rs_, E_.parts(), S);
-        k_acg_c<<<gm, kVT, 0, st_>>>(m_, rs_, ps_, S);
+        k_acg_b<<<gm, kVT, 0, st_>>>(m_, ps_, ys_, xs_, rs_, E_.parts(), S, x2_);
+        k_acg_c<<<gm, kVT, 0, st_>>>(m_, rs_, ps_, S, p2_);
         count_launch(3);
     }
 
@@ -1667,6 +1870,9 @@ private:
     double cg_tol_;
     DBuf<double> dvec_, partial_, rhs_d_;
     double *t_d_, *zy_, *xs_, *rs_, *ps_, *ys_, *r1_;
+    // mixed engine: FP32 (hi, lo) copies of p, sigma p / (h1 + mu) and x
+    DBuf<float2> f2vec_;
+    float2 *p2_ = nullptr, *t2_ = nullptr, *x2_ = nullptr;
 };
 
 }  // namespace
