@@ -733,9 +733,15 @@ __global__ void __launch_bounds__(kThreads, PassCfg<CFG>::kMinBlocks) dense_pass
                                 cacc[0][q] += T * rxv;
                             } else if constexpr (OP == OP_E_LS) {
                                 const TM w = (rdv + cd_at(q)) * inv_reg;
+                                tot[0] += T * expm1_minus_x(steps[0] * w);
+                                // a uniform branch: a one-step pass (the full
+                                // step tried alone) evaluates one series
+                                if (nsteps > 1) {
     #pragma unroll
-                                for (int s2 = 0; s2 < 4; ++s2)
-                                    if (s2 < nsteps) tot[s2] += T * expm1_minus_x(steps[s2] * w);
+                                    for (int s2 = 1; s2 < 4; ++s2)
+                                        if (s2 < nsteps)
+                                            tot[s2] += T * expm1_minus_x(steps[s2] * w);
+                                }
                             } else if constexpr (OP == OP_E_PLAN) {
                                 plan_put<VW>(pv, q, (double)T, p.out, i, m, c0, lane);
                             } else if constexpr (OP == OP_E_GRADLS) {

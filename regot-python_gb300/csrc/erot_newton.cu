@@ -118,33 +118,37 @@ __global__ void k_cg_init(int N, const double* g, double sign, const double* hdi
     }
 }
 
-// y = H p from the HVP pass partials; alpha = r'z / p'y.
+// y = H p from the HVP pass partials; alpha = r'z / p'y. Blocks of (32, 8)
+// threads own 32 entries, rows in the first cdiv(n, 32) blocks and columns
+// after them; the eight threads of an entry merge its partials together
+// (the columns have one partial per row block: 128 at n = 8192, one chain
+// of loads each took most of this kernel's time).
 template <typename Acc>
-__global__ void k_cg_a(const Acc* rp, int nslabs, const Acc* cp, int nrb, int n, int m,
-                       const double* hdiag, const double* p, double reg, double* y, double* parts,
-                       NewtonState* st) {
+__global__ void __launch_bounds__(256) k_cg_a(const Acc* rp, int nslabs, const Acc* cp, int nrb,
+                                              int n, int m, const double* hdiag, const double* p,
+                                              double reg, double* y, double* parts,
+                                              NewtonState* st) {
     if (st->cg_done) return;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gr = (n + 31) / 32;
+    const bool rows = (int)blockIdx.x < gr;
+    const int item = (rows ? (int)blockIdx.x : (int)blockIdx.x - gr) * 32 + (int)threadIdx.x;
+    const double tp = rows ? merge_2d(rp + item, nslabs, (size_t)n, item < n)
+                           : merge_2d(cp + item, nrb, (size_t)m, item < m - 1);
+    if (threadIdx.y != 0) return;  // the rest runs in warp 0 only
     double v[1] = {0.0};
-    if (t < n) {
-        const double tp = merge_strided(rp + t, nslabs, (size_t)n);
-        const double yi = hdiag[t] * p[t] + tp / reg;
-        y[t] = yi;
-        v[0] = p[t] * yi;
-    } else if (t < n + m) {
-        const int j = t - n;
-        double yj = 0.0;
-        if (j < m - 1) {
-            const double tp = merge_strided(cp + j, nrb, (size_t)m);
-            yj = hdiag[t] * p[t] + tp / reg;
-        }
-        y[t] = yj;
-        v[0] = p[t] * yj;
+    const int t = rows ? item : n + item;
+    if (rows ? item < n : item < m) {
+        const double yt = (rows || item < m - 1) ? hdiag[t] * p[t] + tp / reg : 0.0;
+        y[t] = yt;
+        v[0] = p[t] * yt;
     }
     double out[1];
     __threadfence();
-    if (grid_reduce<1>(v, parts, &st->counter, out)) st->alpha = st->rz / out[0];
+    if (warp_grid_reduce<1>(v, parts, &st->counter, out) && threadIdx.x == 0)
+        st->alpha = st->rz / out[0];
 }
+
+int cg_a_grid(int n, int m) { return (n + 31) / 32 + (m + 31) / 32; }
 
 // x += alpha p, r -= alpha y, z = r / diag(H); beta = r'z_new / r'z_old;
 // stop at ||r||^2 < thresh2 or at the iteration limit.
@@ -178,15 +182,21 @@ __global__ void k_cg_b(int N, const double* p, const double* y, const double* hd
 }
 
 // p = z + beta p; refresh the hi/lo bound with |p|.
-__global__ void k_cg_c(int N, const double* z, double* p, NewtonState* st) {
+// p = z + beta p; with rs / cs (mixed), p's FP32 copies in the z entries of
+// the split arrays, which the next HVP pass reads (the duals' hi / lo parts
+// in x and y stay as split once per direction).
+__global__ void k_cg_c(int N, int n, const double* z, double* p, NewtonState* st, float4* rs,
+                       float4* cs) {
     if (st->cg_done) return;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    double pv = 0.0;
     if (t < N) {
-        pv = z[t] + st->beta * p[t];
+        const double pv = z[t] + st->beta * p[t];
         p[t] = pv;
+        if (rs) {
+            if (t < n) rs[t].z = (float)pv;
+            else cs[t - n].z = (float)pv;
+        }
     }
-    block_atomic_max_abs(&st->maxabs, pv);
 }
 
 // g'd and a'd_alpha + b~'d_beta~ for the line search.
@@ -254,7 +264,7 @@ void sinkhorn_newton_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double t
 
     DBuf<double> gamma(N, st), g(N, st), hdiag(N, st), x(N, st), r(N, st), z(N, st), pv(N, st),
         y(N, st), hist(3 * (size_t)hist_cap, st), scratch(8, st), lsout(4, st);
-    DBuf<double> parts(4 * (size_t)cdiv(N, kVecThreads), st);
+    DBuf<double> parts(4 * (size_t)std::max(cdiv(N, kVecThreads), cg_a_grid(n, m)), st);
     DBuf<NewtonState> dst(1, st);
     NewtonState h0{};
     h0.cg_max = cg_max;
@@ -313,21 +323,23 @@ void sinkhorn_newton_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double t
     ph.rx = pv.get();
     ph.cx = pv.get() + n;
     ph.done = &S->cg_done;
+    float4* rs_mut = mixed ? ops.rsplit_mut() : nullptr;
+    float4* cs_mut = mixed ? ops.csplit_mut() : nullptr;
     auto cg_step = [&]() {
-        ops.pass(OP_E_HVP, ph);
+        ops.pass_presplit(OP_E_HVP, ph);
         if (mixed)
-            k_cg_a<float><<<gv, kVecThreads, 0, st>>>(
+            k_cg_a<float><<<cg_a_grid(n, m), dim3(32, 8), 0, st>>>(
                 (const float*)ops.buf().rowpart.get(), sh.nslabs,
                 (const float*)ops.buf().colpart.get(), sh.nrb, n, m, hdiag.get(), pv.get(), reg,
                 y.get(), parts.get(), S);
         else
-            k_cg_a<double><<<gv, kVecThreads, 0, st>>>(
+            k_cg_a<double><<<cg_a_grid(n, m), dim3(32, 8), 0, st>>>(
                 (const double*)ops.buf().rowpart.get(), sh.nslabs,
                 (const double*)ops.buf().colpart.get(), sh.nrb, n, m, hdiag.get(), pv.get(), reg,
                 y.get(), parts.get(), S);
         k_cg_b<<<gv, kVecThreads, 0, st>>>(N, pv.get(), y.get(), hdiag.get(), x.get(), r.get(),
                                              z.get(), parts.get(), S);
-        k_cg_c<<<gv, kVecThreads, 0, st>>>(N, z.get(), pv.get(), S);
+        k_cg_c<<<gv, kVecThreads, 0, st>>>(N, n, z.get(), pv.get(), S, rs_mut, cs_mut);
         count_launch(3);
     };
     cudaGraph_t graph = nullptr;
@@ -373,7 +385,9 @@ void sinkhorn_newton_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double t
         k_cg_init<<<gv, kVecThreads, 0, st>>>(N, g.get(), -1.0, hdiag.get(), cg_tol, x.get(),
                                               r.get(), z.get(), pv.get(), parts.get(), S);
         count_launch();
-        ops.maxabs(gamma.get(), N, pv.get(), N, &S->maxabs);
+        // the split of gamma (and of p = z) for the CG's HVP passes
+        ops.maxabs(gamma.get(), N, nullptr, 0, &S->maxabs);
+        ops.split(ph);
         int batch = 8;
         for (;;) {
             for (int q = 0; q < batch; ++q) REGOT_CUDA(cudaGraphLaunch(exec, st));
@@ -452,7 +466,7 @@ void erot_hess_solve_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, const do
     const PassShape sh = ops.buf().shape;
     DBuf<double> gamma(N, st), g(N, st), hdiag(N, st), x(N, st), r(N, st), z(N, st), pv(N, st),
         y(N, st), rhs(N, st);
-    DBuf<double> parts(4 * (size_t)cdiv(N, kVecThreads), st);
+    DBuf<double> parts(4 * (size_t)std::max(cdiv(N, kVecThreads), cg_a_grid(n, m)), st);
     DBuf<NewtonState> dst(1, st);
     NewtonState h0{};
     h0.cg_max = max_iter > 0 ? max_iter : 2 * (n + m - 1);
@@ -487,30 +501,32 @@ void erot_hess_solve_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, const do
                                           z.get(), pv.get(), parts.get(), S);
     count_launch(2);
     REGOT_CHECK_LAUNCH();
-    ops.maxabs(gamma.get(), N, pv.get(), N, &S->maxabs);
     PassParams ph = pg;
     ph.rx = pv.get();
     ph.cx = pv.get() + n;
     ph.done = &S->cg_done;
+    ops.split(ph);
+    float4* rs_mut = mixed ? ops.rsplit_mut() : nullptr;
+    float4* cs_mut = mixed ? ops.csplit_mut() : nullptr;
     NewtonState hs{};
     for (;;) {
         read_small(ctx, &hs, S, sizeof(hs), st);
         if (hs.cg_done) break;
         for (int q = 0; q < 8; ++q) {  // steps between state reads
-            ops.pass(OP_E_HVP, ph);
+            ops.pass_presplit(OP_E_HVP, ph);
             if (mixed)
-                k_cg_a<float><<<gv, kVecThreads, 0, st>>>(
+                k_cg_a<float><<<cg_a_grid(n, m), dim3(32, 8), 0, st>>>(
                     (const float*)ops.buf().rowpart.get(), sh.nslabs,
                     (const float*)ops.buf().colpart.get(), sh.nrb, n, m, hdiag.get(), pv.get(),
                     reg, y.get(), parts.get(), S);
             else
-                k_cg_a<double><<<gv, kVecThreads, 0, st>>>(
+                k_cg_a<double><<<cg_a_grid(n, m), dim3(32, 8), 0, st>>>(
                     (const double*)ops.buf().rowpart.get(), sh.nslabs,
                     (const double*)ops.buf().colpart.get(), sh.nrb, n, m, hdiag.get(), pv.get(),
                     reg, y.get(), parts.get(), S);
             k_cg_b<<<gv, kVecThreads, 0, st>>>(N, pv.get(), y.get(), hdiag.get(), x.get(), r.get(),
                                                  z.get(), parts.get(), S);
-            k_cg_c<<<gv, kVecThreads, 0, st>>>(N, z.get(), pv.get(), S);
+            k_cg_c<<<gv, kVecThreads, 0, st>>>(N, n, z.get(), pv.get(), S, rs_mut, cs_mut);
             count_launch(3);
         }
     }

@@ -149,6 +149,10 @@ void ErotOps::pass(int op, PassParams p) {
     }
 }
 
+void ErotOps::split(const PassParams& p) {
+    if (mixed_) launch_split(p, rsplit_.get(), csplit_.get(), cdsplit_.get(), st_);
+}
+
 void ErotOps::pass_presplit(int op, PassParams p) {
     if (!p.err) p.err = err_.get();
     if (mixed_) {

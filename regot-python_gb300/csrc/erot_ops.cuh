@@ -56,6 +56,13 @@ public:
     int* err_flag() const { return err_.get(); }
     // Dense pass reusing the FP32 split of the previous pass (mixed mode).
     void pass_presplit(int op, PassParams p);
+    // The FP32 split of p's vectors alone (mixed mode; no-op in FP64), for
+    // passes that follow with pass_presplit.
+    void split(const PassParams& p);
+    // Writable split arrays, for kernels that update one component (the
+    // z = rx / cx entries of a CG vector) between passes.
+    float4* rsplit_mut() { return rsplit_.get(); }
+    float4* csplit_mut() { return csplit_.get(); }
     PassParams base_params() const;
 
     // Maximum of |x| over up to two device vectors, into *out (device).

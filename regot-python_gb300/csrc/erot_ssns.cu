@@ -993,27 +993,57 @@ __device__ __forceinline__ float2 split_df(double v) {
     return make_float2(h, __double2float_rn(v - (double)h));
 }
 
+// The entries of a row are taken four per lane at a time, their loads
+// issued before the products, so that a warp keeps several memory latencies
+// in flight; the products are added in the order of k either way.
 __device__ __forceinline__ double sp_dot(const double* v, const int* c, int cnt,
                                          const double* x) {
     const int lane = threadIdx.x & 31;
     double s = 0.0;
-    for (int k = lane; k < cnt; k += 32) s += v[k] * x[c[k]];
+    int k = lane;
+    for (; k + 96 < cnt; k += 128) {
+        double vv[4];
+        int cc[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            vv[u] = v[k + 32 * u];
+            cc[u] = c[k + 32 * u];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) s += vv[u] * x[cc[u]];
+    }
+    for (; k < cnt; k += 32) s += v[k] * x[c[k]];
     return warp_sum_d(s);
+}
+
+__device__ __forceinline__ void sp_acc(float& s, float& e, float vv, float2 xx) {
+    const float p = vv * xx.x;
+    const float pe = fmaf(vv, xx.x, -p);  // exact: vv xx.x = p + pe
+    float t, te;
+    two_sum_f(s, p, t, te);
+    s = t;
+    e += te + fmaf(vv, xx.y, pe);
 }
 
 __device__ __forceinline__ double sp_dot(const float* v, const int* c, int cnt, const float2* x) {
     const int lane = threadIdx.x & 31;
     float s = 0.f, e = 0.f;
-    for (int k = lane; k < cnt; k += 32) {
-        const float vv = v[k];
-        const float2 xx = x[c[k]];
-        const float p = vv * xx.x;
-        const float pe = fmaf(vv, xx.x, -p);  // exact: vv xx.x = p + pe
-        float t, te;
-        two_sum_f(s, p, t, te);
-        s = t;
-        e += te + fmaf(vv, xx.y, pe);
+    int k = lane;
+    for (; k + 96 < cnt; k += 128) {
+        float vv[4];
+        int cc[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            vv[u] = v[k + 32 * u];
+            cc[u] = c[k + 32 * u];
+        }
+        float2 xx[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) xx[u] = x[cc[u]];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) sp_acc(s, e, vv[u], xx[u]);
     }
+    for (; k < cnt; k += 32) sp_acc(s, e, v[k], x[c[k]]);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         const float so = __shfl_xor_sync(kFull, s, o);
