@@ -626,6 +626,53 @@ __device__ __forceinline__ void r_load(const TM* __restrict__ src, int len, bool
     }
 }
 
+// The next row (column) of a block is fetched while the current one is
+// processed: each thread copies its own vectors of that row into the
+// shared-memory row buffer by cp.async (16 bytes each, the positions it
+// reads back), so no block synchronisation guards the buffer; r_load_next
+// waits for the thread's own copies and moves them into registers, after
+// which the thread may start the following fetch into the same buffer.
+template <typename TM, int VPT>
+__device__ __forceinline__ void r_fetch(const TM* __restrict__ src, int len, TM* sbuf) {
+    constexpr int W = VecOf<TM>::W;
+#pragma unroll
+    for (int c = 0; c < VPT / W; ++c) {
+        const int i0 = W * ((int)threadIdx.x + kRT * c);
+        if (i0 < len)
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                             static_cast<uint32_t>(__cvta_generic_to_shared(sbuf + i0))),
+                         "l"(src + i0)
+                         : "memory");
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+template <typename TM, int VPT>
+__device__ __forceinline__ void r_load_next(const TM* sbuf, int len, TM (&v)[VPT]) {
+    constexpr int W = VecOf<TM>::W;
+    using V = typename VecOf<TM>::V;
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+#pragma unroll
+    for (int c = 0; c < VPT / W; ++c) {
+        const int i0 = W * ((int)threadIdx.x + kRT * c);
+        if (i0 < len) {
+            const V q = *reinterpret_cast<const V*>(sbuf + i0);
+            const TM* e = reinterpret_cast<const TM*>(&q);
+#pragma unroll
+            for (int w = 0; w < W; ++w) v[c * W + w] = (i0 + w < len) ? e[w] : (TM)0;
+        } else {
+#pragma unroll
+            for (int w = 0; w < W; ++w) v[c * W + w] = (TM)0;
+        }
+    }
+}
+
+// Shared bytes of the row buffer of the register kernels.
+template <typename TM, int VPT>
+constexpr size_t r_row_bytes() {
+    return (size_t)kRT * VPT * sizeof(TM);
+}
+
 // Block sum estimate (as block_est_max: TM sums per thread and warp, FP64
 // over warps, with headroom for their rounding) and maximum of the entries
 // v[k] with bit k of `use` set (the others count as 0).
@@ -804,9 +851,14 @@ __global__ void __launch_bounds__(kRT, VPT * sizeof(TM) <= 128 ? 3 : 1) k_col_se
                                                       int n, int m1, double delta, int from_large,
                                                       TM* __restrict__ xout) {
     __shared__ RSmem sh;
+    extern __shared__ __align__(16) unsigned char r_dyn[];
+    TM* sbuf = reinterpret_cast<TM*>(r_dyn);
+    if ((int)blockIdx.x < m1) r_fetch<TM, VPT>(TT + (size_t)blockIdx.x * ldt, n, sbuf);
     for (int j = blockIdx.x; j < m1; j += gridDim.x) {
         TM v[VPT];
-        r_load<TM, VPT>(TT + (size_t)j * ldt, n, true, v);
+        r_load_next<TM, VPT>(sbuf, n, v);
+        if (j + (int)gridDim.x < m1)
+            r_fetch<TM, VPT>(TT + (size_t)(j + gridDim.x) * ldt, n, sbuf);
         double est, mx;
         r_est_max<TM, VPT>(v, ~0ull, sh, est, mx);
         const int k = fix_scale(est);
@@ -828,11 +880,20 @@ __global__ void __launch_bounds__(kRT, VPT * sizeof(TM) <= 64 ? 3 : VPT * sizeof
                                                      int* __restrict__ rcols,
                                                      TM* __restrict__ rvals) {
     __shared__ RSmem sh;
+    extern __shared__ __align__(16) unsigned char r_dyn[];
+    TM* sbuf = reinterpret_cast<TM*>(r_dyn);
     const TM* M = static_cast<const TM*>(a.M);
     const int m1 = a.m1;
+    if (vec && (int)blockIdx.x < a.n) r_fetch<TM, VPT>(M + (size_t)blockIdx.x * a.ldm, m1, sbuf);
     for (int i = blockIdx.x; i < a.n; i += gridDim.x) {
         TM t[VPT];
-        r_load<TM, VPT>(M + (size_t)i * a.ldm, m1, vec != 0, t);
+        if (vec) {
+            r_load_next<TM, VPT>(sbuf, m1, t);
+            if (i + (int)gridDim.x < a.n)
+                r_fetch<TM, VPT>(M + (size_t)(i + gridDim.x) * a.ldm, m1, sbuf);
+        } else {
+            r_load<TM, VPT>(M + (size_t)i * a.ldm, m1, false, t);
+        }
         unsigned long long drop = 0ull;
 #pragma unroll
         for (int k = 0; k < VPT; ++k) {
@@ -880,9 +941,14 @@ __global__ void __launch_bounds__(kRT, VPT * sizeof(TM) <= 128 ? 3 : 1) k_csc_fi
                                                     int* __restrict__ crows,
                                                     TM* __restrict__ cvals) {
     __shared__ RSmem sh;
+    extern __shared__ __align__(16) unsigned char r_dyn[];
+    TM* sbuf = reinterpret_cast<TM*>(r_dyn);
+    if ((int)blockIdx.x < m1) r_fetch<TM, VPT>(TT + (size_t)blockIdx.x * ldt, n, sbuf);
     for (int j = blockIdx.x; j < m1; j += gridDim.x) {
         TM v[VPT];
-        r_load<TM, VPT>(TT + (size_t)j * ldt, n, true, v);
+        r_load_next<TM, VPT>(sbuf, n, v);
+        if (j + (int)gridDim.x < m1)
+            r_fetch<TM, VPT>(TT + (size_t)(j + gridDim.x) * ldt, n, sbuf);
         const TM xj = xcol[j];
         unsigned long long keep = 0ull;
 #pragma unroll
@@ -937,9 +1003,13 @@ void r_dispatch(int vpt, F&& f) {
 // Grid of a register-path kernel: every block resident at once (the blocks
 // loop over rows or columns), at most one block per row or column.
 template <typename Kern>
-int r_grid(Kern kern, int count) {
+int r_grid(Kern kern, int count, size_t smem) {
+    // the row buffer may exceed the default 48 KB of dynamic shared memory
+    // (idempotent; host threads may race here)
+    REGOT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem));
     int occ = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kRT, 0) != cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, kRT, smem) != cudaSuccess ||
         occ < 1)
         occ = 1;
     return std::max(1, std::min(count, device_sm_count() * occ));
@@ -1624,7 +1694,8 @@ public:
         if (rpath()) {
             r_dispatch<TM>(r_vpt<TM>(n_), [&](auto c) {
                 constexpr int V = decltype(c)::value;
-                k_col_select_r<TM, V><<<r_grid(k_col_select_r<TM, V>, m1_), kRT, 0, st_>>>(
+                constexpr size_t sm = r_row_bytes<TM, V>();
+                k_col_select_r<TM, V><<<r_grid(k_col_select_r<TM, V>, m1_, sm), kRT, sm, st_>>>(
                     tt_.get(), ldt_, n_, m1_, delta, from_large, xcol_.get());
             });
         } else {
@@ -1640,7 +1711,8 @@ public:
                                 ? 1 : 0;
             r_dispatch<TM>(r_vpt<TM>(m1_), [&](auto c) {
                 constexpr int V = decltype(c)::value;
-                k_row_stage_r<TM, V><<<r_grid(k_row_stage_r<TM, V>, n_), kRT, 0, st_>>>(
+                constexpr size_t sm = r_row_bytes<TM, V>();
+                k_row_stage_r<TM, V><<<r_grid(k_row_stage_r<TM, V>, n_, sm), kRT, sm, st_>>>(
                     a, m1_, keep_row0, vec, xcol_.get(), delta2, yrow_.get(), rcount_.get(),
                     rcols_.get(), rvals_.get());
             });
@@ -1660,7 +1732,8 @@ public:
         if (rpath()) {
             r_dispatch<TM>(r_vpt<TM>(n_), [&](auto c) {
                 constexpr int V = decltype(c)::value;
-                k_csc_fill_r<TM, V><<<r_grid(k_csc_fill_r<TM, V>, m1_), kRT, 0, st_>>>(
+                constexpr size_t sm = r_row_bytes<TM, V>();
+                k_csc_fill_r<TM, V><<<r_grid(k_csc_fill_r<TM, V>, m1_, sm), kRT, sm, st_>>>(
                     tt_.get(), ldt_, n_, m1_, xcol_.get(), yrow_.get(), n_, ccount_.get(),
                     crows_.get(), cvals_.get());
             });

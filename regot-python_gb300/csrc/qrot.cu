@@ -152,14 +152,18 @@ __global__ void k_rowroot_update(const double* rp, int nslabs, int n, const doub
 // P1 merge: x_i = min(a_i / (rowsum(D)_i / reg), 1)
 template <typename Acc>
 __global__ void k_prim1(const Acc* rp, int nslabs, int n, const double* a, double reg,
-                        double* xr) {
+                        double* xr, float4* rs) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) xr[i] = fmin(a[i] / (merge_strided(rp + i, nslabs, (size_t)n) / reg), 1.0);
+    if (i < n) {
+        const double x = fmin(a[i] / (merge_strided(rp + i, nslabs, (size_t)n) / reg), 1.0);
+        xr[i] = x;
+        if (rs) rs[i].z = (float)x;  // the next passes' row operand, in place
+    }
 }
 // P2 merge: c_j = colsum(D x)/reg; y_j = min(b_j / c_j, 1); f_j = b_j - y_j c_j
 template <typename Acc>
 __global__ void k_prim2(const Acc* cp, int nrb, int m, const double* b, double reg, double* yc,
-                        double* fc, double* parts, QState* st) {
+                        double* fc, double* parts, QState* st, float4* cs) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     double v[1] = {0.0};
     if (j < m) {
@@ -168,6 +172,10 @@ __global__ void k_prim2(const Acc* cp, int nrb, int m, const double* b, double r
         const double f = b[j] - y * c;
         yc[j] = y;
         fc[j] = f;
+        if (cs) {  // the P3 pass's column operands, in place
+            cs[j].z = (float)y;
+            cs[j].w = (float)f;
+        }
         v[0] = f * f;
     }
     double out[1];
@@ -585,37 +593,45 @@ public:
     }
 
     // primal_val (qrot_problem.cpp:10-24)
-    double primal(const double* gamma) {
+    // The three passes share one split of gamma (grid: max |gamma|, from
+    // `grid` when the caller has it); the merge kernels write the next
+    // passes' row and column operands into the split arrays in place.
+    double primal(const double* gamma, const double* grid = nullptr) {
         const PassShape sh = ops_.buf().shape;
         double* xr = vec_.get();
         double* yc = xr + std::max(n_, m_);
         double* fc = yc + std::max(n_, m_);
-        ops_.maxabs(gamma, n_ + m_, nullptr, 0, &state_.get()->maxabs);
+        if (!grid) {
+            ops_.maxabs(gamma, n_ + m_, nullptr, 0, &state_.get()->maxabs);
+            grid = &state_.get()->maxabs;
+        }
         PassParams p = ops_.base_params();
         p.ra = gamma;
         p.cb = gamma + n_;
-        p.grid = &state_.get()->maxabs;
+        p.grid = grid;
         const int gn = cdiv(n_, kVT), gm = cdiv(m_, kVT);
+        float4* rs = mixed_ ? ops_.rsplit_mut() : nullptr;
+        float4* cs = mixed_ ? ops_.csplit_mut() : nullptr;
         ops_.pass(OP_Q_P1, p);
         if (mixed_)
             k_prim1<float><<<gn, kVT, 0, st_>>>((const float*)ops_.buf().rowpart.get(), sh.nslabs,
-                                                 n_, P_->a, reg_, xr);
+                                                 n_, P_->a, reg_, xr, rs);
         else
             k_prim1<double><<<gn, kVT, 0, st_>>>((const double*)ops_.buf().rowpart.get(),
-                                                  sh.nslabs, n_, P_->a, reg_, xr);
+                                                  sh.nslabs, n_, P_->a, reg_, xr, nullptr);
         p.rx = xr;
-        ops_.pass(OP_Q_P2, p);
+        ops_.pass_presplit(OP_Q_P2, p);
         if (mixed_)
             k_prim2<float><<<gm, kVT, 0, st_>>>((const float*)ops_.buf().colpart.get(), sh.nrb,
                                                  m_, P_->b, reg_, yc, fc, parts_.get(),
-                                                 state_.get());
+                                                 state_.get(), cs);
         else
             k_prim2<double><<<gm, kVT, 0, st_>>>((const double*)ops_.buf().colpart.get(), sh.nrb,
                                                   m_, P_->b, reg_, yc, fc, parts_.get(),
-                                                  state_.get());
+                                                  state_.get(), nullptr);
         p.cx = yc;
         p.cx2 = fc;
-        ops_.pass(OP_Q_P3, p);
+        ops_.pass_presplit(OP_Q_P3, p);
         const int blocks = pass_blocks(OP_Q_P3, mixed_, n_, m_);
         k_sum_totals<<<1, 256, 0, st_>>>(ops_.buf().totpart.get(), blocks, scal_.get());
         k_sum_totals<<<1, 256, 0, st_>>>(ops_.buf().totpart.get() + blocks, blocks,
@@ -1433,7 +1449,7 @@ void qrot_lbfgs_dual_device(regot_ctx* ctx, regot_dproblem* P, double reg, doubl
     auto iterate = [&](int xi, double gnorm) {
         stamp();
         double prim = 0.0;
-        if (o.prim_vals) prim = E.primal(xbuf(xi));
+        if (o.prim_vals) prim = E.primal(xbuf(xi), xmax.get() + xi);
         hobj.push_back(last_obj);
         hmar.push_back(gnorm / reg);
         hprim.push_back(prim);
