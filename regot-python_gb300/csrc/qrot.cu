@@ -385,23 +385,26 @@ __global__ void k_acg_init(int m, const double* zy, double tol, double* x, doubl
     }
 }
 
-__global__ void k_acg_a(int m, const double* partial, int chunks, const double* h2,
-                        const double* p, double* y, double* parts, QState* st) {
+// Blocks of (32, 8) threads own 32 columns; the eight threads of a column
+// merge its chunk partials together, then warp 0 carries on.
+__global__ void __launch_bounds__(256) k_acg_a(int m, const double* partial, int chunks,
+                                               const double* h2, const double* p, double* y,
+                                               double* parts, QState* st) {
     if (st->cg_done) return;
     const double mu = st->mu;
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.x * 32 + threadIdx.x;
+    const double u = merge_2d(partial + j, chunks, (size_t)m, j < m);
+    if (threadIdx.y != 0) return;
     double v[1] = {0.0};
     if (j < m) {
-        double u = 0.0;
-#pragma unroll 8
-        for (int c = 0; c < chunks; ++c) u += partial[(size_t)c * m + j];
         const double yj = h2[j] * p[j] + mu * p[j] - u;
         y[j] = yj;
         v[0] = p[j] * yj;
     }
     double out[1];
     __threadfence();
-    if (grid_reduce<1>(v, parts, &st->counter, out)) st->alpha = st->rr / out[0];
+    if (warp_grid_reduce<1>(v, parts, &st->counter, out) && threadIdx.x == 0)
+        st->alpha = st->rr / out[0];
 }
 
 __global__ void k_acg_b(int m, const double* p, const double* y, double* x, double* r,
@@ -1848,8 +1851,8 @@ private:
         const int gm = cdiv(m_, kVT);
         E_.sigma_rows(ps_, p2_, 0.0, true, t_d_, t2_, &S->cg_done, &S->mu);
         E_.sigma_cols(t_d_, t2_, partial_.get(), &S->cg_done);
-        k_acg_a<<<gm, kVT, 0, st_>>>(m_, partial_.get(), kColChunks, E_.h2(), ps_, ys_,
-                                     E_.parts(), S);
+        k_acg_a<<<cdiv(m_, 32), dim3(32, 8), 0, st_>>>(m_, partial_.get(), kColChunks,
+                                                       E_.h2(), ps_, ys_, E_.parts(), S);
         k_acg_b<<<gm, kVT, 0, st_>>>(m_, ps_, ys_, xs_, rs_, E_.parts(), S, x2_);
         k_acg_c<<<gm, kVT, 0, st_>>>(m_, rs_, ps_, S, p2_);
         count_launch(3);
