@@ -419,6 +419,71 @@ __global__ void __launch_bounds__(256) k_tt(DenseArgs a, TM* TT, long long ldt,
     if (tx == 0 && zc) atomicAdd(zeros, (unsigned long long)zc);
 }
 
+// T' for FP32 storage with 16-byte rows (M 16-byte aligned, ldm a multiple
+// of 4): 32 rows x 128 columns per block. Warp w reads rows w, w + 8, ...
+// as float4 per lane (each lane's four columns share their split entries
+// across the rows), the tile is transposed through shared memory (row
+// stride 33: the column-major reads are conflict-free) and written as float4
+// per thread, eight threads per T' row segment.
+__global__ void __launch_bounds__(256) k_tt4(DenseArgs a, float* TT, long long ldt,
+                                             unsigned long long* zeros) {
+    __shared__ float tile[128][33];
+    const float* M = static_cast<const float*>(a.M);
+    const int j0 = blockIdx.x * 128, i0 = blockIdx.y * 32;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int jl = 4 * lane, jg = j0 + jl;
+    unsigned zc = 0;
+    float4 cs4[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e)
+        cs4[e] = jg + e < a.m1 ? a.cs[jg + e] : make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const int il = w + 8 * r, i = i0 + il;
+        float t[4] = {0.f, 0.f, 0.f, 0.f};
+        if (i < a.n) {
+            const float4 rr = a.rs[i];
+            const float* row = M + (size_t)i * a.ldm;
+            float mv[4];
+            if (jg + 3 < a.m1) {
+                const float4 q = __ldg(reinterpret_cast<const float4*>(row + jg));
+                mv[0] = q.x;
+                mv[1] = q.y;
+                mv[2] = q.z;
+                mv[3] = q.w;
+            } else {
+#pragma unroll
+                for (int e = 0; e < 4; ++e) mv[e] = jg + e < a.m1 ? row[jg + e] : 0.f;
+            }
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                if (jg + e < a.m1) {
+                    bool z64;
+                    t[e] = t_mixed(mv[e], rr, cs4[e], a.kexp_f, z64);
+                    zc += z64 ? 1u : 0u;
+                }
+            }
+        }
+#pragma unroll
+        for (int e = 0; e < 4; ++e) tile[jl + e][il] = t[e];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int jr = (int)threadIdx.x / 8 + 32 * q;  // T' row within the tile
+        const int ic = 4 * ((int)threadIdx.x % 8);     // first of its four entries
+        const int j = j0 + jr, i = i0 + ic;
+        if (j < a.m1 && i < a.n) {
+            const float4 v = make_float4(tile[jr][ic], tile[jr][ic + 1], tile[jr][ic + 2],
+                                         tile[jr][ic + 3]);
+            *reinterpret_cast<float4*>(TT + (size_t)j * ldt + i) = v;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) zc += __shfl_xor_sync(kFull, zc, o);
+    if (lane == 0 && zc) atomicAdd(zeros, (unsigned long long)zc);
+}
+
 // Column thresholds x_j (see the file comment).
 template <typename TM>
 __global__ void __launch_bounds__(kSelThreads) k_col_select(const TM* TT, long long ldt, int n,
@@ -1254,24 +1319,39 @@ __global__ void k_schur_rows(Sparse S, const double* p, const double* h, double*
     }
 }
 
-// q_j = (h2_j + shift) p_j - (S' u)_j; alpha = r'z / p'q.
+// q_j = (h2_j + shift) p_j - (S' u)_j and pq_j = p_j q_j. The warps of a
+// block finish their columns independently (no block-wide reduction here:
+// with a warp per column of uneven length, a block barrier kept the early
+// warps waiting); k_schur_alpha adds the pq_j.
 template <typename TM>
 __global__ void k_schur_cols(Sparse S, const double* p, const double* u, const double* h,
-                             double* q, double* parts, SsnState* st) {
+                             double* q, double* pq, SsnState* st) {
     if (st->done) return;
     const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    double v[1] = {0.0};
     if (j < S.m1) {
         const double w = col_dot<TM>(S, j, sp_arg<TM>(u, S.u2));
         if ((threadIdx.x & 31) == 0) {
             const double qj = (h[S.n + j] + st->shift) * p[j] - w;
             q[j] = qj;
-            v[0] = p[j] * qj;
+            pq[j] = p[j] * qj;
         }
     }
-    double out[1];
-    __threadfence();
-    if (grid_reduce<1, true>(v, parts, &st->counter, out)) st->alpha = st->absnew / out[0];
+}
+
+// alpha = r'z / p'q, p'q summed by one block in a fixed order.
+__global__ void __launch_bounds__(1024) k_schur_alpha(int m1, const double* pq, SsnState* st) {
+    if (st->done) return;
+    __shared__ double s_w[32];
+    double s = 0.0;
+    for (int j = threadIdx.x; j < m1; j += 1024) s += pq[j];
+    s = warp_sum_d(s);
+    if ((threadIdx.x & 31) == 0) s_w[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double t = s_w[threadIdx.x];
+        t = warp_sum_d(t);
+        if (threadIdx.x == 0) st->alpha = st->absnew / t;
+    }
 }
 
 // x += alpha p, r -= alpha q, z = r / diag; stop on ||r||^2 < thresh2 or
@@ -1543,6 +1623,7 @@ public:
         z_.alloc(mm, st_);
         p_.alloc(mm, st_);
         q_.alloc(mm, st_);
+        pq_.alloc(mm, st_);
         diag_.alloc(mm, st_);
         parts_.alloc(4 * (size_t)std::max(cdiv(N, kVT), cdiv((long long)std::max(n_, m1_) * 32, 256)),
                      st_);
@@ -1667,13 +1748,12 @@ public:
         if (m1_ <= 0) return 1.0;
         const DenseArgs a = dense_args();
         zeros_.zero();
-        dim3 tgrid(cdiv(m1_, 32), cdiv(n_, 32));
-        k_tt<TM><<<tgrid, dim3(32, 8), 0, st_>>>(a, tt_.get(), ldt_, zeros_.get());
+        transpose(a);
         col_select(delta, density_hint > 0.2 ? 0 : 1);
         row_stage(a, 2.0 * delta, 0);
         csc_fill();
         k_nnz<<<cdiv(n_, kVT), kVT, 0, st_>>>(rcount_.get(), n_, parts_.get(), state_.get());
-        count_launch(2);
+        count_launch();
         REGOT_CHECK_LAUNCH();
         passes_ += 4;
         unsigned long long zc = 0;
@@ -1682,6 +1762,21 @@ public:
         const double nnz = hs.nnz + (double)zc;
         const double dim = (double)(n_ + m_ - 1);
         return (2.0 * nnz + dim) / dim / dim;
+    }
+
+    // T' and the count of FP64 zeros of T.
+    void transpose(const DenseArgs& a) {
+        if constexpr (std::is_same<TM, float>::value) {
+            if (reinterpret_cast<uintptr_t>(P_->M) % 16 == 0 && P_->ldm % 4 == 0) {
+                dim3 grid(cdiv(m1_, 128), cdiv(n_, 32));
+                k_tt4<<<grid, 256, 0, st_>>>(a, tt_.get(), ldt_, zeros_.get());
+                count_launch();
+                return;
+            }
+        }
+        dim3 tgrid(cdiv(m1_, 32), cdiv(n_, 32));
+        k_tt<TM><<<tgrid, dim3(32, 8), 0, st_>>>(a, tt_.get(), ldt_, zeros_.get());
+        count_launch();
     }
 
     // The selection stages of a sparsification: the register path when the
@@ -1886,9 +1981,7 @@ public:
             hist_.alloc(kBins, st_);
         }
         zeros_.zero();
-        dim3 tgrid(cdiv(m1_, 32), cdiv(n_, 32));
-        k_tt<TM><<<tgrid, dim3(32, 8), 0, st_>>>(a, tt_.get(), ldt_, zeros_.get());
-        count_launch();
+        transpose(a);
         const double dd = std::min(std::max(density, 0.0), 1.0);
         const unsigned long long len = (unsigned long long)n_ * (unsigned long long)m1_;
         const unsigned long long k = (unsigned long long)((double)len * dd);
@@ -1989,11 +2082,12 @@ private:
         REGOT_CUDA(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
         k_schur_rows<TM><<<gr, bt, 0, st_>>>(S_, p_.get(), h_.get(), u_.get(), S);
         k_schur_cols<TM><<<gc, bt, 0, st_>>>(S_, p_.get(), u_.get(), h_.get(), q_.get(),
-                                             parts_.get(), S);
+                                             pq_.get(), S);
+        k_schur_alpha<<<1, 1024, 0, st_>>>(m1_, pq_.get(), S);
         k_schur_b<<<gv, kVT, 0, st_>>>(m1_, p_.get(), q_.get(), diag, x, rv_.get(), z_.get(),
                                        parts_.get(), S, S_.x2);
         k_schur_c<<<gv, kVT, 0, st_>>>(m1_, z_.get(), p_.get(), S, S_.p2);
-        count_launch(4);
+        count_launch(5);
         REGOT_CUDA(cudaStreamEndCapture(st_, &graph_));
         g_launch_counter = saved;
         REGOT_CUDA(cudaGraphInstantiate(&exec_, graph_, 0));
@@ -2009,7 +2103,7 @@ private:
     bool jacobi_ = true;
     double cg_tol_ = 1e-10, tol_direct_ = 1e-10;
     int cg_max_ = 0, max_cg_ = 0, max_direct_ = 0;
-    DBuf<double> gamma_, g_, h_, dir_, u_, rv_, z_, p_, q_, diag_, parts_, lsout_;
+    DBuf<double> gamma_, g_, h_, dir_, u_, rv_, z_, p_, q_, pq_, diag_, parts_, lsout_;
     DBuf<double> xt_, tsum_, tmx_;
     DBuf<float2> u2_, d2_, p2_, x2_;  // mixed: FP32 (hi, lo) copies of the CG vectors
     DBuf<float> w32_;

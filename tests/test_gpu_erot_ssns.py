@@ -31,10 +31,13 @@ def _partial_duals(M, a, b, reg, iters):
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("hint", [0.001, 0.5])
-def test_sparsify_pattern(precision, hint):
+@pytest.mark.parametrize("shape", [(300, 257), (304, 260)])
+def test_sparsify_pattern(precision, hint, shape):
     # Same T, same delta: the kept set of the radix-select thresholds equals
-    # the nth_element/sort selection of the reference entry by entry.
-    M, a, b = erot_points(300, 257, seed=5, dtype=np.float64)
+    # the nth_element/sort selection of the reference entry by entry. (With
+    # m a multiple of 4, FP32 rows are 16-byte aligned and T' is formed by
+    # the vectorised transpose.)
+    M, a, b = erot_points(*shape, seed=5, dtype=np.float64)
     Mq = _as_precision(M, precision)
     reg = 0.02
     gamma = _partial_duals(Mq, a, b, reg, 4)
