@@ -478,6 +478,13 @@ __global__ void k_time(unsigned long long t0, unsigned long long* out) {
 }  // namespace
 
 // --------------------------------------------------------------- engine --
+// Scalars of a primal value: the two P3 totals and the merged primal
+// scalars of the state.
+struct PrimRaw {
+    double tot[2];
+    double prim[5];
+};
+
 class QrotEngine {
 public:
     QrotEngine(regot_dproblem* P, double reg, double tau, cudaStream_t st)
@@ -596,10 +603,13 @@ public:
     }
 
     // primal_val (qrot_problem.cpp:10-24)
-    // The three passes share one split of gamma (grid: max |gamma|, from
-    // `grid` when the caller has it); the merge kernels write the next
-    // passes' row and column operands into the split arrays in place.
-    double primal(const double* gamma, const double* grid = nullptr) {
+    // Primal value (primal_val with approx_proj, qrot_problem.cpp): three
+    // passes and their merges, enqueued; the scalars land in *raw when the
+    // stream gets there. The three passes share one split of gamma (grid:
+    // max |gamma|, from `grid` when the caller has it); the merge kernels
+    // write the next passes' row and column operands into the split arrays
+    // in place.
+    void primal_launch(const double* gamma, const double* grid, PrimRaw* raw) {
         const PassShape sh = ops_.buf().shape;
         double* xr = vec_.get();
         double* yc = xr + std::max(n_, m_);
@@ -648,20 +658,28 @@ public:
                                                   state_.get());
         count_launch(5);
         REGOT_CHECK_LAUNCH();
-        double tot[2];
-        QState hs;
-        d2h(tot, scal_.get(), 2 * sizeof(double), st_);
-        d2h(&hs, state_.get(), sizeof(hs), st_);
-        sync(st_);
         passes_ += 3;
-        const double RM = tot[0] / reg_;            // <R, M>, R_ij = P_ij x_i y_j
-        const double RR = tot[1] / (reg_ * reg_);  // ||R||^2
-        const double f2 = hs.prim[0], S = hs.prim[1], eCc = hs.prim[2], xeB = hs.prim[3],
-                     e2 = hs.prim[4];
+        // the scalars the value is formed from, copied to *raw (page-locked:
+        // the copies are asynchronous)
+        d2h(raw->tot, scal_.get(), 2 * sizeof(double), st_);
+        d2h(raw->prim, state_.get()->prim, 5 * sizeof(double), st_);
+    }
+    // The primal value from the scalars of primal_launch (once they landed).
+    double primal_value(const PrimRaw& r) const {
+        const double RM = r.tot[0] / reg_;            // <R, M>, R_ij = P_ij x_i y_j
+        const double RR = r.tot[1] / (reg_ * reg_);  // ||R||^2
+        const double f2 = r.prim[0], S = r.prim[1], eCc = r.prim[2], xeB = r.prim[3],
+                     e2 = r.prim[4];
         // res = R + e f' / S (approx_proj.h:22-24)
         const double val_M = RM + eCc / S;
         const double sqn = RR + 2.0 * xeB / S + e2 * f2 / (S * S);
         return val_M + 0.5 * reg_ * sqn;
+    }
+    double primal(const double* gamma, const double* grid = nullptr) {
+        PrimRaw raw;
+        primal_launch(gamma, grid, &raw);
+        sync(st_);
+        return primal_value(raw);
     }
 
     // beta = optimal_beta(alpha) (qrot_problem.cpp:397-404), into beta (device).
@@ -1449,13 +1467,30 @@ void qrot_lbfgs_dual_device(regot_ctx* ctx, regot_dproblem* P, double reg, doubl
     double last_obj = fx;
     double gg = hs->gg, xx = hs->xx;
     int it = 0;
+    // Primal values (prim_vals) are enqueued with their copy into a
+    // page-locked slot and read after the next synchronisation, which the
+    // line search makes anyway: no synchronisation of their own.
+    struct PrimSlots {
+        PrimRaw s[2];
+    };
+    Pinned<PrimSlots> pslots;
+    int prim_pending = -1;  // history index of the value in flight
+    auto prim_finish = [&]() {
+        if (prim_pending >= 0) {
+            hprim[prim_pending] = E.primal_value(pslots.p->s[prim_pending & 1]);
+            prim_pending = -1;
+        }
+    };
     auto iterate = [&](int xi, double gnorm) {
         stamp();
-        double prim = 0.0;
-        if (o.prim_vals) prim = E.primal(xbuf(xi), xmax.get() + xi);
+        prim_finish();  // the previous iteration's trials synchronised after it
+        if (o.prim_vals) {
+            E.primal_launch(xbuf(xi), xmax.get() + xi, &pslots.p->s[it & 1]);
+            prim_pending = it;
+        }
         hobj.push_back(last_obj);
         hmar.push_back(gnorm / reg);
-        hprim.push_back(prim);
+        hprim.push_back(0.0);
         if (o.verbose >= 1)
             std::printf("iter = %d, objval = %g, ||grad|| = %g\n", it, last_obj, gnorm);
         it++;
@@ -1653,6 +1688,7 @@ void qrot_lbfgs_dual_device(regot_ctx* ctx, regot_dproblem* P, double reg, doubl
     std::vector<unsigned long long> hst(nstamp);
     d2h(hst.data(), stamps.get(), nstamp * sizeof(unsigned long long), st);
     sync(st);
+    prim_finish();
     std::vector<double> htime(hobj.size());
     double cum = 0.0;
     for (size_t q = 0; q < hobj.size(); ++q) {
