@@ -362,6 +362,18 @@ int regot_erot_sparsify_density(regot_ctx* ctx, regot_dproblem* prob, double reg
  * sparsification take the shared-memory path (0: the default choice) and
  * returns the previous setting. No counterpart in the reference. */
 int regot_force_sparsify_path(int shared_memory);
+/* The Schur-complement CG of qrot_assn and qrot_grssn (hess_cg,
+ * src/qrot_cg.cpp:9-50) multiplies by sigma either from the n x m bitmask
+ * of the generalized Jacobian pass or from row and column index lists built
+ * from it, with the whole CG in one thread-block cluster; the lists are
+ * taken when sigma holds at most n m / 64 entries. The cluster exchanges
+ * the CG vectors through distributed shared memory when 8 (n + m) bytes fit
+ * in 200 KB, else through global memory. regot_force_qrot_cg_path forces a
+ * path (1: bitmask, 2: index lists, 3: index lists with the global-memory
+ * exchange, 0: the choice by size) and returns the previous setting. All
+ * give the same directions up to rounding. No counterpart in the
+ * reference. */
+int regot_force_qrot_cg_path(int mode);
 /* QROT Problem::dual_obj_grad (src/qrot_problem.cpp:226-253). */
 int regot_qrot_dual_obj_grad(regot_ctx* ctx, regot_dproblem* prob, double reg,
                              const double* gamma, double* obj, double* grad);

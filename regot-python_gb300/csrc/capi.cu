@@ -830,6 +830,7 @@ extern "C" int regot_force_batch_variant(int variant) { return force_batch_varia
 extern "C" int regot_force_sparsify_path(int shared_memory) {
     return force_sparsify_path(shared_memory);
 }
+extern "C" int regot_force_qrot_cg_path(int mode) { return force_qrot_cg_path(mode); }
 
 extern "C" int regot_batch_variants(regot_ctx* ctx, int* out) {
     return guarded(ctx, [&] {

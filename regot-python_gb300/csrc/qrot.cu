@@ -24,9 +24,12 @@
 //                by sorting.
 // The L-BFGS driver and the ASSN outer loop run on the host in FP64; the
 // ASSN Schur-complement CG (qrot_cg.cpp:9-50: identity preconditioner,
-// relative tolerance 1e-8, at most 2m steps) runs on the device, captured in
-// a CUDA graph.
+// relative tolerance 1e-8, at most 2m steps) runs on the device: with few
+// entries in sigma (the usual case: a couple per row) over row and column
+// index lists in a single thread-block-cluster launch, else over the
+// bitmask in a CUDA graph of its steps.
 #include <algorithm>
+#include <atomic>
 #include <cfloat>
 #include <cmath>
 #include <cstring>
@@ -34,6 +37,7 @@
 #include <vector>
 
 #include "device_util.cuh"
+#include "sm100_util.cuh"
 #include "erot_ops.cuh"
 #include "lbfgs.h"
 #include "solvers.h"
@@ -44,6 +48,12 @@ namespace {
 
 constexpr int kVT = 64;           // vector-kernel block size
 constexpr int kColChunks = 32;    // row chunks of the sigma' y kernel
+
+// Schur CG path: 0 chooses by the number of entries of sigma, 1 always the
+// bitmask products, 2 always the index lists, 3 the index lists with the
+// vectors exchanged through global memory even where shared memory would
+// hold them (force_qrot_cg_path)
+std::atomic<int> g_qrot_cg_path{0};
 
 struct QState {
     unsigned counter;
@@ -471,6 +481,656 @@ __global__ void k_backsub(int n, const double* w, const double* sr2, const doubl
     if (i < n) out[i] = (w[i] - sr2[i]) / (h1[i] + mu);
 }
 
+// ---- compact sigma: row and column index lists built from the bitmask ----
+// At the points ASSN and GRSSN visit, sigma holds a few entries per row
+// (D > 0 on a small fraction of the plan), so the CG products run over
+// index lists instead of testing every bit of the n x m mask at each step.
+// rcnt_i = number of set bits of row i (one warp per row)
+template <int CW, int VW, int LC>
+__global__ void k_cs_row_counts(const uint32_t* bm, int n, int nslabs, int* rcnt) {
+    const int lane = threadIdx.x & 31;
+    const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (i >= n) return;
+    const int W = nslabs * LC;
+    const uint32_t* row = bm + (size_t)i * W;
+    int c = 0;
+    for (int k = lane; k < W; k += 32) c += __popc(row[k]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if (lane == 0) rcnt[i] = c;
+}
+
+// Column j's bit position in the mask (as k_sigma_cols_f reads it).
+template <int CW, int VW>
+__device__ __forceinline__ void bit_of_col(int j, int& sl, int& q, int& L) {
+    sl = j / CW;
+    const int o = j - sl * CW;
+    L = (o % (32 * VW)) / VW;
+    q = (o / (32 * VW)) * VW + (o % VW);
+}
+
+// ccnt[c][j] = set bits of column j among the rows of chunk c
+template <int CW, int VW, int LC>
+__global__ void k_cs_col_counts(const uint32_t* bm, int n, int m, int nslabs, int* ccnt) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = blockIdx.y;
+    if (j >= m) return;
+    int sl, q, L;
+    bit_of_col<CW, VW>(j, sl, q, L);
+    const int rows_per = (n + gridDim.y - 1) / gridDim.y;
+    const int i0 = c * rows_per, i1 = min(n, i0 + rows_per);
+    int cnt = 0;
+    int i = i0;
+    for (; i + 8 <= i1; i += 8) {
+        uint32_t w[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) w[u] = bm[((size_t)(i + u) * nslabs + sl) * LC + q];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) cnt += (w[u] >> L) & 1u;
+    }
+    for (; i < i1; ++i) cnt += (bm[((size_t)i * nslabs + sl) * LC + q] >> L) & 1u;
+    ccnt[(size_t)c * m + j] = cnt;
+}
+
+// Per column: the chunk counts become exclusive offsets within the column,
+// ccol_j = the column's total.
+__global__ void k_cs_col_offsets(int m, int chunks, int* ccnt, int* ccol) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= m) return;
+    int run = 0;
+    for (int c = 0; c < chunks; ++c) {
+        const int v = ccnt[(size_t)c * m + j];
+        ccnt[(size_t)c * m + j] = run;
+        run += v;
+    }
+    ccol[j] = run;
+}
+
+// One block: ptr = exclusive scan of cnt (len + 1 entries, 64-bit running
+// sums; *total = the sum). Entries past 2^31 - 1 are not used: the caller
+// takes the index lists only for totals far below that.
+__device__ void block_excl_scan(const int* cnt, int len, int* ptr, long long* total) {
+    __shared__ long long wsum[32];
+    const int T = blockDim.x, t = threadIdx.x, lane = t & 31, w = t >> 5;
+    const int per = (len + T - 1) / T;
+    const int b = min(len, t * per), e = min(len, b + per);
+    long long s = 0;
+    for (int k = b; k < e; ++k) s += cnt[k];
+    // inclusive scan of the per-thread sums
+    long long inc = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const long long v = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += v;
+    }
+    if (lane == 31) wsum[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        long long v = lane < (T >> 5) ? wsum[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const long long u = __shfl_up_sync(0xffffffffu, v, o);
+            if (lane >= o) v += u;
+        }
+        wsum[lane] = v;
+    }
+    __syncthreads();
+    long long run = inc - s + (w > 0 ? wsum[w - 1] : 0);
+    for (int k = b; k < e; ++k) {
+        ptr[k] = (int)run;
+        run += cnt[k];
+    }
+    if (t == T - 1) {
+        ptr[len] = (int)run;
+        *total = run;
+    }
+    __syncthreads();
+}
+
+__global__ void k_cs_scan(const int* rcnt, int n, int* rowptr, const int* ccol, int m,
+                          int* colptr, long long* nnz) {
+    block_excl_scan(rcnt, n, rowptr, nnz);
+    block_excl_scan(ccol, m, colptr, nnz + 1);
+}
+
+// colidx: the columns of row i's set bits in mask order (one warp per row)
+template <int CW, int VW, int LC>
+__global__ void k_cs_row_fill(const uint32_t* bm, int n, int nslabs, const int* rowptr,
+                              int* colidx) {
+    const int lane = threadIdx.x & 31;
+    const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    if (i >= n) return;
+    const int W = nslabs * LC;
+    const uint32_t* row = bm + (size_t)i * W;
+    int base = rowptr[i];
+    for (int k0 = 0; k0 < W; k0 += 32) {
+        const int k = k0 + lane;
+        uint32_t w = k < W ? row[k] : 0u;
+        const int c = __popc(w);
+        int inc = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, inc, o);
+            if (lane >= o) inc += v;
+        }
+        int pos = base + inc - c;
+        const int sl = k / LC, q = k - (k / LC) * LC;
+        while (w) {
+            const int L = __ffs(w) - 1;
+            w &= w - 1;
+            colidx[pos++] = bit_col<CW, VW, LC>(sl, q, L);
+        }
+        base += __shfl_sync(0xffffffffu, inc, 31);
+    }
+}
+
+// rowidx: the rows of column j's set bits in increasing order; chunk c of
+// the rows starts at colptr_j + ccnt[c][j].
+template <int CW, int VW, int LC>
+__global__ void k_cs_col_fill(const uint32_t* bm, int n, int m, int nslabs, const int* colptr,
+                              const int* ccnt, int* rowidx) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = blockIdx.y;
+    if (j >= m) return;
+    int sl, q, L;
+    bit_of_col<CW, VW>(j, sl, q, L);
+    const int rows_per = (n + gridDim.y - 1) / gridDim.y;
+    const int i0 = c * rows_per, i1 = min(n, i0 + rows_per);
+    int pos = colptr[j] + ccnt[(size_t)c * m + j];
+    int i = i0;
+    for (; i + 8 <= i1; i += 8) {
+        uint32_t w[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) w[u] = bm[((size_t)(i + u) * nslabs + sl) * LC + q];
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+            if ((w[u] >> L) & 1u) rowidx[pos++] = i + u;
+    }
+    for (; i < i1; ++i)
+        if ((bm[((size_t)i * nslabs + sl) * LC + q] >> L) & 1u) rowidx[pos++] = i;
+}
+
+// ---- the whole Schur CG of hess_cg in one thread-block cluster ----
+// The cluster's CTAs split the rows and the columns into contiguous ranges.
+// Phases are separated by the hardware cluster barrier (release / acquire).
+// A dot product is summed per CTA by one warp from the threads' values in
+// shared memory, then over the CTAs from their totals read through
+// distributed shared memory, always in the same order, so every thread of
+// every CTA holds the same bits and takes the same branch. FP64 issues at
+// a small fraction of the FP32 rate on this part, so the kernel keeps its
+// FP64 instructions few: one row and one column per thread at the sizes
+// the list path serves, the reductions on one warp, and 1 / (h1 + mu)
+// formed once per solve.
+constexpr int kCgT = 256;
+
+struct ClusterCgArgs {
+    int n, m, cg_max;
+    double mu, tol;
+    const int *rowptr, *colidx, *colptr, *rowidx;
+    const double *h1, *h2, *w, *z;  // w: the first n entries of the right-hand side, z: the rest
+    double *dinv, *t, *p, *r, *y, *x, *r1;
+    float2 *t2, *p2;                // mixed engine: FP32 (hi, lo) pairs the products read
+    int* it_out;
+};
+
+__device__ __forceinline__ void cluster_barrier() {
+    asm volatile(
+        "barrier.cluster.arrive.release.aligned;\n\t"
+        "barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+__device__ __forceinline__ unsigned cluster_ctarank() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ unsigned cluster_nctarank() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ double ld_dsmem(const double* p, unsigned rank) {
+    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+    unsigned ra;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(ra) : "r"(a), "r"(rank));
+    double v;
+    asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(ra) : "memory");
+    return v;
+}
+// Butterfly sum: each step adds the same two values in both lanes of a
+// pair, so all 32 lanes end with the same bits.
+__device__ __forceinline__ double warp_allsum_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+// Shared memory of one reduction slot. Two slots alternate (p'q, r'r): a
+// CTA may write a slot again only after a cluster barrier that follows
+// every remote read of it.
+struct CgSlot {
+    double cta;    // this CTA's total, read by the others
+    double total;  // the cluster total, for this CTA's threads
+};
+// Sum over the cluster of one value per thread; contains a cluster barrier,
+// which also publishes every global store made before the call.
+__device__ __forceinline__ double cluster_sum(double v, double* vals, CgSlot& slot, unsigned nc) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    vals[threadIdx.x] = v;
+    __syncthreads();
+    if (warp == 0) {
+        double s = 0.0;
+#pragma unroll
+        for (int k = 0; k < kCgT / 32; ++k) s += vals[k * 32 + lane];
+        s = warp_allsum_d(s);
+        if (lane == 0) slot.cta = s;
+    }
+    cluster_barrier();
+    if (warp == 0) {
+        double c = lane < (int)nc ? ld_dsmem(&slot.cta, lane) : 0.0;
+        c = warp_allsum_d(c);
+        if (lane == 0) slot.total = c;
+    }
+    __syncthreads();
+    return slot.total;
+}
+
+// sum_{k in [ptr[i], ptr[i+1])} v[idx[k]]; v written by other CTAs of the
+// cluster, so it is read from L2 (ld.global.cg).
+template <bool MIXED>
+__device__ __forceinline__ double list_sum(const int* ptr, const int* idx, int i, const double* v,
+                                           const float2* v2) {
+    const int b = __ldg(ptr + i), e = __ldg(ptr + i + 1);
+    int k = b;
+    if (MIXED) {
+        float s = 0.f, er = 0.f;
+        for (; k + 4 <= e; k += 4) {
+            float2 u[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) u[q] = __ldcg(v2 + __ldg(idx + k + q));
+#pragma unroll
+            for (int q = 0; q < 4; ++q) cadd(s, er, u[q]);
+        }
+        for (; k < e; ++k) cadd(s, er, __ldcg(v2 + __ldg(idx + k)));
+        return (double)s + (double)er;
+    } else {
+        double acc = 0.0;
+        for (; k + 4 <= e; k += 4) {
+            double u[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) u[q] = __ldcg(v + __ldg(idx + k + q));
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc += u[q];
+        }
+        for (; k < e; ++k) acc += __ldcg(v + __ldg(idx + k));
+        return acc;
+    }
+}
+
+// hess_cg (qrot_cg.cpp:9-50) for Delta = h2 o x + mu x - sigma' ((sigma x) /
+// (h1 + mu)): v = w / (h1 + mu), zy = z - sigma' v, identity-preconditioned
+// CG on zy from 0 to ||r||^2 < tol^2 ||zy||^2 or cg_max steps, then
+// r1 = (w - sigma x) / (h1 + mu). The divisions by h1 + mu are products with
+// its reciprocal (within an ulp of the quotient).
+template <bool MIXED>
+__global__ void __launch_bounds__(kCgT, 1) k_schur_cg_cluster(ClusterCgArgs a) {
+    __shared__ double vals[kCgT];
+    __shared__ CgSlot slot_pq, slot_rr;
+    const unsigned nc = cluster_nctarank(), rk = cluster_ctarank();
+    const int tid = threadIdx.x;
+    const int n = a.n, m = a.m;
+    const double mu = a.mu;
+    const int r0 = (int)((long long)rk * n / nc), r1 = (int)((long long)(rk + 1) * n / nc);
+    const int c0 = (int)((long long)rk * m / nc), c1 = (int)((long long)(rk + 1) * m / nc);
+    // every CTA of the cluster is running before any shared memory is read remotely
+    cluster_barrier();
+    for (int i = r0 + tid; i < r1; i += kCgT) {
+        const double di = 1.0 / (a.h1[i] + mu);
+        a.dinv[i] = di;
+        const double v = a.w[i] * di;
+        if (MIXED) a.t2[i] = split_f2(v);
+        else a.t[i] = v;
+    }
+    cluster_barrier();
+    double part = 0.0;
+    for (int j = c0 + tid; j < c1; j += kCgT) {
+        const double zy = a.z[j] - list_sum<MIXED>(a.colptr, a.rowidx, j, a.t, a.t2);
+        a.x[j] = 0.0;
+        a.r[j] = zy;
+        a.p[j] = zy;
+        if (MIXED) a.p2[j] = split_f2(zy);
+        part += zy * zy;
+    }
+    double rr = cluster_sum(part, vals, slot_rr, nc);
+    const double thresh2 = fmax(a.tol * a.tol * rr, 2.2250738585072014e-308);
+    bool done = rr == 0.0 || rr < thresh2;
+    int it = 0;
+    while (!done) {
+        for (int i = r0 + tid; i < r1; i += kCgT) {
+            const double v = list_sum<MIXED>(a.rowptr, a.colidx, i, a.p, a.p2) * a.dinv[i];
+            if (MIXED) a.t2[i] = split_f2(v);
+            else a.t[i] = v;
+        }
+        cluster_barrier();
+        part = 0.0;
+        for (int j = c0 + tid; j < c1; j += kCgT) {
+            const double u = list_sum<MIXED>(a.colptr, a.rowidx, j, a.t, a.t2);
+            const double pj = a.p[j];
+            const double yj = a.h2[j] * pj + mu * pj - u;
+            a.y[j] = yj;
+            part += pj * yj;
+        }
+        const double alpha = rr / cluster_sum(part, vals, slot_pq, nc);
+        part = 0.0;
+        for (int j = c0 + tid; j < c1; j += kCgT) {
+            a.x[j] += alpha * a.p[j];
+            const double rj = a.r[j] - alpha * a.y[j];
+            a.r[j] = rj;
+            part += rj * rj;
+        }
+        const double rn = cluster_sum(part, vals, slot_rr, nc);
+        ++it;
+        if (rn < thresh2 || it >= a.cg_max || !(rn == rn)) {
+            done = true;
+        } else {
+            const double beta = rn / rr;
+            rr = rn;
+            for (int j = c0 + tid; j < c1; j += kCgT) {
+                const double pj = a.r[j] + beta * a.p[j];
+                a.p[j] = pj;
+                if (MIXED) a.p2[j] = split_f2(pj);
+            }
+            cluster_barrier();
+        }
+    }
+    // r1 = (w - sigma x) / (h1 + mu); the mixed products read x's pairs
+    if (MIXED)
+        for (int j = c0 + tid; j < c1; j += kCgT) a.p2[j] = split_f2(a.x[j]);
+    cluster_barrier();
+    for (int i = r0 + tid; i < r1; i += kCgT)
+        a.r1[i] = (a.w[i] - list_sum<MIXED>(a.rowptr, a.colidx, i, a.x, a.p2)) * a.dinv[i];
+    if (rk == 0 && tid == 0) *a.it_out = it;
+    // no CTA leaves while another may still read its shared memory
+    cluster_barrier();
+}
+
+// ---- the same CG with its vectors exchanged through distributed shared
+// memory ----
+// Every CTA keeps a full copy of the two vectors the sigma products gather
+// from (t = (sigma p) / (h1 + mu) over the rows, p over the columns; FP32
+// (hi, lo) pairs in the mixed engine, FP64 otherwise) in its own shared
+// memory. After forming its slice, a CTA sends the slice to every other
+// CTA with one bulk copy each (cp.async.bulk shared::cta -> shared::cluster)
+// and CTA totals of the dot products go out with st.async; each transfer
+// completes on an mbarrier of the receiving CTA. No step then needs a
+// cluster barrier or a global-memory round trip, and every gather reads
+// local shared memory. One buffer per vector suffices: a CTA can send step
+// k + 1's slice only after every CTA has sent its step-k dot-product
+// totals, that is, after every CTA has finished reading the step-k copy.
+// Waits are bounded (the library's wait limit); a CTA that gives up sets
+// *err and leaves the loop, the others then give up in turn, and all meet
+// at the final cluster barrier.
+constexpr int kDsT = 256;
+constexpr int kDsMaxBytes = 200 * 1024;  // both vectors' copies
+
+struct DsmCgArgs {
+    ClusterCgArgs c;
+    long long polls;
+    int* err;
+};
+
+__device__ __forceinline__ uint32_t mapa_u32(uint32_t addr, uint32_t rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(addr), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ void bulk_s2cluster(uint32_t dst, uint32_t src, uint32_t bytes,
+                                               uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.shared::cta.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+        ::"r"(dst), "r"(src), "r"(bytes), "r"(bar)
+        : "memory");
+}
+__device__ __forceinline__ void st_async_f64(uint32_t dst, double v, uint32_t bar) {
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b64 [%0], %1, [%2];"
+                 ::"r"(dst), "l"(__double_as_longlong(v)), "r"(bar)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_wait_cluster(uint64_t* bar, uint32_t parity, long long polls) {
+    const uint32_t a = sm100::smem_u32(bar);
+    for (long long s = 0; s < polls; ++s) {
+        uint32_t ok;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2, %3;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(ok)
+            : "r"(a), "r"(parity), "r"(100000u)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
+}
+
+// Slice of CTA k (of nc) over len entries: starts at an even index, so that
+// its copy starts on a 16-byte boundary; its copy covers an even number of
+// 8-byte entries (the last slice may carry one unused pad entry).
+struct DsSlices {
+    int per;
+    __device__ DsSlices(int len, unsigned nc) : per(((len + 2 * (int)nc - 1) / (2 * (int)nc)) * 2) {}
+    __device__ int begin(int len, unsigned k) const { return min(len, (int)k * per); }
+    __device__ int end(int len, unsigned k) const { return min(len, (int)k * per + per); }
+    __device__ uint32_t bytes(int len, unsigned k) const {
+        const int c = end(len, k) - begin(len, k);
+        return (uint32_t)(((c + 1) & ~1) * 8);
+    }
+};
+
+// sum_{k in [ptr[i], ptr[i+1])} v[idx[k]] with v in this CTA's shared memory
+template <bool MIXED>
+__device__ __forceinline__ double list_sum_s(const int* ptr, const int* idx, int i,
+                                             const void* vs) {
+    const int b = __ldg(ptr + i), e = __ldg(ptr + i + 1);
+    int k = b;
+    if (MIXED) {
+        const float2* v2 = static_cast<const float2*>(vs);
+        float s = 0.f, er = 0.f;
+        for (; k + 4 <= e; k += 4) {
+            float2 u[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) u[q] = v2[__ldg(idx + k + q)];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) cadd(s, er, u[q]);
+        }
+        for (; k < e; ++k) cadd(s, er, v2[__ldg(idx + k)]);
+        return (double)s + (double)er;
+    } else {
+        const double* v = static_cast<const double*>(vs);
+        double acc = 0.0;
+        for (; k + 4 <= e; k += 4) {
+            double u[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) u[q] = v[__ldg(idx + k + q)];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc += u[q];
+        }
+        for (; k < e; ++k) acc += v[__ldg(idx + k)];
+        return acc;
+    }
+}
+template <bool MIXED>
+__device__ __forceinline__ void put_slot(void* vs, int j, double v) {
+    if (MIXED) static_cast<float2*>(vs)[j] = split_f2(v);
+    else static_cast<double*>(vs)[j] = v;
+}
+
+struct DsShared {
+    double vals[kDsT];
+    double red[2][16];  // CTA totals of p'q and r'r, by sending CTA
+    double bc[2];       // the cluster total and the quotient formed from it
+    uint64_t bar[4];    // arrivals of t, p, the p'q totals, the r'r totals
+    int abort;
+};
+
+template <bool MIXED>
+__global__ void __launch_bounds__(kDsT, 1) k_schur_cg_dsm(DsmCgArgs da) {
+    extern __shared__ __align__(16) unsigned char ds_dyn[];
+    __shared__ DsShared sh;
+    const ClusterCgArgs& a = da.c;
+    const unsigned nc = cluster_nctarank(), rk = cluster_ctarank();
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int n = a.n, m = a.m;
+    const double mu = a.mu;
+    void* Ts = ds_dyn;                                        // (n + 1) & ~1 slots
+    void* Ps = ds_dyn + (size_t)((n + 1) & ~1) * 8;           // (m + 1) & ~1 slots
+    const DsSlices rs(n, nc), cs(m, nc);
+    const int r0 = rs.begin(n, rk), r1 = rs.end(n, rk);
+    const int c0 = cs.begin(m, rk), c1 = cs.end(m, rk);
+    uint32_t t_in = 0, p_in = 0;
+    for (unsigned k = 0; k < nc; ++k)
+        if (k != rk) {
+            t_in += rs.bytes(n, k);
+            p_in += cs.bytes(m, k);
+        }
+    if (tid == 0) {
+        for (int q = 0; q < 4; ++q) sm100::mbar_init(&sh.bar[q], 1);
+        sm100::fence_mbar_init();
+        sh.abort = 0;
+    }
+    uint32_t ph = 0u;  // bit q: the parity barrier q waits for next
+    // barriers initialised and every CTA running before any remote access
+    cluster_barrier();
+
+    // Sends this CTA's slice [b, b + bytes) of vector buffer `vs` to every
+    // other CTA, then waits for theirs (barrier q).
+    auto exchange = [&](void* vs, int b, uint32_t bytes, uint32_t in_bytes, int q) -> bool {
+        sm100::fence_proxy_async_smem();
+        __syncthreads();
+        if (warp == 0) {
+            const uint32_t src = sm100::smem_u32(vs) + (uint32_t)b * 8u;
+            const uint32_t bar = sm100::smem_u32(&sh.bar[q]);
+            if (bytes > 0 && lane < (int)nc && lane != (int)rk)
+                bulk_s2cluster(mapa_u32(src, lane), src, bytes, mapa_u32(bar, lane));
+            if (lane == 0) {
+                sm100::mbar_arrive_expect_tx(&sh.bar[q], in_bytes);
+                if (!mbar_wait_cluster(&sh.bar[q], (ph >> q) & 1u, da.polls)) {
+                    sh.abort = 1;
+                    atomicExch(da.err, 1);
+                }
+            }
+        }
+        __syncthreads();
+        ph ^= 1u << q;
+        return sh.abort == 0;
+    };
+    // Cluster total of one value per thread; bc[1] = num / total (or, with
+    // inv, total / num), formed once.
+    auto all_sum = [&](double v, int slot, double num, bool inv) -> bool {
+        const int q = 2 + slot;
+        sh.vals[tid] = v;
+        __syncthreads();
+        if (warp == 0) {
+            double s = 0.0;
+#pragma unroll
+            for (int k = 0; k < kDsT / 32; ++k) s += sh.vals[k * 32 + lane];
+            s = warp_allsum_d(s);
+            const uint32_t bar = sm100::smem_u32(&sh.bar[q]);
+            if (lane == (int)rk) sh.red[slot][rk] = s;
+            else if (lane < (int)nc)
+                st_async_f64(mapa_u32(sm100::smem_u32(&sh.red[slot][rk]), lane), s,
+                             mapa_u32(bar, lane));
+            if (lane == 0) {
+                sm100::mbar_arrive_expect_tx(&sh.bar[q], (nc - 1) * 8u);
+                if (!mbar_wait_cluster(&sh.bar[q], (ph >> q) & 1u, da.polls)) {
+                    sh.abort = 1;
+                    atomicExch(da.err, 1);
+                }
+            }
+            __syncwarp();
+            double c = lane < (int)nc ? sh.red[slot][lane] : 0.0;
+            c = warp_allsum_d(c);
+            if (lane == 0) {
+                sh.bc[0] = c;
+                sh.bc[1] = inv ? c / num : num / c;
+            }
+        }
+        __syncthreads();
+        ph ^= 1u << q;
+        return sh.abort == 0;
+    };
+
+    bool ok = true;
+    for (int i = r0 + tid; i < r1; i += kDsT) {
+        const double di = 1.0 / (a.h1[i] + mu);
+        a.dinv[i] = di;
+        put_slot<MIXED>(Ts, i, a.w[i] * di);
+    }
+    ok = exchange(Ts, r0, rs.bytes(n, rk), t_in, 0);
+    double part = 0.0;
+    if (ok) {
+        for (int j = c0 + tid; j < c1; j += kDsT) {
+            const double zy = a.z[j] - list_sum_s<MIXED>(a.colptr, a.rowidx, j, Ts);
+            a.x[j] = 0.0;
+            a.r[j] = zy;
+            a.p[j] = zy;
+            put_slot<MIXED>(Ps, j, zy);
+            part += zy * zy;
+        }
+        ok = all_sum(part, 1, 1.0, false);
+    }
+    double rr = sh.bc[0];
+    if (ok) ok = exchange(Ps, c0, cs.bytes(m, rk), p_in, 1);
+    const double thresh2 = fmax(a.tol * a.tol * rr, 2.2250738585072014e-308);
+    bool done = rr == 0.0 || rr < thresh2;
+    int it = 0;
+    while (ok && !done) {
+        for (int i = r0 + tid; i < r1; i += kDsT)
+            put_slot<MIXED>(Ts, i, list_sum_s<MIXED>(a.rowptr, a.colidx, i, Ps) * a.dinv[i]);
+        if (!(ok = exchange(Ts, r0, rs.bytes(n, rk), t_in, 0))) break;
+        part = 0.0;
+        for (int j = c0 + tid; j < c1; j += kDsT) {
+            const double u = list_sum_s<MIXED>(a.colptr, a.rowidx, j, Ts);
+            const double pj = a.p[j];
+            const double yj = a.h2[j] * pj + mu * pj - u;
+            a.y[j] = yj;
+            part += pj * yj;
+        }
+        if (!(ok = all_sum(part, 0, rr, false))) break;
+        const double alpha = sh.bc[1];
+        part = 0.0;
+        for (int j = c0 + tid; j < c1; j += kDsT) {
+            a.x[j] += alpha * a.p[j];
+            const double rj = a.r[j] - alpha * a.y[j];
+            a.r[j] = rj;
+            part += rj * rj;
+        }
+        if (!(ok = all_sum(part, 1, rr, true))) break;
+        const double rn = sh.bc[0];
+        ++it;
+        if (rn < thresh2 || it >= a.cg_max || !(rn == rn)) {
+            done = true;
+        } else {
+            const double beta = sh.bc[1];  // rn / rr
+            rr = rn;
+            for (int j = c0 + tid; j < c1; j += kDsT) {
+                const double pj = a.r[j] + beta * a.p[j];
+                a.p[j] = pj;
+                put_slot<MIXED>(Ps, j, pj);
+            }
+            ok = exchange(Ps, c0, cs.bytes(m, rk), p_in, 1);
+        }
+    }
+    if (ok) {
+        // r1 = (w - sigma x) / (h1 + mu)
+        for (int j = c0 + tid; j < c1; j += kDsT) put_slot<MIXED>(Ps, j, a.x[j]);
+        ok = exchange(Ps, c0, cs.bytes(m, rk), p_in, 1);
+        if (ok)
+            for (int i = r0 + tid; i < r1; i += kDsT)
+                a.r1[i] = (a.w[i] - list_sum_s<MIXED>(a.rowptr, a.colidx, i, Ps)) * a.dinv[i];
+    }
+    if (rk == 0 && tid == 0) *a.it_out = it;
+    // no CTA leaves while another may still write to or read its shared memory
+    cluster_barrier();
+}
+
 __global__ void k_time(unsigned long long t0, unsigned long long* out) {
     *out = globaltimer_ns() - t0;
 }
@@ -775,6 +1435,9 @@ public:
         count_launch();
     }
     bool mixed() const { return mixed_; }
+    // the sigma bitmask of the last eval(..., mask = true) and its slabs per row
+    const uint32_t* bitmask() const { return bm_.get(); }
+    int slabs() { return nslabs(); }
     const double* h1() const { return h_.get(); }
     const double* h2() const { return h_.get() + n_; }
     double* parts() { return parts_.get(); }
@@ -1810,8 +2473,9 @@ namespace {
 // are launched in batches between convergence checks.
 class QrotSchurCG {
 public:
-    QrotSchurCG(QrotEngine& E, double cg_tol)
-        : E_(E), st_(E.stream()), n_(E.n()), m_(E.m()), cg_tol_(cg_tol),
+    // verbose >= 2 prints each solve's CG step count, as hess_cg does
+    QrotSchurCG(QrotEngine& E, double cg_tol, int verbose = 0)
+        : E_(E), st_(E.stream()), n_(E.n()), m_(E.m()), cg_tol_(cg_tol), verbose_(verbose),
           dvec_(8 * (size_t)std::max(n_, m_), st_), partial_((size_t)kColChunks * m_, st_),
           rhs_d_(n_ + m_, st_) {
         if (E.mixed()) {
@@ -1841,6 +2505,7 @@ public:
         const int n = n_, m = m_, N = n + m;
         const int gn = cdiv(n, kVT), gm = cdiv(m, kVT);
         h2d(rhs_d_.get(), rhs.data(), N * sizeof(double), st_);
+        if (solve_compact(mu, out)) return;
         // v = w / (h1 + mu); zy = z - sigma' v
         k_div_h1<<<gn, kVT, 0, st_>>>(n, rhs_d_.get(), E_.h1(), mu, t_d_, t2_);
         count_launch();
@@ -1869,7 +2534,10 @@ public:
         out.resize(N);
         d2h(out.data(), r1_, n * sizeof(double), st_);
         d2h(out.data() + n, xs_, m * sizeof(double), st_);
+        int it = 0;
+        if (verbose_ >= 2) d2h(&it, &S->cg_it, sizeof(int), st_);
         sync(st_);
+        if (verbose_ >= 2) std::printf("[cg] bitmask products, niter = %d\n", it);
     }
 
     ~QrotSchurCG() {
@@ -1877,8 +2545,221 @@ public:
         if (graph_) cudaGraphDestroy(graph_);
     }
 
+    // CG steps of the last compact solve (0 after a bitmask-path solve)
+    int last_compact_steps() const { return last_steps_; }
+
 private:
     static constexpr int kGraphSteps = 8;
+    // sigma is taken as index lists when it holds at most n m / kDenseRatio
+    // entries: the list products then cost less than testing every bit.
+    static constexpr long long kDenseRatio = 64;
+
+    // The compact path: count the set bits of every row and of every
+    // (row chunk, column), scan them into row and column pointers, fill the
+    // index lists, and run the whole CG in one cluster launch. Returns false
+    // (nothing solved) when sigma is too dense for it or no cluster fits.
+    bool solve_compact(double mu, std::vector<double>& out) {
+        last_steps_ = 0;
+        const int mode = g_qrot_cg_path.load(std::memory_order_relaxed);
+        const int C = cluster_ctas(E_.mixed());
+        if (mode == 1 || C == 0) return false;
+        const int n = n_, m = m_;
+        if (!rcnt_.get()) {
+            rcnt_.alloc(n, st_);
+            rowptr_.alloc(n + 1, st_);
+            ccnt_.alloc((size_t)kColChunks * m, st_);
+            ccol_.alloc(m, st_);
+            colptr_.alloc(m + 1, st_);
+            nnz_d_.alloc(2, st_);
+            it_d_.alloc(2, st_);
+            dinv_.alloc(n, st_);
+        }
+        const uint32_t* bm = E_.bitmask();
+        const int ns = E_.slabs();
+        const int warps = 8;
+        const dim3 cgrid(cdiv(m, 128), kColChunks);
+        if (E_.mixed()) {
+            k_cs_row_counts<Geo<float>::CW, Geo<float>::VW, Geo<float>::LC>
+                <<<cdiv(n, warps), warps * 32, 0, st_>>>(bm, n, ns, rcnt_.get());
+            k_cs_col_counts<Geo<float>::CW, Geo<float>::VW, Geo<float>::LC>
+                <<<cgrid, 128, 0, st_>>>(bm, n, m, ns, ccnt_.get());
+        } else {
+            k_cs_row_counts<Geo<double>::CW, Geo<double>::VW, Geo<double>::LC>
+                <<<cdiv(n, warps), warps * 32, 0, st_>>>(bm, n, ns, rcnt_.get());
+            k_cs_col_counts<Geo<double>::CW, Geo<double>::VW, Geo<double>::LC>
+                <<<cgrid, 128, 0, st_>>>(bm, n, m, ns, ccnt_.get());
+        }
+        k_cs_col_offsets<<<cdiv(m, 128), 128, 0, st_>>>(m, kColChunks, ccnt_.get(), ccol_.get());
+        k_cs_scan<<<1, 1024, 0, st_>>>(rcnt_.get(), n, rowptr_.get(), ccol_.get(), m,
+                                       colptr_.get(), nnz_d_.get());
+        count_launch(5);
+        long long nnz[2] = {0, 0};
+        d2h(nnz, nnz_d_.get(), sizeof(nnz), st_);
+        sync(st_);
+        if (nnz[0] != nnz[1])
+            throw Error(REGOT_ERR_NUMERIC, "qrot Schur CG: row and column counts of sigma differ");
+        if (nnz[0] > (long long)INT32_MAX / 2) return false;
+        if (mode == 0 && nnz[0] * kDenseRatio > (long long)n * m) return false;
+        if ((size_t)nnz[0] > idx_cap_) {
+            idx_cap_ = std::max<size_t>((size_t)nnz[0] + nnz[0] / 2, 1024);
+            colidx_.alloc(idx_cap_, st_);
+            rowidx_.alloc(idx_cap_, st_);
+        }
+        if (E_.mixed()) {
+            k_cs_row_fill<Geo<float>::CW, Geo<float>::VW, Geo<float>::LC>
+                <<<cdiv(n, warps), warps * 32, 0, st_>>>(bm, n, ns, rowptr_.get(), colidx_.get());
+            k_cs_col_fill<Geo<float>::CW, Geo<float>::VW, Geo<float>::LC>
+                <<<cgrid, 128, 0, st_>>>(bm, n, m, ns, colptr_.get(), ccnt_.get(), rowidx_.get());
+        } else {
+            k_cs_row_fill<Geo<double>::CW, Geo<double>::VW, Geo<double>::LC>
+                <<<cdiv(n, warps), warps * 32, 0, st_>>>(bm, n, ns, rowptr_.get(), colidx_.get());
+            k_cs_col_fill<Geo<double>::CW, Geo<double>::VW, Geo<double>::LC>
+                <<<cgrid, 128, 0, st_>>>(bm, n, m, ns, colptr_.get(), ccnt_.get(), rowidx_.get());
+        }
+        ClusterCgArgs a;
+        a.n = n;
+        a.m = m;
+        a.cg_max = 2 * m;
+        a.mu = mu;
+        a.tol = cg_tol_;
+        a.rowptr = rowptr_.get();
+        a.colidx = colidx_.get();
+        a.colptr = colptr_.get();
+        a.rowidx = rowidx_.get();
+        a.h1 = E_.h1();
+        a.h2 = E_.h2();
+        a.w = rhs_d_.get();
+        a.z = rhs_d_.get() + n;
+        a.dinv = dinv_.get();
+        a.t = t_d_;
+        a.p = ps_;
+        a.r = rs_;
+        a.y = ys_;
+        a.x = xs_;
+        a.r1 = r1_;
+        a.t2 = t2_;
+        a.p2 = p2_;
+        a.it_out = it_d_.get();
+        // both vectors' copies in every CTA's shared memory when they fit
+        const size_t ds_bytes = (size_t)(((n + 1) & ~1) + ((m + 1) & ~1)) * 8;
+        const int Cd =
+            ds_bytes <= (size_t)kDsMaxBytes && mode != 3 ? dsm_ctas(E_.mixed()) : 0;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(Cd ? Cd : C);
+        cfg.blockDim = dim3(Cd ? kDsT : kCgT);
+        cfg.dynamicSmemBytes = Cd ? ds_bytes : 0;
+        cfg.stream = st_;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = Cd ? Cd : C;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        REGOT_CUDA(cudaMemsetAsync(it_d_.get(), 0, 2 * sizeof(int), st_));
+        if (Cd) {
+            DsmCgArgs da;
+            da.c = a;
+            da.polls = wait_limit();
+            da.err = it_d_.get() + 1;
+            if (E_.mixed())
+                REGOT_CUDA(cudaLaunchKernelEx(&cfg, k_schur_cg_dsm<true>, da));
+            else
+                REGOT_CUDA(cudaLaunchKernelEx(&cfg, k_schur_cg_dsm<false>, da));
+        } else if (E_.mixed()) {
+            REGOT_CUDA(cudaLaunchKernelEx(&cfg, k_schur_cg_cluster<true>, a));
+        } else {
+            REGOT_CUDA(cudaLaunchKernelEx(&cfg, k_schur_cg_cluster<false>, a));
+        }
+        count_launch(3);
+        out.resize(n + m);
+        int it[2] = {0, 0};
+        d2h(out.data(), r1_, n * sizeof(double), st_);
+        d2h(out.data() + n, xs_, m * sizeof(double), st_);
+        d2h(it, it_d_.get(), 2 * sizeof(int), st_);
+        sync(st_);
+        if (it[1])
+            throw Error(REGOT_ERR_TIMEOUT,
+                        "qrot Schur CG: a cluster exchange did not complete within the wait limit");
+        last_steps_ = it[0];
+        if (verbose_ >= 2)
+            std::printf("[cg] index lists (nnz = %lld%s), niter = %d\n", nnz[0],
+                        Cd ? ", shared-memory exchange" : "", it[0]);
+        return true;
+    }
+
+    // CTAs per cluster of the compact CG: 16 where the device takes such a
+    // cluster (a non-portable size), else the largest smaller power of two;
+    // 0 if none fits.
+    static int cluster_ctas(bool mixed) {
+        static const int sizes[2] = {probe_cluster(false), probe_cluster(true)};
+        return sizes[mixed ? 1 : 0];
+    }
+    static int probe_cluster(bool mixed) {
+        auto kern = mixed ? k_schur_cg_cluster<true> : k_schur_cg_cluster<false>;
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+            cudaSuccess) {
+            cudaGetLastError();
+        }
+        for (int c = 16; c >= 1; c >>= 1) {
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(c);
+            cfg.blockDim = dim3(kCgT);
+            cudaLaunchAttribute at[1];
+            at[0].id = cudaLaunchAttributeClusterDimension;
+            at[0].val.clusterDim.x = c;
+            at[0].val.clusterDim.y = 1;
+            at[0].val.clusterDim.z = 1;
+            cfg.attrs = at;
+            cfg.numAttrs = 1;
+            int num = 0;
+            if (cudaOccupancyMaxActiveClusters(&num, kern, &cfg) == cudaSuccess && num > 0)
+                return c;
+            cudaGetLastError();
+        }
+        return 0;
+    }
+
+    // CTAs per cluster of the shared-memory-exchange CG (the largest
+    // dynamic shared memory it may use set once), as cluster_ctas.
+    static int dsm_ctas(bool mixed) {
+        static const int sizes[2] = {probe_dsm(false), probe_dsm(true)};
+        return sizes[mixed ? 1 : 0];
+    }
+    static int probe_dsm(bool mixed) {
+        auto kern = mixed ? k_schur_cg_dsm<true> : k_schur_cg_dsm<false>;
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+                cudaSuccess ||
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 kDsMaxBytes) != cudaSuccess) {
+            cudaGetLastError();
+            return 0;
+        }
+        for (int c = 16; c >= 1; c >>= 1) {
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3(c);
+            cfg.blockDim = dim3(kDsT);
+            cfg.dynamicSmemBytes = kDsMaxBytes;
+            cudaLaunchAttribute at[1];
+            at[0].id = cudaLaunchAttributeClusterDimension;
+            at[0].val.clusterDim.x = c;
+            at[0].val.clusterDim.y = 1;
+            at[0].val.clusterDim.z = 1;
+            cfg.attrs = at;
+            cfg.numAttrs = 1;
+            int num = 0;
+            if (cudaOccupancyMaxActiveClusters(&num, kern, &cfg) == cudaSuccess && num > 0)
+                return c;
+            cudaGetLastError();
+        }
+        return 0;
+    }
+
+    DBuf<int> rcnt_, rowptr_, ccnt_, ccol_, colptr_, colidx_, rowidx_, it_d_;
+    DBuf<long long> nnz_d_;
+    DBuf<double> dinv_;
+    size_t idx_cap_ = 0;
+    int last_steps_ = 0;
 
     // One CG step on Delta = h2 o x + mu x - sigma' ((sigma x) / (h1 + mu)),
     // mu from the state; a no-op once the device flag cg_done is set.
@@ -1923,6 +2804,7 @@ private:
     cudaStream_t st_;
     int n_, m_;
     double cg_tol_;
+    int verbose_;
     DBuf<double> dvec_, partial_, rhs_d_;
     double *t_d_, *zy_, *xs_, *rs_, *ps_, *ys_, *r1_;
     // mixed engine: FP32 (hi, lo) copies of p, sigma p / (h1 + mu) and x
@@ -2069,7 +2951,7 @@ void qrot_assn_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, in
 
     std::vector<double> gamma, g(N), u(N), gu(N), v(N), gv(N), direc(N);
     init_gamma(E, o, gamma);
-    QrotSchurCG cg(E, cg_tol);
+    QrotSchurCG cg(E, cg_tol, o.verbose);
     auto solve = [&](const std::vector<double>& rhs, double mu, std::vector<double>& out) {
         cg.solve(rhs, mu, out);
     };
@@ -2164,7 +3046,7 @@ void qrot_grssn_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, i
     DevClock clock(st);
     std::vector<double> gamma, newgamma(N), g(N), direc(N), rhs(N);
     init_gamma(E, o, gamma);
-    QrotSchurCG cg(E, cg_tol);
+    QrotSchurCG cg(E, cg_tol, o.verbose);
     DBuf<double> xp_d(N, st), d_d(N, st);
     // f, g and the generalized Hessian (sigma bitmask, h1, h2) at gamma
     auto grad_hess = [&]() {
@@ -2669,6 +3551,10 @@ void qrot_pdaam_gpu(regot_ctx* ctx, regot_dproblem* P, double reg, double tol, i
     }
     finish_qrot_with(E, E.gamma(), hobj, hmar, htime, hprim, i, o, res,
                      [&](double* dst) { X.emit(dst); });
+}
+
+int force_qrot_cg_path(int mode) {
+    return g_qrot_cg_path.exchange(mode >= 1 && mode <= 3 ? mode : 0);
 }
 
 }  // namespace regot

@@ -49,6 +49,10 @@ void erot_contract_tc(regot_ctx* ctx, regot_dproblem* P, double reg, const doubl
 // this device so far (-1: none yet) for the classes d <= 4, 8, 16.
 int force_batch_variant(int v);
 int force_sparsify_path(int shared_memory);
+// QROT Schur CG products: 0 chosen by the entries of sigma, 1 the bitmask,
+// 2 the index lists, 3 the index lists with the vectors exchanged through
+// global memory; returns the previous setting (qrot.cu)
+int force_qrot_cg_path(int mode);
 std::vector<int> batch_variants();
 // Batched BCD over point-cloud problems (erot_batch.cu).
 // cost, grad_x, grad_y (host, optional): each problem's regularised OT cost

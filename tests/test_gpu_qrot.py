@@ -70,9 +70,10 @@ def test_qrot_lbfgs_dual(precision):
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_qrot_assn(precision):
+def test_qrot_assn(precision, qrot_cg_path):
     # ASSN converges slowly on this problem; its first iterations follow the
-    # oracle (same Newton / projection / gradient decisions).
+    # oracle (same Newton / projection / gradient decisions), with the CG
+    # products on the bitmask and on the index lists.
     M, a, b = _small()
     Mq = _as_precision(M, precision)
     reg = 0.1
@@ -83,6 +84,58 @@ def test_qrot_assn(precision):
     rt = 1e-5 if precision == "fp64" else 1e-2
     np.testing.assert_allclose(r.mar_errs[:k], o.mar_errs[:k], rtol=rt, atol=1e-12)
     np.testing.assert_allclose(r.prim_vals[:k], o.prim_vals[:k], rtol=rt)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_qrot_assn_dense_sigma(precision, qrot_cg_path):
+    # reg = 100 with uniform weights: D > 0 on about a fifth of the plan, far
+    # above the size-based choice's limit for the index lists; both paths
+    # still follow the oracle to convergence.
+    M, _, _ = _small(seed=4)
+    n, m = M.shape
+    a = np.full(n, 1.0 / n)
+    b = np.full(m, 1.0 / m)
+    Mq = _as_precision(M, precision)
+    reg = 100.0
+    # FP32 M: ||g|| has a floor near 1e-6 here
+    tol = 1e-12 if precision == "fp64" else 1e-5
+    r = regot.qrot_assn(M, a, b, reg, tol=tol, max_iter=8, precision=precision)
+    o = O.qrot_assn(Mq, a, b, reg, tol=tol, max_iter=8)
+    gam = o.dual
+    D = gam[:n, None] + gam[None, n:] - Mq
+    assert (D > 0).mean() > 0.15
+    assert abs(r.niter - o.niter) <= (0 if precision == "fp64" else 1)
+    rt = 1e-6 if precision == "fp64" else 1e-3
+    k = min(sum(1 for v in o.mar_errs if v > (1e-9 if precision == "fp64" else 1e-6)),
+            len(r.mar_errs))
+    np.testing.assert_allclose(r.mar_errs[:k], o.mar_errs[:k], rtol=rt, atol=1e-12)
+    np.testing.assert_allclose(r.obj_vals[:k], o.obj_vals[:k], rtol=rt * 1e-2, atol=1e-12)
+    np.testing.assert_allclose(r.dual, o.dual, rtol=0, atol=1e-8 if precision == "fp64" else 1e-5)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_qrot_assn_cg_paths_agree(precision):
+    # A larger problem on which the size-based choice takes the index lists:
+    # the two CG paths give the same iterates up to the CG tolerance.
+    from regot import _lib
+
+    lib = _lib.load()
+    M, a, b = qrot_points(700, 520, seed=6, dtype=np.float64)
+    reg = 0.05
+    runs = {}
+    for mode in (1, 2, 3, 0):
+        old = lib.regot_force_qrot_cg_path(mode)
+        try:
+            runs[mode] = regot.qrot_assn(M, a, b, reg, tol=1e-10, max_iter=12,
+                                         precision=precision, plan=False)
+        finally:
+            lib.regot_force_qrot_cg_path(old)
+    rt = 1e-6 if precision == "fp64" else 1e-4
+    for mode in (2, 3, 0):
+        assert runs[mode].niter == runs[1].niter
+        np.testing.assert_allclose(runs[mode].mar_errs, runs[1].mar_errs, rtol=rt, atol=1e-12)
+        np.testing.assert_allclose(runs[mode].obj_vals, runs[1].obj_vals, rtol=1e-9, atol=1e-12)
+    np.testing.assert_array_equal(runs[0].mar_errs, runs[2].mar_errs)
 
 
 def test_qrot_readme_history():

@@ -20,7 +20,7 @@ CASES = {
 
 
 @pytest.mark.parametrize("case", list(CASES))
-def test_qrot_grssn_fp64_matches_oracle(case):
+def test_qrot_grssn_fp64_matches_oracle(case, qrot_cg_path):
     make, reg = CASES[case]
     M, a, b = make()
     iters = 8
@@ -33,7 +33,7 @@ def test_qrot_grssn_fp64_matches_oracle(case):
     np.testing.assert_allclose(r.dual, o.dual, rtol=0, atol=1e-6)
 
 
-def test_qrot_grssn_converges_with_the_oracle():
+def test_qrot_grssn_converges_with_the_oracle(qrot_cg_path):
     M, a, b = qrot_points(60, 45, seed=3, dtype=np.float64)
     reg = 0.1
     r = regot.qrot_grssn(M, a, b, reg, tol=1e-8, max_iter=500, precision="fp64")
@@ -45,7 +45,7 @@ def test_qrot_grssn_converges_with_the_oracle():
     np.testing.assert_allclose(r.plan, o.plan, rtol=0, atol=1e-5 * o.plan.max())
 
 
-def test_qrot_grssn_mixed_converges():
+def test_qrot_grssn_mixed_converges(qrot_cg_path):
     M, a, b = qrot_points(60, 45, seed=3, dtype=np.float64)
     Mq = M.astype(np.float32).astype(np.float64)
     reg = 0.1
