@@ -102,6 +102,12 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity
 // 1/k! as constants (no divisions), FP32 up to x^9 (truncation below 2e-9
 // relative), FP64 up to x^17 (below 1e-20); expm1(x) - x beyond, where no
 // cancellation occurs.
+// Root passes' FP32 filter: the bound on |d - (y - c)| (d its FP32 value)
+// relative to the magnitudes involved, and an absolute floor below FP32's
+// normal range.
+constexpr float kRootSlack = 4.76837158203125e-07f;  // 2^-21
+constexpr float kRootFloor = 1e-37f;
+
 template <typename T>
 __device__ __forceinline__ T expm1_minus_x(T x);
 template <>
@@ -473,7 +479,10 @@ __global__ void __launch_bounds__(kThreads, PassCfg<CFG>::kMinBlocks) dense_pass
         // the shared-memory banks (HVP 0.64 -> 0.26 of peak).
         TM ch[LC], clk[LC], cxv[op_uses_cx(OP) ? LC : 1], cx2v[op_uses_cx2(OP) ? LC : 1],
             cdv[op_uses_cd(OP) ? LC : 1];
-        double cbd[ROOT ? LC : 1];
+        // root passes: the column values in FP64 (FP64 M), or rounded to FP32
+        // for the mixed engine's filter (its exact test reloads them)
+        double cbd[(ROOT && !MIXED) ? LC : 1];
+        float cbf[(ROOT && MIXED) ? LC : 1];
         bool cvalid[LC];
 #pragma unroll
         for (int q = 0; q < LC; ++q) {
@@ -482,7 +491,8 @@ __global__ void __launch_bounds__(kThreads, PassCfg<CFG>::kMinBlocks) dense_pass
             const bool ok = j < m;
             cvalid[q] = ok;
             if constexpr (ROOT) {
-                cbd[q] = ok ? p.cb[j] : -INFINITY;
+                if constexpr (MIXED) cbf[q] = ok ? __double2float_rn(p.cb[j]) : -INFINITY;
+                else cbd[q] = ok ? p.cb[j] : -INFINITY;
                 ch[q] = 0;
                 clk[q] = 0;
             } else if constexpr (MIXED) {
@@ -589,6 +599,9 @@ __global__ void __launch_bounds__(kThreads, PassCfg<CFG>::kMinBlocks) dense_pass
                 (void)rxv;
                 (void)rdv;
                 (void)rad;
+                // root passes, mixed engine: the row value in FP32 for the filter
+                const float radf = (ROOT && MIXED) ? __double2float_rn(rad) : 0.f;
+                (void)radf;
                 const VT(&mv)[NV] = mvp[r2];
                     Acc racc[NRa];
     #pragma unroll
@@ -700,16 +713,55 @@ __global__ void __launch_bounds__(kThreads, PassCfg<CFG>::kMinBlocks) dense_pass
                             else a = rh - mval;
                             if (cvalid[q]) cacc[0][q] = fmax(cacc[0][q], (Acc)a);
                         } else if constexpr (COLROOT) {
-                            const double y = (double)mval - rad;
-                            if (cvalid[q] && y < cbd[q]) {
-                                cacc[0][q] += 1.0;
-                                cacc[1][q] += y;
+                            if constexpr (MIXED) {
+                                // y = M - ra_i is below cb_j on a few entries per
+                                // column: an FP32 test rules out the rest, and only
+                                // entries within its error bound (2^-21 of the
+                                // magnitudes, about 8x the worst rounding) take the
+                                // exact FP64 test, so the active set and the sums
+                                // are those of the FP64 test on every entry
+                                const float yf = mval - radf;
+                                const float d = yf - cbf[q];
+                                const float bnd = fmaf(kRootSlack,
+                                                       fabsf(yf) + (fabsf(radf) + fabsf(cbf[q])),
+                                                       kRootFloor);
+                                if (cvalid[q] && !(d > bnd)) {
+                                    const int j = c0 + ((q / VW) * 32 + lane) * VW + (q % VW);
+                                    const double y = (double)mval - rad;
+                                    if (y < p.cb[j]) {
+                                        cacc[0][q] += 1.0;
+                                        cacc[1][q] += y;
+                                    }
+                                }
+                            } else {
+                                const double y = (double)mval - rad;
+                                if (cvalid[q] && y < cbd[q]) {
+                                    cacc[0][q] += 1.0;
+                                    cacc[1][q] += y;
+                                }
                             }
                         } else if constexpr (ROWROOT) {
-                            const double y = (double)mval - cbd[q];
-                            if (cvalid[q] && y < rad) {
-                                racc[0] += 1.0;
-                                racc[1] += y;
+                            if constexpr (MIXED) {
+                                // the same filter for y = M - cb_j below ra_i
+                                const float yf = mval - cbf[q];
+                                const float d = yf - radf;
+                                const float bnd = fmaf(kRootSlack,
+                                                       fabsf(yf) + (fabsf(radf) + fabsf(cbf[q])),
+                                                       kRootFloor);
+                                if (cvalid[q] && !(d > bnd)) {
+                                    const int j = c0 + ((q / VW) * 32 + lane) * VW + (q % VW);
+                                    const double y = (double)mval - p.cb[j];
+                                    if (y < rad) {
+                                        racc[0] += 1.0;
+                                        racc[1] += y;
+                                    }
+                                }
+                            } else {
+                                const double y = (double)mval - cbd[q];
+                                if (cvalid[q] && y < rad) {
+                                    racc[0] += 1.0;
+                                    racc[1] += y;
+                                }
                             }
                         } else if constexpr (EROT) {
                             // T = 2^((ra_i + cb_j - M_ij) log2(e) / reg): exact hi sum,

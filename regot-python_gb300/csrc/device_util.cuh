@@ -106,6 +106,66 @@ __device__ __forceinline__ void two_sum_f(float a, float b, float& s, float& e) 
     e = (a - (s - z)) + (b - z);
 }
 
+// ---- double-word FP32 arithmetic: a value is the unevaluated sum hi + lo
+// of two floats (|lo| <= ulp(hi) / 2), about 48 significant bits. Used where
+// FP64's issue rate and latency on this part would bound a kernel. The
+// algorithms are the published ones: Knuth's TwoSum, Dekker's Fast2Sum, the
+// FMA-based TwoProd, and AccurateDWPlusDW, DWTimesDW and DWDivDW of Joldes,
+// Muller and Popescu, "Tight and rigorous error bounds for basic building
+// blocks of double-word arithmetic" (ACM TOMS 44, 2017). Products that must
+// round on their own are written with __fmul_rn so that they are not
+// contracted into a neighbouring addition. dw_add(x, y) and dw_add(y, x)
+// give the same bits (TwoSum's error term is exact in either order), so a
+// butterfly of dw_add leaves every lane with the same result. ----
+__device__ __forceinline__ float2 fast_two_sum_f(float a, float b) {  // |a| >= |b| or a == 0
+    const float s = a + b;
+    return make_float2(s, b - (s - a));
+}
+__device__ __forceinline__ float2 dw_from(double v) {
+    const float h = __double2float_rn(v);
+    return make_float2(h, __double2float_rn(v - (double)h));
+}
+__device__ __forceinline__ double dw_to(float2 v) { return (double)v.x + (double)v.y; }
+__device__ __forceinline__ float2 dw_add(float2 x, float2 y) {
+    float sh, sl, th, tl;
+    two_sum_f(x.x, y.x, sh, sl);
+    two_sum_f(x.y, y.y, th, tl);
+    const float2 v = fast_two_sum_f(sh, sl + th);
+    return fast_two_sum_f(v.x, tl + v.y);
+}
+__device__ __forceinline__ float2 dw_neg(float2 x) { return make_float2(-x.x, -x.y); }
+__device__ __forceinline__ float2 dw_sub(float2 x, float2 y) { return dw_add(x, dw_neg(y)); }
+__device__ __forceinline__ float2 dw_mul(float2 x, float2 y) {
+    const float ch = __fmul_rn(x.x, y.x);
+    const float cl1 = fmaf(x.x, y.x, -ch);
+    const float tl1 = fmaf(x.x, y.y, __fmul_rn(x.y, y.y));
+    const float cl2 = fmaf(x.y, y.x, tl1);
+    return fast_two_sum_f(ch, cl1 + cl2);
+}
+__device__ __forceinline__ float2 dw_mul_f(float2 x, float y) {
+    const float ch = __fmul_rn(x.x, y);
+    const float cl1 = fmaf(x.x, y, -ch);
+    return fast_two_sum_f(ch, fmaf(x.y, y, cl1));
+}
+__device__ __forceinline__ float2 dw_div(float2 x, float2 y) {
+    const float th = x.x / y.x;
+    const float2 r = dw_mul_f(y, th);
+    float ph, sl;
+    two_sum_f(x.x, -r.x, ph, sl);
+    const float d = sl + (x.y - r.y);
+    return fast_two_sum_f(th, (ph + d) / y.x);
+}
+// x < y for normalised double-word values
+__device__ __forceinline__ bool dw_lt(float2 x, float2 y) {
+    return x.x < y.x || (x.x == y.x && x.y < y.y);
+}
+// compensated sum (s, e) of a TwoSum accumulation, as a double-word value
+__device__ __forceinline__ float2 dw_norm(float s, float e) {
+    float h, l;
+    two_sum_f(s, e, h, l);
+    return make_float2(h, l);
+}
+
 // FP32 partials: compensated FP32 sums (TwoSum, two independent
 // accumulators with their rounding errors beside them), converted to FP64
 // once. FP64 arithmetic issues at a small fraction of the FP32 rate on this

@@ -34,6 +34,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <tuple>
 #include <vector>
 
 #include "device_util.cuh"
@@ -73,33 +74,55 @@ struct QState {
     double prim[6];  // primal-value scalars
     double maxabs;
     double mu;       // shift of the Schur CG (read by its captured steps)
+    int root_rounds; // Newton rounds of the last optimal_alpha / optimal_beta
+    int root_unconverged;
 };
 
 // ---- gradient / objective merge ----
+// Blocks of (32, 8) threads: the first cdiv(n, 32) blocks own 32 rows each,
+// the rest 32 columns each; the eight threads of a row or column merge its
+// partials together (merge_2d), then warp 0 carries on.
 template <typename Acc>
-__global__ void k_q_grad(const Acc* rp, int nslabs, const Acc* cp, int nrb, int n, int m,
-                         int with_counts, const double* gamma, const double* a, const double* b,
-                         double reg, double* grad, double* h1, double* h2, double* parts,
-                         QState* st) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void __launch_bounds__(256) k_q_grad(const Acc* rp, int nslabs, const Acc* cp, int nrb,
+                                               int n, int m, int with_counts,
+                                               const double* gamma, const double* a,
+                                               const double* b, double reg, double* grad,
+                                               double* h1, double* h2, double* parts,
+                                               QState* st) {
+    const int nbr = (n + 31) / 32;
+    const bool rows = (int)blockIdx.x < nbr;
+    const int t = (rows ? (int)blockIdx.x : (int)blockIdx.x - nbr) * 32 + threadIdx.x;
+    const bool valid = rows ? t < n : t < m;
+    double sum, cnt = 0.0;
+    if (rows) {
+        sum = merge_2d(rp + t, nslabs, (size_t)n, valid);
+        if (with_counts) {
+            __syncthreads();
+            cnt = merge_2d(rp + (size_t)nslabs * n + t, nslabs, (size_t)n, valid);
+        }
+    } else {
+        sum = merge_2d(cp + t, nrb, (size_t)m, valid);
+        if (with_counts) {
+            __syncthreads();
+            cnt = merge_2d(cp + (size_t)nrb * m + t, nrb, (size_t)m, valid);
+        }
+    }
+    if (threadIdx.y != 0) return;
     double v[3] = {0.0, 0.0, 0.0};
-    if (t < n) {
-        const double rs = merge_strided(rp + t, nslabs, (size_t)n);
-        grad[t] = rs - reg * a[t];
-        if (with_counts) h1[t] = merge_strided(rp + (size_t)nslabs * n + t, nslabs, (size_t)n);
+    if (valid && rows) {
+        grad[t] = sum - reg * a[t];
+        if (with_counts) h1[t] = cnt;
         v[0] = gamma[t] * a[t];
         v[1] = gamma[t];
-    } else if (t < n + m) {
-        const int j = t - n;
-        const double cs = merge_strided(cp + j, nrb, (size_t)m);
-        grad[t] = cs - reg * b[j];
-        if (with_counts) h2[j] = merge_strided(cp + (size_t)nrb * m + j, nrb, (size_t)m);
-        v[0] = gamma[t] * b[j];
-        v[2] = gamma[t];
+    } else if (valid) {
+        grad[n + t] = sum - reg * b[t];
+        if (with_counts) h2[t] = cnt;
+        v[0] = gamma[n + t] * b[t];
+        v[2] = gamma[n + t];
     }
     double out[3];
     __threadfence();
-    if (grid_reduce<3>(v, parts, &st->counter, out)) {
+    if (warp_grid_reduce<3>(v, parts, &st->counter, out) && threadIdx.x == 0) {
         st->dot_ab = out[0];
         st->sum_a = out[1];
         st->sum_b = out[2];
@@ -130,12 +153,18 @@ __global__ void k_root_init(int m, double* x, double* prev_cnt) {
     }
 }
 
-__global__ void k_root_update(const double* cp, int nrb, int m, const double* b, double reg,
-                              double* x, double* prev_cnt, QState* st) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= m) return;
-    const double cnt = merge_strided(cp + j, nrb, (size_t)m);
-    const double sum = merge_strided(cp + (size_t)nrb * m + j, nrb, (size_t)m);
+// Blocks of (32, 8) threads own 32 columns; the eight threads of a column
+// merge its row-block partials together (a serial chain of FP64 adds per
+// column was latency-bound). The counts are exact in any order.
+__global__ void __launch_bounds__(256) k_root_update(const double* cp, int nrb, int m,
+                                                     const double* b, double reg, double* x,
+                                                     double* prev_cnt, QState* st) {
+    const int j = blockIdx.x * 32 + threadIdx.x;
+    const bool valid = j < m;
+    const double cnt = merge_2d(cp + j, nrb, (size_t)m, valid);
+    __syncthreads();
+    const double sum = merge_2d(cp + (size_t)nrb * m + j, nrb, (size_t)m, valid);
+    if (threadIdx.y != 0 || !valid) return;
     if (cnt != prev_cnt[j]) {
         prev_cnt[j] = cnt;
         x[j] = (reg * b[j] + sum) / cnt;
@@ -156,6 +185,22 @@ __global__ void k_rowroot_update(const double* rp, int nslabs, int n, const doub
         x[i] = (reg * a[i] + sum) / cnt;
         atomicOr(&st->changed, 1);
     }
+}
+
+// Start and condition of the device-side loop of root rounds (the last node
+// of its body): continue while some row or column changed its active set,
+// for at most cap rounds.
+__global__ void k_root_begin(QState* st) {
+    st->changed = 0;
+    st->root_rounds = 0;
+    st->root_unconverged = 0;
+}
+__global__ void k_root_loop(QState* st, int cap, cudaGraphConditionalHandle h) {
+    const int rounds = ++st->root_rounds;
+    const bool changed = st->changed != 0;
+    st->changed = 0;
+    if (changed && rounds >= cap) st->root_unconverged = 1;
+    cudaGraphSetConditional(h, changed && rounds < cap ? 1u : 0u);
 }
 
 // ---- primal value (approx_proj) ----
@@ -894,6 +939,13 @@ __device__ __forceinline__ void st_async_f64(uint32_t dst, double v, uint32_t ba
                  ::"r"(dst), "l"(__double_as_longlong(v)), "r"(bar)
                  : "memory");
 }
+__device__ __forceinline__ void st_async_f2(uint32_t dst, float2 v, uint32_t bar) {
+    const unsigned long long bits =
+        ((unsigned long long)__float_as_uint(v.y) << 32) | __float_as_uint(v.x);
+    asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b64 [%0], %1, [%2];"
+                 ::"r"(dst), "l"(bits), "r"(bar)
+                 : "memory");
+}
 __device__ __forceinline__ bool mbar_wait_cluster(uint64_t* bar, uint32_t parity, long long polls) {
     const uint32_t a = sm100::smem_u32(bar);
     for (long long s = 0; s < polls; ++s) {
@@ -1131,6 +1183,258 @@ __global__ void __launch_bounds__(kDsT, 1) k_schur_cg_dsm(DsmCgArgs da) {
     cluster_barrier();
 }
 
+// ---- the mixed engine's cluster CG in double-word FP32 ----
+// On this part an FP64 add or FMA has a latency of about 63 cycles, a
+// division about 550 and an FP64 <-> FP32 conversion about 64 (measured),
+// and every CG step is a chain of them: the reductions, alpha and beta, the
+// splits the products read. The mixed engine therefore runs the CG itself in
+// double-word FP32 (hi + lo, about 48 bits): x, r, p, y, the reductions,
+// alpha and beta. FP64 is left to the per-solve setup and the results. The
+// right-hand side is scaled by a power of two that brings ||zy|| near 1
+// (exact, so the iterates are the same numbers scaled), which keeps every
+// quantity far inside FP32's exponent range. Same exchange scheme as
+// k_schur_cg_dsm.
+struct DwCgArgs {
+    DsmCgArgs d;
+    float2 *xw, *rw, *pw, *yw;  // double-word CG vectors over the columns
+    float2 *dinvw, *hmw;        // 1 / (h1 + mu) over the rows, h2 + mu over the columns
+};
+
+struct DwShared {
+    float2 vals[kDsT];
+    float2 red[2][16];
+    float2 bc[2];
+    double vals_d[kDsT / 32];
+    double red_d[16];
+    double bc_d;
+    uint64_t bar[4];
+    int abort;
+};
+
+__device__ __forceinline__ float2 shfl_xor_f2(float2 v, int o) {
+    return make_float2(__shfl_xor_sync(0xffffffffu, v.x, o), __shfl_xor_sync(0xffffffffu, v.y, o));
+}
+__device__ __forceinline__ float2 warp_allsum_dw(float2 v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = dw_add(v, shfl_xor_f2(v, o));
+    return v;
+}
+
+__global__ void __launch_bounds__(kDsT, 1) k_schur_cg_dw(DwCgArgs wa) {
+    extern __shared__ __align__(16) unsigned char ds_dyn[];
+    __shared__ DwShared sh;
+    const ClusterCgArgs& a = wa.d.c;
+    const unsigned nc = cluster_nctarank(), rk = cluster_ctarank();
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int n = a.n, m = a.m;
+    const double mu = a.mu;
+    float2* Ts = reinterpret_cast<float2*>(ds_dyn);
+    float2* Ps = reinterpret_cast<float2*>(ds_dyn + (size_t)((n + 1) & ~1) * 8);
+    const DsSlices rs(n, nc), cs(m, nc);
+    const int r0 = rs.begin(n, rk), r1 = rs.end(n, rk);
+    const int c0 = cs.begin(m, rk), c1 = cs.end(m, rk);
+    uint32_t t_in = 0, p_in = 0;
+    for (unsigned k = 0; k < nc; ++k)
+        if (k != rk) {
+            t_in += rs.bytes(n, k);
+            p_in += cs.bytes(m, k);
+        }
+    if (tid == 0) {
+        for (int q = 0; q < 4; ++q) sm100::mbar_init(&sh.bar[q], 1);
+        sm100::fence_mbar_init();
+        sh.abort = 0;
+    }
+    uint32_t ph = 0u;  // bit q: the parity barrier q waits for next
+    cluster_barrier();
+
+    auto wait_bar = [&](int q) {
+        if (!mbar_wait_cluster(&sh.bar[q], (ph >> q) & 1u, wa.d.polls)) {
+            sh.abort = 1;
+            atomicExch(wa.d.err, 1);
+        }
+    };
+    auto exchange = [&](float2* vs, int b, uint32_t bytes, uint32_t in_bytes, int q) -> bool {
+        sm100::fence_proxy_async_smem();
+        __syncthreads();
+        if (warp == 0) {
+            const uint32_t src = sm100::smem_u32(vs) + (uint32_t)b * 8u;
+            const uint32_t bar = sm100::smem_u32(&sh.bar[q]);
+            if (bytes > 0 && lane < (int)nc && lane != (int)rk)
+                bulk_s2cluster(mapa_u32(src, lane), src, bytes, mapa_u32(bar, lane));
+            if (lane == 0) {
+                sm100::mbar_arrive_expect_tx(&sh.bar[q], in_bytes);
+                wait_bar(q);
+            }
+        }
+        __syncthreads();
+        ph ^= 1u << q;
+        return sh.abort == 0;
+    };
+    // Cluster total of one double-word value per thread (slot 0: p'q,
+    // slot 1: r'r); bc[1] = num / total, or total / num with inv.
+    auto all_sum = [&](float2 v, int slot, float2 num, bool inv) -> bool {
+        const int q = 2 + slot;
+        sh.vals[tid] = v;
+        __syncthreads();
+        if (warp == 0) {
+            // fixed tree over the eight warps' values, then a butterfly
+            float2 u[kDsT / 32];
+#pragma unroll
+            for (int k = 0; k < kDsT / 32; ++k) u[k] = sh.vals[k * 32 + lane];
+#pragma unroll
+            for (int w = kDsT / 64; w > 0; w >>= 1)
+#pragma unroll
+                for (int k = 0; k < w; ++k) u[k] = dw_add(u[k], u[k + w]);
+            const float2 s = warp_allsum_dw(u[0]);
+            const uint32_t bar = sm100::smem_u32(&sh.bar[q]);
+            if (lane == (int)rk) sh.red[slot][rk] = s;
+            else if (lane < (int)nc)
+                st_async_f2(mapa_u32(sm100::smem_u32(&sh.red[slot][rk]), lane), s,
+                            mapa_u32(bar, lane));
+            if (lane == 0) {
+                sm100::mbar_arrive_expect_tx(&sh.bar[q], (nc - 1) * 8u);
+                wait_bar(q);
+            }
+            __syncwarp();
+            float2 c = lane < (int)nc ? sh.red[slot][lane] : make_float2(0.f, 0.f);
+#pragma unroll
+            for (int o = 8; o > 0; o >>= 1) c = dw_add(c, shfl_xor_f2(c, o));
+            if (lane == 0) {
+                sh.bc[0] = c;
+                sh.bc[1] = inv ? dw_div(c, num) : dw_div(num, c);
+            }
+        }
+        __syncthreads();
+        ph ^= 1u << q;
+        return sh.abort == 0;
+    };
+
+    // ---- setup in FP64: v = w / (h1 + mu), zy = z - sigma' v, ||zy||^2 ----
+    for (int i = r0 + tid; i < r1; i += kDsT) {
+        const double di = 1.0 / (a.h1[i] + mu);
+        a.dinv[i] = di;
+        wa.dinvw[i] = dw_from(di);
+        Ts[i] = dw_from(a.w[i] * di);
+    }
+    bool ok = exchange(Ts, r0, rs.bytes(n, rk), t_in, 0);
+    double part_d = 0.0;
+    if (ok)
+        for (int j = c0 + tid; j < c1; j += kDsT) {
+            const double zy = a.z[j] - list_sum_s<true>(a.colptr, a.rowidx, j, Ts);
+            a.r[j] = zy;
+            part_d += zy * zy;
+        }
+    // FP64 total of ||zy||^2 (once per solve), by the same exchange of CTA totals
+    double rr0 = 0.0;
+    if (ok) {
+        const double ws = warp_allsum_d(part_d);
+        if (lane == 0) sh.vals_d[warp] = ws;
+        __syncthreads();
+        if (warp == 0) {
+            double s0 = lane < kDsT / 32 ? sh.vals_d[lane] : 0.0;
+            s0 = warp_allsum_d(s0);
+            const uint32_t bar = sm100::smem_u32(&sh.bar[3]);
+            if (lane == (int)rk) sh.red_d[rk] = s0;
+            else if (lane < (int)nc)
+                st_async_f64(mapa_u32(sm100::smem_u32(&sh.red_d[rk]), lane), s0,
+                             mapa_u32(bar, lane));
+            if (lane == 0) {
+                sm100::mbar_arrive_expect_tx(&sh.bar[3], (nc - 1) * 8u);
+                wait_bar(3);
+            }
+            __syncwarp();
+            double c = lane < (int)nc ? sh.red_d[lane] : 0.0;
+            c = warp_allsum_d(c);
+            if (lane == 0) sh.bc_d = c;
+        }
+        __syncthreads();
+        ph ^= 1u << 3;
+        ok = sh.abort == 0;
+        rr0 = sh.bc_d;
+    }
+    // scale 2^-e with ||zy|| = f 2^e, f in [0.5, 1)
+    int ex = 0;
+    if (rr0 > 0.0) frexp(sqrt(rr0), &ex);
+    const double scale = ldexp(1.0, -ex);
+    const float2 thresh = dw_from(fmax(a.tol * a.tol * rr0, 2.2250738585072014e-308) * scale * scale);
+    float2 rr = dw_from(rr0 * scale * scale);
+    bool done = !(rr0 > 0.0) || rr0 < fmax(a.tol * a.tol * rr0, 2.2250738585072014e-308);
+    if (ok)
+        for (int j = c0 + tid; j < c1; j += kDsT) {
+            const float2 zs = dw_from(a.r[j] * scale);
+            wa.xw[j] = make_float2(0.f, 0.f);
+            wa.rw[j] = zs;
+            wa.pw[j] = zs;
+            wa.hmw[j] = dw_from(a.h2[j] + mu);
+            Ps[j] = zs;
+        }
+    if (ok) ok = exchange(Ps, c0, cs.bytes(m, rk), p_in, 1);
+    int it = 0;
+    while (ok && !done) {
+        for (int i = r0 + tid; i < r1; i += kDsT) {
+            const int b = __ldg(a.rowptr + i), e = __ldg(a.rowptr + i + 1);
+            float sx = 0.f, ex2 = 0.f;
+            for (int k = b; k < e; ++k) cadd(sx, ex2, Ps[__ldg(a.colidx + k)]);
+            Ts[i] = dw_mul(dw_norm(sx, ex2), wa.dinvw[i]);
+        }
+        if (!(ok = exchange(Ts, r0, rs.bytes(n, rk), t_in, 0))) break;
+        float2 part = make_float2(0.f, 0.f);
+        for (int j = c0 + tid; j < c1; j += kDsT) {
+            const int b = __ldg(a.colptr + j), e = __ldg(a.colptr + j + 1);
+            float su = 0.f, eu = 0.f;
+            for (int k = b; k < e; ++k) cadd(su, eu, Ts[__ldg(a.rowidx + k)]);
+            const float2 pj = wa.pw[j];
+            const float2 yj = dw_sub(dw_mul(wa.hmw[j], pj), dw_norm(su, eu));
+            wa.yw[j] = yj;
+            part = dw_add(part, dw_mul(pj, yj));
+        }
+        if (!(ok = all_sum(part, 0, rr, false))) break;
+        const float2 alpha = sh.bc[1];
+        part = make_float2(0.f, 0.f);
+        for (int j = c0 + tid; j < c1; j += kDsT) {
+            const float2 pj = wa.pw[j];
+            wa.xw[j] = dw_add(wa.xw[j], dw_mul(alpha, pj));
+            const float2 rj = dw_sub(wa.rw[j], dw_mul(alpha, wa.yw[j]));
+            wa.rw[j] = rj;
+            part = dw_add(part, dw_mul(rj, rj));
+        }
+        if (!(ok = all_sum(part, 1, rr, true))) break;
+        const float2 rn = sh.bc[0];
+        ++it;
+        if (dw_lt(rn, thresh) || it >= a.cg_max || !(rn.x == rn.x)) {
+            done = true;
+        } else {
+            const float2 beta = sh.bc[1];  // rn / rr
+            rr = rn;
+            for (int j = c0 + tid; j < c1; j += kDsT) {
+                const float2 pj = dw_add(wa.rw[j], dw_mul(beta, wa.pw[j]));
+                wa.pw[j] = pj;
+                Ps[j] = pj;
+            }
+            ok = exchange(Ps, c0, cs.bytes(m, rk), p_in, 1);
+        }
+    }
+    if (ok) {
+        // x (unscaled, FP64) and r1 = (w - sigma x) / (h1 + mu)
+        const double inv_scale = ldexp(1.0, ex);
+        for (int j = c0 + tid; j < c1; j += kDsT) {
+            const float2 xj = wa.xw[j];
+            a.x[j] = dw_to(xj) * inv_scale;
+            Ps[j] = xj;
+        }
+        ok = exchange(Ps, c0, cs.bytes(m, rk), p_in, 1);
+        if (ok)
+            for (int i = r0 + tid; i < r1; i += kDsT) {
+                const int b = __ldg(a.rowptr + i), e = __ldg(a.rowptr + i + 1);
+                float sx = 0.f, ex2 = 0.f;
+                for (int k = b; k < e; ++k) cadd(sx, ex2, Ps[__ldg(a.colidx + k)]);
+                a.r1[i] = (a.w[i] - ((double)sx + (double)ex2) * inv_scale) * a.dinv[i];
+            }
+    }
+    if (rk == 0 && tid == 0) *a.it_out = it;
+    cluster_barrier();
+}
+
 __global__ void k_time(unsigned long long t0, unsigned long long* out) {
     *out = globaltimer_ns() - t0;
 }
@@ -1155,7 +1459,10 @@ public:
         grad_.alloc(N, st);
         h_.alloc(N, st);
         vec_.alloc(6 * (size_t)std::max(n_, m_), st);
-        parts_.alloc(6 * (size_t)cdiv(N, kVT), st);
+        // block partials of the merge kernels: up to 6 per 64-thread block,
+        // 3 per (32, 8) block of 32 rows or columns
+        parts_.alloc(std::max(6 * (size_t)cdiv(N, kVT), 3 * (size_t)(cdiv(n_, 32) + cdiv(m_, 32))),
+                     st);
         state_.alloc(1, st);
         QState z{};
         h2d(state_.get(), &z, sizeof(z), st);
@@ -1187,14 +1494,14 @@ public:
         ops_.pass(mask ? OP_Q_GRADMASK : OP_Q_GRAD, p);
         const int blocks = pass_blocks(mask ? OP_Q_GRADMASK : OP_Q_GRAD, mixed_, n_, m_);
         k_sum_totals<<<1, 256, 0, st_>>>(ops_.buf().totpart.get(), blocks, scal_.get());
-        const int g = cdiv(n_ + m_, kVT);
+        const int g = cdiv(n_, 32) + cdiv(m_, 32);
         if (mixed_)
-            k_q_grad<float><<<g, kVT, 0, st_>>>(
+            k_q_grad<float><<<g, dim3(32, 8), 0, st_>>>(
                 (const float*)ops_.buf().rowpart.get(), sh.nslabs,
                 (const float*)ops_.buf().colpart.get(), sh.nrb, n_, m_, mask ? 1 : 0, gamma,
                 P_->a, P_->b, reg_, grad, h_.get(), h_.get() + n_, parts_.get(), state_.get());
         else
-            k_q_grad<double><<<g, kVT, 0, st_>>>(
+            k_q_grad<double><<<g, dim3(32, 8), 0, st_>>>(
                 (const double*)ops_.buf().rowpart.get(), sh.nslabs,
                 (const double*)ops_.buf().colpart.get(), sh.nrb, n_, m_, mask ? 1 : 0, gamma,
                 P_->a, P_->b, reg_, grad, h_.get(), h_.get() + n_, parts_.get(), state_.get());
@@ -1241,14 +1548,14 @@ public:
         k_sum_totals<<<1, 256, 0, st_>>>(ops_.buf().totpart.get(), blocks, scal_.get());
         k_sum_totals<<<1, 256, 0, st_>>>(ops_.buf().totpart.get() + blocks, blocks,
                                           scal_.get() + 1);
-        const int g = cdiv(n_ + m_, kVT);
+        const int g = cdiv(n_, 32) + cdiv(m_, 32);
         if (mixed_)
-            k_q_grad<float><<<g, kVT, 0, st_>>>(
+            k_q_grad<float><<<g, dim3(32, 8), 0, st_>>>(
                 (const float*)ops_.buf().rowpart.get(), sh.nslabs,
                 (const float*)ops_.buf().colpart.get(), sh.nrb, n_, m_, 0, gamma_.get(), P_->a,
                 P_->b, reg_, grad_.get(), h_.get(), h_.get() + n_, parts_.get(), state_.get());
         else
-            k_q_grad<double><<<g, kVT, 0, st_>>>(
+            k_q_grad<double><<<g, dim3(32, 8), 0, st_>>>(
                 (const double*)ops_.buf().rowpart.get(), sh.nslabs,
                 (const double*)ops_.buf().colpart.get(), sh.nrb, n_, m_, 0, gamma_.get(), P_->a,
                 P_->b, reg_, grad_.get(), h_.get(), h_.get() + n_, parts_.get(), state_.get());
@@ -1343,62 +1650,34 @@ public:
     }
 
     // beta = optimal_beta(alpha) (qrot_problem.cpp:397-404), into beta (device).
-    void optimal_beta(const double* alpha, double* beta) {
-        double* prev = vec_.get();
-        const int gm = cdiv(m_, kVT);
-        k_root_init<<<gm, kVT, 0, st_>>>(m_, beta, prev);
-        count_launch();
-        PassParams p = ops_.base_params();
-        p.ra = alpha;
-        p.cb = beta;
-        const PassShape sh = ops_.buf().shape;
-        for (int it = 0; it <= n_ + 1; ++it) {
-            const int zero = 0;
-            h2d(&state_.get()->changed, &zero, sizeof(int), st_);
-            ops_.pass(OP_Q_COLROOT, p);
-            k_root_update<<<gm, kVT, 0, st_>>>((const double*)ops_.buf().colpart.get(), sh.nrb,
-                                               m_, P_->b, reg_, beta, prev, state_.get());
-            count_launch();
-            REGOT_CHECK_LAUNCH();
-            int changed = 0;
-            d2h(&changed, &state_.get()->changed, sizeof(int), st_);
-            sync(st_);
-            ++passes_;
-            if (!changed) return;
-        }
-        throw Error(REGOT_ERR_NUMERIC, "optimal_beta did not converge");
-    }
+    void optimal_beta(const double* alpha, double* beta) { root_solve(false, alpha, beta); }
 
     // alpha = optimal_alpha(beta) (qrot_problem.cpp:409-419), into alpha
     // (device): Newton's method from above on each row's piecewise-linear
     // equation, one OP_Q_ROWROOT pass per round, as optimal_beta for columns.
-    void optimal_alpha(const double* beta, double* alpha) {
-        double* prev = vec_.get();
-        const int gn = cdiv(n_, kVT);
-        k_root_init<<<gn, kVT, 0, st_>>>(n_, alpha, prev);
-        count_launch();
-        PassParams p = ops_.base_params();
-        p.ra = alpha;
-        p.cb = beta;
-        const PassShape sh = ops_.buf().shape;
-        for (int it = 0; it <= m_ + 1; ++it) {
-            const int zero = 0;
-            h2d(&state_.get()->changed, &zero, sizeof(int), st_);
-            ops_.pass(OP_Q_ROWROOT, p);
-            k_rowroot_update<<<gn, kVT, 0, st_>>>((const double*)ops_.buf().rowpart.get(),
-                                                   sh.nslabs, n_, P_->a, reg_, alpha, prev,
-                                                   state_.get());
-            count_launch();
-            REGOT_CHECK_LAUNCH();
-            int changed = 0;
-            d2h(&changed, &state_.get()->changed, sizeof(int), st_);
-            sync(st_);
-            ++passes_;
-            if (!changed) return;
-        }
-        throw Error(REGOT_ERR_NUMERIC, "optimal_alpha did not converge");
-    }
+    void optimal_alpha(const double* beta, double* alpha) { root_solve(true, beta, alpha); }
 
+    // The Newton rounds run as a device-side loop: a graph whose only node
+    // is a conditional WHILE node, its body one root pass, the update of
+    // the roots and k_root_loop (cached per pair of vectors). One launch and
+    // one read of the state per call, where a round trip per round made the
+    // solvers that call these every iteration latency-bound.
+    void root_solve(bool rows, const double* other, double* x) {
+        const int len = rows ? n_ : m_;
+        k_root_init<<<cdiv(len, kVT), kVT, 0, st_>>>(len, x, vec_.get());
+        k_root_begin<<<1, 1, 0, st_>>>(state_.get());
+        count_launch(2);
+        RootGraph& g = root_graph(rows, other, x);
+        REGOT_CUDA(cudaGraphLaunch(g.exec, st_));
+        QState hs;
+        d2h(&hs, state_.get(), sizeof(hs), st_);
+        sync(st_);
+        count_launch(g.kernels * hs.root_rounds);
+        passes_ += hs.root_rounds;
+        if (hs.root_unconverged)
+            throw Error(REGOT_ERR_NUMERIC,
+                        rows ? "optimal_alpha did not converge" : "optimal_beta did not converge");
+    }
     // sigma x (n) with optional division by (h1 + mu); mu from *mu_dev when
     // given. With x2 (the FP32 pairs of x; mixed engine) the compensated
     // FP32 kernel runs and out2, if given, receives the pairs of the result.
@@ -1469,6 +1748,69 @@ private:
     double sum_a_ = 0.0;
     double tau_grad_ = 0.0;
     long long passes_ = 0;
+
+    struct RootGraph {
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        long long kernels = 0;
+    };
+    std::map<std::tuple<bool, const double*, double*>, RootGraph> root_graphs_;
+
+    RootGraph& root_graph(bool rows, const double* other, double* x) {
+        RootGraph& g = root_graphs_[std::make_tuple(rows, other, x)];
+        if (g.exec) return g;
+        const int len = rows ? n_ : m_;
+        REGOT_CUDA(cudaGraphCreate(&g.graph, 0));
+        cudaGraphConditionalHandle h;
+        REGOT_CUDA(cudaGraphConditionalHandleCreate(&h, g.graph, 1, cudaGraphCondAssignDefault));
+        cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+        cp.conditional.handle = h;
+        cp.conditional.type = cudaGraphCondTypeWhile;
+        cp.conditional.size = 1;
+        cudaGraphNode_t node;
+        REGOT_CUDA(cudaGraphAddNode(&node, g.graph, nullptr, nullptr, 0, &cp));
+        cudaGraph_t body = cp.conditional.phGraph_out[0];
+        long long* saved = g_launch_counter;
+        g.kernels = 0;
+        g_launch_counter = &g.kernels;
+        REGOT_CUDA(cudaStreamBeginCaptureToGraph(st_, body, nullptr, nullptr, 0,
+                                                 cudaStreamCaptureModeThreadLocal));
+        try {
+            PassParams p = ops_.base_params();
+            p.ra = rows ? x : other;
+            p.cb = rows ? other : x;
+            const PassShape sh = ops_.buf().shape;
+            // the root passes read ra and cb in FP64: no split of them
+            ops_.pass_presplit(rows ? OP_Q_ROWROOT : OP_Q_COLROOT, p);
+            if (rows)
+                k_rowroot_update<<<cdiv(n_, kVT), kVT, 0, st_>>>(
+                    (const double*)ops_.buf().rowpart.get(), sh.nslabs, n_, P_->a, reg_, x,
+                    vec_.get(), state_.get());
+            else
+                k_root_update<<<cdiv(m_, 32), dim3(32, 8), 0, st_>>>(
+                    (const double*)ops_.buf().colpart.get(), sh.nrb, m_, P_->b, reg_, x,
+                    vec_.get(), state_.get());
+            k_root_loop<<<1, 1, 0, st_>>>(state_.get(), len + 2, h);
+            count_launch(2);
+        } catch (...) {
+            cudaGraph_t tmp = nullptr;
+            cudaStreamEndCapture(st_, &tmp);
+            g_launch_counter = saved;
+            throw;
+        }
+        REGOT_CUDA(cudaStreamEndCapture(st_, &body));
+        g_launch_counter = saved;
+        REGOT_CUDA(cudaGraphInstantiate(&g.exec, g.graph, 0));
+        return g;
+    }
+
+public:
+    ~QrotEngine() {
+        for (auto& kv : root_graphs_) {
+            if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+            if (kv.second.graph) cudaGraphDestroy(kv.second.graph);
+        }
+    }
 };
 
 namespace {
@@ -2545,9 +2887,6 @@ public:
         if (graph_) cudaGraphDestroy(graph_);
     }
 
-    // CG steps of the last compact solve (0 after a bitmask-path solve)
-    int last_compact_steps() const { return last_steps_; }
-
 private:
     static constexpr int kGraphSteps = 8;
     // sigma is taken as index lists when it holds at most n m / kDenseRatio
@@ -2559,7 +2898,6 @@ private:
     // index lists, and run the whole CG in one cluster launch. Returns false
     // (nothing solved) when sigma is too dense for it or no cluster fits.
     bool solve_compact(double mu, std::vector<double>& out) {
-        last_steps_ = 0;
         const int mode = g_qrot_cg_path.load(std::memory_order_relaxed);
         const int C = cluster_ctas(E_.mixed());
         if (mode == 1 || C == 0) return false;
@@ -2662,10 +3000,20 @@ private:
             da.c = a;
             da.polls = wait_limit();
             da.err = it_d_.get() + 1;
-            if (E_.mixed())
-                REGOT_CUDA(cudaLaunchKernelEx(&cfg, k_schur_cg_dsm<true>, da));
-            else
+            if (E_.mixed()) {
+                if (!dw_.get()) dw_.alloc(5 * (size_t)m + n, st_);
+                DwCgArgs wa;
+                wa.d = da;
+                wa.xw = dw_.get();
+                wa.rw = wa.xw + m;
+                wa.pw = wa.rw + m;
+                wa.yw = wa.pw + m;
+                wa.hmw = wa.yw + m;
+                wa.dinvw = wa.hmw + m;
+                REGOT_CUDA(cudaLaunchKernelEx(&cfg, k_schur_cg_dw, wa));
+            } else {
                 REGOT_CUDA(cudaLaunchKernelEx(&cfg, k_schur_cg_dsm<false>, da));
+            }
         } else if (E_.mixed()) {
             REGOT_CUDA(cudaLaunchKernelEx(&cfg, k_schur_cg_cluster<true>, a));
         } else {
@@ -2681,7 +3029,6 @@ private:
         if (it[1])
             throw Error(REGOT_ERR_TIMEOUT,
                         "qrot Schur CG: a cluster exchange did not complete within the wait limit");
-        last_steps_ = it[0];
         if (verbose_ >= 2)
             std::printf("[cg] index lists (nnz = %lld%s), niter = %d\n", nnz[0],
                         Cd ? ", shared-memory exchange" : "", it[0]);
@@ -2723,11 +3070,11 @@ private:
     // CTAs per cluster of the shared-memory-exchange CG (the largest
     // dynamic shared memory it may use set once), as cluster_ctas.
     static int dsm_ctas(bool mixed) {
-        static const int sizes[2] = {probe_dsm(false), probe_dsm(true)};
+        static const int sizes[2] = {probe_dsm(k_schur_cg_dsm<false>), probe_dsm(k_schur_cg_dw)};
         return sizes[mixed ? 1 : 0];
     }
-    static int probe_dsm(bool mixed) {
-        auto kern = mixed ? k_schur_cg_dsm<true> : k_schur_cg_dsm<false>;
+    template <typename Kern>
+    static int probe_dsm(Kern kern) {
         if (cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
                 cudaSuccess ||
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -2758,8 +3105,8 @@ private:
     DBuf<int> rcnt_, rowptr_, ccnt_, ccol_, colptr_, colidx_, rowidx_, it_d_;
     DBuf<long long> nnz_d_;
     DBuf<double> dinv_;
+    DBuf<float2> dw_;  // double-word CG vectors of the mixed engine's cluster CG
     size_t idx_cap_ = 0;
-    int last_steps_ = 0;
 
     // One CG step on Delta = h2 o x + mu x - sigma' ((sigma x) / (h1 + mu)),
     // mu from the state; a no-op once the device flag cg_done is set.
