@@ -1196,8 +1196,8 @@ __global__ void __launch_bounds__(kDsT, 1) k_schur_cg_dsm(DsmCgArgs da) {
 // k_schur_cg_dsm.
 struct DwCgArgs {
     DsmCgArgs d;
-    float2 *xw, *rw, *pw, *yw;  // double-word CG vectors over the columns
-    float2 *dinvw, *hmw;        // 1 / (h1 + mu) over the rows, h2 + mu over the columns
+    int idx_cap;  // ints of dynamic shared memory after the vectors for the
+                  // CTA's index-list slices (each slice fits when >= nnz)
 };
 
 struct DwShared {
@@ -1219,7 +1219,27 @@ __device__ __forceinline__ float2 warp_allsum_dw(float2 v) {
     for (int o = 16; o > 0; o >>= 1) v = dw_add(v, shfl_xor_f2(v, o));
     return v;
 }
+// Compensated sum of v[idx[k]], k in [b, e) (idx and v in shared memory, or
+// idx in global memory when the CTA's slice did not fit).
+__device__ __forceinline__ float2 gather_sum(const int* idx, int b, int e, const float2* v) {
+    float s = 0.f, er = 0.f;
+    int k = b;
+    for (; k + 2 <= e; k += 2) {
+        const float2 u0 = v[idx[k]], u1 = v[idx[k + 1]];
+        cadd(s, er, u0);
+        cadd(s, er, u1);
+    }
+    if (k < e) cadd(s, er, v[idx[k]]);
+    return dw_norm(s, er);
+}
 
+// K: rows and columns per thread (the CTA's slices hold at most K * kDsT).
+// Each thread keeps its rows' and columns' CG state in registers and the
+// CTA's slices of the index lists sit in shared memory: after a
+// cluster-scope acquire, global loads no longer hit L1, and the L2 round
+// trips of re-reading them every step (about 700 cycles per dependent load)
+// had made each phase cost 1-2 thousand cycles.
+template <int K>
 __global__ void __launch_bounds__(kDsT, 1) k_schur_cg_dw(DwCgArgs wa) {
     extern __shared__ __align__(16) unsigned char ds_dyn[];
     __shared__ DwShared sh;
@@ -1230,6 +1250,7 @@ __global__ void __launch_bounds__(kDsT, 1) k_schur_cg_dw(DwCgArgs wa) {
     const double mu = a.mu;
     float2* Ts = reinterpret_cast<float2*>(ds_dyn);
     float2* Ps = reinterpret_cast<float2*>(ds_dyn + (size_t)((n + 1) & ~1) * 8);
+    int* sidx = reinterpret_cast<int*>(ds_dyn + (size_t)(((n + 1) & ~1) + ((m + 1) & ~1)) * 8);
     const DsSlices rs(n, nc), cs(m, nc);
     const int r0 = rs.begin(n, rk), r1 = rs.end(n, rk);
     const int c0 = cs.begin(m, rk), c1 = cs.end(m, rk);
@@ -1244,7 +1265,35 @@ __global__ void __launch_bounds__(kDsT, 1) k_schur_cg_dw(DwCgArgs wa) {
         sm100::fence_mbar_init();
         sh.abort = 0;
     }
+    // this CTA's slices of the index lists, in shared memory when they fit
+    const int rbase = __ldg(a.rowptr + r0), rcount = __ldg(a.rowptr + r1) - rbase;
+    const int cbase = __ldg(a.colptr + c0), ccount = __ldg(a.colptr + c1) - cbase;
+    const bool fit = rcount + ccount <= wa.idx_cap;
+    const int* ridx = fit ? sidx : a.colidx + rbase;
+    const int* cidx = fit ? sidx + rcount : a.rowidx + cbase;
+    if (fit) {
+        for (int k = tid; k < rcount; k += kDsT) sidx[k] = __ldg(a.colidx + rbase + k);
+        for (int k = tid; k < ccount; k += kDsT) sidx[rcount + k] = __ldg(a.rowidx + cbase + k);
+    }
+    // per-thread rows i = r0 + tid + u kDsT and columns j = c0 + tid + u kDsT
+    int rb[K], re[K], cb[K], ce[K];
+    float2 dinv[K], hm[K], x[K], r[K], p[K], y[K];
+#pragma unroll
+    for (int u = 0; u < K; ++u) {
+        const int i = r0 + tid + u * kDsT, j = c0 + tid + u * kDsT;
+        rb[u] = re[u] = cb[u] = ce[u] = 0;
+        if (i < r1) {
+            rb[u] = __ldg(a.rowptr + i) - rbase;
+            re[u] = __ldg(a.rowptr + i + 1) - rbase;
+        }
+        if (j < c1) {
+            cb[u] = __ldg(a.colptr + j) - cbase;
+            ce[u] = __ldg(a.colptr + j + 1) - cbase;
+        }
+        dinv[u] = hm[u] = x[u] = r[u] = p[u] = y[u] = make_float2(0.f, 0.f);
+    }
     uint32_t ph = 0u;  // bit q: the parity barrier q waits for next
+    // barriers initialised, slices staged, every CTA running
     cluster_barrier();
 
     auto wait_bar = [&](int q) {
@@ -1277,7 +1326,6 @@ __global__ void __launch_bounds__(kDsT, 1) k_schur_cg_dw(DwCgArgs wa) {
         sh.vals[tid] = v;
         __syncthreads();
         if (warp == 0) {
-            // fixed tree over the eight warps' values, then a butterfly
             float2 u[kDsT / 32];
 #pragma unroll
             for (int k = 0; k < kDsT / 32; ++k) u[k] = sh.vals[k * 32 + lane];
@@ -1308,22 +1356,72 @@ __global__ void __launch_bounds__(kDsT, 1) k_schur_cg_dw(DwCgArgs wa) {
         ph ^= 1u << q;
         return sh.abort == 0;
     };
+    // exchange and all_sum (slot 1, total / num) in one round: the slice's
+    // bulk copies and the CTA total's st.async complete on barrier 1.
+    auto exchange_sum = [&](float2* vs, int b, uint32_t bytes, uint32_t in_bytes, float2 v,
+                            float2 num) -> bool {
+        sh.vals[tid] = v;
+        sm100::fence_proxy_async_smem();
+        __syncthreads();
+        if (warp == 0) {
+            float2 u[kDsT / 32];
+#pragma unroll
+            for (int k = 0; k < kDsT / 32; ++k) u[k] = sh.vals[k * 32 + lane];
+#pragma unroll
+            for (int w = kDsT / 64; w > 0; w >>= 1)
+#pragma unroll
+                for (int k = 0; k < w; ++k) u[k] = dw_add(u[k], u[k + w]);
+            const float2 t = warp_allsum_dw(u[0]);
+            const uint32_t src = sm100::smem_u32(vs) + (uint32_t)b * 8u;
+            const uint32_t bar = sm100::smem_u32(&sh.bar[1]);
+            if (lane == (int)rk) {
+                sh.red[1][rk] = t;
+            } else if (lane < (int)nc) {
+                const uint32_t rbar = mapa_u32(bar, lane);
+                if (bytes > 0) bulk_s2cluster(mapa_u32(src, lane), src, bytes, rbar);
+                st_async_f2(mapa_u32(sm100::smem_u32(&sh.red[1][rk]), lane), t, rbar);
+            }
+            if (lane == 0) {
+                sm100::mbar_arrive_expect_tx(&sh.bar[1], in_bytes + (nc - 1) * 8u);
+                wait_bar(1);
+            }
+            __syncwarp();
+            float2 c = lane < (int)nc ? sh.red[1][lane] : make_float2(0.f, 0.f);
+#pragma unroll
+            for (int o = 8; o > 0; o >>= 1) c = dw_add(c, shfl_xor_f2(c, o));
+            if (lane == 0) {
+                sh.bc[0] = c;
+                sh.bc[1] = dw_div(c, num);
+            }
+        }
+        __syncthreads();
+        ph ^= 1u << 1;
+        return sh.abort == 0;
+    };
 
     // ---- setup in FP64: v = w / (h1 + mu), zy = z - sigma' v, ||zy||^2 ----
-    for (int i = r0 + tid; i < r1; i += kDsT) {
-        const double di = 1.0 / (a.h1[i] + mu);
-        a.dinv[i] = di;
-        wa.dinvw[i] = dw_from(di);
-        Ts[i] = dw_from(a.w[i] * di);
+#pragma unroll
+    for (int u = 0; u < K; ++u) {
+        const int i = r0 + tid + u * kDsT;
+        if (i < r1) {
+            const double di = 1.0 / (a.h1[i] + mu);
+            a.dinv[i] = di;
+            dinv[u] = dw_from(di);
+            Ts[i] = dw_from(a.w[i] * di);
+        }
     }
     bool ok = exchange(Ts, r0, rs.bytes(n, rk), t_in, 0);
+    double zy[K];
     double part_d = 0.0;
-    if (ok)
-        for (int j = c0 + tid; j < c1; j += kDsT) {
-            const double zy = a.z[j] - list_sum_s<true>(a.colptr, a.rowidx, j, Ts);
-            a.r[j] = zy;
-            part_d += zy * zy;
+#pragma unroll
+    for (int u = 0; u < K; ++u) {
+        const int j = c0 + tid + u * kDsT;
+        zy[u] = 0.0;
+        if (ok && j < c1) {
+            zy[u] = a.z[j] - dw_to(gather_sum(cidx, cb[u], ce[u], Ts));
+            part_d += zy[u] * zy[u];
         }
+    }
     // FP64 total of ||zy||^2 (once per solve), by the same exchange of CTA totals
     double rr0 = 0.0;
     if (ok) {
@@ -1356,82 +1454,93 @@ __global__ void __launch_bounds__(kDsT, 1) k_schur_cg_dw(DwCgArgs wa) {
     int ex = 0;
     if (rr0 > 0.0) frexp(sqrt(rr0), &ex);
     const double scale = ldexp(1.0, -ex);
-    const float2 thresh = dw_from(fmax(a.tol * a.tol * rr0, 2.2250738585072014e-308) * scale * scale);
+    const double thr = fmax(a.tol * a.tol * rr0, 2.2250738585072014e-308);
+    const float2 thresh = dw_from(thr * scale * scale);
     float2 rr = dw_from(rr0 * scale * scale);
-    bool done = !(rr0 > 0.0) || rr0 < fmax(a.tol * a.tol * rr0, 2.2250738585072014e-308);
-    if (ok)
-        for (int j = c0 + tid; j < c1; j += kDsT) {
-            const float2 zs = dw_from(a.r[j] * scale);
-            wa.xw[j] = make_float2(0.f, 0.f);
-            wa.rw[j] = zs;
-            wa.pw[j] = zs;
-            wa.hmw[j] = dw_from(a.h2[j] + mu);
-            Ps[j] = zs;
+    bool done = !(rr0 > 0.0) || rr0 < thr;
+#pragma unroll
+    for (int u = 0; u < K; ++u) {
+        const int j = c0 + tid + u * kDsT;
+        if (ok && j < c1) {
+            r[u] = p[u] = dw_from(zy[u] * scale);
+            hm[u] = dw_from(a.h2[j] + mu);
+            Ps[j] = p[u];
         }
+    }
+    // Ps carries r: the rows' products are sigma p = sigma r + beta sigma p_prev
+    // (s, per row; p_0 = r_0), which lets r travel with the r'r totals
     if (ok) ok = exchange(Ps, c0, cs.bytes(m, rk), p_in, 1);
+    float2 sp[K], beta = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int u = 0; u < K; ++u) sp[u] = make_float2(0.f, 0.f);
     int it = 0;
     while (ok && !done) {
-        for (int i = r0 + tid; i < r1; i += kDsT) {
-            const int b = __ldg(a.rowptr + i), e = __ldg(a.rowptr + i + 1);
-            float sx = 0.f, ex2 = 0.f;
-            for (int k = b; k < e; ++k) cadd(sx, ex2, Ps[__ldg(a.colidx + k)]);
-            Ts[i] = dw_mul(dw_norm(sx, ex2), wa.dinvw[i]);
+#pragma unroll
+        for (int u = 0; u < K; ++u) {
+            const int i = r0 + tid + u * kDsT;
+            if (i < r1) {
+                sp[u] = dw_add(gather_sum(ridx, rb[u], re[u], Ps), dw_mul(beta, sp[u]));
+                Ts[i] = dw_mul(sp[u], dinv[u]);
+            }
         }
         if (!(ok = exchange(Ts, r0, rs.bytes(n, rk), t_in, 0))) break;
         float2 part = make_float2(0.f, 0.f);
-        for (int j = c0 + tid; j < c1; j += kDsT) {
-            const int b = __ldg(a.colptr + j), e = __ldg(a.colptr + j + 1);
-            float su = 0.f, eu = 0.f;
-            for (int k = b; k < e; ++k) cadd(su, eu, Ts[__ldg(a.rowidx + k)]);
-            const float2 pj = wa.pw[j];
-            const float2 yj = dw_sub(dw_mul(wa.hmw[j], pj), dw_norm(su, eu));
-            wa.yw[j] = yj;
-            part = dw_add(part, dw_mul(pj, yj));
+#pragma unroll
+        for (int u = 0; u < K; ++u) {
+            const int j = c0 + tid + u * kDsT;
+            if (j < c1) {
+                p[u] = dw_add(r[u], dw_mul(beta, p[u]));
+                y[u] = dw_sub(dw_mul(hm[u], p[u]), gather_sum(cidx, cb[u], ce[u], Ts));
+                part = dw_add(part, dw_mul(p[u], y[u]));
+            }
         }
         if (!(ok = all_sum(part, 0, rr, false))) break;
         const float2 alpha = sh.bc[1];
         part = make_float2(0.f, 0.f);
-        for (int j = c0 + tid; j < c1; j += kDsT) {
-            const float2 pj = wa.pw[j];
-            wa.xw[j] = dw_add(wa.xw[j], dw_mul(alpha, pj));
-            const float2 rj = dw_sub(wa.rw[j], dw_mul(alpha, wa.yw[j]));
-            wa.rw[j] = rj;
-            part = dw_add(part, dw_mul(rj, rj));
+#pragma unroll
+        for (int u = 0; u < K; ++u) {
+            const int j = c0 + tid + u * kDsT;
+            if (j < c1) {
+                x[u] = dw_add(x[u], dw_mul(alpha, p[u]));
+                r[u] = dw_sub(r[u], dw_mul(alpha, y[u]));
+                Ps[j] = r[u];
+                part = dw_add(part, dw_mul(r[u], r[u]));
+            }
         }
-        if (!(ok = all_sum(part, 1, rr, true))) break;
+        if (!(ok = exchange_sum(Ps, c0, cs.bytes(m, rk), p_in, part, rr))) break;
         const float2 rn = sh.bc[0];
         ++it;
         if (dw_lt(rn, thresh) || it >= a.cg_max || !(rn.x == rn.x)) {
             done = true;
         } else {
-            const float2 beta = sh.bc[1];  // rn / rr
+            beta = sh.bc[1];  // rn / rr
             rr = rn;
-            for (int j = c0 + tid; j < c1; j += kDsT) {
-                const float2 pj = dw_add(wa.rw[j], dw_mul(beta, wa.pw[j]));
-                wa.pw[j] = pj;
-                Ps[j] = pj;
-            }
-            ok = exchange(Ps, c0, cs.bytes(m, rk), p_in, 1);
         }
     }
     if (ok) {
         // x (unscaled, FP64) and r1 = (w - sigma x) / (h1 + mu)
         const double inv_scale = ldexp(1.0, ex);
-        for (int j = c0 + tid; j < c1; j += kDsT) {
-            const float2 xj = wa.xw[j];
-            a.x[j] = dw_to(xj) * inv_scale;
-            Ps[j] = xj;
+#pragma unroll
+        for (int u = 0; u < K; ++u) {
+            const int j = c0 + tid + u * kDsT;
+            if (j < c1) {
+                a.x[j] = dw_to(x[u]) * inv_scale;
+                Ps[j] = x[u];
+            }
         }
         ok = exchange(Ps, c0, cs.bytes(m, rk), p_in, 1);
-        if (ok)
-            for (int i = r0 + tid; i < r1; i += kDsT) {
-                const int b = __ldg(a.rowptr + i), e = __ldg(a.rowptr + i + 1);
-                float sx = 0.f, ex2 = 0.f;
-                for (int k = b; k < e; ++k) cadd(sx, ex2, Ps[__ldg(a.colidx + k)]);
-                a.r1[i] = (a.w[i] - ((double)sx + (double)ex2) * inv_scale) * a.dinv[i];
+        if (ok) {
+#pragma unroll
+            for (int u = 0; u < K; ++u) {
+                const int i = r0 + tid + u * kDsT;
+                if (i < r1)
+                    a.r1[i] = (a.w[i] - dw_to(gather_sum(ridx, rb[u], re[u], Ps)) * inv_scale) *
+                              a.dinv[i];
             }
+        }
     }
     if (rk == 0 && tid == 0) *a.it_out = it;
+    // no CTA leaves while another may still read its shared memory
     cluster_barrier();
 }
 
@@ -2980,12 +3089,23 @@ private:
         a.it_out = it_d_.get();
         // both vectors' copies in every CTA's shared memory when they fit
         const size_t ds_bytes = (size_t)(((n + 1) & ~1) + ((m + 1) & ~1)) * 8;
-        const int Cd =
-            ds_bytes <= (size_t)kDsMaxBytes && mode != 3 ? dsm_ctas(E_.mixed()) : 0;
+        int Cd = ds_bytes <= (size_t)kDsMaxBytes && mode != 3 ? dsm_ctas(E_.mixed()) : 0;
+        // mixed engine: rows and columns per thread of the double-word kernel
+        int K = 0;
+        if (Cd && E_.mixed()) {
+            const int per = std::max(((n + 2 * Cd - 1) / (2 * Cd)) * 2,
+                                     ((m + 2 * Cd - 1) / (2 * Cd)) * 2);
+            K = cdiv(per, kDsT);
+            K = K <= 1 ? 1 : K <= 2 ? 2 : K <= 4 ? 4 : K <= 8 ? 8 : 0;
+            if (!K) Cd = 0;
+        }
+        // the CTAs' index-list slices in the shared memory left over
+        const int idx_cap =
+            (int)std::min<long long>(2 * nnz[0], (long long)(kDsMaxBytes - ds_bytes) / 4) & ~3;
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(Cd ? Cd : C);
         cfg.blockDim = dim3(Cd ? kDsT : kCgT);
-        cfg.dynamicSmemBytes = Cd ? ds_bytes : 0;
+        cfg.dynamicSmemBytes = Cd ? ds_bytes + (K ? (size_t)idx_cap * 4 : 0) : 0;
         cfg.stream = st_;
         cudaLaunchAttribute at[1];
         at[0].id = cudaLaunchAttributeClusterDimension;
@@ -3001,16 +3121,13 @@ private:
             da.polls = wait_limit();
             da.err = it_d_.get() + 1;
             if (E_.mixed()) {
-                if (!dw_.get()) dw_.alloc(5 * (size_t)m + n, st_);
                 DwCgArgs wa;
                 wa.d = da;
-                wa.xw = dw_.get();
-                wa.rw = wa.xw + m;
-                wa.pw = wa.rw + m;
-                wa.yw = wa.pw + m;
-                wa.hmw = wa.yw + m;
-                wa.dinvw = wa.hmw + m;
-                REGOT_CUDA(cudaLaunchKernelEx(&cfg, k_schur_cg_dw, wa));
+                wa.idx_cap = idx_cap;
+                if (K == 1) REGOT_CUDA(cudaLaunchKernelEx(&cfg, k_schur_cg_dw<1>, wa));
+                else if (K == 2) REGOT_CUDA(cudaLaunchKernelEx(&cfg, k_schur_cg_dw<2>, wa));
+                else if (K == 4) REGOT_CUDA(cudaLaunchKernelEx(&cfg, k_schur_cg_dw<4>, wa));
+                else REGOT_CUDA(cudaLaunchKernelEx(&cfg, k_schur_cg_dw<8>, wa));
             } else {
                 REGOT_CUDA(cudaLaunchKernelEx(&cfg, k_schur_cg_dsm<false>, da));
             }
@@ -3070,8 +3187,28 @@ private:
     // CTAs per cluster of the shared-memory-exchange CG (the largest
     // dynamic shared memory it may use set once), as cluster_ctas.
     static int dsm_ctas(bool mixed) {
-        static const int sizes[2] = {probe_dsm(k_schur_cg_dsm<false>), probe_dsm(k_schur_cg_dw)};
+        static const int sizes[2] = {probe_dsm(k_schur_cg_dsm<false>), probe_dw()};
         return sizes[mixed ? 1 : 0];
+    }
+    // every instance of the double-word kernel takes the same cluster and
+    // shared-memory attributes; the cluster size is probed on the first
+    static int probe_dw() {
+        const int c = probe_dsm(k_schur_cg_dw<1>);
+        if (c && (set_dsm_attrs(k_schur_cg_dw<2>) && set_dsm_attrs(k_schur_cg_dw<4>) &&
+                  set_dsm_attrs(k_schur_cg_dw<8>)))
+            return c;
+        return 0;
+    }
+    template <typename Kern>
+    static bool set_dsm_attrs(Kern kern) {
+        if (cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+                cudaSuccess ||
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 kDsMaxBytes) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        return true;
     }
     template <typename Kern>
     static int probe_dsm(Kern kern) {
@@ -3105,7 +3242,6 @@ private:
     DBuf<int> rcnt_, rowptr_, ccnt_, ccol_, colptr_, colidx_, rowidx_, it_d_;
     DBuf<long long> nnz_d_;
     DBuf<double> dinv_;
-    DBuf<float2> dw_;  // double-word CG vectors of the mixed engine's cluster CG
     size_t idx_cap_ = 0;
 
     // One CG step on Delta = h2 o x + mu x - sigma' ((sigma x) / (h1 + mu)),
