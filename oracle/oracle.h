@@ -22,11 +22,17 @@
  *   src/LBFGSpp/LBFGSpp/BFGSMat.h, src/LBFGSpp/LBFGSpp/LineSearchNocedalWright.h,
  *   src/LBFGSpp/LBFGSpp/Param.h, src/solvers.cpp (kwargs defaults).
  *
- * Parity status: UNPINNED. The reference ships no tests, fixtures or golden
- * vectors, and it cannot be compiled here (its numerics need Eigen 5.0.1,
- * which setup.py downloads at build time). The oracle is therefore checked
- * against known-answer problems (separable costs with closed-form plans),
- * KKT conditions, and independent numpy/scipy restatements in tests/.
+ * Parity status: pinned at 8-bit resolution to the reference's own outputs,
+ * and otherwise by known answers. The reference ships no tests, fixtures or
+ * golden vectors, and it cannot be compiled here (its numerics need Eigen
+ * 5.0.1, which setup.py downloads at build time). Its only outputs are the
+ * four plan images of its README (figs/plan_*.png: sinkhorn_bcd reg 0.1,
+ * sinkhorn_ssns reg 0.01, qrot_pdip "cg" reg 0.1 and "fp" reg 0.01 on the
+ * 100 x 80 README example). The oracle's plans fall, entry for entry, in
+ * the colormap bins of those images (tests/test_reference_images_cpu.py).
+ * Beyond that the oracle is checked against known-answer problems
+ * (separable costs with closed-form plans), KKT conditions, and independent
+ * numpy/scipy restatements in tests/.
  *
  * Storage: M is column-major n x m (column j contiguous), like the Eigen
  * MatrixXd the reference computes on; loops run j-outer, i-inner as there.

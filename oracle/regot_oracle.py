@@ -7,8 +7,10 @@ tol=1e-6, max_iter=1000, verbose=0, **kwargs)`` (src/solvers.cpp:463-528),
 so tests can call the oracle and the CUDA path the same way.
 
 Only tests, ``__graft_entry__.smoke()`` and the CPU baseline of ``bench.py``
-use this module. Parity status: unpinned (the reference ships no golden
-vectors and cannot be compiled here).
+use this module. Parity status: pinned at 8-bit resolution to the
+reference's own README plan images (four solves on the 100 x 80 README
+example, tests/test_reference_images_cpu.py); the reference ships no golden
+vectors and cannot be compiled here.
 """
 from __future__ import annotations
 
