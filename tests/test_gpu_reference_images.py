@@ -3,16 +3,16 @@ solves that the reference rendered as figs/plan_*.png (README example,
 100 x 80), read back into tests/golden/reference_images/.
 
 Each GPU plan must fall, entry for entry, in the colormap bins of the
-reference's image (1 bin = 1/256 of the plan's range), with the tolerance
-written per case (in bins) for entries next to a bin edge:
-  - FP64 sinkhorn_bcd and qrot_pdip follow the reference's iterates to
-    rounding (the GPU tests hold them to 1e-6 of the largest entry or
-    better): 1e-3 bins;
-  - FP64 sinkhorn_ssns solves its Newton systems by preconditioned CG where
-    the reference factorises (SimplicialLDLT), and mixed precision stores M
-    in FP32: each stops at a point of marginal error below tol that is not
-    the reference's point, so entries may move by a few 1e-5 of the largest
-    one: 0.03 bins.
+reference's image (1 bin = 1/256 of the plan's range). Measured on a GB300,
+all eight cases need no tolerance at all: every entry of every plan lies in
+its bin. The tolerances below (in bins) excuse only entries within them of a
+bin edge:
+  - FP64 follows the reference's iterates to rounding (the GPU tests hold
+    sinkhorn_bcd and qrot_pdip to 1e-6 of the largest entry or better; FP64
+    sinkhorn_ssns solves its Newton systems by preconditioned CG where the
+    reference factorises): 1e-4 bins;
+  - mixed precision stores M in FP32 and forms T in FP32, so entries may
+    move by a few ulps of the largest one: 1e-3 bins.
 """
 import numpy as np
 import pytest
@@ -24,16 +24,7 @@ pytestmark = pytest.mark.gpu
 
 regot = pytest.importorskip("regot")
 
-TOL_BINS = {
-    ("plan_erot_bcd_reg0_1", "fp64"): 1e-3,
-    ("plan_erot_bcd_reg0_1", "mixed"): 3e-2,
-    ("plan_erot_ssns_reg0_01", "fp64"): 3e-2,
-    ("plan_erot_ssns_reg0_01", "mixed"): 3e-2,
-    ("plan_qrot_pdip_reg0_1", "fp64"): 1e-3,
-    ("plan_qrot_pdip_reg0_1", "mixed"): 3e-2,
-    ("plan_qrot_pdip_reg0_01", "fp64"): 1e-3,
-    ("plan_qrot_pdip_reg0_01", "mixed"): 3e-2,
-}
+TOL_BINS = {"fp64": 1e-4, "mixed": 1e-3}
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
@@ -45,7 +36,7 @@ def test_gpu_plan_reproduces_reference_image(name, precision):
                                        max_iter=call["max_iter"], precision=precision,
                                        **call["kwargs"])
     T = np.asarray(r.plan)
-    tol = TOL_BINS[(name, precision)]
+    tol = TOL_BINS[precision]
     bad = P.violations(T, labels, rgb, tol=tol)
     assert bad == 0, (f"{bad} constraints broken at {tol} bins; "
                       f"needed {P.needed_tol(T, labels, rgb)}")
