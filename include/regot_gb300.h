@@ -256,7 +256,8 @@ typedef struct {
  * at once: one row and one column log-sum-exp kernel per sweep over all
  * problems still running, each problem stopping at its own iteration with
  * the reference's test (marginal error < tol, or max_iter). The sweeps run
- * as a device-side loop. */
+ * as a device-side loop; the last few problems finish in the tail kernel
+ * (regot_set_batch_tail). */
 int regot_erot_solve_batched(regot_ctx* ctx, const regot_batch_desc* desc, double reg, double tol,
                              int max_iter, regot_batch_result* res);
 /* The half-sweeps of a dimension class (d <= 4, <= 8, <= 16) run either on
@@ -272,6 +273,17 @@ int regot_erot_solve_batched(regot_ctx* ctx, const regot_batch_desc* desc, doubl
  * counterpart in the reference. */
 int regot_force_batch_variant(int variant);
 int regot_batch_variants(regot_ctx* ctx, int* out);
+/* The last problems of a batch: once at most `max_active` problems are still
+ * running, the remaining sweeps run in one launch of thread-block clusters,
+ * one cluster of 16 CTAs (8 where the device cannot hold clusters of 16) per
+ * running problem, each running its problem's
+ * sweeps to its stop with cluster barriers between the half-sweeps (the
+ * same arithmetic and stopping test as the per-sweep kernels). 0 keeps the
+ * per-sweep kernels to the end; a value >= the batch size runs the whole
+ * solve this way after the first two sweeps. Returns the previous setting
+ * (default REGOT_BATCH_TAIL_DEFAULT). No counterpart in the reference. */
+#define REGOT_BATCH_TAIL_DEFAULT 64
+int regot_set_batch_tail(int max_active);
 
 /* regot_erot_solve_batched followed by its backward (no counterpart in the
  * reference, which has no derivatives): at each problem's returned duals,

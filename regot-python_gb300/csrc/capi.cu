@@ -827,6 +827,7 @@ extern "C" long long regot_set_wait_limit(long long spins) { return set_wait_lim
 extern "C" int regot_force_pass_config(int cfg) { return force_pass_config(cfg); }
 
 extern "C" int regot_force_batch_variant(int variant) { return force_batch_variant(variant); }
+extern "C" int regot_set_batch_tail(int max_active) { return set_batch_tail(max_active); }
 extern "C" int regot_force_sparsify_path(int shared_memory) {
     return force_sparsify_path(shared_memory);
 }

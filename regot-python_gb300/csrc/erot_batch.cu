@@ -25,7 +25,9 @@
 // The sweeps run as a device-side loop (a conditional WHILE graph node whose
 // body is two sweeps and a loop kernel): it continues while a problem is
 // running, no dual has left the split grid, and fewer than max_iter / 2 + 3
-// bodies have run.
+// bodies have run. Once few problems are left, the rest of their sweeps run
+// in one launch of the tail kernel (k_btail: a thread-block cluster per
+// problem, cluster barriers in place of kernel boundaries).
 #include <algorithm>
 #include <atomic>
 #include <cmath>
@@ -163,18 +165,28 @@ __device__ __forceinline__ float2 bsplit(double v, const BatchState* st, int* re
     return make_float2((float)h, (float)(v - h));
 }
 
+// Loads of vectors that other CTAs write during the same launch (the tail
+// kernel below): COH = true reads them at L2 (ld.global.cg), past any copy
+// in L1 or the read-only path; the per-sweep kernels read them plainly.
+template <bool COH, typename T>
+__device__ __forceinline__ T bld(const T* p) {
+    if constexpr (COH) return __ldcg(p);
+    else return *p;
+}
 
 // Row half-sweep of iterate k for the row blocks `items` (problem, block):
 // S_i = sum_j exp((alpha_i + beta_j - M_ij)/reg) at (alpha_k, beta_k), the
 // new alpha_i = alpha_i + reg (log a_i - log S_i) (sinkhorn_problem_bcd.cpp:
 // 177-201 with the current alpha as shift) with its split, and the block's
-// sum of (S_i - a_i)^2 for the marginal error.
-template <int DP>
+// sum of (S_i - a_i)^2 for the marginal error. A dual leaving the split
+// grid sets *rgf. The column tile is staged in the caller's shared memory:
+// spts holds kBTile x (DP + 1) pairs, spar kBTile pairs.
+template <int DP, bool COH = false>
 __device__ __forceinline__ void row_item(const BatchDev& B, int2 it, const float2* __restrict__ as_cur,
                                          const float2* __restrict__ bs,
                                          const double* __restrict__ alpha_cur, double* alpha_next,
-                                         float2* as_next, double* part, BatchState* st, float k2,
-                                         double reg) {
+                                         float2* as_next, double* part, BatchState* st, int* rgf,
+                                         float k2, double reg, float2* spts, float2* spar) {
     const int p = it.x;
     const int n = B.n[p], m = B.m[p], d = B.d[p];
     const float sc = B.scale[p];
@@ -197,7 +209,7 @@ __device__ __forceinline__ void row_item(const BatchDev& B, int2 it, const float
             if (r & 1) xp[r >> 1][k].y = v;
             else xp[r >> 1][k].x = v;
         }
-        const float2 s = ok ? as_cur[ro + i] : make_float2(0.f, 0.f);
+        const float2 s = ok ? bld<COH>(as_cur + ro + i) : make_float2(0.f, 0.f);
         const float lk = __fmul_rn(s.y, k2);
         if (r & 1) {
             ah[r >> 1].y = s.x;
@@ -212,8 +224,8 @@ __device__ __forceinline__ void row_item(const BatchDev& B, int2 it, const float
     const float2 sc2 = make_float2(sc, sc), k22 = make_float2(k2, k2);
     // columns staged negated and duplicated, (-y, -y), ready for the packed
     // instructions (rows padded by one entry against bank conflicts)
-    __shared__ float2 sy[kBTile][DP + 1];
-    __shared__ float2 sb[kBTile];
+    float2 (*sy)[DP + 1] = reinterpret_cast<float2 (*)[DP + 1]>(spts);
+    float2* sb = spar;
     for (int j0 = 0; j0 < m; j0 += kBTile) {
         const int cnt = min(kBTile, m - j0);
         for (int e = threadIdx.x; e < kBTile * DP; e += kBWarps * 32) {
@@ -222,7 +234,7 @@ __device__ __forceinline__ void row_item(const BatchDev& B, int2 it, const float
             sy[jj][k] = make_float2(v, v);
         }
         for (int jj = threadIdx.x; jj < kBTile; jj += kBWarps * 32)
-            sb[jj] = jj < cnt ? bs[co + j0 + jj] : make_float2(0.f, 0.f);
+            sb[jj] = jj < cnt ? bld<COH>(bs + co + j0 + jj) : make_float2(0.f, 0.f);
         __syncthreads();
         for (int jj = lane; jj < cnt; jj += 32) {
             float2 ny[DP];
@@ -266,9 +278,10 @@ __device__ __forceinline__ void row_item(const BatchDev& B, int2 it, const float
         const double S = row_sum(mxr, smr);
         const double gi = S - B.a[ro + i];
         g2 = gi * gi;
-        const double an = alpha_cur[ro + i] + reg * (B.loga[ro + i] - 0.69314718055994531 * lg2);
+        const double an =
+            bld<COH>(alpha_cur + ro + i) + reg * (B.loga[ro + i] - 0.69314718055994531 * lg2);
         alpha_next[ro + i] = an;
-        as_next[ro + i] = bsplit(an, st, &st->regrid);
+        as_next[ro + i] = bsplit(an, st, rgf);
     }
     // block partial of sum (S_i - a_i)^2 in a fixed order
     __shared__ double s_g2[kBWarps];
@@ -296,7 +309,10 @@ __global__ void __launch_bounds__(kBWarps * 32) k_brow(
     double reg) {
     const int2 it = items[blockIdx.x];
     if (done[it.x]) return;
-    row_item<DP>(B, it, as_cur, bs, alpha_cur, alpha_next, as_next, part, st, k2, reg);
+    __shared__ float2 sy[kBTile][DP + 1];
+    __shared__ float2 sb[kBTile];
+    row_item<DP>(B, it, as_cur, bs, alpha_cur, alpha_next, as_next, part, st, &st->regrid, k2, reg,
+                 &sy[0][0], sb);
 }
 
 
@@ -305,10 +321,11 @@ __global__ void __launch_bounds__(kBWarps * 32) k_brow(
 // log S_j) in place (sinkhorn_problem_bcd.cpp:149-174, current beta as
 // shift). write_split = 0 skips the split (first half-sweep, before the grid
 // is known).
-template <int DP>
+template <int DP, bool COH = false>
 __device__ __forceinline__ void col_item(const BatchDev& B, int2 it, const float2* __restrict__ as,
-                                         float2* bs, double* beta, BatchState* st, float k2,
-                                         double reg, int write_split) {
+                                         float2* bs, double* beta, BatchState* st, int* rgf,
+                                         float k2, double reg, int write_split, float2* spts,
+                                         float2* spar) {
     const int p = it.x;
     const int n = B.n[p], m = B.m[p], d = B.d[p];
     const float sc = B.scale[p];
@@ -331,7 +348,7 @@ __device__ __forceinline__ void col_item(const BatchDev& B, int2 it, const float
             if (r & 1) ny[r >> 1][k].y = v;
             else ny[r >> 1][k].x = v;
         }
-        const float2 s = ok ? bs[co + j] : make_float2(0.f, 0.f);
+        const float2 s = ok ? bld<COH>(bs + co + j) : make_float2(0.f, 0.f);
         const float lk = __fmul_rn(s.y, k2);
         if (r & 1) {
             bh[r >> 1].y = s.x;
@@ -345,8 +362,8 @@ __device__ __forceinline__ void col_item(const BatchDev& B, int2 it, const float
     }
     const float2 sc2 = make_float2(sc, sc), k22 = make_float2(k2, k2);
     // rows staged duplicated, (x, x), for the packed instructions
-    __shared__ float2 sx[kBTile][DP + 1];
-    __shared__ float2 sa[kBTile];
+    float2 (*sx)[DP + 1] = reinterpret_cast<float2 (*)[DP + 1]>(spts);
+    float2* sa = spar;
     for (int i0 = 0; i0 < n; i0 += kBTile) {
         const int cnt = min(kBTile, n - i0);
         for (int e = threadIdx.x; e < kBTile * DP; e += kBWarps * 32) {
@@ -355,7 +372,7 @@ __device__ __forceinline__ void col_item(const BatchDev& B, int2 it, const float
             sx[ii][k] = make_float2(v, v);
         }
         for (int ii = threadIdx.x; ii < kBTile; ii += kBWarps * 32)
-            sa[ii] = ii < cnt ? as[ro + i0 + ii] : make_float2(0.f, 0.f);
+            sa[ii] = ii < cnt ? bld<COH>(as + ro + i0 + ii) : make_float2(0.f, 0.f);
         __syncthreads();
         for (int ii = lane; ii < cnt; ii += 32) {
             float2 xv[DP];
@@ -395,9 +412,10 @@ __device__ __forceinline__ void col_item(const BatchDev& B, int2 it, const float
     const int j = j0c + lane;
     if (lane < kBPer && j < m) {
         const double lg2 = (double)mxr + (double)log2f(smr);
-        const double bn = beta[co + j] + reg * (B.logb[co + j] - 0.69314718055994531 * lg2);
+        const double bn =
+            bld<COH>(beta + co + j) + reg * (B.logb[co + j] - 0.69314718055994531 * lg2);
         beta[co + j] = bn;
-        if (write_split) bs[co + j] = bsplit(bn, st, &st->regrid);
+        if (write_split) bs[co + j] = bsplit(bn, st, rgf);
     }
 }
 
@@ -408,7 +426,9 @@ __global__ void __launch_bounds__(kBWarps * 32) k_bcol(
     int write_split) {
     const int2 it = items[blockIdx.x];
     if (done[it.x]) return;
-    col_item<DP>(B, it, as, bs, beta, st, k2, reg, write_split);
+    __shared__ float2 sx[kBTile][DP + 1];
+    __shared__ float2 sa[kBTile];
+    col_item<DP>(B, it, as, bs, beta, st, &st->regrid, k2, reg, write_split, &sx[0][0], sa);
 }
 
 // ---- tensor-core variant of the half-sweeps ----
@@ -683,6 +703,135 @@ __global__ void k_bloop(BatchState* st, cudaGraphConditionalHandle h) {
     cudaGraphSetConditional(h, go ? 1u : 0u);
 }
 
+// ---- the tail of the batch: one thread-block cluster per running problem ----
+// When few problems are left, a sweep of the graph loop is a handful of short
+// kernels whose launches cost more than their work. The tail kernel instead
+// gives each running problem one cluster of C CTAs (16, or 8 where a device
+// cannot hold clusters of 16), which runs that problem's sweeps to its stop in
+// one launch: CTA r takes the row blocks and the column blocks r, r + C, ...
+// of the problem (the same row_item /
+// col_item arithmetic as the sweep kernels), and a cluster barrier stands
+// where a kernel boundary stood. The problems' clusters are independent and
+// nothing waits across them.
+//
+// Uniform control flow: every decision (stop, regrid) is taken by every CTA
+// of the cluster from the same data read after a barrier (the row blocks'
+// partials, the problem's own regrid flag) and the same local iteration
+// count, so all CTAs leave the sweep loop at the same point and pass the
+// same barriers. Rank 0 alone writes the problem's iteration count, error,
+// done flag and final parity.
+constexpr int kTailCta = 16;  // CTAs per cluster where the device holds such clusters, else 8
+constexpr size_t kTailSmem = (size_t)kBTile * (kBClassDim[kBClasses - 1] + 1) * sizeof(float2) +
+                             (size_t)kBTile * sizeof(float2);
+
+struct TailArgs {
+    BatchDev B;
+    const int* plist;  // the running problems, one per cluster
+    const int* pcls;   // dimension class of each problem
+    float2* as[2];
+    double* a[2];
+    float2* bs;
+    double* beta;
+    double* part;
+    int* done;
+    int* iter;
+    int* fpar;
+    double* mar;
+    int* pflag;        // per problem: a dual left the split grid
+    BatchState* st;
+    int max_iter;
+    int body_cap;
+    int loops0;        // loop bodies run before this launch (for the sweep count)
+    double tol;
+    float k2;
+    double reg;
+};
+
+__device__ __forceinline__ void tail_barrier() {
+    __threadfence();
+    asm volatile(
+        "barrier.cluster.arrive.release.aligned;\n\t"
+        "barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
+}
+
+template <int DP>
+__device__ void tail_solve(const TailArgs& a, int p, int rank, int ncta, float2* spts,
+                           float2* spar) {
+    const BatchDev& B = a.B;
+    const int nb = (B.n[p] + kBItems - 1) / kBItems, mb = (B.m[p] + kBItems - 1) / kBItems;
+    int* rgf = a.pflag + p;
+    __shared__ double s_g;
+    int k = __ldcg(a.iter + p);  // written by rank 0 only, after this read
+    for (int body = 0; body < a.body_cap; ++body) {
+        // alpha of the current iterate in buffers 0 at the start of a body,
+        // as in the graph loop
+        for (int q = 0; q < 2; ++q) {
+            for (int rb = rank; rb < nb; rb += ncta)
+                row_item<DP, true>(B, make_int2(p, rb), a.as[q], a.bs, a.a[q], a.a[1 - q],
+                                   a.as[1 - q], a.part, a.st, rgf, a.k2, a.reg, spts, spar);
+            tail_barrier();
+            // marginal error and stopping test of the iterate (k_bfin)
+            if (threadIdx.x < 32) {
+                double s = 0.0;
+                for (int j = threadIdx.x; j < nb; j += 32) s += __ldcg(a.part + B.rbo[p] + j);
+                s = warp_sum_d(s);
+                if (threadIdx.x == 0) s_g = sqrt(s);
+            }
+            __syncthreads();
+            const double g = s_g;
+            const bool stop = g < a.tol || k >= a.max_iter;
+            if (rank == 0 && threadIdx.x == 0) {
+                a.mar[p] = g;
+                if (stop) {
+                    a.done[p] = 1;
+                    a.fpar[p] = q;
+                    atomicSub(&a.st->active, 1);
+                    atomicMax(&a.st->loops, a.loops0 + body + 1);
+                } else {
+                    a.iter[p] = k + 1;
+                }
+            }
+            if (stop) return;
+            ++k;
+            for (int cb = rank; cb < mb; cb += ncta)
+                col_item<DP, true>(B, make_int2(p, cb), a.as[1 - q], a.bs, a.beta, a.st, rgf,
+                                   a.k2, a.reg, 1, spts, spar);
+            tail_barrier();
+        }
+        // a dual of this problem left the split grid: stop at the body's end
+        // (alpha in buffers 0) for the host to re-split on a new grid. Every
+        // CTA reads the flag before the barrier, and none can set it again
+        // (in the next row half-sweep) before all have passed the barrier,
+        // so all CTAs see the same value.
+        const int rg = __ldcg(rgf);
+        tail_barrier();
+        if (rg) {
+            if (rank == 0 && threadIdx.x == 0) {
+                atomicOr(&a.st->regrid, 1);
+                atomicMax(&a.st->loops, a.loops0 + body + 1);
+            }
+            return;
+        }
+    }
+    if (rank == 0 && threadIdx.x == 0) atomicMax(&a.st->loops, a.loops0 + a.body_cap);
+}
+
+__global__ void __launch_bounds__(kBWarps * 32) k_btail(const TailArgs a) {
+    extern __shared__ __align__(16) float2 tail_smem[];
+    unsigned rank, ncta, cid;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(rank));
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(ncta));
+    asm volatile("mov.u32 %0, %%clusterid.x;" : "=r"(cid));
+    const int p = a.plist[cid];
+    float2* spts = tail_smem;
+    float2* spar = tail_smem + kBTile * (kBClassDim[kBClasses - 1] + 1);
+    switch (a.pcls[p]) {
+        case 0: tail_solve<4>(a, p, (int)rank, (int)ncta, spts, spar); break;
+        case 1: tail_solve<8>(a, p, (int)rank, (int)ncta, spts, spar); break;
+        default: tail_solve<16>(a, p, (int)rank, (int)ncta, spts, spar); break;
+    }
+}
+
 // Backward of the batch: for each problem, the gradient of its regularised
 // OT cost L = a'alpha + b'beta - reg sum T at the returned duals with respect
 // to the points. By the envelope theorem dL/dM = T, and M_ij = s |x_i - y_j|^2
@@ -878,6 +1027,7 @@ void upload_vec(DBuf<T>& buf, const std::vector<T>& v, cudaStream_t st) {
 std::mutex g_bvar_mutex;
 std::map<std::pair<std::string, int>, int> g_bvar;
 std::atomic<int> g_bvar_force{-1};
+std::atomic<int> g_btail{REGOT_BATCH_TAIL_DEFAULT};
 
 std::string bdevice_name() {
     int dev = 0;
@@ -900,9 +1050,41 @@ void configure_tc_sweep() {
     }
 }
 
+// CTAs per tail cluster on the current device: 16 (a non-portable size) when
+// the device can hold a cluster of 16 of these CTAs, else the portable 8.
+int tail_cluster_size() {
+    static std::atomic<int> cached[64] = {};
+    int dev = 0;
+    REGOT_CUDA(cudaGetDevice(&dev));
+    if (dev < 64 && cached[dev].load() > 0) return cached[dev].load();
+    int size = 8;
+    if (cudaFuncSetAttribute(k_btail, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) ==
+        cudaSuccess) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(kTailCta);
+        cfg.blockDim = dim3(kBWarps * 32);
+        cfg.dynamicSmemBytes = kTailSmem;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = kTailCta;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int clusters = 0;
+        if (cudaOccupancyMaxActiveClusters(&clusters, k_btail, &cfg) == cudaSuccess && clusters > 0)
+            size = kTailCta;
+    }
+    cudaGetLastError();  // a refused query leaves no error behind
+    if (dev < 64) cached[dev].store(size);
+    return size;
+}
+
 }  // namespace
 
 int force_batch_variant(int v) { return g_bvar_force.exchange(v == 0 || v == 1 ? v : -1); }
+
+int set_batch_tail(int max_active) { return g_btail.exchange(std::max(0, max_active)); }
 
 std::vector<int> batch_variants() {
     std::vector<int> out(kBClasses, -1);
@@ -953,8 +1135,9 @@ void erot_solve_batched_gpu(regot_ctx* ctx, const regot_batch_desc* D, double re
     // by n) so that the large problems do not finish last.
     // The lists hold the running problems only: they are rebuilt, and the
     // sweep graph captured again, each time the number of running problems
-    // has halved, so that the last sweeps of a few slow problems do not
-    // launch a CTA for every block of every problem.
+    // has halved (or, below 17, each time one has finished), so that the
+    // last sweeps of a few slow problems do not launch a CTA for every block
+    // of every problem.
     std::vector<int2> ritems[kBClasses], citems[kBClasses];
     std::vector<int2> rtc[kBClasses], ctc[kBClasses];  // blocks of 128 (tensor-core sweeps)
     auto build_items = [&](const std::vector<int>& running) {
@@ -1259,7 +1442,17 @@ void erot_solve_batched_gpu(regot_ctx* ctx, const regot_batch_desc* D, double re
     auto set_stop_below = [&](int v) {
         h2d(&S->stop_below, &v, sizeof(int), st);
     };
-    std::vector<int> stop_host(1, P > 16 ? P / 2 : 0);
+    // the graph loop hands over to the tail kernel once at most tail_max
+    // problems run, and rebuilds its items each time the number has halved
+    const int tail_max = g_btail.load();
+    // where the graph loop stops next: after this body when the tail may take
+    // over, else when the running problems have halved (above 16) or one more
+    // has finished
+    auto next_stop = [&](int active, bool try_tail) {
+        if (try_tail && active <= tail_max) return active;
+        return active > 16 ? active / 2 : std::max(active - 1, 0);
+    };
+    std::vector<int> stop_host(1, next_stop(P, true));
     set_stop_below(stop_host[0]);
     std::unique_ptr<BatchGraph> lg(new BatchGraph());
     make_graph(*lg);
@@ -1285,15 +1478,76 @@ void erot_solve_batched_gpu(regot_ctx* ctx, const regot_batch_desc* D, double re
             read_small(ctx, hdone.data(), done.get(), P * sizeof(int), st);
             for (int p = 0; p < P; ++p)
                 if (!hdone[p]) running.push_back(p);
+            if (hs.active <= tail_max) break;
             build_items(running);
             upload_items();
-            stop_host[0] = hs.active > 16 ? hs.active / 2 : 0;
+            stop_host[0] = next_stop(hs.active, false);
             set_stop_below(stop_host[0]);
             lg.reset(new BatchGraph());
             make_graph(*lg);
             acted = true;
         }
         if (!acted) throw Error(REGOT_ERR_NUMERIC, "batched BCD did not terminate");
+    }
+
+    // The tail: one cluster per running problem, each to its stop. A launch
+    // ends early only for problems whose duals left the split grid; those
+    // continue, after a re-split, in the next launch.
+    if (hs.active > 0) {
+        DBuf<int> dcls, plist(P, st), pflag(P, st);
+        upload_vec(dcls, cls, st);
+        const int tail_cta = tail_cluster_size();
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = tail_cta;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        for (;;) {
+            std::vector<int> hdone(P), running;
+            read_small(ctx, hdone.data(), done.get(), P * sizeof(int), st);
+            for (int p = 0; p < P; ++p)
+                if (!hdone[p]) running.push_back(p);
+            if (running.empty()) break;
+            h2d(plist.get(), running.data(), running.size() * sizeof(int), st);
+            pflag.zero();
+            TailArgs ta{};
+            ta.B = B;
+            ta.plist = plist.get();
+            ta.pcls = dcls.get();
+            for (int q = 0; q < 2; ++q) {
+                ta.as[q] = AS[q].get();
+                ta.a[q] = A[q].get();
+            }
+            ta.bs = BS.get();
+            ta.beta = beta.get();
+            ta.part = part.get();
+            ta.done = done.get();
+            ta.iter = iter.get();
+            ta.fpar = fpar.get();
+            ta.mar = mar.get();
+            ta.pflag = pflag.get();
+            ta.st = S;
+            ta.max_iter = max_iter;
+            ta.body_cap = std::max(1, hs.loop_cap - hs.loops);
+            ta.loops0 = hs.loops;
+            ta.tol = tol;
+            ta.k2 = k2;
+            ta.reg = reg;
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3((unsigned)running.size() * tail_cta);
+            cfg.blockDim = dim3(kBWarps * 32);
+            cfg.dynamicSmemBytes = kTailSmem;
+            cfg.stream = st;
+            cfg.attrs = at;
+            cfg.numAttrs = 1;
+            REGOT_CUDA(cudaLaunchKernelEx(&cfg, k_btail, ta));
+            count_launch();
+            read_small(ctx, &hs, S, sizeof(hs), st);
+            if (hs.active == 0) break;
+            if (!hs.regrid || hs.loops >= hs.loop_cap)
+                throw Error(REGOT_ERR_NUMERIC, "batched BCD did not terminate");
+            regrid(0);
+        }
     }
 
     // Backward: costs and point gradients at every problem's last iterate,

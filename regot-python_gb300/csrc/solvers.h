@@ -48,6 +48,10 @@ void erot_contract_tc(regot_ctx* ctx, regot_dproblem* P, double reg, const doubl
 // choice; returns the previous forced value), and the timed choices made on
 // this device so far (-1: none yet) for the classes d <= 4, 8, 16.
 int force_batch_variant(int v);
+// Batched BCD: the number of running problems at or below which the rest of
+// the solve runs in the cluster-per-problem tail kernel (0: never); returns
+// the previous value (erot_batch.cu).
+int set_batch_tail(int max_active);
 int force_sparsify_path(int shared_memory);
 // QROT Schur CG products: 0 chosen by the entries of sigma, 1 the bitmask,
 // 2 the index lists, 3 the index lists with the vectors exchanged through

@@ -153,7 +153,7 @@ EXPORTS = [
     "regot_autotune_clear", "regot_autotune_entries", "regot_force_pass_config",
     "regot_pass_config", "regot_force_batch_variant", "regot_batch_variants",
     "regot_force_sparsify_path",
-    "regot_force_qrot_cg_path",
+    "regot_force_qrot_cg_path", "regot_set_batch_tail",
     "regot_erot_dual_obj_grad_noalloc", "regot_host_alloc", "regot_host_free",
 ]
 
@@ -232,6 +232,7 @@ def load() -> C.CDLL:
         lib.regot_force_batch_variant.argtypes = [C.c_int]
         lib.regot_force_sparsify_path.argtypes = [C.c_int]
         lib.regot_force_qrot_cg_path.argtypes = [C.c_int]
+        lib.regot_set_batch_tail.argtypes = [C.c_int]
         lib.regot_batch_variants.argtypes = [vp, C.POINTER(C.c_int)]
         lib.regot_erot_solve_batched.argtypes = [vp, C.POINTER(BatchDesc), C.c_double,
                                                  C.c_double, C.c_int, C.POINTER(BatchResult)]

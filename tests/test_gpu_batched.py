@@ -30,13 +30,31 @@ def _batch(count, seed, nmin=16, nmax=200, dims=range(1, 17)):
     return xs, ys, as_, bs, scales
 
 
+def _set_tail(v):
+    from regot import _lib
+
+    return _lib.load().regot_set_batch_tail(v)
+
+
+@pytest.fixture(params=["graph", "tail"])
+def batch_tail(request):
+    """Runs a test with the per-sweep kernels to the end ("graph": tail
+    threshold 0) and with the whole solve after the first two sweeps in the
+    cluster-per-problem tail kernel ("tail"), restoring the default after."""
+    old = _set_tail(0 if request.param == "graph" else 1 << 20)
+    try:
+        yield request.param
+    finally:
+        _set_tail(old)
+
+
 def _cost64(x, y, s):
     x = x.astype(np.float64)
     y = y.astype(np.float64)
     return s * ((x[:, None, :] - y[None, :, :]) ** 2).sum(-1)
 
 
-def test_batched_matches_oracle_per_problem():
+def test_batched_matches_oracle_per_problem(batch_tail):
     # tol 1e-6 as in the batched workload: the FP32 row sums carry relative
     # errors of a few 1e-7, so much tighter tolerances stall in FP32
     reg, tol = 0.05, 1e-6
@@ -56,7 +74,7 @@ def test_batched_matches_oracle_per_problem():
         assert np.linalg.norm(g) < 5 * tol
 
 
-def test_batched_max_iter_iterates():
+def test_batched_max_iter_iterates(batch_tail):
     # every problem stops at max_iter: the duals are the oracle's iterate
     reg = 0.05
     xs, ys, as_, bs, sc = _batch(10, seed=6, dims=(2, 3, 7, 12, 16))
@@ -70,7 +88,7 @@ def test_batched_max_iter_iterates():
         np.testing.assert_allclose(r.mar_errs[p], o.mar_errs[-1], rtol=2e-3, atol=1e-9)
 
 
-def test_batched_single_problem_equals_batch_member():
+def test_batched_single_problem_equals_batch_member(batch_tail):
     # a problem's result does not depend on the other problems of the batch
     reg, tol = 0.05, 1e-7
     xs, ys, as_, bs, sc = _batch(6, seed=7)
@@ -93,7 +111,7 @@ def test_batched_rejects_bad_input():
         regot.sinkhorn_bcd_batched(xs, ys, as_, bs, -1.0)
 
 
-def test_batched_backward_matches_fp64_at_the_returned_duals():
+def test_batched_backward_matches_fp64_at_the_returned_duals(batch_tail):
     # grad=True: each problem's cost a'alpha + b'beta - reg sum T (the negated
     # dual objective of the oracle) and dL/dx = 2 s sum_j T_ij (x_i - y_j),
     # dL/dy = 2 s sum_i T_ij (y_j - x_i), checked in FP64 at the duals the
@@ -129,7 +147,7 @@ def test_batched_backward_matches_fp64_at_the_returned_duals():
                                    atol=1e-4 * np.abs(gx).sum())
 
 
-def test_batched_backward_at_max_iter_iterates():
+def test_batched_backward_at_max_iter_iterates(batch_tail):
     # problems stopped by max_iter (odd and even counts, so the last alpha
     # sits in either ping-pong buffer): the backward still uses exactly the
     # returned iterate, whose row sums are still off a by up to 0.1
@@ -176,7 +194,10 @@ def test_batched_tensor_core_cost_tile(scaled):
     xs, ys, as_, bs, sc = _batch(20, seed=8, nmin=40, nmax=400, dims=(3, 6, 8, 11, 16))
     if not scaled:
         sc = [1.0] * len(sc)
+    # the tail kernel computes on the CUDA cores: keep every sweep in the
+    # per-sweep kernels so that the variants are compared over all six
     old = _force(1)
+    old_tail = _set_tail(0)
     try:
         r_tc = regot.sinkhorn_bcd_batched(xs, ys, as_, bs, reg, tol=1e-14, max_iter=6,
                                           cost_scale=sc)
@@ -188,6 +209,7 @@ def test_batched_tensor_core_cost_tile(scaled):
                                             cost_scale=sc)
     finally:
         _force(old)
+        _set_tail(old_tail)
     worst = 0.0
     for p in range(len(xs)):
         assert r_tc.niter[p] == r_cc.niter[p] == 6
@@ -204,3 +226,33 @@ def test_batched_tensor_core_cost_tile(scaled):
         # marginal error on the FP64 cost: tol plus the cost tile's perturbation
         assert np.linalg.norm(g) < tol + 2e-4 * sc[p] * d, (p, np.linalg.norm(g))
     print(f"tensor-core vs CUDA-core duals after 6 sweeps: worst error / bound = {worst:.3f}")
+
+
+@pytest.mark.parametrize("tail", [4, 1 << 20])
+def test_batched_tail_handover_keeps_the_iterates(tail):
+    """The tail kernel runs the same row and column arithmetic and stopping
+    test as the per-sweep kernels (CUDA-core variant forced): handing the
+    last problems over mid-solve (tail 4 of 40) or after two sweeps
+    (tail 2^20) gives the iteration counts of the per-sweep kernels and their
+    duals to FP64 rounding. Only a re-split of the duals on a new grid, which
+    the per-sweep loop applies to all running problems and the tail only to
+    the problem that needs it, can move the FP32 roundings apart."""
+    reg, tol = 0.05, 1e-6
+    xs, ys, as_, bs, sc = _batch(40, seed=9, nmin=16, nmax=300)
+    old = _force(0)
+    old_tail = _set_tail(0)
+    try:
+        ref = regot.sinkhorn_bcd_batched(xs, ys, as_, bs, reg, tol=tol, max_iter=5000,
+                                         cost_scale=sc)
+        _set_tail(tail)
+        r = regot.sinkhorn_bcd_batched(xs, ys, as_, bs, reg, tol=tol, max_iter=5000,
+                                       cost_scale=sc)
+    finally:
+        _force(old)
+        _set_tail(old_tail)
+    np.testing.assert_array_equal(r.niter, ref.niter)
+    worst = max(float(np.abs(r.duals[p] - ref.duals[p]).max()) for p in range(len(xs)))
+    print(f"tail {tail}: largest dual difference to the per-sweep kernels {worst:.3e}")
+    assert worst <= 1e-9
+    for p in range(len(xs)):
+        assert r.mar_errs[p] < tol
