@@ -515,9 +515,29 @@ def ncu_case_more(kind):
     seed 1, reg 0.1, mixed). contract: the tensor-core contractions T Y and
     T'X at n = m = 4096, d = 64 (mixed, at the duals of a BCD solve).
     newton: three sinkhorn_newton iterations at n = m = 8192 (mixed,
-    reg 0.01) from the duals of a BCD solve to 1e-4."""
+    reg 0.01) from the duals of a BCD solve to 1e-4. tail: the 274 x 547
+    (d = 11) problem of the batched workload alone, unscaled cost, 400 sweeps
+    in the cluster-per-problem tail kernel (twice: `-s 1 -c 1` captures the
+    second launch)."""
     import regot
     from problems import erot_points, qrot_points
+
+    if kind == "tail":
+        from regot import _lib
+
+        lib = _lib.load()
+        xs, ys, as_, bs, _ = batched_workload()
+        p = [q for q in range(len(xs)) if xs[q].shape[0] == 274 and ys[q].shape[0] == 547][0]
+        old = lib.regot_set_batch_tail(1 << 20)
+        try:
+            for _ in range(2):
+                r = regot.sinkhorn_bcd_batched([xs[p]], [ys[p]], [as_[p]], [bs[p]], 0.05,
+                                               tol=1e-6, max_iter=400, cost_scale=[1.0])
+        finally:
+            lib.regot_set_batch_tail(old)
+        print("ncu case (tail): problem", p, "niter", int(r.niter[0]), "device ms",
+              round(r.solve_ms, 2))
+        return
 
     if kind == "newton":
         M, a, b = erot_points(N, N, seed=0, dtype=np.float32)
@@ -771,13 +791,13 @@ def main():
                     help="a few passes for an ncu capture (no timing, no JSON)")
     ap.add_argument("--workload",
                     choices=["bcd", "batched", "solvers", "autograd", "passes", "configs",
-                             "sparsify", "qrot", "contract", "newton"],
+                             "sparsify", "qrot", "contract", "newton", "tail"],
                     default="bcd",
                     help="batched: the batched uneven-problem workload (its own JSON line); "
                          "solvers: one line per solver of the solver table; "
                          "configs: the README-example and large-QROT configurations, GPU "
-                         "beside the FP64 oracle; sparsify, qrot, contract, newton: ncu "
-                         "cases only")
+                         "beside the FP64 oracle; sparsify, qrot, contract, newton, tail: "
+                         "ncu cases only")
     ap.add_argument("--probe", choices=["hbm-read", "host-link"],
                     help="measure the ceilings the numbers are read against (no JSON line)")
     args = ap.parse_args()
@@ -807,7 +827,7 @@ def main():
                                            cost_scale=sc, grad=True)
             print("ncu case (batched): sweeps", r.sweeps)
             return
-        if args.workload in ("sparsify", "qrot", "contract", "newton"):
+        if args.workload in ("sparsify", "qrot", "contract", "newton", "tail"):
             ncu_case_more(args.workload)
             return
         M, a, b = erot_points(n, n, seed=0, dtype=np.float32)
