@@ -11,10 +11,12 @@ regot = pytest.importorskip("regot")
 
 # FP64 storage: every element-wise operation in FP64 -> agreement to ~1e-12.
 # Mixed: M rounded to FP32 (the oracle sees the same FP32 values), FP32
-# exp2/accumulation -> relative agreement ~1e-5 on plans and sums, and
-# marginal errors within FP32 rounding of the row sums (absolute ~1e-9,
+# exp2/accumulation: T carries about 1e-7 relative error, so single passes
+# agree to a few 1e-7 (measured on a GB300: gradient 2.5e-7 of max a, HVP
+# 1.2e-7, plan 4.2e-7, optimal_alpha / _beta 2e-8 of reg x 10), and the
+# marginal errors to the FP32 rounding of the row sums (absolute ~1e-9,
 # bounded here by MAR_ATOL).
-TOL = {"fp64": 1e-10, "mixed": 2e-4}
+TOL = {"fp64": 1e-10, "mixed": 2e-6}
 MAR_ATOL = {"fp64": 1e-12, "mixed": 2e-8}
 
 
@@ -91,11 +93,16 @@ def test_sinkhorn_bcd_readme(precision, reg):
         np.testing.assert_allclose(r.mar_errs[:k], o.mar_errs[:k], rtol=1e-3,
                                    atol=MAR_ATOL["mixed"])
         np.testing.assert_allclose(r.obj_vals[-1], o.obj_vals[-1], rtol=1e-6)
-        np.testing.assert_allclose(r.plan, o.plan, rtol=0, atol=2e-4 * o.plan.max())
-    # the returned dual meets the tolerance when checked in FP64 by the oracle
+        # measured 2.7e-7 of the largest entry at both regs
+        np.testing.assert_allclose(r.plan, o.plan, rtol=0, atol=2e-6 * o.plan.max())
+    # the returned dual meets the tolerance when checked in FP64 by the
+    # oracle; mixed precision stops on its FP32-summed marginal error, which
+    # resolves the FP64 one to 2e-7 |a| (measured at reg 0.1: 1.0023 tol)
     f, g = O.erot_dual_obj_grad(Mq, a, b, reg, r.dual)
     if r.niter < 1000:
-        assert np.linalg.norm(g) < (tol if precision == "fp64" else 10 * tol)
+        bound = tol if precision == "fp64" else tol + 2e-7 * max(np.linalg.norm(a),
+                                                                 np.linalg.norm(b))
+        assert np.linalg.norm(g) < bound
     assert all(np.diff(r.run_times) >= 0)
 
 
@@ -124,7 +131,7 @@ def test_sinkhorn_bcd_fallback_paths(precision):
     n, m = M.shape
     reg = 0.05
     for x0 in (np.full(n + m - 1, 1e-3), np.r_[np.full(n, -40.0), np.zeros(m - 1)]):
-        tol = TOL[precision]
+        tol = 1e-10 if precision == "fp64" else 2e-4  # solve tolerance of these runs
         r = regot.sinkhorn_bcd(M, a, b, reg, tol=tol, max_iter=3000, precision=precision, x0=x0)
         o = O.sinkhorn_bcd(Mq, a, b, reg, tol=tol, max_iter=3000, x0=x0)
         assert abs(r.niter - o.niter) <= (1 if precision == "fp64" else 0.05 * o.niter + 3)

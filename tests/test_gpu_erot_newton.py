@@ -38,9 +38,13 @@ def test_sinkhorn_newton_matches_oracle(precision, reg):
     else:
         assert abs(r.niter - o.niter) <= 3
         np.testing.assert_allclose(r.obj_vals[-1], o.obj_vals[-1], rtol=1e-6)
-        np.testing.assert_allclose(r.plan, o.plan, rtol=0, atol=2e-4 * o.plan.max())
+        # the two solves stop at different points of marginal error < tol:
+        # measured 1.9e-6 (reg 0.1) and 3.5e-7 (reg 0.05) of the largest entry
+        np.testing.assert_allclose(r.plan, o.plan, rtol=0, atol=2e-5 * o.plan.max())
+    # Newton's last step overshoots tol: the FP64-evaluated gradient norm of
+    # the mixed duals measured 0.22 tol at both regs
     f, g = O.erot_dual_obj_grad(Mq, a, b, reg, r.dual)
-    assert np.linalg.norm(g) < (tol if precision == "fp64" else 20 * tol)
+    assert np.linalg.norm(g) < tol
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
@@ -50,5 +54,6 @@ def test_newton_agrees_with_bcd(precision):
     reg = 0.05
     rn = regot.sinkhorn_newton(M, a, b, reg, tol=1e-8, max_iter=100, precision=precision)
     rb = regot.sinkhorn_bcd(M, a, b, reg, tol=1e-8, max_iter=5000, precision=precision)
-    np.testing.assert_allclose(rn.plan, rb.plan, rtol=0, atol=1e-4 * rb.plan.max())
-    np.testing.assert_allclose(rn.dual, rb.dual, rtol=0, atol=1e-5)
+    # mixed measured 6.4e-7 of the largest entry and 3.1e-8 on the duals
+    np.testing.assert_allclose(rn.plan, rb.plan, rtol=0, atol=1e-5 * rb.plan.max())
+    np.testing.assert_allclose(rn.dual, rb.dual, rtol=0, atol=1e-6)

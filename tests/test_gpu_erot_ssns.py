@@ -183,10 +183,13 @@ def test_sinkhorn_ssns_matches_oracle(precision, case):
         assert r.niter <= 1.5 * o.niter + 10, (r.niter, o.niter)
         np.testing.assert_allclose(r.obj_vals[-1], o.obj_vals[-1], rtol=1e-6)
         np.testing.assert_allclose(r.densities[0], o.densities[0], rtol=2e-3)
+    # mixed: the solves stop at different points of marginal error < tol,
+    # measured 2.2e-6 (README cases) and 2.4e-7 (points) of the largest entry
     np.testing.assert_allclose(r.plan, o.plan, rtol=0,
-                               atol=(1e-7 if precision == "fp64" else 2e-4) * o.plan.max())
+                               atol=(1e-7 if precision == "fp64" else 2e-5) * o.plan.max())
+    # mixed: the FP64-evaluated gradient norm measured 0.27-0.43 tol
     _, g = O.erot_dual_obj_grad(Mq, a, b, reg, r.dual)
-    assert np.linalg.norm(g) < (tol if precision == "fp64" else 20 * tol)
+    assert np.linalg.norm(g) < tol
 
 
 def test_sinkhorn_ssns_cg_method():
@@ -209,8 +212,9 @@ def test_ssns_agrees_with_bcd(precision):
     reg = 0.05
     rs = regot.sinkhorn_ssns(M, a, b, reg, tol=1e-8, max_iter=200, precision=precision)
     rb = regot.sinkhorn_bcd(M, a, b, reg, tol=1e-8, max_iter=5000, precision=precision)
-    np.testing.assert_allclose(rs.plan, rb.plan, rtol=0, atol=1e-4 * rb.plan.max())
-    np.testing.assert_allclose(rs.dual, rb.dual, rtol=0, atol=1e-5)
+    # mixed measured 6.5e-7 of the largest entry and 2.4e-7 on the duals
+    np.testing.assert_allclose(rs.plan, rb.plan, rtol=0, atol=1e-5 * rb.plan.max())
+    np.testing.assert_allclose(rs.dual, rb.dual, rtol=0, atol=2e-6)
 
 
 def test_ssns_x0_and_errors():
