@@ -40,3 +40,27 @@ def test_gpu_plan_reproduces_reference_image(name, precision):
     bad = P.violations(T, labels, rgb, tol=tol)
     assert bad == 0, (f"{bad} constraints broken at {tol} bins; "
                       f"needed {P.needed_tol(T, labels, rgb)}")
+
+
+# EROT's plan is unique: the GPU's other EROT solvers, converged well below
+# the reference's tol, reproduce its images too (the oracle's do at
+# tolerance 0, tests/test_reference_images_cpu.py).
+CROSS = [
+    ("plan_erot_bcd_reg0_1", "sinkhorn_newton", 1e-9, 1000),
+    ("plan_erot_bcd_reg0_1", "sinkhorn_ssns", 1e-9, 1000),
+    ("plan_erot_ssns_reg0_01", "sinkhorn_newton", 1e-9, 1000),
+    ("plan_erot_ssns_reg0_01", "sinkhorn_bcd", 1e-9, 20000),
+]
+
+
+@pytest.mark.parametrize("name,solver,tol,max_iter", CROSS,
+                         ids=[f"{c[0][5:]}-{c[1]}" for c in CROSS])
+def test_gpu_other_erot_solvers_reproduce_reference_image(name, solver, tol, max_iter):
+    labels, rgb, call = P.load(name)
+    M, a, b = readme_example(100, 80)
+    r = getattr(regot, solver)(M, a, b, call["reg"], tol=tol, max_iter=max_iter,
+                               precision="fp64")
+    assert r.mar_errs[-1] < tol
+    T = np.asarray(r.plan)
+    bad = P.violations(T, labels, rgb, tol=TOL_BINS["fp64"])
+    assert bad == 0, (f"{bad} constraints broken; needed {P.needed_tol(T, labels, rgb)}")

@@ -80,3 +80,26 @@ def test_close_but_different_solves_are_rejected(readme):
     assert P.violations(_solve(readme, call, tol=1e-5).plan, labels, rgb) > 0
     for reg in (0.099, 0.101):
         assert P.violations(_solve(readme, call, reg=reg).plan, labels, rgb) > 0
+
+
+# EROT has a unique plan, so solvers other than the one the reference ran
+# reproduce its image once they are converged well below the reference's
+# tol 1e-6 (the QROT solvers other than PDIP converge too slowly on this
+# problem to be compared the same way).
+CROSS = [
+    ("plan_erot_bcd_reg0_1", "sinkhorn_newton", 1e-9, 1000),
+    ("plan_erot_bcd_reg0_1", "sinkhorn_ssns", 1e-9, 1000),
+    ("plan_erot_bcd_reg0_1", "sinkhorn_bcd", 1e-10, 5000),
+    ("plan_erot_ssns_reg0_01", "sinkhorn_newton", 1e-9, 1000),
+    ("plan_erot_ssns_reg0_01", "sinkhorn_bcd", 1e-9, 20000),
+]
+
+
+@pytest.mark.parametrize("name,solver,tol,max_iter", CROSS,
+                         ids=[f"{c[0][5:]}-{c[1]}" for c in CROSS])
+def test_other_erot_solvers_reproduce_reference_image(readme, name, solver, tol, max_iter):
+    labels, rgb, call = P.load(name)
+    M, a, b = readme
+    r = getattr(O, solver)(M, a, b, call["reg"], tol=tol, max_iter=max_iter)
+    assert r.mar_errs[-1] < tol
+    assert P.violations(r.plan, labels, rgb, tol=0.0) == 0
