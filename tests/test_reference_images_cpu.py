@@ -103,3 +103,13 @@ def test_other_erot_solvers_reproduce_reference_image(readme, name, solver, tol,
     r = getattr(O, solver)(M, a, b, call["reg"], tol=tol, max_iter=max_iter)
     assert r.mar_errs[-1] < tol
     assert P.violations(r.plan, labels, rgb, tol=0.0) == 0
+
+
+def test_checker_edge_cases():
+    """The checker refuses a plan of another shape and finds no tolerance at
+    which an unrelated plan matches."""
+    labels, rgb, _ = P.load("plan_erot_bcd_reg0_1")
+    with pytest.raises(ValueError):
+        P.violations(np.ones((80, 100)), labels, rgb)
+    noise = np.random.default_rng(0).random(labels.shape)
+    assert P.needed_tol(noise, labels, rgb) == float("inf")
